@@ -1,0 +1,118 @@
+/*
+ * grt_oracle.h -- FP64 CPU oracle of the layered-medium Green's-function
+ * pipeline (generalized reflection-transmission method).
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker for the CUDA
+ * product in grtm_cuda_gb300/.  Only tests/, __graft_entry__.smoke() and the
+ * cpu_baseline / reference arm of bench.py may load it.  The product never
+ * links it and never falls back to it.
+ *
+ * It restates, step by step and in plain FP64 C, what the reference
+ * (cangyeone/grtm_cuda, cusrc/popm/func/green.cu) computes, including the
+ * reference's known quirks (they are switchable, see GRTO_FIX_*), so that the
+ * reference's own golden vectors demo/oname_{t,w}.txt can be reproduced.
+ */
+#ifndef GRT_ORACLE_H_
+#define GRT_ORACLE_H_
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GRTO_MAXL 256      /* layers after source-interface insertion */
+
+/* status codes */
+#define GRTO_OK 0
+#define GRTO_ERR_IO 1
+#define GRTO_ERR_PARSE 2
+#define GRTO_ERR_MODEL 3
+#define GRTO_ERR_ARG 4
+#define GRTO_ERR_NOMEM 5
+
+/* k-grid modes */
+#define GRTO_K_REFERENCE 0 /* ragged per-frequency k_max (green.cu:2145-2194) */
+#define GRTO_K_FIXED 1     /* nk_fixed points k_j = j*dk for every frequency */
+
+/* Corrections of reference quirks.  0 = bug-compatible with the reference. */
+#define GRTO_FIX_RLAYER 1  /* receiver layer searched with hr, not hs (green.cu:2092-2101) */
+#define GRTO_FIX_REXUT 2   /* d/dz terms use this (w,k) point's nu, not slot 0's (green.cu:674-675) */
+#define GRTO_FIX_DZ 4      /* d/dz vertical factors without the double nu / reuse quirks
+                              (green.cu:720, 842, 902) */
+/* Not a correction: evaluate the same recursion in the well-conditioned
+ * basis (see grt_oracle.c).  Same results where the reference's 4x4 solve is
+ * well conditioned; accurate also at w -> 0 where the reference loses digits. */
+#define GRTO_STABLE 8
+
+typedef struct grto_job {
+    /* model after source-interface insertion (green.cu:1995-2049) */
+    int n_layer;
+    double h[GRTO_MAXL];   /* thickness; last entry keeps the half-space top depth */
+    double a0[GRTO_MAXL], b0[GRTO_MAXL], rho[GRTO_MAXL], qp[GRTO_MAXL], qs[GRTO_MAXL];
+    double mu[GRTO_MAXL];  /* b0^2 * rho (real, unattenuated) */
+    int inserted;          /* 1 if a source interface was inserted */
+    double hs, hr;         /* source / receiver depth as given, km */
+    int s_layer, r_layer;
+    double zs, zr;         /* depth of source / receiver below the top of its layer */
+    int src_type;          /* 0 single force, otherwise moment tensor */
+    /* time / frequency grid (green.cu:2051-2080) */
+    double dt, t0, taper, twin;
+    int nf1, nf2, n_ptam, log2n;
+    int nw;                /* number of positive frequencies, N/2 */
+    double df, sigma, dk, vmax, vmin;
+    /* wavenumber grid */
+    int k_mode, nk_fixed;
+    int fix;               /* GRTO_FIX_* bits */
+    /* receivers */
+    int n_dist;
+    const double *dist;
+    double dist0;          /* the single distance of an input file */
+} grto_job;
+
+/* Parse a reference input file (format of green.cu:1995-2060). */
+int grto_parse(const char *path, grto_job *job);
+
+/* Build a job from arrays: n_in layers given by depth-to-top ztop (ztop[0] = 0). */
+int grto_model(grto_job *job, int n_in, const double *ztop, const double *vp,
+               const double *vs, const double *rho, const double *qp,
+               const double *qs, double hs, double hr, int src_type);
+
+/* Grid and layer location (green.cu:2065-2101).  sigma_factor: sigma = f / T
+ * (the reference uses 2).  dk_override > 0 replaces the reference's dk. */
+int grto_setup(grto_job *job, double dt, int log2n, double t0, double taper,
+               double sigma_factor, int k_mode, int nk_fixed, double dk_override,
+               int fix);
+
+/* Number of wavenumbers used at frequency index iw. */
+int grto_nk(const grto_job *job, int iw);
+
+/* Total number of (w,k) points. */
+long long grto_nkw(const grto_job *job);
+
+/* Full pipeline for job->n_dist receivers (job->dist).
+ *   spec: n_dist x N x 30 complex (re,im interleaved) after taper and
+ *         Hermitian fill, or NULL;
+ *   sig:  n_dist x N x 30 real time series after the inverse DFT and
+ *         de-damping, or NULL.  N = 2*nw. */
+int grto_run(const grto_job *job, double *spec, double *sig, int nthreads);
+
+/* Per-(w,k) receiver coefficients, for kernel-level comparisons.
+ *   out: 16 complex (re,im) = a0[2], a1[2], a2[2], b1, b2, a0t[2], a1t[2],
+ *   a2t[2], b1t, b2t (a2/b2 are zero for a single force). */
+int grto_point(const grto_job *job, int iw, double k, double *out);
+
+/* Integrand values (15 or 30 columns) at (iw, k) for distance r. */
+int grto_integrand(const grto_job *job, int iw, double k, double r, double *out);
+
+/* Whole reference call: read iname, write oname_w / oname_t like green(). */
+int grto_green(const char *iname, const char *oname_w, const char *oname_t,
+               int nthreads);
+
+/* Bessel functions exactly as the reference evaluates them. */
+double grto_besselj(double x, int n);
+double grto_d_besselj(double x, int n);
+double grto_dd_besselj(double x, int n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
