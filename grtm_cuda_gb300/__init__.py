@@ -1,0 +1,228 @@
+"""GB300 layered-medium Green's functions by the generalized
+reflection-transmission method.
+
+Python front-end over the library's C ABI (include/grtm_gb300.h), loaded with
+ctypes exactly as the reference's scripts load theirs
+(``ctypes.cdll.LoadLibrary("build/libpopm.so").green(iname, oname_w, oname_t)``,
+greent.py:94-98).  All computation runs in the CUDA library; if it is missing
+this module raises instead of falling back to anything else.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libgrtm_gb300.so")
+
+OK, ERR_ARG, ERR_IO, ERR_PARSE, ERR_MODEL, ERR_CUDA, ERR_NOMEM, ERR_TIMEOUT, ERR_UNSUPPORTED = range(9)
+K_REFERENCE, K_FIXED = 0, 1
+FP32, FP64 = 0, 1
+FIX_RLAYER, FIX_REXUT, FIX_DZ = 1, 2, 4
+FIX_ALL = FIX_RLAYER | FIX_REXUT | FIX_DZ
+
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+class Model(ctypes.Structure):
+    _fields_ = [("n_layer", ctypes.c_int), ("ztop", _dp), ("vp", _dp), ("vs", _dp), ("rho", _dp),
+                ("qp", _dp), ("qs", _dp), ("hs", ctypes.c_double), ("hr", ctypes.c_double),
+                ("src_type", ctypes.c_int)]
+
+
+class Opts(ctypes.Structure):
+    _fields_ = [("dt", ctypes.c_double), ("log2n", ctypes.c_int), ("t0", ctypes.c_double),
+                ("taper", ctypes.c_double), ("sigma_factor", ctypes.c_double), ("k_mode", ctypes.c_int),
+                ("nk_fixed", ctypes.c_int), ("dk", ctypes.c_double), ("precision", ctypes.c_int),
+                ("fix", ctypes.c_int)]
+
+
+class Report(ctypes.Structure):
+    _fields_ = [("n_layer", ctypes.c_int), ("s_layer", ctypes.c_int), ("r_layer", ctypes.c_int),
+                ("zs", ctypes.c_double), ("zr", ctypes.c_double), ("nw", ctypes.c_int),
+                ("n_samples", ctypes.c_int), ("n_cols", ctypes.c_int), ("n_wk", ctypes.c_longlong),
+                ("nk_max", ctypes.c_int), ("dk", ctypes.c_double), ("df", ctypes.c_double),
+                ("sigma", ctypes.c_double), ("ms_grt", ctypes.c_float), ("ms_bessel", ctypes.c_float),
+                ("ms_ksum", ctypes.c_float), ("ms_spectral", ctypes.c_float), ("ms_total", ctypes.c_float),
+                ("kernel_launches", ctypes.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+# every symbol the public header declares
+EXPORTS = ("grt_create", "grt_destroy", "grt_last_error", "grt_status_string", "grt_plan_create",
+           "grt_plan_execute", "grt_plan_fetch", "grt_plan_info", "grt_plan_destroy", "grt_run",
+           "grt_green", "green")
+
+_lib = None
+
+
+def build():
+    from . import buildlib
+    return buildlib.build()
+
+
+def lib():
+    """Load the CUDA library (building it first when only sources exist)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        build()
+    L = ctypes.CDLL(LIB_PATH)
+    P = ctypes.POINTER
+    vp = ctypes.c_void_p
+    L.grt_create.argtypes = [P(vp), ctypes.c_int]
+    L.grt_destroy.argtypes = [vp]
+    L.grt_destroy.restype = None
+    L.grt_last_error.argtypes = [vp]
+    L.grt_last_error.restype = ctypes.c_char_p
+    L.grt_status_string.argtypes = [ctypes.c_int]
+    L.grt_status_string.restype = ctypes.c_char_p
+    L.grt_plan_create.argtypes = [vp, P(Model), P(Opts), ctypes.c_int, _dp, P(vp)]
+    L.grt_plan_execute.argtypes = [vp, P(Report)]
+    L.grt_plan_fetch.argtypes = [vp, _dp, _dp]
+    L.grt_plan_info.argtypes = [vp, P(Report)]
+    L.grt_plan_destroy.argtypes = [vp]
+    L.grt_plan_destroy.restype = None
+    L.grt_run.argtypes = [vp, P(Model), P(Opts), ctypes.c_int, _dp, _dp, _dp, P(Report)]
+    L.grt_green.argtypes = [ctypes.c_char_p] * 3
+    L.green.argtypes = [ctypes.c_char_p] * 3
+    L.green.restype = None
+    _lib = L
+    return L
+
+
+class GrtError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{lib().grt_status_string(status).decode()}: {msg}")
+        self.status = status
+
+
+def _arr(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_dp)
+
+
+class Context:
+    """One CUDA stream on one device (grt_create / grt_destroy)."""
+
+    def __init__(self, device=0):
+        self.h = ctypes.c_void_p()
+        rc = lib().grt_create(ctypes.byref(self.h), device)
+        if rc:
+            raise GrtError(rc, "grt_create failed")
+
+    def error(self):
+        return lib().grt_last_error(self.h).decode()
+
+    def close(self):
+        if self.h:
+            lib().grt_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def make_model(ztop, vp, vs, rho, qp, qs, hs, hr=0.0, src_type=0):
+    arrs = [_arr(a) for a in (ztop, vp, vs, rho, qp, qs)]
+    m = Model(len(arrs[0]), *[_ptr(a) for a in arrs], float(hs), float(hr), int(src_type))
+    m._keep = arrs
+    return m
+
+
+def make_opts(dt, log2n, t0=0.0, taper=0.3, sigma_factor=2.0, k_mode=K_REFERENCE, nk_fixed=0, dk=0.0,
+              precision=FP32, fix=0):
+    return Opts(float(dt), int(log2n), float(t0), float(taper), float(sigma_factor), int(k_mode),
+                int(nk_fixed), float(dk), int(precision), int(fix))
+
+
+class Plan:
+    """A model, its grids, its receivers and their device buffers."""
+
+    def __init__(self, ctx, model, opts, dists):
+        self.ctx = ctx
+        self.dists = _arr(np.atleast_1d(dists))
+        self.h = ctypes.c_void_p()
+        rc = lib().grt_plan_create(ctx.h, ctypes.byref(model), ctypes.byref(opts), len(self.dists),
+                                   _ptr(self.dists), ctypes.byref(self.h))
+        if rc:
+            raise GrtError(rc, ctx.error())
+        self.report = Report()
+        lib().grt_plan_info(self.h, ctypes.byref(self.report))
+
+    def execute(self):
+        rc = lib().grt_plan_execute(self.h, ctypes.byref(self.report))
+        if rc:
+            raise GrtError(rc, self.ctx.error())
+        return self.report
+
+    def fetch(self, traces=True, spectra=False):
+        r = self.report
+        shape = (len(self.dists), r.n_cols, r.n_samples)
+        t = np.empty(shape) if traces else None
+        s = np.empty(shape + (2,)) if spectra else None
+        rc = lib().grt_plan_fetch(self.h, _ptr(t) if traces else None, _ptr(s) if spectra else None)
+        if rc:
+            raise GrtError(rc, self.ctx.error())
+        if spectra:
+            s = s[..., 0] + 1j * s[..., 1]
+        return t, s
+
+    def close(self):
+        if self.h:
+            lib().grt_plan_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def run(model, opts, dists, ctx=None, spectra=False):
+    """Green's functions for one model at all distances.
+
+    Returns (traces [n_dist, n_cols, N], spectra or None, report dict)."""
+    own = ctx is None
+    ctx = ctx or Context()
+    try:
+        p = Plan(ctx, model, opts, dists)
+        p.execute()
+        t, s = p.fetch(True, spectra)
+        rep = p.report.as_dict()
+        p.close()
+        return t, s, rep
+    finally:
+        if own:
+            ctx.close()
+
+
+def green(iname, oname_w, oname_t):
+    """The reference's entry point: input file in, two text files out."""
+    rc = lib().grt_green(str(iname).encode(), str(oname_w).encode(), str(oname_t).encode())
+    if rc:
+        raise GrtError(rc, f"green({iname})")
+
+
+def read_table(path, complex_pairs=False):
+    """Read a file written by green() (rows of comma-terminated fields)."""
+    rows = []
+    with open(path) as f:
+        for line in f:
+            vals = [float(x) for x in line.strip().split(",") if x.strip()]
+            if vals:
+                rows.append(vals)
+    a = np.array(rows)
+    if complex_pairs:
+        a = a[:, 0::2] + 1j * a[:, 1::2]
+    return a

@@ -1,0 +1,470 @@
+// grt_api.cu -- C ABI: contexts, plans, kernel launches and the reference's
+// file-to-file entry point green().
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/grtm_gb300.h"
+#include "grt_integrate.cuh"
+#include "grt_job.h"
+#include "grt_kernel.cuh"
+
+using grt::Job;
+using cd = std::complex<double>;
+static const double PI = 3.1415926535897932384626433;
+
+struct grt_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[6] = {};
+    std::string err;
+};
+
+struct grt_plan {
+    grt_ctx *ctx = nullptr;
+    Job J;
+    int prec = 0;
+    int nd = 0, nc = 0, nq = 0, ntiles = 0;
+    int rt = 128, jt = 1;
+    std::vector<double> dist;
+    double slot0[4] = {0, 0, 0, 0};
+    // device buffers
+    void *tab = nullptr, *K = nullptr, *B = nullptr, *S = nullptr, *post = nullptr, *tw = nullptr;
+    void *spec = nullptr, *sig = nullptr;
+    int2 *tiles = nullptr;
+    int *nk = nullptr;
+    long long *koff = nullptr;
+    double *ddist = nullptr, *damp = nullptr;
+    unsigned *derr = nullptr;
+    grt_report rep{};
+};
+
+static int set_err(grt_ctx *ctx, int code, const std::string &msg)
+{
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+#define CU(call)                                                                                        \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess)                                                                          \
+            return set_err(ctx, e_ == cudaErrorMemoryAllocation ? GRT_ERR_NOMEM : GRT_ERR_CUDA,          \
+                           std::string(#call) + ": " + cudaGetErrorString(e_));                        \
+    } while (0)
+
+extern "C" const char *grt_status_string(int s)
+{
+    switch (s) {
+    case GRT_OK: return "ok";
+    case GRT_ERR_ARG: return "invalid argument";
+    case GRT_ERR_IO: return "i/o error";
+    case GRT_ERR_PARSE: return "malformed input file";
+    case GRT_ERR_MODEL: return "unsupported layered model";
+    case GRT_ERR_CUDA: return "CUDA error";
+    case GRT_ERR_NOMEM: return "out of memory";
+    case GRT_ERR_TIMEOUT: return "device wait timed out";
+    case GRT_ERR_UNSUPPORTED: return "unsupported size";
+    default: return "unknown status";
+    }
+}
+
+extern "C" int grt_create(grt_ctx **out, int device)
+{
+    if (!out) return GRT_ERR_ARG;
+    *out = nullptr;
+    std::unique_ptr<grt_ctx> c(new grt_ctx);
+    grt_ctx *ctx = c.get();
+    c->device = device;
+    CU(cudaSetDevice(device));
+    CU(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    for (auto &e : c->ev) CU(cudaEventCreate(&e));
+    *out = c.release();
+    return GRT_OK;
+}
+
+extern "C" void grt_destroy(grt_ctx *ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    for (auto &e : ctx->ev)
+        if (e) cudaEventDestroy(e);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+extern "C" const char *grt_last_error(const grt_ctx *ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+extern "C" void grt_plan_destroy(grt_plan *p)
+{
+    if (!p) return;
+    cudaSetDevice(p->ctx->device);
+    void *bufs[] = {p->tab, p->K, p->B, p->S, p->post, p->tw, p->spec, p->sig, p->tiles, p->nk, p->koff, p->ddist,
+                    p->damp, p->derr};
+    for (void *b : bufs)
+        if (b) cudaFree(b);
+    delete p;
+}
+
+// ------------------------------------------------------------------ host tables
+template <typename R>
+static void build_tables(const Job &J, std::vector<grt::LayerW<R>> &tab, std::vector<R> &post, std::vector<R> &tw,
+                         std::vector<double> &damp)
+{
+    const int L = J.L, nw = J.nw, N = J.N;
+    tab.resize((size_t)nw * L);
+    for (int iw = 0; iw < nw; iw++) {
+        cd w(2 * PI * J.df * iw, -J.sigma);
+        cd lw = std::log(w / (2 * PI));
+        for (int i = 0; i < L; i++) {
+            // attenuation, green.cu:177-180
+            cd cs = 1.0 + lw / (PI * J.qs[i]) + cd(0, 1) / (2.0 * J.qs[i]);
+            cd cp = 1.0 + lw / (PI * J.qp[i]) + cd(0, 1) / (2.0 * J.qp[i]);
+            cd a = J.a0[i] * cp, b = J.b0[i] * cs;
+            cd wa = w / a, wb = w / b;
+            cd wa2 = wa * wa, wb2 = wb * wb, W = wb2 - wa2, iW = 1.0 / W;
+            grt::LayerW<R> &t = tab[(size_t)iw * L + i];
+            t.wa2x = wa2.real(); t.wa2y = wa2.imag(); t.wb2x = wb2.real(); t.wb2y = wb2.imag();
+            t.wa2[0] = (R)wa2.real(); t.wa2[1] = (R)wa2.imag();
+            t.wb2[0] = (R)wb2.real(); t.wb2[1] = (R)wb2.imag();
+            t.W[0] = (R)W.real(); t.W[1] = (R)W.imag();
+            t.iW[0] = (R)iW.real(); t.iW[1] = (R)iW.imag();
+            t.a[0] = (R)a.real(); t.a[1] = (R)a.imag();
+            t.b[0] = (R)b.real(); t.b[1] = (R)b.imag();
+            t.mu = (R)J.mu[i];
+            t.h = (R)J.h[i];
+        }
+    }
+    // phase e^{i w_r t0}, cosine taper and scale df nw / pi (green.cu:1905-1921)
+    post.resize(2 * (size_t)nw);
+    const int wc = (int)((double)nw * (1 - J.taper));
+    const double coef = J.df * nw / PI;
+    for (int iw = 0; iw < nw; iw++) {
+        double st0 = iw > wc ? 0.5 * (1. + std::cos((iw - wc + 1) * PI / (nw - wc + 1))) : 1.0;
+        double phi = 2 * PI * J.df * iw * J.t0;
+        post[2 * iw] = (R)(std::cos(phi) * st0 * coef);
+        post[2 * iw + 1] = (R)(std::sin(phi) * st0 * coef);
+    }
+    tw.resize(N);  // N/2 complex
+    for (int m = 0; m < N / 2; m++) {
+        tw[2 * m] = (R)std::cos(2 * PI * m / N);
+        tw[2 * m + 1] = (R)std::sin(2 * PI * m / N);
+    }
+    // Re(x_n) / N e^{sigma n dt} e^{sigma t0} (green.cu:2236-2237)
+    damp.resize(N);
+    for (int n = 0; n < N; n++) damp[n] = std::exp(n * J.dt * J.sigma) * std::exp(J.t0 * J.sigma) / (double)N;
+}
+
+template <typename R>
+static int upload(grt_plan *p)
+{
+    grt_ctx *ctx = p->ctx;
+    const Job &J = p->J;
+    std::vector<grt::LayerW<R>> tab;
+    std::vector<R> post, tw;
+    std::vector<double> damp;
+    build_tables<R>(J, tab, post, tw, damp);
+    // slot-0 vertical wavenumbers (w = -i sigma, k = 0) of the receiver layer
+    {
+        const auto &t = tab[J.rl];
+        cd r0 = std::sqrt(cd(-t.wa2x, -t.wa2y)), v0 = std::sqrt(cd(-t.wb2x, -t.wb2y));
+        if (r0.real() < 0) r0 = -r0;
+        if (v0.real() < 0) v0 = -v0;
+        p->slot0[0] = r0.real(); p->slot0[1] = r0.imag(); p->slot0[2] = v0.real(); p->slot0[3] = v0.imag();
+    }
+    std::vector<int2> tiles;
+    for (int iw = 0; iw < J.nw; iw++)
+        for (int j0 = 0; j0 < J.nk[iw]; j0 += grt::kGrtThreads) tiles.push_back(make_int2(iw, j0));
+    p->ntiles = (int)tiles.size();
+    const size_t szK = (size_t)p->nq * J.nkw * 2 * sizeof(R);
+    const size_t szB = (size_t)J.nkmax * grt::NBASIS * p->nd * sizeof(R);
+    const size_t ntr = (size_t)p->nd * p->nc;
+    CU(cudaMalloc(&p->tab, tab.size() * sizeof(tab[0])));
+    CU(cudaMalloc(&p->tiles, tiles.size() * sizeof(int2)));
+    CU(cudaMalloc(&p->nk, J.nw * sizeof(int)));
+    CU(cudaMalloc(&p->koff, J.nw * sizeof(long long)));
+    CU(cudaMalloc(&p->ddist, p->nd * sizeof(double)));
+    CU(cudaMalloc(&p->K, szK));
+    CU(cudaMalloc(&p->B, szB));
+    CU(cudaMalloc(&p->S, ntr * J.nw * 2 * sizeof(R)));
+    CU(cudaMalloc(&p->post, post.size() * sizeof(R)));
+    CU(cudaMalloc(&p->tw, tw.size() * sizeof(R)));
+    CU(cudaMalloc(&p->damp, damp.size() * sizeof(double)));
+    CU(cudaMalloc(&p->sig, ntr * J.N * sizeof(R)));
+    CU(cudaMalloc(&p->spec, ntr * J.N * 2 * sizeof(R)));
+    CU(cudaMalloc(&p->derr, sizeof(unsigned)));
+    cudaStream_t st = ctx->stream;
+    CU(cudaMemcpyAsync(p->tab, tab.data(), tab.size() * sizeof(tab[0]), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(p->tiles, tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(p->nk, J.nk.data(), J.nw * sizeof(int), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(p->koff, J.koff.data(), J.nw * sizeof(long long), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(p->ddist, p->dist.data(), p->nd * sizeof(double), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(p->post, post.data(), post.size() * sizeof(R), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(p->tw, tw.data(), tw.size() * sizeof(R), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(p->damp, damp.data(), damp.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    CU(cudaMemsetAsync(p->derr, 0, sizeof(unsigned), st));
+    CU(cudaStreamSynchronize(st));
+    return GRT_OK;
+}
+
+extern "C" int grt_plan_create(grt_ctx *ctx, const grt_model *m, const grt_opts *o, int n_dist, const double *dist,
+                               grt_plan **out)
+{
+    if (!ctx || !m || !o || !out || n_dist < 1 || !dist) return set_err(ctx, GRT_ERR_ARG, "null argument or no receivers");
+    *out = nullptr;
+    for (int i = 0; i < n_dist; i++)
+        if (!(dist[i] > 0)) return set_err(ctx, GRT_ERR_ARG, "distances must be > 0");
+    if (o->precision != GRT_FP32 && o->precision != GRT_FP64) return set_err(ctx, GRT_ERR_ARG, "bad precision");
+    std::unique_ptr<grt_plan> p(new grt_plan);
+    p->ctx = ctx;
+    std::string err;
+    int rc = grt::job_from_layers(m->n_layer, m->ztop, m->vp, m->vs, m->rho, m->qp, m->qs, m->hs, m->hr, m->src_type,
+                                  p->J, err);
+    if (!rc)
+        rc = grt::job_setup(p->J, o->dt, o->log2n, o->t0, o->taper, o->sigma_factor, o->k_mode, o->nk_fixed, o->dk,
+                            o->fix, err);
+    if (rc) return set_err(ctx, rc, err);
+    const Job &J = p->J;
+    p->prec = o->precision;
+    p->nd = n_dist;
+    p->dist.assign(dist, dist + n_dist);
+    p->nc = J.src == 0 ? grt::kSingleNC : grt::kTensorNC;
+    p->nq = J.src == 0 ? grt::QS_N : grt::QT_N;
+    const size_t esz = p->prec ? sizeof(grt::C<double>) : sizeof(grt::C<float>);
+    if ((size_t)J.N * esz > 128 * 1024)
+        return set_err(ctx, GRT_ERR_UNSUPPORTED, "N too large for the shared-memory FFT at this precision");
+    if (J.nkmax > (1 << 24)) return set_err(ctx, GRT_ERR_UNSUPPORTED, "too many wavenumbers");
+    // receivers per block / k-lanes per receiver of the wavenumber sum
+    p->rt = 128;
+    while (p->rt > 1 && p->rt / 2 >= n_dist) p->rt /= 2;
+    p->jt = 128 / p->rt;
+    CU(cudaSetDevice(ctx->device));
+    rc = p->prec ? upload<double>(p.get()) : upload<float>(p.get());
+    if (rc) {
+        grt_plan_destroy(p.release());
+        return rc;
+    }
+    *out = p.release();
+    return GRT_OK;
+}
+
+template <typename R>
+static int execute(grt_plan *p)
+{
+    grt_ctx *ctx = p->ctx;
+    const Job &J = p->J;
+    cudaStream_t st = ctx->stream;
+    int launches = 0;
+    // 1. per-(w,k) GRT kernel
+    grt::GrtArgs<R> A{};
+    A.tab = (const grt::LayerW<R> *)p->tab;
+    A.tiles = p->tiles;
+    A.nk = p->nk;
+    A.koff = p->koff;
+    A.K = (R *)p->K;
+    A.nkw = J.nkw;
+    A.dk = J.dk;
+    A.zs = J.zs;
+    A.zr = J.zr;
+    A.hs_layer = J.h[J.s];
+    A.hr_layer = J.h[J.rl];
+    A.L = J.L; A.s = J.s; A.rl = J.rl; A.src = J.src; A.fix = J.fix; A.nq = p->nq;
+    for (int i = 0; i < 4; i++) A.slot0[i] = (R)p->slot0[i];
+    A.err = p->derr;
+    const size_t smem = (size_t)J.L * sizeof(grt::LayerW<R>);
+    CU(cudaEventRecord(ctx->ev[0], st));
+    grt::grt_point_kernel<R><<<p->ntiles, grt::kGrtThreads, smem, st>>>(A);
+    launches++;
+    CU(cudaGetLastError());
+    CU(cudaEventRecord(ctx->ev[1], st));
+    // 2. Bessel table
+    {
+        long long n = (long long)J.nkmax * p->nd;
+        int blocks = (int)((n + 255) / 256);
+        grt::bessel_table_kernel<R><<<blocks, 256, 0, st>>>((R *)p->B, J.nkmax, p->nd, J.dk, p->ddist);
+        launches++;
+        CU(cudaGetLastError());
+    }
+    CU(cudaEventRecord(ctx->ev[2], st));
+    // 3. wavenumber sum
+    {
+        grt::KsumArgs<R> S{};
+        S.K = (const R *)p->K; S.B = (const R *)p->B; S.nk = p->nk; S.koff = p->koff; S.dist = p->ddist;
+        S.S = (R *)p->S; S.nkw = J.nkw; S.dk = J.dk; S.nw = J.nw; S.nr = p->nd; S.rt = p->rt; S.jt = p->jt;
+        int grid = J.nw * ((p->nd + p->rt - 1) / p->rt);
+        if (J.src == 0) grt::ksum_kernel<R, grt::kSingle><<<grid, grt::kSumThreads, 0, st>>>(S);
+        else grt::ksum_kernel<R, grt::kTensor><<<grid, grt::kSumThreads, 0, st>>>(S);
+        launches++;
+        CU(cudaGetLastError());
+    }
+    CU(cudaEventRecord(ctx->ev[3], st));
+    // 4. spectral stage + inverse DFT
+    {
+        grt::SpecArgs<R> S{};
+        S.S = (const R *)p->S; S.post = (const R *)p->post; S.tw = (const R *)p->tw; S.damp = p->damp;
+        S.spec_out = (R *)p->spec; S.sig_out = (R *)p->sig; S.nw = J.nw; S.logn = J.log2n;
+        size_t smem2 = (size_t)J.N * sizeof(grt::C<R>);
+        CU(cudaFuncSetAttribute(grt::spectral_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
+        int threads = std::min(512, std::max(32, J.N / 2));
+        grt::spectral_kernel<R><<<p->nd * p->nc, threads, smem2, st>>>(S);
+        launches++;
+        CU(cudaGetLastError());
+    }
+    CU(cudaEventRecord(ctx->ev[4], st));
+    CU(cudaEventSynchronize(ctx->ev[4]));
+    unsigned herr = 0;
+    CU(cudaMemcpy(&herr, p->derr, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    if (herr) return set_err(ctx, GRT_ERR_TIMEOUT, "a bounded device wait gave up (layer-table copy)");
+    float t[4];
+    for (int i = 0; i < 4; i++) CU(cudaEventElapsedTime(&t[i], ctx->ev[i], ctx->ev[i + 1]));
+    p->rep.ms_grt = t[0];
+    p->rep.ms_bessel = t[1];
+    p->rep.ms_ksum = t[2];
+    p->rep.ms_spectral = t[3];
+    p->rep.ms_total = t[0] + t[1] + t[2] + t[3];
+    p->rep.kernel_launches = launches;
+    return GRT_OK;
+}
+
+extern "C" int grt_plan_info(const grt_plan *p, grt_report *r)
+{
+    if (!p || !r) return GRT_ERR_ARG;
+    const Job &J = p->J;
+    *r = p->rep;
+    r->n_layer = J.L;
+    r->s_layer = J.s;
+    r->r_layer = J.rl;
+    r->zs = J.zs;
+    r->zr = J.zr;
+    r->nw = J.nw;
+    r->n_samples = J.N;
+    r->n_cols = p->nc;
+    r->n_wk = J.nkw;
+    r->nk_max = J.nkmax;
+    r->dk = J.dk;
+    r->df = J.df;
+    r->sigma = J.sigma;
+    return GRT_OK;
+}
+
+extern "C" int grt_plan_execute(grt_plan *p, grt_report *r)
+{
+    if (!p) return GRT_ERR_ARG;
+    grt_ctx *ctx = p->ctx;
+    CU(cudaSetDevice(ctx->device));
+    int rc = p->prec ? execute<double>(p) : execute<float>(p);
+    if (rc) return rc;
+    if (r) grt_plan_info(p, r);
+    return GRT_OK;
+}
+
+template <typename R>
+static int fetch(grt_plan *p, double *traces, double *spectra)
+{
+    grt_ctx *ctx = p->ctx;
+    const size_t n = (size_t)p->nd * p->nc * p->J.N;
+    std::vector<R> h;
+    if (traces) {
+        h.resize(n);
+        CU(cudaMemcpyAsync(h.data(), p->sig, n * sizeof(R), cudaMemcpyDeviceToHost, ctx->stream));
+        CU(cudaStreamSynchronize(ctx->stream));
+        for (size_t i = 0; i < n; i++) traces[i] = (double)h[i];
+    }
+    if (spectra) {
+        h.resize(2 * n);
+        CU(cudaMemcpyAsync(h.data(), p->spec, 2 * n * sizeof(R), cudaMemcpyDeviceToHost, ctx->stream));
+        CU(cudaStreamSynchronize(ctx->stream));
+        for (size_t i = 0; i < 2 * n; i++) spectra[i] = (double)h[i];
+    }
+    return GRT_OK;
+}
+
+extern "C" int grt_plan_fetch(grt_plan *p, double *traces, double *spectra)
+{
+    if (!p) return GRT_ERR_ARG;
+    grt_ctx *ctx = p->ctx;
+    CU(cudaSetDevice(ctx->device));
+    return p->prec ? fetch<double>(p, traces, spectra) : fetch<float>(p, traces, spectra);
+}
+
+extern "C" int grt_run(grt_ctx *ctx, const grt_model *m, const grt_opts *o, int n_dist, const double *dist,
+                       double *traces, double *spectra, grt_report *r)
+{
+    grt_plan *p = nullptr;
+    int rc = grt_plan_create(ctx, m, o, n_dist, dist, &p);
+    if (rc) return rc;
+    rc = grt_plan_execute(p, r);
+    if (!rc) rc = grt_plan_fetch(p, traces, spectra);
+    grt_plan_destroy(p);
+    return rc;
+}
+
+// ------------------------------------------------------------------ green()
+static int green_impl(const char *iname, const char *oname_w, const char *oname_t, std::string &msg)
+{
+    if (!iname || !oname_w || !oname_t) { msg = "null file name"; return GRT_ERR_ARG; }
+    grt::RawInput in;
+    int rc = grt::read_input(iname, in, msg);
+    if (rc) return rc;
+    const char *pe = getenv("GRT_PRECISION");
+    grt_opts o{};
+    o.dt = in.dt; o.log2n = in.log2n; o.t0 = in.t0; o.taper = in.taper; o.sigma_factor = 2.0;
+    o.k_mode = GRT_K_REFERENCE; o.precision = (pe && !strcmp(pe, "fp64")) ? GRT_FP64 : GRT_FP32; o.fix = 0;
+    grt_model m{(int)in.zt.size(), in.zt.data(), in.vp.data(), in.vs.data(), in.rho.data(), in.qp.data(), in.qs.data(),
+                in.hs, in.hr, in.src};
+    grt_ctx *ctx = nullptr;
+    rc = grt_create(&ctx, 0);
+    if (rc) { msg = "cannot create a CUDA context"; return rc; }
+    grt_plan *p = nullptr;
+    rc = grt_plan_create(ctx, &m, &o, 1, &in.dist, &p);
+    std::vector<double> sig, spec;
+    int N = 0, nc = 0;
+    if (!rc) {
+        N = p->J.N;
+        nc = p->nc;
+        sig.resize((size_t)nc * N);
+        spec.resize((size_t)nc * N * 2);
+        rc = grt_plan_execute(p, nullptr);
+        if (!rc) rc = grt_plan_fetch(p, sig.data(), spec.data());
+        grt_plan_destroy(p);
+    }
+    if (rc) msg = grt_last_error(ctx);
+    grt_destroy(ctx);
+    if (rc) return rc;
+    // writers, green.cu:2242-2258: 30 columns, undefined ones as zero
+    FILE *f = fopen(oname_t, "w");
+    if (!f) { msg = std::string("cannot write ") + oname_t; return GRT_ERR_IO; }
+    for (int n = 0; n < N; n++) {
+        for (int c = 0; c < 30; c++) fprintf(f, "%.18e,", c < nc ? sig[(size_t)c * N + n] : 0.0);
+        fprintf(f, "\n");
+    }
+    fclose(f);
+    f = fopen(oname_w, "w");
+    if (!f) { msg = std::string("cannot write ") + oname_w; return GRT_ERR_IO; }
+    for (int n = 0; n < N; n++) {
+        for (int c = 0; c < 30; c++) {
+            double re = c < nc ? spec[((size_t)c * N + n) * 2] : 0.0, im = c < nc ? spec[((size_t)c * N + n) * 2 + 1] : 0.0;
+            fprintf(f, "%.18e,%.18e,", re, im);
+        }
+        fprintf(f, "\n");
+    }
+    fclose(f);
+    return GRT_OK;
+}
+
+extern "C" int grt_green(const char *iname, const char *oname_w, const char *oname_t)
+{
+    std::string msg;
+    int rc = green_impl(iname, oname_w, oname_t, msg);
+    if (rc) fprintf(stderr, "grt_green: %s (%s)\n", grt_status_string(rc), msg.c_str());
+    return rc;
+}
+
+extern "C" void green(char *iname, char *oname_w, char *oname_t) { (void)grt_green(iname, oname_w, oname_t); }

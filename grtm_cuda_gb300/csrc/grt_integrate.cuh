@@ -1,0 +1,383 @@
+// grt_integrate.cuh -- wavenumber integration and the spectral stage.
+//
+//  bessel_table_kernel  B[j][b][r]: the nine Bessel functions of k_j r the
+//                       integrands use, evaluated once per (k grid, receiver
+//                       set) in FP64 with the reference's own formulas
+//                       (green.cu:1418-1554) -- including the k r argument
+//                       reduction -- and stored in the working precision.
+//  ksum_kernel          S[r][c][iw] = sum_j w_j (integrand c)(w_iw, k_j, r):
+//                       the k-sum of integrate() (green.cu:1873-1903) for all
+//                       receivers at once, driven by the column tables below
+//                       (get_int_val_single / _tensor, green.cu:1558-1716).
+//  spectral_kernel      phase e^{i w t0}, cosine taper and scale
+//                       (green.cu:1905-1921), Hermitian fill (1925-1938),
+//                       inverse DFT and e^{sigma t} de-damping (2227-2239),
+//                       one trace per block, FFT in shared memory.
+#pragma once
+#include "grt_cplx.cuh"
+#include "grt_types.h"
+
+namespace grt {
+
+// ---------------------------------------------------------------- Bessel
+__device__ __forceinline__ double bj0_ref(double x)
+{
+    // Abramowitz & Stegun 9.4.1 / 9.4.3 (as evaluated by the reference)
+    double ax = fabs(x);
+    if (ax <= 3.0) {
+        double y = (ax / 3.0) * (ax / 3.0);
+        return 1.0 + y * (-2.2499997 + y * (1.2656208 + y * (-0.3163866 + y * (0.0444479 + y * (-0.0039444 + y * 0.00021)))));
+    }
+    double t = 3.0 / ax;
+    double f = 0.79788456 + t * (-0.00000077 + t * (-0.0055274 + t * (-0.00009512 + t * (0.00137237 + t * (-0.00072805 + t * 0.00014476)))));
+    double th = ax - 0.78539816 + t * (-0.04166397 + t * (-0.00003954 + t * (0.00262573 + t * (-0.00054125 + t * (-0.00029333 + t * 0.00013558)))));
+    return f * cos(th) / sqrt(ax);
+}
+
+__device__ __forceinline__ double bj1_ref(double x)
+{
+    // Abramowitz & Stegun 9.4.4 / 9.4.6
+    double ax = fabs(x);
+    if (ax <= 3.0) {
+        double y = (ax / 3.0) * (ax / 3.0);
+        return x * (0.5 + y * (-0.56249985 + y * (0.21093573 + y * (-0.03954289 + y * (0.00443319 + y * (-0.00031761 + y * 0.00001109))))));
+    }
+    double t = 3.0 / ax;
+    double f = 0.79788456 + t * (0.00000156 + t * (0.01659667 + t * (0.00017105 + t * (-0.00249511 + t * (0.00113653 + t * (-0.00020033))))));
+    double th = ax - 2.35619449 + t * (0.12499612 + t * (0.0000565 + t * (-0.00637879 + t * (0.00074348 + t * (0.00079824 + t * (-0.00029166))))));
+    return (x >= 0 ? 1.0 : -1.0) * f * cos(th) / sqrt(ax);
+}
+
+// J_n for n >= 0: upward recurrence above n, Miller's downward recurrence
+// below (normalised by J0 + 2 sum J_2m), as green.cu:1467-1529 does
+__device__ __forceinline__ double bjn_ref(double x, int n)
+{
+    if (n == 0) return bj0_ref(x);
+    if (n == 1) return bj1_ref(x);
+    double ax = fabs(x), res;
+    if (ax == 0.0) return 0.0;
+    if (ax > n) {
+        double tox = 2.0 / ax, bjm = bj0_ref(ax), bj = bj1_ref(ax);
+        for (int j = 1; j < n; j++) {
+            double bjp = j * tox * bj - bjm;
+            bjm = bj;
+            bj = bjp;
+        }
+        res = bj;
+    } else {
+        double tox = 2.0 / ax;
+        int m = 2 * ((n + (int)sqrt((double)(40 * n))) / 2);
+        bool acc = false;
+        double sum = 0.0, bjp = 0.0, bj = 1.0;
+        res = 0.0;
+        for (int j = m; j >= 1; j--) {
+            double bjm = j * tox * bj - bjp;
+            bjp = bj;
+            bj = bjm;
+            if (fabs(bj) > 1e10) { bj *= 1e-10; bjp *= 1e-10; res *= 1e-10; sum *= 1e-10; }
+            if (acc) sum += bj;
+            acc = !acc;
+            if (j == n) res = bjp;
+        }
+        sum = 2.0 * sum - bj;
+        res /= sum;
+    }
+    if (x < 0.0 && (n & 1)) res = -res;
+    return res;
+}
+
+__device__ __forceinline__ double dbj_ref(double x, int n)
+{
+    if (fabs(x) < 1e-10) return (bjn_ref(1e-10, n) - bjn_ref(0.0, n)) / 1e-10;
+    return n * bjn_ref(x, n) / x - bjn_ref(x, n + 1);
+}
+
+// the reference's second derivative expression (green.cu:1543-1554)
+__device__ __forceinline__ double ddbj_ref(double x, int n)
+{
+    if (fabs(x) < 1e-10) return (dbj_ref(1e-10, n) - dbj_ref(0.0, n)) / 1e-10;
+    return n * bjn_ref(x, n - 1) / x - bjn_ref(x, n) * (n + n * n + x * x) / x / x;
+}
+
+template <typename R>
+__global__ void bessel_table_kernel(R *B, int nk, int nr, double dk, const double *dist)
+{
+    long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)nk * nr) return;
+    int r = (int)(t % nr);
+    int j = (int)(t / nr);
+    double x = dist[r] * (dk * j);
+    double v[NBASIS];
+    v[BJ0] = bjn_ref(x, 0);
+    v[BJ1] = bjn_ref(x, 1);
+    v[BJ2] = bjn_ref(x, 2);
+    v[BJ0D] = dbj_ref(x, 0);
+    v[BJ1D] = dbj_ref(x, 1);
+    v[BJ2D] = dbj_ref(x, 2);
+    v[BJ0DD] = ddbj_ref(x, 0);
+    v[BJ1DD] = ddbj_ref(x, 1);
+    v[BJ2DD] = ddbj_ref(x, 2);
+#pragma unroll
+    for (int b = 0; b < NBASIS; b++) B[((long long)j * NBASIS + b) * nr + r] = (R)v[b];
+}
+
+// ---------------------------------------------------------------- column tables
+// An integrand column is a sum of terms coef * r^-rpow * (K_q k^kp) J_b(k r).
+struct Pair { int q, kp, b; };
+struct Term { int pair, rpow; double coef; };
+
+// single force, green.cu:1582-1600
+constexpr __device__ Pair kSinglePairs[] = {
+    {QS_B1, 0, BJ1},   {QS_A10, 1, BJ1D},  {QS_A00, 1, BJ0D},  {QS_A10, 0, BJ1},   {QS_B1, 1, BJ1D},
+    {QS_A11, 1, BJ1},  {QS_A01, 1, BJ0},   {QS_B1T, 0, BJ1},   {QS_A1T0, 1, BJ1D}, {QS_A0T0, 1, BJ0D},
+    {QS_A1T0, 0, BJ1}, {QS_B1T, 1, BJ1D},  {QS_A1T1, 1, BJ1},  {QS_A0T1, 1, BJ0},  {QS_A10, 2, BJ1DD},
+    {QS_A00, 2, BJ0DD}, {QS_B1, 2, BJ1DD}, {QS_A11, 2, BJ1D},  {QS_A01, 2, BJ0D},
+};
+constexpr int kSingleNP = sizeof(kSinglePairs) / sizeof(Pair);
+constexpr __device__ Term kSingleTerms[] = {
+    // col 0..4: displacement
+    {0, 1, 1.0}, {1, 0, 1.0},
+    {2, 0, 1.0},
+    {3, 1, 1.0}, {4, 0, 1.0},
+    {5, 0, 1.0},
+    {6, 0, 1.0},
+    // col 5..9: d/dz
+    {7, 1, 1.0}, {8, 0, 1.0},
+    {9, 0, 1.0},
+    {10, 1, 1.0}, {11, 0, 1.0},
+    {12, 0, 1.0},
+    {13, 0, 1.0},
+    // col 10..14: d/dr
+    {0, 2, -1.0}, {4, 0, 1.0}, {14, 0, 1.0},
+    {15, 0, 1.0},
+    {3, 2, -1.0}, {1, 1, 1.0}, {16, 0, 1.0},
+    {17, 0, 1.0},
+    {18, 0, 1.0},
+};
+constexpr __device__ int kSingleCol[16] = {0, 2, 3, 5, 6, 7, 9, 10, 12, 13, 14, 17, 18, 21, 22, 23};  // term ranges
+constexpr int kSingleNC = 15;
+
+// moment tensor, green.cu:1650-1691 (the d/dz block 10-19 is overwritten there)
+constexpr __device__ Pair kTensorPairs[] = {
+    {QT_B2, 0, BJ2},   {QT_A20, 1, BJ2D},  {QT_B1, 0, BJ1},    {QT_A10, 1, BJ1D},  {QT_A21, 1, BJ0D},
+    {QT_A01, 1, BJ0D}, {QT_B2, 1, BJ2D},   {QT_A20, 0, BJ2},   {QT_B2, 1, BJ1D},   {QT_A10, 0, BJ1},
+    {QT_A21, 1, BJ2},  {QT_A11, 1, BJ1},   {QT_A01, 1, BJ0},   {QT_A21, 1, BJ0},   {QT_A20, 2, BJ2DD},
+    {QT_B1, 1, BJ1D},  {QT_A10, 2, BJ1DD}, {QT_A21, 2, BJ0DD}, {QT_A01, 2, BJ0DD}, {QT_B2, 2, BJ2DD},
+    {QT_B2, 2, BJ1DD}, {QT_A21, 2, BJ2D},  {QT_A11, 2, BJ1D},  {QT_A01, 2, BJ0D},  {QT_A21, 2, BJ0D},
+};
+constexpr int kTensorNP = sizeof(kTensorPairs) / sizeof(Pair);
+constexpr __device__ Term kTensorTerms[] = {
+    {0, 1, 2.0}, {1, 0, 1.0},                    // 0
+    {2, 1, 1.0}, {3, 0, 1.0},                    // 1
+    {4, 0, 1.0},                                 // 2
+    {5, 0, 1.0},                                 // 3
+    {6, 0, 1.0}, {7, 1, 2.0},                    // 4
+    {8, 0, 1.0}, {9, 1, 1.0},                    // 5
+    {10, 0, 1.0},                                // 6
+    {11, 0, 1.0},                                // 7
+    {12, 0, 1.0},                                // 8
+    {13, 0, 1.0},                                // 9
+    {0, 2, -2.0}, {6, 1, 2.0}, {14, 0, 1.0},     // 10
+    {2, 2, -1.0}, {15, 1, 1.0}, {16, 0, 1.0},    // 11
+    {17, 0, 1.0},                                // 12
+    {18, 0, 1.0},                                // 13
+    {19, 0, 1.0}, {7, 2, -2.0}, {1, 1, 2.0},     // 14
+    {20, 0, 1.0}, {9, 2, -1.0}, {3, 1, 1.0},     // 15
+    {21, 0, 1.0},                                // 16
+    {22, 0, 1.0},                                // 17
+    {23, 0, 1.0},                                // 18
+    {24, 0, 1.0},                                // 19
+};
+constexpr __device__ int kTensorCol[21] = {0, 2, 4, 5, 6, 8, 10, 11, 12, 13, 14, 17, 20, 21, 22, 25, 28, 29, 30, 31, 32};
+constexpr int kTensorNC = 20;
+
+template <int SRC> struct Cols;
+template <> struct Cols<kSingle> {
+    static constexpr int NP = kSingleNP, NC = kSingleNC, NQ = QS_N;
+    __device__ static constexpr Pair pair(int i) { return kSinglePairs[i]; }
+    __device__ static constexpr Term term(int i) { return kSingleTerms[i]; }
+    __device__ static constexpr int col(int i) { return kSingleCol[i]; }
+};
+template <> struct Cols<kTensor> {
+    static constexpr int NP = kTensorNP, NC = kTensorNC, NQ = QT_N;
+    __device__ static constexpr Pair pair(int i) { return kTensorPairs[i]; }
+    __device__ static constexpr Term term(int i) { return kTensorTerms[i]; }
+    __device__ static constexpr int col(int i) { return kTensorCol[i]; }
+};
+
+// error-free sum s + x = hi + lo (Knuth TwoSum)
+template <typename R> __device__ __forceinline__ void two_sum_acc(R &hi, R &lo, R x)
+{
+    R s = hi + x;
+    R bp = s - hi;
+    R e = (hi - (s - bp)) + (x - bp);
+    hi = s;
+    lo += e;
+}
+
+constexpr int kSumThreads = 128;
+constexpr int kSumChunk = 16;   // k-steps accumulated plainly before a compensated fold
+
+template <typename R>
+struct KsumArgs {
+    const R *K;            // [nq][nkw] complex
+    const R *B;            // [nkmax][NBASIS][nr]
+    const int *nk;         // [nw]
+    const long long *koff; // [nw]
+    const double *dist;    // [nr]
+    R *S;                  // [nr][nc][nw] complex
+    long long nkw;
+    double dk;
+    int nw, nr, rt, jt;    // receivers per block, k-lanes per receiver (rt * jt = 128)
+};
+
+// One thread per (w, receiver, k-lane); k-lanes of a receiver reduce at the end.
+template <typename R, int SRC>
+__global__ void __launch_bounds__(kSumThreads) ksum_kernel(KsumArgs<R> A)
+{
+    using CT = Cols<SRC>;
+    constexpr int NP = CT::NP, NC = CT::NC;
+    __shared__ R red[kSumThreads * 2];
+    const int ntile = (A.nr + A.rt - 1) / A.rt;
+    const int iw = blockIdx.x / ntile;
+    const int r0 = (blockIdx.x % ntile) * A.rt;
+    const int rloc = threadIdx.x % A.rt, lane = threadIdx.x / A.rt;
+    const int r = r0 + rloc;
+    const bool rvalid = r < A.nr;
+    const int rr = rvalid ? r : 0;
+    const int nk = A.nk[iw];
+    const long long off = A.koff[iw];
+    const C<R> *K = reinterpret_cast<const C<R> *>(A.K);
+
+    R hi[NP][2], lo[NP][2];
+#pragma unroll
+    for (int p = 0; p < NP; p++) hi[p][0] = hi[p][1] = lo[p][0] = lo[p][1] = R(0);
+
+    for (int jb = lane * kSumChunk; jb < nk; jb += A.jt * kSumChunk) {
+        R acc[NP][2];
+#pragma unroll
+        for (int p = 0; p < NP; p++) acc[p][0] = acc[p][1] = R(0);
+        const int je = min(jb + kSumChunk, nk);
+        for (int j = jb; j < je; j++) {
+            const double kd = A.dk * j;
+            const R k = (R)kd;
+            const R w = (j == 0) ? (R)(0.5 * A.dk) : (R)A.dk;
+            const R wk[3] = {w, w * k, w * k * k};
+            const R *Bj = A.B + (long long)j * NBASIS * A.nr + rr;
+            R bv[NBASIS];
+#pragma unroll
+            for (int b = 0; b < NBASIS; b++) bv[b] = Bj[(long long)b * A.nr];
+#pragma unroll
+            for (int p = 0; p < NP; p++) {
+                constexpr int dummy = 0;
+                (void)dummy;
+                const Pair P = CT::pair(p);
+                const C<R> kq = K[(long long)P.q * A.nkw + off + j];
+                const R f = wk[P.kp] * bv[P.b];
+                acc[p][0] += kq.x * f;
+                acc[p][1] += kq.y * f;
+            }
+        }
+#pragma unroll
+        for (int p = 0; p < NP; p++) {
+            two_sum_acc(hi[p][0], lo[p][0], acc[p][0]);
+            two_sum_acc(hi[p][1], lo[p][1], acc[p][1]);
+        }
+    }
+    // reduce the k-lanes of each receiver, pair by pair
+    const double dr = A.dist[rr];
+    R col[NC][2];
+#pragma unroll
+    for (int c = 0; c < NC; c++) col[c][0] = col[c][1] = R(0);
+#pragma unroll
+    for (int p = 0; p < NP; p++) {
+        R v0 = hi[p][0] + lo[p][0], v1 = hi[p][1] + lo[p][1];
+        if (A.jt > 1) {
+            __syncthreads();
+            red[2 * threadIdx.x] = v0;
+            red[2 * threadIdx.x + 1] = v1;
+            __syncthreads();
+            if (lane == 0) {
+                R s0 = 0, s1 = 0, c0 = 0, c1 = 0;
+                for (int l = 0; l < A.jt; l++) {
+                    two_sum_acc(s0, c0, red[2 * (l * A.rt + rloc)]);
+                    two_sum_acc(s1, c1, red[2 * (l * A.rt + rloc) + 1]);
+                }
+                v0 = s0 + c0;
+                v1 = s1 + c1;
+            }
+        }
+        // scatter the pair into the columns that use it
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+#pragma unroll
+            for (int t = CT::col(c); t < CT::col(c + 1); t++) {
+                const Term T = CT::term(t);
+                if (T.pair == p) {
+                    const R sc = (R)(T.coef / (T.rpow == 0 ? 1.0 : (T.rpow == 1 ? dr : dr * dr)));
+                    col[c][0] += sc * v0;
+                    col[c][1] += sc * v1;
+                }
+            }
+        }
+    }
+    if (lane != 0 || !rvalid) return;
+    C<R> *S = reinterpret_cast<C<R> *>(A.S);
+#pragma unroll
+    for (int c = 0; c < NC; c++) S[((long long)r * NC + c) * A.nw + iw] = C<R>{col[c][0], col[c][1]};
+}
+
+// ---------------------------------------------------------------- spectral stage
+template <typename R>
+struct SpecArgs {
+    const R *S;            // [ntr][nw] complex  (ntr = nr * nc traces)
+    const R *post;         // [nw] complex: e^{i w t0} * taper * df nw / pi
+    const R *tw;           // [N/2] complex: e^{+2 pi i m / N}
+    const double *damp;    // [N]: e^{sigma (n dt + t0)} / N
+    R *spec_out;           // [ntr][N] complex or null
+    R *sig_out;            // [ntr][N] or null (working precision)
+    int nw, logn;
+};
+
+template <typename R>
+__global__ void __launch_bounds__(512) spectral_kernel(SpecArgs<R> A)
+{
+    extern __shared__ __align__(16) unsigned char smem_spec[];
+    C<R> *x = reinterpret_cast<C<R> *>(smem_spec);
+    const int N = 1 << A.logn, nw = A.nw;
+    const long long tr = blockIdx.x;
+    const C<R> *S = reinterpret_cast<const C<R> *>(A.S) + tr * nw;
+    const C<R> *post = reinterpret_cast<const C<R> *>(A.post);
+    const C<R> *tw = reinterpret_cast<const C<R> *>(A.tw);
+    // full spectrum Y (reference's `out` after Hermitian fill), loaded bit-reversed
+    for (int n = threadIdx.x; n < N; n += blockDim.x) {
+        C<R> y;
+        if (n < nw) y = S[n] * post[n];
+        else if (n == nw) y = C<R>{R(0), R(0)};
+        else y = conj(S[N - n] * post[N - n]);
+        if (A.spec_out) reinterpret_cast<C<R> *>(A.spec_out)[tr * N + n] = y;
+        unsigned rev = __brev((unsigned)n) >> (32 - A.logn);
+        x[rev] = y;
+    }
+    __syncthreads();
+    // in-place radix-2 decimation in time, exp(+2 pi i) kernel
+    for (int s = 1; s <= A.logn; s++) {
+        const int half = 1 << (s - 1);
+        const int tstride = N >> s;
+        for (int b = threadIdx.x; b < N / 2; b += blockDim.x) {
+            const int grp = b >> (s - 1), pos = b & (half - 1);
+            const int i0 = grp * (half << 1) + pos, i1 = i0 + half;
+            const C<R> w = tw[pos * tstride];
+            const C<R> u = x[i0], v = x[i1] * w;
+            x[i0] = u + v;
+            x[i1] = u - v;
+        }
+        __syncthreads();
+    }
+    if (A.sig_out) {
+        for (int n = threadIdx.x; n < N; n += blockDim.x)
+            A.sig_out[tr * N + n] = (R)((double)x[n].x * A.damp[n]);
+    }
+}
+
+}  // namespace grt

@@ -1,0 +1,184 @@
+// grt_job.cpp -- input parsing, source-interface insertion, grid and k grid.
+// Rules follow the reference's host code in cusrc/popm/func/green.cu (cited
+// per function) so that a reference input file gives the same layer table,
+// the same (w,k) list and the same receiver/source placement.
+#include "grt_job.h"
+
+#include <cmath>
+#include <complex>
+#include <cstdio>
+
+namespace grt {
+
+using cd = std::complex<double>;
+static const double PI = 3.1415926535897932384626433;
+
+// green.cu:2001-2049: a copy of the layer holding the source starts at hs when
+// ztop[i-1] < hs < ztop[i]; then thicknesses and mu = b0^2 rho.  The
+// reference always adds one layer, reading uninitialised memory when nothing
+// was inserted; here the layer count is kept in that case.
+static int finish(Job &J, int n, const double *zt, const double *vp, const double *vs, const double *rh,
+                  const double *qp, const double *qs, std::string &err)
+{
+    if (n < 2) { err = "need at least one layer over a half-space"; return kErrModel; }
+    for (int i = 1; i < n; i++)
+        if (!(zt[i] > zt[i - 1])) { err = "layer tops must increase"; return kErrModel; }
+    for (int i = 0; i < n; i++)
+        if (!(vp[i] > 0 && vs[i] > 0 && rh[i] > 0 && qp[i] > 0 && qs[i] > 0 && vp[i] > vs[i])) {
+            err = "layer " + std::to_string(i) + ": need vp > vs > 0, rho > 0, Q > 0";
+            return kErrModel;
+        }
+    J.h.clear(); J.a0.clear(); J.b0.clear(); J.rho.clear(); J.qp.clear(); J.qs.clear();
+    J.inserted = false;
+    auto push = [&](double z, int i) {
+        J.h.push_back(z); J.a0.push_back(vp[i]); J.b0.push_back(vs[i]);
+        J.rho.push_back(rh[i]); J.qp.push_back(qp[i]); J.qs.push_back(qs[i]);
+    };
+    for (int i = 0; i < n; i++) {
+        if (i > 0 && zt[i - 1] < J.hs && zt[i] > J.hs) { push(J.hs, i - 1); J.inserted = true; }
+        push(zt[i], i);
+    }
+    if (!J.inserted && J.hs > zt[n - 1]) { err = "source in the half-space is not supported"; return kErrModel; }
+    if (J.hs < 0 || J.hr < 0) { err = "depths must be >= 0"; return kErrModel; }
+    J.L = (int)J.h.size();
+    if (J.L > 256) { err = "too many layers (max 256 after insertion)"; return kErrModel; }
+    J.vmax = 0; J.vmin = 100000;
+    for (int i = 0; i < J.L; i++) {                      // green.cu:2034-2037
+        J.vmax = std::max(J.vmax, J.a0[i]);
+        J.vmin = std::min(J.vmin, J.b0[i]);
+    }
+    for (int i = 0; i < J.L - 1; i++) J.h[i] = J.h[i + 1] - J.h[i];
+    J.mu.resize(J.L);
+    for (int i = 0; i < J.L; i++) J.mu[i] = J.b0[i] * J.b0[i] * J.rho[i];
+    return kOk;
+}
+
+int job_from_layers(int n, const double *ztop, const double *vp, const double *vs, const double *rho,
+                    const double *qp, const double *qs, double hs, double hr, int src, Job &J,
+                    std::string &err)
+{
+    if (!ztop || !vp || !vs || !rho || !qp || !qs) { err = "null layer array"; return kErrArg; }
+    J = Job();
+    J.hs = hs; J.hr = hr; J.src = src ? 1 : 0;
+    return finish(J, n, ztop, vp, vs, rho, qp, qs, err);
+}
+
+int read_input(const char *path, RawInput &in, std::string &err)
+{
+    FILE *f = fopen(path, "r");
+    if (!f) { err = std::string("cannot open ") + path; return kErrIo; }
+    int n = 0;
+    bool ok = fscanf(f, "%lf %lf %d", &in.hs, &in.hr, &n) == 3 && n >= 2 && n <= 255;
+    if (ok) {
+        in.zt.resize(n); in.vp.resize(n); in.vs.resize(n); in.rho.resize(n); in.qp.resize(n); in.qs.resize(n);
+    }
+    for (int i = 0; ok && i < n; i++)
+        ok = fscanf(f, " %lf , %lf , %lf , %lf , %lf , %lf", &in.zt[i], &in.vp[i], &in.vs[i], &in.rho[i], &in.qp[i],
+                    &in.qs[i]) == 6;
+    ok = ok && fscanf(f, "%lf %lf %d %d %lf %d %lf %lf %d %d", &in.dt, &in.dist, &in.nf1, &in.nf2, &in.twin,
+                      &in.log2n, &in.t0, &in.taper, &in.n_ptam, &in.src) == 10;
+    fclose(f);
+    if (!ok) { err = std::string("malformed input file ") + path; return kErrParse; }
+    return kOk;
+}
+
+// cal_kmax, green.cu:108-162
+static double cal_kmax(const Job &J, cd w, const std::vector<cd> &b, int nf)
+{
+    const int s = J.s, r = J.rl;
+    double pmin = 0, dz = 0, kmax;
+    auto sl = [&](int i) { return std::abs(w / b[i]); };
+    if (r == s - 1) {
+        pmin = std::max(sl(s), sl(s - 1));
+        dz = std::min(J.zs, J.h[r] - J.zr);
+    } else if (r < s - 1) {
+        pmin = std::max(sl(s), sl(s - 1));
+        dz = std::min(J.zs, J.hs - J.hr);
+        for (int l = r; l <= s - 2; l++) {
+            pmin = std::max(pmin, sl(l + 1));
+            dz = std::min(dz, J.h[l]);
+        }
+    } else if (r == s) {
+        pmin = sl(s);
+        dz = std::fabs(J.hr - J.hs);
+    } else if (r == s + 1) {
+        pmin = std::max(sl(s), sl(s + 1));
+        dz = std::min(J.h[s] - J.zs, J.zr);
+    } else {
+        pmin = std::max(sl(s), sl(s + 1));
+        dz = std::min(J.h[s] - J.zs, std::fabs(J.hr - J.hs));
+        for (int l = s + 1; l < r - 1; l++) {
+            pmin = std::max(pmin, sl(l));
+            dz = std::min(dz, J.h[l]);
+        }
+    }
+    if (dz < 0.2) kmax = nf < 10 ? std::min(pmin + 2.0, 20. * pmin) : std::min(pmin + 2.0, 2.0 * pmin);
+    else kmax = std::sqrt((3.0 / dz) * (3.0 / dz) + pmin * pmin);
+    if (kmax - pmin < 0.5) kmax = pmin + 0.5;
+    return kmax;
+}
+
+int job_setup(Job &J, double dt, int log2n, double t0, double taper, double sigma_factor, int k_mode,
+              int nk_fixed, double dk_override, int fix, std::string &err)
+{
+    if (!(dt > 0) || log2n < 2 || log2n > 15) { err = "need dt > 0 and 2 <= log2n <= 15"; return kErrArg; }
+    if (!(taper >= 0 && taper <= 1)) { err = "taper must be in [0, 1]"; return kErrArg; }
+    if (!(sigma_factor > 0)) { err = "sigma_factor must be > 0"; return kErrArg; }
+    if (k_mode == 1 && nk_fixed < 2) { err = "fixed k grid needs nk >= 2"; return kErrArg; }
+    J.dt = dt; J.log2n = log2n; J.t0 = t0; J.taper = taper; J.k_mode = k_mode; J.nk_fixed = nk_fixed;
+    J.fix = fix;
+    // green.cu:2065-2080
+    J.nw = 1 << (log2n - 1);
+    J.N = 2 * J.nw;
+    const double T = J.N * dt;
+    J.df = 1.0 / T;
+    J.sigma = sigma_factor / T;
+    const double vavg = 0.5 * (J.vmax + J.vmin);
+    double Lw = 2.0 * (J.vmax * T + J.vmax / vavg * std::fabs(J.hs - J.hr) + 100.0);
+    J.dk = dk_override > 0 ? dk_override : 2 * PI / Lw;
+    // source layer, green.cu:2081-2090 (the source sits at the bottom of the
+    // layer above an inserted interface)
+    double hs = J.hs, hr = J.hr;
+    J.s = -1;
+    for (int i = 0; i < J.L; i++) {
+        if (hs <= J.h[i]) { J.s = i; J.zs = hs; break; }
+        hs -= J.h[i];
+    }
+    // receiver layer, green.cu:2092-2101: the reference tests the reduced
+    // source depth; the corrected rule (fix bit 1) tests the receiver depth
+    J.rl = -1;
+    for (int i = 0; i < J.L; i++) {
+        double probe = (fix & 1) ? hr : hs;
+        if (probe <= J.h[i]) { J.rl = i; J.zr = hr; break; }
+        hr -= J.h[i];
+    }
+    if (J.s < 0 || J.s > J.L - 2) { err = "source must lie above the half-space"; return kErrModel; }
+    if (J.rl < 0) { err = "receiver layer not found"; return kErrModel; }
+    // wavenumber grid: ragged per-frequency k_max (green.cu:2145-2194) or fixed
+    J.nk.assign(J.nw, 0);
+    J.koff.assign(J.nw, 0);
+    long long tot = 0;
+    J.nkmax = 0;
+    std::vector<cd> b(J.L);
+    for (int iw = 0; iw < J.nw; iw++) {
+        int nk;
+        if (k_mode == 1) {
+            nk = nk_fixed;
+        } else {
+            cd w(2 * PI * J.df * iw, -J.sigma);
+            cd lw = std::log(w / (2 * PI));
+            for (int i = 0; i < J.L; i++) b[i] = J.b0[i] * (1.0 + lw / (PI * J.qs[i]) + cd(0, 1) / (2.0 * J.qs[i]));
+            double km = iw < 3 ? cal_kmax(J, cd(2 * PI * J.df * 3.0, -J.sigma), b, iw) : cal_kmax(J, w, b, iw);
+            km *= 1.1;  // k_factor, green.cu:2063
+            nk = (int)(km / J.dk) + 2;
+        }
+        J.nk[iw] = nk;
+        J.koff[iw] = tot;
+        tot += nk;
+        J.nkmax = std::max(J.nkmax, nk);
+    }
+    J.nkw = tot;
+    return kOk;
+}
+
+}  // namespace grt

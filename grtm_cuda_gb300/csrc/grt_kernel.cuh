@@ -1,0 +1,477 @@
+// grt_kernel.cuh -- the per-(w,k) generalized reflection/transmission kernel.
+//
+// One thread evaluates one (w,k) point for one layered model: interface
+// coefficients, the bottom-up and top-down generalized R/T recursions, the
+// source terms and the receiver coefficients, and writes the receiver
+// coefficients (b1, a0, a1, ... of get_ypars_a_single / _tensor,
+// green.cu:615-1267) for the wavenumber integration.
+//
+// The reference materialises every stage in HBM (about 2.6 KB per
+// (w,k,layer)) and solves each interface with batched cuBLAS 4x4 inverses and
+// GEMMs, (L-1) times over (green.cu:1810-1818).  Here everything stays in
+// registers, the interface solve is closed form, and the recursion is written
+// in a basis in which every quantity stays O(1) as w -> 0, so that FP32 is
+// accurate at all frequencies:
+//   layer eigenvectors   p = (k, r, -2 mu k r, -mu x),
+//                        d = (w/a E_P - w/b E_SV) / (r - v)
+//   with r - v = (wb^2 - wa^2)/(r + v), k - v = wb^2/(k + v), k - r = wa^2/(k + r)
+//   phase matrices       [[e^{-rz}, (e^{-rz} - e^{-vz})/(r - v)], [0, e^{-vz}]]
+//   interface            P = G_D^-1 G_U, Q = H_D^-1 H_U (G, H: even/odd rows of E_d)
+//                        Rd = -(P+Q)^-1 (P-Q), Tu = 2 (P+Q)^-1,
+//                        Td = 2 Q (P+Q)^-1 P,  Ru = (P-Q)(P+Q)^-1
+// The layer table of the block's frequency is staged in shared memory with a
+// TMA bulk copy (cp.async.bulk) completing on an mbarrier.
+#pragma once
+#include "grt_cplx.cuh"
+#include "grt_types.h"
+
+namespace grt {
+
+// ---------------------------------------------------------------- layer data
+template <typename R>
+struct SL {
+    C<R> r, v, rmv, irmv;       // vertical wavenumbers, r - v, 1/(r - v)
+    C<R> p1, p2, p3;            // p0 = k
+    C<R> d0, d1, d2, d3;
+    C<R> detG, detH;
+    C<R> x;
+    R mu;
+};
+
+template <typename R>
+__device__ __forceinline__ void make_layer(const LayerW<R> &T, double k2, R k, SL<R> &L)
+{
+    // branch selection in FP64: Re(k^2 - wa^2) cancels near the branch point
+    C<R> zr = {(R)(k2 - T.wa2x), (R)(-T.wa2y)};
+    C<R> zv = {(R)(k2 - T.wb2x), (R)(-T.wb2y)};
+    L.r = csqrt_(zr);
+    L.v = csqrt_(zv);
+    L.x = C<R>{(R)(2.0 * k2 - T.wb2x), (R)(-T.wb2y)};  // k^2 + v^2 = 2k^2 - wb^2
+    const C<R> wa2 = {T.wa2[0], T.wa2[1]}, wb2 = {T.wb2[0], T.wb2[1]};
+    const C<R> W = {T.W[0], T.W[1]}, iW = {T.iW[0], T.iW[1]};
+    C<R> rpv = L.r + L.v;
+    L.irmv = rpv * iW;                 // 1/(r - v)
+    L.rmv = W * rcp(rpv);              // r - v
+    C<R> dv = wb2 * rcp(k + L.v);      // k - v
+    C<R> dr = wa2 * rcp(k + L.r);      // k - r
+    const R mu = T.mu;
+    L.mu = mu;
+    L.p1 = L.r;
+    L.p2 = L.r * (R(-2) * mu * k);
+    L.p3 = L.x * (-mu);
+    L.d0 = dv * L.irmv;
+    L.d1 = -(dr * L.irmv);
+    L.d2 = (dr * dr - W) * L.irmv * mu;
+    L.d3 = dv * dv * L.irmv * (-mu);
+    C<R> m = wb2 * rpv * iW * mu;      // mu wb^2 / (r - v)
+    L.detG = L.v * m;
+    L.detH = -(L.r * m);
+}
+
+// S^-1 diag(e^{-rz}, e^{-vz}) S  (upper triangular)
+template <typename R>
+__device__ __forceinline__ M2<R> phase(const SL<R> &L, R z, C<R> *ev_out = nullptr)
+{
+    C<R> er = cexp_(L.r * (-z)), ev = cexp_(L.v * (-z));
+    C<R> y = L.rmv * (-z);
+    C<R> dd;
+    if (abs2(y) < R(0.25)) dd = ev * expm1_over_small(y) * (-z);
+    else dd = (er - ev) * L.irmv;
+    if (ev_out) *ev_out = ev;
+    return {er, dd, {R(0), R(0)}, ev};
+}
+
+// S^-1 diag(sg r0 e^{-rz}, sg v0 e^{-vz}) S; r0, v0 = own nu unless given
+template <typename R>
+__device__ __forceinline__ M2<R> dphase(const SL<R> &L, R z, R sg, const C<R> *nu0)
+{
+    C<R> er = cexp_(L.r * (-z)), ev = cexp_(L.v * (-z));
+    C<R> y = L.rmv * (-z);
+    C<R> dd;
+    if (abs2(y) < R(0.25)) dd = ev * expm1_over_small(y) * (-z);
+    else dd = (er - ev) * L.irmv;
+    C<R> r0, v0, off;
+    if (!nu0) {
+        r0 = L.r; v0 = L.v;
+        off = er + L.v * dd;                       // (r e_r - v e_v)/(r - v)
+    } else {
+        r0 = nu0[0]; v0 = nu0[1];
+        off = r0 * dd + ev * (r0 - v0) * L.irmv;   // (r0 e_r - v0 e_v)/(r - v)
+    }
+    return {r0 * er * sg, off * sg, {R(0), R(0)}, v0 * ev * sg};
+}
+
+template <typename R>
+struct IF {
+    M2<R> td, tu, rd, ru;
+    C<R> tdd0, tuu0, rdu0;  // rud0 = -rdu0
+};
+
+// interface between U (upper layer) and D (lower layer)
+template <typename R>
+__device__ __forceinline__ void interface_rt(const SL<R> &U, const SL<R> &D, R k, IF<R> &m)
+{
+    const C<R> kk = {k, R(0)};
+    M2<R> GU = {kk, U.d0, U.p3, U.d3}, HU = {U.p1, U.d1, U.p2, U.d2};
+    M2<R> GDi = inv_det(M2<R>{kk, D.d0, D.p3, D.d3}, D.detG);
+    M2<R> HDi = inv_det(M2<R>{D.p1, D.d1, D.p2, D.d2}, D.detH);
+    M2<R> P = GDi * GU, Q = HDi * HU;
+    M2<R> S = P + Q, Dm = P - Q;
+    M2<R> Si = inv(S);
+    m.rd = (Si * Dm) * R(-1);
+    m.tu = Si * R(2);
+    m.td = (Q * (Si * P)) * R(2);
+    m.ru = Dm * Si;
+    // SH (get_mrt_sh, green.cu:339-353)
+    C<R> wa = U.v * U.mu, wb = D.v * D.mu;
+    C<R> is = rcp(wa + wb);
+    m.tdd0 = wa * is * R(2);
+    m.rdu0 = (wa - wb) * is;
+    m.tuu0 = wb * is * R(2);
+}
+
+template <typename R>
+__device__ __forceinline__ void store_q(const GrtArgs<R> &A, int q, long long idx, C<R> v)
+{
+    reinterpret_cast<C<R> *>(A.K)[(long long)q * A.nkw + idx] = v;
+}
+
+// bounded wait on an mbarrier phase; gives up (error word) instead of hanging
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned int *err)
+{
+    uint32_t done = 0;
+    for (int it = 0; it < (1 << 22); it++) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    if (err) atomicOr(err, 1u);
+    return false;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kGrtThreads) grt_point_kernel(GrtArgs<R> A)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) unsigned long long bar;
+    LayerW<R> *T = reinterpret_cast<LayerW<R> *>(smem_raw);
+
+    const int2 tile = A.tiles[blockIdx.x];
+    const int iw = tile.x;
+    const int j = tile.y + threadIdx.x;
+    const int L = A.L, s = A.s, rl = A.rl;
+    const unsigned bytes = (unsigned)(L * sizeof(LayerW<R>));
+    const uint32_t sbar = (uint32_t)__cvta_generic_to_shared(&bar);
+    const uint32_t sdst = (uint32_t)__cvta_generic_to_shared(T);
+
+    // ---- stage the frequency's layer table: TMA bulk copy -> mbarrier
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sbar) : "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const LayerW<R> *src = A.tab + (size_t)iw * L;
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(sbar), "r"(bytes) : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(sdst),
+            "l"(src), "r"(bytes), "r"(sbar)
+            : "memory");
+    }
+    if (!mbar_wait(sbar, 0, A.err)) return;
+
+    const bool valid = j < A.nk[iw];
+    const int jj = valid ? j : 0;           // idle lanes compute k = 0 and store nothing
+    const double kd = A.dk * jj;
+    const double k2 = kd * kd;
+    const R k = (R)kd;
+    const C<R> zero = {R(0), R(0)};
+
+    // ---------------- bottom-up pass: R^du and T^d from the half-space to s+1
+    SL<R> D, U;
+    make_layer(T[L - 1], k2, k, D);
+    M2<R> Rdu = zero2<R>();
+    C<R> rdu0 = zero;
+    M2<R> PD = eye2<R>();      // r_layer > s: Td(rl) Lam(rl-1) ... Td(s+1)
+    C<R> pd0 = {R(1), R(0)};
+    // receiver coefficients (u0, u0t, U, Ut) -- filled by the pass that sees rl
+    M2<R> Urec = zero2<R>(), Utrec = zero2<R>();
+    C<R> u0 = zero, u0t = zero;
+    const C<R> slot0[2] = {{A.slot0[0], A.slot0[1]}, {A.slot0[2], A.slot0[3]}};
+    const C<R> *nu0 = (A.fix & kFixRexut) ? nullptr : slot0;
+    const R zr = (R)A.zr;
+
+    for (int jf = L - 2; jf >= s; jf--) {
+        make_layer(T[jf], k2, k, U);
+        IF<R> m;
+        interface_rt(U, D, k, m);
+        M2<R> Tdn;
+        C<R> td0n;
+        if (jf == L - 2) {
+            Rdu = m.rd;
+            rdu0 = m.rdu0;
+            Tdn = m.td;
+            td0n = m.tdd0;
+        } else {
+            C<R> ev;
+            M2<R> Lam = phase(D, T[jf + 1].h, &ev);
+            // SH, green.cu:537-548
+            C<R> tem1 = (-m.rdu0) * ev, tem2 = rdu0 * ev, tem3 = m.tuu0 * ev;
+            td0n = m.tdd0 * rcp(R(1) - tem1 * tem2);
+            rdu0 = m.rdu0 + tem3 * tem2 * td0n;
+            // P-SV, green.cu:556-587
+            M2<R> X = ut_mul_right(ut_mul_left(Lam, Rdu), Lam);
+            M2<R> Am = eye_minus(m.ru * X);
+            M2<R> Bm = m.tu * X;
+            Tdn = inv(Am) * m.td;
+            Rdu = m.rd + Bm * Tdn;
+            if (rl > s && jf + 1 < rl) {
+                PD = ut_mul_right(PD, Lam) * Tdn;
+                pd0 = pd0 * ev * td0n;
+            }
+        }
+        if (rl > s && jf + 1 == rl) {
+            PD = Tdn;
+            pd0 = td0n;
+        }
+        if (rl > s && jf == rl) {
+            // receiver below the source, inside layer rl (corrected form)
+            C<R> exv, ldv, luv;
+            M2<R> Ld = phase(U, zr, &ldv), Lu = phase(U, (R)A.hr_layer - zr, &luv);
+            M2<R> Ldt = dphase(U, zr, R(-1), (const C<R> *)nullptr);
+            M2<R> Lut = dphase(U, (R)A.hr_layer - zr, R(1), nu0);
+            M2<R> Ex = phase(U, (R)A.hr_layer, &exv);
+            M2<R> Ed = {{k, R(0)}, U.d0, U.p1, U.d1}, Eu = {{k, R(0)}, U.d0, -U.p1, -U.d1};
+            M2<R> RE = Rdu * Ex;
+            Urec = Ed * Ld + Eu * ut_mul_left(Lu, RE);
+            Utrec = Ed * Ldt + Eu * ut_mul_left(Lut, RE);
+            u0 = luv * rdu0 * exv + ldv;
+            u0t = Lut.d * rdu0 * exv - U.v * ldv;
+        }
+        D = U;
+    }
+    if (rl > s && rl == L - 1) {
+        // receiver in the half-space: only the down-going field
+        make_layer(T[L - 1], k2, k, U);
+        C<R> ldv;
+        M2<R> Ld = phase(U, zr, &ldv);
+        M2<R> Ldt = dphase(U, zr, R(-1), (const C<R> *)nullptr);
+        M2<R> Ed = {{k, R(0)}, U.d0, U.p1, U.d1};
+        Urec = Ed * Ld;
+        Utrec = Ed * Ldt;
+        u0 = ldv;
+        u0t = -(U.v * ldv);
+    }
+    const M2<R> RD = Rdu;      // R^du at the bottom of the source layer
+    const C<R> RD0 = rdu0;
+
+    // ---------------- top-down pass: R^ud and T^u from the free surface to s
+    make_layer(T[0], k2, k, U);
+    M2<R> Rud;
+    {
+        // free surface: R = T^-1 diag(1,-1) T, T = stress rows of E_d,
+        // det T = mu^2 (x^2 - 4 k^2 r v)/(r - v) without cancellation
+        C<R> dv = C<R>{T[0].wb2[0], T[0].wb2[1]} * rcp(k + U.v);
+        C<R> dr = C<R>{T[0].wa2[0], T[0].wa2[1]} * rcp(k + U.r);
+        C<R> W = {T[0].W[0], T[0].W[1]};
+        C<R> ray = U.x * (dr * dr - W) + U.r * dv * dv * (R(2) * k);
+        C<R> detT = ray * U.irmv * (U.mu * U.mu);
+        M2<R> Tm = {U.p2, U.d2, U.p3, U.d3};
+        M2<R> adj = {Tm.d, -Tm.b, -Tm.c, Tm.a};
+        M2<R> DT = {Tm.a, Tm.b, -Tm.c, -Tm.d};
+        Rud = (adj * DT) * rcp(detT);
+    }
+    C<R> rud0 = {R(1), R(0)};
+    M2<R> PC = eye2<R>();      // r_layer < s: Tu(rl+1) Lam(rl+1) ... Tu(s)
+    C<R> pc0 = {R(1), R(0)};
+    for (int jf = 0; jf < s; jf++) {
+        if (jf == rl) {
+            // receiver above the source, inside layer rl (green.cu:775-857)
+            C<R> exv, ldv, luv = zero;
+            const bool last = false;
+            (void)last;
+            M2<R> Ld = phase(U, zr, &ldv), Lu = phase(U, (R)A.hr_layer - zr, &luv);
+            M2<R> Ldt = dphase(U, zr, R(-1), (const C<R> *)nullptr);
+            M2<R> Lut = dphase(U, (R)A.hr_layer - zr, R(1), nu0);
+            M2<R> Ex = phase(U, (R)A.hr_layer, &exv);
+            M2<R> Ed = {{k, R(0)}, U.d0, U.p1, U.d1}, Eu = {{k, R(0)}, U.d0, -U.p1, -U.d1};
+            M2<R> RE = Rud * Ex;
+            Urec = Ed * ut_mul_left(Ld, RE) + Eu * Lu;
+            Utrec = Ed * ut_mul_left(Ldt, RE) + Eu * Lut;
+            u0 = ldv * rud0 * exv + luv;
+            u0t = -(U.v * ldv * rud0 * exv) + Lut.d;
+        }
+        make_layer(T[jf + 1], k2, k, D);
+        IF<R> m;
+        interface_rt(U, D, k, m);
+        C<R> ev;
+        M2<R> Lam = phase(U, T[jf].h, &ev);
+        // SH, green.cu:476-482
+        C<R> tem1 = rud0 * ev, tem2 = m.rdu0 * ev, tem3 = m.tdd0 * ev;
+        C<R> tu0n = m.tuu0 * rcp(R(1) - tem1 * tem2);
+        rud0 = (-m.rdu0) + tem3 * tem1 * tu0n;
+        // P-SV, green.cu:486-519
+        M2<R> X = ut_mul_right(ut_mul_left(Lam, Rud), Lam);
+        M2<R> Am = eye_minus(m.rd * X);
+        M2<R> Bm = m.td * X;
+        M2<R> Tun = inv(Am) * m.tu;
+        Rud = m.ru + Bm * Tun;
+        if (rl < s) {
+            if (jf == rl) {
+                PC = Tun;
+                pc0 = tu0n;
+            } else if (jf > rl) {
+                PC = ut_mul_right(PC, Lam) * Tun;
+                pc0 = pc0 * ev * tu0n;
+            }
+        }
+        U = D;
+    }
+    // U now holds the source layer
+    const M2<R> RU = Rud;
+    const C<R> RU0 = rud0;
+    const SL<R> &S = U;
+    const R zs = (R)A.zs, hs = (R)A.hs_layer;
+
+    // ---------------- source terms (get_src_single / _tensor, green.cu:1271-1413)
+    C<R> sexd1, sexu1;
+    M2<R> Ldn = phase(S, hs - zs, &sexd1), Lup = phase(S, zs, &sexu1);
+    M2<R> ED = ut_mul_right(ut_mul_left(Ldn, RD), Ldn);
+    M2<R> EU = ut_mul_right(ut_mul_left(Lup, RU), Lup);
+    const bool up = (rl < s) || (rl == s && A.zr <= A.zs);
+    // the reverberation and source jump, on the side the receiver sees
+    M2<R> ypsv = up ? inv(eye_minus(ED * EU)) : inv(eye_minus(EU * ED));
+    C<R> y_sh = rcp(R(1) - sexd1 * RD0 * sexd1 * sexu1 * RU0 * sexu1);
+    const R smu = S.mu;
+    C<R> ssh = rcp(S.v * (R(2) * smu));
+    C<R> fu = R(1) + sexd1 * RD0 * sexd1;       // 1 + e R^du e (SH)
+    C<R> fd = sexu1 * RU0 * sexu1;              // e R^ud e (SH)
+    // even / odd source vectors in this basis: f0 = 1/2 G^-1 e3, f1 = -1/2 H^-1 e2
+    C<R> iG = rcp(S.detG), iH = rcp(S.detH);
+    C<R> f1a = S.d1 * iH * R(0.5), f1b = -(S.r * iH * R(0.5));
+    // W+ = I + E R E, W- = E R E - I (below) / I - E R E (above)
+    M2<R> Wp = up ? eye_plus(ED) : eye_plus(EU);
+    M2<R> Wm = up ? minus_eye(ED) : eye_minus(EU);
+
+    // ---------------- receiver propagation (get_ypars_a_*)
+    C<R> y0, y0t;
+    M2<R> y1, y1t;
+    if (rl == s) {
+        const SL<R> &Rv = S;
+        if (A.zr <= A.zs) {
+            C<R> e1v, e2v;
+            M2<R> L1 = phase(Rv, zr, &e1v), L2 = phase(Rv, zs - zr, &e2v);
+            M2<R> L1t = dphase(Rv, zr, R(-1), (const C<R> *)nullptr);
+            M2<R> L2t = dphase(Rv, zs - zr, R(1), (const C<R> *)nullptr);
+            M2<R> Ed = {{k, R(0)}, Rv.d0, Rv.p1, Rv.d1}, Eu = {{k, R(0)}, Rv.d0, -Rv.p1, -Rv.d1};
+            M2<R> RL = ut_mul_right(RU, Lup);
+            Urec = Ed * ut_mul_left(L1, RL) + Eu * L2;
+            Utrec = Ed * ut_mul_left(L1t, RL) + Eu * L2t;
+            u0 = e1v * RU0 * sexu1 + e2v;
+            // green.cu:720 multiplies the up-going term by nu twice
+            u0t = -(Rv.v * e1v * RU0 * sexu1) + ((A.fix & kFixDz) ? Rv.v * e2v : Rv.v * e2v * Rv.v);
+        } else {
+            C<R> e1v, e2v;
+            M2<R> L1 = phase(Rv, zr - zs, &e1v), L2 = phase(Rv, hs - zr, &e2v);
+            M2<R> L1t = dphase(Rv, zr - zs, R(-1), (const C<R> *)nullptr);
+            M2<R> L2t = dphase(Rv, hs - zr, R(1), (const C<R> *)nullptr);
+            M2<R> Ed = {{k, R(0)}, Rv.d0, Rv.p1, Rv.d1}, Eu = {{k, R(0)}, Rv.d0, -Rv.p1, -Rv.d1};
+            M2<R> RL = ut_mul_right(RD, Ldn);
+            Urec = Ed * L1 + Eu * ut_mul_left(L2, RL);
+            Utrec = Ed * L1t + Eu * ut_mul_left(L2t, RL);
+            u0 = e1v + e2v * RD0 * sexd1;
+            u0t = -(Rv.v * e1v) + Rv.v * e2v * RD0 * sexd1;
+        }
+        y0 = u0 * y_sh;
+        y0t = u0t * y_sh;
+        y1 = Urec * ypsv;
+        y1t = Utrec * ypsv;
+    } else if (rl < s) {
+        C<R> yp0 = pc0 * sexu1 * y_sh;
+        M2<R> yp1 = PC * ut_mul_left(Lup, ypsv);
+        y0 = u0 * yp0;
+        // green.cu:842 reuses the updated yu0
+        y0t = (A.fix & kFixDz) ? u0t * yp0 : u0t * y0;
+        y1 = Urec * yp1;
+        y1t = Utrec * yp1;
+    } else {
+        C<R> yp0 = pd0 * sexd1 * y_sh;
+        M2<R> yp1 = PD * ut_mul_left(Ldn, ypsv);
+        y0 = u0 * yp0;
+        y0t = u0t * yp0;
+        y1 = Urec * yp1;
+        y1t = Utrec * yp1;
+    }
+
+    if (!valid) return;
+    const long long idx = A.koff[iw] + j;
+    if (A.src == kSingle) {
+        C<R> f0a = -(S.d0 * iG * R(0.5)), f0b = C<R>{k, R(0)} * iG * R(0.5);
+        C<R> g0a, g0b, g1a, g1b;
+        mv2(Wm, f0a, f0b, &g0a, &g0b);
+        mv2(Wp, f1a, f1b, &g1a, &g1b);
+        C<R> gsh = up ? fu * ssh : (fd + R(1)) * ssh;
+        C<R> a00, a01, a10, a11;
+        mv2(y1, g0a, g0b, &a00, &a01);
+        mv2(y1, g1a, g1b, &a10, &a11);
+        store_q(A, QS_B1, idx, y0 * gsh);
+        store_q(A, QS_A00, idx, a00);
+        store_q(A, QS_A01, idx, a01);
+        store_q(A, QS_A10, idx, a10);
+        store_q(A, QS_A11, idx, a11);
+        mv2(y1t, g0a, g0b, &a00, &a01);
+        mv2(y1t, g1a, g1b, &a10, &a11);
+        store_q(A, QS_B1T, idx, y0t * gsh);
+        store_q(A, QS_A0T0, idx, a00);
+        store_q(A, QS_A0T1, idx, a01);
+        store_q(A, QS_A1T0, idx, a10);
+        store_q(A, QS_A1T1, idx, a11);
+    } else {
+        // s2 = k f1, s1 = -1/(2 mu) G^-1 e0, s0 = H^-1 (alpha', beta')
+        C<R> s2a = f1a * k, s2b = f1b * k;
+        C<R> s1a = -(S.d3 * iG * (R(0.5) / smu)), s1b = -(S.x * iG * R(0.5));
+        C<R> sa = {T[s].a[0], T[s].a[1]}, sb = {T[s].b[0], T[s].b[1]};
+        C<R> ba2 = (sb * sb) * rcp(sa * sa);
+        C<R> al = ba2 * (R(-0.5) / smu);
+        C<R> be = (ba2 * R(2) - R(1)) * (k * R(0.5));
+        C<R> s0a = (S.d2 * al - S.d1 * be) * iH, s0b = (-(S.p2 * al) + S.p1 * be) * iH;
+        C<R> q0a, q0b, q1a, q1b, q2a, q2b;
+        mv2(Wp, s0a, s0b, &q0a, &q0b);
+        mv2(Wm, s1a, s1b, &q1a, &q1b);
+        mv2(Wp, s2a, s2b, &q2a, &q2b);
+        C<R> shf = up ? fu : fd - R(1);
+        C<R> h1 = shf * S.v * ssh, h2 = shf * k * ssh;
+        C<R> v0, v1;
+        store_q(A, QT_B1, idx, y0 * h1);
+        store_q(A, QT_B2, idx, y0 * h2);
+        mv2(y1, q0a, q0b, &v0, &v1);
+        store_q(A, QT_A00, idx, v0);
+        store_q(A, QT_A01, idx, v1);
+        mv2(y1, q1a, q1b, &v0, &v1);
+        store_q(A, QT_A10, idx, v0);
+        store_q(A, QT_A11, idx, v1);
+        mv2(y1, q2a, q2b, &v0, &v1);
+        store_q(A, QT_A20, idx, v0);
+        store_q(A, QT_A21, idx, v1);
+        if (A.nq > QT_N) {
+            store_q(A, QT_N + QT_B1, idx, y0t * h1);
+            store_q(A, QT_N + QT_B2, idx, y0t * h2);
+            mv2(y1t, q0a, q0b, &v0, &v1);
+            store_q(A, QT_N + QT_A00, idx, v0);
+            store_q(A, QT_N + QT_A01, idx, v1);
+            mv2(y1t, q1a, q1b, &v0, &v1);
+            store_q(A, QT_N + QT_A10, idx, v0);
+            store_q(A, QT_N + QT_A11, idx, v1);
+            mv2(y1t, q2a, q2b, &v0, &v1);
+            store_q(A, QT_N + QT_A20, idx, v0);
+            store_q(A, QT_N + QT_A21, idx, v1);
+        }
+    }
+}
+
+}  // namespace grt

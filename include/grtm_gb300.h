@@ -1,0 +1,126 @@
+/*
+ * grtm_gb300.h -- C ABI of the GB300 layered-medium Green's-function library
+ * (generalized reflection-transmission method).
+ *
+ * Drop-in for the reference project cangyeone/grtm_cuda: the library exports
+ * the reference's entry point `green` with its signature and file formats,
+ * plus a status-returning, array-based interface for many receivers.
+ * Plain C types only; every call reports errors through its return value.
+ */
+#ifndef GRTM_GB300_H_
+#define GRTM_GB300_H_
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define GRT_API __attribute__((visibility("default")))
+#else
+#define GRT_API
+#endif
+
+/* status codes */
+#define GRT_OK 0
+#define GRT_ERR_ARG 1          /* bad argument */
+#define GRT_ERR_IO 2           /* file could not be opened or written */
+#define GRT_ERR_PARSE 3        /* malformed input file */
+#define GRT_ERR_MODEL 4        /* layered model the method cannot take */
+#define GRT_ERR_CUDA 5         /* CUDA runtime error (message in grt_last_error) */
+#define GRT_ERR_NOMEM 6        /* device or host allocation failed */
+#define GRT_ERR_TIMEOUT 7      /* a bounded device wait gave up */
+#define GRT_ERR_UNSUPPORTED 8  /* size beyond what this build handles */
+
+/* wavenumber grids */
+#define GRT_K_REFERENCE 0      /* per-frequency k_max rule of the reference, dk = 2 pi / L */
+#define GRT_K_FIXED 1          /* nk_fixed points k_j = j dk at every frequency */
+
+/* working precision of the per-(w,k) kernel and the wavenumber sum */
+#define GRT_FP32 0
+#define GRT_FP64 1
+
+/* corrections of reference quirks; 0 reproduces the reference */
+#define GRT_FIX_RLAYER 1       /* receiver layer located with the receiver depth */
+#define GRT_FIX_REXUT 2        /* d/dz terms use the local vertical wavenumber */
+#define GRT_FIX_DZ 4           /* d/dz terms without the doubled factor / reused product */
+
+/* A layered model: n_layer layers given by the depth of their top (ztop[0] = 0),
+ * the last one being the half-space.  Units: km, km/s, g/cm^3. */
+typedef struct grt_model {
+    int n_layer;
+    const double *ztop, *vp, *vs, *rho, *qp, *qs;
+    double hs;      /* source depth */
+    double hr;      /* receiver depth */
+    int src_type;   /* 0 single force, otherwise moment tensor */
+} grt_model;
+
+typedef struct grt_opts {
+    double dt;            /* sampling interval, s */
+    int log2n;            /* N = 2^log2n samples (2..15) */
+    double t0;            /* reduction time, s */
+    double taper;         /* fraction of the band tapered at the top */
+    double sigma_factor;  /* imaginary frequency sigma = sigma_factor / (N dt); reference: 2 */
+    int k_mode;           /* GRT_K_REFERENCE or GRT_K_FIXED */
+    int nk_fixed;         /* points of the fixed grid */
+    double dk;            /* > 0 overrides the wavenumber step */
+    int precision;        /* GRT_FP32 or GRT_FP64 */
+    int fix;              /* GRT_FIX_* bits */
+} grt_opts;
+
+typedef struct grt_report {
+    int n_layer;          /* after source-interface insertion */
+    int s_layer, r_layer;
+    double zs, zr;
+    int nw;               /* positive frequencies */
+    int n_samples;        /* N */
+    int n_cols;           /* defined output columns: 15 single force, 20 moment tensor */
+    long long n_wk;       /* (w,k) points evaluated */
+    int nk_max;
+    double dk, df, sigma;
+    float ms_grt, ms_bessel, ms_ksum, ms_spectral, ms_total;  /* device time of the last execute */
+    int kernel_launches;  /* kernels launched by the last execute */
+} grt_report;
+
+typedef struct grt_ctx grt_ctx;
+typedef struct grt_plan grt_plan;
+
+/* Contexts own a CUDA stream on one device; not thread-safe. */
+GRT_API int grt_create(grt_ctx **ctx, int device);
+GRT_API void grt_destroy(grt_ctx *ctx);
+GRT_API const char *grt_last_error(const grt_ctx *ctx);
+GRT_API const char *grt_status_string(int status);
+
+/* A plan holds one model, its grids, its receivers and all device buffers.
+ * Creating it uploads the inputs; executing it runs the kernels, leaving the
+ * results in device memory; fetching copies them to the host. */
+GRT_API int grt_plan_create(grt_ctx *ctx, const grt_model *model, const grt_opts *opts, int n_dist,
+                    const double *dist, grt_plan **plan);
+GRT_API int grt_plan_execute(grt_plan *plan, grt_report *report);
+/* traces: [n_dist][n_cols][N] doubles; spectra: [n_dist][n_cols][N] complex as
+ * (re, im) doubles (after taper and Hermitian fill).  Either may be NULL. */
+GRT_API int grt_plan_fetch(grt_plan *plan, double *traces, double *spectra);
+GRT_API int grt_plan_info(const grt_plan *plan, grt_report *report);
+GRT_API void grt_plan_destroy(grt_plan *plan);
+
+/* create + execute + fetch + destroy */
+GRT_API int grt_run(grt_ctx *ctx, const grt_model *model, const grt_opts *opts, int n_dist,
+            const double *dist, double *traces, double *spectra, grt_report *report);
+
+/* The reference's file-to-file call with a status: reads the positional input
+ * file, writes oname_w (N rows x 30 "re,im," pairs) and oname_t (N rows x 30
+ * values), each "%.18e,", exactly as the reference does.  Runs in FP32 unless
+ * the environment variable GRT_PRECISION=fp64. */
+GRT_API int grt_green(const char *iname, const char *oname_w, const char *oname_t);
+
+/* Replaces: extern "C" void green(char *iname, char *oname_w, char *oname_t);
+ * cusrc/popm/popm.h:159-161, defined at cusrc/popm/func/green.cu:1975.
+ * Same signature and files; errors go to stderr (the reference has no
+ * status).  Callers: cusrc/main.cu:8, greent.py:94-98 (ctypes). */
+GRT_API void green(char *iname, char *oname_w, char *oname_t);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
