@@ -210,6 +210,10 @@ static int upload(grt_plan *p)
     CU(cudaMemcpyAsync(p->tw, tw.data(), tw.size() * sizeof(R), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(p->damp, damp.data(), damp.size() * sizeof(double), cudaMemcpyHostToDevice, st));
     CU(cudaMemsetAsync(p->derr, 0, sizeof(unsigned), st));
+    p->rep.h2d_bytes = (long long)(tab.size() * sizeof(tab[0]) + tiles.size() * sizeof(int2) +
+                                   J.nw * (sizeof(int) + sizeof(long long)) + p->nd * sizeof(double) +
+                                   (post.size() + tw.size()) * sizeof(R) + damp.size() * sizeof(double));
+    p->rep.d2h_bytes = (long long)(ntr * J.N * sizeof(R));
     CU(cudaStreamSynchronize(st));
     return GRT_OK;
 }

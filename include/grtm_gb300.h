@@ -81,6 +81,8 @@ typedef struct grt_report {
     double dk, df, sigma;
     float ms_grt, ms_bessel, ms_ksum, ms_spectral, ms_total;  /* device time of the last execute */
     int kernel_launches;  /* kernels launched by the last execute */
+    long long h2d_bytes;  /* bytes the plan uploads (layer tables, grids, receivers) */
+    long long d2h_bytes;  /* bytes one fetch of the traces downloads */
 } grt_report;
 
 typedef struct grt_ctx grt_ctx;

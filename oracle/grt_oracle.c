@@ -1281,6 +1281,65 @@ int grto_run(const grto_job *J, double *spec, double *sig, int nthreads)
     return GRTO_OK;
 }
 
+int grto_run_band(const grto_job *J, int iw0, int iw1, double *sums, int nthreads)
+{
+    const int nd = J->n_dist, ncol = 30;
+    if (nd < 1 || !J->dist || iw0 < 0 || iw1 > J->nw || iw1 <= iw0) return GRTO_ERR_ARG;
+    cplx slot0[2];
+    slot0_nu(J, slot0);
+    cplx *out = (cplx *)calloc((size_t)(iw1 - iw0) * nd * ncol, sizeof(cplx));
+    if (!out) return GRTO_ERR_NOMEM;
+    /* parallel over (frequency, k-block) so that a few frequencies still use all cores */
+    const int kb = 256;
+    int nblk = 0;
+    for (int iw = iw0; iw < iw1; iw++) nblk += (grto_nk(J, iw) + kb - 1) / kb;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel
+#endif
+    {
+        cplx *loc = (cplx *)calloc((size_t)(iw1 - iw0) * nd * ncol, sizeof(cplx));
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 1)
+#endif
+        for (int b = 0; b < nblk; b++) {
+            int iw = iw0, rem = b;
+            for (;; iw++) {
+                int n = (grto_nk(J, iw) + kb - 1) / kb;
+                if (rem < n) break;
+                rem -= n;
+            }
+            int nk = grto_nk(J, iw);
+            cplx a[GRTO_MAXL], bb[GRTO_MAXL], v[30];
+            cplx w = omega(J, iw);
+            attenuate(J, w, a, bb);
+            for (int ik = rem * kb; ik < nk && ik < (rem + 1) * kb; ik++) {
+                double k = J->dk * ik;
+                ypar_t Y;
+                point_any(J, a, bb, k, w, slot0, &Y);
+                double wk = ik == 0 ? J->dk / 2.0 : J->dk;
+                for (int d = 0; d < nd; d++) {
+                    integrand(J->src_type, &Y, k, J->dist[d], v);
+                    cplx *o = loc + ((size_t)(iw - iw0) * nd + d) * ncol;
+                    for (int c = 0; c < ncol; c++) o[c] += v[c] * wk;
+                }
+            }
+        }
+#ifdef _OPENMP
+#pragma omp critical
+#endif
+        for (size_t i = 0; i < (size_t)(iw1 - iw0) * nd * ncol; i++) out[i] += loc[i];
+        free(loc);
+    }
+    if (sums)
+        for (size_t i = 0; i < (size_t)(iw1 - iw0) * nd * ncol; i++) {
+            sums[2 * i] = creal(out[i]);
+            sums[2 * i + 1] = cimag(out[i]);
+        }
+    free(out);
+    return GRTO_OK;
+}
+
 int grto_green(const char *iname, const char *oname_w, const char *oname_t, int nthreads)
 {
     grto_job J;

@@ -95,6 +95,10 @@ long long grto_nkw(const grto_job *job);
  *         de-damping, or NULL.  N = 2*nw. */
 int grto_run(const grto_job *job, double *spec, double *sig, int nthreads);
 
+/* k-sums (before taper) of frequencies iw0 <= iw < iw1 for all receivers:
+ * sums [iw1-iw0][n_dist][30] complex.  Used to time a bounded sample. */
+int grto_run_band(const grto_job *job, int iw0, int iw1, double *sums, int nthreads);
+
 /* Per-(w,k) receiver coefficients, for kernel-level comparisons.
  *   out: 16 complex (re,im) = a0[2], a1[2], a2[2], b1, b2, a0t[2], a1t[2],
  *   a2t[2], b1t, b2t (a2/b2 are zero for a single force). */

@@ -92,6 +92,7 @@ def lib():
         L.grto_nkw.argtypes = [P(Job)]
         L.grto_nkw.restype = ctypes.c_longlong
         L.grto_run.argtypes = [P(Job), dp, dp, ctypes.c_int]
+        L.grto_run_band.argtypes = [P(Job), ctypes.c_int, ctypes.c_int, dp, ctypes.c_int]
         L.grto_point.argtypes = [P(Job), ctypes.c_int, ctypes.c_double, dp]
         L.grto_integrand.argtypes = [P(Job), ctypes.c_int, ctypes.c_double, ctypes.c_double, dp]
         L.grto_green.argtypes = [ctypes.c_char_p] * 3 + [ctypes.c_int]
@@ -152,6 +153,18 @@ def run(job, dists, nthreads=0, want_spec=True, want_sig=True):
     if want_spec:
         spec = spec[..., 0] + 1j * spec[..., 1]
     return spec, sig
+
+
+def run_band(job, dists, iw0, iw1, nthreads=0):
+    """k-sums of frequencies [iw0, iw1) for all receivers: [iw1-iw0, nd, 30] complex."""
+    d = np.ascontiguousarray(np.atleast_1d(dists), dtype=np.float64)
+    job.n_dist = len(d)
+    job.dist = _dp(d)
+    out = np.zeros((iw1 - iw0, len(d), 30, 2))
+    rc = lib().grto_run_band(ctypes.byref(job), iw0, iw1, _dp(out), int(nthreads))
+    job.dist = ctypes.POINTER(ctypes.c_double)()
+    _check(rc, "run_band")
+    return out[..., 0] + 1j * out[..., 1]
 
 
 def point(job, iw, k):
