@@ -54,7 +54,7 @@ class Report(ctypes.Structure):
 # every symbol the public header declares
 EXPORTS = ("grt_create", "grt_destroy", "grt_last_error", "grt_status_string", "grt_plan_create",
            "grt_plan_execute", "grt_plan_fetch", "grt_plan_info", "grt_plan_destroy", "grt_run",
-           "grt_green", "green")
+           "grt_green", "green", "grt_run_noalloc")
 
 _lib = None
 
@@ -91,6 +91,7 @@ def lib():
     L.grt_green.argtypes = [ctypes.c_char_p] * 3
     L.green.argtypes = [ctypes.c_char_p] * 3
     L.green.restype = None
+    L.grt_run_noalloc.argtypes = [ctypes.c_int, P(Model), P(Opts), ctypes.c_int, _dp, _dp]
     _lib = L
     return L
 
@@ -206,6 +207,19 @@ def run(model, opts, dists, ctx=None, spectra=False):
     finally:
         if own:
             ctx.close()
+
+
+def run_noalloc(model, opts, dists, device=0, n_cols=None):
+    """grt_run_noalloc: the same traces as run() for small FP32 jobs, with no
+    device allocation (library-owned scratch; see the C header)."""
+    d = _arr(np.atleast_1d(dists))
+    if n_cols is None:
+        n_cols = 15 if model.src_type == 0 else 20
+    out = np.empty((len(d), n_cols, 1 << opts.log2n))
+    rc = lib().grt_run_noalloc(int(device), ctypes.byref(model), ctypes.byref(opts), len(d), _ptr(d), _ptr(out))
+    if rc:
+        raise GrtError(rc, "grt_run_noalloc (details on stderr)")
+    return out
 
 
 def green(iname, oname_w, oname_t):

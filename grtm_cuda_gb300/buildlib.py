@@ -18,7 +18,7 @@ NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-fvisibility=hidden"]
-SOURCES = ["grt_api.cu", "grt_job.cpp"]
+SOURCES = ["grt_api.cu", "grt_job.cpp", "grt_noalloc.cu"]
 
 
 def _obj(src):

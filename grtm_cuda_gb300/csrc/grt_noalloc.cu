@@ -1,0 +1,260 @@
+// grt_noalloc.cu -- Green's functions for callers that cannot allocate device
+// memory.
+//
+// Some callers cannot call cudaMalloc: a host process whose GPU memory is
+// reserved up front by another runtime (a framework's caching allocator, a
+// service with a fixed device-memory budget), or code running where device
+// allocation is not permitted.  grt_run_noalloc computes the same traces as
+// grt_run for small jobs without allocating anything on the device: every
+// intermediate buffer (per-frequency layer tables, the (w,k) coefficient
+// columns, the Bessel table, the spectra and the traces before download)
+// lives in one file-scope device array of kScratchBytes.  The host-side job
+// tables are staged in a file-scope host array of kStageBytes.
+//
+// Set-up: the first call on a device (made current by that call) looks up the
+// array's device address with cudaGetSymbolAddress and keeps it; make that
+// first call before any stream capture.  Every GPU that loads the library
+// holds the array until the process exits.  All calls share the array (and
+// the host staging array): calls that overlap on the GPU, or run from several
+// host threads at once, race.  The only scratch word that must start at zero
+// (the device error flag) is cleared by every call; all other scratch is
+// fully written before it is read.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "../../include/grtm_gb300.h"
+#include "grt_integrate.cuh"
+#include "grt_job.h"
+#include "grt_kernel.cuh"
+
+namespace {
+
+constexpr size_t kScratchBytes = 32ull << 20;  // device scratch per GPU: 32 MiB
+constexpr size_t kStageBytes = 4ull << 20;     // host staging of the job tables: 4 MiB
+constexpr int kMaxDevices = 64;
+constexpr double PI = 3.1415926535897932384626433;
+
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_grt_scratch[kScratchBytes];
+alignas(256) static unsigned char g_grt_stage[kStageBytes];
+static void *g_scratch_addr[kMaxDevices];
+
+static size_t up256(size_t n) { return (n + 255) & ~size_t(255); }
+
+static int fail(int code, const std::string &msg)
+{
+    fprintf(stderr, "grt_run_noalloc: %s (%s)\n", grt_status_string(code), msg.c_str());
+    return code;
+}
+
+#define CUN(call)                                                                        \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess) return fail(GRT_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+extern "C" GRT_API int grt_run_noalloc(int device, const grt_model *m, const grt_opts *o, int n_dist,
+                                       const double *dist, double *traces)
+{
+    using grt::Job;
+    using cd = std::complex<double>;
+    if (!m || !o || !dist || !traces || n_dist < 1) return fail(GRT_ERR_ARG, "null argument or no receivers");
+    if (device < 0 || device >= kMaxDevices) return fail(GRT_ERR_ARG, "device ordinal out of range");
+    if (o->precision != GRT_FP32) return fail(GRT_ERR_ARG, "the allocation-free entry point runs in FP32 only");
+    for (int i = 0; i < n_dist; i++)
+        if (!(dist[i] > 0)) return fail(GRT_ERR_ARG, "distances must be > 0");
+
+    // set-up, once per device, with that device current
+    CUN(cudaSetDevice(device));
+    if (!g_scratch_addr[device]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_grt_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(GRT_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        g_scratch_addr[device] = p;
+    }
+    unsigned char *scratch = (unsigned char *)g_scratch_addr[device];
+
+    // the job on the host (same rules as grt_run)
+    Job J;
+    std::string err;
+    int rc = grt::job_from_layers(m->n_layer, m->ztop, m->vp, m->vs, m->rho, m->qp, m->qs, m->hs, m->hr,
+                                  m->src_type, J, err);
+    if (!rc) rc = grt::job_setup(J, o->dt, o->log2n, o->t0, o->taper, o->sigma_factor, o->k_mode, o->nk_fixed,
+                                 o->dk, o->fix, err);
+    if (rc) return fail(rc, err);
+    const int L = J.L, nw = J.nw, N = J.N, nd = n_dist;
+    const int nc = J.src == 0 ? grt::kSingleNC : grt::kTensorNC;
+    const int nq = J.src == 0 ? (int)grt::QS_N : (int)grt::QT_N;
+    long long ntiles = 0;
+    for (int iw = 0; iw < nw; iw++) ntiles += (J.nk[iw] + grt::kGrtThreads - 1) / grt::kGrtThreads;
+    if ((size_t)N * sizeof(grt::C<float>) > 128 * 1024) return fail(GRT_ERR_UNSUPPORTED, "N above 16384");
+
+    // layout: staged tables first (same offsets on host and device), then work buffers
+    using LW = grt::LayerW<float>;
+    size_t off = 0;
+    const size_t o_tab = off; off = up256(off + (size_t)nw * L * sizeof(LW));
+    const size_t o_tiles = off; off = up256(off + (size_t)ntiles * sizeof(int2));
+    const size_t o_nk = off; off = up256(off + (size_t)nw * sizeof(int));
+    const size_t o_koff = off; off = up256(off + (size_t)nw * sizeof(long long));
+    const size_t o_dist = off; off = up256(off + (size_t)nd * sizeof(double));
+    const size_t o_post = off; off = up256(off + (size_t)nw * 2 * sizeof(float));
+    const size_t o_tw = off; off = up256(off + (size_t)N * sizeof(float));
+    const size_t o_damp = off; off = up256(off + (size_t)N * sizeof(double));
+    const size_t staged = off;
+    const size_t o_K = off; off = up256(off + (size_t)nq * J.nkw * 2 * sizeof(float));
+    const size_t o_B = off; off = up256(off + (size_t)J.nkmax * grt::NBASIS * nd * sizeof(float));
+    const size_t o_S = off; off = up256(off + (size_t)nd * nc * nw * 2 * sizeof(float));
+    const size_t o_sig = off; off = up256(off + (size_t)nd * nc * N * sizeof(float));
+    const size_t o_err = off; off = up256(off + sizeof(unsigned));
+    if (off > kScratchBytes || staged > kStageBytes) {
+        char msg[256];
+        snprintf(msg, sizeof msg,
+                 "job needs %.1f MiB of device scratch and %.1f MiB of host staging; this entry point holds "
+                 "%zu MiB and %zu MiB (use grt_run for larger jobs)",
+                 off / 1048576.0, staged / 1048576.0, kScratchBytes >> 20, kStageBytes >> 20);
+        return fail(GRT_ERR_UNSUPPORTED, msg);
+    }
+
+    // per-frequency tables into the host staging array (attenuation green.cu:177-180,
+    // phase/taper/scale 1905-1921, de-damping 2236-2237)
+    unsigned char *h = g_grt_stage;
+    LW *tab = (LW *)(h + o_tab);
+    for (int iw = 0; iw < nw; iw++) {
+        cd w(2 * PI * J.df * iw, -J.sigma);
+        cd lw = std::log(w / (2 * PI));
+        for (int i = 0; i < L; i++) {
+            cd cs = 1.0 + lw / (PI * J.qs[i]) + cd(0, 1) / (2.0 * J.qs[i]);
+            cd cp = 1.0 + lw / (PI * J.qp[i]) + cd(0, 1) / (2.0 * J.qp[i]);
+            cd a = J.a0[i] * cp, b = J.b0[i] * cs;
+            cd wa = w / a, wb = w / b;
+            cd wa2 = wa * wa, wb2 = wb * wb, W = wb2 - wa2, iW = 1.0 / W;
+            LW &t = tab[(size_t)iw * L + i];
+            memset(&t, 0, sizeof t);
+            t.wa2x = wa2.real(); t.wa2y = wa2.imag(); t.wb2x = wb2.real(); t.wb2y = wb2.imag();
+            t.wa2[0] = (float)wa2.real(); t.wa2[1] = (float)wa2.imag();
+            t.wb2[0] = (float)wb2.real(); t.wb2[1] = (float)wb2.imag();
+            t.W[0] = (float)W.real(); t.W[1] = (float)W.imag();
+            t.iW[0] = (float)iW.real(); t.iW[1] = (float)iW.imag();
+            t.a[0] = (float)a.real(); t.a[1] = (float)a.imag();
+            t.b[0] = (float)b.real(); t.b[1] = (float)b.imag();
+            t.mu = (float)J.mu[i];
+            t.h = (float)J.h[i];
+        }
+    }
+    int2 *tiles = (int2 *)(h + o_tiles);
+    long long t = 0;
+    for (int iw = 0; iw < nw; iw++)
+        for (int j0 = 0; j0 < J.nk[iw]; j0 += grt::kGrtThreads) tiles[t++] = make_int2(iw, j0);
+    memcpy(h + o_nk, J.nk.data(), (size_t)nw * sizeof(int));
+    memcpy(h + o_koff, J.koff.data(), (size_t)nw * sizeof(long long));
+    memcpy(h + o_dist, dist, (size_t)nd * sizeof(double));
+    float *post = (float *)(h + o_post);
+    const int wc = (int)((double)nw * (1 - J.taper));
+    const double coef = J.df * nw / PI;
+    for (int iw = 0; iw < nw; iw++) {
+        double st0 = iw > wc ? 0.5 * (1. + std::cos((iw - wc + 1) * PI / (nw - wc + 1))) : 1.0;
+        double phi = 2 * PI * J.df * iw * J.t0;
+        post[2 * iw] = (float)(std::cos(phi) * st0 * coef);
+        post[2 * iw + 1] = (float)(std::sin(phi) * st0 * coef);
+    }
+    float *tw = (float *)(h + o_tw);
+    for (int k = 0; k < N / 2; k++) {
+        tw[2 * k] = (float)std::cos(2 * PI * k / N);
+        tw[2 * k + 1] = (float)std::sin(2 * PI * k / N);
+    }
+    double *damp = (double *)(h + o_damp);
+    for (int n = 0; n < N; n++) damp[n] = std::exp(n * J.dt * J.sigma) * std::exp(J.t0 * J.sigma) / (double)N;
+    float slot0[4];
+    {
+        const LW &t0r = tab[J.rl];
+        cd r0 = std::sqrt(cd(-t0r.wa2x, -t0r.wa2y)), v0 = std::sqrt(cd(-t0r.wb2x, -t0r.wb2y));
+        if (r0.real() < 0) r0 = -r0;
+        if (v0.real() < 0) v0 = -v0;
+        slot0[0] = (float)r0.real(); slot0[1] = (float)r0.imag(); slot0[2] = (float)v0.real(); slot0[3] = (float)v0.imag();
+    }
+
+    // upload, clear the error word, run the four kernels on the default stream
+    const cudaStream_t st = 0;
+    CUN(cudaMemcpy(scratch, g_grt_stage, staged, cudaMemcpyHostToDevice));
+    CUN(cudaMemsetAsync(scratch + o_err, 0, sizeof(unsigned), st));
+    grt::GrtArgs<float> A{};
+    A.tab = (const LW *)(scratch + o_tab);
+    A.tiles = (const int2 *)(scratch + o_tiles);
+    A.nk = (const int *)(scratch + o_nk);
+    A.koff = (const long long *)(scratch + o_koff);
+    A.K = (float *)(scratch + o_K);
+    A.nkw = J.nkw;
+    A.dk = J.dk;
+    A.zs = J.zs;
+    A.zr = J.zr;
+    A.hs_layer = J.h[J.s];
+    A.hr_layer = J.h[J.rl];
+    A.L = L; A.s = J.s; A.rl = J.rl; A.src = J.src; A.fix = J.fix; A.nq = nq;
+    for (int i = 0; i < 4; i++) A.slot0[i] = slot0[i];
+    A.err = (unsigned *)(scratch + o_err);
+    grt::grt_point_kernel<float><<<(unsigned)ntiles, grt::kGrtThreads, (size_t)L * sizeof(LW), st>>>(A);
+    CUN(cudaGetLastError());
+    {
+        long long n = (long long)J.nkmax * nd;
+        grt::bessel_table_kernel<float><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+            (float *)(scratch + o_B), J.nkmax, nd, J.dk, (const double *)(scratch + o_dist));
+        CUN(cudaGetLastError());
+    }
+    {
+        grt::KsumArgs<float> S{};
+        S.K = (const float *)(scratch + o_K);
+        S.B = (const float *)(scratch + o_B);
+        S.nk = A.nk;
+        S.koff = A.koff;
+        S.dist = (const double *)(scratch + o_dist);
+        S.S = (float *)(scratch + o_S);
+        S.nkw = J.nkw; S.dk = J.dk; S.nw = nw; S.nr = nd;
+        S.rt = 128;
+        while (S.rt > 1 && S.rt / 2 >= nd) S.rt /= 2;
+        S.jt = 128 / S.rt;
+        unsigned grid = (unsigned)(nw * ((nd + S.rt - 1) / S.rt));
+        if (J.src == 0) grt::ksum_kernel<float, grt::kSingle><<<grid, grt::kSumThreads, 0, st>>>(S);
+        else grt::ksum_kernel<float, grt::kTensor><<<grid, grt::kSumThreads, 0, st>>>(S);
+        CUN(cudaGetLastError());
+    }
+    {
+        grt::SpecArgs<float> S{};
+        S.S = (const float *)(scratch + o_S);
+        S.post = (const float *)(scratch + o_post);
+        S.tw = (const float *)(scratch + o_tw);
+        S.damp = (const double *)(scratch + o_damp);
+        S.spec_out = nullptr;
+        S.sig_out = (float *)(scratch + o_sig);
+        S.nw = nw;
+        S.logn = J.log2n;
+        const size_t smem = (size_t)N * sizeof(grt::C<float>);
+        CUN(cudaFuncSetAttribute(grt::spectral_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        grt::spectral_kernel<float><<<(unsigned)(nd * nc), std::min(512, std::max(32, N / 2)), smem, st>>>(S);
+        CUN(cudaGetLastError());
+    }
+    CUN(cudaStreamSynchronize(st));
+    unsigned herr = 0;
+    CUN(cudaMemcpy(&herr, scratch + o_err, sizeof herr, cudaMemcpyDeviceToHost));
+    if (herr) return fail(GRT_ERR_TIMEOUT, "a bounded device wait gave up (layer-table copy)");
+
+    // download the FP32 traces into the front half of the caller's buffer and
+    // widen them in place, from the end, to doubles
+    const size_t nval = (size_t)nd * nc * N;
+    CUN(cudaMemcpy(traces, scratch + o_sig, nval * sizeof(float), cudaMemcpyDeviceToHost));
+    unsigned char *bytes = (unsigned char *)traces;
+    for (size_t i = nval; i-- > 0;) {
+        float v;
+        memcpy(&v, bytes + i * sizeof(float), sizeof v);
+        double d = v;
+        memcpy(bytes + i * sizeof(double), &d, sizeof d);
+    }
+    return GRT_OK;
+}

@@ -110,6 +110,22 @@ GRT_API void grt_plan_destroy(grt_plan *plan);
 GRT_API int grt_run(grt_ctx *ctx, const grt_model *model, const grt_opts *opts, int n_dist,
             const double *dist, double *traces, double *spectra, grt_report *report);
 
+/* For callers that cannot allocate device memory -- a process whose GPU memory
+ * is reserved by another runtime (a framework's caching allocator, a service
+ * with a fixed device budget) or code running where cudaMalloc is not
+ * permitted.  Same traces as grt_run (FP32 only) for small jobs, allocating
+ * nothing on the device: all intermediates live in one library-owned device
+ * array of 32 MiB per GPU (held from library load until exit) and the job
+ * tables in a 4 MiB host array.  Jobs that need more return
+ * GRT_ERR_UNSUPPORTED with the sizes on stderr.  The first call on a device
+ * does a one-time set-up (cudaGetSymbolAddress); make it before any stream
+ * capture.  Calls share the arrays: calls that overlap on the GPU, or come
+ * from several host threads at once, race.  Runs on the default stream of
+ * `device`; traces: host [n_dist][n_cols][N] doubles.
+ * No counterpart in the reference. */
+GRT_API int grt_run_noalloc(int device, const grt_model *model, const grt_opts *opts, int n_dist,
+                            const double *dist, double *traces);
+
 /* The reference's file-to-file call with a status: reads the positional input
  * file, writes oname_w (N rows x 30 "re,im," pairs) and oname_t (N rows x 30
  * values), each "%.18e,", exactly as the reference does.  Runs in FP32 unless
