@@ -13,7 +13,7 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_lib", "libgrtm_gb300.so")
+LIB_PATH = os.environ.get("GRTM_GB300_LIB", os.path.join(HERE, "_lib", "libgrtm_gb300.so"))
 
 OK, ERR_ARG, ERR_IO, ERR_PARSE, ERR_MODEL, ERR_CUDA, ERR_NOMEM, ERR_TIMEOUT, ERR_UNSUPPORTED = range(9)
 K_REFERENCE, K_FIXED = 0, 1

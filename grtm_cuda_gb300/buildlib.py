@@ -19,6 +19,12 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-fvisibility=hidden"]
 SOURCES = ["grt_api.cu", "grt_job.cpp", "grt_noalloc.cu"]
+# extra nvcc flags (e.g. -DGRT_POINT_MINB=4) and an alternative output path,
+# for timing build variants side by side
+EXTRA = os.environ.get("GRT_NVCC_EXTRA", "").split()
+if os.environ.get("GRT_BUILD_TAG"):
+    BUILD = BUILD + "_" + os.environ["GRT_BUILD_TAG"]
+    LIB = os.path.join(LIBDIR, "libgrtm_gb300_" + os.environ["GRT_BUILD_TAG"] + ".so")
 
 
 def _obj(src):
@@ -36,7 +42,7 @@ def _stale(src):
 
 
 def _compile(src, verbose=False):
-    cmd = [NVCC] + ARCH + FLAGS + (["-Xptxas", "-v"] if verbose else []) + [
+    cmd = [NVCC] + ARCH + FLAGS + EXTRA + (["-Xptxas", "-v"] if verbose else []) + [
         "-c", os.path.join(CSRC, src), "-o", _obj(src)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -140,6 +140,8 @@ static void build_tables(const Job &J, std::vector<grt::LayerW<R>> &tab, std::ve
             t.b[0] = (R)b.real(); t.b[1] = (R)b.imag();
             t.mu = (R)J.mu[i];
             t.h = (R)J.h[i];
+            t.wa2lo = (float)(wa2.real() - (double)(float)wa2.real());
+            t.wb2lo = (float)(wb2.real() - (double)(float)wb2.real());
         }
     }
     // phase e^{i w_r t0}, cosine taper and scale df nw / pi (green.cu:1905-1921)

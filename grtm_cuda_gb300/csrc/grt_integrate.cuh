@@ -252,6 +252,7 @@ __global__ void __launch_bounds__(kSumThreads) ksum_kernel(KsumArgs<R> A)
     R hi[NP][2], lo[NP][2];
 #pragma unroll
     for (int p = 0; p < NP; p++) hi[p][0] = hi[p][1] = lo[p][0] = lo[p][1] = R(0);
+    const R dk = (R)A.dk, dk_half = (R)(0.5 * A.dk);
 
     for (int jb = lane * kSumChunk; jb < nk; jb += A.jt * kSumChunk) {
         R acc[NP][2];
@@ -259,9 +260,9 @@ __global__ void __launch_bounds__(kSumThreads) ksum_kernel(KsumArgs<R> A)
         for (int p = 0; p < NP; p++) acc[p][0] = acc[p][1] = R(0);
         const int je = min(jb + kSumChunk, nk);
         for (int j = jb; j < je; j++) {
-            const double kd = A.dk * j;
-            const R k = (R)kd;
-            const R w = (j == 0) ? (R)(0.5 * A.dk) : (R)A.dk;
+            // k^p weights only scale the coefficients: working precision suffices
+            const R k = dk * (R)j;
+            const R w = (j == 0) ? dk_half : dk;
             const R wk[3] = {w, w * k, w * k * k};
             const R *Bj = A.B + (long long)j * NBASIS * A.nr + rr;
             R bv[NBASIS];

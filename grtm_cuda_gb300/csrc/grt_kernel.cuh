@@ -38,15 +38,36 @@ struct SL {
     R mu;
 };
 
-template <typename R>
-__device__ __forceinline__ void make_layer(const LayerW<R> &T, double k2, R k, SL<R> &L)
+// k^2 carried as an unevaluated sum of two words: FP64 for the FP64 kernel,
+// double-float (hi + lo, about 48 bits) for the FP32 kernel
+template <typename R> struct K2 { double v; };
+template <> struct K2<float> { float hi, lo; };
+__device__ __forceinline__ void make_k2(double k2, K2<double> &o) { o.v = k2; }
+__device__ __forceinline__ void make_k2(double k2, K2<float> &o)
 {
-    // branch selection in FP64: Re(k^2 - wa^2) cancels near the branch point
-    C<R> zr = {(R)(k2 - T.wa2x), (R)(-T.wa2y)};
-    C<R> zv = {(R)(k2 - T.wb2x), (R)(-T.wb2y)};
+    o.hi = (float)k2;
+    o.lo = (float)(k2 - (double)o.hi);
+}
+// Re(c k^2 - w2): the subtraction that selects the vertical-slowness branch.
+// Near the branch point it cancels; the high words cancel exactly (Sterbenz)
+// and the low words supply the digits FP32 alone would lose.
+__device__ __forceinline__ double re_minus(const K2<double> &k2, double c, double w2, float, float)
+{
+    return c * k2.v - w2;
+}
+__device__ __forceinline__ float re_minus(const K2<float> &k2, float c, double, float w2hi, float w2lo)
+{
+    return (c * k2.hi - w2hi) + (c * k2.lo - w2lo);
+}
+
+template <typename R>
+__device__ __forceinline__ void make_layer(const LayerW<R> &T, const K2<R> &k2, R k, SL<R> &L)
+{
+    C<R> zr = {re_minus(k2, R(1), T.wa2x, (float)T.wa2[0], T.wa2lo), -T.wa2[1]};
+    C<R> zv = {re_minus(k2, R(1), T.wb2x, (float)T.wb2[0], T.wb2lo), -T.wb2[1]};
     L.r = csqrt_(zr);
     L.v = csqrt_(zv);
-    L.x = C<R>{(R)(2.0 * k2 - T.wb2x), (R)(-T.wb2y)};  // k^2 + v^2 = 2k^2 - wb^2
+    L.x = C<R>{re_minus(k2, R(2), T.wb2x, (float)T.wb2[0], T.wb2lo), -T.wb2[1]};  // k^2 + v^2 = 2k^2 - wb^2
     const C<R> wa2 = {T.wa2[0], T.wa2[1]}, wb2 = {T.wb2[0], T.wb2[1]};
     const C<R> W = {T.W[0], T.W[1]}, iW = {T.iW[0], T.iW[1]};
     C<R> rpv = L.r + L.v;
@@ -155,7 +176,10 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigne
 }
 
 template <typename R>
-__global__ void __launch_bounds__(kGrtThreads) grt_point_kernel(GrtArgs<R> A)
+#ifndef GRT_POINT_MINB
+#define GRT_POINT_MINB 1   // resident blocks per SM the register allocation must allow
+#endif
+__global__ void __launch_bounds__(kGrtThreads, GRT_POINT_MINB) grt_point_kernel(GrtArgs<R> A)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) unsigned long long bar;
@@ -188,7 +212,8 @@ __global__ void __launch_bounds__(kGrtThreads) grt_point_kernel(GrtArgs<R> A)
     const bool valid = j < A.nk[iw];
     const int jj = valid ? j : 0;           // idle lanes compute k = 0 and store nothing
     const double kd = A.dk * jj;
-    const double k2 = kd * kd;
+    K2<R> k2;
+    make_k2(kd * kd, k2);
     const R k = (R)kd;
     const C<R> zero = {R(0), R(0)};
 

@@ -147,6 +147,8 @@ extern "C" GRT_API int grt_run_noalloc(int device, const grt_model *m, const grt
             t.b[0] = (float)b.real(); t.b[1] = (float)b.imag();
             t.mu = (float)J.mu[i];
             t.h = (float)J.h[i];
+            t.wa2lo = (float)(wa2.real() - (double)(float)wa2.real());
+            t.wb2lo = (float)(wb2.real() - (double)(float)wb2.real());
         }
     }
     int2 *tiles = (int2 *)(h + o_tiles);

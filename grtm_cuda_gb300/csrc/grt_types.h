@@ -19,6 +19,7 @@ struct alignas(16) LayerW {
     R iW[2];                        // 1 / W
     R a[2], b[2];                   // attenuated velocities alpha(w), beta(w)
     R mu, h;                        // b0^2 rho, thickness (half-space: top depth)
+    float wa2lo, wb2lo;             // Re(wa^2) - (float)Re(wa^2), same for wb^2 (double-float low words)
 };
 static_assert(sizeof(LayerW<float>) % 16 == 0, "TMA bulk copies need 16-byte multiples");
 static_assert(sizeof(LayerW<double>) % 16 == 0, "TMA bulk copies need 16-byte multiples");
