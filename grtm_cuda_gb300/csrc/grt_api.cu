@@ -9,12 +9,14 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/grtm_gb300.h"
 #include "grt_integrate.cuh"
 #include "grt_job.h"
 #include "grt_kernel.cuh"
+#include "grt_ksum_tc.cuh"
 
 using grt::Job;
 using cd = std::complex<double>;
@@ -33,6 +35,8 @@ struct grt_plan {
     int prec = 0;
     int nd = 0, nc = 0, nq = 0, ntiles = 0;
     int rt = 128, jt = 1;
+    int use_tc = 0, nsplit = 1, kslice = 0;   // tensor-core wavenumber sum and its split-K
+    void *P = nullptr;                        // split-K partial sums
     std::vector<double> dist;
     double slot0[4] = {0, 0, 0, 0};
     // device buffers
@@ -107,7 +111,7 @@ extern "C" void grt_plan_destroy(grt_plan *p)
     if (!p) return;
     cudaSetDevice(p->ctx->device);
     void *bufs[] = {p->tab, p->K, p->B, p->S, p->post, p->tw, p->spec, p->sig, p->tiles, p->nk, p->koff, p->ddist,
-                    p->damp, p->derr};
+                    p->damp, p->derr, p->P};
     for (void *b : bufs)
         if (b) cudaFree(b);
     delete p;
@@ -202,6 +206,25 @@ static int upload(grt_plan *p)
     CU(cudaMalloc(&p->sig, ntr * J.N * sizeof(R)));
     CU(cudaMalloc(&p->spec, ntr * J.N * 2 * sizeof(R)));
     CU(cudaMalloc(&p->derr, sizeof(unsigned)));
+    if (p->use_tc) {
+        // split the k range so that the CTA count fills whole waves of the SMs (one CTA per SM)
+        int nsm = 148;
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device);
+        const long long tiles = (long long)((J.nw + grt::tc::kW - 1) / grt::tc::kW) * ((p->nd + grt::tc::kN - 1) / grt::tc::kN);
+        int best = 1;
+        double best_cost = 1e30;
+        const int maxs = std::max(1, std::min(64, J.nkmax / (8 * grt::tc::kKT)));
+        for (int s = 1; s <= maxs; s++) {
+            const long long n = tiles * s;
+            const long long waves = (n + nsm - 1) / nsm;
+            // time ~ waves x (k per CTA); small penalty per extra split for the reduction
+            const double cost = (double)waves * ((double)J.nkmax / s + 64.0) + 2.0 * s;
+            if (cost < best_cost) { best_cost = cost; best = s; }
+        }
+        p->nsplit = best;
+        p->kslice = ((J.nkmax + best - 1) / best + grt::tc::kKT - 1) / grt::tc::kKT * grt::tc::kKT;
+        CU(cudaMalloc(&p->P, (size_t)best * ntr * J.nw * 2 * sizeof(float)));
+    }
     cudaStream_t st = ctx->stream;
     CU(cudaMemcpyAsync(p->tab, tab.data(), tab.size() * sizeof(tab[0]), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(p->tiles, tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
@@ -251,6 +274,10 @@ extern "C" int grt_plan_create(grt_ctx *ctx, const grt_model *m, const grt_opts 
     p->rt = 128;
     while (p->rt > 1 && p->rt / 2 >= n_dist) p->rt /= 2;
     p->jt = 128 / p->rt;
+    // FP32 plans sum over wavenumbers on the tensor cores unless GRT_KSUM=simt
+    const char *ks = getenv("GRT_KSUM");
+    p->use_tc = (p->prec == GRT_FP32) && !(ks && !strcmp(ks, "simt"));
+    p->rep.ksum_impl = p->use_tc;
     CU(cudaSetDevice(ctx->device));
     rc = p->prec ? upload<double>(p.get()) : upload<float>(p.get());
     if (rc) {
@@ -258,6 +285,47 @@ extern "C" int grt_plan_create(grt_ctx *ctx, const grt_model *m, const grt_opts 
         return rc;
     }
     *out = p.release();
+    return GRT_OK;
+}
+
+// tensor-core wavenumber sum (FP32 path): split-K partial sums, then TwoSum reduction
+static int launch_ksum_tc(grt_plan *p, cudaStream_t st, int &launches)
+{
+    grt_ctx *ctx = p->ctx;
+    const Job &J = p->J;
+    grt::KsumTcArgs<float> T{};
+    T.K = (const float *)p->K;
+    T.B = (const float *)p->B;
+    T.nk = p->nk;
+    T.koff = p->koff;
+    T.dist = p->ddist;
+    T.P = (float *)p->P;
+    T.nkw = J.nkw;
+    T.dk = J.dk;
+    T.nw = J.nw;
+    T.nr = p->nd;
+    T.nkmax = J.nkmax;
+    T.nsplit = p->nsplit;
+    T.kslice = p->kslice;
+    T.err = p->derr;
+    const int nwt = (J.nw + grt::tc::kW - 1) / grt::tc::kW, nrt = (p->nd + grt::tc::kN - 1) / grt::tc::kN;
+    const unsigned grid = (unsigned)(nwt * nrt * p->nsplit);
+    if (J.src == 0) {
+        const int sm = grt::tc::smem_bytes<grt::kSingle>();
+        CU(cudaFuncSetAttribute(grt::ksum_tc_kernel<grt::kSingle>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+        grt::ksum_tc_kernel<grt::kSingle><<<grid, grt::tc::kThreads, sm, st>>>(T);
+    } else {
+        const int sm = grt::tc::smem_bytes<grt::kTensor>();
+        CU(cudaFuncSetAttribute(grt::ksum_tc_kernel<grt::kTensor>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+        grt::ksum_tc_kernel<grt::kTensor><<<grid, grt::tc::kThreads, sm, st>>>(T);
+    }
+    launches++;
+    CU(cudaGetLastError());
+    const long long n = (long long)p->nd * p->nc * J.nw * 2;
+    grt::ksum_tc_reduce_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>((const float *)p->P, (float *)p->S, n,
+                                                                             p->nsplit);
+    launches++;
+    CU(cudaGetLastError());
     return GRT_OK;
 }
 
@@ -300,7 +368,13 @@ static int execute(grt_plan *p)
     }
     CU(cudaEventRecord(ctx->ev[2], st));
     // 3. wavenumber sum
-    {
+    if constexpr (std::is_same<R, float>::value) {
+        if (p->use_tc) {
+            int rc = launch_ksum_tc(p, st, launches);
+            if (rc) return rc;
+        }
+    }
+    if (!p->use_tc) {
         grt::KsumArgs<R> S{};
         S.K = (const R *)p->K; S.B = (const R *)p->B; S.nk = p->nk; S.koff = p->koff; S.dist = p->ddist;
         S.S = (R *)p->S; S.nkw = J.nkw; S.dk = J.dk; S.nw = J.nw; S.nr = p->nd; S.rt = p->rt; S.jt = p->jt;
@@ -327,7 +401,11 @@ static int execute(grt_plan *p)
     CU(cudaEventSynchronize(ctx->ev[4]));
     unsigned herr = 0;
     CU(cudaMemcpy(&herr, p->derr, sizeof(unsigned), cudaMemcpyDeviceToHost));
-    if (herr) return set_err(ctx, GRT_ERR_TIMEOUT, "a bounded device wait gave up (layer-table copy)");
+    if (herr)
+        return set_err(ctx, GRT_ERR_TIMEOUT,
+                       std::string("a bounded device wait gave up: ") + ((herr & 1) ? "layer-table copy " : "") +
+                           ((herr & 2) ? "tensor-core operand refill " : "") + ((herr & 4) ? "tensor-core issue " : "") +
+                           ((herr & 8) ? "tensor-core drain" : ""));
     float t[4];
     for (int i = 0; i < 4; i++) CU(cudaEventElapsedTime(&t[i], ctx->ev[i], ctx->ev[i + 1]));
     p->rep.ms_grt = t[0];

@@ -99,6 +99,39 @@ __device__ __forceinline__ double ddbj_ref(double x, int n)
     return n * bjn_ref(x, n - 1) / x - bjn_ref(x, n) * (n + n * n + x * x) / x / x;
 }
 
+// FP32 evaluation of the same formulas for x > 3 (the asymptotic branch of
+// A&S 9.4.3 / 9.4.6, where x = k r reaches 10^4): x is reduced modulo 2 pi in
+// FP64 (two-constant Cody-Waite split), the phase polynomial and amplitude
+// are FP32.  J2, J3 by the reference's upward recurrence (used for x > n).
+__device__ __forceinline__ void bessel_big_x(double x, float v[NBASIS])
+{
+    const double TWO_PI_HI = 6.28318530717958623200e+00;   // 2 pi rounded to double
+    const double TWO_PI_LO = 2.44929359829470635445e-16;   // 2 pi - TWO_PI_HI
+    double n = rint(x * 0.15915494309189533577);
+    float xr = (float)fma(-n, TWO_PI_LO, fma(-n, TWO_PI_HI, x));   // x mod 2 pi in [-pi, pi]
+    float xf = (float)x;
+    float t = 3.0f / xf;
+    float f0 = 0.79788456f + t * (-0.00000077f + t * (-0.0055274f + t * (-0.00009512f + t * (0.00137237f + t * (-0.00072805f + t * 0.00014476f)))));
+    float p0 = -0.78539816f + t * (-0.04166397f + t * (-0.00003954f + t * (0.00262573f + t * (-0.00054125f + t * (-0.00029333f + t * 0.00013558f)))));
+    float f1 = 0.79788456f + t * (0.00000156f + t * (0.01659667f + t * (0.00017105f + t * (-0.00249511f + t * (0.00113653f + t * (-0.00020033f))))));
+    float p1 = -2.35619449f + t * (0.12499612f + t * (0.0000565f + t * (-0.00637879f + t * (0.00074348f + t * (0.00079824f + t * (-0.00029166f))))));
+    float is = rsqrtf(xf);
+    float j0 = f0 * cosf(xr + p0) * is;
+    float j1 = f1 * cosf(xr + p1) * is;
+    float ix = 1.0f / xf;
+    float j2 = 2.0f * ix * j1 - j0;                  // x > 3 > n: upward recurrence
+    float j3 = 4.0f * ix * j2 - j1;
+    v[BJ0] = j0;
+    v[BJ1] = j1;
+    v[BJ2] = j2;
+    v[BJ0D] = -j1;                                   // 0 J0 / x - J1
+    v[BJ1D] = ix * j1 - j2;
+    v[BJ2D] = 2.0f * ix * j2 - j3;
+    v[BJ0DD] = -j0;                                  // reference second-derivative expression
+    v[BJ1DD] = ix * j0 - j1 * (2.0f + xf * xf) * ix * ix;
+    v[BJ2DD] = 2.0f * ix * j1 - j2 * (6.0f + xf * xf) * ix * ix;
+}
+
 template <typename R>
 __global__ void bessel_table_kernel(R *B, int nk, int nr, double dk, const double *dist)
 {
@@ -107,6 +140,13 @@ __global__ void bessel_table_kernel(R *B, int nk, int nr, double dk, const doubl
     int r = (int)(t % nr);
     int j = (int)(t / nr);
     double x = dist[r] * (dk * j);
+    if (sizeof(R) == 4 && x > 3.0) {
+        float vf[NBASIS];
+        bessel_big_x(x, vf);
+#pragma unroll
+        for (int b = 0; b < NBASIS; b++) B[((long long)j * NBASIS + b) * nr + r] = (R)vf[b];
+        return;
+    }
     double v[NBASIS];
     v[BJ0] = bjn_ref(x, 0);
     v[BJ1] = bjn_ref(x, 1);
@@ -232,11 +272,16 @@ struct KsumArgs {
 };
 
 // One thread per (w, receiver, k-lane); k-lanes of a receiver reduce at the end.
+// Each thread accumulates the output columns directly:
+//   col_c += (coef_t r^-rpow_t) (w_k k^kp_t J_bt(k r)) K_qt(w, k)
+// over the terms t of column c.  coef_t and rpow_t are compile-time constants
+// of the column tables, so a thread holds 1/r and 1/r^2 and its 2 NC
+// accumulators; k-chunks are summed plainly and folded with TwoSum.
 template <typename R, int SRC>
 __global__ void __launch_bounds__(kSumThreads) ksum_kernel(KsumArgs<R> A)
 {
     using CT = Cols<SRC>;
-    constexpr int NP = CT::NP, NC = CT::NC;
+    constexpr int NC = CT::NC, NQ = CT::NQ;
     __shared__ R red[kSumThreads * 2];
     const int ntile = (A.nr + A.rt - 1) / A.rt;
     const int iw = blockIdx.x / ntile;
@@ -247,17 +292,19 @@ __global__ void __launch_bounds__(kSumThreads) ksum_kernel(KsumArgs<R> A)
     const int rr = rvalid ? r : 0;
     const int nk = A.nk[iw];
     const long long off = A.koff[iw];
-    const C<R> *K = reinterpret_cast<const C<R> *>(A.K);
+    const C<R> *K = reinterpret_cast<const C<R> *>(A.K) + off;
+    const double drr = A.dist[rr];
+    const R ir = (R)(1.0 / drr), ir2 = (R)(1.0 / (drr * drr));
 
-    R hi[NP][2], lo[NP][2];
+    R hi[NC][2], lo[NC][2];
 #pragma unroll
-    for (int p = 0; p < NP; p++) hi[p][0] = hi[p][1] = lo[p][0] = lo[p][1] = R(0);
+    for (int c = 0; c < NC; c++) hi[c][0] = hi[c][1] = lo[c][0] = lo[c][1] = R(0);
     const R dk = (R)A.dk, dk_half = (R)(0.5 * A.dk);
 
     for (int jb = lane * kSumChunk; jb < nk; jb += A.jt * kSumChunk) {
-        R acc[NP][2];
+        R acc[NC][2];
 #pragma unroll
-        for (int p = 0; p < NP; p++) acc[p][0] = acc[p][1] = R(0);
+        for (int c = 0; c < NC; c++) acc[c][0] = acc[c][1] = R(0);
         const int je = min(jb + kSumChunk, nk);
         for (int j = jb; j < je; j++) {
             // k^p weights only scale the coefficients: working precision suffices
@@ -268,31 +315,35 @@ __global__ void __launch_bounds__(kSumThreads) ksum_kernel(KsumArgs<R> A)
             R bv[NBASIS];
 #pragma unroll
             for (int b = 0; b < NBASIS; b++) bv[b] = Bj[(long long)b * A.nr];
+            C<R> kq[NQ];
 #pragma unroll
-            for (int p = 0; p < NP; p++) {
-                constexpr int dummy = 0;
-                (void)dummy;
-                const Pair P = CT::pair(p);
-                const C<R> kq = K[(long long)P.q * A.nkw + off + j];
-                const R f = wk[P.kp] * bv[P.b];
-                acc[p][0] += kq.x * f;
-                acc[p][1] += kq.y * f;
+            for (int q = 0; q < NQ; q++) kq[q] = K[(long long)q * A.nkw + j];
+#pragma unroll
+            for (int c = 0; c < NC; c++) {
+#pragma unroll
+                for (int t = CT::col(c); t < CT::col(c + 1); t++) {
+                    const Term T = CT::term(t);
+                    const Pair P = CT::pair(T.pair);
+                    R f = wk[P.kp] * bv[P.b];
+                    if (T.rpow == 1) f *= ir;
+                    else if (T.rpow == 2) f *= ir2;
+                    f *= (R)T.coef;
+                    acc[c][0] += kq[P.q].x * f;
+                    acc[c][1] += kq[P.q].y * f;
+                }
             }
         }
 #pragma unroll
-        for (int p = 0; p < NP; p++) {
-            two_sum_acc(hi[p][0], lo[p][0], acc[p][0]);
-            two_sum_acc(hi[p][1], lo[p][1], acc[p][1]);
+        for (int c = 0; c < NC; c++) {
+            two_sum_acc(hi[c][0], lo[c][0], acc[c][0]);
+            two_sum_acc(hi[c][1], lo[c][1], acc[c][1]);
         }
     }
-    // reduce the k-lanes of each receiver, pair by pair
-    const double dr = A.dist[rr];
-    R col[NC][2];
+    // reduce the k-lanes of each receiver, column by column
+    C<R> *S = reinterpret_cast<C<R> *>(A.S);
 #pragma unroll
-    for (int c = 0; c < NC; c++) col[c][0] = col[c][1] = R(0);
-#pragma unroll
-    for (int p = 0; p < NP; p++) {
-        R v0 = hi[p][0] + lo[p][0], v1 = hi[p][1] + lo[p][1];
+    for (int c = 0; c < NC; c++) {
+        R v0 = hi[c][0] + lo[c][0], v1 = hi[c][1] + lo[c][1];
         if (A.jt > 1) {
             __syncthreads();
             red[2 * threadIdx.x] = v0;
@@ -308,24 +359,8 @@ __global__ void __launch_bounds__(kSumThreads) ksum_kernel(KsumArgs<R> A)
                 v1 = s1 + c1;
             }
         }
-        // scatter the pair into the columns that use it
-#pragma unroll
-        for (int c = 0; c < NC; c++) {
-#pragma unroll
-            for (int t = CT::col(c); t < CT::col(c + 1); t++) {
-                const Term T = CT::term(t);
-                if (T.pair == p) {
-                    const R sc = (R)(T.coef / (T.rpow == 0 ? 1.0 : (T.rpow == 1 ? dr : dr * dr)));
-                    col[c][0] += sc * v0;
-                    col[c][1] += sc * v1;
-                }
-            }
-        }
+        if (lane == 0 && rvalid) S[((long long)r * NC + c) * A.nw + iw] = C<R>{v0, v1};
     }
-    if (lane != 0 || !rvalid) return;
-    C<R> *S = reinterpret_cast<C<R> *>(A.S);
-#pragma unroll
-    for (int c = 0; c < NC; c++) S[((long long)r * NC + c) * A.nw + iw] = C<R>{col[c][0], col[c][1]};
 }
 
 // ---------------------------------------------------------------- spectral stage

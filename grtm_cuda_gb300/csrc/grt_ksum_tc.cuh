@@ -1,0 +1,364 @@
+// grt_ksum_tc.cuh -- the wavenumber integration on the tensor cores (tcgen05).
+//
+// For every output column c (get_int_val_single / _tensor, green.cu:1558-1716)
+//   S_c(w, r) = sum_k sum_{t in c} K_{q_t}(w, k) * Bt_t(k, r),
+//   Bt_t(k, r) = coef_t r^-rpow_t k^kp_t w_k J_{b_t}(k r),
+// i.e. one GEMM per column whose K dimension runs over (k, term).  A CTA
+// owns 64 frequencies (M = 128 rows: real parts in rows 0-63, imaginary parts
+// in rows 64-127), 16 receivers (N = 16) and a slice of the k range (split-K);
+// the accumulators of all columns live in tensor memory (NC x 16 columns).
+//
+// Precision: 3xTF32 -- each FP32 operand x is split into hi = tf32(x) and
+// lo = tf32(x - hi) and the product is hi*hi + hi*lo + lo*hi with FP32
+// accumulation (about 2^-21 relative per product).  Partial sums of the k
+// slices are added with TwoSum by spectral_tc_kernel.
+//
+// Roles (160 threads): warps 0-3 produce operand tiles in shared memory
+// (canonical K-major layout, no swizzle: 8-row x 16-byte core matrices) and
+// drain the accumulators at the end; warp 4 allocates tensor memory and one
+// of its threads issues tcgen05.mma and tcgen05.commit.  Two pipeline stages,
+// each guarded by a "full" and an "empty" mbarrier.  Every wait is bounded:
+// on timeout the CTA records an error, skips to the end, and still frees its
+// tensor memory.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "grt_integrate.cuh"
+#include "grt_types.h"
+
+namespace grt {
+
+namespace tc {
+
+constexpr int kM = 128;        // rows: 64 frequencies x (re, im)
+constexpr int kW = 64;         // frequencies per CTA
+constexpr int kN = 16;         // receivers per CTA
+constexpr int kKT = 8;         // k per stage = one tf32 MMA K
+constexpr int kStages = 2;
+constexpr int kProducers = 128;
+constexpr int kThreads = kProducers + 32;
+constexpr int kCoreBytes = 128;                      // 8 rows x 16 bytes
+constexpr int kATileBytes = (kM / 8) * (kKT / 4) * kCoreBytes;   // 4096: one q, one split
+constexpr int kBTileBytes = (kN / 8) * (kKT / 4) * kCoreBytes;   // 512: one term, one split
+constexpr uint32_t kTmemCols = 512;
+
+template <int SRC> struct TcCfg;
+template <> struct TcCfg<kSingle> {
+    static constexpr int NQ = QS_N, NC = kSingleNC, NT = 23;
+};
+template <> struct TcCfg<kTensor> {
+    static constexpr int NQ = QT_N, NC = kTensorNC, NT = 32;
+};
+
+template <int SRC> constexpr int stage_bytes()
+{
+    return TcCfg<SRC>::NQ * 2 * kATileBytes + TcCfg<SRC>::NT * 2 * kBTileBytes;
+}
+template <int SRC> constexpr int smem_bytes() { return kStages * stage_bytes<SRC>() + 1024; }
+
+// byte offset of element (row, k) inside a K-major core-matrix tile whose
+// core matrices are ordered (row block, k block) with kKT/4 k blocks per row block
+__device__ __forceinline__ uint32_t tile_off(int row, int k)
+{
+    return (uint32_t)(((row >> 3) * (kKT / 4) + (k >> 2)) * kCoreBytes + (row & 7) * 16 + (k & 3) * 4);
+}
+
+// shared-memory matrix descriptor: K-major, no swizzle.  LBO = distance of
+// core matrices adjacent in K (128 B), SBO = distance of 8-row groups.
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr)
+{
+    const uint64_t lbo = kCoreBytes, sbo = (uint64_t)(kKT / 4) * kCoreBytes;
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+    d |= (uint64_t)(lbo >> 4) << 16;
+    d |= (uint64_t)(sbo >> 4) << 32;
+    d |= (uint64_t)1 << 46;       // descriptor version for sm_100-family tensor cores
+    return d;                     // base offset 0, layout type 0 (no swizzle)
+}
+
+// instruction descriptor: dense, D = F32, A = B = TF32, both K-major, M = 128, N = 16
+constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kN >> 3) << 17) |
+                            ((uint32_t)(kM >> 4) << 24);
+
+__device__ __forceinline__ float tf32_rna(float x)
+{
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+// bounded wait; false after 2^22 polls (a stage takes about a microsecond)
+__device__ __forceinline__ bool mbar_wait_b(uint32_t bar, uint32_t parity)
+{
+    for (int it = 0; it < (1 << 22); it++) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t acc)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
+        "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(acc)
+        : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+}  // namespace tc
+
+template <typename R>
+struct KsumTcArgs {
+    const float *K;          // [nq][nkw] complex
+    const float *B;          // [nkmax][NBASIS][nr]
+    const int *nk;           // [nw]
+    const long long *koff;   // [nw]
+    const double *dist;      // [nr]
+    float *P;                // partial sums [nsplit][nr][nc][nw] complex
+    long long nkw;
+    double dk;
+    int nw, nr, nkmax, nsplit, kslice;   // kslice: k per split (multiple of kKT)
+    unsigned int *err;
+};
+
+template <int SRC>
+__global__ void __launch_bounds__(tc::kThreads, 1) ksum_tc_kernel(KsumTcArgs<float> A)
+{
+    using namespace tc;
+    using CT = Cols<SRC>;
+    constexpr int NQ = TcCfg<SRC>::NQ, NC = TcCfg<SRC>::NC, NT = TcCfg<SRC>::NT;
+    static_assert(NC * kN <= (int)kTmemCols, "accumulators exceed tensor memory");
+    extern __shared__ __align__(1024) unsigned char smem_tc[];
+    __shared__ __align__(8) unsigned long long bars[2 * kStages + 1];
+    __shared__ uint32_t tmem_base_s;
+    __shared__ int fail_s;
+
+    const int nrt = (A.nr + kN - 1) / kN;
+    const int wt = blockIdx.x / (nrt * A.nsplit);
+    const int rem = blockIdx.x % (nrt * A.nsplit);
+    const int rt = rem / A.nsplit, sp = rem % A.nsplit;
+    const int w0 = wt * kW, r0 = rt * kN;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    // k range of this CTA: [kb, ke) within the longest frequency of the tile
+    int nkt = 0;
+    for (int i = 0; i < kW; i++)
+        if (w0 + i < A.nw) nkt = max(nkt, A.nk[w0 + i]);
+    const int kb = sp * A.kslice;
+    const int ke = min(nkt, kb + A.kslice);
+    const int nstage = ke > kb ? (ke - kb + kKT - 1) / kKT : 0;
+
+    unsigned char *sm = (unsigned char *)(((uintptr_t)smem_tc + 1023) & ~(uintptr_t)1023);
+    const uint32_t sm_s = (uint32_t)__cvta_generic_to_shared(sm);
+    auto full_bar = [&](int s) { return (uint32_t)__cvta_generic_to_shared(&bars[s]); };
+    auto empty_bar = [&](int s) { return (uint32_t)__cvta_generic_to_shared(&bars[kStages + s]); };
+    const uint32_t done_bar = (uint32_t)__cvta_generic_to_shared(&bars[2 * kStages]);
+    auto a_tile = [&](int s, int q, int split) {
+        return (uint32_t)(s * stage_bytes<SRC>() + (q * 2 + split) * kATileBytes);
+    };
+    auto b_tile = [&](int s, int t, int split) {
+        return (uint32_t)(s * stage_bytes<SRC>() + NQ * 2 * kATileBytes + (t * 2 + split) * kBTileBytes);
+    };
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; s++) {
+            tc::mbar_init(full_bar(s), kProducers);
+            tc::mbar_init(empty_bar(s), 1);
+        }
+        tc::mbar_init(done_bar, 1);
+        fail_s = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 4) {
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&tmem_base_s);
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst), "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_base_s;
+
+    if (warp < 4) {
+        // ---------------- producers
+        const int tid = threadIdx.x;
+        // per-thread receiver constants for the Bessel-term operand
+        const int br = tid >> 3, bk = tid & 7;          // (receiver, k) of this thread in a stage
+        const int rg = min(r0 + br, A.nr - 1);
+        const bool rok = (r0 + br) < A.nr;
+        const double drr = A.dist[rg];
+        const float ir = (float)(1.0 / drr), ir2 = (float)(1.0 / (drr * drr));
+        const float dk = (float)A.dk;
+        for (int st = 0; st < nstage; st++) {
+            const int s = st % kStages;
+            if (st >= kStages) {
+                if (!tc::mbar_wait_b(empty_bar(s), ((st / kStages) - 1) & 1)) {
+                    atomicOr(A.err, 2u);
+                    fail_s = 1;
+                }
+            }
+            if (fail_s) break;
+            const int k0 = kb + st * kKT;
+            // A operand: K_q(w, k0..k0+7), hi/lo, real rows 0-63, imaginary 64-127
+            for (int it = tid; it < NQ * kW; it += kProducers) {
+                const int q = it / kW, wl = it % kW, w = w0 + wl;
+                float re[kKT], im[kKT];
+                const int nkw_ = (w < A.nw) ? A.nk[w] : 0;
+                const long long base = (w < A.nw) ? ((long long)q * A.nkw + A.koff[w]) : 0;
+#pragma unroll
+                for (int kk = 0; kk < kKT; kk++) {
+                    const int k = k0 + kk;
+                    float2 v = make_float2(0.f, 0.f);
+                    if (k < nkw_ && k < ke) v = reinterpret_cast<const float2 *>(A.K)[base + k];
+                    re[kk] = v.x;
+                    im[kk] = v.y;
+                }
+#pragma unroll
+                for (int part = 0; part < 2; part++) {
+                    const float *src = part ? im : re;
+                    const int row = part * kW + wl;
+#pragma unroll
+                    for (int kq = 0; kq < kKT; kq += 4) {
+                        float4 h, l;
+                        h.x = tc::tf32_rna(src[kq]); l.x = tc::tf32_rna(src[kq] - h.x);
+                        h.y = tc::tf32_rna(src[kq + 1]); l.y = tc::tf32_rna(src[kq + 1] - h.y);
+                        h.z = tc::tf32_rna(src[kq + 2]); l.z = tc::tf32_rna(src[kq + 2] - h.z);
+                        h.w = tc::tf32_rna(src[kq + 3]); l.w = tc::tf32_rna(src[kq + 3] - h.w);
+                        *reinterpret_cast<float4 *>(sm + a_tile(s, q, 0) + tc::tile_off(row, kq)) = h;
+                        *reinterpret_cast<float4 *>(sm + a_tile(s, q, 1) + tc::tile_off(row, kq)) = l;
+                    }
+                }
+            }
+            // B operand: term values coef r^-rpow k^kp w J_b(k r) for (receiver br, k bk)
+            {
+                const int k = k0 + bk;
+                const bool kok = k < ke && rok;
+                float bv[NBASIS];
+#pragma unroll
+                for (int b = 0; b < NBASIS; b++)
+                    bv[b] = kok ? A.B[((long long)k * NBASIS + b) * A.nr + rg] : 0.f;
+                const float kf = dk * (float)k;
+                const float w = (k == 0) ? 0.5f * dk : dk;
+                const float wk[3] = {w, w * kf, w * kf * kf};
+#pragma unroll
+                for (int t = 0; t < NT; t++) {
+                    const Term T = CT::term(t);
+                    const Pair P = CT::pair(T.pair);
+                    float v = wk[P.kp] * bv[P.b] * (float)T.coef;
+                    if (T.rpow == 1) v *= ir;
+                    else if (T.rpow == 2) v *= ir2;
+                    const float h = tc::tf32_rna(v), l = tc::tf32_rna(v - h);
+                    *reinterpret_cast<float *>(sm + b_tile(s, t, 0) + tc::tile_off(br, bk)) = h;
+                    *reinterpret_cast<float *>(sm + b_tile(s, t, 1) + tc::tile_off(br, bk)) = l;
+                }
+            }
+            // make the generic-proxy writes visible to the tensor cores, then signal
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            tc::mbar_arrive(full_bar(s));
+        }
+    } else if (lane == 0) {
+        // ---------------- MMA issuer (one thread of warp 4)
+        for (int st = 0; st < nstage; st++) {
+            const int s = st % kStages;
+            if (!tc::mbar_wait_b(full_bar(s), (st / kStages) & 1)) {
+                atomicOr(A.err, 4u);
+                fail_s = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll 1
+            for (int c = 0; c < NC; c++) {
+                for (int t = CT::col(c); t < CT::col(c + 1); t++) {
+                    const int q = CT::pair(CT::term(t).pair).q;
+                    const uint32_t d = tmem + (uint32_t)(c * kN);
+                    const uint64_t ah = tc::sdesc(sm_s + a_tile(s, q, 0)), al = tc::sdesc(sm_s + a_tile(s, q, 1));
+                    const uint64_t bh = tc::sdesc(sm_s + b_tile(s, t, 0)), bl = tc::sdesc(sm_s + b_tile(s, t, 1));
+                    const uint32_t first = (st == 0 && t == CT::col(c)) ? 0u : 1u;
+                    tc::mma_tf32(d, ah, bh, first);
+                    tc::mma_tf32(d, ah, bl, 1u);
+                    tc::mma_tf32(d, al, bh, 1u);
+                }
+            }
+            tc::mma_commit(empty_bar(s));   // stage s may be refilled once these MMAs finish
+        }
+        tc::mma_commit(done_bar);           // all MMAs of this CTA
+    }
+
+    // ---------------- drain: tensor memory -> partial sums
+    if (warp < 4) {
+        // the issuer always commits done_bar (immediately when it issued nothing)
+        bool ok = nstage > 0;
+        if (!tc::mbar_wait_b(done_bar, 0)) {
+            atomicOr(A.err, 8u);
+            ok = false;
+        }
+        if (fail_s) ok = false;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const int row = warp * 32 + lane;            // the lane of tensor memory this thread reads
+        const int part = row / kW, wl = row % kW, w = w0 + wl;
+        for (int c = 0; c < NC; c++) {
+            uint32_t v[kN];
+            const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * kN);
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                  "=r"(v[15])
+                : "r"(taddr)
+                : "memory");
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (w < A.nw) {
+#pragma unroll
+                for (int j = 0; j < kN; j++) {
+                    const int r = r0 + j;
+                    if (r < A.nr) {
+                        const float val = ok ? __uint_as_float(v[j]) : 0.f;
+                        A.P[((((long long)sp * A.nr + r) * NC + c) * A.nw + w) * 2 + part] = val;
+                    }
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 4) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+    }
+}
+
+// S[r][c][w] = sum over k slices of the partial sums (TwoSum)
+__global__ void ksum_tc_reduce_kernel(const float *P, float *S, long long n, int nsplit)
+{
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float hi = 0.f, lo = 0.f;
+    for (int s = 0; s < nsplit; s++) two_sum_acc(hi, lo, P[(long long)s * n + i]);
+    S[i] = hi + lo;
+}
+
+}  // namespace grt

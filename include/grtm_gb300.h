@@ -83,6 +83,7 @@ typedef struct grt_report {
     int kernel_launches;  /* kernels launched by the last execute */
     long long h2d_bytes;  /* bytes the plan uploads (layer tables, grids, receivers) */
     long long d2h_bytes;  /* bytes one fetch of the traces downloads */
+    int ksum_impl;        /* wavenumber sum: 0 SIMT FP32/FP64, 1 tensor cores (3xTF32) */
 } grt_report;
 
 typedef struct grt_ctx grt_ctx;
