@@ -37,6 +37,8 @@ struct grt_plan {
     int rt = 128, jt = 1;
     int use_tc = 0, nsplit = 1, kslice = 0;   // tensor-core wavenumber sum and its split-K
     void *P = nullptr;                        // split-K partial sums
+    float *Kt = nullptr;                      // coefficients in GEMM operand layout
+    long long *kt_base = nullptr;             // per frequency tile offset into Kt (floats)
     std::vector<double> dist;
     double slot0[4] = {0, 0, 0, 0};
     // device buffers
@@ -111,7 +113,7 @@ extern "C" void grt_plan_destroy(grt_plan *p)
     if (!p) return;
     cudaSetDevice(p->ctx->device);
     void *bufs[] = {p->tab, p->K, p->B, p->S, p->post, p->tw, p->spec, p->sig, p->tiles, p->nk, p->koff, p->ddist,
-                    p->damp, p->derr, p->P};
+                    p->damp, p->derr, p->P, p->Kt, p->kt_base};
     for (void *b : bufs)
         if (b) cudaFree(b);
     delete p;
@@ -197,7 +199,7 @@ static int upload(grt_plan *p)
     CU(cudaMalloc(&p->nk, J.nw * sizeof(int)));
     CU(cudaMalloc(&p->koff, J.nw * sizeof(long long)));
     CU(cudaMalloc(&p->ddist, p->nd * sizeof(double)));
-    CU(cudaMalloc(&p->K, szK));
+    if (!p->use_tc) CU(cudaMalloc(&p->K, szK));
     CU(cudaMalloc(&p->B, szB));
     CU(cudaMalloc(&p->S, ntr * J.nw * 2 * sizeof(R)));
     CU(cudaMalloc(&p->post, post.size() * sizeof(R)));
@@ -224,6 +226,26 @@ static int upload(grt_plan *p)
         p->nsplit = best;
         p->kslice = ((J.nkmax + best - 1) / best + grt::tc::kKT - 1) / grt::tc::kKT * grt::tc::kKT;
         CU(cudaMalloc(&p->P, (size_t)best * ntr * J.nw * 2 * sizeof(float)));
+        // operand blocks of (frequency tile of 64, k stage of 8): nq x (hi, lo) x 1024 floats each
+        const int nwt = (J.nw + grt::tc::kW - 1) / grt::tc::kW;
+        std::vector<long long> base(nwt);
+        long long tot = 0;
+        bool padded = (J.nw % grt::tc::kW) != 0;
+        for (int t = 0; t < nwt; t++) {
+            int mx = 0;
+            for (int i = t * grt::tc::kW; i < std::min(J.nw, (t + 1) * grt::tc::kW); i++) mx = std::max(mx, J.nk[i]);
+            const int ns = (mx + grt::tc::kKT - 1) / grt::tc::kKT;
+            for (int i = t * grt::tc::kW; i < std::min(J.nw, (t + 1) * grt::tc::kW); i++)
+                if (J.nk[i] != ns * grt::tc::kKT) padded = true;
+            base[t] = tot;
+            tot += (long long)ns * p->nq * 2 * grt::tc::kM * grt::tc::kKT;
+        }
+        CU(cudaMalloc(&p->Kt, (size_t)tot * sizeof(float)));
+        CU(cudaMalloc(&p->kt_base, nwt * sizeof(long long)));
+        CU(cudaMemcpyAsync(p->kt_base, base.data(), nwt * sizeof(long long), cudaMemcpyHostToDevice, ctx->stream));
+        // slots beyond a frequency's k range stay zero: the GRT kernel only writes valid (w,k)
+        if (padded) CU(cudaMemsetAsync(p->Kt, 0, (size_t)tot * sizeof(float), ctx->stream));
+        CU(cudaStreamSynchronize(ctx->stream));
     }
     cudaStream_t st = ctx->stream;
     CU(cudaMemcpyAsync(p->tab, tab.data(), tab.size() * sizeof(tab[0]), cudaMemcpyHostToDevice, st));
@@ -294,7 +316,8 @@ static int launch_ksum_tc(grt_plan *p, cudaStream_t st, int &launches)
     grt_ctx *ctx = p->ctx;
     const Job &J = p->J;
     grt::KsumTcArgs<float> T{};
-    T.K = (const float *)p->K;
+    T.Kt = p->Kt;
+    T.kt_base = p->kt_base;
     T.B = (const float *)p->B;
     T.nk = p->nk;
     T.koff = p->koff;
@@ -352,6 +375,8 @@ static int execute(grt_plan *p)
     A.L = J.L; A.s = J.s; A.rl = J.rl; A.src = J.src; A.fix = J.fix; A.nq = p->nq;
     for (int i = 0; i < 4; i++) A.slot0[i] = (R)p->slot0[i];
     A.err = p->derr;
+    A.Kt = p->use_tc ? p->Kt : nullptr;
+    A.kt_base = p->kt_base;
     const size_t smem = (size_t)J.L * sizeof(grt::LayerW<R>);
     CU(cudaEventRecord(ctx->ev[0], st));
     grt::grt_point_kernel<R><<<p->ntiles, grt::kGrtThreads, smem, st>>>(A);

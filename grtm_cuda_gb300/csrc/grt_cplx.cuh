@@ -90,6 +90,24 @@ template <typename R> GRT_HD C<R> expm1_over_small(C<R> y)
     return s;
 }
 
+// ---- operand tiles of the tensor-core wavenumber GEMM (shared by the GRT
+// kernel, which writes them, and the GEMM, which reads them)
+constexpr int kTileK = 8;          // k per tile (one TF32 MMA K step)
+constexpr int kTileRows = 128;     // 64 frequencies x (re, im)
+// byte offset of element (row, k) in a K-major, no-swizzle core-matrix tile:
+// 8-row x 16-byte core matrices ordered (row block, k block), 2 k blocks per row block
+__host__ __device__ constexpr unsigned kt_tile_off(int row, int k)
+{
+    return (unsigned)((((row >> 3) * (kTileK / 4) + (k >> 2)) * 128) + (row & 7) * 16 + (k & 3) * 4);
+}
+// FP32 -> TF32, round to nearest (ties away from zero)
+__device__ __forceinline__ float tf32_rna(float x)
+{
+    unsigned r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
 template <typename R>
 struct M2 {
     C<R> a, b, c, d;  // [[a, b], [c, d]]

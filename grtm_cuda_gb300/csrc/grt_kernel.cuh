@@ -151,10 +151,42 @@ __device__ __forceinline__ void interface_rt(const SL<R> &U, const SL<R> &D, R k
     m.tuu0 = wb * is * R(2);
 }
 
+// where this thread's coefficients go: the flat column K[q][koff + j], or the
+// tensor-core operand block of its (frequency tile, k stage)
+struct KOut {
+    long long idx;        // koff[iw] + j
+    float *blk;           // operand block, or null
+    unsigned ore, oim;    // float offsets of the re / im rows inside a q tile
+};
+
 template <typename R>
-__device__ __forceinline__ void store_q(const GrtArgs<R> &A, int q, long long idx, C<R> v)
+__device__ __forceinline__ KOut make_kout(const GrtArgs<R> &A, int iw, int j)
 {
-    reinterpret_cast<C<R> *>(A.K)[(long long)q * A.nkw + idx] = v;
+    KOut o{A.koff[iw] + j, nullptr, 0u, 0u};
+    if (sizeof(R) == 4 && A.Kt) {
+        const int wl = iw % (kTileRows / 2);
+        o.blk = A.Kt + A.kt_base[iw / (kTileRows / 2)] + (long long)(j / kTileK) * A.nq * 2 * (kTileRows * kTileK);
+        o.ore = kt_tile_off(wl, j % kTileK) / 4;
+        o.oim = kt_tile_off(kTileRows / 2 + wl, j % kTileK) / 4;
+    }
+    return o;
+}
+
+template <typename R>
+__device__ __forceinline__ void store_q(const GrtArgs<R> &A, int q, const KOut &o, C<R> v)
+{
+    if (sizeof(R) == 4 && o.blk) {
+        // TF32 hi / lo words of the 3xTF32 product, [q][hi|lo] tiles of 1024 floats
+        float *t = o.blk + q * 2 * (kTileRows * kTileK);
+        const float x = (float)v.x, y = (float)v.y;
+        const float xh = tf32_rna(x), yh = tf32_rna(y);
+        t[o.ore] = xh;
+        t[kTileRows * kTileK + o.ore] = tf32_rna(x - xh);
+        t[o.oim] = yh;
+        t[kTileRows * kTileK + o.oim] = tf32_rna(y - yh);
+        return;
+    }
+    reinterpret_cast<C<R> *>(A.K)[(long long)q * A.nkw + o.idx] = v;
 }
 
 // bounded wait on an mbarrier phase; gives up (error word) instead of hanging
@@ -434,7 +466,7 @@ __global__ void __launch_bounds__(kGrtThreads, GRT_POINT_MINB) grt_point_kernel(
     }
 
     if (!valid) return;
-    const long long idx = A.koff[iw] + j;
+    const KOut out = make_kout(A, iw, j);
     if (A.src == kSingle) {
         C<R> f0a = -(S.d0 * iG * R(0.5)), f0b = C<R>{k, R(0)} * iG * R(0.5);
         C<R> g0a, g0b, g1a, g1b;
@@ -444,18 +476,18 @@ __global__ void __launch_bounds__(kGrtThreads, GRT_POINT_MINB) grt_point_kernel(
         C<R> a00, a01, a10, a11;
         mv2(y1, g0a, g0b, &a00, &a01);
         mv2(y1, g1a, g1b, &a10, &a11);
-        store_q(A, QS_B1, idx, y0 * gsh);
-        store_q(A, QS_A00, idx, a00);
-        store_q(A, QS_A01, idx, a01);
-        store_q(A, QS_A10, idx, a10);
-        store_q(A, QS_A11, idx, a11);
+        store_q(A, QS_B1, out, y0 * gsh);
+        store_q(A, QS_A00, out, a00);
+        store_q(A, QS_A01, out, a01);
+        store_q(A, QS_A10, out, a10);
+        store_q(A, QS_A11, out, a11);
         mv2(y1t, g0a, g0b, &a00, &a01);
         mv2(y1t, g1a, g1b, &a10, &a11);
-        store_q(A, QS_B1T, idx, y0t * gsh);
-        store_q(A, QS_A0T0, idx, a00);
-        store_q(A, QS_A0T1, idx, a01);
-        store_q(A, QS_A1T0, idx, a10);
-        store_q(A, QS_A1T1, idx, a11);
+        store_q(A, QS_B1T, out, y0t * gsh);
+        store_q(A, QS_A0T0, out, a00);
+        store_q(A, QS_A0T1, out, a01);
+        store_q(A, QS_A1T0, out, a10);
+        store_q(A, QS_A1T1, out, a11);
     } else {
         // s2 = k f1, s1 = -1/(2 mu) G^-1 e0, s0 = H^-1 (alpha', beta')
         C<R> s2a = f1a * k, s2b = f1b * k;
@@ -472,29 +504,29 @@ __global__ void __launch_bounds__(kGrtThreads, GRT_POINT_MINB) grt_point_kernel(
         C<R> shf = up ? fu : fd - R(1);
         C<R> h1 = shf * S.v * ssh, h2 = shf * k * ssh;
         C<R> v0, v1;
-        store_q(A, QT_B1, idx, y0 * h1);
-        store_q(A, QT_B2, idx, y0 * h2);
+        store_q(A, QT_B1, out, y0 * h1);
+        store_q(A, QT_B2, out, y0 * h2);
         mv2(y1, q0a, q0b, &v0, &v1);
-        store_q(A, QT_A00, idx, v0);
-        store_q(A, QT_A01, idx, v1);
+        store_q(A, QT_A00, out, v0);
+        store_q(A, QT_A01, out, v1);
         mv2(y1, q1a, q1b, &v0, &v1);
-        store_q(A, QT_A10, idx, v0);
-        store_q(A, QT_A11, idx, v1);
+        store_q(A, QT_A10, out, v0);
+        store_q(A, QT_A11, out, v1);
         mv2(y1, q2a, q2b, &v0, &v1);
-        store_q(A, QT_A20, idx, v0);
-        store_q(A, QT_A21, idx, v1);
+        store_q(A, QT_A20, out, v0);
+        store_q(A, QT_A21, out, v1);
         if (A.nq > QT_N) {
-            store_q(A, QT_N + QT_B1, idx, y0t * h1);
-            store_q(A, QT_N + QT_B2, idx, y0t * h2);
+            store_q(A, QT_N + QT_B1, out, y0t * h1);
+            store_q(A, QT_N + QT_B2, out, y0t * h2);
             mv2(y1t, q0a, q0b, &v0, &v1);
-            store_q(A, QT_N + QT_A00, idx, v0);
-            store_q(A, QT_N + QT_A01, idx, v1);
+            store_q(A, QT_N + QT_A00, out, v0);
+            store_q(A, QT_N + QT_A01, out, v1);
             mv2(y1t, q1a, q1b, &v0, &v1);
-            store_q(A, QT_N + QT_A10, idx, v0);
-            store_q(A, QT_N + QT_A11, idx, v1);
+            store_q(A, QT_N + QT_A10, out, v0);
+            store_q(A, QT_N + QT_A11, out, v1);
             mv2(y1t, q2a, q2b, &v0, &v1);
-            store_q(A, QT_N + QT_A20, idx, v0);
-            store_q(A, QT_N + QT_A21, idx, v1);
+            store_q(A, QT_N + QT_A20, out, v0);
+            store_q(A, QT_N + QT_A21, out, v1);
         }
     }
 }

@@ -57,12 +57,8 @@ template <int SRC> constexpr int stage_bytes()
 }
 template <int SRC> constexpr int smem_bytes() { return kStages * stage_bytes<SRC>() + 1024; }
 
-// byte offset of element (row, k) inside a K-major core-matrix tile whose
-// core matrices are ordered (row block, k block) with kKT/4 k blocks per row block
-__device__ __forceinline__ uint32_t tile_off(int row, int k)
-{
-    return (uint32_t)(((row >> 3) * (kKT / 4) + (k >> 2)) * kCoreBytes + (row & 7) * 16 + (k & 3) * 4);
-}
+static_assert(kKT == kTileK && kM == kTileRows, "tile shape shared with the GRT kernel");
+__device__ __forceinline__ uint32_t tile_off(int row, int k) { return kt_tile_off(row, k); }
 
 // shared-memory matrix descriptor: K-major, no swizzle.  LBO = distance of
 // core matrices adjacent in K (128 B), SBO = distance of 8-row groups.
@@ -81,12 +77,7 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t saddr)
 constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kN >> 3) << 17) |
                             ((uint32_t)(kM >> 4) << 24);
 
-__device__ __forceinline__ float tf32_rna(float x)
-{
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return __uint_as_float(r);
-}
+__device__ __forceinline__ float tf32_rna(float x) { return grt::tf32_rna(x); }
 
 __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
 {
@@ -132,7 +123,8 @@ __device__ __forceinline__ void mma_commit(uint32_t bar)
 
 template <typename R>
 struct KsumTcArgs {
-    const float *K;          // [nq][nkw] complex
+    const float *Kt;         // operand blocks written by the GRT kernel (see GrtArgs::Kt)
+    const long long *kt_base;
     const float *B;          // [nkmax][NBASIS][nr]
     const int *nk;           // [nw]
     const long long *koff;   // [nw]
@@ -185,7 +177,8 @@ __global__ void __launch_bounds__(tc::kThreads, 1) ksum_tc_kernel(KsumTcArgs<flo
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kStages; s++) {
-            tc::mbar_init(full_bar(s), kProducers);
+            // every producer arrives once, plus producer 0's expect-tx arrival for the A copy
+            tc::mbar_init(full_bar(s), kProducers + 1);
             tc::mbar_init(empty_bar(s), 1);
         }
         tc::mbar_init(done_bar, 1);
@@ -213,6 +206,17 @@ __global__ void __launch_bounds__(tc::kThreads, 1) ksum_tc_kernel(KsumTcArgs<flo
         const double drr = A.dist[rg];
         const float ir = (float)(1.0 / drr), ir2 = (float)(1.0 / (drr * drr));
         const float dk = (float)A.dk;
+        const unsigned a_bytes = (unsigned)(NQ * 2 * kATileBytes);
+        const float *kt_tile = A.Kt + A.kt_base[wt];
+        // Bessel values of the next stage, loaded one stage ahead
+        float bv[NBASIS];
+        auto load_b = [&](int st_) {
+            const int k = kb + st_ * kKT + bk;
+            const bool kok = st_ < nstage && k < ke && rok;
+#pragma unroll
+            for (int b = 0; b < NBASIS; b++) bv[b] = kok ? __ldg(A.B + ((long long)k * NBASIS + b) * A.nr + rg) : 0.f;
+        };
+        load_b(0);
         for (int st = 0; st < nstage; st++) {
             const int s = st % kStages;
             if (st >= kStages) {
@@ -223,44 +227,25 @@ __global__ void __launch_bounds__(tc::kThreads, 1) ksum_tc_kernel(KsumTcArgs<flo
             }
             if (fail_s) break;
             const int k0 = kb + st * kKT;
-            // A operand: K_q(w, k0..k0+7), hi/lo, real rows 0-63, imaginary 64-127
-            for (int it = tid; it < NQ * kW; it += kProducers) {
-                const int q = it / kW, wl = it % kW, w = w0 + wl;
-                float re[kKT], im[kKT];
-                const int nkw_ = (w < A.nw) ? A.nk[w] : 0;
-                const long long base = (w < A.nw) ? ((long long)q * A.nkw + A.koff[w]) : 0;
-#pragma unroll
-                for (int kk = 0; kk < kKT; kk++) {
-                    const int k = k0 + kk;
-                    float2 v = make_float2(0.f, 0.f);
-                    if (k < nkw_ && k < ke) v = reinterpret_cast<const float2 *>(A.K)[base + k];
-                    re[kk] = v.x;
-                    im[kk] = v.y;
-                }
-#pragma unroll
-                for (int part = 0; part < 2; part++) {
-                    const float *src = part ? im : re;
-                    const int row = part * kW + wl;
-#pragma unroll
-                    for (int kq = 0; kq < kKT; kq += 4) {
-                        float4 h, l;
-                        h.x = tc::tf32_rna(src[kq]); l.x = tc::tf32_rna(src[kq] - h.x);
-                        h.y = tc::tf32_rna(src[kq + 1]); l.y = tc::tf32_rna(src[kq + 1] - h.y);
-                        h.z = tc::tf32_rna(src[kq + 2]); l.z = tc::tf32_rna(src[kq + 2] - h.z);
-                        h.w = tc::tf32_rna(src[kq + 3]); l.w = tc::tf32_rna(src[kq + 3] - h.w);
-                        *reinterpret_cast<float4 *>(sm + a_tile(s, q, 0) + tc::tile_off(row, kq)) = h;
-                        *reinterpret_cast<float4 *>(sm + a_tile(s, q, 1) + tc::tile_off(row, kq)) = l;
-                    }
-                }
+            // A operand: one bulk copy of the (frequency tile, k stage) block the
+            // GRT kernel wrote in operand layout
+            if (tid == 0) {
+                const float *src = kt_tile + (long long)(k0 / kKT) * (NQ * 2 * kM * kKT);
+                const uint32_t dst = sm_s + a_tile(s, 0, 0);
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(full_bar(s)), "r"(a_bytes)
+                             : "memory");
+                asm volatile(
+                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                    "l"(src), "r"(a_bytes), "r"(full_bar(s))
+                    : "memory");
             }
             // B operand: term values coef r^-rpow k^kp w J_b(k r) for (receiver br, k bk)
             {
                 const int k = k0 + bk;
-                const bool kok = k < ke && rok;
-                float bv[NBASIS];
+                float cur[NBASIS];
 #pragma unroll
-                for (int b = 0; b < NBASIS; b++)
-                    bv[b] = kok ? A.B[((long long)k * NBASIS + b) * A.nr + rg] : 0.f;
+                for (int b = 0; b < NBASIS; b++) cur[b] = bv[b];
+                load_b(st + 1);
                 const float kf = dk * (float)k;
                 const float w = (k == 0) ? 0.5f * dk : dk;
                 const float wk[3] = {w, w * kf, w * kf * kf};
@@ -268,7 +253,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) ksum_tc_kernel(KsumTcArgs<flo
                 for (int t = 0; t < NT; t++) {
                     const Term T = CT::term(t);
                     const Pair P = CT::pair(T.pair);
-                    float v = wk[P.kp] * bv[P.b] * (float)T.coef;
+                    float v = wk[P.kp] * cur[P.b] * (float)T.coef;
                     if (T.rpow == 1) v *= ir;
                     else if (T.rpow == 2) v *= ir2;
                     const float h = tc::tf32_rna(v), l = tc::tf32_rna(v - h);
@@ -290,15 +275,19 @@ __global__ void __launch_bounds__(tc::kThreads, 1) ksum_tc_kernel(KsumTcArgs<flo
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll 1
+            // fully unrolled: term, operand and accumulator indices are compile-time
+            // constants; descriptors are the stage's base descriptor plus a constant
+            const uint64_t dbase = tc::sdesc(sm_s + (uint32_t)(s * stage_bytes<SRC>()));
+            const uint32_t acc0 = st == 0 ? 0u : 1u;
+#pragma unroll
             for (int c = 0; c < NC; c++) {
+#pragma unroll
                 for (int t = CT::col(c); t < CT::col(c + 1); t++) {
                     const int q = CT::pair(CT::term(t).pair).q;
                     const uint32_t d = tmem + (uint32_t)(c * kN);
-                    const uint64_t ah = tc::sdesc(sm_s + a_tile(s, q, 0)), al = tc::sdesc(sm_s + a_tile(s, q, 1));
-                    const uint64_t bh = tc::sdesc(sm_s + b_tile(s, t, 0)), bl = tc::sdesc(sm_s + b_tile(s, t, 1));
-                    const uint32_t first = (st == 0 && t == CT::col(c)) ? 0u : 1u;
-                    tc::mma_tf32(d, ah, bh, first);
+                    const uint64_t ah = dbase + ((uint64_t)a_tile(0, q, 0) >> 4), al = dbase + ((uint64_t)a_tile(0, q, 1) >> 4);
+                    const uint64_t bh = dbase + ((uint64_t)b_tile(0, t, 0) >> 4), bl = dbase + ((uint64_t)b_tile(0, t, 1) >> 4);
+                    tc::mma_tf32(d, ah, bh, t == CT::col(c) ? acc0 : 1u);
                     tc::mma_tf32(d, ah, bl, 1u);
                     tc::mma_tf32(d, al, bh, 1u);
                 }

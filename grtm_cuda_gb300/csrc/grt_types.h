@@ -48,6 +48,13 @@ struct GrtArgs {
     int L, s, rl, src, fix, nq;
     R slot0[4];                // nu_alpha, nu_beta of layer rl at (w = -i sigma, k = 0)
     unsigned int *err;         // device error word (bounded waits that gave up)
+    // tensor-core layout of the coefficients (FP32 plans): when Kt is set the
+    // kernel writes, instead of K, TF32 hi/lo words straight into the operand
+    // tiles of the wavenumber GEMM: block (frequency tile of 64, k stage of 8)
+    // at Kt + kt_base[tile] + stage * nq * 2048 floats, inside it [q][hi|lo]
+    // K-major core-matrix tiles of 128 rows (re rows 0-63, im rows 64-127).
+    float *Kt;
+    const long long *kt_base;
 };
 
 // Bessel basis functions of k r, in the order the integrand formulas use them
