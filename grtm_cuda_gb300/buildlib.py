@@ -16,8 +16,11 @@ LIB = os.path.join(LIBDIR, "libgrtm_gb300.so")
 
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# FP32 division and square root to ~2 ulp, subnormals flushed: the GRT kernel's
+# 2x2 inverses and complex square roots dominate its instruction count, and
+# its parity with the FP64 oracle is unchanged (FP64 code is not affected)
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
-         "-Xcompiler", "-fvisibility=hidden"]
+         "-Xcompiler", "-fvisibility=hidden", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"]
 SOURCES = ["grt_api.cu", "grt_job.cpp", "grt_noalloc.cu"]
 # extra nvcc flags (e.g. -DGRT_POINT_MINB=4) and an alternative output path,
 # for timing build variants side by side

@@ -66,7 +66,8 @@ template <typename R> GRT_HD C<R> cexp_(C<R> z)
 // principal square root (Re >= 0), cancellation-free form
 template <typename R> GRT_HD C<R> csqrt_(C<R> z)
 {
-    R m = cabs_(z);
+    // |z| without hypot's scaling: arguments here are k^2 - (w/c)^2, far from overflow
+    R m = gsqrt(z.x * z.x + z.y * z.y);
     if (m == R(0)) return {R(0), R(0)};
     if (z.x >= R(0)) {
         R t = gsqrt((m + z.x) * R(0.5));
