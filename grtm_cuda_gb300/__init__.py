@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.environ.get("GRTM_GB300_LIB", os.path.join(HERE, "_lib", "libgrtm_gb300.so"))
 
 OK, ERR_ARG, ERR_IO, ERR_PARSE, ERR_MODEL, ERR_CUDA, ERR_NOMEM, ERR_TIMEOUT, ERR_UNSUPPORTED = range(9)
-K_REFERENCE, K_FIXED = 0, 1
+K_REFERENCE, K_FIXED, K_CUSTOM = 0, 1, 2
 FP32, FP64 = 0, 1
 FIX_RLAYER, FIX_REXUT, FIX_DZ = 1, 2, 4
 FIX_ALL = FIX_RLAYER | FIX_REXUT | FIX_DZ
@@ -34,7 +34,7 @@ class Opts(ctypes.Structure):
     _fields_ = [("dt", ctypes.c_double), ("log2n", ctypes.c_int), ("t0", ctypes.c_double),
                 ("taper", ctypes.c_double), ("sigma_factor", ctypes.c_double), ("k_mode", ctypes.c_int),
                 ("nk_fixed", ctypes.c_int), ("dk", ctypes.c_double), ("precision", ctypes.c_int),
-                ("fix", ctypes.c_int)]
+                ("fix", ctypes.c_int), ("nk_custom", ctypes.POINTER(ctypes.c_int))]
 
 
 class Report(ctypes.Structure):
@@ -53,8 +53,10 @@ class Report(ctypes.Structure):
 
 # every symbol the public header declares
 EXPORTS = ("grt_create", "grt_destroy", "grt_last_error", "grt_status_string", "grt_plan_create",
-           "grt_plan_execute", "grt_plan_fetch", "grt_plan_info", "grt_plan_destroy", "grt_run",
-           "grt_green", "green", "grt_run_noalloc")
+           "grt_plan_execute", "grt_plan_fetch", "grt_plan_fetch_freqs", "grt_plan_info", "grt_plan_destroy", "grt_grid", "grt_run",
+           "grt_green", "green", "grt_run_noalloc", "grt_sweep_kmax", "grt_mlp_create", "grt_mlp_destroy",
+           "grt_mlp_n_params", "grt_mlp_get_params", "grt_mlp_set_params", "grt_mlp_forward",
+           "grt_mlp_loss_grad", "grt_mlp_train")
 
 _lib = None
 
@@ -84,14 +86,30 @@ def lib():
     L.grt_plan_create.argtypes = [vp, P(Model), P(Opts), ctypes.c_int, _dp, P(vp)]
     L.grt_plan_execute.argtypes = [vp, P(Report)]
     L.grt_plan_fetch.argtypes = [vp, _dp, _dp]
+    L.grt_plan_fetch_freqs.argtypes = [vp, ctypes.c_int, P(ctypes.c_int), _dp]
     L.grt_plan_info.argtypes = [vp, P(Report)]
     L.grt_plan_destroy.argtypes = [vp]
     L.grt_plan_destroy.restype = None
+    L.grt_grid.argtypes = [P(Model), P(Opts), P(Report)]
     L.grt_run.argtypes = [vp, P(Model), P(Opts), ctypes.c_int, _dp, _dp, _dp, P(Report)]
     L.grt_green.argtypes = [ctypes.c_char_p] * 3
     L.green.argtypes = [ctypes.c_char_p] * 3
     L.green.restype = None
     L.grt_run_noalloc.argtypes = [ctypes.c_int, P(Model), P(Opts), ctypes.c_int, _dp, _dp]
+    ip = P(ctypes.c_int)
+    fp = P(ctypes.c_float)
+    L.grt_sweep_kmax.argtypes = [vp, P(Model), P(Opts), ctypes.c_int, ip, ctypes.c_int, _dp, ctypes.c_double,
+                                 _dp, _dp, _dp, _dp]
+    L.grt_mlp_create.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong, P(vp)]
+    L.grt_mlp_destroy.argtypes = [vp]
+    L.grt_mlp_destroy.restype = None
+    L.grt_mlp_n_params.argtypes = [vp]
+    L.grt_mlp_get_params.argtypes = [vp, fp]
+    L.grt_mlp_set_params.argtypes = [vp, fp]
+    L.grt_mlp_forward.argtypes = [vp, ctypes.c_int, fp, fp]
+    L.grt_mlp_loss_grad.argtypes = [vp, ctypes.c_int, fp, fp, fp, fp]
+    L.grt_mlp_train.argtypes = [vp, ctypes.c_int, fp, fp, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                ctypes.c_ulonglong, fp]
     _lib = L
     return L
 
@@ -142,9 +160,16 @@ def make_model(ztop, vp, vs, rho, qp, qs, hs, hr=0.0, src_type=0):
 
 
 def make_opts(dt, log2n, t0=0.0, taper=0.3, sigma_factor=2.0, k_mode=K_REFERENCE, nk_fixed=0, dk=0.0,
-              precision=FP32, fix=0):
-    return Opts(float(dt), int(log2n), float(t0), float(taper), float(sigma_factor), int(k_mode),
-                int(nk_fixed), float(dk), int(precision), int(fix))
+              precision=FP32, fix=0, nk_custom=None):
+    """nk_custom: points per frequency (N/2 ints) for K_CUSTOM grids."""
+    o = Opts(float(dt), int(log2n), float(t0), float(taper), float(sigma_factor), int(k_mode),
+             int(nk_fixed), float(dk), int(precision), int(fix), None)
+    if nk_custom is not None:
+        arr = np.ascontiguousarray(nk_custom, dtype=np.int32)
+        o.nk_custom = arr.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+        o._keep = arr
+        o.k_mode = K_CUSTOM
+    return o
 
 
 class Plan:
@@ -179,6 +204,15 @@ class Plan:
             s = s[..., 0] + 1j * s[..., 1]
         return t, s
 
+    def fetch_freqs(self, freq_idx):
+        """Spectra at selected frequency indices: complex [n_dist, n_cols, n_freq]."""
+        fi = np.ascontiguousarray(freq_idx, dtype=np.int32)
+        s = np.empty((len(self.dists), self.report.n_cols, len(fi), 2))
+        rc = lib().grt_plan_fetch_freqs(self.h, len(fi), fi.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _ptr(s))
+        if rc:
+            raise GrtError(rc, self.ctx.error())
+        return s[..., 0] + 1j * s[..., 1]
+
     def close(self):
         if self.h:
             lib().grt_plan_destroy(self.h)
@@ -189,6 +223,40 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+
+def grid(model, opts):
+    """Layer, frequency and wavenumber grid of a job (no device work)."""
+    r = Report()
+    rc = lib().grt_grid(ctypes.byref(model), ctypes.byref(opts), ctypes.byref(r))
+    if rc:
+        raise GrtError(rc, "grt_grid (details on stderr)")
+    return r.as_dict()
+
+
+def sweep_kmax(model, opts, freq_idx, band_r, tol, k_judge=None, ctx=None):
+    """Convergence sweep of the plain grid at selected frequencies and
+    distances (grt_sweep_kmax).  Returns (kmax, tail, dk), each
+    [n_freq, n_band]; tail is None without k_judge."""
+    fi = np.ascontiguousarray(freq_idx, dtype=np.int32)
+    br = _arr(np.atleast_1d(band_r))
+    shape = (len(fi), len(br))
+    kmax, dk = np.empty(shape), np.empty(shape)
+    tail = np.empty(shape) if k_judge is not None else None
+    kj = _arr(np.broadcast_to(k_judge, shape)) if k_judge is not None else None
+    own = ctx is None
+    ctx = ctx or Context()
+    try:
+        rc = lib().grt_sweep_kmax(ctx.h, ctypes.byref(model), ctypes.byref(opts), len(fi),
+                                  fi.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(br), _ptr(br), float(tol),
+                                  _ptr(kj) if kj is not None else None, _ptr(kmax),
+                                  _ptr(tail) if tail is not None else None, _ptr(dk))
+        if rc:
+            raise GrtError(rc, ctx.error())
+    finally:
+        if own:
+            ctx.close()
+    return kmax, tail, dk
 
 
 def run(model, opts, dists, ctx=None, spectra=False):

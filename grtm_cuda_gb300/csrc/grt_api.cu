@@ -16,18 +16,14 @@
 #include "grt_integrate.cuh"
 #include "grt_job.h"
 #include "grt_kernel.cuh"
+#include "grt_tables.h"
 #include "grt_ksum_tc.cuh"
 
 using grt::Job;
 using cd = std::complex<double>;
 static const double PI = 3.1415926535897932384626433;
 
-struct grt_ctx {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    cudaEvent_t ev[6] = {};
-    std::string err;
-};
+#include "grt_ctx.h"
 
 struct grt_plan {
     grt_ctx *ctx = nullptr;
@@ -126,30 +122,7 @@ static void build_tables(const Job &J, std::vector<grt::LayerW<R>> &tab, std::ve
 {
     const int L = J.L, nw = J.nw, N = J.N;
     tab.resize((size_t)nw * L);
-    for (int iw = 0; iw < nw; iw++) {
-        cd w(2 * PI * J.df * iw, -J.sigma);
-        cd lw = std::log(w / (2 * PI));
-        for (int i = 0; i < L; i++) {
-            // attenuation, green.cu:177-180
-            cd cs = 1.0 + lw / (PI * J.qs[i]) + cd(0, 1) / (2.0 * J.qs[i]);
-            cd cp = 1.0 + lw / (PI * J.qp[i]) + cd(0, 1) / (2.0 * J.qp[i]);
-            cd a = J.a0[i] * cp, b = J.b0[i] * cs;
-            cd wa = w / a, wb = w / b;
-            cd wa2 = wa * wa, wb2 = wb * wb, W = wb2 - wa2, iW = 1.0 / W;
-            grt::LayerW<R> &t = tab[(size_t)iw * L + i];
-            t.wa2x = wa2.real(); t.wa2y = wa2.imag(); t.wb2x = wb2.real(); t.wb2y = wb2.imag();
-            t.wa2[0] = (R)wa2.real(); t.wa2[1] = (R)wa2.imag();
-            t.wb2[0] = (R)wb2.real(); t.wb2[1] = (R)wb2.imag();
-            t.W[0] = (R)W.real(); t.W[1] = (R)W.imag();
-            t.iW[0] = (R)iW.real(); t.iW[1] = (R)iW.imag();
-            t.a[0] = (R)a.real(); t.a[1] = (R)a.imag();
-            t.b[0] = (R)b.real(); t.b[1] = (R)b.imag();
-            t.mu = (R)J.mu[i];
-            t.h = (R)J.h[i];
-            t.wa2lo = (float)(wa2.real() - (double)(float)wa2.real());
-            t.wb2lo = (float)(wb2.real() - (double)(float)wb2.real());
-        }
-    }
+    grt::fill_layer_table<R>(J, tab.data());
     // phase e^{i w_r t0}, cosine taper and scale df nw / pi (green.cu:1905-1921)
     post.resize(2 * (size_t)nw);
     const int wc = (int)((double)nw * (1 - J.taper));
@@ -280,7 +253,7 @@ extern "C" int grt_plan_create(grt_ctx *ctx, const grt_model *m, const grt_opts 
                                   p->J, err);
     if (!rc)
         rc = grt::job_setup(p->J, o->dt, o->log2n, o->t0, o->taper, o->sigma_factor, o->k_mode, o->nk_fixed, o->dk,
-                            o->fix, err);
+                            o->fix, err, o->nk_custom);
     if (rc) return set_err(ctx, rc, err);
     const Job &J = p->J;
     p->prec = o->precision;
@@ -463,6 +436,37 @@ extern "C" int grt_plan_info(const grt_plan *p, grt_report *r)
     return GRT_OK;
 }
 
+extern "C" int grt_grid(const grt_model *m, const grt_opts *o, grt_report *r)
+{
+    if (!m || !o || !r) return GRT_ERR_ARG;
+    Job J;
+    std::string err;
+    int rc = grt::job_from_layers(m->n_layer, m->ztop, m->vp, m->vs, m->rho, m->qp, m->qs, m->hs, m->hr, m->src_type,
+                                  J, err);
+    if (!rc)
+        rc = grt::job_setup(J, o->dt, o->log2n, o->t0, o->taper, o->sigma_factor, o->k_mode, o->nk_fixed, o->dk,
+                            o->fix, err, o->nk_custom);
+    if (rc) {
+        fprintf(stderr, "grt_grid: %s\n", err.c_str());
+        return rc;
+    }
+    *r = grt_report{};
+    r->n_layer = J.L;
+    r->s_layer = J.s;
+    r->r_layer = J.rl;
+    r->zs = J.zs;
+    r->zr = J.zr;
+    r->nw = J.nw;
+    r->n_samples = J.N;
+    r->n_cols = J.src == 0 ? grt::kSingleNC : grt::kTensorNC;
+    r->n_wk = J.nkw;
+    r->nk_max = J.nkmax;
+    r->dk = J.dk;
+    r->df = J.df;
+    r->sigma = J.sigma;
+    return GRT_OK;
+}
+
 extern "C" int grt_plan_execute(grt_plan *p, grt_report *r)
 {
     if (!p) return GRT_ERR_ARG;
@@ -495,12 +499,214 @@ static int fetch(grt_plan *p, double *traces, double *spectra)
     return GRT_OK;
 }
 
+template <typename R>
+static int fetch_freqs(grt_plan *p, int n_freq, const int *freq_idx, double *spectra)
+{
+    grt_ctx *ctx = p->ctx;
+    const size_t rows = (size_t)p->nd * p->nc;
+    std::vector<grt::C<R>> h(rows * n_freq);
+    // one strided copy per frequency: element iw of every (receiver, column) row
+    for (int f = 0; f < n_freq; f++)
+        CU(cudaMemcpy2DAsync(h.data() + f * rows, sizeof(grt::C<R>), (const grt::C<R> *)p->spec + freq_idx[f],
+                             (size_t)p->J.N * sizeof(grt::C<R>), sizeof(grt::C<R>), rows, cudaMemcpyDeviceToHost,
+                             ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    for (size_t r = 0; r < rows; r++)
+        for (int f = 0; f < n_freq; f++) {
+            spectra[2 * (r * n_freq + f)] = (double)h[f * rows + r].x;
+            spectra[2 * (r * n_freq + f) + 1] = (double)h[f * rows + r].y;
+        }
+    return GRT_OK;
+}
+
+extern "C" int grt_plan_fetch_freqs(grt_plan *p, int n_freq, const int *freq_idx, double *spectra)
+{
+    if (!p || n_freq < 1 || !freq_idx || !spectra) return GRT_ERR_ARG;
+    grt_ctx *ctx = p->ctx;
+    for (int f = 0; f < n_freq; f++)
+        if (freq_idx[f] < 0 || freq_idx[f] >= p->J.N) return set_err(ctx, GRT_ERR_ARG, "frequency index out of range");
+    CU(cudaSetDevice(ctx->device));
+    return p->prec ? fetch_freqs<double>(p, n_freq, freq_idx, spectra) : fetch_freqs<float>(p, n_freq, freq_idx, spectra);
+}
+
 extern "C" int grt_plan_fetch(grt_plan *p, double *traces, double *spectra)
 {
     if (!p) return GRT_ERR_ARG;
     grt_ctx *ctx = p->ctx;
     CU(cudaSetDevice(ctx->device));
     return p->prec ? fetch<double>(p, traces, spectra) : fetch<float>(p, traces, spectra);
+}
+
+// ------------------------------------------------------------------ convergence sweep
+// One thread per (selected frequency, distance band): envelope of the weighted
+// integrand g(k) = max_q |K_q(w,k)| (1+k)^2 min(1, (k r)^-1/2), its total, and
+// the smallest k_c whose tail sum_{k >= k_c} g stays within tol of the total;
+// also the tail fraction at a given wavenumber (a prediction to judge), and
+// the coarsest step dk*s (s = 1, 2, 4, .., 32) whose sums
+// s dk sum_{j = 0 mod s} K_q(j dk) J0(j dk r) agree with the full-grid sums
+// within tol for every column q (the step's spatial aliasing at distance r).
+constexpr int kStrides = 6;
+
+__global__ void sweep_kmax_kernel(const float *K, long long nkw, int nq, const int *nk, const long long *koff,
+                                  const int *fidx, int nf, const double *band_r, int nb, double dk, double tol,
+                                  const double *kjudge, double *kmax_out, double *tail_out, double *dk_out)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nf * nb) return;
+    const int f = t / nb, b = t % nb, iw = fidx[f];
+    const int n = nk[iw];
+    const long long off = koff[iw];
+    const double r = band_r[b];
+    const grt::C<float> *Kc = reinterpret_cast<const grt::C<float> *>(K);
+    auto g = [&](int j) {
+        float m = 0.f;
+        for (int q = 0; q < nq; q++) {
+            const grt::C<float> v = Kc[(long long)q * nkw + off + j];
+            m = fmaxf(m, sqrtf(v.x * v.x + v.y * v.y));
+        }
+        const double k = dk * j, kr = k * r;
+        return (double)m * (1.0 + k) * (1.0 + k) * (kr > 1.0 ? 1.0 / sqrt(kr) : 1.0);
+    };
+    double tot = 0.0;
+    for (int j = 0; j < n; j++) tot += g(j);
+    double tail = 0.0, tail_at = 0.0;
+    int jc = 0;
+    const int jj = kjudge ? (int)ceil(kjudge[t] / dk) : n;
+    bool found = false;
+    for (int j = n - 1; j >= 0; j--) {
+        tail += g(j);
+        if (j == jj) tail_at = tail;
+        if (!found && tail > tol * tot) {
+            jc = j + 1;
+            found = true;
+        }
+    }
+    kmax_out[t] = dk * (found ? jc : 0);
+    if (tail_out) tail_out[t] = (tot > 0 && jj < n) ? tail_at / tot : 0.0;
+    if (!dk_out) return;
+    // stride test; sums run over the grid up to k_c (the part a sampler keeps)
+    const int ne = found ? jc : n;
+    double emax[kStrides] = {}, ref = 0.0;
+    for (int q = 0; q < nq; q++) {
+        double sx[kStrides] = {}, sy[kStrides] = {};
+        for (int j = 0; j < ne; j++) {
+            const grt::C<float> v = Kc[(long long)q * nkw + off + j];
+            const double w = (j == 0 ? 0.5 : 1.0) * grt::bj0_ref(dk * j * r);
+            const double x = w * v.x, y = w * v.y;
+#pragma unroll
+            for (int s = 0; s < kStrides; s++)
+                if ((j & ((1 << s) - 1)) == 0) {
+                    sx[s] += x * (1 << s);
+                    sy[s] += y * (1 << s);
+                }
+        }
+        ref = fmax(ref, hypot(sx[0], sy[0]));
+        for (int s = 1; s < kStrides; s++) emax[s] = fmax(emax[s], hypot(sx[s] - sx[0], sy[s] - sy[0]));
+    }
+    int sbest = 0;
+    for (int s = 1; s < kStrides && emax[s] <= tol * ref && (ne >> s) >= 8; s++) sbest = s;
+    dk_out[t] = dk * (1 << sbest);
+}
+
+extern "C" int grt_sweep_kmax(grt_ctx *ctx, const grt_model *m, const grt_opts *o, int n_freq, const int *freq_idx,
+                              int n_band, const double *band_r, double tol, const double *k_judge, double *kmax_out,
+                              double *tail_out, double *dk_out)
+{
+    if (!ctx || !m || !o || !freq_idx || !band_r || !kmax_out || n_freq < 1 || n_band < 1 || !(tol > 0))
+        return set_err(ctx, GRT_ERR_ARG, "bad sweep arguments");
+    Job J;
+    std::string err;
+    int rc = grt::job_from_layers(m->n_layer, m->ztop, m->vp, m->vs, m->rho, m->qp, m->qs, m->hs, m->hr, m->src_type,
+                                  J, err);
+    if (!rc)
+        rc = grt::job_setup(J, o->dt, o->log2n, o->t0, o->taper, o->sigma_factor, o->k_mode, o->nk_fixed, o->dk,
+                            o->fix, err, o->nk_custom);
+    if (rc) return set_err(ctx, rc, err);
+    // keep only the selected frequencies: compact coefficient offsets, tiles for them alone
+    std::vector<int> nk_sel(J.nw, 0);
+    std::vector<long long> koff(J.nw, 0);
+    long long tot = 0;
+    std::vector<int2> tiles;
+    for (int f = 0; f < n_freq; f++) {
+        const int iw = freq_idx[f];
+        if (iw < 0 || iw >= J.nw) return set_err(ctx, GRT_ERR_ARG, "frequency index out of range");
+        if (nk_sel[iw]) return set_err(ctx, GRT_ERR_ARG, "repeated frequency index");
+        nk_sel[iw] = J.nk[iw];
+        koff[iw] = tot;
+        tot += J.nk[iw];
+        for (int j0 = 0; j0 < J.nk[iw]; j0 += grt::kGrtThreads) tiles.push_back(make_int2(iw, j0));
+    }
+    const int nq = J.src == 0 ? (int)grt::QS_N : (int)grt::QT_N;
+    std::vector<grt::LayerW<float>> tab;
+    std::vector<float> post, tw;
+    std::vector<double> damp;
+    build_tables<float>(J, tab, post, tw, damp);
+    struct Bufs {
+        std::vector<void *> v;
+        ~Bufs() { for (void *p : v) cudaFree(p); }
+    } bufs;
+    auto dalloc = [&](size_t n) -> void * {
+        void *p = nullptr;
+        if (cudaMalloc(&p, n) != cudaSuccess) return nullptr;
+        bufs.v.push_back(p);
+        return p;
+    };
+    CU(cudaSetDevice(ctx->device));
+    void *d_tab = dalloc(tab.size() * sizeof(tab[0])), *d_tiles = dalloc(tiles.size() * sizeof(int2));
+    void *d_nk = dalloc(J.nw * sizeof(int)), *d_koff = dalloc(J.nw * sizeof(long long));
+    void *d_K = dalloc((size_t)nq * tot * 2 * sizeof(float)), *d_err = dalloc(sizeof(unsigned));
+    void *d_f = dalloc(n_freq * sizeof(int)), *d_r = dalloc(n_band * sizeof(double));
+    void *d_out = dalloc((size_t)n_freq * n_band * 3 * sizeof(double));
+    void *d_judge = k_judge ? dalloc((size_t)n_freq * n_band * sizeof(double)) : nullptr;
+    if (!d_tab || !d_tiles || !d_nk || !d_koff || !d_K || !d_err || !d_f || !d_r || !d_out || (k_judge && !d_judge))
+        return set_err(ctx, GRT_ERR_NOMEM, "sweep buffers");
+    cudaStream_t st = ctx->stream;
+    CU(cudaMemcpyAsync(d_tab, tab.data(), tab.size() * sizeof(tab[0]), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(d_tiles, tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(d_nk, nk_sel.data(), J.nw * sizeof(int), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(d_koff, koff.data(), J.nw * sizeof(long long), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(d_f, freq_idx, n_freq * sizeof(int), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(d_r, band_r, n_band * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (k_judge) CU(cudaMemcpyAsync(d_judge, k_judge, (size_t)n_freq * n_band * sizeof(double), cudaMemcpyHostToDevice, st));
+    CU(cudaMemsetAsync(d_err, 0, sizeof(unsigned), st));
+    grt::GrtArgs<float> A{};
+    A.tab = (const grt::LayerW<float> *)d_tab;
+    A.tiles = (const int2 *)d_tiles;
+    A.nk = (const int *)d_nk;
+    A.koff = (const long long *)d_koff;
+    A.K = (float *)d_K;
+    A.nkw = tot;
+    A.dk = J.dk;
+    A.zs = J.zs;
+    A.zr = J.zr;
+    A.hs_layer = J.h[J.s];
+    A.hr_layer = J.h[J.rl];
+    A.L = J.L; A.s = J.s; A.rl = J.rl; A.src = J.src; A.fix = J.fix; A.nq = nq;
+    {
+        const auto &t = tab[J.rl];
+        cd r0 = std::sqrt(cd(-t.wa2x, -t.wa2y)), v0 = std::sqrt(cd(-t.wb2x, -t.wb2y));
+        if (r0.real() < 0) r0 = -r0;
+        if (v0.real() < 0) v0 = -v0;
+        A.slot0[0] = (float)r0.real(); A.slot0[1] = (float)r0.imag(); A.slot0[2] = (float)v0.real(); A.slot0[3] = (float)v0.imag();
+    }
+    A.err = (unsigned *)d_err;
+    grt::grt_point_kernel<float><<<(unsigned)tiles.size(), grt::kGrtThreads, (size_t)J.L * sizeof(grt::LayerW<float>), st>>>(A);
+    CU(cudaGetLastError());
+    const int nt = n_freq * n_band;
+    double *o_k = (double *)d_out, *o_t = (double *)d_out + nt, *o_d = dk_out ? (double *)d_out + 2 * nt : nullptr;
+    sweep_kmax_kernel<<<(nt + 127) / 128, 128, 0, st>>>((const float *)d_K, tot, nq, (const int *)d_nk,
+                                                        (const long long *)d_koff, (const int *)d_f, n_freq,
+                                                        (const double *)d_r, n_band, J.dk, tol,
+                                                        (const double *)d_judge, o_k, o_t, o_d);
+    CU(cudaGetLastError());
+    CU(cudaMemcpyAsync(kmax_out, o_k, nt * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (tail_out) CU(cudaMemcpyAsync(tail_out, o_t, nt * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (dk_out) CU(cudaMemcpyAsync(dk_out, o_d, nt * sizeof(double), cudaMemcpyDeviceToHost, st));
+    unsigned herr = 0;
+    CU(cudaMemcpyAsync(&herr, d_err, sizeof herr, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    if (herr) return set_err(ctx, GRT_ERR_TIMEOUT, "a bounded device wait gave up (layer-table copy)");
+    return GRT_OK;
 }
 
 extern "C" int grt_run(grt_ctx *ctx, const grt_model *m, const grt_opts *o, int n_dist, const double *dist,

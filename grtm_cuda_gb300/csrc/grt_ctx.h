@@ -1,0 +1,13 @@
+// grt_ctx.h -- the context object behind grt_ctx* (shared by the library's
+// translation units).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+
+struct grt_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[6] = {};
+    std::string err;
+};

@@ -119,8 +119,10 @@ static double cal_kmax(const Job &J, cd w, const std::vector<cd> &b, int nf)
 }
 
 int job_setup(Job &J, double dt, int log2n, double t0, double taper, double sigma_factor, int k_mode,
-              int nk_fixed, double dk_override, int fix, std::string &err)
+              int nk_fixed, double dk_override, int fix, std::string &err, const int *nk_custom)
 {
+    if (k_mode == 2 && !nk_custom) { err = "custom k grid needs nk_custom"; return kErrArg; }
+    if (k_mode < 0 || k_mode > 2) { err = "unknown k grid mode"; return kErrArg; }
     if (!(dt > 0) || log2n < 2 || log2n > 15) { err = "need dt > 0 and 2 <= log2n <= 15"; return kErrArg; }
     if (!(taper >= 0 && taper <= 1)) { err = "taper must be in [0, 1]"; return kErrArg; }
     if (!(sigma_factor > 0)) { err = "sigma_factor must be > 0"; return kErrArg; }
@@ -162,7 +164,10 @@ int job_setup(Job &J, double dt, int log2n, double t0, double taper, double sigm
     std::vector<cd> b(J.L);
     for (int iw = 0; iw < J.nw; iw++) {
         int nk;
-        if (k_mode == 1) {
+        if (k_mode == 2) {
+            nk = nk_custom[iw];
+            if (nk < 2 || nk > (1 << 24)) { err = "custom k grid: need 2 <= nk <= 2^24 at every frequency"; return kErrArg; }
+        } else if (k_mode == 1) {
             nk = nk_fixed;
         } else {
             cd w(2 * PI * J.df * iw, -J.sigma);

@@ -48,6 +48,6 @@ int job_from_layers(int n, const double *ztop, const double *vp, const double *v
                     std::string &err);
 // Grid, layer location and k grid.  sigma = sigma_factor / T (reference: 2).
 int job_setup(Job &J, double dt, int log2n, double t0, double taper, double sigma_factor, int k_mode,
-              int nk_fixed, double dk_override, int fix, std::string &err);
+              int nk_fixed, double dk_override, int fix, std::string &err, const int *nk_custom = nullptr);
 
 }  // namespace grt

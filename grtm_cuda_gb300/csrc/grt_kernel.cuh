@@ -31,6 +31,7 @@ namespace grt {
 template <typename R>
 struct SL {
     C<R> r, v, rmv, irmv;       // vertical wavenumbers, r - v, 1/(r - v)
+    C<R> rlo, vlo;              // FP32 kernel: low words of r and v (double-float); FP64: zero
     C<R> p1, p2, p3;            // p0 = k
     C<R> d0, d1, d2, d3;
     C<R> detG, detH;
@@ -60,13 +61,98 @@ __device__ __forceinline__ float re_minus(const K2<float> &k2, float c, double, 
     return (c * k2.hi - w2hi) + (c * k2.lo - w2lo);
 }
 
+// ---------------------------------------------------------------- double-float
+// Error-free transformations (Knuth's two-sum, FMA two-product).  The FP32
+// kernel uses them where a rounding error would be multiplied by a large
+// factor: the vertical wavenumbers r, v enter the layer phases e^{-r h} as
+// r h, which reaches hundreds of radians at high frequency in thick stacks,
+// so an FP32 rounding of r (relative 6e-8, different at every k) becomes a
+// phase noise of ~1e-5 that the oscillatory wavenumber sum at large distance
+// does not average out.  r, v and the exponents r h, v h are therefore
+// carried as hi + lo pairs (about 44 bits); the R/T algebra stays FP32.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+{
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ void two_prod(float a, float b, float &p, float &e)
+{
+    p = __fmul_rn(a, b);
+    e = fmaf(a, b, -p);
+}
+// k^2 - w2 with w2 = w2hi + w2lo, as hi + lo
+__device__ __forceinline__ void df_minus(const K2<float> &k2, float w2hi, float w2lo, float &hi, float &lo)
+{
+    float s, e;
+    two_sum(k2.hi, -w2hi, s, e);
+    e = __fadd_rn(e, __fsub_rn(k2.lo, w2lo));
+    two_sum(s, e, hi, lo);
+}
+// low word of sqrt(z + zlo) given r0 = fl(sqrt(z)): one Newton step
+// (z + zlo - r0^2) / (2 r0), with r0^2 formed exactly so the residual keeps
+// its digits
+__device__ __forceinline__ C<float> sqrt_lo(C<float> z, C<float> zlo, C<float> r0)
+{
+    if (r0.x == 0.f && r0.y == 0.f) return {0.f, 0.f};
+    float ah, al, bh, bl, ch, cl, th, tl;
+    two_prod(r0.x, r0.x, ah, al);
+    two_prod(r0.y, r0.y, bh, bl);
+    two_prod(r0.x, r0.y, ch, cl);
+    two_sum(ah, -bh, th, tl);
+    const C<float> d = {__fsub_rn(z.x, th) + (((zlo.x - tl) - al) + bl),
+                        __fsub_rn(z.y, 2.f * ch) + (zlo.y - 2.f * cl)};
+    return d * rcp(r0) * 0.5f;
+}
+
+// a depth or thickness as hi + lo (lo = 0 in the FP64 kernel)
+template <typename R> struct Zd { R hi, lo; };
+template <typename R> __device__ __forceinline__ Zd<R> zd(double d)
+{
+    Zd<R> o;
+    o.hi = (R)d;
+    o.lo = (R)(d - (double)o.hi);
+    return o;
+}
+
+// e^{-(nu + nulo)(z + zlo)}, the exponent formed in double-float
+template <typename R>
+__device__ __forceinline__ C<R> exp_nz(C<R> nu, C<R> nulo, Zd<R> z)
+{
+    if constexpr (sizeof(R) == 4) {
+        float px, ex, py, ey;
+        two_prod(nu.x, z.hi, px, ex);
+        two_prod(nu.y, z.hi, py, ey);
+        const C<float> lo = {ex + nulo.x * z.hi + nu.x * z.lo, ey + nulo.y * z.hi + nu.y * z.lo};
+        const C<float> e = cexp_(C<float>{-px, -py});
+        return e - e * lo;   // e^{hi} (1 - lo), |lo| < 1e-4
+    } else {
+        return cexp_(nu * (-z.hi));
+    }
+}
+
 template <typename R>
 __device__ __forceinline__ void make_layer(const LayerW<R> &T, const K2<R> &k2, R k, SL<R> &L)
 {
-    C<R> zr = {re_minus(k2, R(1), T.wa2x, (float)T.wa2[0], T.wa2lo), -T.wa2[1]};
-    C<R> zv = {re_minus(k2, R(1), T.wb2x, (float)T.wb2[0], T.wb2lo), -T.wb2[1]};
-    L.r = csqrt_(zr);
-    L.v = csqrt_(zv);
+    if constexpr (sizeof(R) == 4) {
+        C<R> zr, zrl, zv, zvl;
+        df_minus(k2, T.wa2[0], T.wa2lo, zr.x, zrl.x);
+        df_minus(k2, T.wb2[0], T.wb2lo, zv.x, zvl.x);
+        zr.y = -T.wa2[1];
+        zrl.y = -T.wa2ylo;
+        zv.y = -T.wb2[1];
+        zvl.y = -T.wb2ylo;
+        L.r = csqrt_(zr);
+        L.v = csqrt_(zv);
+        L.rlo = sqrt_lo(zr, zrl, L.r);
+        L.vlo = sqrt_lo(zv, zvl, L.v);
+    } else {
+        C<R> zr = {re_minus(k2, R(1), T.wa2x, 0.f, 0.f), -T.wa2[1]};
+        C<R> zv = {re_minus(k2, R(1), T.wb2x, 0.f, 0.f), -T.wb2[1]};
+        L.r = csqrt_(zr);
+        L.v = csqrt_(zv);
+        L.rlo = L.vlo = C<R>{R(0), R(0)};
+    }
     L.x = C<R>{re_minus(k2, R(2), T.wb2x, (float)T.wb2[0], T.wb2lo), -T.wb2[1]};  // k^2 + v^2 = 2k^2 - wb^2
     const C<R> wa2 = {T.wa2[0], T.wa2[1]}, wb2 = {T.wb2[0], T.wb2[1]};
     const C<R> W = {T.W[0], T.W[1]}, iW = {T.iW[0], T.iW[1]};
@@ -91,9 +177,10 @@ __device__ __forceinline__ void make_layer(const LayerW<R> &T, const K2<R> &k2, 
 
 // S^-1 diag(e^{-rz}, e^{-vz}) S  (upper triangular)
 template <typename R>
-__device__ __forceinline__ M2<R> phase(const SL<R> &L, R z, C<R> *ev_out = nullptr)
+__device__ __forceinline__ M2<R> phase(const SL<R> &L, Zd<R> zz, C<R> *ev_out = nullptr)
 {
-    C<R> er = cexp_(L.r * (-z)), ev = cexp_(L.v * (-z));
+    const R z = zz.hi;
+    C<R> er = exp_nz(L.r, L.rlo, zz), ev = exp_nz(L.v, L.vlo, zz);
     C<R> y = L.rmv * (-z);
     C<R> dd;
     if (abs2(y) < R(0.25)) dd = ev * expm1_over_small(y) * (-z);
@@ -104,9 +191,10 @@ __device__ __forceinline__ M2<R> phase(const SL<R> &L, R z, C<R> *ev_out = nullp
 
 // S^-1 diag(sg r0 e^{-rz}, sg v0 e^{-vz}) S; r0, v0 = own nu unless given
 template <typename R>
-__device__ __forceinline__ M2<R> dphase(const SL<R> &L, R z, R sg, const C<R> *nu0)
+__device__ __forceinline__ M2<R> dphase(const SL<R> &L, Zd<R> zz, R sg, const C<R> *nu0)
 {
-    C<R> er = cexp_(L.r * (-z)), ev = cexp_(L.v * (-z));
+    const R z = zz.hi;
+    C<R> er = exp_nz(L.r, L.rlo, zz), ev = exp_nz(L.v, L.vlo, zz);
     C<R> y = L.rmv * (-z);
     C<R> dd;
     if (abs2(y) < R(0.25)) dd = ev * expm1_over_small(y) * (-z);
@@ -262,6 +350,7 @@ __global__ void __launch_bounds__(kGrtThreads, GRT_POINT_MINB) grt_point_kernel(
     const C<R> slot0[2] = {{A.slot0[0], A.slot0[1]}, {A.slot0[2], A.slot0[3]}};
     const C<R> *nu0 = (A.fix & kFixRexut) ? nullptr : slot0;
     const R zr = (R)A.zr;
+    const Zd<R> Zr = zd<R>(A.zr), Zhr = zd<R>(A.hr_layer), Zhr_r = zd<R>(A.hr_layer - A.zr);
 
     for (int jf = L - 2; jf >= s; jf--) {
         make_layer(T[jf], k2, k, U);
@@ -276,7 +365,7 @@ __global__ void __launch_bounds__(kGrtThreads, GRT_POINT_MINB) grt_point_kernel(
             td0n = m.tdd0;
         } else {
             C<R> ev;
-            M2<R> Lam = phase(D, T[jf + 1].h, &ev);
+            M2<R> Lam = phase(D, Zd<R>{T[jf + 1].h, (R)T[jf + 1].hlo}, &ev);
             // SH, green.cu:537-548
             C<R> tem1 = (-m.rdu0) * ev, tem2 = rdu0 * ev, tem3 = m.tuu0 * ev;
             td0n = m.tdd0 * rcp(R(1) - tem1 * tem2);
@@ -299,10 +388,10 @@ __global__ void __launch_bounds__(kGrtThreads, GRT_POINT_MINB) grt_point_kernel(
         if (rl > s && jf == rl) {
             // receiver below the source, inside layer rl (corrected form)
             C<R> exv, ldv, luv;
-            M2<R> Ld = phase(U, zr, &ldv), Lu = phase(U, (R)A.hr_layer - zr, &luv);
-            M2<R> Ldt = dphase(U, zr, R(-1), (const C<R> *)nullptr);
-            M2<R> Lut = dphase(U, (R)A.hr_layer - zr, R(1), nu0);
-            M2<R> Ex = phase(U, (R)A.hr_layer, &exv);
+            M2<R> Ld = phase(U, Zr, &ldv), Lu = phase(U, Zhr_r, &luv);
+            M2<R> Ldt = dphase(U, Zr, R(-1), (const C<R> *)nullptr);
+            M2<R> Lut = dphase(U, Zhr_r, R(1), nu0);
+            M2<R> Ex = phase(U, Zhr, &exv);
             M2<R> Ed = {{k, R(0)}, U.d0, U.p1, U.d1}, Eu = {{k, R(0)}, U.d0, -U.p1, -U.d1};
             M2<R> RE = Rdu * Ex;
             Urec = Ed * Ld + Eu * ut_mul_left(Lu, RE);
@@ -316,8 +405,8 @@ __global__ void __launch_bounds__(kGrtThreads, GRT_POINT_MINB) grt_point_kernel(
         // receiver in the half-space: only the down-going field
         make_layer(T[L - 1], k2, k, U);
         C<R> ldv;
-        M2<R> Ld = phase(U, zr, &ldv);
-        M2<R> Ldt = dphase(U, zr, R(-1), (const C<R> *)nullptr);
+        M2<R> Ld = phase(U, Zr, &ldv);
+        M2<R> Ldt = dphase(U, Zr, R(-1), (const C<R> *)nullptr);
         M2<R> Ed = {{k, R(0)}, U.d0, U.p1, U.d1};
         Urec = Ed * Ld;
         Utrec = Ed * Ldt;
@@ -352,10 +441,10 @@ __global__ void __launch_bounds__(kGrtThreads, GRT_POINT_MINB) grt_point_kernel(
             C<R> exv, ldv, luv = zero;
             const bool last = false;
             (void)last;
-            M2<R> Ld = phase(U, zr, &ldv), Lu = phase(U, (R)A.hr_layer - zr, &luv);
-            M2<R> Ldt = dphase(U, zr, R(-1), (const C<R> *)nullptr);
-            M2<R> Lut = dphase(U, (R)A.hr_layer - zr, R(1), nu0);
-            M2<R> Ex = phase(U, (R)A.hr_layer, &exv);
+            M2<R> Ld = phase(U, Zr, &ldv), Lu = phase(U, Zhr_r, &luv);
+            M2<R> Ldt = dphase(U, Zr, R(-1), (const C<R> *)nullptr);
+            M2<R> Lut = dphase(U, Zhr_r, R(1), nu0);
+            M2<R> Ex = phase(U, Zhr, &exv);
             M2<R> Ed = {{k, R(0)}, U.d0, U.p1, U.d1}, Eu = {{k, R(0)}, U.d0, -U.p1, -U.d1};
             M2<R> RE = Rud * Ex;
             Urec = Ed * ut_mul_left(Ld, RE) + Eu * Lu;
@@ -367,7 +456,7 @@ __global__ void __launch_bounds__(kGrtThreads, GRT_POINT_MINB) grt_point_kernel(
         IF<R> m;
         interface_rt(U, D, k, m);
         C<R> ev;
-        M2<R> Lam = phase(U, T[jf].h, &ev);
+        M2<R> Lam = phase(U, Zd<R>{T[jf].h, (R)T[jf].hlo}, &ev);
         // SH, green.cu:476-482
         C<R> tem1 = rud0 * ev, tem2 = m.rdu0 * ev, tem3 = m.tdd0 * ev;
         C<R> tu0n = m.tuu0 * rcp(R(1) - tem1 * tem2);
@@ -394,10 +483,13 @@ __global__ void __launch_bounds__(kGrtThreads, GRT_POINT_MINB) grt_point_kernel(
     const C<R> RU0 = rud0;
     const SL<R> &S = U;
     const R zs = (R)A.zs, hs = (R)A.hs_layer;
+    const Zd<R> Zs = zd<R>(A.zs), Zhs_s = zd<R>(A.hs_layer - A.zs), Zs_r = zd<R>(A.zs - A.zr),
+                Zr_s = zd<R>(A.zr - A.zs), Zhs_r = zd<R>(A.hs_layer - A.zr);
+    (void)hs;
 
     // ---------------- source terms (get_src_single / _tensor, green.cu:1271-1413)
     C<R> sexd1, sexu1;
-    M2<R> Ldn = phase(S, hs - zs, &sexd1), Lup = phase(S, zs, &sexu1);
+    M2<R> Ldn = phase(S, Zhs_s, &sexd1), Lup = phase(S, Zs, &sexu1);
     M2<R> ED = ut_mul_right(ut_mul_left(Ldn, RD), Ldn);
     M2<R> EU = ut_mul_right(ut_mul_left(Lup, RU), Lup);
     const bool up = (rl < s) || (rl == s && A.zr <= A.zs);
@@ -422,9 +514,9 @@ __global__ void __launch_bounds__(kGrtThreads, GRT_POINT_MINB) grt_point_kernel(
         const SL<R> &Rv = S;
         if (A.zr <= A.zs) {
             C<R> e1v, e2v;
-            M2<R> L1 = phase(Rv, zr, &e1v), L2 = phase(Rv, zs - zr, &e2v);
-            M2<R> L1t = dphase(Rv, zr, R(-1), (const C<R> *)nullptr);
-            M2<R> L2t = dphase(Rv, zs - zr, R(1), (const C<R> *)nullptr);
+            M2<R> L1 = phase(Rv, Zr, &e1v), L2 = phase(Rv, Zs_r, &e2v);
+            M2<R> L1t = dphase(Rv, Zr, R(-1), (const C<R> *)nullptr);
+            M2<R> L2t = dphase(Rv, Zs_r, R(1), (const C<R> *)nullptr);
             M2<R> Ed = {{k, R(0)}, Rv.d0, Rv.p1, Rv.d1}, Eu = {{k, R(0)}, Rv.d0, -Rv.p1, -Rv.d1};
             M2<R> RL = ut_mul_right(RU, Lup);
             Urec = Ed * ut_mul_left(L1, RL) + Eu * L2;
@@ -434,9 +526,9 @@ __global__ void __launch_bounds__(kGrtThreads, GRT_POINT_MINB) grt_point_kernel(
             u0t = -(Rv.v * e1v * RU0 * sexu1) + ((A.fix & kFixDz) ? Rv.v * e2v : Rv.v * e2v * Rv.v);
         } else {
             C<R> e1v, e2v;
-            M2<R> L1 = phase(Rv, zr - zs, &e1v), L2 = phase(Rv, hs - zr, &e2v);
-            M2<R> L1t = dphase(Rv, zr - zs, R(-1), (const C<R> *)nullptr);
-            M2<R> L2t = dphase(Rv, hs - zr, R(1), (const C<R> *)nullptr);
+            M2<R> L1 = phase(Rv, Zr_s, &e1v), L2 = phase(Rv, Zhs_r, &e2v);
+            M2<R> L1t = dphase(Rv, Zr_s, R(-1), (const C<R> *)nullptr);
+            M2<R> L2t = dphase(Rv, Zhs_r, R(1), (const C<R> *)nullptr);
             M2<R> Ed = {{k, R(0)}, Rv.d0, Rv.p1, Rv.d1}, Eu = {{k, R(0)}, Rv.d0, -Rv.p1, -Rv.d1};
             M2<R> RL = ut_mul_right(RD, Ldn);
             Urec = Ed * L1 + Eu * ut_mul_left(L2, RL);

@@ -32,6 +32,7 @@
 #include "grt_integrate.cuh"
 #include "grt_job.h"
 #include "grt_kernel.cuh"
+#include "grt_tables.h"
 
 namespace {
 
@@ -127,30 +128,7 @@ extern "C" GRT_API int grt_run_noalloc(int device, const grt_model *m, const grt
     // phase/taper/scale 1905-1921, de-damping 2236-2237)
     unsigned char *h = g_grt_stage;
     LW *tab = (LW *)(h + o_tab);
-    for (int iw = 0; iw < nw; iw++) {
-        cd w(2 * PI * J.df * iw, -J.sigma);
-        cd lw = std::log(w / (2 * PI));
-        for (int i = 0; i < L; i++) {
-            cd cs = 1.0 + lw / (PI * J.qs[i]) + cd(0, 1) / (2.0 * J.qs[i]);
-            cd cp = 1.0 + lw / (PI * J.qp[i]) + cd(0, 1) / (2.0 * J.qp[i]);
-            cd a = J.a0[i] * cp, b = J.b0[i] * cs;
-            cd wa = w / a, wb = w / b;
-            cd wa2 = wa * wa, wb2 = wb * wb, W = wb2 - wa2, iW = 1.0 / W;
-            LW &t = tab[(size_t)iw * L + i];
-            memset(&t, 0, sizeof t);
-            t.wa2x = wa2.real(); t.wa2y = wa2.imag(); t.wb2x = wb2.real(); t.wb2y = wb2.imag();
-            t.wa2[0] = (float)wa2.real(); t.wa2[1] = (float)wa2.imag();
-            t.wb2[0] = (float)wb2.real(); t.wb2[1] = (float)wb2.imag();
-            t.W[0] = (float)W.real(); t.W[1] = (float)W.imag();
-            t.iW[0] = (float)iW.real(); t.iW[1] = (float)iW.imag();
-            t.a[0] = (float)a.real(); t.a[1] = (float)a.imag();
-            t.b[0] = (float)b.real(); t.b[1] = (float)b.imag();
-            t.mu = (float)J.mu[i];
-            t.h = (float)J.h[i];
-            t.wa2lo = (float)(wa2.real() - (double)(float)wa2.real());
-            t.wb2lo = (float)(wb2.real() - (double)(float)wb2.real());
-        }
-    }
+    grt::fill_layer_table<float>(J, tab);
     int2 *tiles = (int2 *)(h + o_tiles);
     long long t = 0;
     for (int iw = 0; iw < nw; iw++)

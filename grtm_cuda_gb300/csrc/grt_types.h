@@ -20,6 +20,8 @@ struct alignas(16) LayerW {
     R a[2], b[2];                   // attenuated velocities alpha(w), beta(w)
     R mu, h;                        // b0^2 rho, thickness (half-space: top depth)
     float wa2lo, wb2lo;             // Re(wa^2) - (float)Re(wa^2), same for wb^2 (double-float low words)
+    float wa2ylo, wb2ylo, hlo;      // low words of Im(wa^2), Im(wb^2) and of the thickness
+    float pad_;
 };
 static_assert(sizeof(LayerW<float>) % 16 == 0, "TMA bulk copies need 16-byte multiples");
 static_assert(sizeof(LayerW<double>) % 16 == 0, "TMA bulk copies need 16-byte multiples");

@@ -1,0 +1,356 @@
+"""Learned wavenumber sampling.
+
+The plain method integrates every frequency over a fixed wavenumber grid
+(k_j = j dk, j < nk, dk = 2 pi / L with the reference's aperture rule
+green.cu:2072-2077).  Most of that grid is wasted: at low frequencies the
+integrand has died out long before the top of the grid, and the step is often
+finer than the receivers' distances need.  A small network, trained on
+convergence sweeps that the plain method runs on the GPU, predicts for each
+(model, frequency, distance) the cutoff k_max and the step dk; the GRT kernel
+then evaluates a ragged grid of nk(w) = k_max(w)/dk points (grid mode
+K_CUSTOM).
+
+Network: 15 inputs (12 layer statistics of the model, log w, log r, log zs),
+three hidden layers of 64 SiLU units, 2 outputs (log k_max, log2 of the step
+multiple dk / dk_plain), trained and evaluated by the library's own CUDA
+kernels (grt_mlp_*).  Inputs and targets are standardised with statistics
+stored beside the weights.
+
+The plain fixed grid is both fallback and judge of every prediction: before
+its result is used, the integrand tail beyond the predicted k_max is measured
+on the plain grid at a few spot frequencies and distances, the step is checked
+by the same sweep's aliasing test, and the spectra of every receiver at the
+spot frequencies are compared with the plain grid's.  A receiver that fails
+is recomputed on the plain grid.
+
+No counterpart in the reference.
+"""
+import ctypes
+import math
+import os
+import struct
+import time
+
+import numpy as np
+
+from . import (Context, GrtError, K_CUSTOM, K_FIXED, FP32, Plan, grid, lib, make_model, make_opts, sweep_kmax,
+               synth)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+WEIGHTS = os.path.join(HERE, "data", "ksampler.bin")
+N_FEAT, N_IN, N_OUT = 12, 15, 2
+MAGIC = b"GRTKSMP1"
+
+# the plain grid the sampler is trained against and judged by
+PLAIN = dict(dt=0.05, log2n=13, nk=32768, sigma_factor=math.pi, taper=0.3, t0=0.0)
+
+
+def layer_features(m):
+    """12 statistics of a layered model (dict as from synth): depth of the
+    half-space, min/max Vs, max Vp, thickness-weighted mean Vs, Vs of the
+    source and receiver layers, min Vs between them, layer count, thinnest
+    layer, mean Qs, thickness of the source layer -- all as logs."""
+    tops = np.asarray(m["ztop"], dtype=np.float64)
+    vp, vs, qs = (np.asarray(m[k], dtype=np.float64) for k in ("vp", "vs", "qs"))
+    h = np.diff(tops)
+    s = int(np.searchsorted(tops, m["hs"], side="right") - 1)
+    r = int(np.searchsorted(tops, m.get("hr", 0.0), side="right") - 1)
+    lo, hi = min(s, r), max(s, r)
+    hsrc = h[s] if s < len(h) else 10.0
+    f = [tops[-1], vs.min(), vs.max(), vp.max(), float(np.sum(h * vs[:-1]) / max(np.sum(h), 1e-9)), vs[s], vs[r],
+         vs[lo:hi + 1].min(), float(len(vs)), h.min() if len(h) else 1.0, qs.mean(), hsrc]
+    return np.log(np.maximum(np.asarray(f, dtype=np.float64), 1e-6))
+
+
+def net_inputs(feat, omega, r, zs):
+    """Rows of the 15 network inputs for frequencies omega (rad/s) and
+    distances r (km), broadcast together."""
+    omega, r = np.broadcast_arrays(np.atleast_1d(omega).astype(np.float64), np.atleast_1d(r).astype(np.float64))
+    n = omega.size
+    x = np.empty((n, N_IN), dtype=np.float64)
+    x[:, :N_FEAT] = feat
+    x[:, 12] = np.log(omega.ravel())
+    x[:, 13] = np.log(r.ravel())
+    x[:, 14] = math.log(zs + 0.1)
+    return x
+
+
+class Mlp:
+    """The network on the GPU (grt_mlp_*): forward, loss gradient, Adam."""
+
+    def __init__(self, ctx, n_in=N_IN, n_out=N_OUT, seed=1):
+        self.ctx, self.n_in, self.n_out = ctx, n_in, n_out
+        self.h = ctypes.c_void_p()
+        rc = lib().grt_mlp_create(ctx.h, n_in, n_out, seed, ctypes.byref(self.h))
+        if rc:
+            raise GrtError(rc, ctx.error())
+        self.n_params = lib().grt_mlp_n_params(self.h)
+
+    @staticmethod
+    def _f(a, cols):
+        a = np.ascontiguousarray(a, dtype=np.float32)
+        assert a.ndim == 2 and a.shape[1] == cols
+        return a
+
+    @staticmethod
+    def _fp(a):
+        return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+    def _check(self, rc):
+        if rc:
+            raise GrtError(rc, self.ctx.error())
+
+    def get_params(self):
+        p = np.empty(self.n_params, dtype=np.float32)
+        self._check(lib().grt_mlp_get_params(self.h, self._fp(p)))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.n_params
+        self._check(lib().grt_mlp_set_params(self.h, self._fp(p)))
+
+    def forward(self, x):
+        x = self._f(x, self.n_in)
+        y = np.empty((x.shape[0], self.n_out), dtype=np.float32)
+        self._check(lib().grt_mlp_forward(self.h, x.shape[0], self._fp(x), self._fp(y)))
+        return y
+
+    def loss_grad(self, x, t):
+        x, t = self._f(x, self.n_in), self._f(t, self.n_out)
+        loss = ctypes.c_float()
+        g = np.empty(self.n_params, dtype=np.float32)
+        self._check(lib().grt_mlp_loss_grad(self.h, x.shape[0], self._fp(x), self._fp(t), ctypes.byref(loss),
+                                            self._fp(g)))
+        return loss.value, g
+
+    def train(self, x, t, epochs, batch=256, lr=1e-3, seed=1):
+        x, t = self._f(x, self.n_in), self._f(t, self.n_out)
+        loss = ctypes.c_float()
+        self._check(lib().grt_mlp_train(self.h, x.shape[0], self._fp(x), self._fp(t), int(epochs), int(batch),
+                                        float(lr), int(seed), ctypes.byref(loss)))
+        return loss.value
+
+    def close(self):
+        if self.h:
+            lib().grt_mlp_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------- training data
+def sweep_dataset(ctx, seeds, n_freq=32, n_band=8, tol=1e-4, plain=PLAIN, rng_seed=0, n_layers=40):
+    """Convergence sweeps of the plain grid on seeded crustal models
+    (n_layers layers, source depth U(1, 30) km), n_freq frequencies (log-
+    uniform) x n_band distances (log-uniform in 1-500 km) per model.
+    Returns inputs [n, 15] and targets [n, 2] = (log k_max, log2(dk/dk_plain))."""
+    rng = np.random.default_rng(rng_seed)
+    X, Y = [], []
+    for seed in seeds:
+        m = synth.crust(np.random.default_rng(seed), n_layers, rng.uniform(1.0, 30.0))
+        model = make_model(**m)
+        opts = make_opts(plain["dt"], plain["log2n"], t0=plain["t0"], taper=plain["taper"],
+                         sigma_factor=plain["sigma_factor"], k_mode=K_FIXED, nk_fixed=plain["nk"])
+        gr = grid(model, opts)
+        nw, dkp, df = gr["nw"], gr["dk"], gr["df"]
+        fi = np.unique(np.round(np.exp(rng.uniform(0.0, math.log(nw - 1), 4 * n_freq))).astype(np.int64))
+        fi = np.sort(rng.choice(fi, size=min(n_freq, len(fi)), replace=False))
+        br = np.exp(rng.uniform(math.log(1.0), math.log(500.0), n_band))
+        kmax, _, dk = sweep_kmax(model, opts, fi, br, tol, ctx=ctx)
+        feat = layer_features(m)
+        om = (2 * math.pi * df * fi)[:, None] * np.ones((1, n_band))
+        rr = np.ones((len(fi), 1)) * br[None, :]
+        X.append(net_inputs(feat, om.ravel(), rr.ravel(), m["hs"]))
+        Y.append(np.stack([np.log(np.maximum(kmax.ravel(), 4 * dkp)), np.log2(dk.ravel() / dkp)], axis=1))
+    return np.concatenate(X), np.concatenate(Y)
+
+
+# ---------------------------------------------------------------- the sampler
+class Sampler:
+    """Trained network parameters with their input/output standardisation
+    and the safety margins measured on held-out sweeps."""
+
+    def __init__(self, params, x_mean, x_std, y_mean, y_std, margin_k=1.25, margin_d=1.0, tol=1e-4):
+        self.params = np.ascontiguousarray(params, dtype=np.float32)
+        self.x_mean, self.x_std = np.asarray(x_mean, np.float64), np.asarray(x_std, np.float64)
+        self.y_mean, self.y_std = np.asarray(y_mean, np.float64), np.asarray(y_std, np.float64)
+        self.margin_k, self.margin_d, self.tol = float(margin_k), float(margin_d), float(tol)
+        self._net = None
+
+    # tiny binary file: magic, n_in, n_out, n_params (int32), margins and tol
+    # (float64), then standardisation (float64) and parameters (float32)
+    def save(self, path):
+        os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
+        with open(path, "wb") as f:
+            f.write(MAGIC)
+            f.write(struct.pack("<3i", N_IN, N_OUT, self.params.size))
+            f.write(struct.pack("<3d", self.margin_k, self.margin_d, self.tol))
+            for a in (self.x_mean, self.x_std, self.y_mean, self.y_std):
+                f.write(np.asarray(a, "<f8").tobytes())
+            f.write(self.params.astype("<f4").tobytes())
+
+    @classmethod
+    def load(cls, path=WEIGHTS):
+        with open(path, "rb") as f:
+            b = f.read()
+        if b[:8] != MAGIC:
+            raise ValueError(f"{path}: not a sampler file")
+        n_in, n_out, n_p = struct.unpack_from("<3i", b, 8)
+        if (n_in, n_out) != (N_IN, N_OUT):
+            raise ValueError(f"{path}: network {n_in}->{n_out}, expected {N_IN}->{N_OUT}")
+        mk, md, tol = struct.unpack_from("<3d", b, 20)
+        o = 44
+        arrs = []
+        for n in (n_in, n_in, n_out, n_out):
+            arrs.append(np.frombuffer(b, "<f8", n, o).copy())
+            o += 8 * n
+        p = np.frombuffer(b, "<f4", n_p, o).copy()
+        if o + 4 * n_p != len(b):
+            raise ValueError(f"{path}: size mismatch")
+        return cls(p, *arrs, margin_k=mk, margin_d=md, tol=tol)
+
+    def net(self, ctx):
+        if self._net is None or self._net.ctx is not ctx:
+            self._net = Mlp(ctx)
+            self._net.set_params(self.params)
+        return self._net
+
+    def predict(self, ctx, x):
+        """Un-standardised outputs (log k_max, log2 step multiple) for raw inputs."""
+        z = (np.asarray(x, np.float64) - self.x_mean) / self.x_std
+        y = self.net(ctx).forward(z.astype(np.float32)).astype(np.float64)
+        return y * self.y_std + self.y_mean
+
+    @staticmethod
+    def train_new(ctx, X, Y, epochs=(200, 100, 100), lrs=(2e-3, 5e-4, 1e-4), batch=256, seed=1, val=None):
+        """Fit a fresh network with the library's CUDA kernels.  Returns the
+        sampler and the loss history [(epochs, lr, train loss, val loss)]."""
+        xm, xs = X.mean(0), X.std(0) + 1e-9
+        ym, ys = Y.mean(0), Y.std(0) + 1e-9
+        net = Mlp(ctx, seed=seed)
+        zx, zy = ((X - xm) / xs).astype(np.float32), ((Y - ym) / ys).astype(np.float32)
+        hist = []
+        for i, (ep, lr) in enumerate(zip(epochs, lrs)):
+            tl = net.train(zx, zy, ep, batch, lr, seed + i)
+            vl = None
+            if val is not None:
+                vl, _ = net.loss_grad(((val[0] - xm) / xs).astype(np.float32), ((val[1] - ym) / ys).astype(np.float32))
+            hist.append((ep, lr, tl, vl))
+        s = Sampler(net.get_params(), xm, xs, ym, ys)
+        net.close()
+        return s, hist
+
+    def calibrate(self, ctx, X, Y, q=0.995):
+        """Margins from held-out sweeps: k_max is scaled by the q-quantile of
+        the under-prediction ratio; the step multiple is lowered likewise."""
+        y = self.predict(ctx, X)
+        under_k = np.exp(Y[:, 0] - y[:, 0])            # > 1 where the net predicts too small
+        self.margin_k = float(max(1.0, np.quantile(under_k, q)))
+        over_d = 2.0 ** (y[:, 1] - Y[:, 1])            # > 1 where the net predicts too coarse
+        self.margin_d = float(max(1.0, np.quantile(over_d, q)))
+        return self.margin_k, self.margin_d
+
+    # ------------------------------------------------------------ inference
+    def grid(self, ctx, m, dists, dt, log2n, nk_plain, sigma_factor=math.pi, taper=0.3, t0=0.0):
+        """Learned ragged grid for one model and receiver set: (dk, nk[nw],
+        kmax[nw], plain grid report)."""
+        model = make_model(**m)
+        popts = make_opts(dt, log2n, t0=t0, taper=taper, sigma_factor=sigma_factor, k_mode=K_FIXED, nk_fixed=nk_plain)
+        gr = grid(model, popts)
+        nw, dkp, df = gr["nw"], gr["dk"], gr["df"]
+        om = 2 * math.pi * df * np.maximum(np.arange(nw), 1)
+        d = np.asarray(dists, np.float64)
+        feat = layer_features(m)
+        y = self.predict(ctx, np.concatenate([net_inputs(feat, om, d.min(), m["hs"]),
+                                              net_inputs(feat, om, d.max(), m["hs"])]))
+        kmax = np.exp(y[:nw, 0]) * self.margin_k
+        mult = 2.0 ** np.floor(np.clip(np.min(y[nw:, 1]) - math.log2(self.margin_d), 0.0, 5.0))
+        dk = dkp * mult
+        ktop = (nk_plain - 1) * dkp
+        kmax = np.minimum(kmax, ktop)
+        nk_top = int(ktop / dk) + 1
+        nk = np.clip(np.ceil(kmax / dk).astype(np.int64) + 2, 8, nk_top).astype(np.int32)
+        return dk, nk, nk * dk, gr
+
+
+def spot_frequencies(nw, n=6):
+    """Fixed spread of judge frequencies over the band (index >= 1)."""
+    f = np.unique(np.clip(np.round(np.array([0.02, 0.08, 0.2, 0.4, 0.62, 0.85])[:n] * nw).astype(np.int64), 1,
+                          nw - 1))
+    return f
+
+
+def run_learned(sampler, m, dists, dt, log2n, nk_plain, ctx=None, sigma_factor=math.pi, taper=0.3, t0=0.0,
+                tail_tol=None, spec_tol=2e-3, judge=True):
+    """Traces of one model on the learned grid, judged against the plain grid.
+
+    Returns (traces [n_dist, n_cols, N], info).  info: learned and plain (w,k)
+    counts, step multiple, the judge's tail and spectral figures, the
+    receivers recomputed on the plain grid and the wall time of each part."""
+    own = ctx is None
+    ctx = ctx or Context()
+    try:
+        t_start = time.perf_counter()
+        dists = np.asarray(dists, np.float64)
+        dk, nk, kmax, gr = sampler.grid(ctx, m, dists, dt, log2n, nk_plain, sigma_factor, taper, t0)
+        nw, dkp = gr["nw"], gr["dk"]
+        t_pred = time.perf_counter()
+        model = make_model(**m)
+        lopts = make_opts(dt, log2n, t0=t0, taper=taper, sigma_factor=sigma_factor, dk=dk, nk_custom=nk)
+        plan = Plan(ctx, model, lopts, dists)
+        plan.execute()
+        traces, _ = plan.fetch(True, False)
+        info = dict(nkw_learned=int(nk.sum()), nkw_plain=int(nw) * int(nk_plain), dk_mult=float(dk / dkp),
+                    ms_learned_gpu=plan.report.ms_total, fallback=[], tail_max=0.0, spec_err_max=0.0)
+        t_run = time.perf_counter()
+        if judge:
+            spot = spot_frequencies(nw)
+            popts = make_opts(dt, log2n, t0=t0, taper=taper, sigma_factor=sigma_factor, k_mode=K_FIXED,
+                              nk_fixed=nk_plain)
+            bands = np.unique(np.array([dists.min(), math.sqrt(dists.min() * dists.max()), dists.max()]))
+            tol = sampler.tol if tail_tol is None else tail_tol
+            _, tail, dk_ok = sweep_kmax(model, popts, spot, bands, sampler.tol,
+                                        k_judge=np.repeat(kmax[spot][:, None], len(bands), 1), ctx=ctx)
+            info["tail_max"] = float(tail.max())
+            tail_bad = tail.max(0) > 10 * tol                  # per band
+            step_bad = bool(np.any(dk_ok[:, -1] < dk * (1 - 1e-9)))
+            # plain grid at the spot frequencies only (2 points elsewhere)
+            nk_spot = np.full(nw, 2, np.int32)
+            nk_spot[spot] = nk_plain
+            sp_plan = Plan(ctx, model, make_opts(dt, log2n, t0=t0, taper=taper, sigma_factor=sigma_factor, dk=dkp,
+                                                 nk_custom=nk_spot), dists)
+            sp_plan.execute()
+            s_plain = sp_plan.fetch_freqs(spot)
+            s_learn = plan.fetch_freqs(spot)
+            sp_plan.close()
+            num = np.sqrt(np.sum(np.abs(s_learn - s_plain) ** 2, axis=(1, 2)))
+            den = np.sqrt(np.sum(np.abs(s_plain) ** 2, axis=(1, 2))) + 1e-300
+            err = num / den
+            info["spec_err_max"] = float(err.max())
+            bad = err > spec_tol
+            if step_bad:
+                bad[:] = True
+            else:
+                # a band's tail failure sends the receivers nearest to it back
+                band_of = np.argmin(np.abs(np.log(dists[:, None] / bands[None, :])), axis=1)
+                bad |= tail_bad[band_of]
+            if bad.any():
+                idx = np.nonzero(bad)[0]
+                pplan = Plan(ctx, model, popts, dists[idx])
+                pplan.execute()
+                traces[idx], _ = pplan.fetch(True, False)
+                pplan.close()
+                info["fallback"] = idx.tolist()
+        plan.close()
+        t_end = time.perf_counter()
+        info.update(s_predict=t_pred - t_start, s_learned=t_run - t_pred, s_judge=t_end - t_run,
+                    s_total=t_end - t_start)
+        return traces, info
+    finally:
+        if own:
+            ctx.close()

@@ -1,0 +1,111 @@
+"""Train the learned wavenumber sampler on convergence sweeps of the plain
+grid, and evaluate it on held-out models.
+
+    python -m grtm_cuda_gb300.train_sampler --out grtm_cuda_gb300/data/ksampler.bin
+    python -m grtm_cuda_gb300.train_sampler --eval --weights ... --eval-models 8
+
+Training data: 80 seeded 40-layer crustal models (source depth U(1, 30) km),
+32 frequencies x 8 distances each (20480 sweeps) on the plain grid of
+N = 8192 samples at dt = 0.05 s with nk = 32768; 16 further models for
+validation and the safety margins.  Everything runs on the GPU through the
+library (sweeps: grt_sweep_kmax; training: grt_mlp_train).
+"""
+import argparse
+import json
+import sys
+import time
+
+import numpy as np
+
+from . import Context, FP64, K_FIXED, Plan, make_model, make_opts, synth
+from .learned import PLAIN, WEIGHTS, Sampler, run_learned, sweep_dataset
+
+TRAIN_SEEDS = range(1000, 1080)
+VAL_SEEDS = range(2000, 2016)
+HELD_OUT_SEEDS = range(3000, 3256)
+
+
+def train(out, n_models=80, n_val=16, tol=1e-4, log=sys.stdout, dump=None):
+    ctx = Context()
+    t0 = time.perf_counter()
+    X, Y = sweep_dataset(ctx, list(TRAIN_SEEDS)[:n_models], tol=tol, rng_seed=1)
+    Xv, Yv = sweep_dataset(ctx, list(VAL_SEEDS)[:n_val], tol=tol, rng_seed=2)
+    t1 = time.perf_counter()
+    if dump:
+        np.savez_compressed(dump, X=X.astype(np.float32), Y=Y.astype(np.float32), Xv=Xv.astype(np.float32),
+                            Yv=Yv.astype(np.float32))
+    s, hist = Sampler.train_new(ctx, X, Y, val=(Xv, Yv))
+    t2 = time.perf_counter()
+    s.tol = tol
+    mk, md = s.calibrate(ctx, Xv, Yv)
+    yv = s.predict(ctx, Xv)
+    res = dict(n_train=len(X), n_val=len(Xv), s_sweeps=t1 - t0, s_train=t2 - t1, history=hist,
+               val_rmse_logk=float(np.sqrt(np.mean((yv[:, 0] - Yv[:, 0]) ** 2))),
+               val_rmse_log2dk=float(np.sqrt(np.mean((yv[:, 1] - Yv[:, 1]) ** 2))),
+               margin_k=mk, margin_d=md, target_mean=Y.mean(0).tolist(), target_std=Y.std(0).tolist(),
+               dk_mult_hist=np.bincount(np.round(Y[:, 1]).astype(int), minlength=6).tolist())
+    s.save(out)
+    ctx.close()
+    print(json.dumps(res), file=log)
+    return s, res
+
+
+def evaluate(weights, n_models=8, n_receivers=24, fp64=True, log=sys.stdout):
+    """Learned vs plain FP32 vs plain FP64 on held-out models."""
+    s = Sampler.load(weights)
+    ctx = Context()
+    p = PLAIN
+    rows = []
+    for seed in list(HELD_OUT_SEEDS)[:n_models]:
+        rng = np.random.default_rng(seed)
+        m = synth.crust(rng, 40, rng.uniform(1.0, 30.0))
+        dists = np.sort(rng.uniform(1.0, 500.0, n_receivers))
+        model = make_model(**m)
+        popts = make_opts(p["dt"], p["log2n"], sigma_factor=p["sigma_factor"], k_mode=K_FIXED, nk_fixed=p["nk"])
+        plan = Plan(ctx, model, popts, dists)
+        plan.execute()
+        ms_plain = plan.report.ms_total
+        tp, _ = plan.fetch(True, False)
+        plan.close()
+        tl, info = run_learned(s, m, dists, p["dt"], p["log2n"], p["nk"], ctx=ctx)
+        row = dict(seed=seed, hs=m["hs"], ms_plain=ms_plain, **{k: v for k, v in info.items() if k != "fallback"},
+                   n_fallback=len(info["fallback"]))
+        ref = tp
+        if fp64:
+            popts64 = make_opts(p["dt"], p["log2n"], sigma_factor=p["sigma_factor"], k_mode=K_FIXED,
+                                nk_fixed=p["nk"], precision=FP64)
+            plan = Plan(ctx, model, popts64, dists)
+            plan.execute()
+            ref, _ = plan.fetch(True, False)
+            plan.close()
+        def rel(a):
+            e = np.sqrt(np.sum((a - ref) ** 2, axis=(1, 2)) / np.sum(ref ** 2, axis=(1, 2)))
+            return float(e.max()), float(np.median(e)), float(np.mean(e <= 1e-3))
+        row["learned_vs_ref"] = rel(tl)
+        row["plain_vs_ref"] = rel(tp)
+        rows.append(row)
+        print(json.dumps(row), file=log, flush=True)
+    ctx.close()
+    return rows
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out", default=WEIGHTS)
+    ap.add_argument("--models", type=int, default=80)
+    ap.add_argument("--tol", type=float, default=1e-4)
+    ap.add_argument("--eval", action="store_true")
+    ap.add_argument("--weights", default=WEIGHTS)
+    ap.add_argument("--eval-models", type=int, default=8)
+    ap.add_argument("--receivers", type=int, default=24)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--dump", default=None, help="also write the sweep dataset (npz)")
+    a = ap.parse_args()
+    if a.eval:
+        evaluate(a.weights, a.eval_models, a.receivers, not a.no_fp64)
+    else:
+        train(a.out, a.models, tol=a.tol, dump=a.dump)
+
+
+if __name__ == "__main__":
+    main()

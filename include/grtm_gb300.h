@@ -36,6 +36,7 @@ extern "C" {
 /* wavenumber grids */
 #define GRT_K_REFERENCE 0      /* per-frequency k_max rule of the reference, dk = 2 pi / L */
 #define GRT_K_FIXED 1          /* nk_fixed points k_j = j dk at every frequency */
+#define GRT_K_CUSTOM 2         /* opts.nk_custom[iw] points k_j = j dk at frequency iw */
 
 /* working precision of the per-(w,k) kernel and the wavenumber sum */
 #define GRT_FP32 0
@@ -67,6 +68,7 @@ typedef struct grt_opts {
     double dk;            /* > 0 overrides the wavenumber step */
     int precision;        /* GRT_FP32 or GRT_FP64 */
     int fix;              /* GRT_FIX_* bits */
+    const int *nk_custom; /* GRT_K_CUSTOM: points per frequency, N/2 entries (e.g. a learned grid) */
 } grt_opts;
 
 typedef struct grt_report {
@@ -104,8 +106,47 @@ GRT_API int grt_plan_execute(grt_plan *plan, grt_report *report);
 /* traces: [n_dist][n_cols][N] doubles; spectra: [n_dist][n_cols][N] complex as
  * (re, im) doubles (after taper and Hermitian fill).  Either may be NULL. */
 GRT_API int grt_plan_fetch(grt_plan *plan, double *traces, double *spectra);
+/* spectra at selected frequency indices (0..N-1) only: [n_dist][n_cols][n_freq]
+ * complex as (re, im) doubles */
+GRT_API int grt_plan_fetch_freqs(grt_plan *plan, int n_freq, const int *freq_idx, double *spectra);
 GRT_API int grt_plan_info(const grt_plan *plan, grt_report *report);
 GRT_API void grt_plan_destroy(grt_plan *plan);
+/* Grid of a model and options without a plan or a device: fills the layer,
+ * frequency and wavenumber fields of report (n_wk, nk_max, dk, ...), the
+ * timing fields zero.  Errors as grt_plan_create, message on stderr. */
+GRT_API int grt_grid(const grt_model *model, const grt_opts *opts, grt_report *report);
+
+/* Convergence sweep of the plain method (training data and judge of the
+ * learned wavenumber sampler).  For the frequencies freq_idx[0..n_freq) it
+ * evaluates the per-(w,k) kernel on the grid of opts and returns, for each
+ * frequency and distance r_b, the smallest k_c such that the weighted
+ * integrand envelope g(k) = max_q |K_q(w,k)| (1+k)^2 min(1, (k r_b)^-1/2)
+ * beyond k_c holds at most tol of its total (kmax_out).  Optional outputs:
+ * tail_out, the envelope fraction beyond k_judge[i]; dk_out, the coarsest
+ * step dk*2^s (s <= 5) whose sums of K_q(k) J0(k r_b) up to k_c agree with
+ * the full-grid sums within tol for every column (its spatial aliasing at
+ * r_b).  All outputs [n_freq][n_band].  FP32 kernel.  No counterpart in the
+ * reference (its k_max is the fixed rule of cal_kmax, green.cu:108-162). */
+GRT_API int grt_sweep_kmax(grt_ctx *ctx, const grt_model *model, const grt_opts *opts, int n_freq,
+                           const int *freq_idx, int n_band, const double *band_r, double tol,
+                           const double *k_judge, double *kmax_out, double *tail_out, double *dk_out);
+
+/* The learned sampler's network: n_in -> 64 -> 64 -> 64 -> n_out with SiLU
+ * hidden activations, FP32, trained by the library's own CUDA kernels
+ * (forward, backward, Adam) on mean squared error.  Host arrays in and out,
+ * row-major [n][n_in] / [n][n_out].  No counterpart in the reference. */
+typedef struct grt_mlp grt_mlp;
+GRT_API int grt_mlp_create(grt_ctx *ctx, int n_in, int n_out, unsigned long long seed, grt_mlp **mlp);
+GRT_API void grt_mlp_destroy(grt_mlp *mlp);
+GRT_API int grt_mlp_n_params(const grt_mlp *mlp);
+GRT_API int grt_mlp_get_params(grt_mlp *mlp, float *params);
+GRT_API int grt_mlp_set_params(grt_mlp *mlp, const float *params);
+GRT_API int grt_mlp_forward(grt_mlp *mlp, int n, const float *x, float *y);
+/* loss and its gradient with respect to the parameters (for checks) */
+GRT_API int grt_mlp_loss_grad(grt_mlp *mlp, int n, const float *x, const float *t, float *loss, float *grad);
+/* epochs of shuffled mini-batch Adam; loss of the last batch */
+GRT_API int grt_mlp_train(grt_mlp *mlp, int n, const float *x, const float *t, int epochs, int batch, float lr,
+                          unsigned long long seed, float *loss);
 
 /* create + execute + fetch + destroy */
 GRT_API int grt_run(grt_ctx *ctx, const grt_model *model, const grt_opts *opts, int n_dist,

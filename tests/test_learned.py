@@ -1,0 +1,236 @@
+"""Learned wavenumber sampler: the network's CUDA kernels against the FP64
+numpy oracle, the convergence sweep, and the learned path against the plain
+grid (its judge and fallback) and FP64."""
+import math
+import os
+
+import numpy as np
+import pytest
+
+from oracle import mlp_oracle as MO
+
+N_IN, N_OUT = 15, 2
+
+
+def _data(n, seed=0):
+    rng = np.random.default_rng(seed)
+    x = rng.normal(size=(n, N_IN))
+    t = np.stack([np.sin(x[:, 0]) + 0.5 * x[:, 1] * x[:, 2], np.tanh(x[:, 3] - x[:, 4])], axis=1)
+    return x, t
+
+
+# ---------------------------------------------------------------- CPU
+def test_oracle_gradient_matches_finite_differences():
+    _, n = MO.layout(N_IN, N_OUT)
+    rng = np.random.default_rng(3)
+    p = rng.normal(scale=0.2, size=n)
+    x, t = _data(6)
+    _, g = MO.loss_grad(p, x, t, N_IN, N_OUT)
+    idx = rng.choice(n, 40, replace=False)
+    h = 1e-6
+    for i in idx:
+        e = np.zeros(n)
+        e[i] = h
+        fd = (MO.loss(p + e, x, t, N_IN, N_OUT) - MO.loss(p - e, x, t, N_IN, N_OUT)) / (2 * h)
+        assert abs(fd - g[i]) <= 1e-7 + 1e-5 * abs(fd)
+
+
+def test_sampler_file_roundtrip(tmp_path):
+    from grtm_cuda_gb300.learned import Sampler
+    _, n = MO.layout(N_IN, N_OUT)
+    rng = np.random.default_rng(1)
+    s = Sampler(rng.normal(size=n), rng.normal(size=N_IN), rng.uniform(1, 2, N_IN), rng.normal(size=N_OUT),
+                rng.uniform(1, 2, N_OUT), margin_k=1.3, margin_d=1.5, tol=2e-4)
+    path = str(tmp_path / "k.bin")
+    s.save(path)
+    r = Sampler.load(path)
+    assert np.array_equal(r.params, s.params.astype(np.float32))
+    assert np.array_equal(r.x_std, s.x_std) and np.array_equal(r.y_mean, s.y_mean)
+    assert (r.margin_k, r.margin_d, r.tol) == (1.3, 1.5, 2e-4)
+    with open(path, "r+b") as f:
+        f.write(b"XXXXXXXX")
+    with pytest.raises(ValueError):
+        Sampler.load(path)
+
+
+def test_features_finite_on_generators():
+    from grtm_cuda_gb300 import learned, synth
+    for seed in range(5):
+        for nl in (3, 20, 40, 60):
+            m = synth.crust(np.random.default_rng(seed), nl, 1.0 + 5 * seed)
+            f = learned.layer_features(m)
+            assert f.shape == (12,) and np.all(np.isfinite(f))
+    m, _ = synth.config1_model()
+    assert np.all(np.isfinite(learned.layer_features(m)))
+
+
+def test_committed_weights_load():
+    from grtm_cuda_gb300 import learned
+    if not os.path.exists(learned.WEIGHTS):
+        pytest.skip("no trained sampler in the tree")
+    s = learned.Sampler.load()
+    assert s.params.size == MO.layout(N_IN, N_OUT)[1]
+    assert s.margin_k >= 1.0 and s.margin_d >= 1.0 and 0 < s.tol < 1e-2
+    # the oracle's forward of the committed network gives finite outputs
+    x = np.zeros((4, N_IN))
+    y, _ = MO.forward(s.params, x, N_IN, N_OUT)
+    assert np.all(np.isfinite(y))
+
+
+# ---------------------------------------------------------------- GPU
+@pytest.fixture(scope="module")
+def ctx():
+    import grtm_cuda_gb300 as g
+    c = g.Context()
+    yield c
+    c.close()
+
+
+@pytest.mark.gpu
+def test_mlp_forward_matches_oracle(ctx):
+    from grtm_cuda_gb300.learned import Mlp
+    net = Mlp(ctx, seed=7)
+    p = net.get_params().astype(np.float64)
+    x, _ = _data(300, 1)
+    y = net.forward(x)
+    yo, _ = MO.forward(p, x.astype(np.float32), N_IN, N_OUT)
+    assert np.max(np.abs(y - yo)) <= 1e-5 * (1 + np.max(np.abs(yo)))
+    net.close()
+
+
+@pytest.mark.gpu
+def test_mlp_gradient_matches_oracle(ctx):
+    from grtm_cuda_gb300.learned import Mlp
+    net = Mlp(ctx, seed=11)
+    p = net.get_params().astype(np.float64)
+    for n in (1, 63, 64, 257):
+        x, t = _data(n, n)
+        loss, g = net.loss_grad(x, t)
+        lo, go = MO.loss_grad(p, x.astype(np.float32), t.astype(np.float32), N_IN, N_OUT)
+        assert abs(loss - lo) <= 1e-5 * abs(lo)
+        assert np.linalg.norm(g - go) <= 1e-5 * np.linalg.norm(go)
+    net.close()
+
+
+@pytest.mark.gpu
+def test_mlp_adam_step_matches_oracle(ctx):
+    from grtm_cuda_gb300.learned import Mlp
+    net = Mlp(ctx, seed=5)
+    x, t = _data(128, 9)
+    lr = 1e-3
+    p0 = net.get_params().astype(np.float64)
+    m = np.zeros_like(p0)
+    v = np.zeros_like(p0)
+    for step in (1, 2, 3):
+        # one epoch with one batch of all samples is one full-batch Adam step
+        p = net.get_params().astype(np.float64)
+        _, g = MO.loss_grad(p, x.astype(np.float32), t.astype(np.float32), N_IN, N_OUT)
+        po, m, v = MO.adam(p, g, m, v, step, lr)
+        net.train(x, t, epochs=1, batch=128, lr=lr, seed=step)
+        err = np.abs(net.get_params() - po)
+        # Adam normalises by |g|: where the gradient is at rounding level its
+        # sign, and so the step, is not defined to better than lr
+        big = np.abs(g) > 1e-4 * np.abs(g).max()
+        assert np.max(err[big]) <= 2e-6
+        assert np.max(err) <= 2.5 * lr
+    net.close()
+
+
+@pytest.mark.gpu
+def test_mlp_training_converges(ctx):
+    from grtm_cuda_gb300.learned import Mlp
+    net = Mlp(ctx, seed=2)
+    x, t = _data(4096, 4)
+    l0, _ = net.loss_grad(x, t)
+    net.train(x, t, epochs=60, batch=128, lr=2e-3)
+    l1, _ = net.loss_grad(x, t)
+    assert l1 < 0.05 * l0
+    net.close()
+
+
+def _small_job():
+    import grtm_cuda_gb300 as g
+    from grtm_cuda_gb300 import synth
+    m = synth.crust(np.random.default_rng(5), 12, 8.0)
+    opts = g.make_opts(0.1, 10, sigma_factor=math.pi, k_mode=g.K_FIXED, nk_fixed=4096)
+    return m, g.make_model(**m), opts
+
+
+@pytest.mark.gpu
+def test_sweep_properties(ctx):
+    import grtm_cuda_gb300 as g
+    m, model, opts = _small_job()
+    gr = g.grid(model, opts)
+    fi = np.array([1, 7, 40, 150, 400])
+    br = np.array([2.0, 30.0, 300.0])
+    k4, _, d4 = g.sweep_kmax(model, opts, fi, br, 1e-4, ctx=ctx)
+    k6, _, d6 = g.sweep_kmax(model, opts, fi, br, 1e-6, ctx=ctx)
+    top = 4096 * gr["dk"]
+    assert np.all(k4 > 0) and np.all(k4 <= top) and np.all(k6 <= top)
+    assert np.all(k6 >= k4)                                   # a tighter tolerance never cuts earlier
+    mult = d4 / gr["dk"]
+    assert np.all(np.isin(np.round(mult), [1, 2, 4, 8, 16, 32])) and np.allclose(mult, np.round(mult))
+    # judging the sweep's own cutoff finds a tail within the tolerance
+    _, tail, _ = g.sweep_kmax(model, opts, fi, br, 1e-4, k_judge=k4, ctx=ctx)
+    assert np.all(tail <= 1e-4 + 1e-12)
+    _, tail_lo, _ = g.sweep_kmax(model, opts, fi, br, 1e-4, k_judge=0.5 * k4, ctx=ctx)
+    assert np.all(tail_lo >= tail)
+
+
+@pytest.mark.gpu
+def test_custom_grid_equals_fixed_grid(ctx):
+    """K_CUSTOM with every frequency at the fixed grid's size reproduces it."""
+    import grtm_cuda_gb300 as g
+    m, model, opts = _small_job()
+    d = np.array([5.0, 50.0])
+    t1, _, _ = g.run(model, opts, d, ctx=ctx)
+    nw = g.grid(model, opts)["nw"]
+    t2, _, _ = g.run(model, g.make_opts(0.1, 10, sigma_factor=math.pi, nk_custom=np.full(nw, 4096)), d, ctx=ctx)
+    assert np.array_equal(t1, t2)
+
+
+def _learned_case(seed=3007, n_rec=8):
+    from grtm_cuda_gb300 import synth
+    rng = np.random.default_rng(seed)
+    m = synth.crust(rng, 40, rng.uniform(1.0, 30.0))
+    return m, np.sort(rng.uniform(1.0, 500.0, n_rec))
+
+
+@pytest.mark.gpu
+def test_learned_path_gain_and_accuracy(ctx):
+    """On a held-out model the trained sampler evaluates far fewer (w,k)
+    points than the plain fixed grid and stays within 1e-3 of FP64."""
+    import grtm_cuda_gb300 as g
+    from grtm_cuda_gb300 import learned
+    if not os.path.exists(learned.WEIGHTS):
+        pytest.skip("no trained sampler in the tree")
+    s = learned.Sampler.load()
+    P = learned.PLAIN
+    m, d = _learned_case()
+    model = g.make_model(**m)
+    t64, _, _ = g.run(model, g.make_opts(P["dt"], P["log2n"], sigma_factor=P["sigma_factor"], k_mode=g.K_FIXED,
+                                         nk_fixed=P["nk"], precision=g.FP64), d, ctx=ctx)
+    tl, info = learned.run_learned(s, m, d, P["dt"], P["log2n"], P["nk"], ctx=ctx)
+    err = np.sqrt(np.sum((tl - t64) ** 2, axis=(1, 2)) / np.sum(t64 ** 2, axis=(1, 2)))
+    assert info["nkw_plain"] / info["nkw_learned"] >= 1.5
+    assert np.sqrt(np.sum((tl - t64) ** 2) / np.sum(t64 ** 2)) <= 1e-3
+    assert np.median(err) <= 1e-3
+
+
+@pytest.mark.gpu
+def test_learned_judge_falls_back(ctx):
+    """A sampler that cuts the integral far too early is caught by the judge
+    and its receivers are recomputed on the plain grid."""
+    import grtm_cuda_gb300 as g
+    from grtm_cuda_gb300 import learned
+    if not os.path.exists(learned.WEIGHTS):
+        pytest.skip("no trained sampler in the tree")
+    s = learned.Sampler.load()
+    s.margin_k = 0.2
+    P = learned.PLAIN
+    m, d = _learned_case(3011, 4)
+    tl, info = learned.run_learned(s, m, d, P["dt"], P["log2n"], P["nk"], ctx=ctx)
+    assert len(info["fallback"]) == len(d)
+    tp, _, _ = g.run(g.make_model(**m), g.make_opts(P["dt"], P["log2n"], sigma_factor=P["sigma_factor"],
+                                                     k_mode=g.K_FIXED, nk_fixed=P["nk"]), d, ctx=ctx)
+    assert np.array_equal(tl, tp)
