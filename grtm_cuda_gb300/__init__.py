@@ -34,7 +34,8 @@ class Opts(ctypes.Structure):
     _fields_ = [("dt", ctypes.c_double), ("log2n", ctypes.c_int), ("t0", ctypes.c_double),
                 ("taper", ctypes.c_double), ("sigma_factor", ctypes.c_double), ("k_mode", ctypes.c_int),
                 ("nk_fixed", ctypes.c_int), ("dk", ctypes.c_double), ("precision", ctypes.c_int),
-                ("fix", ctypes.c_int), ("nk_custom", ctypes.POINTER(ctypes.c_int))]
+                ("fix", ctypes.c_int), ("nk_custom", ctypes.POINTER(ctypes.c_int)),
+                ("k_stride", ctypes.POINTER(ctypes.c_int))]
 
 
 class Report(ctypes.Structure):
@@ -99,7 +100,7 @@ def lib():
     ip = P(ctypes.c_int)
     fp = P(ctypes.c_float)
     L.grt_sweep_kmax.argtypes = [vp, P(Model), P(Opts), ctypes.c_int, ip, ctypes.c_int, _dp, ctypes.c_double,
-                                 _dp, _dp, _dp, _dp]
+                                 _dp, _dp, _dp, _dp, _dp, _dp]
     L.grt_mlp_create.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong, P(vp)]
     L.grt_mlp_destroy.argtypes = [vp]
     L.grt_mlp_destroy.restype = None
@@ -160,15 +161,21 @@ def make_model(ztop, vp, vs, rho, qp, qs, hs, hr=0.0, src_type=0):
 
 
 def make_opts(dt, log2n, t0=0.0, taper=0.3, sigma_factor=2.0, k_mode=K_REFERENCE, nk_fixed=0, dk=0.0,
-              precision=FP32, fix=0, nk_custom=None):
-    """nk_custom: points per frequency (N/2 ints) for K_CUSTOM grids."""
+              precision=FP32, fix=0, nk_custom=None, k_stride=None):
+    """nk_custom: points per frequency (N/2 ints) for K_CUSTOM grids;
+    k_stride: optional per-frequency stride m (k_j = j m dk)."""
     o = Opts(float(dt), int(log2n), float(t0), float(taper), float(sigma_factor), int(k_mode),
-             int(nk_fixed), float(dk), int(precision), int(fix), None)
+             int(nk_fixed), float(dk), int(precision), int(fix), None, None)
+    o._keep = []
     if nk_custom is not None:
         arr = np.ascontiguousarray(nk_custom, dtype=np.int32)
         o.nk_custom = arr.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
-        o._keep = arr
+        o._keep.append(arr)
         o.k_mode = K_CUSTOM
+    if k_stride is not None:
+        arr = np.ascontiguousarray(k_stride, dtype=np.int32)
+        o.k_stride = arr.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+        o._keep.append(arr)
     return o
 
 
@@ -234,29 +241,37 @@ def grid(model, opts):
     return r.as_dict()
 
 
-def sweep_kmax(model, opts, freq_idx, band_r, tol, k_judge=None, ctx=None):
+def sweep_kmax(model, opts, freq_idx, band_r, tol=1e-4, tol_abs=None, k_judge=None, ctx=None, env=False,
+               alias=False):
     """Convergence sweep of the plain grid at selected frequencies and
-    distances (grt_sweep_kmax).  Returns (kmax, tail, dk), each
-    [n_freq, n_band]; tail is None without k_judge."""
+    distances (grt_sweep_kmax).  Returns a dict of [n_freq, n_band] arrays:
+    kmax, and tail (with k_judge), env, alias ([..., 6]) when asked."""
     fi = np.ascontiguousarray(freq_idx, dtype=np.int32)
     br = _arr(np.atleast_1d(band_r))
     shape = (len(fi), len(br))
-    kmax, dk = np.empty(shape), np.empty(shape)
-    tail = np.empty(shape) if k_judge is not None else None
+    out = {"kmax": np.empty(shape)}
+    if k_judge is not None:
+        out["tail"] = np.empty(shape)
+    if env:
+        out["env"] = np.empty(shape)
+    if alias:
+        out["alias"] = np.empty(shape + (6,))
     kj = _arr(np.broadcast_to(k_judge, shape)) if k_judge is not None else None
+    ta = _arr(np.broadcast_to(tol_abs, shape)) if tol_abs is not None else None
     own = ctx is None
     ctx = ctx or Context()
+    opt = lambda k: _ptr(out[k]) if k in out else None
     try:
         rc = lib().grt_sweep_kmax(ctx.h, ctypes.byref(model), ctypes.byref(opts), len(fi),
                                   fi.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(br), _ptr(br), float(tol),
-                                  _ptr(kj) if kj is not None else None, _ptr(kmax),
-                                  _ptr(tail) if tail is not None else None, _ptr(dk))
+                                  _ptr(ta) if ta is not None else None, _ptr(kj) if kj is not None else None,
+                                  _ptr(out["kmax"]), opt("tail"), opt("env"), opt("alias"))
         if rc:
             raise GrtError(rc, ctx.error())
     finally:
         if own:
             ctx.close()
-    return kmax, tail, dk
+    return out
 
 
 def run(model, opts, dists, ctx=None, spectra=False):

@@ -41,7 +41,7 @@ struct grt_plan {
     void *tab = nullptr, *K = nullptr, *B = nullptr, *S = nullptr, *post = nullptr, *tw = nullptr;
     void *spec = nullptr, *sig = nullptr;
     int2 *tiles = nullptr;
-    int *nk = nullptr;
+    int *nk = nullptr, *ks = nullptr;
     long long *koff = nullptr;
     double *ddist = nullptr, *damp = nullptr;
     unsigned *derr = nullptr;
@@ -109,7 +109,7 @@ extern "C" void grt_plan_destroy(grt_plan *p)
     if (!p) return;
     cudaSetDevice(p->ctx->device);
     void *bufs[] = {p->tab, p->K, p->B, p->S, p->post, p->tw, p->spec, p->sig, p->tiles, p->nk, p->koff, p->ddist,
-                    p->damp, p->derr, p->P, p->Kt, p->kt_base};
+                    p->damp, p->derr, p->P, p->Kt, p->kt_base, p->ks};
     for (void *b : bufs)
         if (b) cudaFree(b);
     delete p;
@@ -165,12 +165,13 @@ static int upload(grt_plan *p)
         for (int j0 = 0; j0 < J.nk[iw]; j0 += grt::kGrtThreads) tiles.push_back(make_int2(iw, j0));
     p->ntiles = (int)tiles.size();
     const size_t szK = (size_t)p->nq * J.nkw * 2 * sizeof(R);
-    const size_t szB = (size_t)J.nkmax * grt::NBASIS * p->nd * sizeof(R);
+    const size_t szB = (size_t)J.nbrow * grt::NBASIS * p->nd * sizeof(R);
     const size_t ntr = (size_t)p->nd * p->nc;
     CU(cudaMalloc(&p->tab, tab.size() * sizeof(tab[0])));
     CU(cudaMalloc(&p->tiles, tiles.size() * sizeof(int2)));
     CU(cudaMalloc(&p->nk, J.nw * sizeof(int)));
     CU(cudaMalloc(&p->koff, J.nw * sizeof(long long)));
+    CU(cudaMalloc(&p->ks, J.nw * sizeof(int)));
     CU(cudaMalloc(&p->ddist, p->nd * sizeof(double)));
     if (!p->use_tc) CU(cudaMalloc(&p->K, szK));
     CU(cudaMalloc(&p->B, szB));
@@ -225,13 +226,14 @@ static int upload(grt_plan *p)
     CU(cudaMemcpyAsync(p->tiles, tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(p->nk, J.nk.data(), J.nw * sizeof(int), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(p->koff, J.koff.data(), J.nw * sizeof(long long), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(p->ks, J.ks.data(), J.nw * sizeof(int), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(p->ddist, p->dist.data(), p->nd * sizeof(double), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(p->post, post.data(), post.size() * sizeof(R), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(p->tw, tw.data(), tw.size() * sizeof(R), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(p->damp, damp.data(), damp.size() * sizeof(double), cudaMemcpyHostToDevice, st));
     CU(cudaMemsetAsync(p->derr, 0, sizeof(unsigned), st));
     p->rep.h2d_bytes = (long long)(tab.size() * sizeof(tab[0]) + tiles.size() * sizeof(int2) +
-                                   J.nw * (sizeof(int) + sizeof(long long)) + p->nd * sizeof(double) +
+                                   J.nw * (2 * sizeof(int) + sizeof(long long)) + p->nd * sizeof(double) +
                                    (post.size() + tw.size()) * sizeof(R) + damp.size() * sizeof(double));
     p->rep.d2h_bytes = (long long)(ntr * J.N * sizeof(R));
     CU(cudaStreamSynchronize(st));
@@ -253,7 +255,7 @@ extern "C" int grt_plan_create(grt_ctx *ctx, const grt_model *m, const grt_opts 
                                   p->J, err);
     if (!rc)
         rc = grt::job_setup(p->J, o->dt, o->log2n, o->t0, o->taper, o->sigma_factor, o->k_mode, o->nk_fixed, o->dk,
-                            o->fix, err, o->nk_custom);
+                            o->fix, err, o->nk_custom, o->k_stride);
     if (rc) return set_err(ctx, rc, err);
     const Job &J = p->J;
     p->prec = o->precision;
@@ -273,6 +275,12 @@ extern "C" int grt_plan_create(grt_ctx *ctx, const grt_model *m, const grt_opts 
     const char *ks = getenv("GRT_KSUM");
     p->use_tc = (p->prec == GRT_FP32) && !(ks && !strcmp(ks, "simt"));
     p->rep.ksum_impl = p->use_tc;
+    // the tensor-core sum multiplies a tile of 64 frequencies by one Bessel operand:
+    // the frequencies of a tile share their k stride
+    if (p->use_tc)
+        for (int iw = 0; iw < J.nw; iw++)
+            if (J.ks[iw] != J.ks[iw - iw % grt::tc::kW])
+                return set_err(ctx, GRT_ERR_ARG, "k_stride must be constant on each aligned block of 64 frequencies");
     CU(cudaSetDevice(ctx->device));
     rc = p->prec ? upload<double>(p.get()) : upload<float>(p.get());
     if (rc) {
@@ -293,6 +301,7 @@ static int launch_ksum_tc(grt_plan *p, cudaStream_t st, int &launches)
     T.kt_base = p->kt_base;
     T.B = (const float *)p->B;
     T.nk = p->nk;
+    T.ks = p->ks;
     T.koff = p->koff;
     T.dist = p->ddist;
     T.P = (float *)p->P;
@@ -337,6 +346,7 @@ static int execute(grt_plan *p)
     A.tab = (const grt::LayerW<R> *)p->tab;
     A.tiles = p->tiles;
     A.nk = p->nk;
+    A.ks = p->ks;
     A.koff = p->koff;
     A.K = (R *)p->K;
     A.nkw = J.nkw;
@@ -358,9 +368,9 @@ static int execute(grt_plan *p)
     CU(cudaEventRecord(ctx->ev[1], st));
     // 2. Bessel table
     {
-        long long n = (long long)J.nkmax * p->nd;
+        long long n = (long long)J.nbrow * p->nd;
         int blocks = (int)((n + 255) / 256);
-        grt::bessel_table_kernel<R><<<blocks, 256, 0, st>>>((R *)p->B, J.nkmax, p->nd, J.dk, p->ddist);
+        grt::bessel_table_kernel<R><<<blocks, 256, 0, st>>>((R *)p->B, J.nbrow, p->nd, J.dk, p->ddist);
         launches++;
         CU(cudaGetLastError());
     }
@@ -374,7 +384,7 @@ static int execute(grt_plan *p)
     }
     if (!p->use_tc) {
         grt::KsumArgs<R> S{};
-        S.K = (const R *)p->K; S.B = (const R *)p->B; S.nk = p->nk; S.koff = p->koff; S.dist = p->ddist;
+        S.K = (const R *)p->K; S.B = (const R *)p->B; S.nk = p->nk; S.ks = p->ks; S.koff = p->koff; S.dist = p->ddist;
         S.S = (R *)p->S; S.nkw = J.nkw; S.dk = J.dk; S.nw = J.nw; S.nr = p->nd; S.rt = p->rt; S.jt = p->jt;
         int grid = J.nw * ((p->nd + p->rt - 1) / p->rt);
         if (J.src == 0) grt::ksum_kernel<R, grt::kSingle><<<grid, grt::kSumThreads, 0, st>>>(S);
@@ -445,7 +455,7 @@ extern "C" int grt_grid(const grt_model *m, const grt_opts *o, grt_report *r)
                                   J, err);
     if (!rc)
         rc = grt::job_setup(J, o->dt, o->log2n, o->t0, o->taper, o->sigma_factor, o->k_mode, o->nk_fixed, o->dk,
-                            o->fix, err, o->nk_custom);
+                            o->fix, err, o->nk_custom, o->k_stride);
     if (rc) {
         fprintf(stderr, "grt_grid: %s\n", err.c_str());
         return rc;
@@ -538,20 +548,44 @@ extern "C" int grt_plan_fetch(grt_plan *p, double *traces, double *spectra)
 }
 
 // ------------------------------------------------------------------ convergence sweep
-// One thread per (selected frequency, distance band): envelope of the weighted
-// integrand g(k) = max_q |K_q(w,k)| (1+k)^2 min(1, (k r)^-1/2), its total, and
-// the smallest k_c whose tail sum_{k >= k_c} g stays within tol of the total;
-// also the tail fraction at a given wavenumber (a prediction to judge), and
-// the coarsest step dk*s (s = 1, 2, 4, .., 32) whose sums
-// s dk sum_{j = 0 mod s} K_q(j dk) J0(j dk r) agree with the full-grid sums
-// within tol for every column q (the step's spatial aliasing at distance r).
+// One block per (selected frequency, distance band): envelope of the weighted
+// integrand g(k) = max_q |K_q(w,k)| (1+k)^2 min(1, (k r)^-1/2) and its total;
+// the smallest k_c whose tail sum_{k >= k_c} g stays within a threshold (tol
+// times the total, or an absolute threshold per pair); the tail fraction at
+// a given wavenumber (a prediction to judge); and, if asked, the aliasing of
+// coarser steps: with S_q^(s) = s dk sum_{j = 0 mod s, j < k_c/dk} K_q(j dk)
+// J0(j dk r), alias[0] = max_q |S_q^(1)| and alias[s] = max_q |S_q^(2^s) -
+// S_q^(1)| for s = 1..5 (the step's spatial aliasing at distance r).
 constexpr int kStrides = 6;
+constexpr int kSweepThreads = 128;
 
-__global__ void sweep_kmax_kernel(const float *K, long long nkw, int nq, const int *nk, const long long *koff,
-                                  const int *fidx, int nf, const double *band_r, int nb, double dk, double tol,
-                                  const double *kjudge, double *kmax_out, double *tail_out, double *dk_out)
+__device__ double block_sum(double v, double *red)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    red[threadIdx.x] = v;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+        __syncthreads();
+    }
+    const double r = red[0];
+    __syncthreads();
+    return r;
+}
+
+struct SweepOut {
+    const double *tol_abs, *kjudge;
+    double *kmax, *tail, *env, *alias;
+};
+
+__global__ void __launch_bounds__(kSweepThreads) sweep_kmax_kernel(
+    const float *K, long long nkw, int nq, const int *nk, const long long *koff, const int *fidx, int nf,
+    const double *band_r, int nb, double dk, double tol, SweepOut O)
+{
+    __shared__ double red[kSweepThreads];
+    __shared__ double chunk[kSweepThreads + 1];   // suffix sums of the threads' chunks
+    __shared__ int jc_s;
+    __shared__ double tail_at_s;
+    const int t = blockIdx.x;
     if (t >= nf * nb) return;
     const int f = t / nb, b = t % nb, iw = fidx[f];
     const int n = nk[iw];
@@ -567,60 +601,91 @@ __global__ void sweep_kmax_kernel(const float *K, long long nkw, int nq, const i
         const double k = dk * j, kr = k * r;
         return (double)m * (1.0 + k) * (1.0 + k) * (kr > 1.0 ? 1.0 / sqrt(kr) : 1.0);
     };
-    double tot = 0.0;
-    for (int j = 0; j < n; j++) tot += g(j);
-    double tail = 0.0, tail_at = 0.0;
-    int jc = 0;
-    const int jj = kjudge ? (int)ceil(kjudge[t] / dk) : n;
-    bool found = false;
-    for (int j = n - 1; j >= 0; j--) {
-        tail += g(j);
-        if (j == jj) tail_at = tail;
-        if (!found && tail > tol * tot) {
-            jc = j + 1;
-            found = true;
-        }
+    // thread c owns the contiguous chunk [c n / T, (c + 1) n / T)
+    const int T = blockDim.x, c = threadIdx.x;
+    const int j0 = (int)((long long)c * n / T), j1 = (int)((long long)(c + 1) * n / T);
+    double s = 0.0;
+    for (int j = j0; j < j1; j++) s += g(j);
+    chunk[c] = s;
+    __syncthreads();
+    if (c == 0) {
+        chunk[T] = 0.0;
+        for (int i = T - 1; i >= 0; i--) chunk[i] += chunk[i + 1];   // chunk[i] = sum over chunks >= i
+        jc_s = 0;
+        tail_at_s = 0.0;
     }
-    kmax_out[t] = dk * (found ? jc : 0);
-    if (tail_out) tail_out[t] = (tot > 0 && jj < n) ? tail_at / tot : 0.0;
-    if (!dk_out) return;
-    // stride test; sums run over the grid up to k_c (the part a sampler keeps)
-    const int ne = found ? jc : n;
+    __syncthreads();
+    const double tot = chunk[0];
+    const double thr = O.tol_abs ? O.tol_abs[t] : tol * tot;
+    // the crossing tail(j) > thr lies in the last chunk whose suffix exceeds it
+    if (chunk[c] > thr && !(chunk[c + 1] > thr)) {
+        double tail = chunk[c + 1];
+        int jc = j0;
+        for (int j = j1 - 1; j >= j0; j--) {
+            tail += g(j);
+            if (tail > thr) { jc = j + 1; break; }
+        }
+        jc_s = jc;
+    }
+    const int jj = O.kjudge ? (int)ceil(O.kjudge[t] / dk) : n;
+    if (jj < n && jj >= j0 && jj < j1) {
+        double tail = chunk[c + 1];
+        for (int j = j1 - 1; j >= jj; j--) tail += g(j);
+        tail_at_s = tail;
+    }
+    __syncthreads();
+    const int jc = jc_s;
+    if (c == 0) {
+        O.kmax[t] = dk * jc;
+        if (O.tail) O.tail[t] = (tot > 0 && jj < n) ? tail_at_s / tot : 0.0;
+        if (O.env) O.env[t] = tot;
+    }
+    if (!O.alias) return;
+    // stride sums over the grid up to k_c (the part a sampler keeps)
+    const int ne = jc > 0 ? jc : n;
     double emax[kStrides] = {}, ref = 0.0;
     for (int q = 0; q < nq; q++) {
         double sx[kStrides] = {}, sy[kStrides] = {};
-        for (int j = 0; j < ne; j++) {
+        for (int j = c; j < ne; j += T) {
             const grt::C<float> v = Kc[(long long)q * nkw + off + j];
-            const double w = (j == 0 ? 0.5 : 1.0) * grt::bj0_ref(dk * j * r);
+            const double w = (j == 0 ? 0.5 : 1.0) * dk * grt::bj0_ref(dk * j * r);
             const double x = w * v.x, y = w * v.y;
 #pragma unroll
-            for (int s = 0; s < kStrides; s++)
-                if ((j & ((1 << s) - 1)) == 0) {
-                    sx[s] += x * (1 << s);
-                    sy[s] += y * (1 << s);
+            for (int st = 0; st < kStrides; st++)
+                if ((j & ((1 << st) - 1)) == 0) {
+                    sx[st] += x * (1 << st);
+                    sy[st] += y * (1 << st);
                 }
         }
+#pragma unroll
+        for (int st = 0; st < kStrides; st++) {
+            sx[st] = block_sum(sx[st], red);
+            sy[st] = block_sum(sy[st], red);
+        }
         ref = fmax(ref, hypot(sx[0], sy[0]));
-        for (int s = 1; s < kStrides; s++) emax[s] = fmax(emax[s], hypot(sx[s] - sx[0], sy[s] - sy[0]));
+        for (int st = 1; st < kStrides; st++) emax[st] = fmax(emax[st], hypot(sx[st] - sx[0], sy[st] - sy[0]));
     }
-    int sbest = 0;
-    for (int s = 1; s < kStrides && emax[s] <= tol * ref && (ne >> s) >= 8; s++) sbest = s;
-    dk_out[t] = dk * (1 << sbest);
+    if (c == 0) {
+        O.alias[(long long)t * kStrides] = ref;
+        for (int st = 1; st < kStrides; st++) O.alias[(long long)t * kStrides + st] = emax[st];
+    }
 }
 
 extern "C" int grt_sweep_kmax(grt_ctx *ctx, const grt_model *m, const grt_opts *o, int n_freq, const int *freq_idx,
-                              int n_band, const double *band_r, double tol, const double *k_judge, double *kmax_out,
-                              double *tail_out, double *dk_out)
+                              int n_band, const double *band_r, double tol, const double *tol_abs,
+                              const double *k_judge, double *kmax_out, double *tail_out, double *env_out,
+                              double *alias_out)
 {
     if (!ctx || !m || !o || !freq_idx || !band_r || !kmax_out || n_freq < 1 || n_band < 1 || !(tol > 0))
         return set_err(ctx, GRT_ERR_ARG, "bad sweep arguments");
+    if (o->k_stride) return set_err(ctx, GRT_ERR_ARG, "sweeps run on a unit-stride grid (k_stride must be NULL)");
     Job J;
     std::string err;
     int rc = grt::job_from_layers(m->n_layer, m->ztop, m->vp, m->vs, m->rho, m->qp, m->qs, m->hs, m->hr, m->src_type,
                                   J, err);
     if (!rc)
         rc = grt::job_setup(J, o->dt, o->log2n, o->t0, o->taper, o->sigma_factor, o->k_mode, o->nk_fixed, o->dk,
-                            o->fix, err, o->nk_custom);
+                            o->fix, err, o->nk_custom, o->k_stride);
     if (rc) return set_err(ctx, rc, err);
     // keep only the selected frequencies: compact coefficient offsets, tiles for them alone
     std::vector<int> nk_sel(J.nw, 0);
@@ -656,9 +721,12 @@ extern "C" int grt_sweep_kmax(grt_ctx *ctx, const grt_model *m, const grt_opts *
     void *d_nk = dalloc(J.nw * sizeof(int)), *d_koff = dalloc(J.nw * sizeof(long long));
     void *d_K = dalloc((size_t)nq * tot * 2 * sizeof(float)), *d_err = dalloc(sizeof(unsigned));
     void *d_f = dalloc(n_freq * sizeof(int)), *d_r = dalloc(n_band * sizeof(double));
-    void *d_out = dalloc((size_t)n_freq * n_band * 3 * sizeof(double));
-    void *d_judge = k_judge ? dalloc((size_t)n_freq * n_band * sizeof(double)) : nullptr;
-    if (!d_tab || !d_tiles || !d_nk || !d_koff || !d_K || !d_err || !d_f || !d_r || !d_out || (k_judge && !d_judge))
+    const size_t nt_ = (size_t)n_freq * n_band;
+    void *d_out = dalloc(nt_ * (3 + kStrides) * sizeof(double));
+    void *d_judge = k_judge ? dalloc(nt_ * sizeof(double)) : nullptr;
+    void *d_tabs = tol_abs ? dalloc(nt_ * sizeof(double)) : nullptr;
+    if (!d_tab || !d_tiles || !d_nk || !d_koff || !d_K || !d_err || !d_f || !d_r || !d_out || (k_judge && !d_judge) ||
+        (tol_abs && !d_tabs))
         return set_err(ctx, GRT_ERR_NOMEM, "sweep buffers");
     cudaStream_t st = ctx->stream;
     CU(cudaMemcpyAsync(d_tab, tab.data(), tab.size() * sizeof(tab[0]), cudaMemcpyHostToDevice, st));
@@ -667,7 +735,8 @@ extern "C" int grt_sweep_kmax(grt_ctx *ctx, const grt_model *m, const grt_opts *
     CU(cudaMemcpyAsync(d_koff, koff.data(), J.nw * sizeof(long long), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(d_f, freq_idx, n_freq * sizeof(int), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(d_r, band_r, n_band * sizeof(double), cudaMemcpyHostToDevice, st));
-    if (k_judge) CU(cudaMemcpyAsync(d_judge, k_judge, (size_t)n_freq * n_band * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (k_judge) CU(cudaMemcpyAsync(d_judge, k_judge, nt_ * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (tol_abs) CU(cudaMemcpyAsync(d_tabs, tol_abs, nt_ * sizeof(double), cudaMemcpyHostToDevice, st));
     CU(cudaMemsetAsync(d_err, 0, sizeof(unsigned), st));
     grt::GrtArgs<float> A{};
     A.tab = (const grt::LayerW<float> *)d_tab;
@@ -693,15 +762,21 @@ extern "C" int grt_sweep_kmax(grt_ctx *ctx, const grt_model *m, const grt_opts *
     grt::grt_point_kernel<float><<<(unsigned)tiles.size(), grt::kGrtThreads, (size_t)J.L * sizeof(grt::LayerW<float>), st>>>(A);
     CU(cudaGetLastError());
     const int nt = n_freq * n_band;
-    double *o_k = (double *)d_out, *o_t = (double *)d_out + nt, *o_d = dk_out ? (double *)d_out + 2 * nt : nullptr;
-    sweep_kmax_kernel<<<(nt + 127) / 128, 128, 0, st>>>((const float *)d_K, tot, nq, (const int *)d_nk,
-                                                        (const long long *)d_koff, (const int *)d_f, n_freq,
-                                                        (const double *)d_r, n_band, J.dk, tol,
-                                                        (const double *)d_judge, o_k, o_t, o_d);
+    SweepOut O{};
+    O.tol_abs = (const double *)d_tabs;
+    O.kjudge = (const double *)d_judge;
+    O.kmax = (double *)d_out;
+    O.tail = tail_out ? (double *)d_out + nt : nullptr;
+    O.env = env_out ? (double *)d_out + 2 * nt : nullptr;
+    O.alias = alias_out ? (double *)d_out + 3 * nt : nullptr;
+    sweep_kmax_kernel<<<nt, kSweepThreads, 0, st>>>((const float *)d_K, tot, nq, (const int *)d_nk,
+                                                    (const long long *)d_koff, (const int *)d_f, n_freq,
+                                                    (const double *)d_r, n_band, J.dk, tol, O);
     CU(cudaGetLastError());
-    CU(cudaMemcpyAsync(kmax_out, o_k, nt * sizeof(double), cudaMemcpyDeviceToHost, st));
-    if (tail_out) CU(cudaMemcpyAsync(tail_out, o_t, nt * sizeof(double), cudaMemcpyDeviceToHost, st));
-    if (dk_out) CU(cudaMemcpyAsync(dk_out, o_d, nt * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(kmax_out, O.kmax, nt * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (tail_out) CU(cudaMemcpyAsync(tail_out, O.tail, nt * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (env_out) CU(cudaMemcpyAsync(env_out, O.env, nt * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (alias_out) CU(cudaMemcpyAsync(alias_out, O.alias, (size_t)nt * kStrides * sizeof(double), cudaMemcpyDeviceToHost, st));
     unsigned herr = 0;
     CU(cudaMemcpyAsync(&herr, d_err, sizeof herr, cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));

@@ -261,8 +261,9 @@ constexpr int kSumChunk = 16;   // k-steps accumulated plainly before a compensa
 template <typename R>
 struct KsumArgs {
     const R *K;            // [nq][nkw] complex
-    const R *B;            // [nkmax][NBASIS][nr]
+    const R *B;            // [nbrow][NBASIS][nr], row i at k = i dk
     const int *nk;         // [nw]
+    const int *ks;         // [nw] k stride m: frequency iw sums k_j = j m dk (null: 1)
     const long long *koff; // [nw]
     const double *dist;    // [nr]
     R *S;                  // [nr][nc][nw] complex
@@ -299,7 +300,8 @@ __global__ void __launch_bounds__(kSumThreads) ksum_kernel(KsumArgs<R> A)
     R hi[NC][2], lo[NC][2];
 #pragma unroll
     for (int c = 0; c < NC; c++) hi[c][0] = hi[c][1] = lo[c][0] = lo[c][1] = R(0);
-    const R dk = (R)A.dk, dk_half = (R)(0.5 * A.dk);
+    const int m = A.ks ? A.ks[iw] : 1;
+    const R dk = (R)(A.dk * m), dk_half = (R)(0.5 * A.dk * m);
 
     for (int jb = lane * kSumChunk; jb < nk; jb += A.jt * kSumChunk) {
         R acc[NC][2];
@@ -311,7 +313,7 @@ __global__ void __launch_bounds__(kSumThreads) ksum_kernel(KsumArgs<R> A)
             const R k = dk * (R)j;
             const R w = (j == 0) ? dk_half : dk;
             const R wk[3] = {w, w * k, w * k * k};
-            const R *Bj = A.B + (long long)j * NBASIS * A.nr + rr;
+            const R *Bj = A.B + (long long)j * m * NBASIS * A.nr + rr;
             R bv[NBASIS];
 #pragma unroll
             for (int b = 0; b < NBASIS; b++) bv[b] = Bj[(long long)b * A.nr];

@@ -119,8 +119,10 @@ static double cal_kmax(const Job &J, cd w, const std::vector<cd> &b, int nf)
 }
 
 int job_setup(Job &J, double dt, int log2n, double t0, double taper, double sigma_factor, int k_mode,
-              int nk_fixed, double dk_override, int fix, std::string &err, const int *nk_custom)
+              int nk_fixed, double dk_override, int fix, std::string &err, const int *nk_custom,
+              const int *k_stride)
 {
+    if (k_stride && k_mode != 2) { err = "a k stride needs a custom grid (nk_custom)"; return kErrArg; }
     if (k_mode == 2 && !nk_custom) { err = "custom k grid needs nk_custom"; return kErrArg; }
     if (k_mode < 0 || k_mode > 2) { err = "unknown k grid mode"; return kErrArg; }
     if (!(dt > 0) || log2n < 2 || log2n > 15) { err = "need dt > 0 and 2 <= log2n <= 15"; return kErrArg; }
@@ -159,6 +161,8 @@ int job_setup(Job &J, double dt, int log2n, double t0, double taper, double sigm
     // wavenumber grid: ragged per-frequency k_max (green.cu:2145-2194) or fixed
     J.nk.assign(J.nw, 0);
     J.koff.assign(J.nw, 0);
+    J.ks.assign(J.nw, 1);
+    J.nbrow = 0;
     long long tot = 0;
     J.nkmax = 0;
     std::vector<cd> b(J.L);
@@ -177,10 +181,16 @@ int job_setup(Job &J, double dt, int log2n, double t0, double taper, double sigm
             km *= 1.1;  // k_factor, green.cu:2063
             nk = (int)(km / J.dk) + 2;
         }
+        if (k_stride) {
+            if (k_stride[iw] < 1 || k_stride[iw] > 64) { err = "k stride must be in 1..64"; return kErrArg; }
+            J.ks[iw] = k_stride[iw];
+        }
+        if ((long long)(nk - 1) * J.ks[iw] + 1 > (1 << 24)) { err = "custom k grid: (nk - 1) * stride too large"; return kErrArg; }
         J.nk[iw] = nk;
         J.koff[iw] = tot;
         tot += nk;
         J.nkmax = std::max(J.nkmax, nk);
+        J.nbrow = std::max(J.nbrow, (nk - 1) * J.ks[iw] + 1);
     }
     J.nkw = tot;
     return kOk;

@@ -28,6 +28,8 @@ struct Job {
     std::vector<long long> koff;                 // prefix sums of nk
     long long nkw = 0;
     int nkmax = 0;
+    std::vector<int> ks;                         // per frequency k stride m: k_j = j m dk
+    int nbrow = 0;                               // Bessel-table rows: max (nk - 1) m + 1
 };
 
 // status codes (the public header repeats them)
@@ -48,6 +50,7 @@ int job_from_layers(int n, const double *ztop, const double *vp, const double *v
                     std::string &err);
 // Grid, layer location and k grid.  sigma = sigma_factor / T (reference: 2).
 int job_setup(Job &J, double dt, int log2n, double t0, double taper, double sigma_factor, int k_mode,
-              int nk_fixed, double dk_override, int fix, std::string &err, const int *nk_custom = nullptr);
+              int nk_fixed, double dk_override, int fix, std::string &err, const int *nk_custom = nullptr,
+              const int *k_stride = nullptr);
 
 }  // namespace grt

@@ -327,11 +327,14 @@ __global__ void __launch_bounds__(kGrtThreads, GRT_POINT_MINB) grt_point_kernel(
             "l"(src), "r"(bytes), "r"(sbar)
             : "memory");
     }
+    // lanes past the frequency's last wavenumber leave now (no block-wide
+    // synchronisation follows; lane 0 of a tile is always valid and waits
+    // for the table copy it issued): evaluating them would hold their warps
+    if (j >= A.nk[iw]) return;
     if (!mbar_wait(sbar, 0, A.err)) return;
 
-    const bool valid = j < A.nk[iw];
-    const int jj = valid ? j : 0;           // idle lanes compute k = 0 and store nothing
-    const double kd = A.dk * jj;
+    const int jj = j;
+    const double kd = A.dk * (A.ks ? A.ks[iw] : 1) * jj;
     K2<R> k2;
     make_k2(kd * kd, k2);
     const R k = (R)kd;
@@ -557,7 +560,6 @@ __global__ void __launch_bounds__(kGrtThreads, GRT_POINT_MINB) grt_point_kernel(
         y1t = Utrec * yp1;
     }
 
-    if (!valid) return;
     const KOut out = make_kout(A, iw, j);
     if (A.src == kSingle) {
         C<R> f0a = -(S.d0 * iG * R(0.5)), f0b = C<R>{k, R(0)} * iG * R(0.5);

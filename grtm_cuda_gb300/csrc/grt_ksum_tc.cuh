@@ -125,8 +125,9 @@ template <typename R>
 struct KsumTcArgs {
     const float *Kt;         // operand blocks written by the GRT kernel (see GrtArgs::Kt)
     const long long *kt_base;
-    const float *B;          // [nkmax][NBASIS][nr]
+    const float *B;          // [nbrow][NBASIS][nr], row i at k = i dk
     const int *nk;           // [nw]
+    const int *ks;           // [nw] k stride, constant on each tile of kW frequencies (null: 1)
     const long long *koff;   // [nw]
     const double *dist;      // [nr]
     float *P;                // partial sums [nsplit][nr][nc][nw] complex
@@ -205,7 +206,8 @@ __global__ void __launch_bounds__(tc::kThreads, 1) ksum_tc_kernel(KsumTcArgs<flo
         const bool rok = (r0 + br) < A.nr;
         const double drr = A.dist[rg];
         const float ir = (float)(1.0 / drr), ir2 = (float)(1.0 / (drr * drr));
-        const float dk = (float)A.dk;
+        const int ksm = A.ks ? A.ks[w0] : 1;
+        const float dk = (float)(A.dk * ksm);
         const unsigned a_bytes = (unsigned)(NQ * 2 * kATileBytes);
         const float *kt_tile = A.Kt + A.kt_base[wt];
         // Bessel values of the next stage, loaded one stage ahead
@@ -214,7 +216,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) ksum_tc_kernel(KsumTcArgs<flo
             const int k = kb + st_ * kKT + bk;
             const bool kok = st_ < nstage && k < ke && rok;
 #pragma unroll
-            for (int b = 0; b < NBASIS; b++) bv[b] = kok ? __ldg(A.B + ((long long)k * NBASIS + b) * A.nr + rg) : 0.f;
+            for (int b = 0; b < NBASIS; b++) bv[b] = kok ? __ldg(A.B + ((long long)k * ksm * NBASIS + b) * A.nr + rg) : 0.f;
         };
         load_b(0);
         for (int st = 0; st < nstage; st++) {

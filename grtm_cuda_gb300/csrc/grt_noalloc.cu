@@ -83,6 +83,7 @@ extern "C" GRT_API int grt_run_noalloc(int device, const grt_model *m, const grt
     }
     unsigned char *scratch = (unsigned char *)g_scratch_addr[device];
 
+    if (o->k_mode == GRT_K_CUSTOM || o->k_stride) return fail(GRT_ERR_UNSUPPORTED, "custom k grids need grt_run");
     // the job on the host (same rules as grt_run)
     Job J;
     std::string err;

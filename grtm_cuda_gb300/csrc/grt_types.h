@@ -41,6 +41,7 @@ struct GrtArgs {
     const LayerW<R> *tab;      // [nw][L]
     const int2 *tiles;         // (iw, j0) per block
     const int *nk;             // [nw]
+    const int *ks;             // [nw] k stride m: k_j = j m dk (null: 1)
     const long long *koff;     // [nw] offset of frequency iw in the flattened (w,k) list
     R *K;                      // [nq][nkw] complex (re, im)
     long long nkw;

@@ -18,10 +18,10 @@ stored beside the weights.
 
 The plain fixed grid is both fallback and judge of every prediction: before
 its result is used, the integrand tail beyond the predicted k_max is measured
-on the plain grid at a few spot frequencies and distances, the step is checked
-by the same sweep's aliasing test, and the spectra of every receiver at the
-spot frequencies are compared with the plain grid's.  A receiver that fails
-is recomputed on the plain grid.
+on the plain grid at a few spot frequencies and distances, and the spectra of
+every receiver at the spot frequencies (which carry any aliasing of a coarser
+step at that receiver's distance) are compared with the plain grid's.  A
+receiver that fails is recomputed on the plain grid.
 
 No counterpart in the reference.
 """
@@ -33,16 +33,35 @@ import time
 
 import numpy as np
 
-from . import (Context, GrtError, K_CUSTOM, K_FIXED, FP32, Plan, grid, lib, make_model, make_opts, sweep_kmax,
-               synth)
+from . import FIX_ALL, K_FIXED, Context, GrtError, Plan, grid, lib, make_model, make_opts, sweep_kmax, synth
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 WEIGHTS = os.path.join(HERE, "data", "ksampler.bin")
 N_FEAT, N_IN, N_OUT = 12, 15, 2
 MAGIC = b"GRTKSMP1"
 
-# the plain grid the sampler is trained against and judged by
-PLAIN = dict(dt=0.05, log2n=13, nk=32768, sigma_factor=math.pi, taper=0.3, t0=0.0)
+# the plain grid the sampler is trained against and judged by.  Synthetic
+# models run with the reference's quirks corrected (FIX_ALL): with its
+# receiver-layer search (green.cu:2092-2101) a surface receiver whose source
+# sits deeper in its layer than the top layer is thick lands at a negative
+# depth in a deeper layer, and the field grows like e^{nu |z|} (overflow).
+PLAIN = dict(dt=0.05, log2n=13, nk=32768, sigma_factor=math.pi, taper=0.3, t0=0.0, fix=FIX_ALL)
+
+
+def plain_opts(plain=PLAIN, **over):
+    """Options of the plain fixed grid (keyword overrides, e.g. precision)."""
+    kw = dict(t0=plain["t0"], taper=plain["taper"], sigma_factor=plain["sigma_factor"], k_mode=K_FIXED,
+              nk_fixed=plain["nk"], fix=plain["fix"])
+    kw.update(over)
+    return make_opts(plain["dt"], plain["log2n"], **kw)
+
+
+def custom_opts(nk, dk, plain=PLAIN, **over):
+    """Options of a ragged grid nk[w] with step dk, otherwise as the plain grid."""
+    kw = dict(t0=plain["t0"], taper=plain["taper"], sigma_factor=plain["sigma_factor"], dk=dk, nk_custom=nk,
+              fix=plain["fix"])
+    kw.update(over)
+    return make_opts(plain["dt"], plain["log2n"], **kw)
 
 
 def layer_features(m):
@@ -144,7 +163,38 @@ class Mlp:
 
 
 # ---------------------------------------------------------------- training data
-def sweep_dataset(ctx, seeds, n_freq=32, n_band=8, tol=1e-4, plain=PLAIN, rng_seed=0, n_layers=40):
+def taper_weight(iw, nw, taper):
+    """The cosine taper the spectral stage applies at frequency index iw
+    (green.cu:1909-1921)."""
+    iw = np.asarray(iw, np.float64)
+    wc = int(nw * (1 - taper))
+    w = 0.5 * (1 + np.cos((iw - wc + 1) * math.pi / (nw - wc + 1)))
+    return np.where(iw > wc, w, 1.0)
+
+
+def sweep_targets(ctx, model, opts, fi, br, tol, nw, taper):
+    """Targets of the sampler at frequencies fi and distances br.
+
+    The cutoff k_c(w, r) keeps the envelope tail beyond it below tol times
+    the envelope's peak over the sampled frequencies at that distance,
+    relative to the taper weight of w (a frequency the taper removes needs
+    no integral); the step multiple 2^s(w, r) is the coarsest whose
+    aliasing error stays below tol times that frequency's own k-sum
+    magnitude (aliasing is not averaged away across frequencies: it shifts
+    energy in time).  Two sweeps: totals and aliasing, then the cutoffs at
+    those absolute thresholds."""
+    s1 = sweep_kmax(model, opts, fi, br, tol, ctx=ctx, env=True, alias=True)
+    w = np.maximum(taper_weight(fi, nw, taper), 1e-6)[:, None]
+    thr = tol * s1["env"].max(0)[None, :] / w
+    kmax = sweep_kmax(model, opts, fi, br, tol, tol_abs=thr, ctx=ctx)["kmax"]
+    al = s1["alias"]
+    ok = al[..., 1:] <= tol * al[..., :1]                       # [f, b, 5]
+    # coarsest s with every finer stride passing too
+    l2 = np.cumprod(ok, axis=2).sum(axis=2)
+    return kmax, l2, s1
+
+
+def sweep_dataset(ctx, seeds, n_freq=8, n_band=8, tol=1e-4, plain=PLAIN, rng_seed=0, n_layers=40):
     """Convergence sweeps of the plain grid on seeded crustal models
     (n_layers layers, source depth U(1, 30) km), n_freq frequencies (log-
     uniform) x n_band distances (log-uniform in 1-500 km) per model.
@@ -154,19 +204,18 @@ def sweep_dataset(ctx, seeds, n_freq=32, n_band=8, tol=1e-4, plain=PLAIN, rng_se
     for seed in seeds:
         m = synth.crust(np.random.default_rng(seed), n_layers, rng.uniform(1.0, 30.0))
         model = make_model(**m)
-        opts = make_opts(plain["dt"], plain["log2n"], t0=plain["t0"], taper=plain["taper"],
-                         sigma_factor=plain["sigma_factor"], k_mode=K_FIXED, nk_fixed=plain["nk"])
+        opts = plain_opts(plain)
         gr = grid(model, opts)
         nw, dkp, df = gr["nw"], gr["dk"], gr["df"]
         fi = np.unique(np.round(np.exp(rng.uniform(0.0, math.log(nw - 1), 4 * n_freq))).astype(np.int64))
         fi = np.sort(rng.choice(fi, size=min(n_freq, len(fi)), replace=False))
         br = np.exp(rng.uniform(math.log(1.0), math.log(500.0), n_band))
-        kmax, _, dk = sweep_kmax(model, opts, fi, br, tol, ctx=ctx)
+        kmax, l2, _ = sweep_targets(ctx, model, opts, fi, br, tol, nw, plain["taper"])
         feat = layer_features(m)
         om = (2 * math.pi * df * fi)[:, None] * np.ones((1, n_band))
         rr = np.ones((len(fi), 1)) * br[None, :]
         X.append(net_inputs(feat, om.ravel(), rr.ravel(), m["hs"]))
-        Y.append(np.stack([np.log(np.maximum(kmax.ravel(), 4 * dkp)), np.log2(dk.ravel() / dkp)], axis=1))
+        Y.append(np.stack([np.log(np.maximum(kmax.ravel(), 4 * dkp)), l2.ravel().astype(np.float64)], axis=1))
     return np.concatenate(X), np.concatenate(Y)
 
 
@@ -245,48 +294,56 @@ class Sampler:
         net.close()
         return s, hist
 
-    def calibrate(self, ctx, X, Y, q=0.995):
-        """Margins from held-out sweeps: k_max is scaled by the q-quantile of
-        the under-prediction ratio; the step multiple is lowered likewise."""
+    def calibrate(self, ctx, X, Y, q_k=0.995, q_d=0.95):
+        """Margins from held-out sweeps: k_max is scaled by the q_k-quantile of
+        the under-prediction ratio; the step multiple is lowered by the
+        q_d-quantile of its over-prediction (the judge catches the rest)."""
         y = self.predict(ctx, X)
         under_k = np.exp(Y[:, 0] - y[:, 0])            # > 1 where the net predicts too small
-        self.margin_k = float(max(1.0, np.quantile(under_k, q)))
+        self.margin_k = float(max(1.0, np.quantile(under_k, q_k)))
         over_d = 2.0 ** (y[:, 1] - Y[:, 1])            # > 1 where the net predicts too coarse
-        self.margin_d = float(max(1.0, np.quantile(over_d, q)))
+        self.margin_d = float(max(1.0, np.quantile(over_d, q_d)))
         return self.margin_k, self.margin_d
 
     # ------------------------------------------------------------ inference
-    def grid(self, ctx, m, dists, dt, log2n, nk_plain, sigma_factor=math.pi, taper=0.3, t0=0.0):
-        """Learned ragged grid for one model and receiver set: (dk, nk[nw],
-        kmax[nw], plain grid report)."""
+    def grid(self, ctx, m, dists, plain=PLAIN, tile=64, use_stride=True):
+        """Learned ragged grid for one model and receiver set: (nk[nw],
+        stride[nw], kmax[nw], plain grid report).  Frequency iw takes
+        nk[iw] points k_j = j stride[iw] dk_plain.  k_max per frequency is
+        the prediction at the nearest receiver (the cutoff falls with
+        distance); the stride the finest prediction at the farthest receiver
+        over each aligned tile of `tile` frequencies (the tensor-core sum
+        multiplies a tile by one Bessel operand), floored to a power of two."""
         model = make_model(**m)
-        popts = make_opts(dt, log2n, t0=t0, taper=taper, sigma_factor=sigma_factor, k_mode=K_FIXED, nk_fixed=nk_plain)
-        gr = grid(model, popts)
+        gr = grid(model, plain_opts(plain))
+        nk_plain = plain["nk"]
         nw, dkp, df = gr["nw"], gr["dk"], gr["df"]
         om = 2 * math.pi * df * np.maximum(np.arange(nw), 1)
         d = np.asarray(dists, np.float64)
         feat = layer_features(m)
         y = self.predict(ctx, np.concatenate([net_inputs(feat, om, d.min(), m["hs"]),
                                               net_inputs(feat, om, d.max(), m["hs"])]))
-        kmax = np.exp(y[:nw, 0]) * self.margin_k
-        mult = 2.0 ** np.floor(np.clip(np.min(y[nw:, 1]) - math.log2(self.margin_d), 0.0, 5.0))
-        dk = dkp * mult
-        ktop = (nk_plain - 1) * dkp
-        kmax = np.minimum(kmax, ktop)
-        nk_top = int(ktop / dk) + 1
-        nk = np.clip(np.ceil(kmax / dk).astype(np.int64) + 2, 8, nk_top).astype(np.int32)
-        return dk, nk, nk * dk, gr
+        kmax = np.minimum(np.exp(y[:nw, 0]) * self.margin_k, (nk_plain - 1) * dkp)
+        l2 = np.clip(y[nw:, 1] - math.log2(self.margin_d), 0.0, 5.0) if use_stride else np.zeros(nw)
+        nt = (nw + tile - 1) // tile
+        l2t = np.full(nt * tile, np.inf)
+        l2t[:nw] = l2
+        l2t = np.floor(l2t.reshape(nt, tile).min(1))
+        stride = np.repeat((2 ** l2t).astype(np.int64), tile)[:nw]
+        nk_top = (nk_plain - 1) // stride + 1                 # stay inside the plain grid
+        nk = np.clip(np.ceil(kmax / (dkp * stride)).astype(np.int64) + 2, 8, nk_top)
+        return nk.astype(np.int32), stride.astype(np.int32), (nk - 1) * stride * dkp, gr
 
 
-def spot_frequencies(nw, n=6):
-    """Fixed spread of judge frequencies over the band (index >= 1)."""
-    f = np.unique(np.clip(np.round(np.array([0.02, 0.08, 0.2, 0.4, 0.62, 0.85])[:n] * nw).astype(np.int64), 1,
-                          nw - 1))
-    return f
+def spot_frequencies(nw):
+    """Judge frequencies: log-spaced from the lowest bin, then spread over
+    the band (indices >= 1)."""
+    f = np.array([1, 2, 4, 8, 16, 32]) * max(1, nw // 4096)
+    f = np.concatenate([f, np.round(np.array([0.02, 0.05, 0.12, 0.25, 0.45, 0.65, 0.85]) * nw)])
+    return np.unique(np.clip(f.astype(np.int64), 1, nw - 1))
 
 
-def run_learned(sampler, m, dists, dt, log2n, nk_plain, ctx=None, sigma_factor=math.pi, taper=0.3, t0=0.0,
-                tail_tol=None, spec_tol=2e-3, judge=True):
+def run_learned(sampler, m, dists, ctx=None, plain=PLAIN, tail_tol=None, spec_tol=2e-3, judge=True, use_stride=True):
     """Traces of one model on the learned grid, judged against the plain grid.
 
     Returns (traces [n_dist, n_cols, N], info).  info: learned and plain (w,k)
@@ -297,33 +354,35 @@ def run_learned(sampler, m, dists, dt, log2n, nk_plain, ctx=None, sigma_factor=m
     try:
         t_start = time.perf_counter()
         dists = np.asarray(dists, np.float64)
-        dk, nk, kmax, gr = sampler.grid(ctx, m, dists, dt, log2n, nk_plain, sigma_factor, taper, t0)
+        nk_plain = plain["nk"]
+        nk, stride, kmax, gr = sampler.grid(ctx, m, dists, plain, use_stride=use_stride)
         nw, dkp = gr["nw"], gr["dk"]
         t_pred = time.perf_counter()
         model = make_model(**m)
-        lopts = make_opts(dt, log2n, t0=t0, taper=taper, sigma_factor=sigma_factor, dk=dk, nk_custom=nk)
-        plan = Plan(ctx, model, lopts, dists)
+        plan = Plan(ctx, model, custom_opts(nk, dkp, plain, k_stride=stride), dists)
         plan.execute()
         traces, _ = plan.fetch(True, False)
-        info = dict(nkw_learned=int(nk.sum()), nkw_plain=int(nw) * int(nk_plain), dk_mult=float(dk / dkp),
-                    ms_learned_gpu=plan.report.ms_total, fallback=[], tail_max=0.0, spec_err_max=0.0)
+        info = dict(nkw_learned=int(nk.sum()), nkw_plain=int(nw) * int(nk_plain),
+                    stride_mean=float(np.mean(stride)), ms_learned_gpu=plan.report.ms_total, fallback=[],
+                    tail_max=0.0, spec_err_max=0.0)
         t_run = time.perf_counter()
         if judge:
             spot = spot_frequencies(nw)
-            popts = make_opts(dt, log2n, t0=t0, taper=taper, sigma_factor=sigma_factor, k_mode=K_FIXED,
-                              nk_fixed=nk_plain)
+            popts = plain_opts(plain)
             bands = np.unique(np.array([dists.min(), math.sqrt(dists.min() * dists.max()), dists.max()]))
             tol = sampler.tol if tail_tol is None else tail_tol
-            _, tail, dk_ok = sweep_kmax(model, popts, spot, bands, sampler.tol,
-                                        k_judge=np.repeat(kmax[spot][:, None], len(bands), 1), ctx=ctx)
-            info["tail_max"] = float(tail.max())
-            tail_bad = tail.max(0) > 10 * tol                  # per band
-            step_bad = bool(np.any(dk_ok[:, -1] < dk * (1 - 1e-9)))
+            sw = sweep_kmax(model, popts, spot, bands, sampler.tol,
+                            k_judge=np.repeat(kmax[spot][:, None], len(bands), 1), ctx=ctx, env=True)
+            # the tail beyond the prediction, against the threshold the
+            # targets were made with (peak envelope over the spot frequencies)
+            w = np.maximum(taper_weight(spot, nw, plain["taper"]), 1e-6)[:, None]
+            excess = sw["tail"] * sw["env"] * w / (tol * sw["env"].max(0)[None, :])
+            info["tail_max"] = float(excess.max())
+            tail_bad = excess.max(0) > 10.0                                         # per band
             # plain grid at the spot frequencies only (2 points elsewhere)
             nk_spot = np.full(nw, 2, np.int32)
             nk_spot[spot] = nk_plain
-            sp_plan = Plan(ctx, model, make_opts(dt, log2n, t0=t0, taper=taper, sigma_factor=sigma_factor, dk=dkp,
-                                                 nk_custom=nk_spot), dists)
+            sp_plan = Plan(ctx, model, custom_opts(nk_spot, dkp, plain), dists)
             sp_plan.execute()
             s_plain = sp_plan.fetch_freqs(spot)
             s_learn = plan.fetch_freqs(spot)
@@ -332,13 +391,12 @@ def run_learned(sampler, m, dists, dt, log2n, nk_plain, ctx=None, sigma_factor=m
             den = np.sqrt(np.sum(np.abs(s_plain) ** 2, axis=(1, 2))) + 1e-300
             err = num / den
             info["spec_err_max"] = float(err.max())
-            bad = err > spec_tol
-            if step_bad:
-                bad[:] = True
-            else:
-                # a band's tail failure sends the receivers nearest to it back
-                band_of = np.argmin(np.abs(np.log(dists[:, None] / bands[None, :])), axis=1)
-                bad |= tail_bad[band_of]
+            bad = ~(err <= spec_tol)                           # NaN fails too
+            # the cutoff falls with distance: a band's tail verdict covers the
+            # receivers beyond it (the step is judged by the spectra above,
+            # at each receiver's own distance)
+            below = np.clip(np.searchsorted(bands, dists * (1 + 1e-12), side="right") - 1, 0, len(bands) - 1)
+            bad |= tail_bad[below]
             if bad.any():
                 idx = np.nonzero(bad)[0]
                 pplan = Plan(ctx, model, popts, dists[idx])

@@ -4,9 +4,9 @@ grid, and evaluate it on held-out models.
     python -m grtm_cuda_gb300.train_sampler --out grtm_cuda_gb300/data/ksampler.bin
     python -m grtm_cuda_gb300.train_sampler --eval --weights ... --eval-models 8
 
-Training data: 80 seeded 40-layer crustal models (source depth U(1, 30) km),
-32 frequencies x 8 distances each (20480 sweeps) on the plain grid of
-N = 8192 samples at dt = 0.05 s with nk = 32768; 16 further models for
+Training data: 320 seeded 40-layer crustal models (source depth U(1, 30) km),
+8 frequencies x 8 distances each (20480 sweeps) on the plain grid of
+N = 8192 samples at dt = 0.05 s with nk = 32768; 64 further models for
 validation and the safety margins.  Everything runs on the GPU through the
 library (sweeps: grt_sweep_kmax; training: grt_mlp_train).
 """
@@ -17,15 +17,15 @@ import time
 
 import numpy as np
 
-from . import Context, FP64, K_FIXED, Plan, make_model, make_opts, synth
-from .learned import PLAIN, WEIGHTS, Sampler, run_learned, sweep_dataset
+from . import FP64, Context, Plan, make_model, synth
+from .learned import PLAIN, WEIGHTS, Sampler, plain_opts, run_learned, sweep_dataset
 
-TRAIN_SEEDS = range(1000, 1080)
-VAL_SEEDS = range(2000, 2016)
+TRAIN_SEEDS = range(1000, 1320)
+VAL_SEEDS = range(2000, 2064)
 HELD_OUT_SEEDS = range(3000, 3256)
 
 
-def train(out, n_models=80, n_val=16, tol=1e-4, log=sys.stdout, dump=None):
+def train(out, n_models=320, n_val=64, tol=1e-4, log=sys.stdout, dump=None):
     ctx = Context()
     t0 = time.perf_counter()
     X, Y = sweep_dataset(ctx, list(TRAIN_SEEDS)[:n_models], tol=tol, rng_seed=1)
@@ -50,31 +50,27 @@ def train(out, n_models=80, n_val=16, tol=1e-4, log=sys.stdout, dump=None):
     return s, res
 
 
-def evaluate(weights, n_models=8, n_receivers=24, fp64=True, log=sys.stdout):
+def evaluate(weights, n_models=8, n_receivers=24, fp64=True, log=sys.stdout, use_stride=True):
     """Learned vs plain FP32 vs plain FP64 on held-out models."""
     s = Sampler.load(weights)
     ctx = Context()
-    p = PLAIN
     rows = []
     for seed in list(HELD_OUT_SEEDS)[:n_models]:
         rng = np.random.default_rng(seed)
         m = synth.crust(rng, 40, rng.uniform(1.0, 30.0))
         dists = np.sort(rng.uniform(1.0, 500.0, n_receivers))
         model = make_model(**m)
-        popts = make_opts(p["dt"], p["log2n"], sigma_factor=p["sigma_factor"], k_mode=K_FIXED, nk_fixed=p["nk"])
-        plan = Plan(ctx, model, popts, dists)
+        plan = Plan(ctx, model, plain_opts(), dists)
         plan.execute()
         ms_plain = plan.report.ms_total
         tp, _ = plan.fetch(True, False)
         plan.close()
-        tl, info = run_learned(s, m, dists, p["dt"], p["log2n"], p["nk"], ctx=ctx)
+        tl, info = run_learned(s, m, dists, ctx=ctx, use_stride=use_stride)
         row = dict(seed=seed, hs=m["hs"], ms_plain=ms_plain, **{k: v for k, v in info.items() if k != "fallback"},
                    n_fallback=len(info["fallback"]))
         ref = tp
         if fp64:
-            popts64 = make_opts(p["dt"], p["log2n"], sigma_factor=p["sigma_factor"], k_mode=K_FIXED,
-                                nk_fixed=p["nk"], precision=FP64)
-            plan = Plan(ctx, model, popts64, dists)
+            plan = Plan(ctx, model, plain_opts(precision=FP64), dists)
             plan.execute()
             ref, _ = plan.fetch(True, False)
             plan.close()
@@ -92,7 +88,7 @@ def evaluate(weights, n_models=8, n_receivers=24, fp64=True, log=sys.stdout):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=WEIGHTS)
-    ap.add_argument("--models", type=int, default=80)
+    ap.add_argument("--models", type=int, default=320)
     ap.add_argument("--tol", type=float, default=1e-4)
     ap.add_argument("--eval", action="store_true")
     ap.add_argument("--weights", default=WEIGHTS)
@@ -100,9 +96,10 @@ def main():
     ap.add_argument("--receivers", type=int, default=24)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--dump", default=None, help="also write the sweep dataset (npz)")
+    ap.add_argument("--no-stride", action="store_true", help="evaluate with unit k stride")
     a = ap.parse_args()
     if a.eval:
-        evaluate(a.weights, a.eval_models, a.receivers, not a.no_fp64)
+        evaluate(a.weights, a.eval_models, a.receivers, not a.no_fp64, use_stride=not a.no_stride)
     else:
         train(a.out, a.models, tol=a.tol, dump=a.dump)
 

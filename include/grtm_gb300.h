@@ -69,6 +69,9 @@ typedef struct grt_opts {
     int precision;        /* GRT_FP32 or GRT_FP64 */
     int fix;              /* GRT_FIX_* bits */
     const int *nk_custom; /* GRT_K_CUSTOM: points per frequency, N/2 entries (e.g. a learned grid) */
+    const int *k_stride;  /* GRT_K_CUSTOM, optional: per-frequency stride m in 1..64, k_j = j m dk
+                           * (N/2 entries; NULL = 1).  FP32 plans (tensor-core sum) need one stride
+                           * per aligned block of 64 frequencies. */
 } grt_opts;
 
 typedef struct grt_report {
@@ -118,18 +121,23 @@ GRT_API int grt_grid(const grt_model *model, const grt_opts *opts, grt_report *r
 
 /* Convergence sweep of the plain method (training data and judge of the
  * learned wavenumber sampler).  For the frequencies freq_idx[0..n_freq) it
- * evaluates the per-(w,k) kernel on the grid of opts and returns, for each
- * frequency and distance r_b, the smallest k_c such that the weighted
- * integrand envelope g(k) = max_q |K_q(w,k)| (1+k)^2 min(1, (k r_b)^-1/2)
- * beyond k_c holds at most tol of its total (kmax_out).  Optional outputs:
- * tail_out, the envelope fraction beyond k_judge[i]; dk_out, the coarsest
- * step dk*2^s (s <= 5) whose sums of K_q(k) J0(k r_b) up to k_c agree with
- * the full-grid sums within tol for every column (its spatial aliasing at
- * r_b).  All outputs [n_freq][n_band].  FP32 kernel.  No counterpart in the
- * reference (its k_max is the fixed rule of cal_kmax, green.cu:108-162). */
+ * evaluates the per-(w,k) kernel on the grid of opts (unit stride) and, for
+ * each frequency and distance r_b, forms the weighted integrand envelope
+ * g(k) = max_q |K_q(w,k)| (1+k)^2 min(1, (k r_b)^-1/2).  Outputs, all
+ * [n_freq][n_band] (alias_out [n_freq][n_band][6]); all but kmax_out optional:
+ *   kmax_out   smallest k_c whose envelope tail beyond k_c is at most tol times
+ *              the envelope total, or at most tol_abs[i] when tol_abs is given;
+ *   tail_out   envelope fraction beyond k_judge[i] (needs k_judge);
+ *   env_out    envelope total;
+ *   alias_out  with S_q^(s) = s dk sum_{j = 0 mod s, j dk < k_c} K_q J0(k r_b):
+ *              [0] = max_q |S_q^(1)|, [s] = max_q |S_q^(2^s) - S_q^(1)| (s = 1..5),
+ *              the spatial aliasing of a 2^s times coarser step at r_b.
+ * FP32 kernel.  No counterpart in the reference (its k_max is the fixed rule
+ * of cal_kmax, green.cu:108-162). */
 GRT_API int grt_sweep_kmax(grt_ctx *ctx, const grt_model *model, const grt_opts *opts, int n_freq,
                            const int *freq_idx, int n_band, const double *band_r, double tol,
-                           const double *k_judge, double *kmax_out, double *tail_out, double *dk_out);
+                           const double *tol_abs, const double *k_judge, double *kmax_out, double *tail_out,
+                           double *env_out, double *alias_out);
 
 /* The learned sampler's network: n_in -> 64 -> 64 -> 64 -> n_out with SiLU
  * hidden activations, FP32, trained by the library's own CUDA kernels
@@ -164,6 +172,7 @@ GRT_API int grt_run(grt_ctx *ctx, const grt_model *model, const grt_opts *opts, 
  * capture.  Calls share the arrays: calls that overlap on the GPU, or come
  * from several host threads at once, race.  Runs on the default stream of
  * `device`; traces: host [n_dist][n_cols][N] doubles.
+ * Reference-rule and fixed grids only (GRT_K_CUSTOM: GRT_ERR_UNSUPPORTED).
  * No counterpart in the reference. */
 GRT_API int grt_run_noalloc(int device, const grt_model *model, const grt_opts *opts, int n_dist,
                             const double *dist, double *traces);

@@ -163,18 +163,20 @@ def test_sweep_properties(ctx):
     gr = g.grid(model, opts)
     fi = np.array([1, 7, 40, 150, 400])
     br = np.array([2.0, 30.0, 300.0])
-    k4, _, d4 = g.sweep_kmax(model, opts, fi, br, 1e-4, ctx=ctx)
-    k6, _, d6 = g.sweep_kmax(model, opts, fi, br, 1e-6, ctx=ctx)
+    s4 = g.sweep_kmax(model, opts, fi, br, 1e-4, ctx=ctx, env=True, alias=True)
+    k4, k6 = s4["kmax"], g.sweep_kmax(model, opts, fi, br, 1e-6, ctx=ctx)["kmax"]
     top = 4096 * gr["dk"]
     assert np.all(k4 > 0) and np.all(k4 <= top) and np.all(k6 <= top)
     assert np.all(k6 >= k4)                                   # a tighter tolerance never cuts earlier
-    mult = d4 / gr["dk"]
-    assert np.all(np.isin(np.round(mult), [1, 2, 4, 8, 16, 32])) and np.allclose(mult, np.round(mult))
+    # an absolute threshold equal to tol x total gives the same cutoff
+    ka = g.sweep_kmax(model, opts, fi, br, 1.0, tol_abs=1e-4 * s4["env"], ctx=ctx)["kmax"]
+    assert np.allclose(ka, k4)
+    assert np.all(s4["alias"][..., 0] > 0) and np.all(np.isfinite(s4["alias"]))
     # judging the sweep's own cutoff finds a tail within the tolerance
-    _, tail, _ = g.sweep_kmax(model, opts, fi, br, 1e-4, k_judge=k4, ctx=ctx)
-    assert np.all(tail <= 1e-4 + 1e-12)
-    _, tail_lo, _ = g.sweep_kmax(model, opts, fi, br, 1e-4, k_judge=0.5 * k4, ctx=ctx)
-    assert np.all(tail_lo >= tail)
+    t1 = g.sweep_kmax(model, opts, fi, br, 1e-4, k_judge=k4, ctx=ctx)["tail"]
+    assert np.all(t1 <= 1e-4 + 1e-12)
+    t2 = g.sweep_kmax(model, opts, fi, br, 1e-4, k_judge=0.5 * k4, ctx=ctx)["tail"]
+    assert np.all(t2 >= t1)
 
 
 @pytest.mark.gpu
@@ -187,6 +189,51 @@ def test_custom_grid_equals_fixed_grid(ctx):
     nw = g.grid(model, opts)["nw"]
     t2, _, _ = g.run(model, g.make_opts(0.1, 10, sigma_factor=math.pi, nk_custom=np.full(nw, 4096)), d, ctx=ctx)
     assert np.array_equal(t1, t2)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("impl", ["tc", "simt"])
+def test_strided_grid_equals_scaled_step(ctx, impl, monkeypatch):
+    """k_j = j m dk on a stride-m grid are the points of a unit-stride grid of
+    step m dk: both give the same traces (to FP32 rounding of the points)."""
+    import grtm_cuda_gb300 as g
+    if impl == "simt":
+        monkeypatch.setenv("GRT_KSUM", "simt")
+    m, model, opts = _small_job()
+    gr = g.grid(model, opts)
+    nw, dk = gr["nw"], gr["dk"]
+    d = np.array([3.0, 40.0, 250.0])
+    nk = np.full(nw, 1024, np.int32)
+    stride = np.repeat(np.array([1, 2, 4, 2, 8, 1, 2, 4]), 64)[:nw].astype(np.int32)
+    # the same points frequency by frequency: one plan per stride value
+    s1 = np.zeros((len(d), 20, 2 * nw), dtype=complex)
+    for sv in np.unique(stride):
+        _, s, _ = g.run(model, g.make_opts(0.1, 10, sigma_factor=math.pi, dk=dk * sv, nk_custom=nk), d, ctx=ctx,
+                        spectra=True)
+        sel = np.nonzero(stride == sv)[0]
+        s1[..., sel] = s[..., sel]
+    _, s0, _ = g.run(model, g.make_opts(0.1, 10, sigma_factor=math.pi, dk=dk, nk_custom=nk, k_stride=stride), d,
+                     ctx=ctx, spectra=True)
+    err = np.abs(s0[..., :nw] - s1[..., :nw]).max() / np.abs(s1[..., :nw]).max()
+    assert err <= 2e-6
+
+
+@pytest.mark.gpu
+def test_stride_tile_rule(ctx, monkeypatch):
+    """The tensor-core sum needs one stride per aligned tile of 64 frequencies;
+    the SIMT sum takes any per-frequency stride."""
+    import grtm_cuda_gb300 as g
+    m, model, opts = _small_job()
+    nw = g.grid(model, opts)["nw"]
+    stride = np.ones(nw, np.int32)
+    stride[5] = 2
+    o = g.make_opts(0.1, 10, sigma_factor=math.pi, nk_custom=np.full(nw, 512), k_stride=stride)
+    with pytest.raises(g.GrtError) as e:
+        g.run(model, o, [10.0], ctx=ctx)
+    assert e.value.status == g.ERR_ARG
+    monkeypatch.setenv("GRT_KSUM", "simt")
+    t, _, _ = g.run(model, o, [10.0], ctx=ctx)
+    assert np.all(np.isfinite(t))
 
 
 def _learned_case(seed=3007, n_rec=8):
@@ -205,12 +252,10 @@ def test_learned_path_gain_and_accuracy(ctx):
     if not os.path.exists(learned.WEIGHTS):
         pytest.skip("no trained sampler in the tree")
     s = learned.Sampler.load()
-    P = learned.PLAIN
     m, d = _learned_case()
     model = g.make_model(**m)
-    t64, _, _ = g.run(model, g.make_opts(P["dt"], P["log2n"], sigma_factor=P["sigma_factor"], k_mode=g.K_FIXED,
-                                         nk_fixed=P["nk"], precision=g.FP64), d, ctx=ctx)
-    tl, info = learned.run_learned(s, m, d, P["dt"], P["log2n"], P["nk"], ctx=ctx)
+    t64, _, _ = g.run(model, learned.plain_opts(precision=g.FP64), d, ctx=ctx)
+    tl, info = learned.run_learned(s, m, d, ctx=ctx)
     err = np.sqrt(np.sum((tl - t64) ** 2, axis=(1, 2)) / np.sum(t64 ** 2, axis=(1, 2)))
     assert info["nkw_plain"] / info["nkw_learned"] >= 1.5
     assert np.sqrt(np.sum((tl - t64) ** 2) / np.sum(t64 ** 2)) <= 1e-3
@@ -227,10 +272,8 @@ def test_learned_judge_falls_back(ctx):
         pytest.skip("no trained sampler in the tree")
     s = learned.Sampler.load()
     s.margin_k = 0.2
-    P = learned.PLAIN
     m, d = _learned_case(3011, 4)
-    tl, info = learned.run_learned(s, m, d, P["dt"], P["log2n"], P["nk"], ctx=ctx)
+    tl, info = learned.run_learned(s, m, d, ctx=ctx)
     assert len(info["fallback"]) == len(d)
-    tp, _, _ = g.run(g.make_model(**m), g.make_opts(P["dt"], P["log2n"], sigma_factor=P["sigma_factor"],
-                                                     k_mode=g.K_FIXED, nk_fixed=P["nk"]), d, ctx=ctx)
+    tp, _, _ = g.run(g.make_model(**m), learned.plain_opts(), d, ctx=ctx)
     assert np.array_equal(tl, tp)
