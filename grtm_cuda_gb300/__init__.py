@@ -52,12 +52,34 @@ class Report(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class Job(ctypes.Structure):
+    _fields_ = [("model", ctypes.POINTER(Model)), ("opts", ctypes.POINTER(Opts)), ("n_dist", ctypes.c_int),
+                ("dist", _dp)]
+
+
+TUNE_MAX = 16
+
+
+class Tune(ctypes.Structure):
+    _fields_ = [("tuned", ctypes.c_int), ("grt_threads", ctypes.c_int), ("grt_blocks", ctypes.c_int),
+                ("n_cand", ctypes.c_int), ("cand_threads", ctypes.c_int * TUNE_MAX),
+                ("cand_blocks", ctypes.c_int * TUNE_MAX), ("cand_ms", ctypes.c_float * TUNE_MAX),
+                ("sample_fraction", ctypes.c_double)]
+
+    def as_dict(self):
+        n = self.n_cand
+        return {"tuned": self.tuned, "grt_threads": self.grt_threads, "grt_blocks": self.grt_blocks,
+                "candidates": [(self.cand_threads[i], self.cand_blocks[i], self.cand_ms[i]) for i in range(n)],
+                "sample_fraction": self.sample_fraction}
+
+
 # every symbol the public header declares
 EXPORTS = ("grt_create", "grt_destroy", "grt_last_error", "grt_status_string", "grt_plan_create",
            "grt_plan_execute", "grt_plan_fetch", "grt_plan_fetch_freqs", "grt_plan_info", "grt_plan_destroy", "grt_grid", "grt_run",
            "grt_green", "green", "grt_run_noalloc", "grt_sweep_kmax", "grt_mlp_create", "grt_mlp_destroy",
            "grt_mlp_n_params", "grt_mlp_get_params", "grt_mlp_set_params", "grt_mlp_forward",
-           "grt_mlp_loss_grad", "grt_mlp_train")
+           "grt_mlp_loss_grad", "grt_mlp_train", "grt_batch_create", "grt_batch_execute", "grt_batch_fetch",
+           "grt_batch_fetch_freqs", "grt_batch_info", "grt_batch_destroy")
 
 _lib = None
 
@@ -111,6 +133,13 @@ def lib():
     L.grt_mlp_loss_grad.argtypes = [vp, ctypes.c_int, fp, fp, fp, fp]
     L.grt_mlp_train.argtypes = [vp, ctypes.c_int, fp, fp, ctypes.c_int, ctypes.c_int, ctypes.c_float,
                                 ctypes.c_ulonglong, fp]
+    L.grt_batch_create.argtypes = [vp, ctypes.c_int, P(Job), ctypes.c_int, P(vp)]
+    L.grt_batch_execute.argtypes = [vp, P(Report)]
+    L.grt_batch_fetch.argtypes = [vp, ctypes.c_int, _dp, _dp]
+    L.grt_batch_fetch_freqs.argtypes = [vp, ctypes.c_int, ctypes.c_int, ip, _dp]
+    L.grt_batch_info.argtypes = [vp, ctypes.c_int, P(Report), P(Tune)]
+    L.grt_batch_destroy.argtypes = [vp]
+    L.grt_batch_destroy.restype = None
     _lib = L
     return L
 
@@ -272,6 +301,73 @@ def sweep_kmax(model, opts, freq_idx, band_r, tol=1e-4, tol_abs=None, k_judge=No
         if own:
             ctx.close()
     return out
+
+
+class Batch:
+    """Many jobs (model, opts, distances) executed as one CUDA graph with a
+    single persistent GRT launch (grt_batch_*)."""
+
+    def __init__(self, ctx, jobs, autotune=True):
+        self.ctx = ctx
+        self._keep = []
+        arr = (Job * len(jobs))()
+        self.dists = []
+        for i, (model, opts, dists) in enumerate(jobs):
+            d = _arr(np.atleast_1d(dists))
+            self._keep += [model, opts, d]
+            self.dists.append(d)
+            arr[i] = Job(ctypes.pointer(model), ctypes.pointer(opts), len(d), _ptr(d))
+        self.h = ctypes.c_void_p()
+        rc = lib().grt_batch_create(ctx.h, len(jobs), arr, int(bool(autotune)), ctypes.byref(self.h))
+        if rc:
+            raise GrtError(rc, ctx.error())
+        self.report = Report()
+
+    def execute(self):
+        rc = lib().grt_batch_execute(self.h, ctypes.byref(self.report))
+        if rc:
+            raise GrtError(rc, self.ctx.error())
+        return self.report
+
+    def info(self, job=-1):
+        r, t = Report(), Tune()
+        rc = lib().grt_batch_info(self.h, int(job), ctypes.byref(r), ctypes.byref(t))
+        if rc:
+            raise GrtError(rc, "grt_batch_info")
+        return r.as_dict(), t.as_dict()
+
+    def fetch(self, job, traces=True, spectra=False):
+        r, _ = self.info(job)
+        shape = (len(self.dists[job]), r["n_cols"], r["n_samples"])
+        t = np.empty(shape) if traces else None
+        s = np.empty(shape + (2,)) if spectra else None
+        rc = lib().grt_batch_fetch(self.h, int(job), _ptr(t) if traces else None, _ptr(s) if spectra else None)
+        if rc:
+            raise GrtError(rc, self.ctx.error())
+        if spectra:
+            s = s[..., 0] + 1j * s[..., 1]
+        return t, s
+
+    def fetch_freqs(self, job, freq_idx):
+        r, _ = self.info(job)
+        fi = np.ascontiguousarray(freq_idx, dtype=np.int32)
+        s = np.empty((len(self.dists[job]), r["n_cols"], len(fi), 2))
+        rc = lib().grt_batch_fetch_freqs(self.h, int(job), len(fi), fi.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                         _ptr(s))
+        if rc:
+            raise GrtError(rc, self.ctx.error())
+        return s[..., 0] + 1j * s[..., 1]
+
+    def close(self):
+        if self.h:
+            lib().grt_batch_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def run(model, opts, dists, ctx=None, spectra=False):

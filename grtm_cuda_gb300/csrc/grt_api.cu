@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <string>
 #include <type_traits>
@@ -45,6 +46,7 @@ struct grt_plan {
     long long *koff = nullptr;
     double *ddist = nullptr, *damp = nullptr;
     unsigned *derr = nullptr;
+    bool own_derr = true;                     // false inside a batch (the batch's error word)
     grt_report rep{};
 };
 
@@ -109,10 +111,25 @@ extern "C" void grt_plan_destroy(grt_plan *p)
     if (!p) return;
     cudaSetDevice(p->ctx->device);
     void *bufs[] = {p->tab, p->K, p->B, p->S, p->post, p->tw, p->spec, p->sig, p->tiles, p->nk, p->koff, p->ddist,
-                    p->damp, p->derr, p->P, p->Kt, p->kt_base, p->ks};
+                    p->damp, p->own_derr ? p->derr : nullptr, p->P, p->Kt, p->kt_base, p->ks};
     for (void *b : bufs)
         if (b) cudaFree(b);
     delete p;
+}
+
+// Raise a kernel's dynamic shared-memory limit (never lower it: a captured
+// graph replays launches of several sizes).  Not thread-safe, like contexts.
+template <typename F>
+static cudaError_t raise_smem_limit(F *kernel, int bytes)
+{
+    static std::map<std::pair<int, const void *>, int> current;   // (device, kernel) -> limit set
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int &cur = current[{dev, (const void *)kernel}];
+    if (bytes <= cur) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) cur = bytes;
+    return e;
 }
 
 // ------------------------------------------------------------------ host tables
@@ -317,11 +334,11 @@ static int launch_ksum_tc(grt_plan *p, cudaStream_t st, int &launches)
     const unsigned grid = (unsigned)(nwt * nrt * p->nsplit);
     if (J.src == 0) {
         const int sm = grt::tc::smem_bytes<grt::kSingle>();
-        CU(cudaFuncSetAttribute(grt::ksum_tc_kernel<grt::kSingle>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+        CU(raise_smem_limit(grt::ksum_tc_kernel<grt::kSingle>, sm));
         grt::ksum_tc_kernel<grt::kSingle><<<grid, grt::tc::kThreads, sm, st>>>(T);
     } else {
         const int sm = grt::tc::smem_bytes<grt::kTensor>();
-        CU(cudaFuncSetAttribute(grt::ksum_tc_kernel<grt::kTensor>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+        CU(raise_smem_limit(grt::ksum_tc_kernel<grt::kTensor>, sm));
         grt::ksum_tc_kernel<grt::kTensor><<<grid, grt::tc::kThreads, sm, st>>>(T);
     }
     launches++;
@@ -334,14 +351,11 @@ static int launch_ksum_tc(grt_plan *p, cudaStream_t st, int &launches)
     return GRT_OK;
 }
 
+// ------------------------------------------------------------------ stages
 template <typename R>
-static int execute(grt_plan *p)
+static grt::GrtArgs<R> grt_args(const grt_plan *p)
 {
-    grt_ctx *ctx = p->ctx;
     const Job &J = p->J;
-    cudaStream_t st = ctx->stream;
-    int launches = 0;
-    // 1. per-(w,k) GRT kernel
     grt::GrtArgs<R> A{};
     A.tab = (const grt::LayerW<R> *)p->tab;
     A.tiles = p->tiles;
@@ -360,60 +374,94 @@ static int execute(grt_plan *p)
     A.err = p->derr;
     A.Kt = p->use_tc ? p->Kt : nullptr;
     A.kt_base = p->kt_base;
+    return A;
+}
+
+template <typename R>
+static int launch_bessel(grt_plan *p, cudaStream_t st, int &launches)
+{
+    grt_ctx *ctx = p->ctx;
+    const Job &J = p->J;
+    const long long n = (long long)J.nbrow * p->nd;
+    const int blocks = (int)((n + 255) / 256);
+    grt::bessel_table_kernel<R><<<blocks, 256, 0, st>>>((R *)p->B, J.nbrow, p->nd, J.dk, p->ddist);
+    launches++;
+    CU(cudaGetLastError());
+    return GRT_OK;
+}
+
+template <typename R>
+static int launch_ksum(grt_plan *p, cudaStream_t st, int &launches)
+{
+    grt_ctx *ctx = p->ctx;
+    const Job &J = p->J;
+    if constexpr (std::is_same<R, float>::value) {
+        if (p->use_tc) return launch_ksum_tc(p, st, launches);
+    }
+    grt::KsumArgs<R> S{};
+    S.K = (const R *)p->K; S.B = (const R *)p->B; S.nk = p->nk; S.ks = p->ks; S.koff = p->koff; S.dist = p->ddist;
+    S.S = (R *)p->S; S.nkw = J.nkw; S.dk = J.dk; S.nw = J.nw; S.nr = p->nd; S.rt = p->rt; S.jt = p->jt;
+    const int grid = J.nw * ((p->nd + p->rt - 1) / p->rt);
+    if (J.src == 0) grt::ksum_kernel<R, grt::kSingle><<<grid, grt::kSumThreads, 0, st>>>(S);
+    else grt::ksum_kernel<R, grt::kTensor><<<grid, grt::kSumThreads, 0, st>>>(S);
+    launches++;
+    CU(cudaGetLastError());
+    return GRT_OK;
+}
+
+template <typename R>
+static int launch_spectral(grt_plan *p, cudaStream_t st, int &launches)
+{
+    grt_ctx *ctx = p->ctx;
+    const Job &J = p->J;
+    grt::SpecArgs<R> S{};
+    S.S = (const R *)p->S; S.post = (const R *)p->post; S.tw = (const R *)p->tw; S.damp = p->damp;
+    S.spec_out = (R *)p->spec; S.sig_out = (R *)p->sig; S.nw = J.nw; S.logn = J.log2n;
+    const size_t smem2 = (size_t)J.N * sizeof(grt::C<R>);
+    CU(raise_smem_limit(grt::spectral_kernel<R>, (int)smem2));
+    const int threads = std::min(512, std::max(32, J.N / 2));
+    grt::spectral_kernel<R><<<p->nd * p->nc, threads, smem2, st>>>(S);
+    launches++;
+    CU(cudaGetLastError());
+    return GRT_OK;
+}
+
+static int check_device_error(grt_ctx *ctx, const unsigned *derr)
+{
+    unsigned herr = 0;
+    CU(cudaMemcpy(&herr, derr, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    if (herr)
+        return set_err(ctx, GRT_ERR_TIMEOUT,
+                       std::string("a bounded device wait gave up: ") + ((herr & 1) ? "layer-table copy " : "") +
+                           ((herr & 2) ? "tensor-core operand refill " : "") + ((herr & 4) ? "tensor-core issue " : "") +
+                           ((herr & 8) ? "tensor-core drain" : ""));
+    return GRT_OK;
+}
+
+template <typename R>
+static int execute(grt_plan *p)
+{
+    grt_ctx *ctx = p->ctx;
+    const Job &J = p->J;
+    cudaStream_t st = ctx->stream;
+    int launches = 0, rc;
+    // 1. per-(w,k) GRT kernel
+    const grt::GrtArgs<R> A = grt_args<R>(p);
     const size_t smem = (size_t)J.L * sizeof(grt::LayerW<R>);
     CU(cudaEventRecord(ctx->ev[0], st));
     grt::grt_point_kernel<R><<<p->ntiles, grt::kGrtThreads, smem, st>>>(A);
     launches++;
     CU(cudaGetLastError());
     CU(cudaEventRecord(ctx->ev[1], st));
-    // 2. Bessel table
-    {
-        long long n = (long long)J.nbrow * p->nd;
-        int blocks = (int)((n + 255) / 256);
-        grt::bessel_table_kernel<R><<<blocks, 256, 0, st>>>((R *)p->B, J.nbrow, p->nd, J.dk, p->ddist);
-        launches++;
-        CU(cudaGetLastError());
-    }
+    // 2. Bessel table, 3. wavenumber sum, 4. spectral stage + inverse DFT
+    if ((rc = launch_bessel<R>(p, st, launches))) return rc;
     CU(cudaEventRecord(ctx->ev[2], st));
-    // 3. wavenumber sum
-    if constexpr (std::is_same<R, float>::value) {
-        if (p->use_tc) {
-            int rc = launch_ksum_tc(p, st, launches);
-            if (rc) return rc;
-        }
-    }
-    if (!p->use_tc) {
-        grt::KsumArgs<R> S{};
-        S.K = (const R *)p->K; S.B = (const R *)p->B; S.nk = p->nk; S.ks = p->ks; S.koff = p->koff; S.dist = p->ddist;
-        S.S = (R *)p->S; S.nkw = J.nkw; S.dk = J.dk; S.nw = J.nw; S.nr = p->nd; S.rt = p->rt; S.jt = p->jt;
-        int grid = J.nw * ((p->nd + p->rt - 1) / p->rt);
-        if (J.src == 0) grt::ksum_kernel<R, grt::kSingle><<<grid, grt::kSumThreads, 0, st>>>(S);
-        else grt::ksum_kernel<R, grt::kTensor><<<grid, grt::kSumThreads, 0, st>>>(S);
-        launches++;
-        CU(cudaGetLastError());
-    }
+    if ((rc = launch_ksum<R>(p, st, launches))) return rc;
     CU(cudaEventRecord(ctx->ev[3], st));
-    // 4. spectral stage + inverse DFT
-    {
-        grt::SpecArgs<R> S{};
-        S.S = (const R *)p->S; S.post = (const R *)p->post; S.tw = (const R *)p->tw; S.damp = p->damp;
-        S.spec_out = (R *)p->spec; S.sig_out = (R *)p->sig; S.nw = J.nw; S.logn = J.log2n;
-        size_t smem2 = (size_t)J.N * sizeof(grt::C<R>);
-        CU(cudaFuncSetAttribute(grt::spectral_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
-        int threads = std::min(512, std::max(32, J.N / 2));
-        grt::spectral_kernel<R><<<p->nd * p->nc, threads, smem2, st>>>(S);
-        launches++;
-        CU(cudaGetLastError());
-    }
+    if ((rc = launch_spectral<R>(p, st, launches))) return rc;
     CU(cudaEventRecord(ctx->ev[4], st));
     CU(cudaEventSynchronize(ctx->ev[4]));
-    unsigned herr = 0;
-    CU(cudaMemcpy(&herr, p->derr, sizeof(unsigned), cudaMemcpyDeviceToHost));
-    if (herr)
-        return set_err(ctx, GRT_ERR_TIMEOUT,
-                       std::string("a bounded device wait gave up: ") + ((herr & 1) ? "layer-table copy " : "") +
-                           ((herr & 2) ? "tensor-core operand refill " : "") + ((herr & 4) ? "tensor-core issue " : "") +
-                           ((herr & 8) ? "tensor-core drain" : ""));
+    if ((rc = check_device_error(ctx, p->derr))) return rc;
     float t[4];
     for (int i = 0; i < 4; i++) CU(cudaEventElapsedTime(&t[i], ctx->ev[i], ctx->ev[i + 1]));
     p->rep.ms_grt = t[0];
@@ -858,3 +906,317 @@ extern "C" int grt_green(const char *iname, const char *oname_w, const char *ona
 }
 
 extern "C" void green(char *iname, char *oname_w, char *oname_t) { (void)grt_green(iname, oname_w, oname_t); }
+
+// ------------------------------------------------------------------ batches
+// Many jobs (models of any layer count, receiver sets, grids and lengths)
+// executed together: one persistent launch of the batched GRT kernel over the
+// tiles of every job, then each job's Bessel table, wavenumber sum and
+// spectral stage on one of four side streams (the Bessel tables overlap the
+// GRT launch).  The whole execution is captured once into a CUDA graph and
+// replayed.  The GRT launch shape (threads per block = wavenumbers per tile,
+// persistent grid size) is chosen by timing the candidates on the batch.
+namespace {
+constexpr int kSide = 4;
+constexpr int kNtOpts[3] = {64, 128, 256};
+}
+
+struct grt_batch {
+    grt_ctx *ctx = nullptr;
+    std::vector<grt_plan *> jobs;
+    int prec = 0, maxL = 0, nsm = 0;
+    void *d_args = nullptr;          // GrtArgs<R>[n_jobs]
+    int4 *d_tiles[3] = {};           // tile lists for 64 / 128 / 256 threads per block
+    int ntiles[3] = {};
+    long long points = 0;
+    unsigned *derr = nullptr;
+    cudaStream_t side[kSide] = {};
+    cudaEvent_t ev_start = nullptr, ev_grt = nullptr, ev_end = nullptr;    // timing (graph event-record nodes)
+    cudaEvent_t fork0 = nullptr, fork1 = nullptr, join[kSide] = {};         // dependencies between streams
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    grt_tune tune{};
+    grt_report rep{};
+};
+
+extern "C" void grt_batch_destroy(grt_batch *b)
+{
+    if (!b) return;
+    cudaSetDevice(b->ctx->device);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    for (grt_plan *p : b->jobs) grt_plan_destroy(p);
+    cudaFree(b->d_args);
+    for (auto *t : b->d_tiles) cudaFree(t);
+    cudaFree(b->derr);
+    for (auto &s : b->side)
+        if (s) cudaStreamDestroy(s);
+    cudaEvent_t evs[] = {b->ev_start, b->ev_grt, b->ev_end, b->fork0, b->fork1};
+    for (auto e : evs)
+        if (e) cudaEventDestroy(e);
+    for (auto e : b->join)
+        if (e) cudaEventDestroy(e);
+    delete b;
+}
+
+template <typename R>
+static int batch_launch_grt(grt_batch *b, int which, int grid, int ntiles, cudaStream_t st)
+{
+    grt_ctx *ctx = b->ctx;
+    const size_t smem = (size_t)b->maxL * sizeof(grt::LayerW<R>);
+    const grt::GrtArgs<R> *args = (const grt::GrtArgs<R> *)b->d_args;
+    switch (kNtOpts[which]) {
+    case 64: grt::grt_batch_kernel<R, 64><<<grid, 64, smem, st>>>(args, b->d_tiles[which], ntiles, b->derr); break;
+    case 128: grt::grt_batch_kernel<R, 128><<<grid, 128, smem, st>>>(args, b->d_tiles[which], ntiles, b->derr); break;
+    default: grt::grt_batch_kernel<R, 256><<<grid, 256, smem, st>>>(args, b->d_tiles[which], ntiles, b->derr); break;
+    }
+    CU(cudaGetLastError());
+    return GRT_OK;
+}
+
+template <typename R>
+static int batch_occupancy(int which, size_t smem, int *blocks)
+{
+    cudaError_t e;
+    switch (kNtOpts[which]) {
+    case 64: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, grt::grt_batch_kernel<R, 64>, 64, smem); break;
+    case 128: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, grt::grt_batch_kernel<R, 128>, 128, smem); break;
+    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, grt::grt_batch_kernel<R, 256>, 256, smem); break;
+    }
+    if (*blocks < 1) *blocks = 1;
+    return e == cudaSuccess ? GRT_OK : GRT_ERR_CUDA;
+}
+
+// time the candidate shapes on a prefix of the tiles (about 30M points)
+template <typename R>
+static int batch_autotune(grt_batch *b, bool run)
+{
+    grt_ctx *ctx = b->ctx;
+    cudaStream_t st = ctx->stream;
+    const size_t smem = (size_t)b->maxL * sizeof(grt::LayerW<R>);
+    const double frac = std::min(1.0, 3.0e7 / (double)std::max(1LL, b->points));
+    int n = 0;
+    float best = 1e30f;
+    for (int w = 0; w < 3; w++) {
+        int occ = 1;
+        if (batch_occupancy<R>(w, smem, &occ)) return set_err(ctx, GRT_ERR_CUDA, "occupancy query failed");
+        for (int m = 1; m <= 4; m *= 2) {
+            const int grid = b->nsm * occ * m;
+            float ms = 0.f;
+            if (run) {
+                const int nt = std::max(1, (int)(b->ntiles[w] * frac));
+                if (n == 0) {   // warm-up of the first shape
+                    int rc = batch_launch_grt<R>(b, w, grid, nt, st);
+                    if (rc) return rc;
+                }
+                CU(cudaEventRecord(ctx->ev[0], st));
+                int rc = batch_launch_grt<R>(b, w, grid, nt, st);
+                if (rc) return rc;
+                CU(cudaEventRecord(ctx->ev[1], st));
+                CU(cudaEventSynchronize(ctx->ev[1]));
+                CU(cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]));
+            }
+            if (n < GRT_TUNE_MAX) {
+                b->tune.cand_threads[n] = kNtOpts[w];
+                b->tune.cand_blocks[n] = grid;
+                b->tune.cand_ms[n] = ms;
+            }
+            n++;
+            const bool pick = run ? ms < best : (kNtOpts[w] == 128 && m == 1);
+            if (pick) {
+                best = ms;
+                b->tune.grt_threads = kNtOpts[w];
+                b->tune.grt_blocks = grid;
+            }
+        }
+    }
+    b->tune.n_cand = std::min(n, GRT_TUNE_MAX);
+    b->tune.tuned = run;
+    b->tune.sample_fraction = run ? frac : 0.0;
+    return check_device_error(ctx, b->derr);
+}
+
+// a timing event: inside a stream capture it must become a graph node (external)
+static cudaError_t record_timing(cudaEvent_t ev, cudaStream_t st)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(st, &cs);
+    if (e != cudaSuccess) return e;
+    return cs == cudaStreamCaptureStatusActive ? cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal)
+                                               : cudaEventRecord(ev, st);
+}
+
+template <typename R>
+static int batch_record(grt_batch *b, cudaStream_t st)
+{
+    grt_ctx *ctx = b->ctx;
+    int launches = 0, rc;
+    int w = 0;
+    while (kNtOpts[w] != b->tune.grt_threads) w++;
+    // timing events are recorded as graph nodes (external), the fork/join
+    // events only order the streams
+    CU(record_timing(b->ev_start, st));
+    CU(cudaEventRecord(b->fork0, st));
+    for (int s = 0; s < kSide; s++) CU(cudaStreamWaitEvent(b->side[s], b->fork0, 0));
+    // Bessel tables depend on the receivers only: they run beside the GRT launch
+    for (size_t j = 0; j < b->jobs.size(); j++)
+        if ((rc = launch_bessel<R>(b->jobs[j], b->side[j % kSide], launches))) return rc;
+    if ((rc = batch_launch_grt<R>(b, w, b->tune.grt_blocks, b->ntiles[w], st))) return rc;
+    launches++;
+    CU(record_timing(b->ev_grt, st));
+    CU(cudaEventRecord(b->fork1, st));
+    for (int s = 0; s < kSide; s++) CU(cudaStreamWaitEvent(b->side[s], b->fork1, 0));
+    for (size_t j = 0; j < b->jobs.size(); j++) {
+        cudaStream_t ss = b->side[j % kSide];
+        if ((rc = launch_ksum<R>(b->jobs[j], ss, launches))) return rc;
+        if ((rc = launch_spectral<R>(b->jobs[j], ss, launches))) return rc;
+    }
+    for (int s = 0; s < kSide; s++) {
+        CU(cudaEventRecord(b->join[s], b->side[s]));
+        CU(cudaStreamWaitEvent(st, b->join[s], 0));
+    }
+    CU(record_timing(b->ev_end, st));
+    b->rep.kernel_launches = launches;
+    return GRT_OK;
+}
+
+template <typename R>
+static int batch_build(grt_batch *b, int autotune)
+{
+    grt_ctx *ctx = b->ctx;
+    cudaStream_t st = ctx->stream;
+    // per-job arguments in device memory; every job reports waits to the batch's error word
+    std::vector<grt::GrtArgs<R>> args;
+    for (grt_plan *p : b->jobs) {
+        // all of the job's kernels report bounded-wait failures to the batch's word
+        if (p->own_derr) cudaFree(p->derr);
+        p->derr = b->derr;
+        p->own_derr = false;
+        args.push_back(grt_args<R>(p));
+    }
+    CU(cudaMalloc(&b->d_args, args.size() * sizeof(args[0])));
+    CU(cudaMemcpyAsync(b->d_args, args.data(), args.size() * sizeof(args[0]), cudaMemcpyHostToDevice, st));
+    for (int w = 0; w < 3; w++) {
+        std::vector<int4> tl;
+        for (size_t j = 0; j < b->jobs.size(); j++) {
+            const Job &J = b->jobs[j]->J;
+            for (int iw = 0; iw < J.nw; iw++)
+                for (int j0 = 0; j0 < J.nk[iw]; j0 += kNtOpts[w]) tl.push_back(make_int4((int)j, iw, j0, 0));
+        }
+        b->ntiles[w] = (int)tl.size();
+        CU(cudaMalloc(&b->d_tiles[w], tl.size() * sizeof(int4)));
+        CU(cudaMemcpyAsync(b->d_tiles[w], tl.data(), tl.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
+    }
+    const size_t smem = (size_t)b->maxL * sizeof(grt::LayerW<R>);
+    CU(raise_smem_limit(grt::grt_batch_kernel<R, 64>, (int)smem));
+    CU(raise_smem_limit(grt::grt_batch_kernel<R, 128>, (int)smem));
+    CU(raise_smem_limit(grt::grt_batch_kernel<R, 256>, (int)smem));
+    CU(cudaStreamSynchronize(st));
+    int rc = batch_autotune<R>(b, autotune != 0);
+    if (rc) return rc;
+    // one uncaptured pass sets the kernels' attributes, then the capture
+    if ((rc = batch_record<R>(b, st))) return rc;
+    CU(cudaStreamSynchronize(st));
+    if ((rc = check_device_error(ctx, b->derr))) return rc;
+    CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    rc = batch_record<R>(b, st);
+    cudaGraph_t g = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(st, &g);
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    CU(ce);
+    b->graph = g;
+    CU(cudaGraphInstantiate(&b->exec, g, 0));
+    return GRT_OK;
+}
+
+extern "C" int grt_batch_create(grt_ctx *ctx, int n_jobs, const grt_job *jobs, int autotune, grt_batch **out)
+{
+    if (!ctx || !jobs || !out || n_jobs < 1) return set_err(ctx, GRT_ERR_ARG, "bad batch arguments");
+    *out = nullptr;
+    std::unique_ptr<grt_batch, void (*)(grt_batch *)> b(new grt_batch, grt_batch_destroy);
+    b->ctx = ctx;
+    CU(cudaSetDevice(ctx->device));
+    for (int j = 0; j < n_jobs; j++) {
+        if (!jobs[j].model || !jobs[j].opts) return set_err(ctx, GRT_ERR_ARG, "batch job without model or options");
+        if (j > 0 && jobs[j].opts->precision != jobs[0].opts->precision)
+            return set_err(ctx, GRT_ERR_ARG, "all jobs of a batch share one precision");
+        grt_plan *p = nullptr;
+        int rc = grt_plan_create(ctx, jobs[j].model, jobs[j].opts, jobs[j].n_dist, jobs[j].dist, &p);
+        if (rc) return set_err(ctx, rc, "job " + std::to_string(j) + ": " + ctx->err);
+        b->jobs.push_back(p);
+        b->maxL = std::max(b->maxL, p->J.L);
+        b->points += p->J.nkw;
+    }
+    b->prec = jobs[0].opts->precision;
+    CU(cudaDeviceGetAttribute(&b->nsm, cudaDevAttrMultiProcessorCount, ctx->device));
+    CU(cudaMalloc(&b->derr, sizeof(unsigned)));
+    CU(cudaMemset(b->derr, 0, sizeof(unsigned)));
+    for (auto &s : b->side) CU(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    CU(cudaEventCreate(&b->ev_start));
+    CU(cudaEventCreate(&b->ev_grt));
+    CU(cudaEventCreate(&b->ev_end));
+    CU(cudaEventCreateWithFlags(&b->fork0, cudaEventDisableTiming));
+    CU(cudaEventCreateWithFlags(&b->fork1, cudaEventDisableTiming));
+    for (auto &e : b->join) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    int rc = b->prec ? batch_build<double>(b.get(), autotune) : batch_build<float>(b.get(), autotune);
+    if (rc) return rc;
+    *out = b.release();
+    return GRT_OK;
+}
+
+extern "C" int grt_batch_execute(grt_batch *b, grt_report *r)
+{
+    if (!b) return GRT_ERR_ARG;
+    grt_ctx *ctx = b->ctx;
+    CU(cudaSetDevice(ctx->device));
+    CU(cudaGraphLaunch(b->exec, ctx->stream));
+    CU(cudaEventSynchronize(b->ev_end));
+    int rc = check_device_error(ctx, b->derr);
+    if (rc) return rc;
+    float t_grt = 0.f, t_all = 0.f;
+    CU(cudaEventElapsedTime(&t_grt, b->ev_start, b->ev_grt));
+    CU(cudaEventElapsedTime(&t_all, b->ev_start, b->ev_end));
+    b->rep.ms_grt = t_grt;
+    b->rep.ms_total = t_all;
+    b->rep.ms_bessel = b->rep.ms_ksum = b->rep.ms_spectral = 0.f;
+    long long nwk = 0, h2d = 0, d2h = 0;
+    int ncol = 0;
+    for (grt_plan *p : b->jobs) {
+        nwk += p->J.nkw;
+        h2d += p->rep.h2d_bytes;
+        d2h += p->rep.d2h_bytes;
+        ncol = std::max(ncol, p->nc);
+    }
+    b->rep.n_wk = nwk;
+    b->rep.h2d_bytes = h2d;
+    b->rep.d2h_bytes = d2h;
+    b->rep.n_cols = ncol;
+    b->rep.ksum_impl = b->jobs[0]->use_tc;
+    if (r) *r = b->rep;
+    return GRT_OK;
+}
+
+extern "C" int grt_batch_fetch(grt_batch *b, int job, double *traces, double *spectra)
+{
+    if (!b || job < 0 || job >= (int)b->jobs.size()) return GRT_ERR_ARG;
+    return grt_plan_fetch(b->jobs[job], traces, spectra);
+}
+
+extern "C" int grt_batch_fetch_freqs(grt_batch *b, int job, int n_freq, const int *freq_idx, double *spectra)
+{
+    if (!b || job < 0 || job >= (int)b->jobs.size()) return GRT_ERR_ARG;
+    return grt_plan_fetch_freqs(b->jobs[job], n_freq, freq_idx, spectra);
+}
+
+extern "C" int grt_batch_info(const grt_batch *b, int job, grt_report *r, grt_tune *t)
+{
+    if (!b || job < -1 || job >= (int)b->jobs.size()) return GRT_ERR_ARG;
+    if (r) {
+        if (job < 0) *r = b->rep;
+        else grt_plan_info(b->jobs[job], r);
+    }
+    if (t) *t = b->tune;
+    return GRT_OK;
+}

@@ -295,44 +295,12 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigne
     return false;
 }
 
+// The per-(w,k) evaluation of one thread: job A, its layer table for
+// frequency iw already staged in T, wavenumber index j (< nk[iw]).
 template <typename R>
-#ifndef GRT_POINT_MINB
-#define GRT_POINT_MINB 1   // resident blocks per SM the register allocation must allow
-#endif
-__global__ void __launch_bounds__(kGrtThreads, GRT_POINT_MINB) grt_point_kernel(GrtArgs<R> A)
+__device__ __forceinline__ void grt_point(const GrtArgs<R> &A, const LayerW<R> *T, int iw, int j)
 {
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    __shared__ __align__(8) unsigned long long bar;
-    LayerW<R> *T = reinterpret_cast<LayerW<R> *>(smem_raw);
-
-    const int2 tile = A.tiles[blockIdx.x];
-    const int iw = tile.x;
-    const int j = tile.y + threadIdx.x;
     const int L = A.L, s = A.s, rl = A.rl;
-    const unsigned bytes = (unsigned)(L * sizeof(LayerW<R>));
-    const uint32_t sbar = (uint32_t)__cvta_generic_to_shared(&bar);
-    const uint32_t sdst = (uint32_t)__cvta_generic_to_shared(T);
-
-    // ---- stage the frequency's layer table: TMA bulk copy -> mbarrier
-    if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sbar) : "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        const LayerW<R> *src = A.tab + (size_t)iw * L;
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(sbar), "r"(bytes) : "memory");
-        asm volatile(
-            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(sdst),
-            "l"(src), "r"(bytes), "r"(sbar)
-            : "memory");
-    }
-    // lanes past the frequency's last wavenumber leave now (no block-wide
-    // synchronisation follows; lane 0 of a tile is always valid and waits
-    // for the table copy it issued): evaluating them would hold their warps
-    if (j >= A.nk[iw]) return;
-    if (!mbar_wait(sbar, 0, A.err)) return;
-
     const int jj = j;
     const double kd = A.dk * (A.ks ? A.ks[iw] : 1) * jj;
     K2<R> k2;
@@ -622,6 +590,96 @@ __global__ void __launch_bounds__(kGrtThreads, GRT_POINT_MINB) grt_point_kernel(
             store_q(A, QT_N + QT_A20, out, v0);
             store_q(A, QT_N + QT_A21, out, v1);
         }
+    }
+}
+
+#ifndef GRT_POINT_MINB
+#define GRT_POINT_MINB 1   // resident blocks per SM the register allocation must allow
+#endif
+
+// stage the layer table of (job, frequency) into shared memory with a TMA bulk
+// copy issued by thread 0; every thread waits on the mbarrier phase
+template <typename R>
+__device__ __forceinline__ bool stage_table(const GrtArgs<R> &A, int iw, LayerW<R> *T, uint32_t sbar,
+                                            uint32_t phase, bool wait)
+{
+    if (threadIdx.x == 0) {
+        const unsigned bytes = (unsigned)(A.L * sizeof(LayerW<R>));
+        const uint32_t sdst = (uint32_t)__cvta_generic_to_shared(T);
+        const LayerW<R> *src = A.tab + (size_t)iw * A.L;
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(sbar), "r"(bytes) : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(sdst),
+            "l"(src), "r"(bytes), "r"(sbar)
+            : "memory");
+    }
+    return wait ? mbar_wait(sbar, phase, A.err) : true;
+}
+
+// One job: one block per (frequency, block of kGrtThreads wavenumbers).
+template <typename R>
+__global__ void __launch_bounds__(kGrtThreads, GRT_POINT_MINB) grt_point_kernel(GrtArgs<R> A)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) unsigned long long bar;
+    LayerW<R> *T = reinterpret_cast<LayerW<R> *>(smem_raw);
+    const int2 tile = A.tiles[blockIdx.x];
+    const int iw = tile.x;
+    const int j = tile.y + threadIdx.x;
+    const uint32_t sbar = (uint32_t)__cvta_generic_to_shared(&bar);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sbar) : "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    stage_table(A, iw, T, sbar, 0, false);
+    // lanes past the frequency's last wavenumber leave now (no block-wide
+    // synchronisation follows; lane 0 of a tile is always valid and waits
+    // for the table copy it issued): evaluating them would hold their warps
+    if (j >= A.nk[iw]) return;
+    if (!mbar_wait(sbar, 0, A.err)) return;
+    grt_point(A, T, iw, j);
+}
+
+// Many jobs in one persistent launch.  tiles[t] = (job, frequency, first
+// wavenumber index, 0), ordered job by job and frequency by frequency; block
+// b takes the contiguous run [b n / G, (b + 1) n / G) of the n tiles, so it
+// restages the layer table only when the (job, frequency) changes.  NT
+// threads per block evaluate NT consecutive wavenumbers of a tile.
+template <typename R, int NT>
+__global__ void __launch_bounds__(NT, 1) grt_batch_kernel(const GrtArgs<R> *__restrict__ jobs,
+                                                           const int4 *__restrict__ tiles, int ntiles,
+                                                           unsigned int *err)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) unsigned long long bar;
+    LayerW<R> *T = reinterpret_cast<LayerW<R> *>(smem_raw);
+    const uint32_t sbar = (uint32_t)__cvta_generic_to_shared(&bar);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sbar) : "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    const int t0 = (int)((long long)blockIdx.x * ntiles / gridDim.x);
+    const int t1 = (int)((long long)(blockIdx.x + 1) * ntiles / gridDim.x);
+    int cur_job = -1, cur_iw = -1;
+    uint32_t phase = 0;
+    for (int t = t0; t < t1; t++) {
+        const int4 tl = tiles[t];
+        const GrtArgs<R> &A = jobs[tl.x];
+        if (tl.x != cur_job || tl.y != cur_iw) {
+            __syncthreads();                       // every thread is done with the old table
+            const bool ok = stage_table(A, tl.y, T, sbar, phase, true);
+            if (__syncthreads_or(!ok)) {
+                if (threadIdx.x == 0) atomicOr(err, 1u);
+                return;
+            }
+            phase ^= 1u;
+            cur_job = tl.x;
+            cur_iw = tl.y;
+        }
+        const int j = tl.z + threadIdx.x;
+        if (j < A.nk[tl.y]) grt_point(A, T, tl.y, j);
     }
 }
 

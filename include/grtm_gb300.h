@@ -156,6 +156,43 @@ GRT_API int grt_mlp_loss_grad(grt_mlp *mlp, int n, const float *x, const float *
 GRT_API int grt_mlp_train(grt_mlp *mlp, int n, const float *x, const float *t, int epochs, int batch, float lr,
                           unsigned long long seed, float *loss);
 
+/* Batches: many jobs -- layered models with any layer count, source depth,
+ * receiver set, grid and length -- executed together.  The per-(w,k) kernel
+ * runs as one persistent launch over the wavenumber tiles of every job; each
+ * job's Bessel table, wavenumber sum and spectral stage follow on side
+ * streams; the whole execution is captured once into a CUDA graph, so each
+ * grt_batch_execute is a single graph launch.  With autotune != 0 the GRT
+ * launch shape (wavenumbers per tile = threads per block, persistent grid
+ * size) is picked by timing the candidates on a sample of the batch's tiles;
+ * otherwise 128 threads and one block per resident slot.  All jobs share one
+ * precision.  No counterpart in the reference (one model per call). */
+typedef struct grt_job {
+    const grt_model *model;
+    const grt_opts *opts;
+    int n_dist;
+    const double *dist;
+} grt_job;
+
+#define GRT_TUNE_MAX 16
+typedef struct grt_tune {
+    int tuned;                     /* 1 when the shape was picked by timing */
+    int grt_threads, grt_blocks;   /* chosen GRT launch shape */
+    int n_cand;                    /* candidates tried */
+    int cand_threads[GRT_TUNE_MAX], cand_blocks[GRT_TUNE_MAX];
+    float cand_ms[GRT_TUNE_MAX];   /* their times on the sample */
+    double sample_fraction;        /* fraction of the tiles timed */
+} grt_tune;
+
+typedef struct grt_batch grt_batch;
+GRT_API int grt_batch_create(grt_ctx *ctx, int n_jobs, const grt_job *jobs, int autotune, grt_batch **batch);
+/* report: aggregate (n_wk, bytes, launches; ms_grt and ms_total of the graph) */
+GRT_API int grt_batch_execute(grt_batch *batch, grt_report *report);
+GRT_API int grt_batch_fetch(grt_batch *batch, int job, double *traces, double *spectra);
+GRT_API int grt_batch_fetch_freqs(grt_batch *batch, int job, int n_freq, const int *freq_idx, double *spectra);
+/* job = -1: the batch's aggregate report */
+GRT_API int grt_batch_info(const grt_batch *batch, int job, grt_report *report, grt_tune *tune);
+GRT_API void grt_batch_destroy(grt_batch *batch);
+
 /* create + execute + fetch + destroy */
 GRT_API int grt_run(grt_ctx *ctx, const grt_model *model, const grt_opts *opts, int n_dist,
             const double *dist, double *traces, double *spectra, grt_report *report);

@@ -1,0 +1,60 @@
+"""Batches of uneven jobs in one graph: the batched persistent GRT launch
+and the per-job stages must give exactly what the jobs give one by one."""
+import math
+
+import numpy as np
+import pytest
+
+
+def _jobs(g, precision):
+    from grtm_cuda_gb300 import synth
+    out = []
+    for seed, nl, log2n, nr in ((11, 3, 9, 5), (12, 17, 10, 23), (13, 41, 9, 2)):
+        rng = np.random.default_rng(seed)
+        m = synth.crust(rng, nl, rng.uniform(1.0, 30.0))
+        d = np.sort(rng.uniform(5.0, 400.0, nr))
+        o = g.make_opts(0.05, log2n, sigma_factor=math.pi, k_mode=g.K_FIXED, nk_fixed=600 + 37 * seed,
+                        precision=precision, fix=g.FIX_ALL)
+        out.append((g.make_model(**m), o, d))
+    return out
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import grtm_cuda_gb300 as g
+    c = g.Context()
+    yield c
+    c.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_batch_equals_single_jobs(ctx, prec):
+    import grtm_cuda_gb300 as g
+    jobs = _jobs(g, g.FP32 if prec == "fp32" else g.FP64)
+    b = g.Batch(ctx, jobs, autotune=(prec == "fp32"))
+    rep = b.execute()
+    assert rep.n_wk == sum(g.grid(m, o)["n_wk"] for m, o, _ in jobs)
+    first = [b.fetch(j)[0] for j in range(len(jobs))]
+    b.execute()                                        # the graph replays
+    for j, (m, o, d) in enumerate(jobs):
+        t1, _, _ = g.run(m, o, d, ctx=ctx)
+        t2 = b.fetch(j)[0]
+        assert np.array_equal(t2, first[j])
+        assert np.array_equal(t1, t2)
+    _, tune = b.info()
+    if prec == "fp32":
+        assert tune["tuned"] == 1 and len(tune["candidates"]) >= 3
+        assert (tune["grt_threads"], tune["grt_blocks"]) in [(c[0], c[1]) for c in tune["candidates"]]
+    b.close()
+
+
+@pytest.mark.gpu
+def test_batch_rejects_mixed_precision(ctx):
+    import grtm_cuda_gb300 as g
+    jobs = _jobs(g, g.FP32)
+    m, o, d = jobs[1]
+    o64 = g.make_opts(0.05, 10, sigma_factor=math.pi, k_mode=g.K_FIXED, nk_fixed=512, precision=g.FP64)
+    with pytest.raises(g.GrtError) as e:
+        g.Batch(ctx, [jobs[0], (m, o64, d)])
+    assert e.value.status == g.ERR_ARG
