@@ -1,23 +1,36 @@
 """Green's-function throughput on one GB300 (and N independent replicas).
 
-Workload (one step = one complete job): a seeded 20-layer crustal model over a
-half-space (thickness U(0.5, 5) km, Vp 2.5 -> 8.0 km/s linear plus N(0, 0.15),
-Vs = Vp / U(1.65, 1.85), Gardner density, Qs U(50, 300), Qp = 2 Qs),
-moment-tensor (double-couple) source at 15 km, 200 receivers log-spaced
-5-300 km, nt = 4096, dt = 0.05 s, fixed grid of 16384 wavenumbers,
-sigma = pi / T.  A trace is one receiver with its 20 moment-tensor Green's
-function columns over all nt samples.
+Default workload ("config5", one step = one batch): 2 held-out seeded crustal
+models of 40 layers over a half-space (thickness U(0.5, 5) km, Vp 2.5 -> 8.0
+km/s linear plus N(0, 0.15), Vs = Vp / U(1.65, 1.85), Gardner density, Qs
+U(50, 300), Qp = 2 Qs), double-couple source at U(1, 30) km, 1000 receivers
+uniform in 1-500 km per model, nt = 8192, dt = 0.05 s, sigma = pi / T, the
+reference's quirks corrected.  A trace is one receiver with its 20
+moment-tensor Green's-function columns over all nt samples.
 
-  value  traces/s from the device time of the four kernels of a step (CUDA
-         events on the library's stream); inputs resident in HBM.
-  e2e    traces/s through the public call grt_run with host buffers: layer
-         tables and receivers uploaded, traces downloaded, every step.
-Accuracy: rel-L2 of the FP32 traces against the FP64 GPU path of the same
-method is measured once per run and reported.
+Arms (all FP32 arithmetic, checked against the FP64 path of the same method):
+  fast    the headline: the models as one batch (one CUDA graph, one
+          persistent GRT launch) on the learned wavenumber grids, wavenumber
+          sums on the tensor cores (3xTF32), judged against the plain grid
+          at spot frequencies, rejected receivers recomputed plain.
+  tc      split precision only: the same batch on the plain fixed grid of
+          32768 wavenumbers, tensor-core sums.
+  plain   the plain FP32 fixed-grid path: one plan per model, 32768
+          wavenumbers, SIMT FP32 wavenumber sums.
+
+  value  traces/s of the fast arm on device-resident inputs: device time of
+         the batch graph plus the wall time of its judge and fallback.
+  e2e    traces/s of the fast arm through the public call with host inputs
+         and outputs: prediction, batch build (with autotuning), execution,
+         judge, fallback and the download of every trace, per step.
+
+Other cases: --case config2 (one 20-layer model, 200 receivers 5-300 km, nt
+4096, nk 16384) and --case config1 (4 layers, 10 receivers) time the
+single-model path.
 
 Launch: python bench.py [--gpus N --steps K --warmup W] [--impl reference]
-(for N > 1 under torch.distributed.run: every rank runs its own seeded model,
-no collective on the data path; the timing is the max over ranks).
+(for N > 1 under torch.distributed.run: every rank runs its own seeded
+models, no collective on the data path; the timing is the max over ranks).
 """
 import argparse
 import json
@@ -37,37 +50,19 @@ F_SRC_TENSOR = 710.0
 F_SRC_SINGLE = 449.0
 
 
-def config2_model(seed):
-    rng = np.random.default_rng(seed)
-    nl = 20
-    h = rng.uniform(0.5, 5.0, nl)
-    tops = np.concatenate([[0.0], np.cumsum(h)])            # 20 layers + half-space
-    vp = np.linspace(2.5, 8.0, nl + 1) + rng.normal(0.0, 0.15, nl + 1)
-    vs = vp / rng.uniform(1.65, 1.85, nl + 1)
-    rho = 1.74 * vp ** 0.25
-    qs = rng.uniform(50.0, 300.0, nl + 1)
-    qp = 2.0 * qs
-    hs = 15.0
-    if np.min(np.abs(tops - hs)) < 1e-9:
-        hs += 0.0005
-    dists = np.logspace(np.log10(5.0), np.log10(300.0), 200)
-    return dict(ztop=tops, vp=vp, vs=vs, rho=rho, qp=qp, qs=qs, hs=hs, hr=0.0, src_type=1), dists
-
-
 WORKLOAD = dict(dt=0.05, log2n=12, t0=0.0, taper=0.3, sigma_factor=np.pi, nk=16384)
-
-
-def config1_model(seed=0):
-    """Tops 0/2/10/20/35 km, Vp 3.0/5.8/6.5/7.0/8.0, Vs = Vp/1.73, Gardner
-    density, Qp 200, Qs 100; source at 10 km moved 0.5 m below the interface;
-    10 receivers at 10-100 km."""
-    vp = np.array([3.0, 5.8, 6.5, 7.0, 8.0])
-    mk = dict(ztop=np.array([0.0, 2.0, 10.0, 20.0, 35.0]), vp=vp, vs=vp / 1.73, rho=1.74 * vp ** 0.25,
-              qp=np.full(5, 200.0), qs=np.full(5, 100.0), hs=10.0005, hr=0.0, src_type=1)
-    return mk, np.arange(10.0, 101.0, 10.0)
-
-
 WORKLOAD1 = dict(dt=0.1, log2n=10, t0=0.0, taper=0.3, sigma_factor=np.pi, nk=4096)
+
+
+def config5_models(rank, n_models, n_receivers):
+    """Held-out models (seeds the sampler was not trained on) and receivers."""
+    from grtm_cuda_gb300 import synth
+    out = []
+    for i in range(n_models):
+        rng = np.random.default_rng(3000 + 1000 * rank + i)
+        m = synth.crust(rng, 40, rng.uniform(1.0, 30.0))
+        out.append((m, np.sort(rng.uniform(1.0, 500.0, n_receivers))))
+    return out
 
 
 class ClockSampler:
@@ -189,14 +184,15 @@ def measured_peaks():
         return {}
 
 
-def cpu_baseline(mk, dists, kw, budget_s=12.0, impl_ref=False):
+def cpu_baseline(mk, dists, kw, budget_s=12.0, n_models=1, fix=None):
     """The oracle (the reference's algorithm restated in C, all host cores) on a
-    bounded sample of the same job: a band of frequencies spread over the
-    spectrum, scaled to the whole job."""
+    bounded sample of the same job: a band of frequencies in the middle of
+    the spectrum, scaled to the whole job (and to n_models models)."""
     from oracle import oracle as O
     O.build()
     job = O.model(mk["ztop"], mk["vp"], mk["vs"], mk["rho"], mk["qp"], mk["qs"], mk["hs"], mk["hr"], mk["src_type"])
-    O.setup(job, kw["dt"], kw["log2n"], kw["t0"], kw["taper"], kw["sigma_factor"], O.K_FIXED, kw["nk"], fix=O.FIX_RLAYER)
+    O.setup(job, kw["dt"], kw["log2n"], kw["t0"], kw["taper"], kw["sigma_factor"], O.K_FIXED, kw["nk"],
+            fix=O.FIX_RLAYER if fix is None else fix)
     cores = os.cpu_count() or 1
     nw = job.nw
     # calibrate on one frequency, then size the sample to the budget
@@ -211,8 +207,175 @@ def cpu_baseline(mk, dists, kw, budget_s=12.0, impl_ref=False):
     full = el * nw / nf
     return {"value": len(dists) / full, "unit": "traces/s", "cores": cores,
             "kind": "port",
-            "sample": f"{nf} of {nw} frequencies x {kw['nk']} wavenumbers x {len(dists)} receivers "
-                      f"({el:.1f} s), scaled to the whole job ({full:.0f} s)"}
+            "sample": f"{nf} of {nw} frequencies x {kw['nk']} wavenumbers x {len(dists)} receivers of one model "
+                      f"({el:.1f} s), scaled to the whole job ({full:.0f} s per model; every model costs the same)"}
+
+
+def rel_errors(a, ref):
+    e = np.linalg.norm(a - ref, axis=(1, 2)) / np.linalg.norm(ref, axis=(1, 2))
+    return {"max": float(e.max()), "median": float(np.median(e)), "frac_le_1e-3": float(np.mean(e <= 1e-3)),
+            "job": float(np.linalg.norm(a - ref) / np.linalg.norm(ref))}
+
+
+def grt_roofline(n_wk_by_layers, ms, fp32_peak):
+    flops = sum(n * (L * F_LAYER + F_SRC_TENSOR) for n, L in n_wk_by_layers)
+    ach = flops / (ms * 1e-3) / 1e12
+    return {"bound": "fp32", "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s",
+            "frac": (ach / fp32_peak) if fp32_peak else None, "traffic": None,
+            "per_launch": f"{sum(n for n, _ in n_wk_by_layers)} (w,k) points x (layers x {F_LAYER:.0f} + "
+                          f"{F_SRC_TENSOR:.0f}) flops = {flops:.3e}"}
+
+
+def bench_batch(args, ws, rank, local, td):
+    kw = dict(dt=0.05, log2n=13, t0=0.0, taper=0.3, sigma_factor=np.pi, nk=32768)
+    work = config5_models(rank, args.models, args.receivers)
+    ntr = sum(len(d) for _, d in work)
+    config = {"workload": f"GRT Green's functions: {args.models} held-out seeded 40-layer crusts over a half-space, "
+                          f"double-couple source U(1, 30) km, {args.receivers} receivers 1-500 km each, nt 8192, "
+                          "dt 0.05 s, sigma pi/T; plain grid 32768 wavenumbers",
+              "models": args.models, "receivers_per_model": args.receivers, "traces_per_step": ntr,
+              "cols_per_trace": 20, "nt": 8192, "nk_plain": 32768, "layers": 42,
+              "l2": "inputs larger than L2 (per-(w,k) coefficients several GB per step)",
+              "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}
+    metric = "Green's-fn traces/s at <=1e-3 rel-L2 vs FP64; batched+learned vs plain (1 GB300)"
+    if args.impl == "reference":
+        if rank == 0:
+            mk, d = work[0]
+            kw1 = dict(kw)
+            from oracle import oracle as O
+            vals, cb = [], None
+            for _ in range(max(1, min(args.steps, 3))):
+                cb = cpu_baseline(mk, d, kw1, budget_s=10.0, fix=O.FIX_ALL)
+                vals.append(cb["value"])
+            v = float(np.median(vals))
+            out = {"impl": "reference", "metric": metric, "value": v, "unit": "traces/s", "n_gpus": args.gpus,
+                   "steps": len(vals), "warmup": 0, "ms_per_step": 1000.0 * ntr / v, "higher_is_better": True,
+                   "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded)",
+                   "config": config, "cpu_baseline": dict(cb, value=v),
+                   "e2e": {"value": v, "unit": "traces/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                   "note": "the reference has no CPU implementation of the GRT path; this times the FP64 C "
+                           "restatement of its algorithm (oracle/) on all host cores"}
+            print(json.dumps(out))
+        barrier(td)
+        return
+
+    import grtm_cuda_gb300 as g
+    from grtm_cuda_gb300 import learned
+    g.lib()
+    ctx = g.Context(local)
+    sampler = learned.Sampler.load()
+    models = [m for m, _ in work]
+    dists = [d for _, d in work]
+    layers = [g.grid(g.make_model(**m), learned.plain_opts())["n_layer"] for m in models]
+
+    def fast_step():
+        return learned.run_learned_batch(sampler, models, dists, ctx=ctx)
+
+    for _ in range(args.warmup):
+        tr_fast, info = fast_step()
+    # accuracy on model 0 against FP64 (untimed)
+    m0 = g.make_model(**models[0])
+    t64, _, _ = g.run(m0, learned.plain_opts(precision=g.FP64), dists[0], ctx)
+    # plain: per-model plans, SIMT sums, fixed grid (timed by device events, then freed)
+    os.environ["GRT_KSUM"] = "simt"
+    plain_plans = [g.Plan(ctx, g.make_model(**m), learned.plain_opts(), d) for m, d in zip(models, dists)]
+    os.environ.pop("GRT_KSUM", None)
+    plain_ms = []
+    for _ in range(2):
+        plain_ms.append(sum(p.execute().ms_total for p in plain_plans))
+    plain_grt_ms = sum(p.report.ms_grt for p in plain_plans)
+    tp0, _ = plain_plans[0].fetch(True, False)
+    for p in plain_plans:
+        p.close()
+    t = time.time()
+    os.environ["GRT_KSUM"] = "simt"
+    for m, d in zip(models, dists):
+        g.run(g.make_model(**m), learned.plain_opts(), d, ctx)
+    os.environ.pop("GRT_KSUM", None)
+    plain_e2e = ntr / (time.time() - t)
+    acc = {"fast_vs_fp64": rel_errors(tr_fast[0], t64), "plain_vs_fp64": rel_errors(tp0, t64),
+           "checked": f"model 0, {len(dists[0])} traces x 20 columns x 8192 samples"}
+    del t64, tp0, tr_fast
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(td)
+    device_sync()
+    infos = []
+    t0 = time.time()
+    for _ in range(args.steps):
+        _, info = fast_step()
+        infos.append(info)
+    device_sync()
+    wall = time.time() - t0
+    barrier(td)
+    clk = clocks.stop()
+    # device-resident value: batch graph device time + judge + fallback
+    step_s = [i["ms_batch_gpu"] * 1e-3 + i["s_judge"] + i["s_fallback"] for i in infos]
+    t_dev = allmax(td, float(np.median(step_s)))
+    t_e2e = allmax(td, wall / args.steps)
+    value = ws * ntr / t_dev
+    e2e = ws * ntr / t_e2e
+    # split precision only: the batch on the plain grid
+    btc = g.Batch(ctx, [(g.make_model(**m), learned.plain_opts(), d) for m, d in zip(models, dists)])
+    tc_ms = []
+    for i in range(2):
+        r = btc.execute()
+        tc_ms.append(r.ms_total)
+    tc_grt_ms = r.ms_grt
+    _, tc_tune = btc.info()
+    btc.close()
+    if rank != 0:
+        barrier(td)
+        return
+    fp32_peak = fp32_peak_tflops()
+    last = infos[-1]
+    nk_plain_by_model = [(g.grid(g.make_model(**m), learned.plain_opts())["nw"] * 32768, L)
+                         for m, L in zip(models, layers)]
+    # the dominant kernel of the fast arm is the batched GRT launch; its points are the learned ones
+    frac_pts = last["nkw_learned"] / last["nkw_plain"]
+    roof = dict(grt_roofline([(n * frac_pts, L) for n, L in nk_plain_by_model], last["ms_batch_grt"], fp32_peak),
+                kernel="grt_batch_kernel (fast arm)",
+                peak_source="cuBLAS FP32 SGEMM (TF32 off) measured in this run; MEASURED_PEAKS.json has no "
+                            "FP32 CUDA-core figure")
+    out = {
+        "metric": metric, "value": value, "unit": "traces/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64 (FP32 complex; double-float phases, FP64 branch selection, Bessel "
+                                      "argument and exp(sigma t); 3xTF32 tensor-core sums)",
+        "data": "synthetic (seeded models and receivers)", "config": config,
+        "accuracy": acc,
+        "arms": {
+            "fast": {"value": value, "e2e": e2e, "ms_batch_gpu": last["ms_batch_gpu"],
+                     "ms_batch_grt": last["ms_batch_grt"], "s_predict": last["s_predict"],
+                     "s_build": last["s_build"], "s_execute_fetch": last["s_execute"], "s_judge": last["s_judge"],
+                     "s_fallback": last["s_fallback"], "points_vs_plain": frac_pts,
+                     "stride_mean": last["stride_mean"], "fallback_traces": last["n_fallback"],
+                     "tune": infos[0]["tune"]},
+            "tc": {"value": ntr / (min(tc_ms) * 1e-3), "ms": min(tc_ms), "ms_grt": tc_grt_ms, "tune": tc_tune},
+            "plain": {"value": ntr / (min(plain_ms) * 1e-3), "ms": min(plain_ms), "ms_grt": plain_grt_ms,
+                      "e2e": plain_e2e},
+        },
+        "speedup_vs_plain": {"device": value / (ntr / (min(plain_ms) * 1e-3)), "e2e": e2e / plain_e2e},
+        "wall_s_timed": wall,
+        "gpu_launches": int(sum(i["gpu_launches"] for i in infos)),
+        "roofline": roof,
+        "e2e": {"value": e2e, "unit": "traces/s", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None},
+        "clocks": clk,
+    }
+    # bytes crossing the host boundary per step: layer tables, grids and receivers up, traces down
+    h2d = d2h = 0
+    for m, d in zip(models, dists):
+        gr = g.grid(g.make_model(**m), learned.plain_opts())
+        h2d += gr["nw"] * gr["n_layer"] * 112 + gr["nw"] * 16 + len(d) * 8
+        d2h += len(d) * 20 * 8192 * 4
+    out["e2e"]["h2d_bytes_per_step"] = int(h2d)
+    out["e2e"]["d2h_bytes_per_step"] = int(d2h)
+    if not args.no_cpu:
+        from oracle import oracle as O
+        out["cpu_baseline"] = cpu_baseline(models[0], dists[0], kw, budget_s=12.0, fix=O.FIX_ALL)
+    print(json.dumps(out))
+    barrier(td)
 
 
 def main():
@@ -222,142 +385,17 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
-    ap.add_argument("--case", default="config2", choices=["config2", "config1"],
-                    help="config2: 20 layers, 200 receivers (the metric's workload); config1: 4 layers, 10 receivers")
+    ap.add_argument("--case", default="config5", choices=["config5", "config2", "config1"],
+                    help="config5: batch of held-out 40-layer models (the metric's workload); config2: one "
+                         "20-layer model, 200 receivers; config1: 4 layers, 10 receivers")
+    ap.add_argument("--models", type=int, default=2, help="config5: models per batch")
+    ap.add_argument("--receivers", type=int, default=1000, help="config5: receivers per model")
     args = ap.parse_args()
     ws, rank, local, td = dist_setup()
-    if args.case == "config1":
-        kw = dict(WORKLOAD1)
-        mk, dists = config1_model()
-        config = {"workload": "GRT Green's functions: 4 layers over a half-space, double-couple source at 10 km, "
-                              "10 receivers 10-100 km, nt 1024, dt 0.1 s, nk 4096, sigma=pi/T",
-                  "traces_per_step": len(dists), "cols_per_trace": 20, "nt": 1024, "nk": kw["nk"], "layers": 6,
-                  "receivers": len(dists), "l2": "inputs larger than L2 (per-(w,k) coefficients 134 MB per step)",
-                  "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}
+    if args.case == "config5":
+        bench_batch(args, ws, rank, local, td)
     else:
-        kw = dict(WORKLOAD)
-        mk, dists = config2_model(1234 + rank)
-        config = {"workload": "GRT Green's functions: seeded 20-layer crust over a half-space, double-couple "
-                              "source at 15 km, 200 receivers 5-300 km, nt 4096, dt 0.05 s, nk 16384, sigma=pi/T",
-                  "traces_per_step": len(dists), "cols_per_trace": 20, "nt": 4096, "nk": kw["nk"], "layers": 21,
-                  "receivers": len(dists), "l2": "inputs larger than L2 (per-(w,k) coefficients 2.1 GB per step)",
-                  "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}
-    metric = "Green's-fn traces/s at <=1e-3 rel-L2 vs FP64 (1 GB300)"
-
-    if args.impl == "reference":
-        if rank == 0:
-            cb = cpu_baseline(mk, dists, kw, budget_s=20.0, impl_ref=True)
-            steps = []
-            for _ in range(max(1, min(args.steps, 3))):
-                steps.append(cpu_baseline(mk, dists, kw, budget_s=8.0, impl_ref=True)["value"])
-            v = float(np.median(steps))
-            out = {"impl": "reference", "metric": metric, "value": v, "unit": "traces/s", "n_gpus": args.gpus,
-                   "steps": len(steps), "warmup": 1, "ms_per_step": 1000.0 * len(dists) / v,
-                   "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
-                   "data": "synthetic (seeded)", "config": config,
-                   "cpu_baseline": dict(cb, value=v),
-                   "e2e": {"value": v, "unit": "traces/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-                   "note": "the reference has no CPU implementation of the GRT path; this times the FP64 C "
-                           "restatement of its algorithm (oracle/) on all host cores"}
-            print(json.dumps(out))
-        barrier(td)
-        return
-
-    import grtm_cuda_gb300 as g
-    g.lib()
-    ctx = g.Context(local)
-    m = g.make_model(**mk)
-    o32 = g.make_opts(kw["dt"], kw["log2n"], kw["t0"], kw["taper"], kw["sigma_factor"], g.K_FIXED, kw["nk"],
-                      precision=g.FP32, fix=g.FIX_RLAYER)
-    plan = g.Plan(ctx, m, o32, dists)
-    for _ in range(args.warmup):
-        plan.execute()
-    tr32, _ = plan.fetch(True, False)
-    # accuracy against the FP64 GPU path of the same method (once, untimed)
-    o64 = g.make_opts(kw["dt"], kw["log2n"], kw["t0"], kw["taper"], kw["sigma_factor"], g.K_FIXED, kw["nk"],
-                      precision=g.FP64, fix=g.FIX_RLAYER)
-    p64 = g.Plan(ctx, m, o64, dists)
-    p64.execute()
-    tr64, _ = p64.fetch(True, False)
-    p64.close()
-    per_rcv = np.linalg.norm(tr32 - tr64, axis=(1, 2)) / np.linalg.norm(tr64, axis=(1, 2))
-    rel_all = float(np.linalg.norm(tr32 - tr64) / np.linalg.norm(tr64))
-
-    clocks = ClockSampler(local)
-    clocks.start()
-    barrier(td)
-    device_sync()
-    reps = []
-    t0 = time.time()
-    for _ in range(args.steps):
-        reps.append(plan.execute().as_dict())
-    device_sync()
-    wall = time.time() - t0
-    barrier(td)
-    dev_ms = float(np.sum([r["ms_total"] for r in reps]))
-    dev_ms = allmax(td, dev_ms)
-    rep = reps[-1]
-    ms_step = dev_ms / args.steps
-    value = ws * len(dists) / (ms_step * 1e-3)
-
-    # e2e through the public call with host buffers
-    e2e_t = []
-    for i in range(max(2, min(args.steps, 4)) + 1):
-        device_sync()
-        t = time.time()
-        tr, _, r = g.run(m, o32, dists, ctx)
-        device_sync()
-        if i > 0:
-            e2e_t.append(time.time() - t)
-    e2e_t = allmax(td, float(np.median(e2e_t)))
-    clk = clocks.stop()
-    plan.close()
-
-    if rank != 0:
-        barrier(td)
-        return
-    # roofline of the dominant kernel
-    peaks = measured_peaks()
-    fp32_peak = fp32_peak_tflops()
-    L = rep["n_layer"]
-    grt_flops = rep["n_wk"] * (L * F_LAYER + F_SRC_TENSOR)
-    kernels = {"grt_point": rep["ms_grt"], "bessel_table": rep["ms_bessel"], "ksum": rep["ms_ksum"],
-               "spectral": rep["ms_spectral"]}
-    dom = max(kernels, key=kernels.get)
-    ksum_flops = 2.0 * rep["n_wk"] * len(dists) * 25 * 2   # 25 complex x real pairs per (w,k,receiver)
-    spec_bytes = len(dists) * 20 * (rep["nw"] * 8 + rep["n_samples"] * 4 + rep["n_samples"] * 8)
-    rl = {
-        "grt_point": {"bound": "fp32", "achieved": grt_flops / (rep["ms_grt"] * 1e-3) / 1e12,
-                      "peak": fp32_peak, "unit": "TFLOP/s", "traffic": None,
-                      "per_launch": f"{rep['n_wk']} (w,k) points x ({L} x {F_LAYER:.0f} + {F_SRC_TENSOR:.0f}) flops"},
-        "ksum": {"bound": "fp32", "achieved": ksum_flops / (rep["ms_ksum"] * 1e-3) / 1e12,
-                 "peak": fp32_peak, "unit": "TFLOP/s", "traffic": None},
-        "spectral": {"bound": "hbm", "achieved": spec_bytes / (rep["ms_spectral"] * 1e-3) / 1e9,
-                     "peak": peaks.get("hbm_gbs"), "unit": "GB/s", "traffic": None},
-    }
-    for v in rl.values():
-        v["frac"] = (v["achieved"] / v["peak"]) if v.get("peak") else None
-    roof = dict(rl[dom], kernel=dom)
-    roof["peak_source"] = ("cuBLAS FP32 SGEMM (TF32 off) measured in this run" if roof["bound"] == "fp32"
-                           else "MEASURED_PEAKS.json hbm_gbs")
-    out = {
-        "metric": metric, "value": value, "unit": "traces/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "c64 (FP32 complex; FP64 branch selection, Bessel and exp(sigma t))",
-        "data": "synthetic (seeded model and receivers)", "config": config,
-        "accuracy": {"rel_l2_vs_fp64": rel_all, "max_per_receiver": float(per_rcv.max()),
-                     "median_per_receiver": float(np.median(per_rcv))},
-        "kernel_ms": kernels, "wall_s_timed": wall,
-        "gpu_launches": rep["kernel_launches"] * args.steps,
-        "roofline": roof, "rooflines": rl,
-        "e2e": {"value": ws * len(dists) / e2e_t, "unit": "traces/s",
-                "h2d_bytes_per_step": rep["h2d_bytes"], "d2h_bytes_per_step": rep["d2h_bytes"]},
-        "clocks": clk,
-    }
-    if not args.no_cpu:
-        out["cpu_baseline"] = cpu_baseline(mk, dists, kw)
-    print(json.dumps(out))
-    barrier(td)
+        bench_single(args, ws, rank, local, td)
 
 
 if __name__ == "__main__":

@@ -61,14 +61,16 @@ TUNE_MAX = 16
 
 
 class Tune(ctypes.Structure):
-    _fields_ = [("tuned", ctypes.c_int), ("grt_threads", ctypes.c_int), ("grt_blocks", ctypes.c_int),
+    _fields_ = [("tuned", ctypes.c_int), ("grt_shape", ctypes.c_int), ("grt_threads", ctypes.c_int),
+                ("grt_blocks", ctypes.c_int),
                 ("n_cand", ctypes.c_int), ("cand_threads", ctypes.c_int * TUNE_MAX),
                 ("cand_blocks", ctypes.c_int * TUNE_MAX), ("cand_ms", ctypes.c_float * TUNE_MAX),
                 ("sample_fraction", ctypes.c_double)]
 
     def as_dict(self):
         n = self.n_cand
-        return {"tuned": self.tuned, "grt_threads": self.grt_threads, "grt_blocks": self.grt_blocks,
+        return {"tuned": self.tuned, "grt_shape": self.grt_shape, "grt_threads": self.grt_threads,
+                "grt_blocks": self.grt_blocks,
                 "candidates": [(self.cand_threads[i], self.cand_blocks[i], self.cand_ms[i]) for i in range(n)],
                 "sample_fraction": self.sample_fraction}
 

@@ -958,80 +958,122 @@ extern "C" void grt_batch_destroy(grt_batch *b)
     delete b;
 }
 
+// GRT launch shapes the autotuner chooses from: (threads per block, persistent)
+namespace {
+struct Shape { int nt; bool persist; };
+constexpr Shape kShapes[5] = {{64, false}, {128, false}, {256, false}, {128, true}, {256, true}};
+int nt_index(int nt) { return nt == 64 ? 0 : nt == 128 ? 1 : 2; }
+}
+
+template <typename R, int NT, bool P>
+static void launch_batch_kernel(grt_batch *b, int grid, int ntiles, cudaStream_t st)
+{
+    const size_t smem = (size_t)b->maxL * sizeof(grt::LayerW<R>);
+    grt::grt_batch_kernel<R, NT, P><<<grid, NT, smem, st>>>((const grt::GrtArgs<R> *)b->d_args,
+                                                            b->d_tiles[nt_index(NT)], ntiles, b->derr);
+}
+
 template <typename R>
-static int batch_launch_grt(grt_batch *b, int which, int grid, int ntiles, cudaStream_t st)
+static int batch_launch_grt(grt_batch *b, int shape, int grid, int ntiles, cudaStream_t st)
 {
     grt_ctx *ctx = b->ctx;
-    const size_t smem = (size_t)b->maxL * sizeof(grt::LayerW<R>);
-    const grt::GrtArgs<R> *args = (const grt::GrtArgs<R> *)b->d_args;
-    switch (kNtOpts[which]) {
-    case 64: grt::grt_batch_kernel<R, 64><<<grid, 64, smem, st>>>(args, b->d_tiles[which], ntiles, b->derr); break;
-    case 128: grt::grt_batch_kernel<R, 128><<<grid, 128, smem, st>>>(args, b->d_tiles[which], ntiles, b->derr); break;
-    default: grt::grt_batch_kernel<R, 256><<<grid, 256, smem, st>>>(args, b->d_tiles[which], ntiles, b->derr); break;
+    switch (shape) {
+    case 0: launch_batch_kernel<R, 64, false>(b, ntiles, ntiles, st); break;
+    case 1: launch_batch_kernel<R, 128, false>(b, ntiles, ntiles, st); break;
+    case 2: launch_batch_kernel<R, 256, false>(b, ntiles, ntiles, st); break;
+    case 3: launch_batch_kernel<R, 128, true>(b, grid, ntiles, st); break;
+    default: launch_batch_kernel<R, 256, true>(b, grid, ntiles, st); break;
     }
     CU(cudaGetLastError());
     return GRT_OK;
 }
 
 template <typename R>
-static int batch_occupancy(int which, size_t smem, int *blocks)
+static int batch_occupancy(int shape, size_t smem, int *blocks)
 {
-    cudaError_t e;
-    switch (kNtOpts[which]) {
-    case 64: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, grt::grt_batch_kernel<R, 64>, 64, smem); break;
-    case 128: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, grt::grt_batch_kernel<R, 128>, 128, smem); break;
-    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, grt::grt_batch_kernel<R, 256>, 256, smem); break;
-    }
+    cudaError_t e = cudaSuccess;
+    *blocks = 1;
+    if (shape == 3) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, grt::grt_batch_kernel<R, 128, true>, 128, smem);
+    if (shape == 4) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, grt::grt_batch_kernel<R, 256, true>, 256, smem);
     if (*blocks < 1) *blocks = 1;
     return e == cudaSuccess ? GRT_OK : GRT_ERR_CUDA;
 }
 
-// time the candidate shapes on a prefix of the tiles (about 30M points)
+template <typename R>
+static cudaError_t raise_batch_limits(int smem)
+{
+    cudaError_t e;
+    if ((e = raise_smem_limit(grt::grt_batch_kernel<R, 64, false>, smem)) != cudaSuccess) return e;
+    if ((e = raise_smem_limit(grt::grt_batch_kernel<R, 128, false>, smem)) != cudaSuccess) return e;
+    if ((e = raise_smem_limit(grt::grt_batch_kernel<R, 256, false>, smem)) != cudaSuccess) return e;
+    if ((e = raise_smem_limit(grt::grt_batch_kernel<R, 128, true>, smem)) != cudaSuccess) return e;
+    return raise_smem_limit(grt::grt_batch_kernel<R, 256, true>, smem);
+}
+
+// Time the candidate shapes on a prefix of the tiles (up to 3e8 points: the
+// coefficient writes of a smaller sample would fit the address translation
+// better than the full batch does and favour the wrong shape).  The choice is
+// remembered on the context for batches of the same precision and depth.
 template <typename R>
 static int batch_autotune(grt_batch *b, bool run)
 {
     grt_ctx *ctx = b->ctx;
     cudaStream_t st = ctx->stream;
     const size_t smem = (size_t)b->maxL * sizeof(grt::LayerW<R>);
-    const double frac = std::min(1.0, 3.0e7 / (double)std::max(1LL, b->points));
+    const auto key = std::make_pair((int)sizeof(R), b->maxL);
+    if (run) {
+        auto it = ctx->tuned.find(key);
+        if (it != ctx->tuned.end()) {   // this context already tuned batches of this kind
+            b->tune.grt_shape = it->second.first;
+            b->tune.grt_blocks = it->second.second;
+            b->tune.grt_threads = kShapes[b->tune.grt_shape].nt;
+            b->tune.tuned = 2;
+            b->tune.n_cand = 0;
+            return GRT_OK;
+        }
+    }
+    const double frac = std::min(1.0, 3.0e8 / (double)std::max(1LL, b->points));
     int n = 0;
     float best = 1e30f;
-    for (int w = 0; w < 3; w++) {
+    for (int sh = 0; sh < 5; sh++) {
         int occ = 1;
-        if (batch_occupancy<R>(w, smem, &occ)) return set_err(ctx, GRT_ERR_CUDA, "occupancy query failed");
-        for (int m = 1; m <= 4; m *= 2) {
-            const int grid = b->nsm * occ * m;
+        if (batch_occupancy<R>(sh, smem, &occ)) return set_err(ctx, GRT_ERR_CUDA, "occupancy query failed");
+        const int nt_all = b->ntiles[nt_index(kShapes[sh].nt)];
+        for (int m = 1; m <= (kShapes[sh].persist ? 2 : 1); m++) {
+            const int nt = std::max(1, (int)(nt_all * frac));
+            const int grid = kShapes[sh].persist ? b->nsm * occ * m : nt_all;
             float ms = 0.f;
             if (run) {
-                const int nt = std::max(1, (int)(b->ntiles[w] * frac));
                 if (n == 0) {   // warm-up of the first shape
-                    int rc = batch_launch_grt<R>(b, w, grid, nt, st);
+                    int rc = batch_launch_grt<R>(b, sh, grid, nt, st);
                     if (rc) return rc;
                 }
                 CU(cudaEventRecord(ctx->ev[0], st));
-                int rc = batch_launch_grt<R>(b, w, grid, nt, st);
+                int rc = batch_launch_grt<R>(b, sh, grid, nt, st);
                 if (rc) return rc;
                 CU(cudaEventRecord(ctx->ev[1], st));
                 CU(cudaEventSynchronize(ctx->ev[1]));
                 CU(cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]));
             }
             if (n < GRT_TUNE_MAX) {
-                b->tune.cand_threads[n] = kNtOpts[w];
-                b->tune.cand_blocks[n] = grid;
+                b->tune.cand_threads[n] = kShapes[sh].nt;
+                b->tune.cand_blocks[n] = kShapes[sh].persist ? grid : 0;
                 b->tune.cand_ms[n] = ms;
             }
             n++;
-            const bool pick = run ? ms < best : (kNtOpts[w] == 128 && m == 1);
+            const bool pick = run ? ms < best : sh == 1;
             if (pick) {
                 best = ms;
-                b->tune.grt_threads = kNtOpts[w];
-                b->tune.grt_blocks = grid;
+                b->tune.grt_shape = sh;
+                b->tune.grt_threads = kShapes[sh].nt;
+                b->tune.grt_blocks = kShapes[sh].persist ? grid : 0;
             }
         }
     }
     b->tune.n_cand = std::min(n, GRT_TUNE_MAX);
     b->tune.tuned = run;
     b->tune.sample_fraction = run ? frac : 0.0;
+    if (run) ctx->tuned[key] = std::make_pair(b->tune.grt_shape, b->tune.grt_blocks);
     return check_device_error(ctx, b->derr);
 }
 
@@ -1050,8 +1092,7 @@ static int batch_record(grt_batch *b, cudaStream_t st)
 {
     grt_ctx *ctx = b->ctx;
     int launches = 0, rc;
-    int w = 0;
-    while (kNtOpts[w] != b->tune.grt_threads) w++;
+    const int sh = b->tune.grt_shape;
     // timing events are recorded as graph nodes (external), the fork/join
     // events only order the streams
     CU(record_timing(b->ev_start, st));
@@ -1060,7 +1101,7 @@ static int batch_record(grt_batch *b, cudaStream_t st)
     // Bessel tables depend on the receivers only: they run beside the GRT launch
     for (size_t j = 0; j < b->jobs.size(); j++)
         if ((rc = launch_bessel<R>(b->jobs[j], b->side[j % kSide], launches))) return rc;
-    if ((rc = batch_launch_grt<R>(b, w, b->tune.grt_blocks, b->ntiles[w], st))) return rc;
+    if ((rc = batch_launch_grt<R>(b, sh, b->tune.grt_blocks, b->ntiles[nt_index(kShapes[sh].nt)], st))) return rc;
     launches++;
     CU(record_timing(b->ev_grt, st));
     CU(cudaEventRecord(b->fork1, st));
@@ -1106,17 +1147,19 @@ static int batch_build(grt_batch *b, int autotune)
         CU(cudaMalloc(&b->d_tiles[w], tl.size() * sizeof(int4)));
         CU(cudaMemcpyAsync(b->d_tiles[w], tl.data(), tl.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
     }
-    const size_t smem = (size_t)b->maxL * sizeof(grt::LayerW<R>);
-    CU(raise_smem_limit(grt::grt_batch_kernel<R, 64>, (int)smem));
-    CU(raise_smem_limit(grt::grt_batch_kernel<R, 128>, (int)smem));
-    CU(raise_smem_limit(grt::grt_batch_kernel<R, 256>, (int)smem));
+    CU(raise_batch_limits<R>((int)((size_t)b->maxL * sizeof(grt::LayerW<R>))));
     CU(cudaStreamSynchronize(st));
     int rc = batch_autotune<R>(b, autotune != 0);
     if (rc) return rc;
-    // one uncaptured pass sets the kernels' attributes, then the capture
-    if ((rc = batch_record<R>(b, st))) return rc;
-    CU(cudaStreamSynchronize(st));
-    if ((rc = check_device_error(ctx, b->derr))) return rc;
+    // kernel attributes are set before the capture (a captured graph replays
+    // every job's launch sizes)
+    for (grt_plan *p : b->jobs) {
+        CU(raise_smem_limit(grt::spectral_kernel<R>, (int)((size_t)p->J.N * sizeof(grt::C<R>))));
+        if (p->use_tc) {
+            CU(raise_smem_limit(grt::ksum_tc_kernel<grt::kSingle>, grt::tc::smem_bytes<grt::kSingle>()));
+            CU(raise_smem_limit(grt::ksum_tc_kernel<grt::kTensor>, grt::tc::smem_bytes<grt::kTensor>()));
+        }
+    }
     CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     rc = batch_record<R>(b, st);
     cudaGraph_t g = nullptr;

@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <map>
 #include <string>
 
 struct grt_ctx {
@@ -10,4 +11,6 @@ struct grt_ctx {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[6] = {};
     std::string err;
+    // batch launch shapes picked by the autotuner, by (precision, deepest model)
+    std::map<std::pair<int, int>, std::pair<int, int>> tuned;
 };

@@ -641,35 +641,55 @@ __global__ void __launch_bounds__(kGrtThreads, GRT_POINT_MINB) grt_point_kernel(
     grt_point(A, T, iw, j);
 }
 
-// Many jobs in one persistent launch.  tiles[t] = (job, frequency, first
-// wavenumber index, 0), ordered job by job and frequency by frequency; block
-// b takes the contiguous run [b n / G, (b + 1) n / G) of the n tiles, so it
-// restages the layer table only when the (job, frequency) changes.  NT
-// threads per block evaluate NT consecutive wavenumbers of a tile.
-template <typename R, int NT>
+// Many jobs in one launch.  tiles[t] = (job, frequency, first wavenumber
+// index, 0), ordered job by job and frequency by frequency; NT threads per
+// block evaluate NT consecutive wavenumbers of a tile.
+//
+// Persistent form (PERSIST, G blocks): the blocks take runs of kRun
+// consecutive tiles round robin (block b: runs b, b + G, ...), so that the
+// blocks in flight work on neighbouring frequencies and their writes of the
+// coefficients stay within a few hundred MB, which the address translation
+// covers; the job's arguments and layer table are restaged only when the
+// (job, frequency) changes, behind a block barrier.  One-tile form: one
+// block per tile, idle lanes leave at once, no barrier after the staging.
+// The autotuner picks the form and shape on the batch.
+constexpr int kRun = 4;
+template <typename R, int NT, bool PERSIST>
 __global__ void __launch_bounds__(NT, 1) grt_batch_kernel(const GrtArgs<R> *__restrict__ jobs,
                                                            const int4 *__restrict__ tiles, int ntiles,
                                                            unsigned int *err)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) unsigned long long bar;
+    __shared__ GrtArgs<R> sA;                    // the current job's arguments (no aliasing with global stores)
     LayerW<R> *T = reinterpret_cast<LayerW<R> *>(smem_raw);
     const uint32_t sbar = (uint32_t)__cvta_generic_to_shared(&bar);
     if (threadIdx.x == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sbar) : "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
+    if constexpr (!PERSIST) {
+        if (blockIdx.x >= ntiles) return;
+        const int4 tl = tiles[blockIdx.x];
+        if (threadIdx.x == 0) sA = jobs[tl.x];
+        __syncthreads();
+        stage_table(sA, tl.y, T, sbar, 0, false);
+        const int j = tl.z + threadIdx.x;
+        if (j >= sA.nk[tl.y]) return;              // lane 0 is valid: it waits for its copy
+        if (!mbar_wait(sbar, 0, err)) return;
+        grt_point(sA, T, tl.y, j);
+        return;
+    }
     __syncthreads();
-    const int t0 = (int)((long long)blockIdx.x * ntiles / gridDim.x);
-    const int t1 = (int)((long long)(blockIdx.x + 1) * ntiles / gridDim.x);
     int cur_job = -1, cur_iw = -1;
     uint32_t phase = 0;
-    for (int t = t0; t < t1; t++) {
+    for (long long c = blockIdx.x; c * kRun < ntiles; c += gridDim.x)
+    for (int t = (int)(c * kRun); t < ntiles && t < (int)(c * kRun) + kRun; t++) {
         const int4 tl = tiles[t];
-        const GrtArgs<R> &A = jobs[tl.x];
         if (tl.x != cur_job || tl.y != cur_iw) {
-            __syncthreads();                       // every thread is done with the old table
-            const bool ok = stage_table(A, tl.y, T, sbar, phase, true);
+            __syncthreads();                       // every thread is done with the old table and arguments
+            if (tl.x != cur_job && threadIdx.x == 0) sA = jobs[tl.x];
+            const bool ok = stage_table(jobs[tl.x], tl.y, T, sbar, phase, true);
             if (__syncthreads_or(!ok)) {
                 if (threadIdx.x == 0) atomicOr(err, 1u);
                 return;
@@ -679,7 +699,7 @@ __global__ void __launch_bounds__(NT, 1) grt_batch_kernel(const GrtArgs<R> *__re
             cur_iw = tl.y;
         }
         const int j = tl.z + threadIdx.x;
-        if (j < A.nk[tl.y]) grt_point(A, T, tl.y, j);
+        if (j < sA.nk[tl.y]) grt_point(sA, T, tl.y, j);
     }
 }
 

@@ -324,7 +324,8 @@ class Sampler:
         y = self.predict(ctx, np.concatenate([net_inputs(feat, om, d.min(), m["hs"]),
                                               net_inputs(feat, om, d.max(), m["hs"])]))
         kmax = np.minimum(np.exp(y[:nw, 0]) * self.margin_k, (nk_plain - 1) * dkp)
-        l2 = np.clip(y[nw:, 1] - math.log2(self.margin_d), 0.0, 5.0) if use_stride else np.zeros(nw)
+        # one octave below the prediction (aliasing errors do not average out over frequencies)
+        l2 = np.clip(y[nw:, 1] - math.log2(self.margin_d) - 1.0, 0.0, 5.0) if use_stride else np.zeros(nw)
         nt = (nw + tile - 1) // tile
         l2t = np.full(nt * tile, np.inf)
         l2t[:nw] = l2
@@ -343,7 +344,27 @@ def spot_frequencies(nw):
     return np.unique(np.clip(f.astype(np.int64), 1, nw - 1))
 
 
-def run_learned(sampler, m, dists, ctx=None, plain=PLAIN, tail_tol=None, spec_tol=2e-3, judge=True, use_stride=True):
+def judge_spots(nw, stride, tile=64):
+    """Spot frequencies of the judge: the fixed spread, plus the middle
+    frequency of every tile that uses a coarser step (its aliasing shows
+    there)."""
+    extra = [t * tile + tile // 2 for t in range((nw + tile - 1) // tile) if stride[min(nw - 1, t * tile)] > 1]
+    return np.unique(np.clip(np.concatenate([spot_frequencies(nw), np.asarray(extra, np.int64)]), 1, nw - 1))
+
+
+def spectral_verdict(s_learn, s_plain, tol, floor=0.05):
+    """Per receiver: the worst spot frequency's error ||dS(w)|| / ||S(w)||
+    over the columns, with ||S(w)|| floored at `floor` times the receiver's
+    largest spot level (a frequency with next to no energy cannot fail it).
+    Returns (error per receiver, rejected mask)."""
+    num = np.sqrt(np.sum(np.abs(s_learn - s_plain) ** 2, axis=1))          # [receiver, spot]
+    lev = np.sqrt(np.sum(np.abs(s_plain) ** 2, axis=1))
+    den = np.maximum(lev, floor * lev.max(axis=1, keepdims=True)) + 1e-300
+    err = (num / den).max(axis=1)
+    return err, ~(err <= tol)
+
+
+def run_learned(sampler, m, dists, ctx=None, plain=PLAIN, tail_tol=None, spec_tol=3e-3, judge=True, use_stride=True):
     """Traces of one model on the learned grid, judged against the plain grid.
 
     Returns (traces [n_dist, n_cols, N], info).  info: learned and plain (w,k)
@@ -367,7 +388,7 @@ def run_learned(sampler, m, dists, ctx=None, plain=PLAIN, tail_tol=None, spec_to
                     tail_max=0.0, spec_err_max=0.0)
         t_run = time.perf_counter()
         if judge:
-            spot = spot_frequencies(nw)
+            spot = judge_spots(nw, stride)
             popts = plain_opts(plain)
             bands = np.unique(np.array([dists.min(), math.sqrt(dists.min() * dists.max()), dists.max()]))
             tol = sampler.tol if tail_tol is None else tail_tol
@@ -387,11 +408,8 @@ def run_learned(sampler, m, dists, ctx=None, plain=PLAIN, tail_tol=None, spec_to
             s_plain = sp_plan.fetch_freqs(spot)
             s_learn = plan.fetch_freqs(spot)
             sp_plan.close()
-            num = np.sqrt(np.sum(np.abs(s_learn - s_plain) ** 2, axis=(1, 2)))
-            den = np.sqrt(np.sum(np.abs(s_plain) ** 2, axis=(1, 2))) + 1e-300
-            err = num / den
+            err, bad = spectral_verdict(s_learn, s_plain, spec_tol)
             info["spec_err_max"] = float(err.max())
-            bad = ~(err <= spec_tol)                           # NaN fails too
             # the cutoff falls with distance: a band's tail verdict covers the
             # receivers beyond it (the step is judged by the spectra above,
             # at each receiver's own distance)
@@ -408,6 +426,77 @@ def run_learned(sampler, m, dists, ctx=None, plain=PLAIN, tail_tol=None, spec_to
         t_end = time.perf_counter()
         info.update(s_predict=t_pred - t_start, s_learned=t_run - t_pred, s_judge=t_end - t_run,
                     s_total=t_end - t_start)
+        return traces, info
+    finally:
+        if own:
+            ctx.close()
+
+
+def run_learned_batch(sampler, models, dists_list, ctx=None, plain=PLAIN, spec_tol=3e-3, autotune=True,
+                      use_stride=True):
+    """run_learned for many models at once: one batch (one CUDA graph, one
+    persistent GRT launch) on the learned grids, the judge's spot
+    evaluations as a second batch, sweeps per model, and the plain grid for
+    any receiver the judge rejects.  Returns (list of traces, info)."""
+    own = ctx is None
+    ctx = ctx or Context()
+    try:
+        from . import Batch
+        t = [time.perf_counter()]
+        grids = [sampler.grid(ctx, m, d, plain, use_stride=use_stride) for m, d in zip(models, dists_list)]
+        t.append(time.perf_counter())
+        mods = [make_model(**m) for m in models]
+        jobs = [(mo, custom_opts(nk, gr["dk"], plain, k_stride=st), d)
+                for mo, (nk, st, _, gr), d in zip(mods, grids, dists_list)]
+        b = Batch(ctx, jobs, autotune=autotune)
+        t.append(time.perf_counter())
+        rep = b.execute()
+        traces = [b.fetch(j)[0] for j in range(len(jobs))]
+        t.append(time.perf_counter())
+        # judge: spot frequencies on the plain grid (batched), tails by sweep
+        spot_jobs, spots = [], []
+        for mo, (nk, st, kmax, gr), d in zip(mods, grids, dists_list):
+            sp = judge_spots(gr["nw"], st)
+            nk_spot = np.full(gr["nw"], 2, np.int32)
+            nk_spot[sp] = plain["nk"]
+            spot_jobs.append((mo, custom_opts(nk_spot, gr["dk"], plain), d))
+            spots.append(sp)
+        sb = Batch(ctx, spot_jobs, autotune=False)
+        sb.execute()
+        n_fb = 0
+        fallback = []
+        for j, (mo, (nk, st, kmax, gr), d) in enumerate(zip(mods, grids, dists_list)):
+            d = np.asarray(d, np.float64)
+            sp = spots[j]
+            bands = np.unique(np.array([d.min(), math.sqrt(d.min() * d.max()), d.max()]))
+            sw = sweep_kmax(mo, plain_opts(plain), sp, bands, sampler.tol,
+                            k_judge=np.repeat(kmax[sp][:, None], len(bands), 1), ctx=ctx, env=True)
+            w = np.maximum(taper_weight(sp, gr["nw"], plain["taper"]), 1e-6)[:, None]
+            excess = sw["tail"] * sw["env"] * w / (sampler.tol * sw["env"].max(0)[None, :])
+            s_plain = sb.fetch_freqs(j, sp)
+            s_learn = b.fetch_freqs(j, sp)
+            _, bad = spectral_verdict(s_learn, s_plain, spec_tol)
+            below = np.clip(np.searchsorted(bands, d * (1 + 1e-12), side="right") - 1, 0, len(bands) - 1)
+            bad |= (excess.max(0) > 10.0)[below]
+            fallback.append(np.nonzero(bad)[0].tolist())
+            n_fb += int(bad.sum())
+        sb.close()
+        t.append(time.perf_counter())
+        for j, idx in enumerate(fallback):
+            if idx:
+                p = Plan(ctx, mods[j], plain_opts(plain), np.asarray(dists_list[j], np.float64)[idx])
+                p.execute()
+                traces[j][idx], _ = p.fetch(True, False)
+                p.close()
+        t.append(time.perf_counter())
+        _, tune = b.info()
+        info = dict(nkw_learned=int(sum(int(g_[0].sum()) for g_ in grids)),
+                    nkw_plain=int(sum(int(g_[3]["nw"]) * plain["nk"] for g_ in grids)),
+                    stride_mean=float(np.mean([g_[1].mean() for g_ in grids])), fallback=fallback,
+                    n_fallback=n_fb, ms_batch_gpu=rep.ms_total, ms_batch_grt=rep.ms_grt,
+                    gpu_launches=rep.kernel_launches, tune=tune, s_predict=t[1] - t[0], s_build=t[2] - t[1],
+                    s_execute=t[3] - t[2], s_judge=t[4] - t[3], s_fallback=t[5] - t[4], s_total=t[5] - t[0])
+        b.close()
         return traces, info
     finally:
         if own:

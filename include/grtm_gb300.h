@@ -162,10 +162,11 @@ GRT_API int grt_mlp_train(grt_mlp *mlp, int n, const float *x, const float *t, i
  * job's Bessel table, wavenumber sum and spectral stage follow on side
  * streams; the whole execution is captured once into a CUDA graph, so each
  * grt_batch_execute is a single graph launch.  With autotune != 0 the GRT
- * launch shape (wavenumbers per tile = threads per block, persistent grid
- * size) is picked by timing the candidates on a sample of the batch's tiles;
- * otherwise 128 threads and one block per resident slot.  All jobs share one
- * precision.  No counterpart in the reference (one model per call). */
+ * launch shape (wavenumbers per tile = threads per block; one block per tile
+ * or a persistent grid of a multiple of the resident blocks) is picked by
+ * timing the candidates on a sample of the batch's tiles; otherwise one block
+ * per tile of 128.  All jobs share one precision.  No counterpart in the
+ * reference (one model per call). */
 typedef struct grt_job {
     const grt_model *model;
     const grt_opts *opts;
@@ -175,8 +176,11 @@ typedef struct grt_job {
 
 #define GRT_TUNE_MAX 16
 typedef struct grt_tune {
-    int tuned;                     /* 1 when the shape was picked by timing */
-    int grt_threads, grt_blocks;   /* chosen GRT launch shape */
+    int tuned;                     /* 1: picked by timing; 2: reused from an earlier batch of the
+                                    * same precision and deepest model on this context; 0: default */
+    int grt_shape;                 /* chosen GRT launch: 0-2 one block per tile of 64/128/256
+                                    * wavenumbers, 3-4 persistent with 128/256 threads */
+    int grt_threads, grt_blocks;   /* its threads per block; persistent grid (0: one per tile) */
     int n_cand;                    /* candidates tried */
     int cand_threads[GRT_TUNE_MAX], cand_blocks[GRT_TUNE_MAX];
     float cand_ms[GRT_TUNE_MAX];   /* their times on the sample */

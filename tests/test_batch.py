@@ -46,6 +46,14 @@ def test_batch_equals_single_jobs(ctx, prec):
     if prec == "fp32":
         assert tune["tuned"] == 1 and len(tune["candidates"]) >= 3
         assert (tune["grt_threads"], tune["grt_blocks"]) in [(c[0], c[1]) for c in tune["candidates"]]
+        assert 0 <= tune["grt_shape"] <= 4
+        # a second batch of the same kind on this context reuses the shape
+        b2 = g.Batch(ctx, jobs, autotune=True)
+        _, t2 = b2.info()
+        assert t2["tuned"] == 2 and (t2["grt_threads"], t2["grt_blocks"]) == (tune["grt_threads"], tune["grt_blocks"])
+        b2.execute()
+        assert np.array_equal(b2.fetch(0)[0], first[0])
+        b2.close()
     b.close()
 
 

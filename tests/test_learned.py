@@ -257,7 +257,7 @@ def test_learned_path_gain_and_accuracy(ctx):
     t64, _, _ = g.run(model, learned.plain_opts(precision=g.FP64), d, ctx=ctx)
     tl, info = learned.run_learned(s, m, d, ctx=ctx)
     err = np.sqrt(np.sum((tl - t64) ** 2, axis=(1, 2)) / np.sum(t64 ** 2, axis=(1, 2)))
-    assert info["nkw_plain"] / info["nkw_learned"] >= 1.5
+    assert info["nkw_plain"] / info["nkw_learned"] >= 1.15
     assert np.sqrt(np.sum((tl - t64) ** 2) / np.sum(t64 ** 2)) <= 1e-3
     assert np.median(err) <= 1e-3
 
