@@ -52,6 +52,7 @@ F_SRC_SINGLE = 449.0
 
 WORKLOAD = dict(dt=0.05, log2n=12, t0=0.0, taper=0.3, sigma_factor=np.pi, nk=16384)
 WORKLOAD1 = dict(dt=0.1, log2n=10, t0=0.0, taper=0.3, sigma_factor=np.pi, nk=4096)
+WORKLOAD3S = dict(dt=0.05, log2n=10, t0=0.0, taper=0.3, sigma_factor=np.pi, nk=4096)
 
 
 def config5_models(rank, n_models, n_receivers):
@@ -192,7 +193,7 @@ def cpu_baseline(mk, dists, kw, budget_s=12.0, n_models=1, fix=None):
     O.build()
     job = O.model(mk["ztop"], mk["vp"], mk["vs"], mk["rho"], mk["qp"], mk["qs"], mk["hs"], mk["hr"], mk["src_type"])
     O.setup(job, kw["dt"], kw["log2n"], kw["t0"], kw["taper"], kw["sigma_factor"], O.K_FIXED, kw["nk"],
-            fix=O.FIX_RLAYER if fix is None else fix)
+            fix=O.FIX_ALL if fix is None else fix)
     cores = os.cpu_count() or 1
     nw = job.nw
     # calibrate on one frequency, then size the sample to the budget
@@ -217,11 +218,20 @@ def rel_errors(a, ref):
             "job": float(np.linalg.norm(a - ref) / np.linalg.norm(ref))}
 
 
+# DRAM bytes per (w,k) point of the FP32 GRT kernel (tensor-core operand layout), from one ncu capture
+# of the small 40-layer case: 6.1 MB read + 215.1 MB written for 2.10 M points (profiles/grt_point_config3s.md)
+GRT_DRAM_BYTES_PER_POINT = (6.128128e6 + 215.1104e6) / (512 * 4096)
+
+
 def grt_roofline(n_wk_by_layers, ms, fp32_peak):
     flops = sum(n * (L * F_LAYER + F_SRC_TENSOR) for n, L in n_wk_by_layers)
     ach = flops / (ms * 1e-3) / 1e12
+    pts = sum(n for n, _ in n_wk_by_layers)
     return {"bound": "fp32", "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s",
-            "frac": (ach / fp32_peak) if fp32_peak else None, "traffic": None,
+            "frac": (ach / fp32_peak) if fp32_peak else None,
+            "traffic": pts * GRT_DRAM_BYTES_PER_POINT,
+            "traffic_note": "bytes per launch, scaled by the points from the small-case ncu capture "
+                            f"({GRT_DRAM_BYTES_PER_POINT:.1f} B per point; the writes grow with the points)",
             "per_launch": f"{sum(n for n, _ in n_wk_by_layers)} (w,k) points x (layers x {F_LAYER:.0f} + "
                           f"{F_SRC_TENSOR:.0f}) flops = {flops:.3e}"}
 
@@ -378,6 +388,152 @@ def bench_batch(args, ws, rank, local, td):
     barrier(td)
 
 
+def bench_single(args, ws, rank, local, td):
+    """One model per step through a plan (the single-model path)."""
+    from grtm_cuda_gb300 import synth
+    if args.case == "config3s":
+        kw = dict(WORKLOAD3S)
+        mk, dists = synth.config3_model(1234 + rank, n_receivers=64)
+        config = {"workload": "GRT Green's functions, small profiling case: seeded 40-layer crust over a half-space, "
+                              "double-couple source at 15 km, 64 receivers 1-500 km, nt 1024, dt 0.05 s, nk 4096, "
+                              "sigma=pi/T",
+                  "traces_per_step": len(dists), "cols_per_trace": 20, "nt": 1024, "nk": kw["nk"], "layers": 42,
+                  "receivers": len(dists), "l2": "inputs larger than L2 (coefficients 268 MB per step)",
+                  "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}
+    elif args.case == "config1":
+        kw = dict(WORKLOAD1)
+        mk, dists = synth.config1_model()
+        config = {"workload": "GRT Green's functions: 4 layers over a half-space, double-couple source at 10 km, "
+                              "10 receivers 10-100 km, nt 1024, dt 0.1 s, nk 4096, sigma=pi/T",
+                  "traces_per_step": len(dists), "cols_per_trace": 20, "nt": 1024, "nk": kw["nk"], "layers": 6,
+                  "receivers": len(dists), "l2": "inputs larger than L2 (per-(w,k) coefficients 134 MB per step)",
+                  "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}
+    else:
+        kw = dict(WORKLOAD)
+        mk, dists = synth.config2_model(1234 + rank)
+        config = {"workload": "GRT Green's functions: seeded 20-layer crust over a half-space, double-couple "
+                              "source at 15 km, 200 receivers 5-300 km, nt 4096, dt 0.05 s, nk 16384, sigma=pi/T",
+                  "traces_per_step": len(dists), "cols_per_trace": 20, "nt": 4096, "nk": kw["nk"], "layers": 21,
+                  "receivers": len(dists), "l2": "inputs larger than L2 (per-(w,k) coefficients 2.1 GB per step)",
+                  "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}
+    metric = "Green's-fn traces/s at <=1e-3 rel-L2 vs FP64 (1 GB300)"
+
+    if args.impl == "reference":
+        if rank == 0:
+            cb = cpu_baseline(mk, dists, kw, budget_s=20.0)
+            steps = []
+            for _ in range(max(1, min(args.steps, 3))):
+                steps.append(cpu_baseline(mk, dists, kw, budget_s=8.0)["value"])
+            v = float(np.median(steps))
+            out = {"impl": "reference", "metric": metric, "value": v, "unit": "traces/s", "n_gpus": args.gpus,
+                   "steps": len(steps), "warmup": 1, "ms_per_step": 1000.0 * len(dists) / v,
+                   "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+                   "data": "synthetic (seeded)", "config": config,
+                   "cpu_baseline": dict(cb, value=v),
+                   "e2e": {"value": v, "unit": "traces/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                   "note": "the reference has no CPU implementation of the GRT path; this times the FP64 C "
+                           "restatement of its algorithm (oracle/) on all host cores"}
+            print(json.dumps(out))
+        barrier(td)
+        return
+
+    import grtm_cuda_gb300 as g
+    g.lib()
+    ctx = g.Context(local)
+    m = g.make_model(**mk)
+    o32 = g.make_opts(kw["dt"], kw["log2n"], kw["t0"], kw["taper"], kw["sigma_factor"], g.K_FIXED, kw["nk"],
+                      precision=g.FP32, fix=g.FIX_ALL)
+    plan = g.Plan(ctx, m, o32, dists)
+    for _ in range(args.warmup):
+        plan.execute()
+    tr32, _ = plan.fetch(True, False)
+    # accuracy against the FP64 GPU path of the same method (once, untimed)
+    o64 = g.make_opts(kw["dt"], kw["log2n"], kw["t0"], kw["taper"], kw["sigma_factor"], g.K_FIXED, kw["nk"],
+                      precision=g.FP64, fix=g.FIX_ALL)
+    p64 = g.Plan(ctx, m, o64, dists)
+    p64.execute()
+    tr64, _ = p64.fetch(True, False)
+    p64.close()
+    per_rcv = np.linalg.norm(tr32 - tr64, axis=(1, 2)) / np.linalg.norm(tr64, axis=(1, 2))
+    rel_all = float(np.linalg.norm(tr32 - tr64) / np.linalg.norm(tr64))
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(td)
+    device_sync()
+    reps = []
+    t0 = time.time()
+    for _ in range(args.steps):
+        reps.append(plan.execute().as_dict())
+    device_sync()
+    wall = time.time() - t0
+    barrier(td)
+    dev_ms = float(np.sum([r["ms_total"] for r in reps]))
+    dev_ms = allmax(td, dev_ms)
+    rep = reps[-1]
+    ms_step = dev_ms / args.steps
+    value = ws * len(dists) / (ms_step * 1e-3)
+
+    # e2e through the public call with host buffers
+    e2e_t = []
+    for i in range(max(2, min(args.steps, 4)) + 1):
+        device_sync()
+        t = time.time()
+        tr, _, r = g.run(m, o32, dists, ctx)
+        device_sync()
+        if i > 0:
+            e2e_t.append(time.time() - t)
+    e2e_t = allmax(td, float(np.median(e2e_t)))
+    clk = clocks.stop()
+    plan.close()
+
+    if rank != 0:
+        barrier(td)
+        return
+    # roofline of the dominant kernel
+    peaks = measured_peaks()
+    fp32_peak = fp32_peak_tflops()
+    L = rep["n_layer"]
+    grt_flops = rep["n_wk"] * (L * F_LAYER + F_SRC_TENSOR)
+    kernels = {"grt_point": rep["ms_grt"], "bessel_table": rep["ms_bessel"], "ksum": rep["ms_ksum"],
+               "spectral": rep["ms_spectral"]}
+    dom = max(kernels, key=kernels.get)
+    ksum_flops = 2.0 * rep["n_wk"] * len(dists) * 25 * 2   # 25 complex x real pairs per (w,k,receiver)
+    spec_bytes = len(dists) * 20 * (rep["nw"] * 8 + rep["n_samples"] * 4 + rep["n_samples"] * 8)
+    rl = {
+        "grt_point": {"bound": "fp32", "achieved": grt_flops / (rep["ms_grt"] * 1e-3) / 1e12,
+                      "peak": fp32_peak, "unit": "TFLOP/s", "traffic": None,
+                      "per_launch": f"{rep['n_wk']} (w,k) points x ({L} x {F_LAYER:.0f} + {F_SRC_TENSOR:.0f}) flops"},
+        "ksum": {"bound": "fp32", "achieved": ksum_flops / (rep["ms_ksum"] * 1e-3) / 1e12,
+                 "peak": fp32_peak, "unit": "TFLOP/s", "traffic": None},
+        "spectral": {"bound": "hbm", "achieved": spec_bytes / (rep["ms_spectral"] * 1e-3) / 1e9,
+                     "peak": peaks.get("hbm_gbs"), "unit": "GB/s", "traffic": None},
+    }
+    for v in rl.values():
+        v["frac"] = (v["achieved"] / v["peak"]) if v.get("peak") else None
+    roof = dict(rl[dom], kernel=dom)
+    roof["peak_source"] = ("cuBLAS FP32 SGEMM (TF32 off) measured in this run" if roof["bound"] == "fp32"
+                           else "MEASURED_PEAKS.json hbm_gbs")
+    out = {
+        "metric": metric, "value": value, "unit": "traces/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64 (FP32 complex; FP64 branch selection, Bessel and exp(sigma t))",
+        "data": "synthetic (seeded model and receivers)", "config": config,
+        "accuracy": {"rel_l2_vs_fp64": rel_all, "max_per_receiver": float(per_rcv.max()),
+                     "median_per_receiver": float(np.median(per_rcv))},
+        "kernel_ms": kernels, "wall_s_timed": wall,
+        "gpu_launches": rep["kernel_launches"] * args.steps,
+        "roofline": roof, "rooflines": rl,
+        "e2e": {"value": ws * len(dists) / e2e_t, "unit": "traces/s",
+                "h2d_bytes_per_step": rep["h2d_bytes"], "d2h_bytes_per_step": rep["d2h_bytes"]},
+        "clocks": clk,
+    }
+    if not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(mk, dists, kw)
+    print(json.dumps(out))
+    barrier(td)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -385,9 +541,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
-    ap.add_argument("--case", default="config5", choices=["config5", "config2", "config1"],
+    ap.add_argument("--case", default="config5", choices=["config5", "config2", "config1", "config3s"],
                     help="config5: batch of held-out 40-layer models (the metric's workload); config2: one "
-                         "20-layer model, 200 receivers; config1: 4 layers, 10 receivers")
+                         "20-layer model, 200 receivers; config1: 4 layers, 10 receivers; config3s: one 40-layer "
+                         "model, 64 receivers, nt 1024, nk 4096 (small profiling case)")
     ap.add_argument("--models", type=int, default=2, help="config5: models per batch")
     ap.add_argument("--receivers", type=int, default=1000, help="config5: receivers per model")
     args = ap.parse_args()
