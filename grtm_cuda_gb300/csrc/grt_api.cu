@@ -33,6 +33,7 @@ struct grt_plan {
     int nd = 0, nc = 0, nq = 0, ntiles = 0;
     int rt = 128, jt = 1;
     int use_tc = 0, nsplit = 1, kslice = 0;   // tensor-core wavenumber sum and its split-K
+    int bt_rows = 0;                          // > 0: Bessel table tiled by 16 receivers (unit strides)
     void *P = nullptr;                        // split-K partial sums
     float *Kt = nullptr;                      // coefficients in GEMM operand layout
     long long *kt_base = nullptr;             // per frequency tile offset into Kt (floats)
@@ -182,7 +183,13 @@ static int upload(grt_plan *p)
         for (int j0 = 0; j0 < J.nk[iw]; j0 += grt::kGrtThreads) tiles.push_back(make_int2(iw, j0));
     p->ntiles = (int)tiles.size();
     const size_t szK = (size_t)p->nq * J.nkw * 2 * sizeof(R);
-    const size_t szB = (size_t)J.nbrow * grt::NBASIS * p->nd * sizeof(R);
+    // the tensor-core sum reads the Bessel table in receiver tiles of 16 when
+    // every frequency has a unit stride (a stage's rows are then contiguous)
+    bool unit = true;
+    for (int m : J.ks) unit = unit && m == 1;
+    if (p->use_tc && unit) p->bt_rows = (J.nbrow + grt::tc::kKT - 1) / grt::tc::kKT * grt::tc::kKT;
+    const size_t szB = p->bt_rows ? (size_t)((p->nd + 15) / 16) * 16 * p->bt_rows * grt::NBASIS * sizeof(R)
+                                  : (size_t)J.nbrow * grt::NBASIS * p->nd * sizeof(R);
     const size_t ntr = (size_t)p->nd * p->nc;
     CU(cudaMalloc(&p->tab, tab.size() * sizeof(tab[0])));
     CU(cudaMalloc(&p->tiles, tiles.size() * sizeof(int2)));
@@ -192,6 +199,7 @@ static int upload(grt_plan *p)
     CU(cudaMalloc(&p->ddist, p->nd * sizeof(double)));
     if (!p->use_tc) CU(cudaMalloc(&p->K, szK));
     CU(cudaMalloc(&p->B, szB));
+    if (p->bt_rows) CU(cudaMemsetAsync(p->B, 0, szB, ctx->stream));   // padding rows and receivers stay zero
     CU(cudaMalloc(&p->S, ntr * J.nw * 2 * sizeof(R)));
     CU(cudaMalloc(&p->post, post.size() * sizeof(R)));
     CU(cudaMalloc(&p->tw, tw.size() * sizeof(R)));
@@ -317,6 +325,7 @@ static int launch_ksum_tc(grt_plan *p, cudaStream_t st, int &launches)
     T.Kt = p->Kt;
     T.kt_base = p->kt_base;
     T.B = (const float *)p->B;
+    T.bt_rows = p->bt_rows;
     T.nk = p->nk;
     T.ks = p->ks;
     T.koff = p->koff;
@@ -384,7 +393,7 @@ static int launch_bessel(grt_plan *p, cudaStream_t st, int &launches)
     const Job &J = p->J;
     const long long n = (long long)J.nbrow * p->nd;
     const int blocks = (int)((n + 255) / 256);
-    grt::bessel_table_kernel<R><<<blocks, 256, 0, st>>>((R *)p->B, J.nbrow, p->nd, J.dk, p->ddist);
+    grt::bessel_table_kernel<R><<<blocks, 256, 0, st>>>((R *)p->B, J.nbrow, p->nd, J.dk, p->ddist, p->bt_rows);
     launches++;
     CU(cudaGetLastError());
     return GRT_OK;

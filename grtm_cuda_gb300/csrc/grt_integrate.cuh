@@ -132,8 +132,17 @@ __device__ __forceinline__ void bessel_big_x(double x, float v[NBASIS])
     v[BJ2DD] = 2.0f * ix * j1 - j2 * (6.0f + xf * xf) * ix * ix;
 }
 
+// tile_rows = 0: layout B[j][b][r]; tile_rows > 0: receiver tiles of 16,
+// B[r / 16][j][b][r % 16] with tile_rows rows per tile (a stage of the
+// tensor-core sum then reads 8 consecutive rows as one contiguous block)
+__device__ __forceinline__ long long btab_index(int j, int b, int r, int nr, int tile_rows)
+{
+    if (tile_rows > 0) return (((long long)(r >> 4) * tile_rows + j) * NBASIS + b) * 16 + (r & 15);
+    return ((long long)j * NBASIS + b) * nr + r;
+}
+
 template <typename R>
-__global__ void bessel_table_kernel(R *B, int nk, int nr, double dk, const double *dist)
+__global__ void bessel_table_kernel(R *B, int nk, int nr, double dk, const double *dist, int tile_rows)
 {
     long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= (long long)nk * nr) return;
@@ -144,7 +153,7 @@ __global__ void bessel_table_kernel(R *B, int nk, int nr, double dk, const doubl
         float vf[NBASIS];
         bessel_big_x(x, vf);
 #pragma unroll
-        for (int b = 0; b < NBASIS; b++) B[((long long)j * NBASIS + b) * nr + r] = (R)vf[b];
+        for (int b = 0; b < NBASIS; b++) B[btab_index(j, b, r, nr, tile_rows)] = (R)vf[b];
         return;
     }
     double v[NBASIS];
@@ -158,7 +167,7 @@ __global__ void bessel_table_kernel(R *B, int nk, int nr, double dk, const doubl
     v[BJ1DD] = ddbj_ref(x, 1);
     v[BJ2DD] = ddbj_ref(x, 2);
 #pragma unroll
-    for (int b = 0; b < NBASIS; b++) B[((long long)j * NBASIS + b) * nr + r] = (R)v[b];
+    for (int b = 0; b < NBASIS; b++) B[btab_index(j, b, r, nr, tile_rows)] = (R)v[b];
 }
 
 // ---------------------------------------------------------------- column tables

@@ -1,17 +1,23 @@
 // grt_ksum_tc.cuh -- the wavenumber integration on the tensor cores (tcgen05).
 //
 // For every output column c (get_int_val_single / _tensor, green.cu:1558-1716)
-//   S_c(w, r) = sum_k sum_{t in c} K_{q_t}(w, k) * Bt_t(k, r),
-//   Bt_t(k, r) = coef_t r^-rpow_t k^kp_t w_k J_{b_t}(k r),
-// i.e. one GEMM per column whose K dimension runs over (k, term).  A CTA
-// owns 64 frequencies (M = 128 rows: real parts in rows 0-63, imaginary parts
-// in rows 64-127), 16 receivers (N = 16) and a slice of the k range (split-K);
-// the accumulators of all columns live in tensor memory (NC x 16 columns).
+//   S_c(w, r) = sum_{t in c} coef_t r^-rpow_t D_{p(t)}(w, r),
+//   D_p(w, r) = sum_k K_{q_p}(w, k) * w_k k^kp_p J_{b_p}(k r),
+// one GEMM per pair p = (coefficient column q, power of k, Bessel function);
+// the terms that share a pair differ only by a receiver-dependent factor,
+// applied when the accumulators are drained.  The pairs are grouped by q, so
+// that one MMA multiplies the coefficient tile of q by the Bessel operands of
+// all its pairs at once (N = 16 receivers x pairs of q): each stage reads
+// every coefficient tile from shared memory three times (3xTF32) instead of
+// three times per term.  A CTA owns 64 frequencies (M = 128 rows: real parts
+// in rows 0-63, imaginary parts in rows 64-127), 16 receivers and a slice of
+// the k range (split-K); the accumulators of all pairs live in tensor memory
+// (pairs x 16 columns).
 //
 // Precision: 3xTF32 -- each FP32 operand x is split into hi = tf32(x) and
 // lo = tf32(x - hi) and the product is hi*hi + hi*lo + lo*hi with FP32
 // accumulation (about 2^-21 relative per product).  Partial sums of the k
-// slices are added with TwoSum by spectral_tc_kernel.
+// slices are added with TwoSum by ksum_tc_reduce_kernel.
 //
 // Roles (160 threads): warps 0-3 produce operand tiles in shared memory
 // (canonical K-major layout, no swizzle: 8-row x 16-byte core matrices) and
@@ -43,19 +49,40 @@ constexpr int kATileBytes = (kM / 8) * (kKT / 4) * kCoreBytes;   // 4096: one q,
 constexpr int kBTileBytes = (kN / 8) * (kKT / 4) * kCoreBytes;   // 512: one term, one split
 constexpr uint32_t kTmemCols = 512;
 
-template <int SRC> struct TcCfg;
-template <> struct TcCfg<kSingle> {
-    static constexpr int NQ = QS_N, NC = kSingleNC, NT = 23;
+template <int SRC> struct TcCfg {
+    static constexpr int NQ = Cols<SRC>::NQ, NC = Cols<SRC>::NC, NP = Cols<SRC>::NP;
 };
-template <> struct TcCfg<kTensor> {
-    static constexpr int NQ = QT_N, NC = kTensorNC, NT = 32;
+
+// the pairs in order of their coefficient column q: slot[p] is pair p's
+// position, first[q] / count[q] the run of q's pairs
+template <int SRC> struct PairGroups {
+    int order[32], slot[32], first[16], count[16];
 };
+template <int SRC> constexpr PairGroups<SRC> make_groups()
+{
+    PairGroups<SRC> g{};
+    int n = 0;
+    for (int q = 0; q < Cols<SRC>::NQ; q++) {
+        g.first[q] = n;
+        g.count[q] = 0;
+        for (int p = 0; p < Cols<SRC>::NP; p++)
+            if (Cols<SRC>::pair(p).q == q) {
+                g.order[n] = p;
+                g.slot[p] = n;
+                n++;
+                g.count[q]++;
+            }
+    }
+    return g;
+}
 
 template <int SRC> constexpr int stage_bytes()
 {
-    return TcCfg<SRC>::NQ * 2 * kATileBytes + TcCfg<SRC>::NT * 2 * kBTileBytes;
+    return TcCfg<SRC>::NQ * 2 * kATileBytes + TcCfg<SRC>::NP * 2 * kBTileBytes;
 }
-template <int SRC> constexpr int smem_bytes() { return kStages * stage_bytes<SRC>() + 1024; }
+// raw Bessel rows of one stage: 8 rows x NBASIS x 16 receivers (tiled table)
+constexpr int kRawBytes = kKT * NBASIS * kN * 4;
+template <int SRC> constexpr int smem_bytes() { return kStages * (stage_bytes<SRC>() + kRawBytes) + 1024; }
 
 static_assert(kKT == kTileK && kM == kTileRows, "tile shape shared with the GRT kernel");
 __device__ __forceinline__ uint32_t tile_off(int row, int k) { return kt_tile_off(row, k); }
@@ -73,9 +100,11 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t saddr)
     return d;                     // base offset 0, layout type 0 (no swizzle)
 }
 
-// instruction descriptor: dense, D = F32, A = B = TF32, both K-major, M = 128, N = 16
-constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kN >> 3) << 17) |
-                            ((uint32_t)(kM >> 4) << 24);
+// instruction descriptor: dense, D = F32, A = B = TF32, both K-major, M = 128, N = n
+constexpr uint32_t idesc_n(int n)
+{
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kM >> 4) << 24);
+}
 
 __device__ __forceinline__ float tf32_rna(float x) { return grt::tf32_rna(x); }
 
@@ -104,13 +133,13 @@ __device__ __forceinline__ bool mbar_wait_b(uint32_t bar, uint32_t parity)
     return false;
 }
 
-__device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t acc)
+__device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc)
 {
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
         "setp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
-        "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(acc)
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
         : "memory");
 }
 __device__ __forceinline__ void mma_commit(uint32_t bar)
@@ -125,7 +154,8 @@ template <typename R>
 struct KsumTcArgs {
     const float *Kt;         // operand blocks written by the GRT kernel (see GrtArgs::Kt)
     const long long *kt_base;
-    const float *B;          // [nbrow][NBASIS][nr], row i at k = i dk
+    const float *B;          // [nbrow][NBASIS][nr], row i at k = i dk; or tiled (bt_rows > 0)
+    int bt_rows;             // > 0: B is [nr / 16][bt_rows][NBASIS][16] (unit strides only)
     const int *nk;           // [nw]
     const int *ks;           // [nw] k stride, constant on each tile of kW frequencies (null: 1)
     const long long *koff;   // [nw]
@@ -142,10 +172,11 @@ __global__ void __launch_bounds__(tc::kThreads, 1) ksum_tc_kernel(KsumTcArgs<flo
 {
     using namespace tc;
     using CT = Cols<SRC>;
-    constexpr int NQ = TcCfg<SRC>::NQ, NC = TcCfg<SRC>::NC, NT = TcCfg<SRC>::NT;
-    static_assert(NC * kN <= (int)kTmemCols, "accumulators exceed tensor memory");
+    constexpr int NQ = TcCfg<SRC>::NQ, NC = TcCfg<SRC>::NC, NP = TcCfg<SRC>::NP;
+    constexpr PairGroups<SRC> G = make_groups<SRC>();
+    static_assert(NP * kN <= (int)kTmemCols, "accumulators exceed tensor memory");
     extern __shared__ __align__(1024) unsigned char smem_tc[];
-    __shared__ __align__(8) unsigned long long bars[2 * kStages + 1];
+    __shared__ __align__(8) unsigned long long bars[3 * kStages + 1];
     __shared__ uint32_t tmem_base_s;
     __shared__ int fail_s;
 
@@ -169,11 +200,15 @@ __global__ void __launch_bounds__(tc::kThreads, 1) ksum_tc_kernel(KsumTcArgs<flo
     auto full_bar = [&](int s) { return (uint32_t)__cvta_generic_to_shared(&bars[s]); };
     auto empty_bar = [&](int s) { return (uint32_t)__cvta_generic_to_shared(&bars[kStages + s]); };
     const uint32_t done_bar = (uint32_t)__cvta_generic_to_shared(&bars[2 * kStages]);
+    auto raw_bar = [&](int s) { return (uint32_t)__cvta_generic_to_shared(&bars[2 * kStages + 1 + s]); };
+    const bool tiled = A.bt_rows > 0;
+    auto raw_off = [&](int s) { return (uint32_t)(kStages * stage_bytes<SRC>() + s * kRawBytes); };
     auto a_tile = [&](int s, int q, int split) {
         return (uint32_t)(s * stage_bytes<SRC>() + (q * 2 + split) * kATileBytes);
     };
-    auto b_tile = [&](int s, int t, int split) {
-        return (uint32_t)(s * stage_bytes<SRC>() + NQ * 2 * kATileBytes + (t * 2 + split) * kBTileBytes);
+    // B operands: split-major, pairs in q order, 16 rows (receivers) per pair
+    auto b_tile = [&](int s, int slot, int split) {
+        return (uint32_t)(s * stage_bytes<SRC>() + NQ * 2 * kATileBytes + (split * NP + slot) * kBTileBytes);
     };
 
     if (threadIdx.x == 0) {
@@ -183,6 +218,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) ksum_tc_kernel(KsumTcArgs<flo
             tc::mbar_init(empty_bar(s), 1);
         }
         tc::mbar_init(done_bar, 1);
+        for (int s = 0; s < kStages; s++) tc::mbar_init(raw_bar(s), 1);
         fail_s = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -200,17 +236,35 @@ __global__ void __launch_bounds__(tc::kThreads, 1) ksum_tc_kernel(KsumTcArgs<flo
     if (warp < 4) {
         // ---------------- producers
         const int tid = threadIdx.x;
-        // per-thread receiver constants for the Bessel-term operand
-        const int br = tid >> 3, bk = tid & 7;          // (receiver, k) of this thread in a stage
+        // (receiver, k) of this thread in a stage: a warp covers one 8-receiver x
+        // 4-k core matrix, so its B-operand stores fill 32 distinct banks
+        const int br = (warp & 1) * 8 + (lane >> 2), bk = (warp >> 1) * 4 + (lane & 3);
         const int rg = min(r0 + br, A.nr - 1);
         const bool rok = (r0 + br) < A.nr;
-        const double drr = A.dist[rg];
-        const float ir = (float)(1.0 / drr), ir2 = (float)(1.0 / (drr * drr));
         const int ksm = A.ks ? A.ks[w0] : 1;
         const float dk = (float)(A.dk * ksm);
         const unsigned a_bytes = (unsigned)(NQ * 2 * kATileBytes);
         const float *kt_tile = A.Kt + A.kt_base[wt];
-        // Bessel values of the next stage, loaded one stage ahead
+        const float *braw = tiled ? A.B + (size_t)rt * A.bt_rows * NBASIS * kN : nullptr;
+        // tiled table: the raw rows of a stage arrive by one bulk copy, a stage ahead
+        auto issue_raw = [&](int st_) {
+            const int s_ = st_ % kStages;
+            const float *src = braw + (size_t)(kb + st_ * kKT) * NBASIS * kN;
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(raw_bar(s_)),
+                         "r"((unsigned)kRawBytes)
+                         : "memory");
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                    sm_s + raw_off(s_)),
+                "l"(src), "r"((unsigned)kRawBytes), "r"(raw_bar(s_))
+                : "memory");
+        };
+        int raw_issued = 0;
+        if (tiled && tid == 0 && nstage > 0) {
+            issue_raw(0);
+            raw_issued = 1;
+        }
+        // untiled table: Bessel values of the next stage loaded one stage ahead
         float bv[NBASIS];
         auto load_b = [&](int st_) {
             const int k = kb + st_ * kKT + bk;
@@ -218,7 +272,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) ksum_tc_kernel(KsumTcArgs<flo
 #pragma unroll
             for (int b = 0; b < NBASIS; b++) bv[b] = kok ? __ldg(A.B + ((long long)k * ksm * NBASIS + b) * A.nr + rg) : 0.f;
         };
-        load_b(0);
+        if (!tiled) load_b(0);
         for (int st = 0; st < nstage; st++) {
             const int s = st % kStages;
             if (st >= kStages) {
@@ -227,11 +281,27 @@ __global__ void __launch_bounds__(tc::kThreads, 1) ksum_tc_kernel(KsumTcArgs<flo
                     fail_s = 1;
                 }
             }
-            if (fail_s) break;
+            // all producers are past stage st - 1 (its raw buffer may be refilled) and
+            // take one decision on failure: the OR over the producers of what each saw
+            // (the issuing warp may set fail_s at any time)
+            int any_fail;
+            asm volatile(
+                "{\n\t.reg .pred p, q;\n\t"
+                "setp.ne.s32 p, %1, 0;\n\t"
+                "bar.red.or.pred q, 1, %2, p;\n\t"
+                "selp.s32 %0, 1, 0, q;\n\t}\n"
+                : "=r"(any_fail)
+                : "r"((int)fail_s), "n"(kProducers)
+                : "memory");
+            if (any_fail) break;
             const int k0 = kb + st * kKT;
-            // A operand: one bulk copy of the (frequency tile, k stage) block the
-            // GRT kernel wrote in operand layout
             if (tid == 0) {
+                if (tiled && st + 1 < nstage) {
+                    issue_raw(st + 1);
+                    raw_issued = st + 2;
+                }
+                // A operand: one bulk copy of the (frequency tile, k stage) block the
+                // GRT kernel wrote in operand layout
                 const float *src = kt_tile + (long long)(k0 / kKT) * (NQ * 2 * kM * kKT);
                 const uint32_t dst = sm_s + a_tile(s, 0, 0);
                 asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(full_bar(s)), "r"(a_bytes)
@@ -241,31 +311,45 @@ __global__ void __launch_bounds__(tc::kThreads, 1) ksum_tc_kernel(KsumTcArgs<flo
                     "l"(src), "r"(a_bytes), "r"(full_bar(s))
                     : "memory");
             }
-            // B operand: term values coef r^-rpow k^kp w J_b(k r) for (receiver br, k bk)
+            // B operand: pair values k^kp w J_b(k r) for (receiver br, k bk)
             {
                 const int k = k0 + bk;
                 float cur[NBASIS];
+                if (tiled) {
+                    if (!tc::mbar_wait_b(raw_bar(s), (st / kStages) & 1)) {
+                        atomicOr(A.err, 2u);
+                        fail_s = 1;
+                    }
+                    const float *rs = reinterpret_cast<const float *>(sm + raw_off(s));
+                    const bool kok = k < ke && rok;
 #pragma unroll
-                for (int b = 0; b < NBASIS; b++) cur[b] = bv[b];
-                load_b(st + 1);
+                    for (int b = 0; b < NBASIS; b++) cur[b] = kok ? rs[(bk * NBASIS + b) * kN + br] : 0.f;
+                } else {
+#pragma unroll
+                    for (int b = 0; b < NBASIS; b++) cur[b] = bv[b];
+                    load_b(st + 1);
+                }
                 const float kf = dk * (float)k;
                 const float w = (k == 0) ? 0.5f * dk : dk;
                 const float wk[3] = {w, w * kf, w * kf * kf};
 #pragma unroll
-                for (int t = 0; t < NT; t++) {
-                    const Term T = CT::term(t);
-                    const Pair P = CT::pair(T.pair);
-                    float v = wk[P.kp] * cur[P.b] * (float)T.coef;
-                    if (T.rpow == 1) v *= ir;
-                    else if (T.rpow == 2) v *= ir2;
+                for (int p = 0; p < NP; p++) {
+                    const Pair P = CT::pair(p);
+                    const float v = wk[P.kp] * cur[P.b];
                     const float h = tc::tf32_rna(v), l = tc::tf32_rna(v - h);
-                    *reinterpret_cast<float *>(sm + b_tile(s, t, 0) + tc::tile_off(br, bk)) = h;
-                    *reinterpret_cast<float *>(sm + b_tile(s, t, 1) + tc::tile_off(br, bk)) = l;
+                    *reinterpret_cast<float *>(sm + b_tile(s, G.slot[p], 0) + tc::tile_off(br, bk)) = h;
+                    *reinterpret_cast<float *>(sm + b_tile(s, G.slot[p], 1) + tc::tile_off(br, bk)) = l;
                 }
             }
             // make the generic-proxy writes visible to the tensor cores, then signal
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             tc::mbar_arrive(full_bar(s));
+        }
+        // a raw copy issued for a stage that was never consumed (early exit) is
+        // waited for (bounded) before the block can leave
+        if (tiled && tid == 0 && raw_issued > 0) {
+            const int last = raw_issued - 1;
+            tc::mbar_wait_b(raw_bar(last % kStages), (last / kStages) & 1);
         }
     } else if (lane == 0) {
         // ---------------- MMA issuer (one thread of warp 4)
@@ -277,22 +361,21 @@ __global__ void __launch_bounds__(tc::kThreads, 1) ksum_tc_kernel(KsumTcArgs<flo
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            // fully unrolled: term, operand and accumulator indices are compile-time
+            // fully unrolled: group, operand and accumulator offsets are compile-time
             // constants; descriptors are the stage's base descriptor plus a constant
             const uint64_t dbase = tc::sdesc(sm_s + (uint32_t)(s * stage_bytes<SRC>()));
             const uint32_t acc0 = st == 0 ? 0u : 1u;
 #pragma unroll
-            for (int c = 0; c < NC; c++) {
-#pragma unroll
-                for (int t = CT::col(c); t < CT::col(c + 1); t++) {
-                    const int q = CT::pair(CT::term(t).pair).q;
-                    const uint32_t d = tmem + (uint32_t)(c * kN);
-                    const uint64_t ah = dbase + ((uint64_t)a_tile(0, q, 0) >> 4), al = dbase + ((uint64_t)a_tile(0, q, 1) >> 4);
-                    const uint64_t bh = dbase + ((uint64_t)b_tile(0, t, 0) >> 4), bl = dbase + ((uint64_t)b_tile(0, t, 1) >> 4);
-                    tc::mma_tf32(d, ah, bh, t == CT::col(c) ? acc0 : 1u);
-                    tc::mma_tf32(d, ah, bl, 1u);
-                    tc::mma_tf32(d, al, bh, 1u);
-                }
+            for (int q = 0; q < NQ; q++) {
+                if (G.count[q] == 0) continue;
+                const uint32_t idesc = tc::idesc_n(G.count[q] * kN);
+                const uint32_t d = tmem + (uint32_t)(G.first[q] * kN);
+                const uint64_t ah = dbase + ((uint64_t)a_tile(0, q, 0) >> 4), al = dbase + ((uint64_t)a_tile(0, q, 1) >> 4);
+                const uint64_t bh = dbase + ((uint64_t)b_tile(0, G.first[q], 0) >> 4);
+                const uint64_t bl = dbase + ((uint64_t)b_tile(0, G.first[q], 1) >> 4);
+                tc::mma_tf32(d, ah, bh, idesc, acc0);
+                tc::mma_tf32(d, ah, bl, idesc, 1u);
+                tc::mma_tf32(d, al, bh, idesc, 1u);
             }
             tc::mma_commit(empty_bar(s));   // stage s may be refilled once these MMAs finish
         }
@@ -311,25 +394,44 @@ __global__ void __launch_bounds__(tc::kThreads, 1) ksum_tc_kernel(KsumTcArgs<flo
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const int row = warp * 32 + lane;            // the lane of tensor memory this thread reads
         const int part = row / kW, wl = row % kW, w = w0 + wl;
+        // receiver factors r^-1, r^-2 of the terms
+        float irj[kN], ir2j[kN];
+#pragma unroll
+        for (int j = 0; j < kN; j++) {
+            const double dj = A.dist[min(r0 + j, A.nr - 1)];
+            irj[j] = (float)(1.0 / dj);
+            ir2j[j] = (float)(1.0 / (dj * dj));
+        }
+#pragma unroll
         for (int c = 0; c < NC; c++) {
-            uint32_t v[kN];
-            const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * kN);
-            asm volatile(
-                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
-                  "=r"(v[15])
-                : "r"(taddr)
-                : "memory");
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            float acc[kN];
+#pragma unroll
+            for (int j = 0; j < kN; j++) acc[j] = 0.f;
+#pragma unroll
+            for (int t = CT::col(c); t < CT::col(c + 1); t++) {
+                const Term T = CT::term(t);
+                uint32_t v[kN];
+                const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(G.slot[T.pair] * kN);
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                      "=r"(v[15])
+                    : "r"(taddr)
+                    : "memory");
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                const float cf = (float)T.coef;
+#pragma unroll
+                for (int j = 0; j < kN; j++) {
+                    const float f = T.rpow == 1 ? cf * irj[j] : T.rpow == 2 ? cf * ir2j[j] : cf;
+                    acc[j] = fmaf(f, __uint_as_float(v[j]), acc[j]);
+                }
+            }
             if (w < A.nw) {
 #pragma unroll
                 for (int j = 0; j < kN; j++) {
                     const int r = r0 + j;
-                    if (r < A.nr) {
-                        const float val = ok ? __uint_as_float(v[j]) : 0.f;
-                        A.P[((((long long)sp * A.nr + r) * NC + c) * A.nw + w) * 2 + part] = val;
-                    }
+                    if (r < A.nr) A.P[((((long long)sp * A.nr + r) * NC + c) * A.nw + w) * 2 + part] = ok ? acc[j] : 0.f;
                 }
             }
         }

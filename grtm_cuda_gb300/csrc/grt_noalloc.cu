@@ -186,7 +186,7 @@ extern "C" GRT_API int grt_run_noalloc(int device, const grt_model *m, const grt
     {
         long long n = (long long)J.nkmax * nd;
         grt::bessel_table_kernel<float><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
-            (float *)(scratch + o_B), J.nkmax, nd, J.dk, (const double *)(scratch + o_dist));
+            (float *)(scratch + o_B), J.nkmax, nd, J.dk, (const double *)(scratch + o_dist), 0);
         CUN(cudaGetLastError());
     }
     {
