@@ -52,6 +52,50 @@ class Report(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class Source(ctypes.Structure):
+    _fields_ = [("m", ctypes.c_double * 6), ("n_stf", ctypes.c_int), ("stf", _dp)]
+
+
+def make_source(m6, stf=None):
+    """A moment-tensor source (Mxx, Myy, Mzz, Mxy, Mxz, Myz) with an optional
+    source-time function sampled at the job's dt."""
+    s = Source()
+    for i in range(6):
+        s.m[i] = float(m6[i])
+    if stf is not None:
+        a = _arr(stf)
+        s.n_stf = len(a)
+        s.stf = _ptr(a)
+        s._keep = a
+    return s
+
+
+R_EARTH = 6371.0
+
+
+def flatten(model, r_earth=R_EARTH):
+    """Earth-flattened copy of a model dict (ztop, vp, vs, rho, qp, qs, hs,
+    hr, src_type): grt_flatten."""
+    zt, vp, vs = (_arr(model[k]) for k in ("ztop", "vp", "vs"))
+    n = len(zt)
+    zf, vpf, vsf = np.empty(n), np.empty(n), np.empty(n)
+    hs, hr = ctypes.c_double(), ctypes.c_double()
+    rc = lib().grt_flatten(n, _ptr(zt), _ptr(vp), _ptr(vs), float(model["hs"]), float(model.get("hr", 0.0)),
+                           float(r_earth), _ptr(zf), _ptr(vpf), _ptr(vsf), ctypes.byref(hs), ctypes.byref(hr))
+    if rc:
+        raise GrtError(rc, "grt_flatten (details on stderr)")
+    out = dict(model)
+    out.update(ztop=zf, vp=vpf, vs=vsf, hs=hs.value, hr=hr.value)
+    return out
+
+
+def dc_moment(strike, dip, rake, m0=1.0):
+    """Moment tensor (Mxx, Myy, Mzz, Mxy, Mxz, Myz) of a double couple."""
+    m = (ctypes.c_double * 6)()
+    lib().grt_dc_moment(float(strike), float(dip), float(rake), float(m0), m)
+    return np.array(list(m))
+
+
 class Job(ctypes.Structure):
     _fields_ = [("model", ctypes.POINTER(Model)), ("opts", ctypes.POINTER(Opts)), ("n_dist", ctypes.c_int),
                 ("dist", _dp)]
@@ -81,7 +125,8 @@ EXPORTS = ("grt_create", "grt_destroy", "grt_last_error", "grt_status_string", "
            "grt_green", "green", "grt_run_noalloc", "grt_sweep_kmax", "grt_mlp_create", "grt_mlp_destroy",
            "grt_mlp_n_params", "grt_mlp_get_params", "grt_mlp_set_params", "grt_mlp_forward",
            "grt_mlp_loss_grad", "grt_mlp_train", "grt_batch_create", "grt_batch_execute", "grt_batch_fetch",
-           "grt_batch_fetch_freqs", "grt_batch_info", "grt_batch_destroy")
+           "grt_batch_fetch_freqs", "grt_batch_info", "grt_batch_destroy", "grt_dc_moment", "grt_plan_synth",
+           "grt_batch_synth", "grt_flatten")
 
 _lib = None
 
@@ -142,6 +187,12 @@ def lib():
     L.grt_batch_info.argtypes = [vp, ctypes.c_int, P(Report), P(Tune)]
     L.grt_batch_destroy.argtypes = [vp]
     L.grt_batch_destroy.restype = None
+    L.grt_flatten.argtypes = [ctypes.c_int, _dp, _dp, _dp, ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp,
+                              _dp, _dp, _dp, _dp]
+    L.grt_dc_moment.argtypes = [ctypes.c_double] * 4 + [_dp]
+    L.grt_dc_moment.restype = None
+    L.grt_plan_synth.argtypes = [vp, P(Source), _dp, _dp]
+    L.grt_batch_synth.argtypes = [vp, ctypes.c_int, P(Source), _dp, _dp]
     _lib = L
     return L
 
@@ -241,6 +292,17 @@ class Plan:
         if spectra:
             s = s[..., 0] + 1j * s[..., 1]
         return t, s
+
+    def synth(self, m6, azimuth, stf=None):
+        """Seismograms [n_dist, 3 (Z, R, T), N] for moment tensor m6 at the
+        receivers' azimuths (degrees), convolved with stf (samples at dt)."""
+        src = make_source(m6, stf)
+        az = _arr(np.broadcast_to(azimuth, self.dists.shape))
+        out = np.empty((len(self.dists), 3, self.report.n_samples))
+        rc = lib().grt_plan_synth(self.h, ctypes.byref(src), _ptr(az), _ptr(out))
+        if rc:
+            raise GrtError(rc, self.ctx.error())
+        return out
 
     def fetch_freqs(self, freq_idx):
         """Spectra at selected frequency indices: complex [n_dist, n_cols, n_freq]."""
@@ -349,6 +411,17 @@ class Batch:
         if spectra:
             s = s[..., 0] + 1j * s[..., 1]
         return t, s
+
+    def synth(self, job, m6, azimuth, stf=None):
+        """Seismograms of one job [n_dist, 3 (Z, R, T), N]."""
+        r, _ = self.info(job)
+        src = make_source(m6, stf)
+        az = _arr(np.broadcast_to(azimuth, self.dists[job].shape))
+        out = np.empty((len(self.dists[job]), 3, r["n_samples"]))
+        rc = lib().grt_batch_synth(self.h, int(job), ctypes.byref(src), _ptr(az), _ptr(out))
+        if rc:
+            raise GrtError(rc, self.ctx.error())
+        return out
 
     def fetch_freqs(self, job, freq_idx):
         r, _ = self.info(job)

@@ -1272,3 +1272,123 @@ extern "C" int grt_batch_info(const grt_batch *b, int job, grt_report *r, grt_tu
     if (t) *t = b->tune;
     return GRT_OK;
 }
+
+// ------------------------------------------------------------------ seismograms
+// Moment tensor of a double couple (Aki & Richards, Box 4.4; x north, y east,
+// z down): strike, dip, rake in degrees, scalar moment m0.
+extern "C" void grt_dc_moment(double strike, double dip, double rake, double m0, double *m)
+{
+    if (!m) return;
+    const double d2r = PI / 180.0;
+    const double f = strike * d2r, d = dip * d2r, l = rake * d2r;
+    const double sd = std::sin(d), cd = std::cos(d), s2d = std::sin(2 * d), c2d = std::cos(2 * d);
+    const double sl = std::sin(l), cl = std::cos(l), sf = std::sin(f), cf = std::cos(f);
+    const double s2f = std::sin(2 * f), c2f = std::cos(2 * f);
+    m[0] = -m0 * (sd * cl * s2f + s2d * sl * sf * sf);          // Mxx
+    m[1] = m0 * (sd * cl * s2f - s2d * sl * cf * cf);           // Myy
+    m[2] = m0 * s2d * sl;                                       // Mzz
+    m[3] = m0 * (sd * cl * c2f + 0.5 * s2d * sl * s2f);         // Mxy
+    m[4] = -m0 * (cd * cl * cf + c2d * sl * sf);                // Mxz
+    m[5] = -m0 * (cd * cl * sf - c2d * sl * cf);                // Myz
+}
+
+// weights of the displacement columns (0-9) of the moment-tensor output for
+// component Z, R, T at azimuth phi (degrees clockwise from north)
+static void mt_weights(const double *m, double phi_deg, double w[3][grt::kTensorNC])
+{
+    for (int i = 0; i < 3; i++)
+        for (int c = 0; c < grt::kTensorNC; c++) w[i][c] = 0.0;
+    const double ph = phi_deg * PI / 180.0;
+    const double w2c = 0.5 * (m[0] - m[1]), w2s = m[3], w1c = m[4], w1s = m[5], w0 = m[2], w0h = 0.5 * (m[0] + m[1]);
+    const double c2 = w2c * std::cos(2 * ph) + w2s * std::sin(2 * ph), s2 = -w2c * std::sin(2 * ph) + w2s * std::cos(2 * ph);
+    const double c1 = w1c * std::cos(ph) + w1s * std::sin(ph), s1 = -w1c * std::sin(ph) + w1s * std::cos(ph);
+    // Z: m = 2, 1, 0 families and the horizontal-isotropic part of the m = 2 family
+    w[0][6] = c2; w[0][7] = c1; w[0][8] = w0; w[0][9] = w0h;
+    // R
+    w[1][0] = c2; w[1][1] = c1; w[1][3] = w0; w[1][2] = w0h;
+    // T
+    w[2][4] = s2; w[2][5] = s1;
+}
+
+template <typename R>
+static int synth(grt_plan *p, const grt_source *src, const double *azimuth, double *seis)
+{
+    grt_ctx *ctx = p->ctx;
+    const Job &J = p->J;
+    const int nd = p->nd, nc = p->nc, N = J.N, nw = J.nw;
+    std::vector<R> W((size_t)nd * 3 * nc, R(0));
+    for (int r = 0; r < nd; r++) {
+        double w[3][grt::kTensorNC];
+        mt_weights(src->m, azimuth[r], w);
+        for (int i = 0; i < 3; i++)
+            for (int c = 0; c < nc; c++) W[((size_t)r * 3 + i) * nc + c] = (R)w[i][c];
+    }
+    // source-time spectrum at the complex frequency: dt sum_n s_n e^{-sigma n dt} e^{-i w n dt}
+    std::vector<R> stf;
+    if (src->n_stf > 0) {
+        stf.resize(2 * (size_t)nw);
+        for (int k = 0; k < nw; k++) {
+            cd acc(0, 0);
+            const double wk = 2 * PI * J.df * k;
+            for (int n = 0; n < src->n_stf; n++) {
+                const double t = n * J.dt;
+                acc += src->stf[n] * std::exp(-J.sigma * t) * std::exp(cd(0, -wk * t));
+            }
+            acc *= J.dt;
+            stf[2 * k] = (R)acc.real();
+            stf[2 * k + 1] = (R)acc.imag();
+        }
+    }
+    struct Bufs {
+        std::vector<void *> v;
+        ~Bufs() { for (void *q : v) cudaFree(q); }
+    } bufs;
+    void *dW = nullptr, *dS = nullptr, *dO = nullptr;
+    CU(cudaMalloc(&dW, W.size() * sizeof(R))); bufs.v.push_back(dW);
+    if (!stf.empty()) { CU(cudaMalloc(&dS, stf.size() * sizeof(R))); bufs.v.push_back(dS); }
+    const size_t nout = (size_t)nd * 3 * N;
+    CU(cudaMalloc(&dO, nout * sizeof(R))); bufs.v.push_back(dO);
+    cudaStream_t st = ctx->stream;
+    CU(cudaMemcpyAsync(dW, W.data(), W.size() * sizeof(R), cudaMemcpyHostToDevice, st));
+    if (dS) CU(cudaMemcpyAsync(dS, stf.data(), stf.size() * sizeof(R), cudaMemcpyHostToDevice, st));
+    grt::SynthArgs<R> A{};
+    A.S = (const R *)p->S; A.W = (const R *)dW; A.stf = (const R *)dS; A.post = (const R *)p->post;
+    A.tw = (const R *)p->tw; A.damp = p->damp; A.out = (R *)dO;
+    A.nw = nw; A.logn = J.log2n; A.nc = nc; A.nout = 3;
+    const size_t smem = (size_t)N * sizeof(grt::C<R>);
+    CU(raise_smem_limit(grt::synth_kernel<R>, (int)smem));
+    const int threads = std::min(512, std::max(32, N / 2));
+    grt::synth_kernel<R><<<nd * 3, threads, smem, st>>>(A);
+    CU(cudaGetLastError());
+    std::vector<R> h(nout);
+    CU(cudaMemcpyAsync(h.data(), dO, nout * sizeof(R), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    for (size_t i = 0; i < nout; i++) seis[i] = (double)h[i];
+    return GRT_OK;
+}
+
+extern "C" int grt_plan_synth(grt_plan *p, const grt_source *src, const double *azimuth, double *seis)
+{
+    if (!p || !src || !azimuth || !seis) return GRT_ERR_ARG;
+    grt_ctx *ctx = p->ctx;
+    if (p->J.src == 0) return set_err(ctx, GRT_ERR_UNSUPPORTED, "seismograms need a moment-tensor job");
+    if (src->n_stf < 0 || (src->n_stf > 0 && !src->stf) || src->n_stf > p->J.N)
+        return set_err(ctx, GRT_ERR_ARG, "source-time function: 0 <= n_stf <= N samples");
+    CU(cudaSetDevice(ctx->device));
+    return p->prec ? synth<double>(p, src, azimuth, seis) : synth<float>(p, src, azimuth, seis);
+}
+
+extern "C" int grt_batch_synth(grt_batch *b, int job, const grt_source *src, const double *azimuth, double *seis)
+{
+    if (!b || job < 0 || job >= (int)b->jobs.size()) return GRT_ERR_ARG;
+    return grt_plan_synth(b->jobs[job], src, azimuth, seis);
+}
+
+extern "C" int grt_flatten(int n_layer, const double *ztop, const double *vp, const double *vs, double hs, double hr,
+                           double r_earth, double *ztop_f, double *vp_f, double *vs_f, double *hs_f, double *hr_f)
+{
+    std::string err;
+    const int rc = grt::flatten(n_layer, ztop, vp, vs, hs, hr, r_earth, ztop_f, vp_f, vs_f, hs_f, hr_f, err);
+    if (rc) fprintf(stderr, "grt_flatten: %s\n", err.c_str());
+    return rc;
+}

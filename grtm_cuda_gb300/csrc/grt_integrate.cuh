@@ -386,6 +386,74 @@ struct SpecArgs {
     int nw, logn;
 };
 
+// in-place radix-2 decimation-in-time inverse DFT (exp(+2 pi i) kernel) of the
+// bit-reversed spectrum in x, then Re(x) e^{sigma t} / N into out
+template <typename R>
+__device__ __forceinline__ void ifft_dedamp(C<R> *x, const C<R> *tw, const double *damp, int logn, R *out)
+{
+    const int N = 1 << logn;
+    for (int s = 1; s <= logn; s++) {
+        const int half = 1 << (s - 1);
+        const int tstride = N >> s;
+        for (int b = threadIdx.x; b < N / 2; b += blockDim.x) {
+            const int grp = b >> (s - 1), pos = b & (half - 1);
+            const int i0 = grp * (half << 1) + pos, i1 = i0 + half;
+            const C<R> w = tw[pos * tstride];
+            const C<R> u = x[i0], v = x[i1] * w;
+            x[i0] = u + v;
+            x[i1] = u - v;
+        }
+        __syncthreads();
+    }
+    if (out)
+        for (int n = threadIdx.x; n < N; n += blockDim.x) out[n] = (R)((double)x[n].x * damp[n]);
+}
+
+// Seismograms: per (receiver, component) block, the Green's-function columns'
+// spectra combined with real weights W[trace][col] (azimuth and moment
+// tensor), times the source-time spectrum stf[w] (null: impulse), then the
+// same phase/taper/scale, Hermitian fill, inverse DFT and de-damping as the
+// spectral stage.
+template <typename R>
+struct SynthArgs {
+    const R *S;            // [nr][nc][nw] complex wavenumber sums
+    const R *W;            // [nr * nout][nc] combination weights
+    const R *stf;          // [nw] complex source-time spectrum, or null
+    const R *post, *tw;
+    const double *damp;
+    R *out;                // [nr * nout][N]
+    int nw, logn, nc, nout;
+};
+
+template <typename R>
+__global__ void __launch_bounds__(512) synth_kernel(SynthArgs<R> A)
+{
+    extern __shared__ __align__(16) unsigned char smem_syn[];
+    C<R> *x = reinterpret_cast<C<R> *>(smem_syn);
+    const int N = 1 << A.logn, nw = A.nw;
+    const long long tr = blockIdx.x;
+    const long long r = tr / A.nout;
+    const C<R> *S = reinterpret_cast<const C<R> *>(A.S) + r * A.nc * nw;
+    const R *W = A.W + tr * A.nc;
+    const C<R> *post = reinterpret_cast<const C<R> *>(A.post);
+    const C<R> *stf = reinterpret_cast<const C<R> *>(A.stf);
+    for (int n = threadIdx.x; n <= nw; n += blockDim.x) {
+        C<R> y = {R(0), R(0)};
+        if (n < nw) {
+            for (int c = 0; c < A.nc; c++) {
+                const R wc = W[c];
+                if (wc != R(0)) y = y + S[(long long)c * nw + n] * wc;
+            }
+            y = y * post[n];
+            if (stf) y = y * stf[n];
+        }
+        x[__brev((unsigned)n) >> (32 - A.logn)] = y;                       // n = nw: 0 (Nyquist)
+        if (n > 0 && n < nw) x[__brev((unsigned)(N - n)) >> (32 - A.logn)] = conj(y);
+    }
+    __syncthreads();
+    ifft_dedamp(x, reinterpret_cast<const C<R> *>(A.tw), A.damp, A.logn, A.out + tr * N);
+}
+
 template <typename R>
 __global__ void __launch_bounds__(512) spectral_kernel(SpecArgs<R> A)
 {

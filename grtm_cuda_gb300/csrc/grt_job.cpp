@@ -196,4 +196,35 @@ int job_setup(Job &J, double dt, int log2n, double t0, double taper, double sigm
     return kOk;
 }
 
+int flatten(int n, const double *ztop, const double *vp, const double *vs, double hs, double hr, double r_earth,
+            double *ztop_f, double *vp_f, double *vs_f, double *hs_f, double *hr_f, std::string &err)
+{
+    if (n < 1 || !ztop || !vp || !vs || !ztop_f || !vp_f || !vs_f || !(r_earth > 0)) {
+        err = "bad flattening arguments";
+        return kErrArg;
+    }
+    // greent.py:13-47: a layer of thickness h whose bottom lies at radius r is
+    // stretched by s = R / (r + h/2), and so are its velocities; the tops of the
+    // flat model are the running sum of the stretched thicknesses; the half-space
+    // takes the factor at its top
+    double r = r_earth, top = 0.0;
+    for (int i = 0; i < n; i++) {
+        const double h = i + 1 < n ? ztop[i + 1] - ztop[i] : 0.0;
+        if (!(h >= 0)) { err = "layer tops must increase"; return kErrModel; }
+        r -= h;
+        if (!(r > 0)) { err = "model deeper than the Earth radius"; return kErrModel; }
+        const double sc = r_earth / (r + 0.5 * h);
+        ztop_f[i] = top;
+        vp_f[i] = vp[i] * sc;
+        vs_f[i] = vs[i] * sc;
+        top += h * sc;
+    }
+    // greent.py:65-67: depths by z_f = R ln(R / (R - z))
+    auto fz = [&](double z) { return r_earth * std::log(r_earth / (r_earth - z)); };
+    if (!(hs < r_earth) || !(hr < r_earth)) { err = "depth beyond the Earth radius"; return kErrModel; }
+    if (hs_f) *hs_f = fz(hs);
+    if (hr_f) *hr_f = fz(hr);
+    return kOk;
+}
+
 }  // namespace grt

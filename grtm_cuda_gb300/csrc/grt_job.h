@@ -53,4 +53,9 @@ int job_setup(Job &J, double dt, int log2n, double t0, double taper, double sigm
               int nk_fixed, double dk_override, int fix, std::string &err, const int *nk_custom = nullptr,
               const int *k_stride = nullptr);
 
+// Earth-flattening transform of a spherical layered model (the reference's
+// caller-side step, greent.py:13-47 and 65-67); density and Q unchanged.
+int flatten(int n, const double *ztop, const double *vp, const double *vs, double hs, double hr, double r_earth,
+            double *ztop_f, double *vp_f, double *vs_f, double *hs_f, double *hr_f, std::string &err);
+
 }  // namespace grt

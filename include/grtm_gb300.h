@@ -197,6 +197,43 @@ GRT_API int grt_batch_fetch_freqs(grt_batch *batch, int job, int n_freq, const i
 GRT_API int grt_batch_info(const grt_batch *batch, int job, grt_report *report, grt_tune *tune);
 GRT_API void grt_batch_destroy(grt_batch *batch);
 
+/* Earth-flattening transform of a spherical model (the reference's caller-side
+ * preprocessing, greent.py:13-47 and 65-67, moved into the library): a layer
+ * of thickness h whose bottom lies at radius r is stretched by R / (r + h/2),
+ * and so are its Vp and Vs; the flat tops are the running sum of the
+ * stretched thicknesses; source and receiver depths map by R ln(R / (R - z)).
+ * Density and Q are unchanged.  Host only (no device). */
+GRT_API int grt_flatten(int n_layer, const double *ztop, const double *vp, const double *vs, double hs, double hr,
+                        double r_earth, double *ztop_f, double *vp_f, double *vs_f, double *hs_f, double *hr_f);
+
+/* Seismograms from a moment-tensor job: after grt_plan_execute (or
+ * grt_batch_execute), the receivers' Green's-function columns are combined
+ * for a source mechanism and azimuth, convolved with a source-time function,
+ * and brought to the time domain in one fused kernel (combination, source
+ * spectrum, phase/taper/scale, Hermitian fill, inverse DFT, e^{sigma t}).
+ * Combination, in the azimuthal families of the displacement columns 0-9
+ * (m = 2: columns 0, 4, 6; m = 1: 1, 5, 7; m = 0: 3, 8; the isotropic
+ * horizontal part of the m = 2 family: 2, 9), phi = azimuth:
+ *   Z = c2 G6 + c1 G7 + Mzz G8 + h G9,  R = c2 G0 + c1 G1 + Mzz G3 + h G2,
+ *   T = s2 G4 + s1 G5,
+ *   c2 = (Mxx-Myy)/2 cos 2phi + Mxy sin 2phi, s2 = -(Mxx-Myy)/2 sin 2phi + Mxy cos 2phi,
+ *   c1 = Mxz cos phi + Myz sin phi,            s1 = -Mxz sin phi + Myz cos phi,
+ *   h = (Mxx+Myy)/2.
+ * The source-time function s_n (at opts.dt) enters as dt sum_n s_n e^{-i (w - i sigma) n dt},
+ * so the seismogram is dt sum_m s_m G(t - m dt) (circularly, with the damped
+ * wrap-around of the method).  No counterpart in the reference, which stops
+ * at the columns. */
+typedef struct grt_source {
+    double m[6];          /* Mxx, Myy, Mzz, Mxy, Mxz, Myz; x north, y east, z down */
+    int n_stf;            /* source-time samples (0: impulse) */
+    const double *stf;
+} grt_source;
+/* double couple: strike, dip, rake in degrees, scalar moment m0 -> m[6] (Aki & Richards, Box 4.4) */
+GRT_API void grt_dc_moment(double strike, double dip, double rake, double m0, double *m);
+/* azimuth: degrees clockwise from north, one per receiver; seis: [n_dist][3 (Z, R, T)][N] */
+GRT_API int grt_plan_synth(grt_plan *plan, const grt_source *src, const double *azimuth, double *seis);
+GRT_API int grt_batch_synth(grt_batch *batch, int job, const grt_source *src, const double *azimuth, double *seis);
+
 /* create + execute + fetch + destroy */
 GRT_API int grt_run(grt_ctx *ctx, const grt_model *model, const grt_opts *opts, int n_dist,
             const double *dist, double *traces, double *spectra, grt_report *report);
