@@ -18,7 +18,7 @@ LIB_PATH = os.environ.get("GRTM_GB300_LIB", os.path.join(HERE, "_lib", "libgrtm_
 OK, ERR_ARG, ERR_IO, ERR_PARSE, ERR_MODEL, ERR_CUDA, ERR_NOMEM, ERR_TIMEOUT, ERR_UNSUPPORTED = range(9)
 K_REFERENCE, K_FIXED, K_CUSTOM = 0, 1, 2
 FP32, FP64 = 0, 1
-FIX_RLAYER, FIX_REXUT, FIX_DZ = 1, 2, 4
+FIX_RLAYER, FIX_REXUT, FIX_DZ, FIX_COLS = 1, 2, 4, 8
 FIX_ALL = FIX_RLAYER | FIX_REXUT | FIX_DZ
 
 _dp = ctypes.POINTER(ctypes.c_double)

@@ -34,6 +34,7 @@ struct grt_plan {
     int rt = 128, jt = 1;
     int use_tc = 0, nsplit = 1, kslice = 0;   // tensor-core wavenumber sum and its split-K
     int bt_rows = 0;                          // > 0: Bessel table tiled by 16 receivers (unit strides)
+    int cols = 0;                             // output column layout (grt::ColKind)
     void *P = nullptr;                        // split-K partial sums
     float *Kt = nullptr;                      // coefficients in GEMM operand layout
     long long *kt_base = nullptr;             // per frequency tile offset into Kt (floats)
@@ -131,6 +132,21 @@ static cudaError_t raise_smem_limit(F *kernel, int bytes)
     cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e == cudaSuccess) cur = bytes;
     return e;
+}
+
+// output column layout, count and coefficient columns of a job
+static int col_kind(const Job &J)
+{
+    const bool fix = (J.fix & grt::kFixCols) != 0;
+    return J.src == 0 ? (fix ? grt::kColSingleFix : grt::kColSingle) : (fix ? grt::kColTensorFix : grt::kColTensor);
+}
+static int col_count(int kind)
+{
+    return kind == grt::kColTensorFix ? grt::kTensorFixNC : (kind == grt::kColTensor ? grt::kTensorNC : grt::kSingleNC);
+}
+static int coef_count(int kind)
+{
+    return kind == grt::kColTensorFix ? 2 * grt::QT_N : (kind == grt::kColTensor ? grt::QT_N : grt::QS_N);
 }
 
 // ------------------------------------------------------------------ host tables
@@ -286,8 +302,9 @@ extern "C" int grt_plan_create(grt_ctx *ctx, const grt_model *m, const grt_opts 
     p->prec = o->precision;
     p->nd = n_dist;
     p->dist.assign(dist, dist + n_dist);
-    p->nc = J.src == 0 ? grt::kSingleNC : grt::kTensorNC;
-    p->nq = J.src == 0 ? grt::QS_N : grt::QT_N;
+    p->cols = col_kind(J);
+    p->nc = col_count(p->cols);
+    p->nq = coef_count(p->cols);
     const size_t esz = p->prec ? sizeof(grt::C<double>) : sizeof(grt::C<float>);
     if ((size_t)J.N * esz > 128 * 1024)
         return set_err(ctx, GRT_ERR_UNSUPPORTED, "N too large for the shared-memory FFT at this precision");
@@ -298,7 +315,9 @@ extern "C" int grt_plan_create(grt_ctx *ctx, const grt_model *m, const grt_opts 
     p->jt = 128 / p->rt;
     // FP32 plans sum over wavenumbers on the tensor cores unless GRT_KSUM=simt
     const char *ks = getenv("GRT_KSUM");
-    p->use_tc = (p->prec == GRT_FP32) && !(ks && !strcmp(ks, "simt"));
+    // the corrected 30-column tensor layout needs 16 coefficient columns: beyond the
+    // tensor-core sum's shared and tensor memory, it runs the SIMT sum
+    p->use_tc = (p->prec == GRT_FP32) && !(ks && !strcmp(ks, "simt")) && p->cols != grt::kColTensorFix;
     p->rep.ksum_impl = p->use_tc;
     // the tensor-core sum multiplies a tile of 64 frequencies by one Bessel operand:
     // the frequencies of a tile share their k stride
@@ -341,14 +360,18 @@ static int launch_ksum_tc(grt_plan *p, cudaStream_t st, int &launches)
     T.err = p->derr;
     const int nwt = (J.nw + grt::tc::kW - 1) / grt::tc::kW, nrt = (p->nd + grt::tc::kN - 1) / grt::tc::kN;
     const unsigned grid = (unsigned)(nwt * nrt * p->nsplit);
-    if (J.src == 0) {
-        const int sm = grt::tc::smem_bytes<grt::kSingle>();
-        CU(raise_smem_limit(grt::ksum_tc_kernel<grt::kSingle>, sm));
-        grt::ksum_tc_kernel<grt::kSingle><<<grid, grt::tc::kThreads, sm, st>>>(T);
+    if (p->cols == grt::kColSingle) {
+        const int sm = grt::tc::smem_bytes<grt::kColSingle>();
+        CU(raise_smem_limit(grt::ksum_tc_kernel<grt::kColSingle>, sm));
+        grt::ksum_tc_kernel<grt::kColSingle><<<grid, grt::tc::kThreads, sm, st>>>(T);
+    } else if (p->cols == grt::kColSingleFix) {
+        const int sm = grt::tc::smem_bytes<grt::kColSingleFix>();
+        CU(raise_smem_limit(grt::ksum_tc_kernel<grt::kColSingleFix>, sm));
+        grt::ksum_tc_kernel<grt::kColSingleFix><<<grid, grt::tc::kThreads, sm, st>>>(T);
     } else {
-        const int sm = grt::tc::smem_bytes<grt::kTensor>();
-        CU(raise_smem_limit(grt::ksum_tc_kernel<grt::kTensor>, sm));
-        grt::ksum_tc_kernel<grt::kTensor><<<grid, grt::tc::kThreads, sm, st>>>(T);
+        const int sm = grt::tc::smem_bytes<grt::kColTensor>();
+        CU(raise_smem_limit(grt::ksum_tc_kernel<grt::kColTensor>, sm));
+        grt::ksum_tc_kernel<grt::kColTensor><<<grid, grt::tc::kThreads, sm, st>>>(T);
     }
     launches++;
     CU(cudaGetLastError());
@@ -393,7 +416,8 @@ static int launch_bessel(grt_plan *p, cudaStream_t st, int &launches)
     const Job &J = p->J;
     const long long n = (long long)J.nbrow * p->nd;
     const int blocks = (int)((n + 255) / 256);
-    grt::bessel_table_kernel<R><<<blocks, 256, 0, st>>>((R *)p->B, J.nbrow, p->nd, J.dk, p->ddist, p->bt_rows);
+    grt::bessel_table_kernel<R><<<blocks, 256, 0, st>>>((R *)p->B, J.nbrow, p->nd, J.dk, p->ddist, p->bt_rows,
+                                                        (J.fix & grt::kFixCols) ? 1 : 0);
     launches++;
     CU(cudaGetLastError());
     return GRT_OK;
@@ -411,8 +435,12 @@ static int launch_ksum(grt_plan *p, cudaStream_t st, int &launches)
     S.K = (const R *)p->K; S.B = (const R *)p->B; S.nk = p->nk; S.ks = p->ks; S.koff = p->koff; S.dist = p->ddist;
     S.S = (R *)p->S; S.nkw = J.nkw; S.dk = J.dk; S.nw = J.nw; S.nr = p->nd; S.rt = p->rt; S.jt = p->jt;
     const int grid = J.nw * ((p->nd + p->rt - 1) / p->rt);
-    if (J.src == 0) grt::ksum_kernel<R, grt::kSingle><<<grid, grt::kSumThreads, 0, st>>>(S);
-    else grt::ksum_kernel<R, grt::kTensor><<<grid, grt::kSumThreads, 0, st>>>(S);
+    switch (p->cols) {
+    case grt::kColSingle: grt::ksum_kernel<R, grt::kColSingle><<<grid, grt::kSumThreads, 0, st>>>(S); break;
+    case grt::kColSingleFix: grt::ksum_kernel<R, grt::kColSingleFix><<<grid, grt::kSumThreads, 0, st>>>(S); break;
+    case grt::kColTensorFix: grt::ksum_kernel<R, grt::kColTensorFix><<<grid, grt::kSumThreads, 0, st>>>(S); break;
+    default: grt::ksum_kernel<R, grt::kColTensor><<<grid, grt::kSumThreads, 0, st>>>(S); break;
+    }
     launches++;
     CU(cudaGetLastError());
     return GRT_OK;
@@ -525,7 +553,7 @@ extern "C" int grt_grid(const grt_model *m, const grt_opts *o, grt_report *r)
     r->zr = J.zr;
     r->nw = J.nw;
     r->n_samples = J.N;
-    r->n_cols = J.src == 0 ? grt::kSingleNC : grt::kTensorNC;
+    r->n_cols = col_count(col_kind(J));
     r->n_wk = J.nkw;
     r->nk_max = J.nkmax;
     r->dk = J.dk;
@@ -1165,8 +1193,9 @@ static int batch_build(grt_batch *b, int autotune)
     for (grt_plan *p : b->jobs) {
         CU(raise_smem_limit(grt::spectral_kernel<R>, (int)((size_t)p->J.N * sizeof(grt::C<R>))));
         if (p->use_tc) {
-            CU(raise_smem_limit(grt::ksum_tc_kernel<grt::kSingle>, grt::tc::smem_bytes<grt::kSingle>()));
-            CU(raise_smem_limit(grt::ksum_tc_kernel<grt::kTensor>, grt::tc::smem_bytes<grt::kTensor>()));
+            CU(raise_smem_limit(grt::ksum_tc_kernel<grt::kColSingle>, grt::tc::smem_bytes<grt::kColSingle>()));
+            CU(raise_smem_limit(grt::ksum_tc_kernel<grt::kColSingleFix>, grt::tc::smem_bytes<grt::kColSingleFix>()));
+            CU(raise_smem_limit(grt::ksum_tc_kernel<grt::kColTensor>, grt::tc::smem_bytes<grt::kColTensor>()));
         }
     }
     CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -1294,10 +1323,10 @@ extern "C" void grt_dc_moment(double strike, double dip, double rake, double m0,
 
 // weights of the displacement columns (0-9) of the moment-tensor output for
 // component Z, R, T at azimuth phi (degrees clockwise from north)
-static void mt_weights(const double *m, double phi_deg, double w[3][grt::kTensorNC])
+static void mt_weights(const double *m, double phi_deg, double w[3][grt::kTensorFixNC])
 {
     for (int i = 0; i < 3; i++)
-        for (int c = 0; c < grt::kTensorNC; c++) w[i][c] = 0.0;
+        for (int c = 0; c < grt::kTensorFixNC; c++) w[i][c] = 0.0;
     const double ph = phi_deg * PI / 180.0;
     const double w2c = 0.5 * (m[0] - m[1]), w2s = m[3], w1c = m[4], w1s = m[5], w0 = m[2], w0h = 0.5 * (m[0] + m[1]);
     const double c2 = w2c * std::cos(2 * ph) + w2s * std::sin(2 * ph), s2 = -w2c * std::sin(2 * ph) + w2s * std::cos(2 * ph);
@@ -1318,7 +1347,7 @@ static int synth(grt_plan *p, const grt_source *src, const double *azimuth, doub
     const int nd = p->nd, nc = p->nc, N = J.N, nw = J.nw;
     std::vector<R> W((size_t)nd * 3 * nc, R(0));
     for (int r = 0; r < nd; r++) {
-        double w[3][grt::kTensorNC];
+        double w[3][grt::kTensorFixNC];
         mt_weights(src->m, azimuth[r], w);
         for (int i = 0; i < 3; i++)
             for (int c = 0; c < nc; c++) W[((size_t)r * 3 + i) * nc + c] = (R)w[i][c];

@@ -93,6 +93,18 @@ __device__ __forceinline__ double dbj_ref(double x, int n)
 }
 
 // the reference's second derivative expression (green.cu:1543-1554)
+// J_n''(x) from Bessel's equation: -J_{n-1}/x + ((n^2 + n)/x^2 - 1) J_n
+// (series near 0), the corrected-columns form
+__device__ __forceinline__ double ddbj_exact(double x, int n)
+{
+    if (fabs(x) < 1e-3) {
+        const double x2 = x * x;
+        return n == 0 ? -0.5 + 3.0 * x2 / 16.0 : n == 1 ? -0.375 * x : 0.25 - x2 / 8.0;
+    }
+    const double jm = n == 0 ? -bjn_ref(x, 1) : bjn_ref(x, n - 1);
+    return -jm / x + ((double)(n * n + n) / (x * x) - 1.0) * bjn_ref(x, n);
+}
+
 __device__ __forceinline__ double ddbj_ref(double x, int n)
 {
     if (fabs(x) < 1e-10) return (dbj_ref(1e-10, n) - dbj_ref(0.0, n)) / 1e-10;
@@ -103,7 +115,7 @@ __device__ __forceinline__ double ddbj_ref(double x, int n)
 // A&S 9.4.3 / 9.4.6, where x = k r reaches 10^4): x is reduced modulo 2 pi in
 // FP64 (two-constant Cody-Waite split), the phase polynomial and amplitude
 // are FP32.  J2, J3 by the reference's upward recurrence (used for x > n).
-__device__ __forceinline__ void bessel_big_x(double x, float v[NBASIS])
+__device__ __forceinline__ void bessel_big_x(double x, float v[NBASIS], bool exact)
 {
     const double TWO_PI_HI = 6.28318530717958623200e+00;   // 2 pi rounded to double
     const double TWO_PI_LO = 2.44929359829470635445e-16;   // 2 pi - TWO_PI_HI
@@ -127,9 +139,15 @@ __device__ __forceinline__ void bessel_big_x(double x, float v[NBASIS])
     v[BJ0D] = -j1;                                   // 0 J0 / x - J1
     v[BJ1D] = ix * j1 - j2;
     v[BJ2D] = 2.0f * ix * j2 - j3;
-    v[BJ0DD] = -j0;                                  // reference second-derivative expression
-    v[BJ1DD] = ix * j0 - j1 * (2.0f + xf * xf) * ix * ix;
-    v[BJ2DD] = 2.0f * ix * j1 - j2 * (6.0f + xf * xf) * ix * ix;
+    if (exact) {                                     // Bessel's equation
+        v[BJ0DD] = j1 * ix - j0;
+        v[BJ1DD] = -j0 * ix + (2.0f * ix * ix - 1.0f) * j1;
+        v[BJ2DD] = -j1 * ix + (6.0f * ix * ix - 1.0f) * j2;
+    } else {                                         // reference second-derivative expression
+        v[BJ0DD] = -j0;
+        v[BJ1DD] = ix * j0 - j1 * (2.0f + xf * xf) * ix * ix;
+        v[BJ2DD] = 2.0f * ix * j1 - j2 * (6.0f + xf * xf) * ix * ix;
+    }
 }
 
 // tile_rows = 0: layout B[j][b][r]; tile_rows > 0: receiver tiles of 16,
@@ -142,7 +160,7 @@ __device__ __forceinline__ long long btab_index(int j, int b, int r, int nr, int
 }
 
 template <typename R>
-__global__ void bessel_table_kernel(R *B, int nk, int nr, double dk, const double *dist, int tile_rows)
+__global__ void bessel_table_kernel(R *B, int nk, int nr, double dk, const double *dist, int tile_rows, int exact_dd)
 {
     long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= (long long)nk * nr) return;
@@ -151,7 +169,7 @@ __global__ void bessel_table_kernel(R *B, int nk, int nr, double dk, const doubl
     double x = dist[r] * (dk * j);
     if (sizeof(R) == 4 && x > 3.0) {
         float vf[NBASIS];
-        bessel_big_x(x, vf);
+        bessel_big_x(x, vf, exact_dd != 0);
 #pragma unroll
         for (int b = 0; b < NBASIS; b++) B[btab_index(j, b, r, nr, tile_rows)] = (R)vf[b];
         return;
@@ -163,9 +181,9 @@ __global__ void bessel_table_kernel(R *B, int nk, int nr, double dk, const doubl
     v[BJ0D] = dbj_ref(x, 0);
     v[BJ1D] = dbj_ref(x, 1);
     v[BJ2D] = dbj_ref(x, 2);
-    v[BJ0DD] = ddbj_ref(x, 0);
-    v[BJ1DD] = ddbj_ref(x, 1);
-    v[BJ2DD] = ddbj_ref(x, 2);
+    v[BJ0DD] = exact_dd ? ddbj_exact(x, 0) : ddbj_ref(x, 0);
+    v[BJ1DD] = exact_dd ? ddbj_exact(x, 1) : ddbj_ref(x, 1);
+    v[BJ2DD] = exact_dd ? ddbj_exact(x, 2) : ddbj_ref(x, 2);
 #pragma unroll
     for (int b = 0; b < NBASIS; b++) B[btab_index(j, b, r, nr, tile_rows)] = (R)v[b];
 }
@@ -240,6 +258,81 @@ constexpr __device__ Term kTensorTerms[] = {
 constexpr __device__ int kTensorCol[21] = {0, 2, 4, 5, 6, 8, 10, 11, 12, 13, 14, 17, 20, 21, 22, 25, 28, 29, 30, 31, 32};
 constexpr int kTensorNC = 20;
 
+// corrected single force: the d/dr column 10 term b1 k J1'(kr) carries 1/r
+constexpr __device__ Term kSingleFixTerms[] = {
+    {0, 1, 1.0}, {1, 0, 1.0},
+    {2, 0, 1.0},
+    {3, 1, 1.0}, {4, 0, 1.0},
+    {5, 0, 1.0},
+    {6, 0, 1.0},
+    {7, 1, 1.0}, {8, 0, 1.0},
+    {9, 0, 1.0},
+    {10, 1, 1.0}, {11, 0, 1.0},
+    {12, 0, 1.0},
+    {13, 0, 1.0},
+    {0, 2, -1.0}, {4, 1, 1.0}, {14, 0, 1.0},
+    {15, 0, 1.0},
+    {3, 2, -1.0}, {1, 1, 1.0}, {16, 0, 1.0},
+    {17, 0, 1.0},
+    {18, 0, 1.0},
+};
+
+// corrected moment tensor: 30 columns -- displacement 0-9 (column 5, the m = 1
+// transverse term, with b1 where green.cu:1657 has b2), d/dz 10-19 from the
+// z-derivative coefficients (the block green.cu:1666-1677 writes and then
+// overwrites), d/dr 20-29 (green.cu:1680-1691, column 25 with b1)
+constexpr int QTT = QT_N;   // offset of the z-derivative coefficient columns
+constexpr __device__ Pair kTensorFixPairs[] = {
+    {QT_B2, 0, BJ2},   {QT_A20, 1, BJ2D},  {QT_B1, 0, BJ1},    {QT_A10, 1, BJ1D},  {QT_A21, 1, BJ0D},
+    {QT_A01, 1, BJ0D}, {QT_B2, 1, BJ2D},   {QT_A20, 0, BJ2},   {QT_B2, 1, BJ1D},   {QT_A10, 0, BJ1},
+    {QT_A21, 1, BJ2},  {QT_A11, 1, BJ1},   {QT_A01, 1, BJ0},   {QT_A21, 1, BJ0},   {QT_A20, 2, BJ2DD},
+    {QT_B1, 1, BJ1D},  {QT_A10, 2, BJ1DD}, {QT_A21, 2, BJ0DD}, {QT_A01, 2, BJ0DD}, {QT_B2, 2, BJ2DD},
+    {QT_B2, 2, BJ1DD}, {QT_A21, 2, BJ2D},  {QT_A11, 2, BJ1D},  {QT_A01, 2, BJ0D},  {QT_A21, 2, BJ0D},
+    // 25..38: z-derivative coefficients
+    {QTT + QT_B2, 0, BJ2},   {QTT + QT_A20, 1, BJ2D}, {QTT + QT_B1, 0, BJ1},  {QTT + QT_A10, 1, BJ1D},
+    {QTT + QT_A21, 1, BJ0D}, {QTT + QT_A01, 1, BJ0D}, {QTT + QT_B2, 1, BJ2D}, {QTT + QT_A20, 0, BJ2},
+    {QTT + QT_B1, 1, BJ1D},  {QTT + QT_A10, 0, BJ1},  {QTT + QT_A21, 1, BJ2}, {QTT + QT_A11, 1, BJ1},
+    {QTT + QT_A01, 1, BJ0},  {QTT + QT_A21, 1, BJ0},
+    // 39: b1 k^2 J1''
+    {QT_B1, 2, BJ1DD},
+};
+constexpr int kTensorFixNP = sizeof(kTensorFixPairs) / sizeof(Pair);
+constexpr __device__ Term kTensorFixTerms[] = {
+    {0, 1, 2.0}, {1, 0, 1.0},                    // 0
+    {2, 1, 1.0}, {3, 0, 1.0},                    // 1
+    {4, 0, 1.0},                                 // 2
+    {5, 0, 1.0},                                 // 3
+    {6, 0, 1.0}, {7, 1, 2.0},                    // 4
+    {15, 0, 1.0}, {9, 1, 1.0},                   // 5
+    {10, 0, 1.0},                                // 6
+    {11, 0, 1.0},                                // 7
+    {12, 0, 1.0},                                // 8
+    {13, 0, 1.0},                                // 9
+    {25, 1, 2.0}, {26, 0, 1.0},                  // 10: d/dz
+    {27, 1, 1.0}, {28, 0, 1.0},                  // 11
+    {29, 0, 1.0},                                // 12
+    {30, 0, 1.0},                                // 13
+    {31, 0, 1.0}, {32, 1, 2.0},                  // 14
+    {33, 0, 1.0}, {34, 1, 1.0},                  // 15
+    {35, 0, 1.0},                                // 16
+    {36, 0, 1.0},                                // 17
+    {37, 0, 1.0},                                // 18
+    {38, 0, 1.0},                                // 19
+    {0, 2, -2.0}, {6, 1, 2.0}, {14, 0, 1.0},     // 20: d/dr
+    {2, 2, -1.0}, {15, 1, 1.0}, {16, 0, 1.0},    // 21
+    {17, 0, 1.0},                                // 22
+    {18, 0, 1.0},                                // 23
+    {19, 0, 1.0}, {7, 2, -2.0}, {1, 1, 2.0},     // 24
+    {39, 0, 1.0}, {9, 2, -1.0}, {3, 1, 1.0},     // 25
+    {21, 0, 1.0},                                // 26
+    {22, 0, 1.0},                                // 27
+    {23, 0, 1.0},                                // 28
+    {24, 0, 1.0},                                // 29
+};
+constexpr __device__ int kTensorFixCol[31] = {0,  2,  4,  5,  6,  8,  10, 11, 12, 13, 14, 16, 18, 19, 20, 22,
+                                              24, 25, 26, 27, 28, 31, 34, 35, 36, 39, 42, 43, 44, 45, 46};
+constexpr int kTensorFixNC = 30;
+
 template <int SRC> struct Cols;
 template <> struct Cols<kSingle> {
     static constexpr int NP = kSingleNP, NC = kSingleNC, NQ = QS_N;
@@ -252,6 +345,18 @@ template <> struct Cols<kTensor> {
     __device__ static constexpr Pair pair(int i) { return kTensorPairs[i]; }
     __device__ static constexpr Term term(int i) { return kTensorTerms[i]; }
     __device__ static constexpr int col(int i) { return kTensorCol[i]; }
+};
+template <> struct Cols<kColSingleFix> {
+    static constexpr int NP = kSingleNP, NC = kSingleNC, NQ = QS_N;
+    __device__ static constexpr Pair pair(int i) { return kSinglePairs[i]; }
+    __device__ static constexpr Term term(int i) { return kSingleFixTerms[i]; }
+    __device__ static constexpr int col(int i) { return kSingleCol[i]; }
+};
+template <> struct Cols<kColTensorFix> {
+    static constexpr int NP = kTensorFixNP, NC = kTensorFixNC, NQ = 2 * QT_N;
+    __device__ static constexpr Pair pair(int i) { return kTensorFixPairs[i]; }
+    __device__ static constexpr Term term(int i) { return kTensorFixTerms[i]; }
+    __device__ static constexpr int col(int i) { return kTensorFixCol[i]; }
 };
 
 // error-free sum s + x = hi + lo (Knuth TwoSum)

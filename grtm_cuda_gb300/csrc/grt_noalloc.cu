@@ -84,6 +84,7 @@ extern "C" GRT_API int grt_run_noalloc(int device, const grt_model *m, const grt
     unsigned char *scratch = (unsigned char *)g_scratch_addr[device];
 
     if (o->k_mode == GRT_K_CUSTOM || o->k_stride) return fail(GRT_ERR_UNSUPPORTED, "custom k grids need grt_run");
+    if (o->fix & GRT_FIX_COLS) return fail(GRT_ERR_UNSUPPORTED, "corrected column layouts need grt_run");
     // the job on the host (same rules as grt_run)
     Job J;
     std::string err;
@@ -186,7 +187,7 @@ extern "C" GRT_API int grt_run_noalloc(int device, const grt_model *m, const grt
     {
         long long n = (long long)J.nkmax * nd;
         grt::bessel_table_kernel<float><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
-            (float *)(scratch + o_B), J.nkmax, nd, J.dk, (const double *)(scratch + o_dist), 0);
+            (float *)(scratch + o_B), J.nkmax, nd, J.dk, (const double *)(scratch + o_dist), 0, 0);
         CUN(cudaGetLastError());
     }
     {

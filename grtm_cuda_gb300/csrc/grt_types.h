@@ -28,13 +28,17 @@ static_assert(sizeof(LayerW<double>) % 16 == 0, "TMA bulk copies need 16-byte mu
 
 // column sets of the per-(w,k) receiver coefficients written by the GRT kernel
 enum SrcKind { kSingle = 0, kTensor = 1 };
+// output column layouts: the reference's (bug-compatible) ones, and the
+// corrected ones selected by GRT_FIX_COLS (single force: the d/dr column 10
+// with its 1/r; moment tensor: 30 defined columns, d/dz in 10-19, d/dr in 20-29)
+enum ColKind { kColSingle = 0, kColTensor = 1, kColSingleFix = 2, kColTensorFix = 3 };
 // single force: b1, a0[0], a0[1], a1[0], a1[1] and their d/dz versions
 enum QSingle { QS_B1 = 0, QS_A00, QS_A01, QS_A10, QS_A11, QS_B1T, QS_A0T0, QS_A0T1, QS_A1T0, QS_A1T1, QS_N };
 // moment tensor: b1, b2, a0[0..1], a1[0..1], a2[0..1]
 enum QTensor { QT_B1 = 0, QT_B2, QT_A00, QT_A01, QT_A10, QT_A11, QT_A20, QT_A21, QT_N };
 
 // reference-quirk switches (0 = reproduce the reference)
-enum Fix { kFixRLayer = 1, kFixRexut = 2, kFixDz = 4 };
+enum Fix { kFixRLayer = 1, kFixRexut = 2, kFixDz = 4, kFixCols = 8 };
 
 template <typename R>
 struct GrtArgs {

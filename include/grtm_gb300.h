@@ -46,6 +46,11 @@ extern "C" {
 #define GRT_FIX_RLAYER 1       /* receiver layer located with the receiver depth */
 #define GRT_FIX_REXUT 2        /* d/dz terms use the local vertical wavenumber */
 #define GRT_FIX_DZ 4           /* d/dz terms without the doubled factor / reused product */
+#define GRT_FIX_COLS 8         /* corrected output columns: moment tensor 30 defined columns (0-9
+                                * displacement, 10-19 d/dz, 20-29 d/dr; the m = 1 transverse terms
+                                * with b1), single force d/dr column 10 with its 1/r, Bessel second
+                                * derivatives from Bessel's equation.  The 30-column layout runs the
+                                * SIMT wavenumber sum. */
 
 /* A layered model: n_layer layers given by the depth of their top (ztop[0] = 0),
  * the last one being the half-space.  Units: km, km/s, g/cm^3. */
@@ -80,7 +85,7 @@ typedef struct grt_report {
     double zs, zr;
     int nw;               /* positive frequencies */
     int n_samples;        /* N */
-    int n_cols;           /* defined output columns: 15 single force, 20 moment tensor */
+    int n_cols;           /* defined output columns: 15 single force, 20 moment tensor (30 with GRT_FIX_COLS) */
     long long n_wk;       /* (w,k) points evaluated */
     int nk_max;
     double dk, df, sigma;

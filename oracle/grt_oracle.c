@@ -196,6 +196,17 @@ double grto_dd_besselj(double x, int n)
     return (double)n * grto_besselj(x, n - 1) / x - grto_besselj(x, n) * (n + n * n + x * x) / x / x;
 }
 
+/* J_n''(x) from Bessel's equation, -J_{n-1}/x + ((n^2 + n)/x^2 - 1) J_n (series near 0) */
+double grto_dd_besselj_exact(double x, int n)
+{
+    if (fabs(x) < 1e-3) {
+        double x2 = x * x;
+        return n == 0 ? -0.5 + 3.0 * x2 / 16.0 : n == 1 ? -0.375 * x : 0.25 - x2 / 8.0;
+    }
+    double jm = n == 0 ? -grto_besselj(x, 1) : grto_besselj(x, n - 1);
+    return -jm / x + ((double)(n * n + n) / (x * x) - 1.0) * grto_besselj(x, n);
+}
+
 /* ------------------------------------------------------------------ */
 /* input parsing, green.cu:1989-2060                                    */
 /* ------------------------------------------------------------------ */
@@ -1102,12 +1113,15 @@ static void point_any(const grto_job *J, const cplx *alpha, const cplx *beta, do
 /* integrands at one distance: get_int_val_single green.cu:1558-1621,
  * get_int_val_tensor green.cu:1626-1716 (columns 10-19 overwritten there by
  * the d/dr terms; 20-29 are never written and are zero here) */
-static void integrand(int src_type, const ypar_t *p, double k, double dist, cplx out[30])
+static void integrand(int src_type, int fix, const ypar_t *p, double k, double dist, cplx out[30])
 {
     double x = dist * k;
+    int cf = (fix & GRTO_FIX_COLS) != 0;
     double j0 = grto_besselj(x, 0), j1 = grto_besselj(x, 1), j2 = grto_besselj(x, 2);
     double j0d = grto_d_besselj(x, 0), j1d = grto_d_besselj(x, 1), j2d = grto_d_besselj(x, 2);
-    double j0dd = grto_dd_besselj(x, 0), j1dd = grto_dd_besselj(x, 1), j2dd = grto_dd_besselj(x, 2);
+    double j0dd = cf ? grto_dd_besselj_exact(x, 0) : grto_dd_besselj(x, 0);
+    double j1dd = cf ? grto_dd_besselj_exact(x, 1) : grto_dd_besselj(x, 1);
+    double j2dd = cf ? grto_dd_besselj_exact(x, 2) : grto_dd_besselj(x, 2);
     for (int i = 0; i < 30; i++) out[i] = 0;
     if (src_type == 0) {
         out[0] = p->b1 * j1 / dist + p->a1[0] * k * j1d;
@@ -1120,32 +1134,47 @@ static void integrand(int src_type, const ypar_t *p, double k, double dist, cplx
         out[7] = p->a1t[0] * j1 / dist + p->b1t * k * j1d;
         out[8] = p->a1t[1] * k * j1;
         out[9] = p->a0t[1] * k * j0;
-        out[10] = -p->b1 * j1 / dist / dist + p->b1 * j1d * k + p->a1[0] * k * j1dd * k;
+        /* green.cu:1596 writes b1 j1d k without the 1/r of d/dr (b1 J1(kr)/r) */
+        out[10] = -p->b1 * j1 / dist / dist + p->b1 * j1d * k / (cf ? dist : 1.0) + p->a1[0] * k * j1dd * k;
         out[11] = p->a0[0] * k * j0dd * k;
         out[12] = -p->a1[0] * j1 / dist / dist + p->a1[0] * j1d * k / dist + p->b1 * k * j1dd * k;
         out[13] = p->a1[1] * k * j1d * k;
         out[14] = p->a0[1] * k * j0d * k;
     } else {
+        cplx b1u = cf ? p->b1 : p->b2, b1tu = cf ? p->b1t : p->b2t;   /* green.cu:1657, 1672, 1686 use b2 */
         out[0] = p->b2 * 2.0 * j2 / dist + p->a2[0] * k * j2d;
         out[1] = p->b1 * j1 / dist + p->a1[0] * k * j1d;
         out[2] = p->a2[1] * k * j0d;
         out[3] = p->a0[1] * k * j0d;
         out[4] = p->b2 * k * j2d + 2.0 * p->a2[0] * j2 / dist;
-        out[5] = p->b2 * k * j1d + p->a1[0] * j1 / dist;
+        out[5] = b1u * k * j1d + p->a1[0] * j1 / dist;
         out[6] = p->a2[1] * k * j2;
         out[7] = p->a1[1] * k * j1;
         out[8] = p->a0[1] * k * j0;
         out[9] = p->a2[1] * k * j0;
-        out[10] = -p->b2 * 2.0 * j2 / dist / dist + p->b2 * 2.0 * j2d * k / dist + p->a2[0] * k * j2dd * k;
-        out[11] = -p->b1 * j1 / dist / dist + p->b1 * j1d * k / dist + p->a1[0] * k * j1dd * k;
-        out[12] = p->a2[1] * k * j0dd * k;
-        out[13] = p->a0[1] * k * j0dd * k;
-        out[14] = p->b2 * k * j2dd * k - 2.0 * p->a2[0] * j2 / dist / dist + 2.0 * p->a2[0] * j2d * k / dist;
-        out[15] = p->b2 * k * j1dd * k - p->a1[0] * j1 / dist / dist + p->a1[0] * j1d * k / dist;
-        out[16] = p->a2[1] * k * j2d * k;
-        out[17] = p->a1[1] * k * j1d * k;
-        out[18] = p->a0[1] * k * j0d * k;
-        out[19] = p->a2[1] * k * j0d * k;
+        int o = cf ? 20 : 10;   /* d/dr block: 20-29 corrected, 10-19 (over d/dz) in the reference */
+        if (cf) {
+            out[10] = p->b2t * 2.0 * j2 / dist + p->a2t[0] * k * j2d;
+            out[11] = p->b1t * j1 / dist + p->a1t[0] * k * j1d;
+            out[12] = p->a2t[1] * k * j0d;
+            out[13] = p->a0t[1] * k * j0d;
+            out[14] = p->b2t * k * j2d + 2.0 * p->a2t[0] * j2 / dist;
+            out[15] = b1tu * k * j1d + p->a1t[0] * j1 / dist;
+            out[16] = p->a2t[1] * k * j2;
+            out[17] = p->a1t[1] * k * j1;
+            out[18] = p->a0t[1] * k * j0;
+            out[19] = p->a2t[1] * k * j0;
+        }
+        out[o + 0] = -p->b2 * 2.0 * j2 / dist / dist + p->b2 * 2.0 * j2d * k / dist + p->a2[0] * k * j2dd * k;
+        out[o + 1] = -p->b1 * j1 / dist / dist + p->b1 * j1d * k / dist + p->a1[0] * k * j1dd * k;
+        out[o + 2] = p->a2[1] * k * j0dd * k;
+        out[o + 3] = p->a0[1] * k * j0dd * k;
+        out[o + 4] = p->b2 * k * j2dd * k - 2.0 * p->a2[0] * j2 / dist / dist + 2.0 * p->a2[0] * j2d * k / dist;
+        out[o + 5] = b1u * k * j1dd * k - p->a1[0] * j1 / dist / dist + p->a1[0] * j1d * k / dist;
+        out[o + 6] = p->a2[1] * k * j2d * k;
+        out[o + 7] = p->a1[1] * k * j1d * k;
+        out[o + 8] = p->a0[1] * k * j0d * k;
+        out[o + 9] = p->a2[1] * k * j0d * k;
     }
 }
 
@@ -1182,7 +1211,7 @@ int grto_integrand(const grto_job *J, int iw, double k, double r, double *out)
     attenuate(J, w, a, b);
     slot0_nu(J, slot0);
     point_any(J, a, b, k, w, slot0, &Y);
-    integrand(J->src_type, &Y, k, r, v);
+    integrand(J->src_type, J->fix, &Y, k, r, v);
     for (int i = 0; i < 30; i++) { out[2 * i] = creal(v[i]); out[2 * i + 1] = cimag(v[i]); }
     return GRTO_OK;
 }
@@ -1234,7 +1263,7 @@ int grto_run(const grto_job *J, double *spec, double *sig, int nthreads)
             ypar_t Y;
             point_any(J, a, b, k, w, slot0, &Y);
             for (int d = 0; d < nd; d++) {
-                integrand(J->src_type, &Y, k, dist[d], v);
+                integrand(J->src_type, J->fix, &Y, k, dist[d], v);
                 cplx *o = out + ((size_t)d * N + iw) * ncol;
                 if (ik == 0) for (int c = 0; c < ncol; c++) o[c] = v[c] * J->dk / 2.0;
                 else for (int c = 0; c < ncol; c++) o[c] += v[c] * J->dk;
@@ -1319,7 +1348,7 @@ int grto_run_band(const grto_job *J, int iw0, int iw1, double *sums, int nthread
                 point_any(J, a, bb, k, w, slot0, &Y);
                 double wk = ik == 0 ? J->dk / 2.0 : J->dk;
                 for (int d = 0; d < nd; d++) {
-                    integrand(J->src_type, &Y, k, J->dist[d], v);
+                    integrand(J->src_type, J->fix, &Y, k, J->dist[d], v);
                     cplx *o = loc + ((size_t)(iw - iw0) * nd + d) * ncol;
                     for (int c = 0; c < ncol; c++) o[c] += v[c] * wk;
                 }

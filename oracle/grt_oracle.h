@@ -42,6 +42,14 @@ extern "C" {
  * basis (see grt_oracle.c).  Same results where the reference's 4x4 solve is
  * well conditioned; accurate also at w -> 0 where the reference loses digits. */
 #define GRTO_STABLE 8
+/* Corrected output columns (not the reference's layout): moment tensor with
+ * 30 defined columns -- displacement 0-9 (the m = 1 transverse term with b1
+ * where green.cu:1657 has b2), d/dz 10-19 from the z-derivative coefficients
+ * (the block green.cu:1666-1677 writes and then overwrites), d/dr 20-29
+ * (green.cu:1680-1691, column 25 with b1); single force: the d/dr column 10
+ * with the 1/r of its b1 k J1' term; second Bessel derivatives from Bessel's
+ * equation instead of dd_besselj (green.cu:1540-1554). */
+#define GRTO_FIX_COLS 16
 
 typedef struct grto_job {
     /* model after source-interface insertion (green.cu:1995-2049) */
@@ -115,6 +123,7 @@ int grto_green(const char *iname, const char *oname_w, const char *oname_t,
 double grto_besselj(double x, int n);
 double grto_d_besselj(double x, int n);
 double grto_dd_besselj(double x, int n);
+double grto_dd_besselj_exact(double x, int n);
 
 #ifdef __cplusplus
 }

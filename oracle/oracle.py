@@ -22,6 +22,7 @@ FIX_REXUT = 2
 FIX_DZ = 4
 FIX_ALL = FIX_RLAYER | FIX_REXUT | FIX_DZ
 STABLE = 8
+FIX_COLS = 16   # corrected output columns (not the reference layout)
 MAXL = 256
 
 
