@@ -126,7 +126,7 @@ EXPORTS = ("grt_create", "grt_destroy", "grt_last_error", "grt_status_string", "
            "grt_mlp_n_params", "grt_mlp_get_params", "grt_mlp_set_params", "grt_mlp_forward",
            "grt_mlp_loss_grad", "grt_mlp_train", "grt_batch_create", "grt_batch_execute", "grt_batch_fetch",
            "grt_batch_fetch_freqs", "grt_batch_info", "grt_batch_destroy", "grt_dc_moment", "grt_plan_synth",
-           "grt_batch_synth", "grt_flatten")
+           "grt_batch_synth", "grt_flatten", "grt_plan_write")
 
 _lib = None
 
@@ -187,6 +187,7 @@ def lib():
     L.grt_batch_info.argtypes = [vp, ctypes.c_int, P(Report), P(Tune)]
     L.grt_batch_destroy.argtypes = [vp]
     L.grt_batch_destroy.restype = None
+    L.grt_plan_write.argtypes = [vp, ctypes.c_char_p]
     L.grt_flatten.argtypes = [ctypes.c_int, _dp, _dp, _dp, ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp,
                               _dp, _dp, _dp, _dp]
     L.grt_dc_moment.argtypes = [ctypes.c_double] * 4 + [_dp]
@@ -292,6 +293,12 @@ class Plan:
         if spectra:
             s = s[..., 0] + 1j * s[..., 1]
         return t, s
+
+    def write(self, path):
+        """Traces to a binary file (grt_plan_write); read back with read_bin."""
+        rc = lib().grt_plan_write(self.h, str(path).encode())
+        if rc:
+            raise GrtError(rc, self.ctx.error())
 
     def synth(self, m6, azimuth, stf=None):
         """Seismograms [n_dist, 3 (Z, R, T), N] for moment tensor m6 at the
@@ -481,6 +488,25 @@ def green(iname, oname_w, oname_t):
     rc = lib().grt_green(str(iname).encode(), str(oname_w).encode(), str(oname_t).encode())
     if rc:
         raise GrtError(rc, f"green({iname})")
+
+
+def read_bin(path):
+    """A file written by grt_plan_write: dict with dt, t0, sigma, dist and
+    traces float32 [n_dist, n_cols, N]."""
+    with open(path, "rb") as f:
+        b = f.read()
+    if b[:8] != b"GRTMBIN1":
+        raise ValueError(f"{path}: not a GRTMBIN1 file")
+    ver, nd, nc, n = np.frombuffer(b, "<i4", 4, 8)
+    if ver != 1:
+        raise ValueError(f"{path}: version {ver}")
+    dt, t0, sigma = np.frombuffer(b, "<f8", 3, 24)
+    dist = np.frombuffer(b, "<f8", nd, 48).copy()
+    o = 48 + 8 * nd
+    tr = np.frombuffer(b, "<f4", nd * nc * n, o).reshape(nd, nc, n).copy()
+    if o + 4 * tr.size != len(b):
+        raise ValueError(f"{path}: size mismatch")
+    return {"dt": float(dt), "t0": float(t0), "sigma": float(sigma), "dist": dist, "traces": tr}
 
 
 def read_table(path, complex_pairs=False):

@@ -1421,3 +1421,34 @@ extern "C" int grt_flatten(int n_layer, const double *ztop, const double *vp, co
     if (rc) fprintf(stderr, "grt_flatten: %s\n", err.c_str());
     return rc;
 }
+
+// ------------------------------------------------------------------ binary output
+// "GRTMBIN1", int32 version (1), n_dist, n_cols, N, float64 dt, t0, sigma,
+// float64 dist[n_dist], then the traces as float32 [n_dist][n_cols][N]
+// (little-endian, as the host writes them).  FP64 plans store their traces
+// rounded to float32.
+extern "C" int grt_plan_write(grt_plan *p, const char *path)
+{
+    if (!p || !path) return GRT_ERR_ARG;
+    grt_ctx *ctx = p->ctx;
+    const Job &J = p->J;
+    const size_t n = (size_t)p->nd * p->nc * J.N;
+    std::vector<float> tr(n);
+    CU(cudaSetDevice(ctx->device));
+    if (p->prec) {
+        std::vector<double> h(n);
+        CU(cudaMemcpy(h.data(), p->sig, n * sizeof(double), cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < n; i++) tr[i] = (float)h[i];
+    } else {
+        CU(cudaMemcpy(tr.data(), p->sig, n * sizeof(float), cudaMemcpyDeviceToHost));
+    }
+    FILE *f = fopen(path, "wb");
+    if (!f) return set_err(ctx, GRT_ERR_IO, std::string("cannot write ") + path);
+    const int32_t hdr[4] = {1, p->nd, p->nc, J.N};
+    const double par[3] = {J.dt, J.t0, J.sigma};
+    bool ok = fwrite("GRTMBIN1", 1, 8, f) == 8 && fwrite(hdr, sizeof hdr, 1, f) == 1 && fwrite(par, sizeof par, 1, f) == 1 &&
+              fwrite(p->dist.data(), sizeof(double), p->nd, f) == (size_t)p->nd &&
+              fwrite(tr.data(), sizeof(float), n, f) == n;
+    ok = (fclose(f) == 0) && ok;
+    return ok ? GRT_OK : set_err(ctx, GRT_ERR_IO, std::string("short write to ") + path);
+}

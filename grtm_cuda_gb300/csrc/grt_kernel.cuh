@@ -323,13 +323,35 @@ __device__ __forceinline__ void grt_point(const GrtArgs<R> &A, const LayerW<R> *
     const R zr = (R)A.zr;
     const Zd<R> Zr = zd<R>(A.zr), Zhr = zd<R>(A.hr_layer), Zhr_r = zd<R>(A.hr_layer - A.zr);
 
-    for (int jf = L - 2; jf >= s; jf--) {
+    // Depth truncation: below the source (below the receiver when it lies
+    // deeper), a wave reflected from beneath the layer where the slower, S,
+    // vertical wavenumber has accumulated sum Re(v) h > lim comes back damped
+    // by e^{-2 lim} (2e-9 FP32, 4e-18 FP64), under the working precision; the
+    // recursion starts there with the layer beneath as the half-space.  At
+    // wavenumbers where S is evanescent this skips most of the deep stack.
+    int jlow = L - 2;
+    {
+        const R lim = sizeof(R) == 4 ? R(10) : R(20);
+        const int j0 = rl > s ? rl + 1 : s + 1;
+        R e = R(0);
+        for (int jl = j0; jl <= L - 3; jl++) {
+            const C<R> zv = {k * k - T[jl].wb2[0], -T[jl].wb2[1]};
+            e += csqrt_(zv).x * T[jl].h;
+            if (e > lim) {
+                jlow = jl;
+                break;
+            }
+        }
+    }
+    if (jlow < L - 2) make_layer(T[jlow + 1], k2, k, D);
+
+    for (int jf = jlow; jf >= s; jf--) {
         make_layer(T[jf], k2, k, U);
         IF<R> m;
         interface_rt(U, D, k, m);
         M2<R> Tdn;
         C<R> td0n;
-        if (jf == L - 2) {
+        if (jf == jlow) {
             Rdu = m.rd;
             rdu0 = m.rdu0;
             Tdn = m.td;

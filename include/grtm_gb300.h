@@ -202,6 +202,13 @@ GRT_API int grt_batch_fetch_freqs(grt_batch *batch, int job, int n_freq, const i
 GRT_API int grt_batch_info(const grt_batch *batch, int job, grt_report *report, grt_tune *tune);
 GRT_API void grt_batch_destroy(grt_batch *batch);
 
+/* Binary output of a plan's traces (beside the reference's %.18e text,
+ * green.cu:2242-2258, which dominates wall time at many receivers):
+ * "GRTMBIN1", int32 version (1), n_dist, n_cols, N, float64 dt, t0, sigma,
+ * float64 dist[n_dist], float32 traces [n_dist][n_cols][N], little-endian.
+ * No counterpart in the reference. */
+GRT_API int grt_plan_write(grt_plan *plan, const char *path);
+
 /* Earth-flattening transform of a spherical model (the reference's caller-side
  * preprocessing, greent.py:13-47 and 65-67, moved into the library): a layer
  * of thickness h whose bottom lies at radius r is stretched by R / (r + h/2),

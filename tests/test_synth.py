@@ -93,3 +93,14 @@ def test_synthesis_needs_moment_tensor(job):
         ps.synth(g.dc_moment(0, 90, 0), [0.0])
     assert e.value.status == g.ERR_UNSUPPORTED
     ps.close()
+
+
+@pytest.mark.gpu
+def test_binary_output_roundtrip(job, tmp_path):
+    g, p, tr, o = job
+    path = tmp_path / "g.bin"
+    p.write(path)
+    b = g.read_bin(path)
+    assert b["traces"].shape == tr.shape and np.array_equal(b["dist"], p.dists)
+    assert b["dt"] == o.dt and b["sigma"] == p.report.sigma
+    assert np.array_equal(b["traces"], tr.astype(np.float32))
