@@ -22,7 +22,7 @@ Arms (all FP32 arithmetic, checked against the FP64 path of the same method):
          the batch graph plus the wall time of its judge and fallback.
   e2e    traces/s of the fast arm through the public call with host inputs
          and outputs: prediction, batch build (with autotuning), execution,
-         judge, fallback and the download of every trace, per step.
+         judge, fallback and the download of every trace (float32), per step.
 
 Other cases: --case config2 (one 20-layer model, 200 receivers 5-300 km, nt
 4096, nk 16384) and --case config1 (4 layers, 10 receivers) time the

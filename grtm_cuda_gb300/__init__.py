@@ -126,7 +126,7 @@ EXPORTS = ("grt_create", "grt_destroy", "grt_last_error", "grt_status_string", "
            "grt_mlp_n_params", "grt_mlp_get_params", "grt_mlp_set_params", "grt_mlp_forward",
            "grt_mlp_loss_grad", "grt_mlp_train", "grt_batch_create", "grt_batch_execute", "grt_batch_fetch",
            "grt_batch_fetch_freqs", "grt_batch_info", "grt_batch_destroy", "grt_dc_moment", "grt_plan_synth",
-           "grt_batch_synth", "grt_flatten", "grt_plan_write")
+           "grt_batch_synth", "grt_flatten", "grt_plan_write", "grt_plan_fetch_f32", "grt_batch_fetch_f32")
 
 _lib = None
 
@@ -188,6 +188,8 @@ def lib():
     L.grt_batch_destroy.argtypes = [vp]
     L.grt_batch_destroy.restype = None
     L.grt_plan_write.argtypes = [vp, ctypes.c_char_p]
+    L.grt_plan_fetch_f32.argtypes = [vp, P(ctypes.c_float)]
+    L.grt_batch_fetch_f32.argtypes = [vp, ctypes.c_int, P(ctypes.c_float)]
     L.grt_flatten.argtypes = [ctypes.c_int, _dp, _dp, _dp, ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp,
                               _dp, _dp, _dp, _dp]
     L.grt_dc_moment.argtypes = [ctypes.c_double] * 4 + [_dp]
@@ -406,6 +408,15 @@ class Batch:
         if rc:
             raise GrtError(rc, "grt_batch_info")
         return r.as_dict(), t.as_dict()
+
+    def fetch_f32(self, job):
+        """Traces of one job as float32 [n_dist, n_cols, N]."""
+        r, _ = self.info(job)
+        t = np.empty((len(self.dists[job]), r["n_cols"], r["n_samples"]), dtype=np.float32)
+        rc = lib().grt_batch_fetch_f32(self.h, int(job), t.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+        if rc:
+            raise GrtError(rc, self.ctx.error())
+        return t
 
     def fetch(self, job, traces=True, spectra=False):
         r, _ = self.info(job)

@@ -1452,3 +1452,27 @@ extern "C" int grt_plan_write(grt_plan *p, const char *path)
     ok = (fclose(f) == 0) && ok;
     return ok ? GRT_OK : set_err(ctx, GRT_ERR_IO, std::string("short write to ") + path);
 }
+
+// traces as float32 (the working precision of FP32 plans: no widening on the host)
+extern "C" int grt_plan_fetch_f32(grt_plan *p, float *traces)
+{
+    if (!p || !traces) return GRT_ERR_ARG;
+    grt_ctx *ctx = p->ctx;
+    const size_t n = (size_t)p->nd * p->nc * p->J.N;
+    CU(cudaSetDevice(ctx->device));
+    if (p->prec) {
+        std::vector<double> h(n);
+        CU(cudaMemcpy(h.data(), p->sig, n * sizeof(double), cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < n; i++) traces[i] = (float)h[i];
+        return GRT_OK;
+    }
+    CU(cudaMemcpyAsync(traces, p->sig, n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    return GRT_OK;
+}
+
+extern "C" int grt_batch_fetch_f32(grt_batch *b, int job, float *traces)
+{
+    if (!b || job < 0 || job >= (int)b->jobs.size()) return GRT_ERR_ARG;
+    return grt_plan_fetch_f32(b->jobs[job], traces);
+}

@@ -435,9 +435,9 @@ def run_learned(sampler, m, dists, ctx=None, plain=PLAIN, tail_tol=None, spec_to
 def run_learned_batch(sampler, models, dists_list, ctx=None, plain=PLAIN, spec_tol=3e-3, autotune=True,
                       use_stride=True):
     """run_learned for many models at once: one batch (one CUDA graph, one
-    persistent GRT launch) on the learned grids, the judge's spot
-    evaluations as a second batch, sweeps per model, and the plain grid for
-    any receiver the judge rejects.  Returns (list of traces, info)."""
+    GRT launch) on the learned grids, the judge's spot evaluations as a
+    second batch, sweeps per model, and the plain grid for any receiver the
+    judge rejects.  Returns (list of float32 traces, info)."""
     own = ctx is None
     ctx = ctx or Context()
     try:
@@ -451,7 +451,7 @@ def run_learned_batch(sampler, models, dists_list, ctx=None, plain=PLAIN, spec_t
         b = Batch(ctx, jobs, autotune=autotune)
         t.append(time.perf_counter())
         rep = b.execute()
-        traces = [b.fetch(j)[0] for j in range(len(jobs))]
+        traces = [b.fetch_f32(j) for j in range(len(jobs))]
         t.append(time.perf_counter())
         # judge: spot frequencies on the plain grid (batched), tails by sweep
         spot_jobs, spots = [], []
@@ -486,7 +486,7 @@ def run_learned_batch(sampler, models, dists_list, ctx=None, plain=PLAIN, spec_t
             if idx:
                 p = Plan(ctx, mods[j], plain_opts(plain), np.asarray(dists_list[j], np.float64)[idx])
                 p.execute()
-                traces[j][idx], _ = p.fetch(True, False)
+                traces[j][idx] = p.fetch(True, False)[0].astype(np.float32)
                 p.close()
         t.append(time.perf_counter())
         _, tune = b.info()

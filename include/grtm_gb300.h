@@ -114,6 +114,8 @@ GRT_API int grt_plan_execute(grt_plan *plan, grt_report *report);
 /* traces: [n_dist][n_cols][N] doubles; spectra: [n_dist][n_cols][N] complex as
  * (re, im) doubles (after taper and Hermitian fill).  Either may be NULL. */
 GRT_API int grt_plan_fetch(grt_plan *plan, double *traces, double *spectra);
+/* traces as float32 [n_dist][n_cols][N] (FP32 plans: their working precision) */
+GRT_API int grt_plan_fetch_f32(grt_plan *plan, float *traces);
 /* spectra at selected frequency indices (0..N-1) only: [n_dist][n_cols][n_freq]
  * complex as (re, im) doubles */
 GRT_API int grt_plan_fetch_freqs(grt_plan *plan, int n_freq, const int *freq_idx, double *spectra);
@@ -197,6 +199,7 @@ GRT_API int grt_batch_create(grt_ctx *ctx, int n_jobs, const grt_job *jobs, int 
 /* report: aggregate (n_wk, bytes, launches; ms_grt and ms_total of the graph) */
 GRT_API int grt_batch_execute(grt_batch *batch, grt_report *report);
 GRT_API int grt_batch_fetch(grt_batch *batch, int job, double *traces, double *spectra);
+GRT_API int grt_batch_fetch_f32(grt_batch *batch, int job, float *traces);
 GRT_API int grt_batch_fetch_freqs(grt_batch *batch, int job, int n_freq, const int *freq_idx, double *spectra);
 /* job = -1: the batch's aggregate report */
 GRT_API int grt_batch_info(const grt_batch *batch, int job, grt_report *report, grt_tune *tune);

@@ -36,6 +36,8 @@ def test_batch_equals_single_jobs(ctx, prec):
     rep = b.execute()
     assert rep.n_wk == sum(g.grid(m, o)["n_wk"] for m, o, _ in jobs)
     first = [b.fetch(j)[0] for j in range(len(jobs))]
+    for j in range(len(jobs)):
+        assert np.array_equal(b.fetch_f32(j), first[j].astype(np.float32))
     b.execute()                                        # the graph replays
     for j, (m, o, d) in enumerate(jobs):
         t1, _, _ = g.run(m, o, d, ctx=ctx)
