@@ -461,8 +461,11 @@ def run_learned_batch(sampler, models, dists_list, ctx=None, plain=PLAIN, spec_t
             nk_spot[sp] = plain["nk"]
             spot_jobs.append((mo, custom_opts(nk_spot, gr["dk"], plain), d))
             spots.append(sp)
+        tj = [time.perf_counter()]
         sb = Batch(ctx, spot_jobs, autotune=False)
+        tj.append(time.perf_counter())
         sb.execute()
+        tj.append(time.perf_counter())
         n_fb = 0
         fallback = []
         for j, (mo, (nk, st, kmax, gr), d) in enumerate(zip(mods, grids, dists_list)):
@@ -480,6 +483,7 @@ def run_learned_batch(sampler, models, dists_list, ctx=None, plain=PLAIN, spec_t
             bad |= (excess.max(0) > 10.0)[below]
             fallback.append(np.nonzero(bad)[0].tolist())
             n_fb += int(bad.sum())
+        tj.append(time.perf_counter())
         sb.close()
         t.append(time.perf_counter())
         for j, idx in enumerate(fallback):
@@ -495,7 +499,8 @@ def run_learned_batch(sampler, models, dists_list, ctx=None, plain=PLAIN, spec_t
                     stride_mean=float(np.mean([g_[1].mean() for g_ in grids])), fallback=fallback,
                     n_fallback=n_fb, ms_batch_gpu=rep.ms_total, ms_batch_grt=rep.ms_grt,
                     gpu_launches=rep.kernel_launches, tune=tune, s_predict=t[1] - t[0], s_build=t[2] - t[1],
-                    s_execute=t[3] - t[2], s_judge=t[4] - t[3], s_fallback=t[5] - t[4], s_total=t[5] - t[0])
+                    s_execute=t[3] - t[2], s_judge=t[4] - t[3], s_fallback=t[5] - t[4], s_total=t[5] - t[0],
+                    s_judge_parts=dict(spot_build=tj[1] - tj[0], spot_exec=tj[2] - tj[1], sweeps_compare=tj[3] - tj[2]))
         b.close()
         return traces, info
     finally:
