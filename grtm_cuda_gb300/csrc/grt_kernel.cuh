@@ -27,6 +27,23 @@
 
 namespace grt {
 
+// Inlining policy of the large helpers.  Fully inlined, the per-point body
+// outgrows the instruction cache (a dozen call sites of the complex
+// exponential alone, each with the slow path of sincosf); one out-of-line
+// copy of the chosen helpers keeps the hot loop resident.
+#ifndef GRT_INLINE_EXP
+#define GRT_INLINE_EXP __noinline__
+#endif
+#ifndef GRT_INLINE_LAYER
+#define GRT_INLINE_LAYER __forceinline__
+#endif
+#ifndef GRT_INLINE_IF
+#define GRT_INLINE_IF __forceinline__
+#endif
+#ifndef GRT_INLINE_PHASE
+#define GRT_INLINE_PHASE __forceinline__
+#endif
+
 // ---------------------------------------------------------------- layer data
 template <typename R>
 struct SL {
@@ -117,7 +134,7 @@ template <typename R> __device__ __forceinline__ Zd<R> zd(double d)
 
 // e^{-(nu + nulo)(z + zlo)}, the exponent formed in double-float
 template <typename R>
-__device__ __forceinline__ C<R> exp_nz(C<R> nu, C<R> nulo, Zd<R> z)
+__device__ GRT_INLINE_EXP C<R> exp_nz(C<R> nu, C<R> nulo, Zd<R> z)
 {
     if constexpr (sizeof(R) == 4) {
         float px, ex, py, ey;
@@ -132,7 +149,7 @@ __device__ __forceinline__ C<R> exp_nz(C<R> nu, C<R> nulo, Zd<R> z)
 }
 
 template <typename R>
-__device__ __forceinline__ void make_layer(const LayerW<R> &T, const K2<R> &k2, R k, SL<R> &L)
+__device__ GRT_INLINE_LAYER void make_layer(const LayerW<R> &T, const K2<R> &k2, R k, SL<R> &L)
 {
     if constexpr (sizeof(R) == 4) {
         C<R> zr, zrl, zv, zvl;
@@ -177,7 +194,7 @@ __device__ __forceinline__ void make_layer(const LayerW<R> &T, const K2<R> &k2, 
 
 // S^-1 diag(e^{-rz}, e^{-vz}) S  (upper triangular)
 template <typename R>
-__device__ __forceinline__ M2<R> phase(const SL<R> &L, Zd<R> zz, C<R> *ev_out = nullptr)
+__device__ GRT_INLINE_PHASE M2<R> phase(const SL<R> &L, Zd<R> zz, C<R> *ev_out = nullptr)
 {
     const R z = zz.hi;
     C<R> er = exp_nz(L.r, L.rlo, zz), ev = exp_nz(L.v, L.vlo, zz);
@@ -191,7 +208,7 @@ __device__ __forceinline__ M2<R> phase(const SL<R> &L, Zd<R> zz, C<R> *ev_out = 
 
 // S^-1 diag(sg r0 e^{-rz}, sg v0 e^{-vz}) S; r0, v0 = own nu unless given
 template <typename R>
-__device__ __forceinline__ M2<R> dphase(const SL<R> &L, Zd<R> zz, R sg, const C<R> *nu0)
+__device__ GRT_INLINE_PHASE M2<R> dphase(const SL<R> &L, Zd<R> zz, R sg, const C<R> *nu0)
 {
     const R z = zz.hi;
     C<R> er = exp_nz(L.r, L.rlo, zz), ev = exp_nz(L.v, L.vlo, zz);
@@ -218,7 +235,7 @@ struct IF {
 
 // interface between U (upper layer) and D (lower layer)
 template <typename R>
-__device__ __forceinline__ void interface_rt(const SL<R> &U, const SL<R> &D, R k, IF<R> &m)
+__device__ GRT_INLINE_IF void interface_rt(const SL<R> &U, const SL<R> &D, R k, IF<R> &m)
 {
     const C<R> kk = {k, R(0)};
     M2<R> GU = {kk, U.d0, U.p3, U.d3}, HU = {U.p1, U.d1, U.p2, U.d2};
