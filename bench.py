@@ -22,7 +22,8 @@ Arms (all FP32 arithmetic, checked against the FP64 path of the same method):
          the batch graph plus the wall time of its judge and fallback.
   e2e    traces/s of the fast arm through the public call with host inputs
          and outputs: prediction, batch build (with autotuning), execution,
-         judge, fallback and the download of every trace (float32), per step.
+         judge, fallback and the download of every trace (float32, into
+         page-locked host arrays allocated once), per step.
 
 Other cases: --case config2 (one 20-layer model, 200 receivers 5-300 km, nt
 4096, nk 16384) and --case config1 (4 layers, 10 receivers) time the
@@ -278,8 +279,12 @@ def bench_batch(args, ws, rank, local, td):
     dists = [d for _, d in work]
     layers = [g.grid(g.make_model(**m), learned.plain_opts())["n_layer"] for m in models]
 
+    # the traces come back into page-locked host arrays, allocated once
+    grids0 = [g.grid(g.make_model(**m), learned.plain_opts()) for m in models]
+    pinned = [g.pinned_empty((len(d), gr["n_cols"], gr["n_samples"])) for d, gr in zip(dists, grids0)]
+
     def fast_step():
-        return learned.run_learned_batch(sampler, models, dists, ctx=ctx)
+        return learned.run_learned_batch(sampler, models, dists, ctx=ctx, out=pinned)
 
     for _ in range(args.warmup):
         tr_fast, info = fast_step()
@@ -358,7 +363,8 @@ def bench_batch(args, ws, rank, local, td):
         "arms": {
             "fast": {"value": value, "e2e": e2e, "ms_batch_gpu": last["ms_batch_gpu"],
                      "ms_batch_grt": last["ms_batch_grt"], "s_predict": last["s_predict"],
-                     "s_build": last["s_build"], "s_execute_fetch": last["s_execute"], "s_judge": last["s_judge"],
+                     "s_build": last["s_build"], "s_execute_fetch": last["s_execute"], "s_fetch": last["s_fetch"],
+                     "s_judge": last["s_judge"],
                      "s_fallback": last["s_fallback"], "judge_parts": last.get("s_judge_parts"),
                      "points_vs_plain": frac_pts,
                      "stride_mean": last["stride_mean"], "fallback_traces": last["n_fallback"],

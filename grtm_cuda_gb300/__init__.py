@@ -35,7 +35,8 @@ class Opts(ctypes.Structure):
                 ("taper", ctypes.c_double), ("sigma_factor", ctypes.c_double), ("k_mode", ctypes.c_int),
                 ("nk_fixed", ctypes.c_int), ("dk", ctypes.c_double), ("precision", ctypes.c_int),
                 ("fix", ctypes.c_int), ("nk_custom", ctypes.POINTER(ctypes.c_int)),
-                ("k_stride", ctypes.POINTER(ctypes.c_int))]
+                ("k_stride", ctypes.POINTER(ctypes.c_int)), ("n_freq_sel", ctypes.c_int),
+                ("freq_sel", ctypes.POINTER(ctypes.c_int)), ("k_slice", ctypes.c_int)]
 
 
 class Report(ctypes.Structure):
@@ -46,7 +47,7 @@ class Report(ctypes.Structure):
                 ("sigma", ctypes.c_double), ("ms_grt", ctypes.c_float), ("ms_bessel", ctypes.c_float),
                 ("ms_ksum", ctypes.c_float), ("ms_spectral", ctypes.c_float), ("ms_total", ctypes.c_float),
                 ("kernel_launches", ctypes.c_int), ("h2d_bytes", ctypes.c_longlong),
-                ("d2h_bytes", ctypes.c_longlong), ("ksum_impl", ctypes.c_int)]
+                ("d2h_bytes", ctypes.c_longlong), ("ksum_impl", ctypes.c_int), ("k_slice", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -68,6 +69,31 @@ def make_source(m6, stf=None):
         s.stf = _ptr(a)
         s._keep = a
     return s
+
+
+class _HostBuf:
+    """Page-locked host memory from grt_host_alloc, freed when the last
+    array over it goes (numpy keeps this object as the arrays' base)."""
+
+    def __init__(self, nbytes, dtype, shape):
+        self.p = ctypes.c_void_p()
+        rc = lib().grt_host_alloc(max(1, nbytes), ctypes.byref(self.p))
+        if rc:
+            raise GrtError(rc, "grt_host_alloc")
+        self.__array_interface__ = {"shape": tuple(shape), "typestr": np.dtype(dtype).str,
+                                    "data": (self.p.value, False), "version": 3}
+
+    def __del__(self):
+        if self.p:
+            lib().grt_host_free(self.p)
+            self.p = ctypes.c_void_p()
+
+
+def pinned_empty(shape, dtype=np.float32):
+    """An uninitialised array in page-locked host memory: the destination of
+    fetches that should run at the host link's full rate."""
+    shape = tuple(int(x) for x in np.atleast_1d(shape))
+    return np.asarray(_HostBuf(int(np.prod(shape)) * np.dtype(dtype).itemsize, dtype, shape))
 
 
 R_EARTH = 6371.0
@@ -126,7 +152,8 @@ EXPORTS = ("grt_create", "grt_destroy", "grt_last_error", "grt_status_string", "
            "grt_mlp_n_params", "grt_mlp_get_params", "grt_mlp_set_params", "grt_mlp_forward",
            "grt_mlp_loss_grad", "grt_mlp_train", "grt_batch_create", "grt_batch_execute", "grt_batch_fetch",
            "grt_batch_fetch_freqs", "grt_batch_info", "grt_batch_destroy", "grt_dc_moment", "grt_plan_synth",
-           "grt_batch_synth", "grt_flatten", "grt_plan_write", "grt_plan_fetch_f32", "grt_batch_fetch_f32")
+           "grt_batch_synth", "grt_flatten", "grt_plan_write", "grt_plan_fetch_f32", "grt_batch_fetch_f32",
+           "grt_host_alloc", "grt_host_free", "grt_trim")
 
 _lib = None
 
@@ -190,6 +217,11 @@ def lib():
     L.grt_plan_write.argtypes = [vp, ctypes.c_char_p]
     L.grt_plan_fetch_f32.argtypes = [vp, P(ctypes.c_float)]
     L.grt_batch_fetch_f32.argtypes = [vp, ctypes.c_int, P(ctypes.c_float)]
+    L.grt_host_alloc.argtypes = [ctypes.c_size_t, P(vp)]
+    L.grt_host_free.argtypes = [vp]
+    L.grt_host_free.restype = None
+    L.grt_trim.argtypes = [vp]
+    L.grt_trim.restype = None
     L.grt_flatten.argtypes = [ctypes.c_int, _dp, _dp, _dp, ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp,
                               _dp, _dp, _dp, _dp]
     L.grt_dc_moment.argtypes = [ctypes.c_double] * 4 + [_dp]
@@ -226,6 +258,11 @@ class Context:
     def error(self):
         return lib().grt_last_error(self.h).decode()
 
+    def trim(self):
+        """Return the device memory cached for reuse by later plans."""
+        if self.h:
+            lib().grt_trim(self.h)
+
     def close(self):
         if self.h:
             lib().grt_destroy(self.h)
@@ -246,11 +283,13 @@ def make_model(ztop, vp, vs, rho, qp, qs, hs, hr=0.0, src_type=0):
 
 
 def make_opts(dt, log2n, t0=0.0, taper=0.3, sigma_factor=2.0, k_mode=K_REFERENCE, nk_fixed=0, dk=0.0,
-              precision=FP32, fix=0, nk_custom=None, k_stride=None):
+              precision=FP32, fix=0, nk_custom=None, k_stride=None, freq_sel=None, k_slice=0):
     """nk_custom: points per frequency (N/2 ints) for K_CUSTOM grids;
-    k_stride: optional per-frequency stride m (k_j = j m dk)."""
+    k_stride: optional per-frequency stride m (k_j = j m dk);
+    freq_sel: evaluate only these frequency indices (a spectra-only plan);
+    k_slice: wavenumbers per split-K slice of the tensor-core sum (0: auto)."""
     o = Opts(float(dt), int(log2n), float(t0), float(taper), float(sigma_factor), int(k_mode),
-             int(nk_fixed), float(dk), int(precision), int(fix), None, None)
+             int(nk_fixed), float(dk), int(precision), int(fix), None, None, 0, None, int(k_slice))
     o._keep = []
     if nk_custom is not None:
         arr = np.ascontiguousarray(nk_custom, dtype=np.int32)
@@ -260,6 +299,11 @@ def make_opts(dt, log2n, t0=0.0, taper=0.3, sigma_factor=2.0, k_mode=K_REFERENCE
     if k_stride is not None:
         arr = np.ascontiguousarray(k_stride, dtype=np.int32)
         o.k_stride = arr.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+        o._keep.append(arr)
+    if freq_sel is not None:
+        arr = np.ascontiguousarray(freq_sel, dtype=np.int32)
+        o.freq_sel = arr.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+        o.n_freq_sel = len(arr)
         o._keep.append(arr)
     return o
 
@@ -409,10 +453,14 @@ class Batch:
             raise GrtError(rc, "grt_batch_info")
         return r.as_dict(), t.as_dict()
 
-    def fetch_f32(self, job):
-        """Traces of one job as float32 [n_dist, n_cols, N]."""
+    def fetch_f32(self, job, out=None):
+        """Traces of one job as float32 [n_dist, n_cols, N], into `out` when
+        given (e.g. a pinned_empty array, reused from call to call)."""
         r, _ = self.info(job)
-        t = np.empty((len(self.dists[job]), r["n_cols"], r["n_samples"]), dtype=np.float32)
+        shape = (len(self.dists[job]), r["n_cols"], r["n_samples"])
+        t = np.empty(shape, dtype=np.float32) if out is None else out
+        if t.shape != shape or t.dtype != np.float32 or not t.flags.c_contiguous:
+            raise ValueError(f"out must be a C-contiguous float32 array of shape {shape}")
         rc = lib().grt_batch_fetch_f32(self.h, int(job), t.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
         if rc:
             raise GrtError(rc, self.ctx.error())

@@ -2,6 +2,7 @@
 // file-to-file entry point green().
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -33,6 +34,7 @@ struct grt_plan {
     int nd = 0, nc = 0, nq = 0, ntiles = 0;
     int rt = 128, jt = 1;
     int use_tc = 0, nsplit = 1, kslice = 0;   // tensor-core wavenumber sum and its split-K
+    int kslice_req = 0;                       // requested k per slice (0: chosen here)
     int bt_rows = 0;                          // > 0: Bessel table tiled by 16 receivers (unit strides)
     int cols = 0;                             // output column layout (grt::ColKind)
     void *P = nullptr;                        // split-K partial sums
@@ -45,7 +47,7 @@ struct grt_plan {
     void *spec = nullptr, *sig = nullptr;
     int2 *tiles = nullptr;
     int *nk = nullptr, *ks = nullptr;
-    long long *koff = nullptr;
+    long long *koff = nullptr, *tfirst = nullptr;
     double *ddist = nullptr, *damp = nullptr;
     unsigned *derr = nullptr;
     bool own_derr = true;                     // false inside a batch (the batch's error word)
@@ -65,6 +67,81 @@ static int set_err(grt_ctx *ctx, int code, const std::string &msg)
             return set_err(ctx, e_ == cudaErrorMemoryAllocation ? GRT_ERR_NOMEM : GRT_ERR_CUDA,          \
                            std::string(#call) + ": " + cudaGetErrorString(e_));                        \
     } while (0)
+
+// ------------------------------------------------------------------ device memory
+// Plans and batches take their device memory from the context's cache:
+// blocks a destroyed plan releases are kept (up to half the device memory)
+// and handed to the next request of a similar size, so a plan or batch made
+// per call pays neither cudaMalloc's page mapping nor cudaFree's device-wide
+// synchronisation.  All work on a context's memory is ordered on its stream
+// (batch graphs join their side streams back into it), so a block is reused
+// only by work queued after the work that last used it.
+static size_t pool_round(size_t n)
+{
+    const size_t g = n < ((size_t)1 << 20) ? 256 : ((size_t)2 << 20);
+    return (std::max<size_t>(n, 1) + g - 1) / g * g;
+}
+
+static void pool_trim(grt_ctx *ctx, size_t keep)
+{
+    while (ctx->pooled > keep && !ctx->pool.empty()) {
+        auto it = std::prev(ctx->pool.end());   // largest first
+        cudaFree(it->second);
+        ctx->pooled -= it->first;
+        ctx->pool.erase(it);
+    }
+}
+
+template <typename T>
+static cudaError_t dev_alloc(grt_ctx *ctx, T **out, size_t bytes)
+{
+    const size_t n = pool_round(bytes);
+    void *p = nullptr;
+    auto it = ctx->pool.lower_bound(n);
+    if (it != ctx->pool.end() && it->first <= n + n / 8) {
+        p = it->second;
+        ctx->live[p] = it->first;
+        ctx->pooled -= it->first;
+        ctx->pool.erase(it);
+        *out = (T *)p;
+        return cudaSuccess;
+    }
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e == cudaErrorMemoryAllocation && ctx->pooled) {
+        cudaGetLastError();
+        pool_trim(ctx, 0);
+        e = cudaMalloc(&p, n);
+    }
+    if (e != cudaSuccess) {
+        *out = nullptr;
+        return e;
+    }
+    ctx->live[p] = n;
+    *out = (T *)p;
+    return cudaSuccess;
+}
+
+static void dev_free(grt_ctx *ctx, void *p)
+{
+    if (!p) return;
+    auto it = ctx->live.find(p);
+    if (it == ctx->live.end()) {
+        cudaFree(p);
+        return;
+    }
+    ctx->pool.emplace(it->second, p);
+    ctx->pooled += it->second;
+    ctx->live.erase(it);
+    if (ctx->pooled > ctx->pool_cap) pool_trim(ctx, ctx->pool_cap);
+}
+
+extern "C" void grt_trim(grt_ctx *ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    pool_trim(ctx, 0);
+}
 
 extern "C" const char *grt_status_string(int s)
 {
@@ -92,6 +169,9 @@ extern "C" int grt_create(grt_ctx **out, int device)
     CU(cudaSetDevice(device));
     CU(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     for (auto &e : c->ev) CU(cudaEventCreate(&e));
+    size_t free_b = 0, total_b = 0;
+    CU(cudaMemGetInfo(&free_b, &total_b));
+    c->pool_cap = total_b / 2;
     *out = c.release();
     return GRT_OK;
 }
@@ -102,7 +182,11 @@ extern "C" void grt_destroy(grt_ctx *ctx)
     cudaSetDevice(ctx->device);
     for (auto &e : ctx->ev)
         if (e) cudaEventDestroy(e);
-    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->stream) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaStreamDestroy(ctx->stream);
+    }
+    pool_trim(ctx, 0);
     delete ctx;
 }
 
@@ -113,9 +197,8 @@ extern "C" void grt_plan_destroy(grt_plan *p)
     if (!p) return;
     cudaSetDevice(p->ctx->device);
     void *bufs[] = {p->tab, p->K, p->B, p->S, p->post, p->tw, p->spec, p->sig, p->tiles, p->nk, p->koff, p->ddist,
-                    p->damp, p->own_derr ? p->derr : nullptr, p->P, p->Kt, p->kt_base, p->ks};
-    for (void *b : bufs)
-        if (b) cudaFree(b);
+                    p->damp, p->own_derr ? p->derr : nullptr, p->P, p->Kt, p->kt_base, p->ks, p->tfirst};
+    for (void *b : bufs) dev_free(p->ctx, b);
     delete p;
 }
 
@@ -154,18 +237,20 @@ template <typename R>
 static void build_tables(const Job &J, std::vector<grt::LayerW<R>> &tab, std::vector<R> &post, std::vector<R> &tw,
                          std::vector<double> &damp)
 {
-    const int L = J.L, nw = J.nw, N = J.N;
+    const int L = J.L, nw = J.nw, nwf = J.nwf, N = J.N;
     tab.resize((size_t)nw * L);
     grt::fill_layer_table<R>(J, tab.data());
-    // phase e^{i w_r t0}, cosine taper and scale df nw / pi (green.cu:1905-1921)
+    // phase e^{i w_r t0}, cosine taper and scale df nw / pi (green.cu:1905-1921),
+    // nw the grid's positive frequencies, at the frequency of each row
     post.resize(2 * (size_t)nw);
-    const int wc = (int)((double)nw * (1 - J.taper));
-    const double coef = J.df * nw / PI;
-    for (int iw = 0; iw < nw; iw++) {
-        double st0 = iw > wc ? 0.5 * (1. + std::cos((iw - wc + 1) * PI / (nw - wc + 1))) : 1.0;
+    const int wc = (int)((double)nwf * (1 - J.taper));
+    const double coef = J.df * nwf / PI;
+    for (int row = 0; row < nw; row++) {
+        const int iw = grt::job_freq(J, row);
+        double st0 = iw > wc ? 0.5 * (1. + std::cos((iw - wc + 1) * PI / (nwf - wc + 1))) : 1.0;
         double phi = 2 * PI * J.df * iw * J.t0;
-        post[2 * iw] = (R)(std::cos(phi) * st0 * coef);
-        post[2 * iw + 1] = (R)(std::sin(phi) * st0 * coef);
+        post[2 * row] = (R)(std::cos(phi) * st0 * coef);
+        post[2 * row + 1] = (R)(std::sin(phi) * st0 * coef);
     }
     tw.resize(N);  // N/2 complex
     for (int m = 0; m < N / 2; m++) {
@@ -187,17 +272,16 @@ static int upload(grt_plan *p)
     std::vector<double> damp;
     build_tables<R>(J, tab, post, tw, damp);
     // slot-0 vertical wavenumbers (w = -i sigma, k = 0) of the receiver layer
-    {
-        const auto &t = tab[J.rl];
-        cd r0 = std::sqrt(cd(-t.wa2x, -t.wa2y)), v0 = std::sqrt(cd(-t.wb2x, -t.wb2y));
-        if (r0.real() < 0) r0 = -r0;
-        if (v0.real() < 0) v0 = -v0;
-        p->slot0[0] = r0.real(); p->slot0[1] = r0.imag(); p->slot0[2] = v0.real(); p->slot0[3] = v0.imag();
+    grt::slot0_wavenumbers(J, p->slot0);
+    // tiles of kGrtThreads wavenumbers, listed on the device from one offset per frequency
+    std::vector<long long> tfirst(J.nw);
+    long long ntl = 0;
+    for (int iw = 0; iw < J.nw; iw++) {
+        tfirst[iw] = ntl;
+        ntl += (J.nk[iw] + grt::kGrtThreads - 1) / grt::kGrtThreads;
     }
-    std::vector<int2> tiles;
-    for (int iw = 0; iw < J.nw; iw++)
-        for (int j0 = 0; j0 < J.nk[iw]; j0 += grt::kGrtThreads) tiles.push_back(make_int2(iw, j0));
-    p->ntiles = (int)tiles.size();
+    if (ntl >= (1LL << 31)) return set_err(ctx, GRT_ERR_UNSUPPORTED, "too many (w,k) tiles for one launch");
+    p->ntiles = (int)ntl;
     const size_t szK = (size_t)p->nq * J.nkw * 2 * sizeof(R);
     // the tensor-core sum reads the Bessel table in receiver tiles of 16 when
     // every frequency has a unit stride (a stage's rows are then contiguous)
@@ -207,22 +291,25 @@ static int upload(grt_plan *p)
     const size_t szB = p->bt_rows ? (size_t)((p->nd + 15) / 16) * 16 * p->bt_rows * grt::NBASIS * sizeof(R)
                                   : (size_t)J.nbrow * grt::NBASIS * p->nd * sizeof(R);
     const size_t ntr = (size_t)p->nd * p->nc;
-    CU(cudaMalloc(&p->tab, tab.size() * sizeof(tab[0])));
-    CU(cudaMalloc(&p->tiles, tiles.size() * sizeof(int2)));
-    CU(cudaMalloc(&p->nk, J.nw * sizeof(int)));
-    CU(cudaMalloc(&p->koff, J.nw * sizeof(long long)));
-    CU(cudaMalloc(&p->ks, J.nw * sizeof(int)));
-    CU(cudaMalloc(&p->ddist, p->nd * sizeof(double)));
-    if (!p->use_tc) CU(cudaMalloc(&p->K, szK));
-    CU(cudaMalloc(&p->B, szB));
+    CU(dev_alloc(ctx, &p->tab, tab.size() * sizeof(tab[0])));
+    CU(dev_alloc(ctx, &p->tiles, ntl * sizeof(int2)));
+    CU(dev_alloc(ctx, &p->tfirst, J.nw * sizeof(long long)));
+    CU(dev_alloc(ctx, &p->nk, J.nw * sizeof(int)));
+    CU(dev_alloc(ctx, &p->koff, J.nw * sizeof(long long)));
+    CU(dev_alloc(ctx, &p->ks, J.nw * sizeof(int)));
+    CU(dev_alloc(ctx, &p->ddist, p->nd * sizeof(double)));
+    if (!p->use_tc) CU(dev_alloc(ctx, &p->K, szK));
+    CU(dev_alloc(ctx, &p->B, szB));
     if (p->bt_rows) CU(cudaMemsetAsync(p->B, 0, szB, ctx->stream));   // padding rows and receivers stay zero
-    CU(cudaMalloc(&p->S, ntr * J.nw * 2 * sizeof(R)));
-    CU(cudaMalloc(&p->post, post.size() * sizeof(R)));
-    CU(cudaMalloc(&p->tw, tw.size() * sizeof(R)));
-    CU(cudaMalloc(&p->damp, damp.size() * sizeof(double)));
-    CU(cudaMalloc(&p->sig, ntr * J.N * sizeof(R)));
-    CU(cudaMalloc(&p->spec, ntr * J.N * 2 * sizeof(R)));
-    CU(cudaMalloc(&p->derr, sizeof(unsigned)));
+    CU(dev_alloc(ctx, &p->S, ntr * J.nw * 2 * sizeof(R)));
+    CU(dev_alloc(ctx, &p->post, post.size() * sizeof(R)));
+    CU(dev_alloc(ctx, &p->tw, tw.size() * sizeof(R)));
+    CU(dev_alloc(ctx, &p->damp, damp.size() * sizeof(double)));
+    // spectra-only plans (a frequency selection) keep [tr][row] spectra and no traces
+    const bool sel = !J.fsel.empty();
+    if (!sel) CU(dev_alloc(ctx, &p->sig, ntr * J.N * sizeof(R)));
+    CU(dev_alloc(ctx, &p->spec, ntr * (sel ? J.nw : J.N) * 2 * sizeof(R)));
+    CU(dev_alloc(ctx, &p->derr, sizeof(unsigned)));
     if (p->use_tc) {
         // split the k range so that the CTA count fills whole waves of the SMs (one CTA per SM)
         int nsm = 148;
@@ -240,7 +327,12 @@ static int upload(grt_plan *p)
         }
         p->nsplit = best;
         p->kslice = ((J.nkmax + best - 1) / best + grt::tc::kKT - 1) / grt::tc::kKT * grt::tc::kKT;
-        CU(cudaMalloc(&p->P, (size_t)best * ntr * J.nw * 2 * sizeof(float)));
+        if (p->kslice_req > 0) {
+            p->kslice = p->kslice_req;
+            p->nsplit = (J.nkmax + p->kslice - 1) / p->kslice;
+        }
+        p->rep.k_slice = p->kslice;
+        CU(dev_alloc(ctx, &p->P, (size_t)best * ntr * J.nw * 2 * sizeof(float)));
         // operand blocks of (frequency tile of 64, k stage of 8): nq x (hi, lo) x 1024 floats each
         const int nwt = (J.nw + grt::tc::kW - 1) / grt::tc::kW;
         std::vector<long long> base(nwt);
@@ -255,8 +347,8 @@ static int upload(grt_plan *p)
             base[t] = tot;
             tot += (long long)ns * p->nq * 2 * grt::tc::kM * grt::tc::kKT;
         }
-        CU(cudaMalloc(&p->Kt, (size_t)tot * sizeof(float)));
-        CU(cudaMalloc(&p->kt_base, nwt * sizeof(long long)));
+        CU(dev_alloc(ctx, &p->Kt, (size_t)tot * sizeof(float)));
+        CU(dev_alloc(ctx, &p->kt_base, nwt * sizeof(long long)));
         CU(cudaMemcpyAsync(p->kt_base, base.data(), nwt * sizeof(long long), cudaMemcpyHostToDevice, ctx->stream));
         // slots beyond a frequency's k range stay zero: the GRT kernel only writes valid (w,k)
         if (padded) CU(cudaMemsetAsync(p->Kt, 0, (size_t)tot * sizeof(float), ctx->stream));
@@ -264,8 +356,10 @@ static int upload(grt_plan *p)
     }
     cudaStream_t st = ctx->stream;
     CU(cudaMemcpyAsync(p->tab, tab.data(), tab.size() * sizeof(tab[0]), cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(p->tiles, tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(p->nk, J.nk.data(), J.nw * sizeof(int), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(p->tfirst, tfirst.data(), J.nw * sizeof(long long), cudaMemcpyHostToDevice, st));
+    grt::plan_tiles_kernel<<<J.nw, 256, 0, st>>>(p->nk, p->tfirst, grt::kGrtThreads, p->tiles);
+    CU(cudaGetLastError());
     CU(cudaMemcpyAsync(p->koff, J.koff.data(), J.nw * sizeof(long long), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(p->ks, J.ks.data(), J.nw * sizeof(int), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(p->ddist, p->dist.data(), p->nd * sizeof(double), cudaMemcpyHostToDevice, st));
@@ -273,10 +367,10 @@ static int upload(grt_plan *p)
     CU(cudaMemcpyAsync(p->tw, tw.data(), tw.size() * sizeof(R), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(p->damp, damp.data(), damp.size() * sizeof(double), cudaMemcpyHostToDevice, st));
     CU(cudaMemsetAsync(p->derr, 0, sizeof(unsigned), st));
-    p->rep.h2d_bytes = (long long)(tab.size() * sizeof(tab[0]) + tiles.size() * sizeof(int2) +
-                                   J.nw * (2 * sizeof(int) + sizeof(long long)) + p->nd * sizeof(double) +
+    p->rep.h2d_bytes = (long long)(tab.size() * sizeof(tab[0]) +
+                                   J.nw * (2 * sizeof(int) + 2 * sizeof(long long)) + p->nd * sizeof(double) +
                                    (post.size() + tw.size()) * sizeof(R) + damp.size() * sizeof(double));
-    p->rep.d2h_bytes = (long long)(ntr * J.N * sizeof(R));
+    p->rep.d2h_bytes = (long long)(ntr * (sel ? 2 * J.nw : J.N) * sizeof(R));
     CU(cudaStreamSynchronize(st));
     return GRT_OK;
 }
@@ -297,6 +391,7 @@ extern "C" int grt_plan_create(grt_ctx *ctx, const grt_model *m, const grt_opts 
     if (!rc)
         rc = grt::job_setup(p->J, o->dt, o->log2n, o->t0, o->taper, o->sigma_factor, o->k_mode, o->nk_fixed, o->dk,
                             o->fix, err, o->nk_custom, o->k_stride);
+    if (!rc && (o->n_freq_sel > 0 || o->freq_sel)) rc = grt::job_select(p->J, o->n_freq_sel, o->freq_sel, err);
     if (rc) return set_err(ctx, rc, err);
     const Job &J = p->J;
     p->prec = o->precision;
@@ -318,6 +413,11 @@ extern "C" int grt_plan_create(grt_ctx *ctx, const grt_model *m, const grt_opts 
     // the corrected 30-column tensor layout needs 16 coefficient columns: beyond the
     // tensor-core sum's shared and tensor memory, it runs the SIMT sum
     p->use_tc = (p->prec == GRT_FP32) && !(ks && !strcmp(ks, "simt")) && p->cols != grt::kColTensorFix;
+    if (o->k_slice < 0 || o->k_slice % grt::tc::kKT)
+        return set_err(ctx, GRT_ERR_ARG, "k_slice must be a non-negative multiple of 8");
+    if (o->k_slice > 0 && (J.nkmax + o->k_slice - 1) / o->k_slice > 4096)
+        return set_err(ctx, GRT_ERR_ARG, "k_slice too small: more than 4096 slices");
+    p->kslice_req = o->k_slice;
     p->rep.ksum_impl = p->use_tc;
     // the tensor-core sum multiplies a tile of 64 frequencies by one Bessel operand:
     // the frequencies of a tile share their k stride
@@ -454,6 +554,15 @@ static int launch_spectral(grt_plan *p, cudaStream_t st, int &launches)
     grt::SpecArgs<R> S{};
     S.S = (const R *)p->S; S.post = (const R *)p->post; S.tw = (const R *)p->tw; S.damp = p->damp;
     S.spec_out = (R *)p->spec; S.sig_out = (R *)p->sig; S.nw = J.nw; S.logn = J.log2n;
+    if (!J.fsel.empty()) {
+        // spectra-only plan: phase, taper and scale of each selected frequency
+        const long long n = (long long)p->nd * p->nc * J.nw;
+        const unsigned blocks = (unsigned)std::min<long long>((n + 255) / 256, 65535);
+        grt::select_kernel<R><<<blocks, 256, 0, st>>>((const R *)p->S, (const R *)p->post, (R *)p->spec, n, J.nw);
+        launches++;
+        CU(cudaGetLastError());
+        return GRT_OK;
+    }
     const size_t smem2 = (size_t)J.N * sizeof(grt::C<R>);
     CU(raise_smem_limit(grt::spectral_kernel<R>, (int)smem2));
     const int threads = std::min(512, std::max(32, J.N / 2));
@@ -541,6 +650,7 @@ extern "C" int grt_grid(const grt_model *m, const grt_opts *o, grt_report *r)
     if (!rc)
         rc = grt::job_setup(J, o->dt, o->log2n, o->t0, o->taper, o->sigma_factor, o->k_mode, o->nk_fixed, o->dk,
                             o->fix, err, o->nk_custom, o->k_stride);
+    if (!rc && (o->n_freq_sel > 0 || o->freq_sel)) rc = grt::job_select(J, o->n_freq_sel, o->freq_sel, err);
     if (rc) {
         fprintf(stderr, "grt_grid: %s\n", err.c_str());
         return rc;
@@ -601,10 +711,16 @@ static int fetch_freqs(grt_plan *p, int n_freq, const int *freq_idx, double *spe
     const size_t rows = (size_t)p->nd * p->nc;
     std::vector<grt::C<R>> h(rows * n_freq);
     // one strided copy per frequency: element iw of every (receiver, column) row
-    for (int f = 0; f < n_freq; f++)
-        CU(cudaMemcpy2DAsync(h.data() + f * rows, sizeof(grt::C<R>), (const grt::C<R> *)p->spec + freq_idx[f],
-                             (size_t)p->J.N * sizeof(grt::C<R>), sizeof(grt::C<R>), rows, cudaMemcpyDeviceToHost,
+    // full plans: spec [tr][N] by frequency; selections: spec [tr][row]
+    const Job &J = p->J;
+    const size_t pitch = J.fsel.empty() ? (size_t)J.N : (size_t)J.nw;
+    for (int f = 0; f < n_freq; f++) {
+        int col = freq_idx[f];
+        if (!J.fsel.empty()) col = (int)(std::find(J.fsel.begin(), J.fsel.end(), col) - J.fsel.begin());
+        CU(cudaMemcpy2DAsync(h.data() + f * rows, sizeof(grt::C<R>), (const grt::C<R> *)p->spec + col,
+                             pitch * sizeof(grt::C<R>), sizeof(grt::C<R>), rows, cudaMemcpyDeviceToHost,
                              ctx->stream));
+    }
     CU(cudaStreamSynchronize(ctx->stream));
     for (size_t r = 0; r < rows; r++)
         for (int f = 0; f < n_freq; f++) {
@@ -619,7 +735,9 @@ extern "C" int grt_plan_fetch_freqs(grt_plan *p, int n_freq, const int *freq_idx
     if (!p || n_freq < 1 || !freq_idx || !spectra) return GRT_ERR_ARG;
     grt_ctx *ctx = p->ctx;
     for (int f = 0; f < n_freq; f++)
-        if (freq_idx[f] < 0 || freq_idx[f] >= p->J.N) return set_err(ctx, GRT_ERR_ARG, "frequency index out of range");
+        if (freq_idx[f] < 0 || freq_idx[f] >= p->J.N ||
+            (!p->J.fsel.empty() && std::find(p->J.fsel.begin(), p->J.fsel.end(), freq_idx[f]) == p->J.fsel.end()))
+            return set_err(ctx, GRT_ERR_ARG, "frequency index out of range or not selected");
     CU(cudaSetDevice(ctx->device));
     return p->prec ? fetch_freqs<double>(p, n_freq, freq_idx, spectra) : fetch_freqs<float>(p, n_freq, freq_idx, spectra);
 }
@@ -628,6 +746,7 @@ extern "C" int grt_plan_fetch(grt_plan *p, double *traces, double *spectra)
 {
     if (!p) return GRT_ERR_ARG;
     grt_ctx *ctx = p->ctx;
+    if (!p->J.fsel.empty()) return set_err(ctx, GRT_ERR_UNSUPPORTED, "a frequency-selection plan has spectra only");
     CU(cudaSetDevice(ctx->device));
     return p->prec ? fetch<double>(p, traces, spectra) : fetch<float>(p, traces, spectra);
 }
@@ -772,32 +891,30 @@ extern "C" int grt_sweep_kmax(grt_ctx *ctx, const grt_model *m, const grt_opts *
         rc = grt::job_setup(J, o->dt, o->log2n, o->t0, o->taper, o->sigma_factor, o->k_mode, o->nk_fixed, o->dk,
                             o->fix, err, o->nk_custom, o->k_stride);
     if (rc) return set_err(ctx, rc, err);
-    // keep only the selected frequencies: compact coefficient offsets, tiles for them alone
-    std::vector<int> nk_sel(J.nw, 0);
-    std::vector<long long> koff(J.nw, 0);
-    long long tot = 0;
+    // keep only the selected frequencies as rows: tables, offsets and tiles for them alone
+    if (o->n_freq_sel > 0 || o->freq_sel) return set_err(ctx, GRT_ERR_ARG, "sweeps take their frequencies from freq_idx");
+    rc = grt::job_select(J, n_freq, freq_idx, err);
+    if (rc) return set_err(ctx, rc, err);
+    std::vector<int> rows(n_freq);
     std::vector<int2> tiles;
     for (int f = 0; f < n_freq; f++) {
-        const int iw = freq_idx[f];
-        if (iw < 0 || iw >= J.nw) return set_err(ctx, GRT_ERR_ARG, "frequency index out of range");
-        if (nk_sel[iw]) return set_err(ctx, GRT_ERR_ARG, "repeated frequency index");
-        nk_sel[iw] = J.nk[iw];
-        koff[iw] = tot;
-        tot += J.nk[iw];
-        for (int j0 = 0; j0 < J.nk[iw]; j0 += grt::kGrtThreads) tiles.push_back(make_int2(iw, j0));
+        rows[f] = f;
+        for (int j0 = 0; j0 < J.nk[f]; j0 += grt::kGrtThreads) tiles.push_back(make_int2(f, j0));
     }
+    const long long tot = J.nkw;
     const int nq = J.src == 0 ? (int)grt::QS_N : (int)grt::QT_N;
     std::vector<grt::LayerW<float>> tab;
     std::vector<float> post, tw;
     std::vector<double> damp;
     build_tables<float>(J, tab, post, tw, damp);
     struct Bufs {
+        grt_ctx *c;
         std::vector<void *> v;
-        ~Bufs() { for (void *p : v) cudaFree(p); }
-    } bufs;
+        ~Bufs() { for (void *p : v) dev_free(c, p); }
+    } bufs{ctx, {}};
     auto dalloc = [&](size_t n) -> void * {
         void *p = nullptr;
-        if (cudaMalloc(&p, n) != cudaSuccess) return nullptr;
+        if (dev_alloc(ctx, &p, n) != cudaSuccess) return nullptr;
         bufs.v.push_back(p);
         return p;
     };
@@ -816,9 +933,9 @@ extern "C" int grt_sweep_kmax(grt_ctx *ctx, const grt_model *m, const grt_opts *
     cudaStream_t st = ctx->stream;
     CU(cudaMemcpyAsync(d_tab, tab.data(), tab.size() * sizeof(tab[0]), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(d_tiles, tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(d_nk, nk_sel.data(), J.nw * sizeof(int), cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(d_koff, koff.data(), J.nw * sizeof(long long), cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(d_f, freq_idx, n_freq * sizeof(int), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(d_nk, J.nk.data(), J.nw * sizeof(int), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(d_koff, J.koff.data(), J.nw * sizeof(long long), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(d_f, rows.data(), n_freq * sizeof(int), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(d_r, band_r, n_band * sizeof(double), cudaMemcpyHostToDevice, st));
     if (k_judge) CU(cudaMemcpyAsync(d_judge, k_judge, nt_ * sizeof(double), cudaMemcpyHostToDevice, st));
     if (tol_abs) CU(cudaMemcpyAsync(d_tabs, tol_abs, nt_ * sizeof(double), cudaMemcpyHostToDevice, st));
@@ -837,11 +954,9 @@ extern "C" int grt_sweep_kmax(grt_ctx *ctx, const grt_model *m, const grt_opts *
     A.hr_layer = J.h[J.rl];
     A.L = J.L; A.s = J.s; A.rl = J.rl; A.src = J.src; A.fix = J.fix; A.nq = nq;
     {
-        const auto &t = tab[J.rl];
-        cd r0 = std::sqrt(cd(-t.wa2x, -t.wa2y)), v0 = std::sqrt(cd(-t.wb2x, -t.wb2y));
-        if (r0.real() < 0) r0 = -r0;
-        if (v0.real() < 0) v0 = -v0;
-        A.slot0[0] = (float)r0.real(); A.slot0[1] = (float)r0.imag(); A.slot0[2] = (float)v0.real(); A.slot0[3] = (float)v0.imag();
+        double s0[4];
+        grt::slot0_wavenumbers(J, s0);
+        for (int i = 0; i < 4; i++) A.slot0[i] = (float)s0[i];
     }
     A.err = (unsigned *)d_err;
     grt::grt_point_kernel<float><<<(unsigned)tiles.size(), grt::kGrtThreads, (size_t)J.L * sizeof(grt::LayerW<float>), st>>>(A);
@@ -962,6 +1077,7 @@ struct grt_batch {
     std::vector<grt_plan *> jobs;
     int prec = 0, maxL = 0, nsm = 0;
     void *d_args = nullptr;          // GrtArgs<R>[n_jobs]
+    void *d_rows = nullptr;          // per (job, frequency) row: id, nk, first tile of each width
     int4 *d_tiles[3] = {};           // tile lists for 64 / 128 / 256 threads per block
     int ntiles[3] = {};
     long long points = 0;
@@ -982,9 +1098,10 @@ extern "C" void grt_batch_destroy(grt_batch *b)
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
     for (grt_plan *p : b->jobs) grt_plan_destroy(p);
-    cudaFree(b->d_args);
-    for (auto *t : b->d_tiles) cudaFree(t);
-    cudaFree(b->derr);
+    dev_free(b->ctx, b->d_args);
+    dev_free(b->ctx, b->d_rows);
+    for (auto *t : b->d_tiles) dev_free(b->ctx, t);
+    dev_free(b->ctx, b->derr);
     for (auto &s : b->side)
         if (s) cudaStreamDestroy(s);
     cudaEvent_t evs[] = {b->ev_start, b->ev_grt, b->ev_end, b->fork0, b->fork1};
@@ -1166,23 +1283,46 @@ static int batch_build(grt_batch *b, int autotune)
     std::vector<grt::GrtArgs<R>> args;
     for (grt_plan *p : b->jobs) {
         // all of the job's kernels report bounded-wait failures to the batch's word
-        if (p->own_derr) cudaFree(p->derr);
+        if (p->own_derr) dev_free(ctx, p->derr);
         p->derr = b->derr;
         p->own_derr = false;
         args.push_back(grt_args<R>(p));
     }
-    CU(cudaMalloc(&b->d_args, args.size() * sizeof(args[0])));
+    CU(dev_alloc(ctx, &b->d_args, args.size() * sizeof(args[0])));
     CU(cudaMemcpyAsync(b->d_args, args.data(), args.size() * sizeof(args[0]), cudaMemcpyHostToDevice, st));
-    for (int w = 0; w < 3; w++) {
-        std::vector<int4> tl;
-        for (size_t j = 0; j < b->jobs.size(); j++) {
-            const Job &J = b->jobs[j]->J;
-            for (int iw = 0; iw < J.nw; iw++)
-                for (int j0 = 0; j0 < J.nk[iw]; j0 += kNtOpts[w]) tl.push_back(make_int4((int)j, iw, j0, 0));
+    // tile lists for each block width, written on the device from one offset per (job, frequency)
+    std::vector<int2> row_id;
+    std::vector<int> row_nk;
+    for (size_t j = 0; j < b->jobs.size(); j++) {
+        const Job &J = b->jobs[j]->J;
+        for (int iw = 0; iw < J.nw; iw++) {
+            row_id.push_back(make_int2((int)j, iw));
+            row_nk.push_back(J.nk[iw]);
         }
-        b->ntiles[w] = (int)tl.size();
-        CU(cudaMalloc(&b->d_tiles[w], tl.size() * sizeof(int4)));
-        CU(cudaMemcpyAsync(b->d_tiles[w], tl.data(), tl.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
+    }
+    const size_t nrow = row_id.size();
+    CU(dev_alloc(ctx, &b->d_rows, nrow * (sizeof(int2) + sizeof(int) + 3 * sizeof(long long)) + 8));
+    int2 *d_id = (int2 *)b->d_rows;
+    int *d_nk = (int *)(d_id + nrow);
+    long long *d_first = (long long *)(((uintptr_t)(d_nk + nrow) + 7) & ~(uintptr_t)7);
+    CU(cudaMemcpyAsync(d_id, row_id.data(), nrow * sizeof(int2), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(d_nk, row_nk.data(), nrow * sizeof(int), cudaMemcpyHostToDevice, st));
+    std::vector<long long> first(3 * nrow);
+    for (int w = 0; w < 3; w++) {
+        long long n = 0;
+        for (size_t r = 0; r < nrow; r++) {
+            first[w * nrow + r] = n;
+            n += (row_nk[r] + kNtOpts[w] - 1) / kNtOpts[w];
+        }
+        if (n >= (1LL << 31)) return set_err(ctx, GRT_ERR_UNSUPPORTED, "too many (w,k) tiles for one launch");
+        b->ntiles[w] = (int)n;
+        CU(dev_alloc(ctx, &b->d_tiles[w], n * sizeof(int4)));
+    }
+    CU(cudaMemcpyAsync(d_first, first.data(), 3 * nrow * sizeof(long long), cudaMemcpyHostToDevice, st));
+    for (int w = 0; w < 3; w++) {
+        grt::batch_tiles_kernel<<<(unsigned)nrow, 256, 0, st>>>(d_id, d_nk, d_first + w * nrow, kNtOpts[w],
+                                                                b->d_tiles[w]);
+        CU(cudaGetLastError());
     }
     CU(raise_batch_limits<R>((int)((size_t)b->maxL * sizeof(grt::LayerW<R>))));
     CU(cudaStreamSynchronize(st));
@@ -1232,7 +1372,7 @@ extern "C" int grt_batch_create(grt_ctx *ctx, int n_jobs, const grt_job *jobs, i
     }
     b->prec = jobs[0].opts->precision;
     CU(cudaDeviceGetAttribute(&b->nsm, cudaDevAttrMultiProcessorCount, ctx->device));
-    CU(cudaMalloc(&b->derr, sizeof(unsigned)));
+    CU(dev_alloc(ctx, &b->derr, sizeof(unsigned)));
     CU(cudaMemset(b->derr, 0, sizeof(unsigned)));
     for (auto &s : b->side) CU(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     CU(cudaEventCreate(&b->ev_start));
@@ -1369,14 +1509,15 @@ static int synth(grt_plan *p, const grt_source *src, const double *azimuth, doub
         }
     }
     struct Bufs {
+        grt_ctx *c;
         std::vector<void *> v;
-        ~Bufs() { for (void *q : v) cudaFree(q); }
-    } bufs;
+        ~Bufs() { for (void *q : v) dev_free(c, q); }
+    } bufs{ctx, {}};
     void *dW = nullptr, *dS = nullptr, *dO = nullptr;
-    CU(cudaMalloc(&dW, W.size() * sizeof(R))); bufs.v.push_back(dW);
-    if (!stf.empty()) { CU(cudaMalloc(&dS, stf.size() * sizeof(R))); bufs.v.push_back(dS); }
+    CU(dev_alloc(ctx, &dW, W.size() * sizeof(R))); bufs.v.push_back(dW);
+    if (!stf.empty()) { CU(dev_alloc(ctx, &dS, stf.size() * sizeof(R))); bufs.v.push_back(dS); }
     const size_t nout = (size_t)nd * 3 * N;
-    CU(cudaMalloc(&dO, nout * sizeof(R))); bufs.v.push_back(dO);
+    CU(dev_alloc(ctx, &dO, nout * sizeof(R))); bufs.v.push_back(dO);
     cudaStream_t st = ctx->stream;
     CU(cudaMemcpyAsync(dW, W.data(), W.size() * sizeof(R), cudaMemcpyHostToDevice, st));
     if (dS) CU(cudaMemcpyAsync(dS, stf.data(), stf.size() * sizeof(R), cudaMemcpyHostToDevice, st));
@@ -1401,6 +1542,7 @@ extern "C" int grt_plan_synth(grt_plan *p, const grt_source *src, const double *
     if (!p || !src || !azimuth || !seis) return GRT_ERR_ARG;
     grt_ctx *ctx = p->ctx;
     if (p->J.src == 0) return set_err(ctx, GRT_ERR_UNSUPPORTED, "seismograms need a moment-tensor job");
+    if (!p->J.fsel.empty()) return set_err(ctx, GRT_ERR_UNSUPPORTED, "a frequency-selection plan has spectra only");
     if (src->n_stf < 0 || (src->n_stf > 0 && !src->stf) || src->n_stf > p->J.N)
         return set_err(ctx, GRT_ERR_ARG, "source-time function: 0 <= n_stf <= N samples");
     CU(cudaSetDevice(ctx->device));
@@ -1432,6 +1574,7 @@ extern "C" int grt_plan_write(grt_plan *p, const char *path)
     if (!p || !path) return GRT_ERR_ARG;
     grt_ctx *ctx = p->ctx;
     const Job &J = p->J;
+    if (!J.fsel.empty()) return set_err(ctx, GRT_ERR_UNSUPPORTED, "a frequency-selection plan has spectra only");
     const size_t n = (size_t)p->nd * p->nc * J.N;
     std::vector<float> tr(n);
     CU(cudaSetDevice(ctx->device));
@@ -1458,6 +1601,7 @@ extern "C" int grt_plan_fetch_f32(grt_plan *p, float *traces)
 {
     if (!p || !traces) return GRT_ERR_ARG;
     grt_ctx *ctx = p->ctx;
+    if (!p->J.fsel.empty()) return set_err(ctx, GRT_ERR_UNSUPPORTED, "a frequency-selection plan has spectra only");
     const size_t n = (size_t)p->nd * p->nc * p->J.N;
     CU(cudaSetDevice(ctx->device));
     if (p->prec) {
@@ -1469,6 +1613,23 @@ extern "C" int grt_plan_fetch_f32(grt_plan *p, float *traces)
     CU(cudaMemcpyAsync(traces, p->sig, n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
     CU(cudaStreamSynchronize(ctx->stream));
     return GRT_OK;
+}
+
+extern "C" int grt_host_alloc(size_t bytes, void **ptr)
+{
+    if (!ptr || bytes == 0) return GRT_ERR_ARG;
+    *ptr = nullptr;
+    const cudaError_t e = cudaHostAlloc(ptr, bytes, cudaHostAllocPortable);
+    if (e != cudaSuccess) {
+        *ptr = nullptr;
+        return e == cudaErrorMemoryAllocation ? GRT_ERR_NOMEM : GRT_ERR_CUDA;
+    }
+    return GRT_OK;
+}
+
+extern "C" void grt_host_free(void *ptr)
+{
+    if (ptr) cudaFreeHost(ptr);
 }
 
 extern "C" int grt_batch_fetch_f32(grt_batch *b, int job, float *traces)

@@ -13,4 +13,9 @@ struct grt_ctx {
     std::string err;
     // batch launch shapes picked by the autotuner, by (precision, deepest model)
     std::map<std::pair<int, int>, std::pair<int, int>> tuned;
+    // device blocks released by plans and batches, kept for reuse (by size),
+    // and the blocks handed out from this cache
+    std::multimap<size_t, void *> pool;
+    std::map<void *, size_t> live;
+    size_t pooled = 0, pool_cap = 0;
 };

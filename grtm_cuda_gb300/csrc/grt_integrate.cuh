@@ -559,6 +559,17 @@ __global__ void __launch_bounds__(512) synth_kernel(SynthArgs<R> A)
     ifft_dedamp(x, reinterpret_cast<const C<R> *>(A.tw), A.damp, A.logn, A.out + tr * N);
 }
 
+// Spectra-only plans (a frequency selection): Y[tr][row] = S[tr][row] post[row],
+// the phase, taper and scale of the spectral stage without fill or transform.
+template <typename R>
+__global__ void select_kernel(const R *S, const R *post, R *out, long long n, int nw)
+{
+    const C<R> *s = reinterpret_cast<const C<R> *>(S), *q = reinterpret_cast<const C<R> *>(post);
+    C<R> *y = reinterpret_cast<C<R> *>(out);
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+        y[e] = s[e] * q[e % nw];
+}
+
 template <typename R>
 __global__ void __launch_bounds__(512) spectral_kernel(SpecArgs<R> A)
 {

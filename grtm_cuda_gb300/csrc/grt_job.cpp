@@ -4,6 +4,7 @@
 // the same (w,k) list and the same receiver/source placement.
 #include "grt_job.h"
 
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -133,6 +134,8 @@ int job_setup(Job &J, double dt, int log2n, double t0, double taper, double sigm
     J.fix = fix;
     // green.cu:2065-2080
     J.nw = 1 << (log2n - 1);
+    J.nwf = J.nw;
+    J.fsel.clear();
     J.N = 2 * J.nw;
     const double T = J.N * dt;
     J.df = 1.0 / T;
@@ -193,6 +196,38 @@ int job_setup(Job &J, double dt, int log2n, double t0, double taper, double sigm
         J.nbrow = std::max(J.nbrow, (nk - 1) * J.ks[iw] + 1);
     }
     J.nkw = tot;
+    return kOk;
+}
+
+int job_select(Job &J, int n, const int *sel, std::string &err)
+{
+    if (n < 1 || !sel) { err = "empty frequency selection"; return kErrArg; }
+    if (!J.fsel.empty() || J.nw != J.nwf) { err = "frequencies already selected"; return kErrArg; }
+    std::vector<char> seen(J.nwf, 0);
+    for (int i = 0; i < n; i++) {
+        if (sel[i] < 0 || sel[i] >= J.nwf) { err = "selected frequency out of range (0..N/2-1)"; return kErrArg; }
+        if (seen[sel[i]]) { err = "repeated selected frequency"; return kErrArg; }
+        seen[sel[i]] = 1;
+    }
+    std::vector<int> nk(n), ks(n);
+    std::vector<long long> koff(n);
+    long long tot = 0;
+    J.nkmax = 0;
+    J.nbrow = 0;
+    for (int i = 0; i < n; i++) {
+        nk[i] = J.nk[sel[i]];
+        ks[i] = J.ks[sel[i]];
+        koff[i] = tot;
+        tot += nk[i];
+        J.nkmax = std::max(J.nkmax, nk[i]);
+        J.nbrow = std::max(J.nbrow, (nk[i] - 1) * ks[i] + 1);
+    }
+    J.nk.swap(nk);
+    J.ks.swap(ks);
+    J.koff.swap(koff);
+    J.nkw = tot;
+    J.fsel.assign(sel, sel + n);
+    J.nw = n;
     return kOk;
 }
 

@@ -20,7 +20,9 @@ struct Job {
     int nf1 = 0, nf2 = 0, n_ptam = 0;
     // time / frequency grid (green.cu:2051-2080)
     double dt = 0, t0 = 0, taper = 0;
-    int log2n = 0, nw = 0, N = 0;
+    int log2n = 0, nw = 0, N = 0;                // nw: frequency rows evaluated
+    int nwf = 0;                                 // positive frequencies of the grid (N/2)
+    std::vector<int> fsel;                       // frequency of each row (empty: row = frequency)
     double df = 0, sigma = 0, dk = 0, vmax = 0, vmin = 0;
     // wavenumber grid
     int k_mode = 0, nk_fixed = 0, fix = 0;
@@ -52,6 +54,12 @@ int job_from_layers(int n, const double *ztop, const double *vp, const double *v
 int job_setup(Job &J, double dt, int log2n, double t0, double taper, double sigma_factor, int k_mode,
               int nk_fixed, double dk_override, int fix, std::string &err, const int *nk_custom = nullptr,
               const int *k_stride = nullptr);
+
+// Keep only the frequencies sel[0..n) (distinct, 0 <= sel[i] < N/2, any
+// order) as the job's rows, with their wavenumber grids.
+int job_select(Job &J, int n, const int *sel, std::string &err);
+// frequency index of row iw
+inline int job_freq(const Job &J, int iw) { return J.fsel.empty() ? iw : J.fsel[iw]; }
 
 // Earth-flattening transform of a spherical layered model (the reference's
 // caller-side step, greent.py:13-47 and 65-67); density and Q unchanged.

@@ -655,6 +655,28 @@ __device__ __forceinline__ bool stage_table(const GrtArgs<R> &A, int iw, LayerW<
     return wait ? mbar_wait(sbar, phase, A.err) : true;
 }
 
+// Tile lists written on the device (the host sends one offset per row):
+// row r (a frequency of one job) has ceil(nk_r / nt) tiles from first[r] on.
+// Plans: (frequency, first k); batches: (job, frequency, first k, 0).  One
+// block per row.
+static __global__ void plan_tiles_kernel(const int *nk, const long long *first, int nt, int2 *tiles)
+{
+    const int r = blockIdx.x;
+    const int n = (nk[r] + nt - 1) / nt;
+    int2 *out = tiles + first[r];
+    for (int c = threadIdx.x; c < n; c += blockDim.x) out[c] = make_int2(r, c * nt);
+}
+
+static __global__ void batch_tiles_kernel(const int2 *row_id, const int *row_nk, const long long *first, int nt,
+                                          int4 *tiles)
+{
+    const int r = blockIdx.x;
+    const int2 id = row_id[r];
+    const int n = (row_nk[r] + nt - 1) / nt;
+    int4 *out = tiles + first[r];
+    for (int c = threadIdx.x; c < n; c += blockDim.x) out[c] = make_int4(id.x, id.y, c * nt, 0);
+}
+
 // One job: one block per (frequency, block of kGrtThreads wavenumbers).
 template <typename R>
 __global__ void __launch_bounds__(kGrtThreads, GRT_POINT_MINB) grt_point_kernel(GrtArgs<R> A)

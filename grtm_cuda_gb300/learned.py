@@ -64,6 +64,16 @@ def custom_opts(nk, dk, plain=PLAIN, **over):
     return make_opts(plain["dt"], plain["log2n"], **kw)
 
 
+def spot_opts(nw, dk, spots, k_slice, plain=PLAIN):
+    """The plain grid (step dk) at the judge's spot frequencies alone: a
+    spectra-only plan whose frequency tiles hold nothing but spots.  With the
+    learned plan's k_slice both add a frequency's wavenumbers in the same
+    order, so their difference is the learned grid's own error and not the
+    FP32 rounding of two differently split sums."""
+    return custom_opts(np.full(nw, plain["nk"], np.int32), dk, plain, freq_sel=np.asarray(spots, np.int32),
+                       k_slice=int(k_slice))
+
+
 def layer_features(m):
     """12 statistics of a layered model (dict as from synth): depth of the
     half-space, min/max Vs, max Vp, thickness-weighted mean Vs, Vs of the
@@ -400,10 +410,8 @@ def run_learned(sampler, m, dists, ctx=None, plain=PLAIN, tail_tol=None, spec_to
             excess = sw["tail"] * sw["env"] * w / (tol * sw["env"].max(0)[None, :])
             info["tail_max"] = float(excess.max())
             tail_bad = excess.max(0) > 10.0                                         # per band
-            # plain grid at the spot frequencies only (2 points elsewhere)
-            nk_spot = np.full(nw, 2, np.int32)
-            nk_spot[spot] = nk_plain
-            sp_plan = Plan(ctx, model, custom_opts(nk_spot, dkp, plain), dists)
+            # plain grid at the spot frequencies only (a spectra-only plan)
+            sp_plan = Plan(ctx, model, spot_opts(nw, dkp, spot, plan.report.k_slice, plain), dists)
             sp_plan.execute()
             s_plain = sp_plan.fetch_freqs(spot)
             s_learn = plan.fetch_freqs(spot)
@@ -433,11 +441,13 @@ def run_learned(sampler, m, dists, ctx=None, plain=PLAIN, tail_tol=None, spec_to
 
 
 def run_learned_batch(sampler, models, dists_list, ctx=None, plain=PLAIN, spec_tol=3e-3, autotune=True,
-                      use_stride=True):
+                      use_stride=True, out=None):
     """run_learned for many models at once: one batch (one CUDA graph, one
     GRT launch) on the learned grids, the judge's spot evaluations as a
     second batch, sweeps per model, and the plain grid for any receiver the
-    judge rejects.  Returns (list of float32 traces, info)."""
+    judge rejects.  Returns (list of float32 traces, info); with `out` (one
+    float32 [n_dist, n_cols, N] array per model, e.g. pinned_empty ones) the
+    traces are fetched into those arrays."""
     own = ctx is None
     ctx = ctx or Context()
     try:
@@ -451,15 +461,14 @@ def run_learned_batch(sampler, models, dists_list, ctx=None, plain=PLAIN, spec_t
         b = Batch(ctx, jobs, autotune=autotune)
         t.append(time.perf_counter())
         rep = b.execute()
-        traces = [b.fetch_f32(j) for j in range(len(jobs))]
+        t_exec = time.perf_counter()
+        traces = [b.fetch_f32(j, None if out is None else out[j]) for j in range(len(jobs))]
         t.append(time.perf_counter())
         # judge: spot frequencies on the plain grid (batched), tails by sweep
         spot_jobs, spots = [], []
-        for mo, (nk, st, kmax, gr), d in zip(mods, grids, dists_list):
+        for j, (mo, (nk, st, kmax, gr), d) in enumerate(zip(mods, grids, dists_list)):
             sp = judge_spots(gr["nw"], st)
-            nk_spot = np.full(gr["nw"], 2, np.int32)
-            nk_spot[sp] = plain["nk"]
-            spot_jobs.append((mo, custom_opts(nk_spot, gr["dk"], plain), d))
+            spot_jobs.append((mo, spot_opts(gr["nw"], gr["dk"], sp, b.info(j)[0]["k_slice"], plain), d))
             spots.append(sp)
         tj = [time.perf_counter()]
         sb = Batch(ctx, spot_jobs, autotune=False)
@@ -499,7 +508,8 @@ def run_learned_batch(sampler, models, dists_list, ctx=None, plain=PLAIN, spec_t
                     stride_mean=float(np.mean([g_[1].mean() for g_ in grids])), fallback=fallback,
                     n_fallback=n_fb, ms_batch_gpu=rep.ms_total, ms_batch_grt=rep.ms_grt,
                     gpu_launches=rep.kernel_launches, tune=tune, s_predict=t[1] - t[0], s_build=t[2] - t[1],
-                    s_execute=t[3] - t[2], s_judge=t[4] - t[3], s_fallback=t[5] - t[4], s_total=t[5] - t[0],
+                    s_execute=t[3] - t[2], s_fetch=t[3] - t_exec, s_judge=t[4] - t[3], s_fallback=t[5] - t[4],
+                    s_total=t[5] - t[0],
                     s_judge_parts=dict(spot_build=tj[1] - tj[0], spot_exec=tj[2] - tj[1], sweeps_compare=tj[3] - tj[2]))
         b.close()
         return traces, info

@@ -77,13 +77,19 @@ typedef struct grt_opts {
     const int *k_stride;  /* GRT_K_CUSTOM, optional: per-frequency stride m in 1..64, k_j = j m dk
                            * (N/2 entries; NULL = 1).  FP32 plans (tensor-core sum) need one stride
                            * per aligned block of 64 frequencies. */
+    int n_freq_sel;       /* > 0: evaluate only these positive frequencies (a spectra-only plan: */
+    const int *freq_sel;  /* distinct indices in 0..N/2-1, any order; grt_plan_fetch_freqs reads them,
+                           * traces, synthesis and files are GRT_ERR_UNSUPPORTED).  0 / NULL: all. */
+    int k_slice;          /* FP32 tensor-core sum: wavenumbers per split-K slice, a multiple of 8 (0: chosen
+                           * to fill the GPU).  Plans with one k_slice add each frequency's wavenumbers in
+                           * the same order: their sums agree bit for bit on a common k range. */
 } grt_opts;
 
 typedef struct grt_report {
     int n_layer;          /* after source-interface insertion */
     int s_layer, r_layer;
     double zs, zr;
-    int nw;               /* positive frequencies */
+    int nw;               /* positive frequencies evaluated (N/2, or n_freq_sel) */
     int n_samples;        /* N */
     int n_cols;           /* defined output columns: 15 single force, 20 moment tensor (30 with GRT_FIX_COLS) */
     long long n_wk;       /* (w,k) points evaluated */
@@ -94,14 +100,19 @@ typedef struct grt_report {
     long long h2d_bytes;  /* bytes the plan uploads (layer tables, grids, receivers) */
     long long d2h_bytes;  /* bytes one fetch of the traces downloads */
     int ksum_impl;        /* wavenumber sum: 0 SIMT FP32/FP64, 1 tensor cores (3xTF32) */
+    int k_slice;          /* tensor-core sum: wavenumbers per split-K slice (0 for the SIMT sum) */
 } grt_report;
 
 typedef struct grt_ctx grt_ctx;
 typedef struct grt_plan grt_plan;
 
-/* Contexts own a CUDA stream on one device; not thread-safe. */
+/* Contexts own a CUDA stream on one device and a cache of the device memory
+ * their plans and batches release (reused by the next ones, up to half the
+ * device memory); not thread-safe.  Destroy plans and batches first. */
 GRT_API int grt_create(grt_ctx **ctx, int device);
 GRT_API void grt_destroy(grt_ctx *ctx);
+/* Return the context's cached device memory to the driver. */
+GRT_API void grt_trim(grt_ctx *ctx);
 GRT_API const char *grt_last_error(const grt_ctx *ctx);
 GRT_API const char *grt_status_string(int status);
 
@@ -116,8 +127,14 @@ GRT_API int grt_plan_execute(grt_plan *plan, grt_report *report);
 GRT_API int grt_plan_fetch(grt_plan *plan, double *traces, double *spectra);
 /* traces as float32 [n_dist][n_cols][N] (FP32 plans: their working precision) */
 GRT_API int grt_plan_fetch_f32(grt_plan *plan, float *traces);
+/* Page-locked host memory (cudaHostAlloc) for fetch destinations: copies into
+ * it run at the host link's full rate instead of through a staging buffer.
+ * Allocate once and reuse: pinning is slow.  No counterpart in the reference. */
+GRT_API int grt_host_alloc(size_t bytes, void **ptr);
+GRT_API void grt_host_free(void *ptr);
 /* spectra at selected frequency indices (0..N-1) only: [n_dist][n_cols][n_freq]
- * complex as (re, im) doubles */
+ * complex as (re, im) doubles.  A plan made with opts.freq_sel answers for
+ * its selected frequencies only (others: GRT_ERR_ARG). */
 GRT_API int grt_plan_fetch_freqs(grt_plan *plan, int n_freq, const int *freq_idx, double *spectra);
 GRT_API int grt_plan_info(const grt_plan *plan, grt_report *report);
 GRT_API void grt_plan_destroy(grt_plan *plan);
@@ -139,8 +156,9 @@ GRT_API int grt_grid(const grt_model *model, const grt_opts *opts, grt_report *r
  *   alias_out  with S_q^(s) = s dk sum_{j = 0 mod s, j dk < k_c} K_q J0(k r_b):
  *              [0] = max_q |S_q^(1)|, [s] = max_q |S_q^(2^s) - S_q^(1)| (s = 1..5),
  *              the spatial aliasing of a 2^s times coarser step at r_b.
- * FP32 kernel.  No counterpart in the reference (its k_max is the fixed rule
- * of cal_kmax, green.cu:108-162). */
+ * FP32 kernel; layer tables for the listed frequencies only (opts.freq_sel
+ * must be empty).  No counterpart in the reference (its k_max is the fixed
+ * rule of cal_kmax, green.cu:108-162). */
 GRT_API int grt_sweep_kmax(grt_ctx *ctx, const grt_model *model, const grt_opts *opts, int n_freq,
                            const int *freq_idx, int n_band, const double *band_r, double tol,
                            const double *tol_abs, const double *k_judge, double *kmax_out, double *tail_out,
@@ -265,7 +283,8 @@ GRT_API int grt_run(grt_ctx *ctx, const grt_model *model, const grt_opts *opts, 
  * capture.  Calls share the arrays: calls that overlap on the GPU, or come
  * from several host threads at once, race.  Runs on the default stream of
  * `device`; traces: host [n_dist][n_cols][N] doubles.
- * Reference-rule and fixed grids only (GRT_K_CUSTOM: GRT_ERR_UNSUPPORTED).
+ * Reference-rule and fixed grids of all frequencies only (GRT_K_CUSTOM or a
+ * frequency selection: GRT_ERR_UNSUPPORTED).
  * No counterpart in the reference. */
 GRT_API int grt_run_noalloc(int device, const grt_model *model, const grt_opts *opts, int n_dist,
                             const double *dist, double *traces);

@@ -17,7 +17,9 @@ def main():
     seeds = [float(m["hs"]) for m, _ in work]
     bench.barrier(td)
     t = bench.allmax(td, 1.0 + rank)
-    print(json.dumps({"rank": rank, "ws": ws, "max": t, "hs": seeds}), flush=True)
+    # one write per line: the two ranks share the pipe
+    sys.stdout.flush()
+    os.write(1, (json.dumps({"rank": rank, "ws": ws, "max": t, "hs": seeds}) + "\n").encode())
     bench.barrier(td)
 
 

@@ -3,6 +3,7 @@ collective; ranks run their own seeded models and only the step time is
 max-reduced."""
 import json
 import os
+import re
 import subprocess
 import sys
 
@@ -18,7 +19,7 @@ def test_two_rank_replicas():
            "--master-addr", "127.0.0.1", "--master-port", "29517", os.path.join(HERE, "dist_child.py")]
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=240, env=env)
     assert r.returncode == 0, r.stderr[-2000:]
-    rows = [json.loads(l) for l in r.stdout.splitlines() if l.startswith("{")]
+    rows = [json.loads(x) for x in re.findall(r"\{[^{}]*\}", r.stdout)]
     assert sorted(x["rank"] for x in rows) == [0, 1]
     assert all(x["ws"] == 2 and x["max"] == 2.0 for x in rows)
     # each rank draws its own models

@@ -258,6 +258,7 @@ def test_learned_path_gain_and_accuracy(ctx):
     tl, info = learned.run_learned(s, m, d, ctx=ctx)
     err = np.sqrt(np.sum((tl - t64) ** 2, axis=(1, 2)) / np.sum(t64 ** 2, axis=(1, 2)))
     assert info["nkw_plain"] / info["nkw_learned"] >= 1.15
+    assert info["fallback"] == []                      # a sound grid passes its judge
     assert np.sqrt(np.sum((tl - t64) ** 2) / np.sum(t64 ** 2)) <= 1e-3
     assert np.median(err) <= 1e-3
 
