@@ -35,7 +35,7 @@ struct grt_plan {
     int rt = 128, jt = 1;
     int use_tc = 0, nsplit = 1, kslice = 0;   // tensor-core wavenumber sum and its split-K
     int kslice_req = 0;                       // requested k per slice (0: chosen here)
-    int bt_rows = 0;                          // > 0: Bessel table tiled by 16 receivers (unit strides)
+    int bt_rows = 0;                          // > 0: Bessel table tiled by 32 receivers (unit strides)
     int cols = 0;                             // output column layout (grt::ColKind)
     void *P = nullptr;                        // split-K partial sums
     float *Kt = nullptr;                      // coefficients in GEMM operand layout
@@ -227,6 +227,12 @@ static int col_count(int kind)
 {
     return kind == grt::kColTensorFix ? grt::kTensorFixNC : (kind == grt::kColTensor ? grt::kTensorNC : grt::kSingleNC);
 }
+// operand tiles per stage block of the tensor-core sum (coefficient columns it reads)
+static int tc_tiles(int kind)
+{
+    constexpr grt::TcPlan ts = grt::make_tcplan<grt::kColSingle>(), tt = grt::make_tcplan<grt::kColTensor>();
+    return kind == grt::kColTensor ? tt.nqu : (kind == grt::kColTensorFix ? 0 : ts.nqu);
+}
 static int coef_count(int kind)
 {
     return kind == grt::kColTensorFix ? 2 * grt::QT_N : (kind == grt::kColTensor ? grt::QT_N : grt::QS_N);
@@ -283,12 +289,13 @@ static int upload(grt_plan *p)
     if (ntl >= (1LL << 31)) return set_err(ctx, GRT_ERR_UNSUPPORTED, "too many (w,k) tiles for one launch");
     p->ntiles = (int)ntl;
     const size_t szK = (size_t)p->nq * J.nkw * 2 * sizeof(R);
-    // the tensor-core sum reads the Bessel table in receiver tiles of 16 when
+    // the tensor-core sum reads the Bessel table in receiver tiles of 32 when
     // every frequency has a unit stride (a stage's rows are then contiguous)
     bool unit = true;
     for (int m : J.ks) unit = unit && m == 1;
     if (p->use_tc && unit) p->bt_rows = (J.nbrow + grt::tc::kKT - 1) / grt::tc::kKT * grt::tc::kKT;
-    const size_t szB = p->bt_rows ? (size_t)((p->nd + 15) / 16) * 16 * p->bt_rows * grt::NBASIS * sizeof(R)
+    const size_t szB = p->bt_rows ? (size_t)((p->nd + grt::kBesselTile - 1) / grt::kBesselTile) * grt::kBesselTile *
+                                        p->bt_rows * grt::NBASIS * sizeof(R)
                                   : (size_t)J.nbrow * grt::NBASIS * p->nd * sizeof(R);
     const size_t ntr = (size_t)p->nd * p->nc;
     CU(dev_alloc(ctx, &p->tab, tab.size() * sizeof(tab[0])));
@@ -311,10 +318,12 @@ static int upload(grt_plan *p)
     CU(dev_alloc(ctx, &p->spec, ntr * (sel ? J.nw : J.N) * 2 * sizeof(R)));
     CU(dev_alloc(ctx, &p->derr, sizeof(unsigned)));
     if (p->use_tc) {
-        // split the k range so that the CTA count fills whole waves of the SMs (one CTA per SM)
+        // split the k range so that the CTA count (both column groups) fills whole
+        // waves of the SMs (one CTA per SM)
         int nsm = 148;
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device);
-        const long long tiles = (long long)((J.nw + grt::tc::kW - 1) / grt::tc::kW) * ((p->nd + grt::tc::kN - 1) / grt::tc::kN);
+        const long long tiles =
+            2LL * ((J.nw + grt::tc::kW - 1) / grt::tc::kW) * ((p->nd + grt::tc::kN - 1) / grt::tc::kN);
         int best = 1;
         double best_cost = 1e30;
         const int maxs = std::max(1, std::min(64, J.nkmax / (8 * grt::tc::kKT)));
@@ -332,7 +341,8 @@ static int upload(grt_plan *p)
             p->nsplit = (J.nkmax + p->kslice - 1) / p->kslice;
         }
         p->rep.k_slice = p->kslice;
-        CU(dev_alloc(ctx, &p->P, (size_t)best * ntr * J.nw * 2 * sizeof(float)));
+        // partial sums of every (k slice, column group)
+        CU(dev_alloc(ctx, &p->P, (size_t)p->nsplit * 2 * ntr * J.nw * 2 * sizeof(float)));
         // operand blocks of (frequency tile of 64, k stage of 8): nq x (hi, lo) x 1024 floats each
         const int nwt = (J.nw + grt::tc::kW - 1) / grt::tc::kW;
         std::vector<long long> base(nwt);
@@ -345,7 +355,7 @@ static int upload(grt_plan *p)
             for (int i = t * grt::tc::kW; i < std::min(J.nw, (t + 1) * grt::tc::kW); i++)
                 if (J.nk[i] != ns * grt::tc::kKT) padded = true;
             base[t] = tot;
-            tot += (long long)ns * p->nq * 2 * grt::tc::kM * grt::tc::kKT;
+            tot += (long long)ns * tc_tiles(p->cols) * 2 * grt::tc::kM * grt::tc::kKT;
         }
         CU(dev_alloc(ctx, &p->Kt, (size_t)tot * sizeof(float)));
         CU(dev_alloc(ctx, &p->kt_base, nwt * sizeof(long long)));
@@ -435,6 +445,22 @@ extern "C" int grt_plan_create(grt_ctx *ctx, const grt_model *m, const grt_opts 
     return GRT_OK;
 }
 
+template <int SRC>
+static cudaError_t raise_tc_limits()
+{
+    return raise_smem_limit(grt::ksum_tc_kernel<SRC>, grt::tc::smem_bytes<SRC>());
+}
+
+// one launch for both column groups: 2 CTAs per (frequency tile, receiver tile, k slice)
+template <int SRC>
+static cudaError_t launch_tc_groups(const grt::KsumTcArgs<float> &T, unsigned grid, cudaStream_t st)
+{
+    cudaError_t e = raise_tc_limits<SRC>();
+    if (e != cudaSuccess) return e;
+    grt::ksum_tc_kernel<SRC><<<2 * grid, grt::tc::kThreads, grt::tc::smem_bytes<SRC>(), st>>>(T);
+    return cudaGetLastError();
+}
+
 // tensor-core wavenumber sum (FP32 path): split-K partial sums, then TwoSum reduction
 static int launch_ksum_tc(grt_plan *p, cudaStream_t st, int &launches)
 {
@@ -460,24 +486,13 @@ static int launch_ksum_tc(grt_plan *p, cudaStream_t st, int &launches)
     T.err = p->derr;
     const int nwt = (J.nw + grt::tc::kW - 1) / grt::tc::kW, nrt = (p->nd + grt::tc::kN - 1) / grt::tc::kN;
     const unsigned grid = (unsigned)(nwt * nrt * p->nsplit);
-    if (p->cols == grt::kColSingle) {
-        const int sm = grt::tc::smem_bytes<grt::kColSingle>();
-        CU(raise_smem_limit(grt::ksum_tc_kernel<grt::kColSingle>, sm));
-        grt::ksum_tc_kernel<grt::kColSingle><<<grid, grt::tc::kThreads, sm, st>>>(T);
-    } else if (p->cols == grt::kColSingleFix) {
-        const int sm = grt::tc::smem_bytes<grt::kColSingleFix>();
-        CU(raise_smem_limit(grt::ksum_tc_kernel<grt::kColSingleFix>, sm));
-        grt::ksum_tc_kernel<grt::kColSingleFix><<<grid, grt::tc::kThreads, sm, st>>>(T);
-    } else {
-        const int sm = grt::tc::smem_bytes<grt::kColTensor>();
-        CU(raise_smem_limit(grt::ksum_tc_kernel<grt::kColTensor>, sm));
-        grt::ksum_tc_kernel<grt::kColTensor><<<grid, grt::tc::kThreads, sm, st>>>(T);
-    }
+    if (p->cols == grt::kColSingle) CU(launch_tc_groups<grt::kColSingle>(T, grid, st));
+    else if (p->cols == grt::kColSingleFix) CU(launch_tc_groups<grt::kColSingleFix>(T, grid, st));
+    else CU(launch_tc_groups<grt::kColTensor>(T, grid, st));
     launches++;
-    CU(cudaGetLastError());
     const long long n = (long long)p->nd * p->nc * J.nw * 2;
     grt::ksum_tc_reduce_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>((const float *)p->P, (float *)p->S, n,
-                                                                             p->nsplit);
+                                                                             2 * p->nsplit);
     launches++;
     CU(cudaGetLastError());
     return GRT_OK;
@@ -506,6 +521,7 @@ static grt::GrtArgs<R> grt_args(const grt_plan *p)
     A.err = p->derr;
     A.Kt = p->use_tc ? p->Kt : nullptr;
     A.kt_base = p->kt_base;
+    A.nqt = tc_tiles(p->cols);
     return A;
 }
 
@@ -1333,9 +1349,9 @@ static int batch_build(grt_batch *b, int autotune)
     for (grt_plan *p : b->jobs) {
         CU(raise_smem_limit(grt::spectral_kernel<R>, (int)((size_t)p->J.N * sizeof(grt::C<R>))));
         if (p->use_tc) {
-            CU(raise_smem_limit(grt::ksum_tc_kernel<grt::kColSingle>, grt::tc::smem_bytes<grt::kColSingle>()));
-            CU(raise_smem_limit(grt::ksum_tc_kernel<grt::kColSingleFix>, grt::tc::smem_bytes<grt::kColSingleFix>()));
-            CU(raise_smem_limit(grt::ksum_tc_kernel<grt::kColTensor>, grt::tc::smem_bytes<grt::kColTensor>()));
+            CU(raise_tc_limits<grt::kColSingle>());
+            CU(raise_tc_limits<grt::kColSingleFix>());
+            CU(raise_tc_limits<grt::kColTensor>());
         }
     }
     CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));

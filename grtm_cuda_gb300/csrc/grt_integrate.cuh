@@ -153,9 +153,14 @@ __device__ __forceinline__ void bessel_big_x(double x, float v[NBASIS], bool exa
 // tile_rows = 0: layout B[j][b][r]; tile_rows > 0: receiver tiles of 16,
 // B[r / 16][j][b][r % 16] with tile_rows rows per tile (a stage of the
 // tensor-core sum then reads 8 consecutive rows as one contiguous block)
+// Bessel table layouts: [row][basis][receiver], or tiled for the tensor-core
+// sum, [receiver / 32][row][basis][32] with the receivers of row j permuted by
+// r ^ 8 (j & 3) (so that a warp's reads of 8 receivers x 4 rows hit 32 banks)
+constexpr int kBesselTile = 32;
 __device__ __forceinline__ long long btab_index(int j, int b, int r, int nr, int tile_rows)
 {
-    if (tile_rows > 0) return (((long long)(r >> 4) * tile_rows + j) * NBASIS + b) * 16 + (r & 15);
+    if (tile_rows > 0)
+        return (((long long)(r >> 5) * tile_rows + j) * NBASIS + b) * kBesselTile + ((r & 31) ^ ((j & 3) << 3));
     return ((long long)j * NBASIS + b) * nr + r;
 }
 
@@ -358,6 +363,72 @@ template <> struct Cols<kColTensorFix> {
     __device__ static constexpr Term term(int i) { return kTensorFixTerms[i]; }
     __device__ static constexpr int col(int i) { return kTensorFixCol[i]; }
 };
+
+// ---------------------------------------------------------------- tensor-core plan
+// How the tensor-core wavenumber sum divides a column layout: the coefficient
+// columns q that feed some pair (the others are neither stored for it nor
+// read), dealt into two groups of about equal pair counts, largest first (one
+// CTA per group: the accumulators of half of the pairs for 32 receivers fit
+// in tensor memory), and the operand tiles of a stage block ordered group by
+// group, q by q, so that a group's tiles are one contiguous copy.
+struct TcPlan {
+    int nqu;                    // coefficient columns stored for the tensor cores
+    int qslot[16];              // operand tile of column q in a stage block (-1: not stored)
+    int gq0[2], gnq[2];         // first tile and number of tiles of each group
+    int gnp[2];                 // pairs of each group
+    int gpair[2][32];           // group-local slot -> pair (slots in tile order)
+    int pslot[40], pgrp[40];    // pair -> group-local slot, group
+    int tfirst[16], tcount[16]; // per tile: first group-local slot and number of its pairs
+};
+
+#pragma nv_diagnostic push
+#pragma nv_diag_suppress 20091
+template <int SRC>
+__host__ __device__ constexpr TcPlan make_tcplan()
+{
+    static_assert(SRC == kColSingle || SRC == kColTensor || SRC == kColSingleFix, "tensor-core layouts only");
+    constexpr int NQ = Cols<SRC>::NQ, NP = Cols<SRC>::NP;
+    auto pair_q = [](int p) { return SRC == kColTensor ? kTensorPairs[p].q : kSinglePairs[p].q; };
+    TcPlan t{};
+    int cnt[16] = {}, grp[16] = {};
+    for (int q = 0; q < 16; q++) {
+        grp[q] = -1;
+        t.qslot[q] = -1;
+    }
+    for (int p = 0; p < NP; p++) cnt[pair_q(p)]++;
+    int load[2] = {0, 0};
+    for (int it = 0; it < NQ; it++) {
+        int best = -1;
+        for (int q = 0; q < NQ; q++)
+            if (grp[q] < 0 && cnt[q] > 0 && (best < 0 || cnt[q] > cnt[best])) best = q;
+        if (best < 0) break;
+        const int g = load[1] < load[0] ? 1 : 0;
+        grp[best] = g;
+        load[g] += cnt[best];
+    }
+    int pos = 0;
+    for (int g = 0; g < 2; g++) {
+        t.gq0[g] = pos;
+        for (int q = 0; q < NQ; q++) {
+            if (grp[q] != g) continue;
+            t.qslot[q] = pos;
+            t.tfirst[pos] = t.gnp[g];
+            t.tcount[pos] = cnt[q];
+            for (int p = 0; p < NP; p++)
+                if (pair_q(p) == q) {
+                    t.gpair[g][t.gnp[g]] = p;
+                    t.pslot[p] = t.gnp[g];
+                    t.pgrp[p] = g;
+                    t.gnp[g]++;
+                }
+            pos++;
+            t.gnq[g]++;
+        }
+    }
+    t.nqu = pos;
+    return t;
+}
+#pragma nv_diagnostic pop
 
 // error-free sum s + x = hi + lo (Knuth TwoSum)
 template <typename R> __device__ __forceinline__ void two_sum_acc(R &hi, R &lo, R x)

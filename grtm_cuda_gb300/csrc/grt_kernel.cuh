@@ -23,6 +23,7 @@
 // TMA bulk copy (cp.async.bulk) completing on an mbarrier.
 #pragma once
 #include "grt_cplx.cuh"
+#include "grt_integrate.cuh"
 #include "grt_types.h"
 
 namespace grt {
@@ -270,19 +271,24 @@ __device__ __forceinline__ KOut make_kout(const GrtArgs<R> &A, int iw, int j)
     KOut o{A.koff[iw] + j, nullptr, 0u, 0u};
     if (sizeof(R) == 4 && A.Kt) {
         const int wl = iw % (kTileRows / 2);
-        o.blk = A.Kt + A.kt_base[iw / (kTileRows / 2)] + (long long)(j / kTileK) * A.nq * 2 * (kTileRows * kTileK);
+        o.blk = A.Kt + A.kt_base[iw / (kTileRows / 2)] + (long long)(j / kTileK) * A.nqt * 2 * (kTileRows * kTileK);
         o.ore = kt_tile_off(wl, j % kTileK) / 4;
         o.oim = kt_tile_off(kTileRows / 2 + wl, j % kTileK) / 4;
     }
     return o;
 }
 
-template <typename R>
+// SRCK: the job's source kind (kSingle / kTensor), which fixes the tensor-core
+// tile of each coefficient column (make_tcplan; columns no pair reads are not stored)
+template <int SRCK, typename R>
 __device__ __forceinline__ void store_q(const GrtArgs<R> &A, int q, const KOut &o, C<R> v)
 {
     if (sizeof(R) == 4 && o.blk) {
-        // TF32 hi / lo words of the 3xTF32 product, [q][hi|lo] tiles of 1024 floats
-        float *t = o.blk + q * 2 * (kTileRows * kTileK);
+        constexpr TcPlan tp = make_tcplan<SRCK == kTensor ? kColTensor : kColSingle>();
+        const int slot = q < 16 ? tp.qslot[q] : -1;
+        if (slot < 0) return;
+        // TF32 hi / lo words of the 3xTF32 product, [tile][hi|lo] tiles of 1024 floats
+        float *t = o.blk + slot * 2 * (kTileRows * kTileK);
         const float x = (float)v.x, y = (float)v.y;
         const float xh = tf32_rna(x), yh = tf32_rna(y);
         t[o.ore] = xh;
@@ -577,18 +583,18 @@ __device__ __forceinline__ void grt_point(const GrtArgs<R> &A, const LayerW<R> *
         C<R> a00, a01, a10, a11;
         mv2(y1, g0a, g0b, &a00, &a01);
         mv2(y1, g1a, g1b, &a10, &a11);
-        store_q(A, QS_B1, out, y0 * gsh);
-        store_q(A, QS_A00, out, a00);
-        store_q(A, QS_A01, out, a01);
-        store_q(A, QS_A10, out, a10);
-        store_q(A, QS_A11, out, a11);
+        store_q<kSingle>(A, QS_B1, out, y0 * gsh);
+        store_q<kSingle>(A, QS_A00, out, a00);
+        store_q<kSingle>(A, QS_A01, out, a01);
+        store_q<kSingle>(A, QS_A10, out, a10);
+        store_q<kSingle>(A, QS_A11, out, a11);
         mv2(y1t, g0a, g0b, &a00, &a01);
         mv2(y1t, g1a, g1b, &a10, &a11);
-        store_q(A, QS_B1T, out, y0t * gsh);
-        store_q(A, QS_A0T0, out, a00);
-        store_q(A, QS_A0T1, out, a01);
-        store_q(A, QS_A1T0, out, a10);
-        store_q(A, QS_A1T1, out, a11);
+        store_q<kSingle>(A, QS_B1T, out, y0t * gsh);
+        store_q<kSingle>(A, QS_A0T0, out, a00);
+        store_q<kSingle>(A, QS_A0T1, out, a01);
+        store_q<kSingle>(A, QS_A1T0, out, a10);
+        store_q<kSingle>(A, QS_A1T1, out, a11);
     } else {
         // s2 = k f1, s1 = -1/(2 mu) G^-1 e0, s0 = H^-1 (alpha', beta')
         C<R> s2a = f1a * k, s2b = f1b * k;
@@ -605,29 +611,29 @@ __device__ __forceinline__ void grt_point(const GrtArgs<R> &A, const LayerW<R> *
         C<R> shf = up ? fu : fd - R(1);
         C<R> h1 = shf * S.v * ssh, h2 = shf * k * ssh;
         C<R> v0, v1;
-        store_q(A, QT_B1, out, y0 * h1);
-        store_q(A, QT_B2, out, y0 * h2);
+        store_q<kTensor>(A, QT_B1, out, y0 * h1);
+        store_q<kTensor>(A, QT_B2, out, y0 * h2);
         mv2(y1, q0a, q0b, &v0, &v1);
-        store_q(A, QT_A00, out, v0);
-        store_q(A, QT_A01, out, v1);
+        store_q<kTensor>(A, QT_A00, out, v0);
+        store_q<kTensor>(A, QT_A01, out, v1);
         mv2(y1, q1a, q1b, &v0, &v1);
-        store_q(A, QT_A10, out, v0);
-        store_q(A, QT_A11, out, v1);
+        store_q<kTensor>(A, QT_A10, out, v0);
+        store_q<kTensor>(A, QT_A11, out, v1);
         mv2(y1, q2a, q2b, &v0, &v1);
-        store_q(A, QT_A20, out, v0);
-        store_q(A, QT_A21, out, v1);
+        store_q<kTensor>(A, QT_A20, out, v0);
+        store_q<kTensor>(A, QT_A21, out, v1);
         if (A.nq > QT_N) {
-            store_q(A, QT_N + QT_B1, out, y0t * h1);
-            store_q(A, QT_N + QT_B2, out, y0t * h2);
+            store_q<kTensor>(A, QT_N + QT_B1, out, y0t * h1);
+            store_q<kTensor>(A, QT_N + QT_B2, out, y0t * h2);
             mv2(y1t, q0a, q0b, &v0, &v1);
-            store_q(A, QT_N + QT_A00, out, v0);
-            store_q(A, QT_N + QT_A01, out, v1);
+            store_q<kTensor>(A, QT_N + QT_A00, out, v0);
+            store_q<kTensor>(A, QT_N + QT_A01, out, v1);
             mv2(y1t, q1a, q1b, &v0, &v1);
-            store_q(A, QT_N + QT_A10, out, v0);
-            store_q(A, QT_N + QT_A11, out, v1);
+            store_q<kTensor>(A, QT_N + QT_A10, out, v0);
+            store_q<kTensor>(A, QT_N + QT_A11, out, v1);
             mv2(y1t, q2a, q2b, &v0, &v1);
-            store_q(A, QT_N + QT_A20, out, v0);
-            store_q(A, QT_N + QT_A21, out, v1);
+            store_q<kTensor>(A, QT_N + QT_A20, out, v0);
+            store_q<kTensor>(A, QT_N + QT_A21, out, v1);
         }
     }
 }

@@ -7,25 +7,36 @@
 // the terms that share a pair differ only by a receiver-dependent factor,
 // applied when the accumulators are drained.  The pairs are grouped by q, so
 // that one MMA multiplies the coefficient tile of q by the Bessel operands of
-// all its pairs at once (N = 16 receivers x pairs of q): each stage reads
-// every coefficient tile from shared memory three times (3xTF32) instead of
-// three times per term.  A CTA owns 64 frequencies (M = 128 rows: real parts
-// in rows 0-63, imaginary parts in rows 64-127), 16 receivers and a slice of
-// the k range (split-K); the accumulators of all pairs live in tensor memory
-// (pairs x 16 columns).
+// all its pairs at once (N = 32 receivers x pairs of q).
+//
+// Work division (make_tcplan): the coefficient columns are dealt into two
+// groups of about equal pair counts (even and odd CTAs of one launch); a CTA
+// owns 64 frequencies (M = 128 rows: real parts in rows 0-63, imaginary
+// parts in rows 64-127), 32 receivers, one group and a slice of the k range
+// (split-K).  The accumulators of the group's pairs live in tensor memory
+// (pairs x 32 columns).  Halving the pairs per CTA doubles the receivers an
+// operand tile is multiplied with: shared-memory traffic per multiply-add
+// (operand copies, tensor-core reads, Bessel-operand stores), the limit of the
+// earlier 16-receiver form, falls by 40 %, and a stage shrinks enough for
+// three of them to fit.
 //
 // Precision: 3xTF32 -- each FP32 operand x is split into hi = tf32(x) and
 // lo = tf32(x - hi) and the product is hi*hi + hi*lo + lo*hi with FP32
 // accumulation (about 2^-21 relative per product).  Partial sums of the k
-// slices are added with TwoSum by ksum_tc_reduce_kernel.
+// slices and of the two groups are added with TwoSum by ksum_tc_reduce_kernel.
 //
-// Roles (160 threads): warps 0-3 produce operand tiles in shared memory
-// (canonical K-major layout, no swizzle: 8-row x 16-byte core matrices) and
-// drain the accumulators at the end; warp 4 allocates tensor memory and one
-// of its threads issues tcgen05.mma and tcgen05.commit.  Two pipeline stages,
-// each guarded by a "full" and an "empty" mbarrier.  Every wait is bounded:
-// on timeout the CTA records an error, skips to the end, and still frees its
-// tensor memory.
+// Roles (320 threads): warps 0-7 produce the Bessel operand tiles in shared
+// memory (canonical K-major layout, no swizzle: 8-row x 16-byte core
+// matrices), one (receiver, k) of a stage per thread, and drain the
+// accumulators at the end (warps w and w + 4 share a quarter of the
+// tensor-memory lanes and split the output columns); one thread of warp 8
+// issues the bulk copies of the coefficient tiles and raw Bessel rows up to
+// three stages ahead; warp 9 allocates tensor memory and one of its threads
+// issues tcgen05.mma and tcgen05.commit.  Each stage is guarded by "full"
+// (producers), "land" (coefficient copy), "raw" (Bessel copy) and "empty"
+// (MMAs done) mbarriers.  Every wait is bounded: on timeout the CTA records
+// an error, skips to the end, waits (bounded) for its copies in flight and
+// still frees its tensor memory.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -39,50 +50,41 @@ namespace tc {
 
 constexpr int kM = 128;        // rows: 64 frequencies x (re, im)
 constexpr int kW = 64;         // frequencies per CTA
-constexpr int kN = 16;         // receivers per CTA
+constexpr int kN = 32;         // receivers per CTA
 constexpr int kKT = 8;         // k per stage = one tf32 MMA K
-constexpr int kStages = 2;
-constexpr int kProducers = 128;
-constexpr int kThreads = kProducers + 32;
+constexpr int kStages = 3;
+constexpr int kProdWarps = 8;  // 32 receivers x 8 k per stage, one per thread
+constexpr int kProducers = 32 * kProdWarps;
+constexpr int kCopyWarp = kProdWarps, kMmaWarp = kProdWarps + 1;
+constexpr int kThreads = kProducers + 64;
 constexpr int kCoreBytes = 128;                      // 8 rows x 16 bytes
 constexpr int kATileBytes = (kM / 8) * (kKT / 4) * kCoreBytes;   // 4096: one q, one split
-constexpr int kBTileBytes = (kN / 8) * (kKT / 4) * kCoreBytes;   // 512: one term, one split
+constexpr int kBTileBytes = (kN / 8) * (kKT / 4) * kCoreBytes;   // 1024: one pair, one split
+constexpr int kRawBytes = kKT * NBASIS * kN * 4;                 // raw Bessel rows of a stage
 constexpr uint32_t kTmemCols = 512;
+static_assert(kN == kBesselTile, "a CTA's receivers are one tile of the Bessel table");
+static_assert(kProducers == kN * kKT, "one producer per (receiver, k) of a stage");
 
-template <int SRC> struct TcCfg {
-    static constexpr int NQ = Cols<SRC>::NQ, NC = Cols<SRC>::NC, NP = Cols<SRC>::NP;
+// one group of a column layout's tensor-core plan
+template <int SRC, int GRP> struct TcGroup {
+    static constexpr TcPlan P = make_tcplan<SRC>();
+    static constexpr int NQ = P.gnq[GRP];     // operand tiles (coefficient columns)
+    static constexpr int NP = P.gnp[GRP];     // pairs
+    static constexpr int Q0 = P.gq0[GRP];     // first tile in a stage block
+    static constexpr int NQU = P.nqu;         // tiles in a stage block (both groups)
+    static constexpr int kABytes = NQ * 2 * kATileBytes;
+    static constexpr int kBBytes = NP * 2 * kBTileBytes;
+    static constexpr int kStageBytes = kABytes + kBBytes + kRawBytes;
+    static_assert(NP * kN <= (int)kTmemCols, "accumulators exceed tensor memory");
+    static_assert(kStageBytes % 1024 == 0, "stages stay 1024-byte aligned");
 };
 
-// the pairs in order of their coefficient column q: slot[p] is pair p's
-// position, first[q] / count[q] the run of q's pairs
-template <int SRC> struct PairGroups {
-    int order[32], slot[32], first[16], count[16];
-};
-template <int SRC> constexpr PairGroups<SRC> make_groups()
+template <int SRC> constexpr int smem_bytes()
 {
-    PairGroups<SRC> g{};
-    int n = 0;
-    for (int q = 0; q < Cols<SRC>::NQ; q++) {
-        g.first[q] = n;
-        g.count[q] = 0;
-        for (int p = 0; p < Cols<SRC>::NP; p++)
-            if (Cols<SRC>::pair(p).q == q) {
-                g.order[n] = p;
-                g.slot[p] = n;
-                n++;
-                g.count[q]++;
-            }
-    }
-    return g;
+    return kStages * (TcGroup<SRC, 1>::kStageBytes > TcGroup<SRC, 0>::kStageBytes ? TcGroup<SRC, 1>::kStageBytes
+                                                                                  : TcGroup<SRC, 0>::kStageBytes) +
+           1024;
 }
-
-template <int SRC> constexpr int stage_bytes()
-{
-    return TcCfg<SRC>::NQ * 2 * kATileBytes + TcCfg<SRC>::NP * 2 * kBTileBytes;
-}
-// raw Bessel rows of one stage: 8 rows x NBASIS x 16 receivers (tiled table)
-constexpr int kRawBytes = kKT * NBASIS * kN * 4;
-template <int SRC> constexpr int smem_bytes() { return kStages * (stage_bytes<SRC>() + kRawBytes) + 1024; }
 
 static_assert(kKT == kTileK && kM == kTileRows, "tile shape shared with the GRT kernel");
 __device__ __forceinline__ uint32_t tile_off(int row, int k) { return kt_tile_off(row, k); }
@@ -116,6 +118,17 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar)
 {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+// bulk copy global -> shared, completion on an mbarrier (16-byte aligned, size a multiple of 16)
+__device__ __forceinline__ void bulk_copy(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
 // bounded wait; false after 2^22 polls (a stage takes about a microsecond)
 __device__ __forceinline__ bool mbar_wait_b(uint32_t bar, uint32_t parity)
 {
@@ -148,6 +161,21 @@ __device__ __forceinline__ void mma_commit(uint32_t bar)
                  : "memory");
 }
 
+// the Bessel basis functions a group uses, as a bit mask (evaluated at compile time)
+#pragma nv_diagnostic push
+#pragma nv_diag_suppress 20091
+template <int SRC, int GRP> __host__ __device__ constexpr unsigned group_basis_mask()
+{
+    const TcPlan T = make_tcplan<SRC>();
+    unsigned m = 0;
+    for (int s = 0; s < T.gnp[GRP]; s++) {
+        const int p = T.gpair[GRP][s];
+        m |= 1u << (SRC == kColTensor ? kTensorPairs[p].b : kSinglePairs[p].b);
+    }
+    return m;
+}
+#pragma nv_diagnostic pop
+
 }  // namespace tc
 
 template <typename R>
@@ -155,34 +183,35 @@ struct KsumTcArgs {
     const float *Kt;         // operand blocks written by the GRT kernel (see GrtArgs::Kt)
     const long long *kt_base;
     const float *B;          // [nbrow][NBASIS][nr], row i at k = i dk; or tiled (bt_rows > 0)
-    int bt_rows;             // > 0: B is [nr / 16][bt_rows][NBASIS][16] (unit strides only)
+    int bt_rows;             // > 0: B is [nr / 32][bt_rows][NBASIS][32] (unit strides only, btab_index)
     const int *nk;           // [nw]
     const int *ks;           // [nw] k stride, constant on each tile of kW frequencies (null: 1)
     const long long *koff;   // [nw]
     const double *dist;      // [nr]
-    float *P;                // partial sums [nsplit][nr][nc][nw] complex
+    float *P;                // partial sums [nsplit][2 groups][nr][nc][nw] complex
     long long nkw;
     double dk;
     int nw, nr, nkmax, nsplit, kslice;   // kslice: k per split (multiple of kKT)
     unsigned int *err;
 };
 
-template <int SRC>
-__global__ void __launch_bounds__(tc::kThreads, 1) ksum_tc_kernel(KsumTcArgs<float> A)
+// One CTA of column group GRP; blk = (frequency tile, receiver tile, k slice).
+template <int SRC, int GRP>
+__device__ __forceinline__ void ksum_tc_cta(const KsumTcArgs<float> &A, int blk, unsigned char *smem_tc,
+                                            unsigned long long *bars, float *ir_s)
 {
     using namespace tc;
     using CT = Cols<SRC>;
-    constexpr int NQ = TcCfg<SRC>::NQ, NC = TcCfg<SRC>::NC, NP = TcCfg<SRC>::NP;
-    constexpr PairGroups<SRC> G = make_groups<SRC>();
-    static_assert(NP * kN <= (int)kTmemCols, "accumulators exceed tensor memory");
-    extern __shared__ __align__(1024) unsigned char smem_tc[];
-    __shared__ __align__(8) unsigned long long bars[3 * kStages + 1];
+    using TG = TcGroup<SRC, GRP>;
+    constexpr int NC = CT::NC, NQ = TG::NQ, NP = TG::NP;
+    constexpr TcPlan TP = make_tcplan<SRC>();
+    constexpr unsigned kBasis = group_basis_mask<SRC, GRP>();
     __shared__ uint32_t tmem_base_s;
     __shared__ int fail_s;
 
     const int nrt = (A.nr + kN - 1) / kN;
-    const int wt = blockIdx.x / (nrt * A.nsplit);
-    const int rem = blockIdx.x % (nrt * A.nsplit);
+    const int wt = blk / (nrt * A.nsplit);
+    const int rem = blk % (nrt * A.nsplit);
     const int rt = rem / A.nsplit, sp = rem % A.nsplit;
     const int w0 = wt * kW, r0 = rt * kN;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -197,32 +226,40 @@ __global__ void __launch_bounds__(tc::kThreads, 1) ksum_tc_kernel(KsumTcArgs<flo
 
     unsigned char *sm = (unsigned char *)(((uintptr_t)smem_tc + 1023) & ~(uintptr_t)1023);
     const uint32_t sm_s = (uint32_t)__cvta_generic_to_shared(sm);
-    auto full_bar = [&](int s) { return (uint32_t)__cvta_generic_to_shared(&bars[s]); };
-    auto empty_bar = [&](int s) { return (uint32_t)__cvta_generic_to_shared(&bars[kStages + s]); };
-    const uint32_t done_bar = (uint32_t)__cvta_generic_to_shared(&bars[2 * kStages]);
-    auto raw_bar = [&](int s) { return (uint32_t)__cvta_generic_to_shared(&bars[2 * kStages + 1 + s]); };
+    auto bar_at = [&](int i) { return (uint32_t)__cvta_generic_to_shared(&bars[i]); };
+    auto full_bar = [&](int s) { return bar_at(s); };                   // producers' B tiles
+    auto empty_bar = [&](int s) { return bar_at(kStages + s); };        // the stage's MMAs are done
+    auto land_bar = [&](int s) { return bar_at(2 * kStages + s); };     // coefficient tiles copied
+    auto raw_bar = [&](int s) { return bar_at(3 * kStages + s); };      // raw Bessel rows copied
+    const uint32_t done_bar = bar_at(4 * kStages);
     const bool tiled = A.bt_rows > 0;
-    auto raw_off = [&](int s) { return (uint32_t)(kStages * stage_bytes<SRC>() + s * kRawBytes); };
-    auto a_tile = [&](int s, int q, int split) {
-        return (uint32_t)(s * stage_bytes<SRC>() + (q * 2 + split) * kATileBytes);
+    // stage s: [A: NQ x (hi, lo) tiles][B: (hi | lo) x NP tiles][raw Bessel rows]
+    auto a_tile = [&](int s, int i, int split) {
+        return (uint32_t)(s * TG::kStageBytes + (i * 2 + split) * kATileBytes);
     };
-    // B operands: split-major, pairs in q order, 16 rows (receivers) per pair
     auto b_tile = [&](int s, int slot, int split) {
-        return (uint32_t)(s * stage_bytes<SRC>() + NQ * 2 * kATileBytes + (split * NP + slot) * kBTileBytes);
+        return (uint32_t)(s * TG::kStageBytes + TG::kABytes + (split * NP + slot) * kBTileBytes);
     };
+    auto raw_off = [&](int s) { return (uint32_t)(s * TG::kStageBytes + TG::kABytes + TG::kBBytes); };
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kStages; s++) {
-            // every producer arrives once, plus producer 0's expect-tx arrival for the A copy
-            tc::mbar_init(full_bar(s), kProducers + 1);
+            tc::mbar_init(full_bar(s), kProducers);
             tc::mbar_init(empty_bar(s), 1);
+            tc::mbar_init(land_bar(s), 1);
+            tc::mbar_init(raw_bar(s), 1);
         }
         tc::mbar_init(done_bar, 1);
-        for (int s = 0; s < kStages; s++) tc::mbar_init(raw_bar(s), 1);
         fail_s = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 4) {
+    // receiver factors r^-1, r^-2 of the drain's terms
+    if (threadIdx.x < kN) {
+        const double dj = A.dist[min(r0 + (int)threadIdx.x, A.nr - 1)];
+        ir_s[threadIdx.x] = (float)(1.0 / dj);
+        ir_s[kN + threadIdx.x] = (float)(1.0 / (dj * dj));
+    }
+    if (warp == kMmaWarp) {
         const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&tmem_base_s);
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst), "r"(kTmemCols)
                      : "memory");
@@ -233,146 +270,126 @@ __global__ void __launch_bounds__(tc::kThreads, 1) ksum_tc_kernel(KsumTcArgs<flo
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_base_s;
 
-    if (warp < 4) {
-        // ---------------- producers
-        const int tid = threadIdx.x;
+    if (warp == kCopyWarp) {
+        // ---------------- bulk copies, up to kStages ahead of the MMAs
+        if (lane == 0) {
+            const float *kt_tile = A.Kt + A.kt_base[wt];
+            const float *braw = tiled ? A.B + (size_t)rt * A.bt_rows * NBASIS * kN : nullptr;
+            int issued = 0;
+            for (int st = 0; st < nstage; st++) {
+                const int s = st % kStages;
+                if (st >= kStages && !tc::mbar_wait_b(empty_bar(s), ((st / kStages) - 1) & 1)) {
+                    atomicOr(A.err, 2u);
+                    fail_s = 1;
+                    break;
+                }
+                if (fail_s) break;
+                const int k0 = kb + st * kKT;
+                // this group's coefficient tiles of the (frequency tile, k stage) block
+                const float *src = kt_tile + ((long long)(k0 / kKT) * TG::NQU + TG::Q0) * (2 * kM * kKT);
+                tc::mbar_expect_tx(land_bar(s), (uint32_t)TG::kABytes);
+                tc::bulk_copy(sm_s + a_tile(s, 0, 0), src, (uint32_t)TG::kABytes, land_bar(s));
+                if (tiled) {
+                    tc::mbar_expect_tx(raw_bar(s), (uint32_t)kRawBytes);
+                    tc::bulk_copy(sm_s + raw_off(s), braw + (size_t)k0 * NBASIS * kN, (uint32_t)kRawBytes, raw_bar(s));
+                }
+                issued = st + 1;
+            }
+            // copies still in flight are waited for (bounded) before the block may leave
+            for (int st = max(0, issued - kStages); st < issued; st++) {
+                tc::mbar_wait_b(land_bar(st % kStages), (st / kStages) & 1);
+                if (tiled) tc::mbar_wait_b(raw_bar(st % kStages), (st / kStages) & 1);
+            }
+        }
+    } else if (warp < kProdWarps) {
+        // ---------------- producers of the Bessel operand
         // (receiver, k) of this thread in a stage: a warp covers one 8-receiver x
         // 4-k core matrix, so its B-operand stores fill 32 distinct banks
-        const int br = (warp & 1) * 8 + (lane >> 2), bk = (warp >> 1) * 4 + (lane & 3);
+        const int br = (warp & 3) * 8 + (lane >> 2), bk = (warp >> 2) * 4 + (lane & 3);
         const int rg = min(r0 + br, A.nr - 1);
         const bool rok = (r0 + br) < A.nr;
         const int ksm = A.ks ? A.ks[w0] : 1;
         const float dk = (float)(A.dk * ksm);
-        const unsigned a_bytes = (unsigned)(NQ * 2 * kATileBytes);
-        const float *kt_tile = A.Kt + A.kt_base[wt];
-        const float *braw = tiled ? A.B + (size_t)rt * A.bt_rows * NBASIS * kN : nullptr;
-        // tiled table: the raw rows of a stage arrive by one bulk copy, a stage ahead
-        auto issue_raw = [&](int st_) {
-            const int s_ = st_ % kStages;
-            const float *src = braw + (size_t)(kb + st_ * kKT) * NBASIS * kN;
-            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(raw_bar(s_)),
-                         "r"((unsigned)kRawBytes)
-                         : "memory");
-            asm volatile(
-                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                    sm_s + raw_off(s_)),
-                "l"(src), "r"((unsigned)kRawBytes), "r"(raw_bar(s_))
-                : "memory");
-        };
-        int raw_issued = 0;
-        if (tiled && tid == 0 && nstage > 0) {
-            issue_raw(0);
-            raw_issued = 1;
-        }
+        // the tiled table permutes a row's receivers by r ^ 8 (k & 3); kb is a multiple of 8
+        const int bcol = br ^ ((bk & 3) << 3);
         // untiled table: Bessel values of the next stage loaded one stage ahead
         float bv[NBASIS];
         auto load_b = [&](int st_) {
             const int k = kb + st_ * kKT + bk;
             const bool kok = st_ < nstage && k < ke && rok;
 #pragma unroll
-            for (int b = 0; b < NBASIS; b++) bv[b] = kok ? __ldg(A.B + ((long long)k * ksm * NBASIS + b) * A.nr + rg) : 0.f;
+            for (int b = 0; b < NBASIS; b++)
+                if ((kBasis >> b) & 1u)
+                    bv[b] = kok ? __ldg(A.B + ((long long)k * ksm * NBASIS + b) * A.nr + rg) : 0.f;
         };
         if (!tiled) load_b(0);
+        // each producer runs on its own (no barrier among them: the copy thread
+        // refills a stage's raw rows only after its MMAs, hence after every
+        // producer has read them); a wait that gives up ends this producer's loop
         for (int st = 0; st < nstage; st++) {
             const int s = st % kStages;
-            if (st >= kStages) {
-                if (!tc::mbar_wait_b(empty_bar(s), ((st / kStages) - 1) & 1)) {
-                    atomicOr(A.err, 2u);
-                    fail_s = 1;
-                }
-            }
-            // all producers are past stage st - 1 (its raw buffer may be refilled) and
-            // take one decision on failure: the OR over the producers of what each saw
-            // (the issuing warp may set fail_s at any time)
-            int any_fail;
-            asm volatile(
-                "{\n\t.reg .pred p, q;\n\t"
-                "setp.ne.s32 p, %1, 0;\n\t"
-                "bar.red.or.pred q, 1, %2, p;\n\t"
-                "selp.s32 %0, 1, 0, q;\n\t}\n"
-                : "=r"(any_fail)
-                : "r"((int)fail_s), "n"(kProducers)
-                : "memory");
-            if (any_fail) break;
-            const int k0 = kb + st * kKT;
-            if (tid == 0) {
-                if (tiled && st + 1 < nstage) {
-                    issue_raw(st + 1);
-                    raw_issued = st + 2;
-                }
-                // A operand: one bulk copy of the (frequency tile, k stage) block the
-                // GRT kernel wrote in operand layout
-                const float *src = kt_tile + (long long)(k0 / kKT) * (NQ * 2 * kM * kKT);
-                const uint32_t dst = sm_s + a_tile(s, 0, 0);
-                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(full_bar(s)), "r"(a_bytes)
-                             : "memory");
-                asm volatile(
-                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-                    "l"(src), "r"(a_bytes), "r"(full_bar(s))
-                    : "memory");
+            if (st >= kStages && !tc::mbar_wait_b(empty_bar(s), ((st / kStages) - 1) & 1)) {
+                atomicOr(A.err, 2u);
+                fail_s = 1;
+                break;
             }
             // B operand: pair values k^kp w J_b(k r) for (receiver br, k bk)
-            {
-                const int k = k0 + bk;
-                float cur[NBASIS];
-                if (tiled) {
-                    if (!tc::mbar_wait_b(raw_bar(s), (st / kStages) & 1)) {
-                        atomicOr(A.err, 2u);
-                        fail_s = 1;
-                    }
-                    const float *rs = reinterpret_cast<const float *>(sm + raw_off(s));
-                    const bool kok = k < ke && rok;
-#pragma unroll
-                    for (int b = 0; b < NBASIS; b++) cur[b] = kok ? rs[(bk * NBASIS + b) * kN + br] : 0.f;
-                } else {
-#pragma unroll
-                    for (int b = 0; b < NBASIS; b++) cur[b] = bv[b];
-                    load_b(st + 1);
+            const int k = kb + st * kKT + bk;
+            float cur[NBASIS];
+            if (tiled) {
+                if (!tc::mbar_wait_b(raw_bar(s), (st / kStages) & 1)) {
+                    atomicOr(A.err, 2u);
+                    fail_s = 1;
+                    break;
                 }
-                const float kf = dk * (float)k;
-                const float w = (k == 0) ? 0.5f * dk : dk;
-                const float wk[3] = {w, w * kf, w * kf * kf};
+                const float *rs = reinterpret_cast<const float *>(sm + raw_off(s));
+                const bool kok = k < ke && rok;
 #pragma unroll
-                for (int p = 0; p < NP; p++) {
-                    const Pair P = CT::pair(p);
-                    const float v = wk[P.kp] * cur[P.b];
-                    const float h = tc::tf32_rna(v), l = tc::tf32_rna(v - h);
-                    *reinterpret_cast<float *>(sm + b_tile(s, G.slot[p], 0) + tc::tile_off(br, bk)) = h;
-                    *reinterpret_cast<float *>(sm + b_tile(s, G.slot[p], 1) + tc::tile_off(br, bk)) = l;
-                }
+                for (int b = 0; b < NBASIS; b++)
+                    if ((kBasis >> b) & 1u) cur[b] = kok ? rs[(bk * NBASIS + b) * kN + bcol] : 0.f;
+            } else {
+#pragma unroll
+                for (int b = 0; b < NBASIS; b++) cur[b] = bv[b];
+                load_b(st + 1);
+            }
+            const float kf = dk * (float)k;
+            const float w = (k == 0) ? 0.5f * dk : dk;
+            const float wk[3] = {w, w * kf, w * kf * kf};
+#pragma unroll
+            for (int slot = 0; slot < NP; slot++) {
+                const Pair P = CT::pair(TP.gpair[GRP][slot]);
+                const float v = wk[P.kp] * cur[P.b];
+                const float h = tc::tf32_rna(v), l = tc::tf32_rna(v - h);
+                *reinterpret_cast<float *>(sm + b_tile(s, slot, 0) + tc::tile_off(br, bk)) = h;
+                *reinterpret_cast<float *>(sm + b_tile(s, slot, 1) + tc::tile_off(br, bk)) = l;
             }
             // make the generic-proxy writes visible to the tensor cores, then signal
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             tc::mbar_arrive(full_bar(s));
         }
-        // a raw copy issued for a stage that was never consumed (early exit) is
-        // waited for (bounded) before the block can leave
-        if (tiled && tid == 0 && raw_issued > 0) {
-            const int last = raw_issued - 1;
-            tc::mbar_wait_b(raw_bar(last % kStages), (last / kStages) & 1);
-        }
     } else if (lane == 0) {
-        // ---------------- MMA issuer (one thread of warp 4)
+        // ---------------- MMA issuer (one thread of warp 9)
         for (int st = 0; st < nstage; st++) {
             const int s = st % kStages;
-            if (!tc::mbar_wait_b(full_bar(s), (st / kStages) & 1)) {
+            const uint32_t par = (st / kStages) & 1;
+            if (!tc::mbar_wait_b(land_bar(s), par) || !tc::mbar_wait_b(full_bar(s), par)) {
                 atomicOr(A.err, 4u);
                 fail_s = 1;
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            // fully unrolled: group, operand and accumulator offsets are compile-time
+            // fully unrolled: tile, operand and accumulator offsets are compile-time
             // constants; descriptors are the stage's base descriptor plus a constant
-            const uint64_t dbase = tc::sdesc(sm_s + (uint32_t)(s * stage_bytes<SRC>()));
+            const uint64_t dbase = tc::sdesc(sm_s + (uint32_t)(s * TG::kStageBytes));
             const uint32_t acc0 = st == 0 ? 0u : 1u;
 #pragma unroll
-            for (int q = 0; q < NQ; q++) {
-                if (G.count[q] == 0) continue;
-                const uint32_t idesc = tc::idesc_n(G.count[q] * kN);
-                const uint32_t d = tmem + (uint32_t)(G.first[q] * kN);
-                const uint64_t ah = dbase + ((uint64_t)a_tile(0, q, 0) >> 4), al = dbase + ((uint64_t)a_tile(0, q, 1) >> 4);
-                const uint64_t bh = dbase + ((uint64_t)b_tile(0, G.first[q], 0) >> 4);
-                const uint64_t bl = dbase + ((uint64_t)b_tile(0, G.first[q], 1) >> 4);
+            for (int i = 0; i < NQ; i++) {
+                const int first = TP.tfirst[TG::Q0 + i], count = TP.tcount[TG::Q0 + i];
+                const uint32_t idesc = tc::idesc_n(count * kN);
+                const uint32_t d = tmem + (uint32_t)(first * kN);
+                const uint64_t ah = dbase + ((uint64_t)a_tile(0, i, 0) >> 4), al = dbase + ((uint64_t)a_tile(0, i, 1) >> 4);
+                const uint64_t bh = dbase + ((uint64_t)b_tile(0, first, 0) >> 4);
+                const uint64_t bl = dbase + ((uint64_t)b_tile(0, first, 1) >> 4);
                 tc::mma_tf32(d, ah, bh, idesc, acc0);
                 tc::mma_tf32(d, ah, bl, idesc, 1u);
                 tc::mma_tf32(d, al, bh, idesc, 1u);
@@ -383,7 +400,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) ksum_tc_kernel(KsumTcArgs<flo
     }
 
     // ---------------- drain: tensor memory -> partial sums
-    if (warp < 4) {
+    if (warp < kProdWarps) {
         // the issuer always commits done_bar (immediately when it issued nothing)
         bool ok = nstage > 0;
         if (!tc::mbar_wait_b(done_bar, 0)) {
@@ -392,38 +409,37 @@ __global__ void __launch_bounds__(tc::kThreads, 1) ksum_tc_kernel(KsumTcArgs<flo
         }
         if (fail_s) ok = false;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const int row = warp * 32 + lane;            // the lane of tensor memory this thread reads
+        const int quarter = warp & 3, half = warp >> 2;   // output columns c = half (mod 2)
+        const int row = quarter * 32 + lane;              // the lane of tensor memory this thread reads
         const int part = row / kW, wl = row % kW, w = w0 + wl;
-        // receiver factors r^-1, r^-2 of the terms
-        float irj[kN], ir2j[kN];
-#pragma unroll
-        for (int j = 0; j < kN; j++) {
-            const double dj = A.dist[min(r0 + j, A.nr - 1)];
-            irj[j] = (float)(1.0 / dj);
-            ir2j[j] = (float)(1.0 / (dj * dj));
-        }
+        const long long psplit = (long long)sp * 2 + GRP;
 #pragma unroll
         for (int c = 0; c < NC; c++) {
+            if ((c & 1) != half) continue;
             float acc[kN];
 #pragma unroll
             for (int j = 0; j < kN; j++) acc[j] = 0.f;
 #pragma unroll
             for (int t = CT::col(c); t < CT::col(c + 1); t++) {
                 const Term T = CT::term(t);
+                if (TP.pgrp[T.pair] != GRP) continue;
                 uint32_t v[kN];
-                const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(G.slot[T.pair] * kN);
+                const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(TP.pslot[T.pair] * kN);
                 asm volatile(
-                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                    "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                    "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
                     : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
                       "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
-                      "=r"(v[15])
+                      "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+                      "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+                      "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
                     : "r"(taddr)
                     : "memory");
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
                 const float cf = (float)T.coef;
 #pragma unroll
                 for (int j = 0; j < kN; j++) {
-                    const float f = T.rpow == 1 ? cf * irj[j] : T.rpow == 2 ? cf * ir2j[j] : cf;
+                    const float f = T.rpow == 1 ? cf * ir_s[j] : T.rpow == 2 ? cf * ir_s[kN + j] : cf;
                     acc[j] = fmaf(f, __uint_as_float(v[j]), acc[j]);
                 }
             }
@@ -431,26 +447,38 @@ __global__ void __launch_bounds__(tc::kThreads, 1) ksum_tc_kernel(KsumTcArgs<flo
 #pragma unroll
                 for (int j = 0; j < kN; j++) {
                     const int r = r0 + j;
-                    if (r < A.nr) A.P[((((long long)sp * A.nr + r) * NC + c) * A.nw + w) * 2 + part] = ok ? acc[j] : 0.f;
+                    if (r < A.nr) A.P[((((psplit * A.nr + r) * NC + c) * A.nw + w) * 2 + part)] = ok ? acc[j] : 0.f;
                 }
             }
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (warp == 4) {
+    if (warp == kMmaWarp) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
     }
 }
 
-// S[r][c][w] = sum over k slices of the partial sums (TwoSum)
-__global__ void ksum_tc_reduce_kernel(const float *P, float *S, long long n, int nsplit)
+// Both column groups in one launch (even blocks group 0, odd blocks group 1),
+// so that their CTAs share the waves of the SMs.
+template <int SRC>
+__global__ void __launch_bounds__(tc::kThreads, 1) ksum_tc_kernel(KsumTcArgs<float> A)
+{
+    extern __shared__ __align__(1024) unsigned char smem_tc[];
+    __shared__ __align__(8) unsigned long long bars[4 * tc::kStages + 1];
+    __shared__ float ir_s[2 * tc::kN];
+    if (blockIdx.x & 1) ksum_tc_cta<SRC, 1>(A, (int)(blockIdx.x >> 1), smem_tc, bars, ir_s);
+    else ksum_tc_cta<SRC, 0>(A, (int)(blockIdx.x >> 1), smem_tc, bars, ir_s);
+}
+
+// S[r][c][w] = sum over the partial sums (k slices x groups) with TwoSum
+__global__ void ksum_tc_reduce_kernel(const float *P, float *S, long long n, int nparts)
 {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= n) return;
     float hi = 0.f, lo = 0.f;
-    for (int s = 0; s < nsplit; s++) two_sum_acc(hi, lo, P[(long long)s * n + i]);
+    for (int s = 0; s < nparts; s++) two_sum_acc(hi, lo, P[(long long)s * n + i]);
     S[i] = hi + lo;
 }
 

@@ -58,10 +58,12 @@ struct GrtArgs {
     // tensor-core layout of the coefficients (FP32 plans): when Kt is set the
     // kernel writes, instead of K, TF32 hi/lo words straight into the operand
     // tiles of the wavenumber GEMM: block (frequency tile of 64, k stage of 8)
-    // at Kt + kt_base[tile] + stage * nq * 2048 floats, inside it [q][hi|lo]
-    // K-major core-matrix tiles of 128 rows (re rows 0-63, im rows 64-127).
+    // at Kt + kt_base[tile] + stage * nqt * 2048 floats, inside it [tile][hi|lo]
+    // K-major core-matrix tiles of 128 rows (re rows 0-63, im rows 64-127),
+    // one tile per coefficient column the sum reads (make_tcplan)
     float *Kt;
     const long long *kt_base;
+    int nqt;
 };
 
 // Bessel basis functions of k r, in the order the integrand formulas use them
