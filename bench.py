@@ -220,8 +220,8 @@ def rel_errors(a, ref):
 
 
 # DRAM bytes per (w,k) point of the FP32 GRT kernel (tensor-core operand layout), from one ncu capture
-# of the small 40-layer case: 6.1 MB read + 215.1 MB written for 2.10 M points (profiles/grt_point_config3s.md)
-GRT_DRAM_BYTES_PER_POINT = (6.128128e6 + 215.1104e6) / (512 * 4096)
+# of the small 40-layer case: 5.7 MB read + 181.3 MB written for 2.10 M points (profiles/grt_point_config3s.md)
+GRT_DRAM_BYTES_PER_POINT = (5.668864e6 + 181.344512e6) / (512 * 4096)
 
 
 def grt_roofline(n_wk_by_layers, ms, fp32_peak):
@@ -640,6 +640,46 @@ def bench_single(args, ws, rank, local, td):
     barrier(td)
 
 
+def bench_tile(args, ws, rank, local, td):
+    """The tensor-core wavenumber sum alone on one frequency tile of the default
+    workload: model 0, 64 frequencies spread over the band (a spectra-only
+    plan), 32768 wavenumbers, 1000 receivers; reports the sum's device time
+    and its tensor-core rate (the profiling case of that kernel)."""
+    import grtm_cuda_gb300 as g
+    from grtm_cuda_gb300 import learned
+    (m, d), = config5_models(rank, 1, args.receivers)
+    sel = np.linspace(1, 4095, 64).astype(np.int32)
+    ctx = g.Context(local)
+    plan = g.Plan(ctx, g.make_model(**m), learned.plain_opts(freq_sel=sel), d)
+    for _ in range(args.warmup):
+        plan.execute()
+    barrier(td)
+    ms = [plan.execute().ms_ksum for _ in range(args.steps)]
+    r = plan.report
+    plan.close()
+    ctx.close()
+    t = float(np.median(ms)) * 1e-3
+    # executed MMA work: 3 TF32 products x (25 pairs x 32-receiver tiles x 128 rows x k)
+    n_rt = (len(d) + 31) // 32
+    mma_flop = 3 * 2 * 25 * n_rt * 32 * 128 * 32768
+    algo_flop = 2 * 2 * 64 * 32768 * len(d) * 32
+    out = {"metric": "tensor-core wavenumber sum, one 64-frequency tile (TFLOP/s, algorithmic)",
+           "value": algo_flop / t / 1e12, "unit": "TFLOP/s", "n_gpus": ws, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32 (3xTF32 products, FP32 accumulation)", "data": "synthetic (seeded)",
+           "config": {"workload": "k-sum tile: held-out 40-layer model 0 of the default workload, 64 frequencies "
+                                  "spread over nt 8192, 32768 wavenumbers, %d receivers" % len(d),
+                      "l2": "inputs larger than L2 (coefficients 235 MB, Bessel table 1.2 GB)"},
+           "roofline": {"bound": "tensor", "achieved": mma_flop / t / 1e12, "peak": 1100.0, "unit": "TFLOP/s",
+                        "frac": mma_flop / t / 1e12 / 1100.0, "traffic": None,
+                        "peak_source": "nominal dense TF32 tensor rate of GB300 (no measured TF32 figure)",
+                        "kernel": "ksum_tc_kernel<tensor>", "k_slice": r.k_slice},
+           "gpu_launches": 2 * args.steps}
+    if rank == 0:
+        print(json.dumps(out))
+    barrier(td)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -647,10 +687,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
-    ap.add_argument("--case", default="config5", choices=["config5", "config4", "config2", "config1", "config3s"],
+    ap.add_argument("--case", default="config5",
+                    choices=["config5", "config4", "config2", "config1", "config3s", "tile"],
                     help="config5: batch of held-out 40-layer models (the metric's workload); config2: one "
                          "20-layer model, 200 receivers; config1: 4 layers, 10 receivers; config3s: one 40-layer "
-                         "model, 64 receivers, nt 1024, nk 4096 (small profiling case)")
+                         "model, 64 receivers, nt 1024, nk 4096 (small profiling case); tile: the tensor-core "
+                         "wavenumber sum on one 64-frequency tile of config5's model 0")
     ap.add_argument("--models", type=int, default=2, help="config5: models per batch")
     ap.add_argument("--receivers", type=int, default=1000, help="config5: receivers per model")
     ap.add_argument("--chunk", type=int, default=32, help="config4: models per batch")
@@ -658,6 +700,8 @@ def main():
     ws, rank, local, td = dist_setup()
     if args.case == "config5":
         bench_batch(args, ws, rank, local, td)
+    elif args.case == "tile":
+        bench_tile(args, ws, rank, local, td)
     elif args.case == "config4":
         if args.models == 2:
             args.models = 256

@@ -244,7 +244,7 @@ __device__ __forceinline__ void ksum_tc_cta(const KsumTcArgs<float> &A, int blk,
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kStages; s++) {
-            tc::mbar_init(full_bar(s), kProducers);
+            tc::mbar_init(full_bar(s), kProdWarps);   // one arrival per producer warp
             tc::mbar_init(empty_bar(s), 1);
             tc::mbar_init(land_bar(s), 1);
             tc::mbar_init(raw_bar(s), 1);
@@ -323,12 +323,14 @@ __device__ __forceinline__ void ksum_tc_cta(const KsumTcArgs<float> &A, int blk,
                     bv[b] = kok ? __ldg(A.B + ((long long)k * ksm * NBASIS + b) * A.nr + rg) : 0.f;
         };
         if (!tiled) load_b(0);
-        // each producer runs on its own (no barrier among them: the copy thread
-        // refills a stage's raw rows only after its MMAs, hence after every
-        // producer has read them); a wait that gives up ends this producer's loop
+        // each producer warp runs on its own (no barrier among them: the copy
+        // thread refills a stage's raw rows only after its MMAs, hence after every
+        // producer has read them); a wait that gives up in any lane ends the
+        // warp's loop (one decision per warp, as its lanes share a __syncwarp)
         for (int st = 0; st < nstage; st++) {
             const int s = st % kStages;
-            if (st >= kStages && !tc::mbar_wait_b(empty_bar(s), ((st / kStages) - 1) & 1)) {
+            const bool free_ok = st < kStages || tc::mbar_wait_b(empty_bar(s), ((st / kStages) - 1) & 1);
+            if (__any_sync(0xffffffffu, !free_ok)) {
                 atomicOr(A.err, 2u);
                 fail_s = 1;
                 break;
@@ -337,7 +339,8 @@ __device__ __forceinline__ void ksum_tc_cta(const KsumTcArgs<float> &A, int blk,
             const int k = kb + st * kKT + bk;
             float cur[NBASIS];
             if (tiled) {
-                if (!tc::mbar_wait_b(raw_bar(s), (st / kStages) & 1)) {
+                const bool raw_ok = tc::mbar_wait_b(raw_bar(s), (st / kStages) & 1);
+                if (__any_sync(0xffffffffu, !raw_ok)) {
                     atomicOr(A.err, 2u);
                     fail_s = 1;
                     break;
@@ -363,9 +366,11 @@ __device__ __forceinline__ void ksum_tc_cta(const KsumTcArgs<float> &A, int blk,
                 *reinterpret_cast<float *>(sm + b_tile(s, slot, 0) + tc::tile_off(br, bk)) = h;
                 *reinterpret_cast<float *>(sm + b_tile(s, slot, 1) + tc::tile_off(br, bk)) = l;
             }
-            // make the generic-proxy writes visible to the tensor cores, then signal
+            // make the generic-proxy writes visible to the tensor cores, then one
+            // lane signals for the warp
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            tc::mbar_arrive(full_bar(s));
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(full_bar(s));
         }
     } else if (lane == 0) {
         // ---------------- MMA issuer (one thread of warp 9)
