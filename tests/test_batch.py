@@ -68,3 +68,30 @@ def test_batch_rejects_mixed_precision(ctx):
     with pytest.raises(g.GrtError) as e:
         g.Batch(ctx, [jobs[0], (m, o64, d)])
     assert e.value.status == g.ERR_ARG
+
+
+@pytest.mark.gpu
+def test_pinned_fetch_and_cached_memory(ctx):
+    """Fetches into page-locked arrays equal ordinary ones; batches rebuilt on
+    the context's cached memory, and after returning it to the driver, give
+    the same traces."""
+    import grtm_cuda_gb300 as g
+    jobs = _jobs(g, g.FP32)
+    b = g.Batch(ctx, jobs, autotune=False)
+    b.execute()
+    ref = [b.fetch_f32(j) for j in range(len(jobs))]
+    outs = [g.pinned_empty(r.shape) for r in ref]
+    for j, o in enumerate(outs):
+        assert b.fetch_f32(j, out=o) is o
+        assert np.array_equal(o, ref[j])
+    with pytest.raises(ValueError):
+        b.fetch_f32(0, out=np.empty(ref[0].shape, np.float64))
+    b.close()
+    for trim in (False, True):
+        if trim:
+            ctx.trim()
+        b = g.Batch(ctx, jobs, autotune=False)
+        b.execute()
+        for j in range(len(jobs)):
+            assert np.array_equal(b.fetch_f32(j), ref[j])
+        b.close()
