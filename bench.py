@@ -369,6 +369,7 @@ def bench_batch(args, ws, rank, local, td):
             "fast": {"value": value, "e2e": e2e, "ms_batch_gpu": last["ms_batch_gpu"],
                      "ms_batch_grt": last["ms_batch_grt"], "s_predict": last["s_predict"],
                      "s_build": last["s_build"], "s_execute_fetch": last["s_execute"], "s_fetch": last["s_fetch"],
+                     "s_fetch_wait": last["s_fetch_wait"],
                      "s_judge": last["s_judge"],
                      "s_fallback": last["s_fallback"], "judge_parts": last.get("s_judge_parts"),
                      "points_vs_plain": frac_pts,

@@ -153,7 +153,7 @@ EXPORTS = ("grt_create", "grt_destroy", "grt_last_error", "grt_status_string", "
            "grt_mlp_loss_grad", "grt_mlp_train", "grt_batch_create", "grt_batch_execute", "grt_batch_fetch",
            "grt_batch_fetch_freqs", "grt_batch_info", "grt_batch_destroy", "grt_dc_moment", "grt_plan_synth",
            "grt_batch_synth", "grt_flatten", "grt_plan_write", "grt_plan_fetch_f32", "grt_batch_fetch_f32",
-           "grt_host_alloc", "grt_host_free", "grt_trim")
+           "grt_host_alloc", "grt_host_free", "grt_trim", "grt_batch_fetch_f32_async", "grt_batch_wait")
 
 _lib = None
 
@@ -220,6 +220,8 @@ def lib():
     L.grt_host_alloc.argtypes = [ctypes.c_size_t, P(vp)]
     L.grt_host_free.argtypes = [vp]
     L.grt_host_free.restype = None
+    L.grt_batch_fetch_f32_async.argtypes = [vp, ctypes.c_int, P(ctypes.c_float)]
+    L.grt_batch_wait.argtypes = [vp]
     L.grt_trim.argtypes = [vp]
     L.grt_trim.restype = None
     L.grt_flatten.argtypes = [ctypes.c_int, _dp, _dp, _dp, ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp,
@@ -427,6 +429,7 @@ class Batch:
     def __init__(self, ctx, jobs, autotune=True):
         self.ctx = ctx
         self._keep = []
+        self._pending = []
         arr = (Job * len(jobs))()
         self.dists = []
         for i, (model, opts, dists) in enumerate(jobs):
@@ -465,6 +468,27 @@ class Batch:
         if rc:
             raise GrtError(rc, self.ctx.error())
         return t
+
+    def fetch_f32_async(self, job, out):
+        """Start downloading one job's float32 traces into `out` (a
+        pinned_empty array of shape [n_dist, n_cols, N]); returns at once.
+        `out` must not be read before wait()."""
+        r, _ = self.info(job)
+        shape = (len(self.dists[job]), r["n_cols"], r["n_samples"])
+        if out.shape != shape or out.dtype != np.float32 or not out.flags.c_contiguous:
+            raise ValueError(f"out must be a C-contiguous float32 array of shape {shape}")
+        rc = lib().grt_batch_fetch_f32_async(self.h, int(job), out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+        if rc:
+            raise GrtError(rc, self.ctx.error())
+        self._pending.append(out)
+        return out
+
+    def wait(self):
+        """Wait for the downloads fetch_f32_async started."""
+        rc = lib().grt_batch_wait(self.h)
+        self._pending = []
+        if rc:
+            raise GrtError(rc, self.ctx.error())
 
     def fetch(self, job, traces=True, spectra=False):
         r, _ = self.info(job)

@@ -35,6 +35,7 @@ struct grt_plan {
     int rt = 128, jt = 1;
     int use_tc = 0, nsplit = 1, kslice = 0;   // tensor-core wavenumber sum and its split-K
     int kslice_req = 0;                       // requested k per slice (0: chosen here)
+    int gspec = 0;                            // compiled form of the GRT evaluation (grt::GrtSpec)
     int bt_rows = 0;                          // > 0: Bessel table tiled by 32 receivers (unit strides)
     int cols = 0;                             // output column layout (grt::ColKind)
     void *P = nullptr;                        // split-K partial sums
@@ -428,6 +429,10 @@ extern "C" int grt_plan_create(grt_ctx *ctx, const grt_model *m, const grt_opts 
     if (o->k_slice > 0 && (J.nkmax + o->k_slice - 1) / o->k_slice > 4096)
         return set_err(ctx, GRT_ERR_ARG, "k_slice too small: more than 4096 slices");
     p->kslice_req = o->k_slice;
+    // FP32 moment-tensor jobs with the receiver above the source's layer (and the
+    // reference's 8 coefficient columns) run the GRT evaluation compiled for that case
+    p->gspec = (p->prec == GRT_FP32 && J.src == 1 && J.rl < J.s && p->nq == grt::QT_N) ? grt::kSpecAboveTensor
+                                                                                       : grt::kSpecGeneric;
     p->rep.ksum_impl = p->use_tc;
     // the tensor-core sum multiplies a tile of 64 frequencies by one Bessel operand:
     // the frequencies of a tile share their k stride
@@ -611,7 +616,14 @@ static int execute(grt_plan *p)
     const grt::GrtArgs<R> A = grt_args<R>(p);
     const size_t smem = (size_t)J.L * sizeof(grt::LayerW<R>);
     CU(cudaEventRecord(ctx->ev[0], st));
-    grt::grt_point_kernel<R><<<p->ntiles, grt::kGrtThreads, smem, st>>>(A);
+    bool launched = false;
+    if constexpr (std::is_same<R, float>::value) {
+        if (p->gspec == grt::kSpecAboveTensor) {
+            grt::grt_point_kernel<R, grt::kSpecAboveTensor><<<p->ntiles, grt::kGrtThreads, smem, st>>>(A);
+            launched = true;
+        }
+    }
+    if (!launched) grt::grt_point_kernel<R><<<p->ntiles, grt::kGrtThreads, smem, st>>>(A);
     launches++;
     CU(cudaGetLastError());
     CU(cudaEventRecord(ctx->ev[1], st));
@@ -1092,6 +1104,7 @@ struct grt_batch {
     grt_ctx *ctx = nullptr;
     std::vector<grt_plan *> jobs;
     int prec = 0, maxL = 0, nsm = 0;
+    int gspec = 0;                   // every job allows the specialised GRT form (grt::GrtSpec)
     void *d_args = nullptr;          // GrtArgs<R>[n_jobs]
     void *d_rows = nullptr;          // per (job, frequency) row: id, nk, first tile of each width
     int4 *d_tiles[3] = {};           // tile lists for 64 / 128 / 256 threads per block
@@ -1099,6 +1112,7 @@ struct grt_batch {
     long long points = 0;
     unsigned *derr = nullptr;
     cudaStream_t side[kSide] = {};
+    cudaStream_t copy = nullptr;     // trace downloads started by grt_batch_fetch_f32_async
     cudaEvent_t ev_start = nullptr, ev_grt = nullptr, ev_end = nullptr;    // timing (graph event-record nodes)
     cudaEvent_t fork0 = nullptr, fork1 = nullptr, join[kSide] = {};         // dependencies between streams
     cudaGraph_t graph = nullptr;
@@ -1111,6 +1125,10 @@ extern "C" void grt_batch_destroy(grt_batch *b)
 {
     if (!b) return;
     cudaSetDevice(b->ctx->device);
+    if (b->copy) {
+        cudaStreamSynchronize(b->copy);
+        cudaStreamDestroy(b->copy);
+    }
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
     for (grt_plan *p : b->jobs) grt_plan_destroy(p);
@@ -1139,6 +1157,14 @@ template <typename R, int NT, bool P>
 static void launch_batch_kernel(grt_batch *b, int grid, int ntiles, cudaStream_t st)
 {
     const size_t smem = (size_t)b->maxL * sizeof(grt::LayerW<R>);
+    // one-tile forms of FP32 batches whose jobs all allow it: the specialised evaluation
+    if constexpr (!P && std::is_same<R, float>::value) {
+        if (b->gspec == grt::kSpecAboveTensor) {
+            grt::grt_batch_kernel<R, NT, P, grt::kSpecAboveTensor><<<grid, NT, smem, st>>>(
+                (const grt::GrtArgs<R> *)b->d_args, b->d_tiles[nt_index(NT)], ntiles, b->derr);
+            return;
+        }
+    }
     grt::grt_batch_kernel<R, NT, P><<<grid, NT, smem, st>>>((const grt::GrtArgs<R> *)b->d_args,
                                                             b->d_tiles[nt_index(NT)], ntiles, b->derr);
 }
@@ -1177,6 +1203,14 @@ static cudaError_t raise_batch_limits(int smem)
     if ((e = raise_smem_limit(grt::grt_batch_kernel<R, 128, false>, smem)) != cudaSuccess) return e;
     if ((e = raise_smem_limit(grt::grt_batch_kernel<R, 256, false>, smem)) != cudaSuccess) return e;
     if ((e = raise_smem_limit(grt::grt_batch_kernel<R, 128, true>, smem)) != cudaSuccess) return e;
+    if constexpr (std::is_same<R, float>::value) {
+        if ((e = raise_smem_limit(grt::grt_batch_kernel<R, 64, false, grt::kSpecAboveTensor>, smem)) != cudaSuccess)
+            return e;
+        if ((e = raise_smem_limit(grt::grt_batch_kernel<R, 128, false, grt::kSpecAboveTensor>, smem)) != cudaSuccess)
+            return e;
+        if ((e = raise_smem_limit(grt::grt_batch_kernel<R, 256, false, grt::kSpecAboveTensor>, smem)) != cudaSuccess)
+            return e;
+    }
     return raise_smem_limit(grt::grt_batch_kernel<R, 256, true>, smem);
 }
 
@@ -1387,10 +1421,14 @@ extern "C" int grt_batch_create(grt_ctx *ctx, int n_jobs, const grt_job *jobs, i
         b->points += p->J.nkw;
     }
     b->prec = jobs[0].opts->precision;
+    b->gspec = grt::kSpecAboveTensor;
+    for (grt_plan *p : b->jobs)
+        if (p->gspec != grt::kSpecAboveTensor) b->gspec = grt::kSpecGeneric;
     CU(cudaDeviceGetAttribute(&b->nsm, cudaDevAttrMultiProcessorCount, ctx->device));
     CU(dev_alloc(ctx, &b->derr, sizeof(unsigned)));
     CU(cudaMemset(b->derr, 0, sizeof(unsigned)));
     for (auto &s : b->side) CU(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    CU(cudaStreamCreateWithFlags(&b->copy, cudaStreamNonBlocking));
     CU(cudaEventCreate(&b->ev_start));
     CU(cudaEventCreate(&b->ev_grt));
     CU(cudaEventCreate(&b->ev_end));
@@ -1408,6 +1446,7 @@ extern "C" int grt_batch_execute(grt_batch *b, grt_report *r)
     if (!b) return GRT_ERR_ARG;
     grt_ctx *ctx = b->ctx;
     CU(cudaSetDevice(ctx->device));
+    CU(cudaStreamSynchronize(b->copy));     // downloads of the previous results are done
     CU(cudaGraphLaunch(b->exec, ctx->stream));
     CU(cudaEventSynchronize(b->ev_end));
     int rc = check_device_error(ctx, b->derr);
@@ -1646,6 +1685,29 @@ extern "C" int grt_host_alloc(size_t bytes, void **ptr)
 extern "C" void grt_host_free(void *ptr)
 {
     if (ptr) cudaFreeHost(ptr);
+}
+
+extern "C" int grt_batch_fetch_f32_async(grt_batch *b, int job, float *traces)
+{
+    if (!b || job < 0 || job >= (int)b->jobs.size() || !traces) return GRT_ERR_ARG;
+    grt_plan *p = b->jobs[job];
+    grt_ctx *ctx = b->ctx;
+    if (p->prec != GRT_FP32) return set_err(ctx, GRT_ERR_UNSUPPORTED, "asynchronous fetches are for FP32 batches");
+    if (!p->J.fsel.empty()) return set_err(ctx, GRT_ERR_UNSUPPORTED, "a frequency-selection plan has spectra only");
+    CU(cudaSetDevice(ctx->device));
+    // grt_batch_execute returned after the graph finished: the traces are final
+    const size_t n = (size_t)p->nd * p->nc * p->J.N;
+    CU(cudaMemcpyAsync(traces, p->sig, n * sizeof(float), cudaMemcpyDeviceToHost, b->copy));
+    return GRT_OK;
+}
+
+extern "C" int grt_batch_wait(grt_batch *b)
+{
+    if (!b) return GRT_ERR_ARG;
+    grt_ctx *ctx = b->ctx;
+    CU(cudaSetDevice(ctx->device));
+    CU(cudaStreamSynchronize(b->copy));
+    return GRT_OK;
 }
 
 extern "C" int grt_batch_fetch_f32(grt_batch *b, int job, float *traces)

@@ -37,6 +37,9 @@ enum QSingle { QS_B1 = 0, QS_A00, QS_A01, QS_A10, QS_A11, QS_B1T, QS_A0T0, QS_A0
 // moment tensor: b1, b2, a0[0..1], a1[0..1], a2[0..1]
 enum QTensor { QT_B1 = 0, QT_B2, QT_A00, QT_A01, QT_A10, QT_A11, QT_A20, QT_A21, QT_N };
 
+// compiled forms of the per-(w,k) GRT evaluation (see grt_point)
+enum GrtSpec { kSpecGeneric = 0, kSpecAboveTensor = 1 };
+
 // reference-quirk switches (0 = reproduce the reference)
 enum Fix { kFixRLayer = 1, kFixRexut = 2, kFixDz = 4, kFixCols = 8 };
 

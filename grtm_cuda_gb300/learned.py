@@ -462,6 +462,8 @@ def run_learned_batch(sampler, models, dists_list, ctx=None, plain=PLAIN, spec_t
         t.append(time.perf_counter())
         rep = b.execute()
         t_exec = time.perf_counter()
+        # (started asynchronously, the downloads held up the judge's own small
+        # copies behind them on the copy engine: 20 -> 83 ms of judge)
         traces = [b.fetch_f32(j, None if out is None else out[j]) for j in range(len(jobs))]
         t.append(time.perf_counter())
         # judge: spot frequencies on the plain grid (batched), tails by sweep
@@ -494,6 +496,8 @@ def run_learned_batch(sampler, models, dists_list, ctx=None, plain=PLAIN, spec_t
             n_fb += int(bad.sum())
         tj.append(time.perf_counter())
         sb.close()
+        t_wait = time.perf_counter()
+        b.wait()
         t.append(time.perf_counter())
         for j, idx in enumerate(fallback):
             if idx:
@@ -508,7 +512,8 @@ def run_learned_batch(sampler, models, dists_list, ctx=None, plain=PLAIN, spec_t
                     stride_mean=float(np.mean([g_[1].mean() for g_ in grids])), fallback=fallback,
                     n_fallback=n_fb, ms_batch_gpu=rep.ms_total, ms_batch_grt=rep.ms_grt,
                     gpu_launches=rep.kernel_launches, tune=tune, s_predict=t[1] - t[0], s_build=t[2] - t[1],
-                    s_execute=t[3] - t[2], s_fetch=t[3] - t_exec, s_judge=t[4] - t[3], s_fallback=t[5] - t[4],
+                    s_execute=t[3] - t[2], s_fetch=t[3] - t_exec, s_fetch_wait=t[4] - t_wait,
+                    s_judge=t_wait - t[3], s_fallback=t[5] - t[4],
                     s_total=t[5] - t[0],
                     s_judge_parts=dict(spot_build=tj[1] - tj[0], spot_exec=tj[2] - tj[1], sweeps_compare=tj[3] - tj[2]))
         b.close()

@@ -218,6 +218,14 @@ GRT_API int grt_batch_create(grt_ctx *ctx, int n_jobs, const grt_job *jobs, int 
 GRT_API int grt_batch_execute(grt_batch *batch, grt_report *report);
 GRT_API int grt_batch_fetch(grt_batch *batch, int job, double *traces, double *spectra);
 GRT_API int grt_batch_fetch_f32(grt_batch *batch, int job, float *traces);
+/* The same without waiting (FP32 batches): the copy of the last execute's
+ * traces into `traces` (page-locked memory from grt_host_alloc, left
+ * untouched until grt_batch_wait returns) runs on the batch's own copy stream
+ * beside later work on the context, such as the sampler's judge.
+ * grt_batch_wait waits for every copy started; grt_batch_execute and
+ * grt_batch_destroy wait for them first. */
+GRT_API int grt_batch_fetch_f32_async(grt_batch *batch, int job, float *traces);
+GRT_API int grt_batch_wait(grt_batch *batch);
 GRT_API int grt_batch_fetch_freqs(grt_batch *batch, int job, int n_freq, const int *freq_idx, double *spectra);
 /* job = -1: the batch's aggregate report */
 GRT_API int grt_batch_info(const grt_batch *batch, int job, grt_report *report, grt_tune *tune);

@@ -95,3 +95,29 @@ def test_pinned_fetch_and_cached_memory(ctx):
         for j in range(len(jobs)):
             assert np.array_equal(b.fetch_f32(j), ref[j])
         b.close()
+
+
+@pytest.mark.gpu
+def test_async_fetch_matches(ctx):
+    """Downloads started by fetch_f32_async equal synchronous ones after wait();
+    the next execute waits for them."""
+    import grtm_cuda_gb300 as g
+    jobs = _jobs(g, g.FP32)
+    b = g.Batch(ctx, jobs, autotune=False)
+    b.execute()
+    ref = [b.fetch_f32(j) for j in range(len(jobs))]
+    outs = [g.pinned_empty(r.shape) for r in ref]
+    for j, o in enumerate(outs):
+        b.fetch_f32_async(j, o)
+    b.execute()                      # waits for the downloads, then recomputes the same
+    b.wait()
+    for j, o in enumerate(outs):
+        assert np.array_equal(o, ref[j])
+    b.close()
+    jobs64 = _jobs(g, g.FP64)
+    b = g.Batch(ctx, jobs64, autotune=False)
+    b.execute()
+    with pytest.raises(g.GrtError) as e:
+        b.fetch_f32_async(0, g.pinned_empty(b.fetch_f32(0).shape))
+    assert e.value.status == g.ERR_UNSUPPORTED
+    b.close()
