@@ -85,7 +85,10 @@ class _HostBuf:
 
     def __del__(self):
         if self.p:
-            lib().grt_host_free(self.p)
+            try:
+                lib().grt_host_free(self.p)
+            except Exception:      # interpreter shutdown: the process frees it
+                pass
             self.p = ctypes.c_void_p()
 
 

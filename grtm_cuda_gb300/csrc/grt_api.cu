@@ -236,7 +236,7 @@ static int tc_tiles(int kind)
 }
 static int coef_count(int kind)
 {
-    return kind == grt::kColTensorFix ? 2 * grt::QT_N : (kind == grt::kColTensor ? grt::QT_N : grt::QS_N);
+    return kind == grt::kColTensorFix ? 2 * (int)grt::QT_N : (kind == grt::kColTensor ? (int)grt::QT_N : (int)grt::QS_N);
 }
 
 // ------------------------------------------------------------------ host tables
