@@ -127,7 +127,7 @@ def dc_moment(strike, dip, rake, m0=1.0):
 
 class Job(ctypes.Structure):
     _fields_ = [("model", ctypes.POINTER(Model)), ("opts", ctypes.POINTER(Opts)), ("n_dist", ctypes.c_int),
-                ("dist", _dp)]
+                ("dist", _dp), ("out_f32", ctypes.POINTER(ctypes.c_float))]
 
 
 TUNE_MAX = 16
@@ -429,7 +429,10 @@ class Batch:
     """Many jobs (model, opts, distances) executed as one CUDA graph with a
     single persistent GRT launch (grt_batch_*)."""
 
-    def __init__(self, ctx, jobs, autotune=True):
+    def __init__(self, ctx, jobs, autotune=True, outs=None):
+        """outs: optional list (per job) of float32 pinned_empty arrays of shape
+        [n_dist, n_cols, N] (or None): each execute downloads the job's traces
+        into its array inside the graph, beside the later jobs' work."""
         self.ctx = ctx
         self._keep = []
         self._pending = []
@@ -439,7 +442,14 @@ class Batch:
             d = _arr(np.atleast_1d(dists))
             self._keep += [model, opts, d]
             self.dists.append(d)
-            arr[i] = Job(ctypes.pointer(model), ctypes.pointer(opts), len(d), _ptr(d))
+            o = None if outs is None else outs[i]
+            op = None
+            if o is not None:
+                if o.dtype != np.float32 or not o.flags.c_contiguous or o.shape[0] != len(d):
+                    raise ValueError("outs: C-contiguous float32 arrays [n_dist, n_cols, N]")
+                self._keep.append(o)
+                op = o.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+            arr[i] = Job(ctypes.pointer(model), ctypes.pointer(opts), len(d), _ptr(d), op)
         self.h = ctypes.c_void_p()
         rc = lib().grt_batch_create(ctx.h, len(jobs), arr, int(bool(autotune)), ctypes.byref(self.h))
         if rc:

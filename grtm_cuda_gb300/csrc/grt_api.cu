@@ -1113,6 +1113,9 @@ struct grt_batch {
     unsigned *derr = nullptr;
     cudaStream_t side[kSide] = {};
     cudaStream_t copy = nullptr;     // trace downloads started by grt_batch_fetch_f32_async
+    std::vector<float *> outs;       // per job: page-locked destination the graph downloads into (or null)
+    std::vector<cudaEvent_t> done;   // per job: its stages finished (orders the in-graph download)
+    bool has_out = false;
     cudaEvent_t ev_start = nullptr, ev_grt = nullptr, ev_end = nullptr;    // timing (graph event-record nodes)
     cudaEvent_t fork0 = nullptr, fork1 = nullptr, join[kSide] = {};         // dependencies between streams
     cudaGraph_t graph = nullptr;
@@ -1142,6 +1145,8 @@ extern "C" void grt_batch_destroy(grt_batch *b)
     for (auto e : evs)
         if (e) cudaEventDestroy(e);
     for (auto e : b->join)
+        if (e) cudaEventDestroy(e);
+    for (auto e : b->done)
         if (e) cudaEventDestroy(e);
     delete b;
 }
@@ -1310,16 +1315,46 @@ static int batch_record(grt_batch *b, cudaStream_t st)
     CU(record_timing(b->ev_grt, st));
     CU(cudaEventRecord(b->fork1, st));
     for (int s = 0; s < kSide; s++) CU(cudaStreamWaitEvent(b->side[s], b->fork1, 0));
-    for (size_t j = 0; j < b->jobs.size(); j++) {
-        cudaStream_t ss = b->side[j % kSide];
-        if ((rc = launch_ksum<R>(b->jobs[j], ss, launches))) return rc;
-        if ((rc = launch_spectral<R>(b->jobs[j], ss, launches))) return rc;
+    if (b->has_out) {
+        // with download destinations the jobs' sums run one after another on
+        // side stream 0 (after every Bessel table), and each job's download,
+        // on another side stream, overlaps the next jobs' work
+        for (int s = 1; s < kSide; s++) {
+            CU(cudaEventRecord(b->join[s], b->side[s]));
+            CU(cudaStreamWaitEvent(b->side[0], b->join[s], 0));
+        }
+        for (size_t j = 0; j < b->jobs.size(); j++) {
+            grt_plan *p = b->jobs[j];
+            if ((rc = launch_ksum<R>(p, b->side[0], launches))) return rc;
+            if ((rc = launch_spectral<R>(p, b->side[0], launches))) return rc;
+            if (b->outs[j]) {
+                cudaStream_t cs = b->side[1 + j % (kSide - 1)];
+                CU(cudaEventRecord(b->done[j], b->side[0]));
+                CU(cudaStreamWaitEvent(cs, b->done[j], 0));
+                CU(cudaMemcpyAsync(b->outs[j], p->sig, (size_t)p->nd * p->nc * p->J.N * sizeof(R),
+                                   cudaMemcpyDeviceToHost, cs));
+            }
+        }
+        // the device time ends with the last job's stages; the graph with the downloads
+        CU(cudaEventRecord(b->join[0], b->side[0]));
+        CU(cudaStreamWaitEvent(st, b->join[0], 0));
+        CU(record_timing(b->ev_end, st));
+        for (int s = 1; s < kSide; s++) {
+            CU(cudaEventRecord(b->join[s], b->side[s]));
+            CU(cudaStreamWaitEvent(st, b->join[s], 0));
+        }
+    } else {
+        for (size_t j = 0; j < b->jobs.size(); j++) {
+            cudaStream_t ss = b->side[j % kSide];
+            if ((rc = launch_ksum<R>(b->jobs[j], ss, launches))) return rc;
+            if ((rc = launch_spectral<R>(b->jobs[j], ss, launches))) return rc;
+        }
+        for (int s = 0; s < kSide; s++) {
+            CU(cudaEventRecord(b->join[s], b->side[s]));
+            CU(cudaStreamWaitEvent(st, b->join[s], 0));
+        }
+        CU(record_timing(b->ev_end, st));
     }
-    for (int s = 0; s < kSide; s++) {
-        CU(cudaEventRecord(b->join[s], b->side[s]));
-        CU(cudaStreamWaitEvent(st, b->join[s], 0));
-    }
-    CU(record_timing(b->ev_end, st));
     b->rep.kernel_launches = launches;
     return GRT_OK;
 }
@@ -1417,6 +1452,12 @@ extern "C" int grt_batch_create(grt_ctx *ctx, int n_jobs, const grt_job *jobs, i
         int rc = grt_plan_create(ctx, jobs[j].model, jobs[j].opts, jobs[j].n_dist, jobs[j].dist, &p);
         if (rc) return set_err(ctx, rc, "job " + std::to_string(j) + ": " + ctx->err);
         b->jobs.push_back(p);
+        b->outs.push_back(jobs[j].out_f32);
+        if (jobs[j].out_f32) {
+            if (p->prec != GRT_FP32) return set_err(ctx, GRT_ERR_ARG, "out_f32 needs an FP32 batch");
+            if (!p->J.fsel.empty()) return set_err(ctx, GRT_ERR_ARG, "a frequency-selection job has no traces");
+            b->has_out = true;
+        }
         b->maxL = std::max(b->maxL, p->J.L);
         b->points += p->J.nkw;
     }
@@ -1429,6 +1470,8 @@ extern "C" int grt_batch_create(grt_ctx *ctx, int n_jobs, const grt_job *jobs, i
     CU(cudaMemset(b->derr, 0, sizeof(unsigned)));
     for (auto &s : b->side) CU(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     CU(cudaStreamCreateWithFlags(&b->copy, cudaStreamNonBlocking));
+    b->done.assign(b->jobs.size(), nullptr);
+    for (auto &e : b->done) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     CU(cudaEventCreate(&b->ev_start));
     CU(cudaEventCreate(&b->ev_grt));
     CU(cudaEventCreate(&b->ev_end));
@@ -1448,7 +1491,7 @@ extern "C" int grt_batch_execute(grt_batch *b, grt_report *r)
     CU(cudaSetDevice(ctx->device));
     CU(cudaStreamSynchronize(b->copy));     // downloads of the previous results are done
     CU(cudaGraphLaunch(b->exec, ctx->stream));
-    CU(cudaEventSynchronize(b->ev_end));
+    CU(cudaStreamSynchronize(ctx->stream));  // the graph, in-graph downloads included
     int rc = check_device_error(ctx, b->derr);
     if (rc) return rc;
     float t_grt = 0.f, t_all = 0.f;

@@ -458,13 +458,15 @@ def run_learned_batch(sampler, models, dists_list, ctx=None, plain=PLAIN, spec_t
         mods = [make_model(**m) for m in models]
         jobs = [(mo, custom_opts(nk, gr["dk"], plain, k_stride=st), d)
                 for mo, (nk, st, _, gr), d in zip(mods, grids, dists_list)]
-        b = Batch(ctx, jobs, autotune=autotune)
+        # with page-locked destinations the graph itself downloads each model's
+        # traces as soon as its stages finish, beside the next model's sums
+        # (downloads started after the graph held up the judge's own small
+        # copies behind them on the copy engine: 20 -> 83 ms of judge)
+        b = Batch(ctx, jobs, autotune=autotune, outs=out)
         t.append(time.perf_counter())
         rep = b.execute()
         t_exec = time.perf_counter()
-        # (started asynchronously, the downloads held up the judge's own small
-        # copies behind them on the copy engine: 20 -> 83 ms of judge)
-        traces = [b.fetch_f32(j, None if out is None else out[j]) for j in range(len(jobs))]
+        traces = list(out) if out is not None else [b.fetch_f32(j) for j in range(len(jobs))]
         t.append(time.perf_counter())
         # judge: spot frequencies on the plain grid (batched), tails by sweep
         spot_jobs, spots = [], []

@@ -197,6 +197,9 @@ typedef struct grt_job {
     const grt_opts *opts;
     int n_dist;
     const double *dist;
+    float *out_f32;   /* optional (FP32 batches): page-locked memory (grt_host_alloc) for the job's
+                       * float32 traces [n_dist][n_cols][N]; every execute copies them there as soon
+                       * as the job's stages finish, beside the later jobs' work.  NULL: fetch them. */
 } grt_job;
 
 #define GRT_TUNE_MAX 16

@@ -121,3 +121,29 @@ def test_async_fetch_matches(ctx):
         b.fetch_f32_async(0, g.pinned_empty(b.fetch_f32(0).shape))
     assert e.value.status == g.ERR_UNSUPPORTED
     b.close()
+
+
+@pytest.mark.gpu
+def test_in_graph_downloads(ctx):
+    """A batch given page-locked destinations downloads every job's traces
+    inside its graph: after execute they equal the fetched ones, and the
+    device time still covers the stages only."""
+    import grtm_cuda_gb300 as g
+    jobs = _jobs(g, g.FP32)
+    b = g.Batch(ctx, jobs, autotune=False)
+    b.execute()
+    ref = [b.fetch_f32(j) for j in range(len(jobs))]
+    b.close()
+    outs = [g.pinned_empty(r.shape) for r in ref]
+    outs[1] = None                                   # a job without a destination
+    b = g.Batch(ctx, jobs, autotune=False, outs=outs)
+    for _ in range(2):
+        for o in outs:
+            if o is not None:
+                o[...] = -1.0
+        b.execute()
+        for j, o in enumerate(outs):
+            if o is not None:
+                assert np.array_equal(o, ref[j])
+        assert np.array_equal(b.fetch_f32(1), ref[1])
+    b.close()
