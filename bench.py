@@ -1,6 +1,6 @@
 """Green's-function throughput on one GB300 (and N independent replicas).
 
-Default workload ("config5", one step = one batch): 2 held-out seeded crustal
+Default workload ("batch40", one step = one batch): 2 held-out seeded crustal
 models of 40 layers over a half-space (thickness U(0.5, 5) km, Vp 2.5 -> 8.0
 km/s linear plus N(0, 0.15), Vs = Vp / U(1.65, 1.85), Gardner density, Qs
 U(50, 300), Qp = 2 Qs), double-couple source at U(1, 30) km, 1000 receivers
@@ -25,9 +25,11 @@ Arms (all FP32 arithmetic, checked against the FP64 path of the same method):
          judge, fallback and the download of every trace (float32, into
          page-locked host arrays allocated once), per step.
 
-Other cases: --case config2 (one 20-layer model, 200 receivers 5-300 km, nt
-4096, nk 16384) and --case config1 (4 layers, 10 receivers) time the
-single-model path.
+Other cases: --case crust20 (one 20-layer model, 200 receivers 5-300 km, nt
+4096, nk 16384), --case crust4 (4 layers, 10 receivers) and --case crust40s
+(one 40-layer model, 64 receivers, nt 1024, nk 4096: the small profiling
+case) time the single-model path; --case uneven256 times 256 uneven models
+in batches; --case tile times the tensor-core wavenumber sum alone.
 
 Launch: python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 (for N > 1 under torch.distributed.run: every rank runs its own seeded
@@ -51,12 +53,12 @@ F_SRC_TENSOR = 710.0
 F_SRC_SINGLE = 449.0
 
 
-WORKLOAD = dict(dt=0.05, log2n=12, t0=0.0, taper=0.3, sigma_factor=np.pi, nk=16384)
-WORKLOAD1 = dict(dt=0.1, log2n=10, t0=0.0, taper=0.3, sigma_factor=np.pi, nk=4096)
-WORKLOAD3S = dict(dt=0.05, log2n=10, t0=0.0, taper=0.3, sigma_factor=np.pi, nk=4096)
+WORKLOAD_CRUST20 = dict(dt=0.05, log2n=12, t0=0.0, taper=0.3, sigma_factor=np.pi, nk=16384)
+WORKLOAD_CRUST4 = dict(dt=0.1, log2n=10, t0=0.0, taper=0.3, sigma_factor=np.pi, nk=4096)
+WORKLOAD_CRUST40S = dict(dt=0.05, log2n=10, t0=0.0, taper=0.3, sigma_factor=np.pi, nk=4096)
 
 
-def config5_models(rank, n_models, n_receivers):
+def heldout_models(rank, n_models, n_receivers):
     """Held-out models (seeds the sampler was not trained on) and receivers."""
     from grtm_cuda_gb300 import synth
     out = []
@@ -186,31 +188,71 @@ def measured_peaks():
         return {}
 
 
-def cpu_baseline(mk, dists, kw, budget_s=12.0, n_models=1, fix=None):
+class CpuSample:
     """The oracle (the reference's algorithm restated in C, all host cores) on a
-    bounded sample of the same job: a band of frequencies in the middle of
-    the spectrum, scaled to the whole job (and to n_models models)."""
-    from oracle import oracle as O
-    O.build()
-    job = O.model(mk["ztop"], mk["vp"], mk["vs"], mk["rho"], mk["qp"], mk["qs"], mk["hs"], mk["hr"], mk["src_type"])
-    O.setup(job, kw["dt"], kw["log2n"], kw["t0"], kw["taper"], kw["sigma_factor"], O.K_FIXED, kw["nk"],
-            fix=O.FIX_ALL if fix is None else fix)
-    cores = os.cpu_count() or 1
-    nw = job.nw
-    # calibrate on one frequency, then size the sample to the budget
-    t = time.time()
-    O.run_band(job, dists, nw // 2, nw // 2 + 1, cores)
-    t1 = time.time() - t
-    nf = int(max(1, min(nw, budget_s / max(t1, 1e-3))))
-    iw0 = (nw - nf) // 2
-    t = time.time()
-    O.run_band(job, dists, iw0, iw0 + nf, cores)
-    el = time.time() - t
-    full = el * nw / nf
-    return {"value": len(dists) / full, "unit": "traces/s", "cores": cores,
-            "kind": "port",
-            "sample": f"{nf} of {nw} frequencies x {kw['nk']} wavenumbers x {len(dists)} receivers of one model "
-                      f"({el:.1f} s), scaled to the whole job ({full:.0f} s per model; every model costs the same)"}
+    bounded sample of one job: a band of frequencies in the middle of the
+    spectrum, timed and scaled to the whole job (every frequency of a fixed
+    wavenumber grid costs the same)."""
+
+    def __init__(self, mk, dists, kw, fix=None):
+        from oracle import oracle as O
+        O.build()
+        self.O = O
+        self.job = O.model(mk["ztop"], mk["vp"], mk["vs"], mk["rho"], mk["qp"], mk["qs"], mk["hs"], mk["hr"],
+                           mk["src_type"])
+        O.setup(self.job, kw["dt"], kw["log2n"], kw["t0"], kw["taper"], kw["sigma_factor"], O.K_FIXED, kw["nk"],
+                fix=O.FIX_ALL if fix is None else fix)
+        self.dists = dists
+        self.nk = kw["nk"]
+        self.cores = os.cpu_count() or 1
+        self.nw = self.job.nw
+
+    def time_band(self, nf):
+        """Seconds for nf frequencies in the middle of the spectrum."""
+        iw0 = (self.nw - nf) // 2
+        t = time.time()
+        self.O.run_band(self.job, self.dists, iw0, iw0 + nf, self.cores)
+        return time.time() - t
+
+    def frequencies_for(self, budget_s):
+        """Frequencies one sample of about budget_s seconds takes (calibrated on one)."""
+        return int(max(1, min(self.nw, budget_s / max(self.time_band(1), 1e-3))))
+
+    def rate(self, nf, el):
+        """Traces/s of the whole job from nf frequencies timed at el seconds."""
+        return len(self.dists) / (el * self.nw / nf)
+
+    def describe(self, nf, el, value):
+        full = el * self.nw / nf
+        return {"value": value, "unit": "traces/s", "cores": self.cores, "kind": "port",
+                "sample": f"{nf} of {self.nw} frequencies x {self.nk} wavenumbers x {len(self.dists)} receivers of "
+                          f"one model ({el:.1f} s), scaled to the whole job ({full:.0f} s per model; every model "
+                          "costs the same)"}
+
+
+def cpu_baseline(mk, dists, kw, budget_s=12.0, fix=None):
+    """One bounded oracle sample of the job (about budget_s seconds), as the
+    bench line's cpu_baseline."""
+    s = CpuSample(mk, dists, kw, fix)
+    nf = s.frequencies_for(budget_s)
+    el = s.time_band(nf)
+    return s.describe(nf, el, s.rate(nf, el))
+
+
+def reference_steps(args, mk, dists, kw, fix=None):
+    """The reference arm: args.warmup untimed one-frequency runs, then exactly
+    args.steps timed samples of the oracle on all host cores, each a band of
+    frequencies sized so the whole run stays within about two minutes.
+    Returns (median traces/s, the cpu_baseline description)."""
+    s = CpuSample(mk, dists, kw, fix)
+    for _ in range(args.warmup):
+        s.time_band(1)
+    steps = max(1, args.steps)
+    nf = s.frequencies_for(min(10.0, max(2.0, 100.0 / steps)))
+    els = [s.time_band(nf) for _ in range(steps)]
+    vals = [s.rate(nf, el) for el in els]
+    v = float(np.median(vals))
+    return v, s.describe(nf, float(np.median(els)), v)
 
 
 def rel_errors(a, ref):
@@ -220,7 +262,7 @@ def rel_errors(a, ref):
 
 
 # DRAM bytes per (w,k) point of the FP32 GRT kernel (tensor-core operand layout), from one ncu capture
-# of the small 40-layer case: 5.7 MB read + 181.3 MB written for 2.10 M points (profiles/grt_point_config3s.md)
+# of the small 40-layer case: 5.7 MB read + 181.3 MB written for 2.10 M points (profiles/grt_point_crust40s.md)
 GRT_DRAM_BYTES_PER_POINT = (5.668864e6 + 181.344512e6) / (512 * 4096)
 
 
@@ -239,7 +281,7 @@ def grt_roofline(n_wk_by_layers, ms, fp32_peak):
 
 def bench_batch(args, ws, rank, local, td):
     kw = dict(dt=0.05, log2n=13, t0=0.0, taper=0.3, sigma_factor=np.pi, nk=32768)
-    work = config5_models(rank, args.models, args.receivers)
+    work = heldout_models(rank, args.models, args.receivers)
     ntr = sum(len(d) for _, d in work)
     config = {"workload": f"GRT Green's functions: {args.models} held-out seeded 40-layer crusts over a half-space, "
                           f"double-couple source U(1, 30) km, {args.receivers} receivers 1-500 km each, nt 8192, "
@@ -252,20 +294,16 @@ def bench_batch(args, ws, rank, local, td):
     if args.impl == "reference":
         if rank == 0:
             mk, d = work[0]
-            kw1 = dict(kw)
             from oracle import oracle as O
-            vals, cb = [], None
-            for _ in range(max(1, min(args.steps, 3))):
-                cb = cpu_baseline(mk, d, kw1, budget_s=10.0, fix=O.FIX_ALL)
-                vals.append(cb["value"])
-            v = float(np.median(vals))
+            v, cb = reference_steps(args, mk, d, kw, fix=O.FIX_ALL)
             out = {"impl": "reference", "metric": metric, "value": v, "unit": "traces/s", "n_gpus": args.gpus,
-                   "steps": len(vals), "warmup": 0, "ms_per_step": 1000.0 * ntr / v, "higher_is_better": True,
-                   "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded)",
-                   "config": config, "cpu_baseline": dict(cb, value=v),
+                   "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * ntr / v,
+                   "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+                   "data": "synthetic (seeded)", "config": config, "cpu_baseline": cb,
                    "e2e": {"value": v, "unit": "traces/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
                    "note": "the reference has no CPU implementation of the GRT path; this times the FP64 C "
-                           "restatement of its algorithm (oracle/) on all host cores"}
+                           "restatement of its algorithm (oracle/) on all host cores, each step a bounded "
+                           "sample of the workload (cpu_baseline.sample) scaled to the whole step"}
             print(json.dumps(out))
         barrier(td)
         return
@@ -401,14 +439,14 @@ def bench_batch(args, ws, rank, local, td):
     barrier(td)
 
 
-def bench_config4(args, ws, rank, local, td):
+def bench_uneven(args, ws, rank, local, td):
     """Batched uneven instances: seeded models with 3-60 layers, source U(1,30)
     km, 16-512 receivers in 5-400 km, N in {1024, 2048, 4096} at dt 0.05 s,
     the reference's k rule, run as batches of up to --chunk models (one CUDA
     graph each) against the same jobs as one plan at a time."""
     import grtm_cuda_gb300 as g
     from grtm_cuda_gb300 import synth
-    work = synth.config4_models(4000 + rank, args.models)
+    work = synth.uneven_models(4000 + rank, args.models)
     chunk = max(1, args.chunk)
     config = {"workload": f"{args.models} seeded uneven models: 3-60 layers, source U(1, 30) km, random double "
                           "couple, 16-512 receivers 5-400 km, nt 1024/2048/4096, dt 0.05 s, sigma pi/T, reference "
@@ -421,11 +459,14 @@ def bench_config4(args, ws, rank, local, td):
         if rank == 0:
             w = work[0]
             kw = dict(dt=0.05, log2n=w["log2n"], t0=0.0, taper=0.3, sigma_factor=np.pi, nk=8192)
-            cb = cpu_baseline(w["model"], w["dists"], kw, budget_s=10.0)
-            print(json.dumps({"impl": "reference", "metric": metric, "value": cb["value"], "unit": "traces/s",
-                              "n_gpus": args.gpus, "config": config, "cpu_baseline": cb,
-                              "e2e": {"value": cb["value"], "unit": "traces/s", "h2d_bytes_per_step": 0,
-                                      "d2h_bytes_per_step": 0}}))
+            v, cb = reference_steps(args, w["model"], w["dists"], kw)
+            print(json.dumps({"impl": "reference", "metric": metric, "value": v, "unit": "traces/s",
+                              "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                              "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+                              "data": "synthetic (seeded)", "config": config, "cpu_baseline": cb,
+                              "e2e": {"value": v, "unit": "traces/s", "h2d_bytes_per_step": 0,
+                                      "d2h_bytes_per_step": 0},
+                              "note": "model 0 of the set on a fixed grid of 8192 wavenumbers"}))
         barrier(td)
         return
     g.lib()
@@ -498,26 +539,26 @@ def bench_config4(args, ws, rank, local, td):
 def bench_single(args, ws, rank, local, td):
     """One model per step through a plan (the single-model path)."""
     from grtm_cuda_gb300 import synth
-    if args.case == "config3s":
-        kw = dict(WORKLOAD3S)
-        mk, dists = synth.config3_model(1234 + rank, n_receivers=64)
+    if args.case == "crust40s":
+        kw = dict(WORKLOAD_CRUST40S)
+        mk, dists = synth.crust40_model(1234 + rank, n_receivers=64)
         config = {"workload": "GRT Green's functions, small profiling case: seeded 40-layer crust over a half-space, "
                               "double-couple source at 15 km, 64 receivers 1-500 km, nt 1024, dt 0.05 s, nk 4096, "
                               "sigma=pi/T",
                   "traces_per_step": len(dists), "cols_per_trace": 20, "nt": 1024, "nk": kw["nk"], "layers": 42,
                   "receivers": len(dists), "l2": "inputs larger than L2 (coefficients 268 MB per step)",
                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}
-    elif args.case == "config1":
-        kw = dict(WORKLOAD1)
-        mk, dists = synth.config1_model()
+    elif args.case == "crust4":
+        kw = dict(WORKLOAD_CRUST4)
+        mk, dists = synth.crust4_model()
         config = {"workload": "GRT Green's functions: 4 layers over a half-space, double-couple source at 10 km, "
                               "10 receivers 10-100 km, nt 1024, dt 0.1 s, nk 4096, sigma=pi/T",
                   "traces_per_step": len(dists), "cols_per_trace": 20, "nt": 1024, "nk": kw["nk"], "layers": 6,
                   "receivers": len(dists), "l2": "inputs larger than L2 (per-(w,k) coefficients 134 MB per step)",
                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}
     else:
-        kw = dict(WORKLOAD)
-        mk, dists = synth.config2_model(1234 + rank)
+        kw = dict(WORKLOAD_CRUST20)
+        mk, dists = synth.crust20_model(1234 + rank)
         config = {"workload": "GRT Green's functions: seeded 20-layer crust over a half-space, double-couple "
                               "source at 15 km, 200 receivers 5-300 km, nt 4096, dt 0.05 s, nk 16384, sigma=pi/T",
                   "traces_per_step": len(dists), "cols_per_trace": 20, "nt": 4096, "nk": kw["nk"], "layers": 21,
@@ -527,19 +568,15 @@ def bench_single(args, ws, rank, local, td):
 
     if args.impl == "reference":
         if rank == 0:
-            cb = cpu_baseline(mk, dists, kw, budget_s=20.0)
-            steps = []
-            for _ in range(max(1, min(args.steps, 3))):
-                steps.append(cpu_baseline(mk, dists, kw, budget_s=8.0)["value"])
-            v = float(np.median(steps))
+            v, cb = reference_steps(args, mk, dists, kw)
             out = {"impl": "reference", "metric": metric, "value": v, "unit": "traces/s", "n_gpus": args.gpus,
-                   "steps": len(steps), "warmup": 1, "ms_per_step": 1000.0 * len(dists) / v,
+                   "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * len(dists) / v,
                    "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
-                   "data": "synthetic (seeded)", "config": config,
-                   "cpu_baseline": dict(cb, value=v),
+                   "data": "synthetic (seeded)", "config": config, "cpu_baseline": cb,
                    "e2e": {"value": v, "unit": "traces/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
                    "note": "the reference has no CPU implementation of the GRT path; this times the FP64 C "
-                           "restatement of its algorithm (oracle/) on all host cores"}
+                           "restatement of its algorithm (oracle/) on all host cores, each step a bounded "
+                           "sample of the workload (cpu_baseline.sample) scaled to the whole step"}
             print(json.dumps(out))
         barrier(td)
         return
@@ -648,7 +685,7 @@ def bench_tile(args, ws, rank, local, td):
     and its tensor-core rate (the profiling case of that kernel)."""
     import grtm_cuda_gb300 as g
     from grtm_cuda_gb300 import learned
-    (m, d), = config5_models(rank, 1, args.receivers)
+    (m, d), = heldout_models(rank, 1, args.receivers)
     sel = np.linspace(1, 4095, 64).astype(np.int32)
     ctx = g.Context(local)
     plan = g.Plan(ctx, g.make_model(**m), learned.plain_opts(freq_sel=sel), d)
@@ -688,25 +725,26 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
-    ap.add_argument("--case", default="config5",
-                    choices=["config5", "config4", "config2", "config1", "config3s", "tile"],
-                    help="config5: batch of held-out 40-layer models (the metric's workload); config2: one "
-                         "20-layer model, 200 receivers; config1: 4 layers, 10 receivers; config3s: one 40-layer "
+    ap.add_argument("--case", default="batch40",
+                    choices=["batch40", "uneven256", "crust20", "crust4", "crust40s", "tile"],
+                    help="batch40: batch of held-out 40-layer models (the metric's workload); crust20: one "
+                         "20-layer model, 200 receivers; crust4: 4 layers, 10 receivers; crust40s: one 40-layer "
                          "model, 64 receivers, nt 1024, nk 4096 (small profiling case); tile: the tensor-core "
-                         "wavenumber sum on one 64-frequency tile of config5's model 0")
-    ap.add_argument("--models", type=int, default=2, help="config5: models per batch")
-    ap.add_argument("--receivers", type=int, default=1000, help="config5: receivers per model")
-    ap.add_argument("--chunk", type=int, default=32, help="config4: models per batch")
+                         "wavenumber sum on one 64-frequency tile of batch40's model 0; uneven256: 256 uneven models "
+                         "in batches")
+    ap.add_argument("--models", type=int, default=2, help="batch40: models per batch")
+    ap.add_argument("--receivers", type=int, default=1000, help="batch40: receivers per model")
+    ap.add_argument("--chunk", type=int, default=32, help="uneven256: models per batch")
     args = ap.parse_args()
     ws, rank, local, td = dist_setup()
-    if args.case == "config5":
+    if args.case == "batch40":
         bench_batch(args, ws, rank, local, td)
     elif args.case == "tile":
         bench_tile(args, ws, rank, local, td)
-    elif args.case == "config4":
+    elif args.case == "uneven256":
         if args.models == 2:
             args.models = 256
-        bench_config4(args, ws, rank, local, td)
+        bench_uneven(args, ws, rank, local, td)
     else:
         bench_single(args, ws, rank, local, td)
 

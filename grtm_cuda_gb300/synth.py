@@ -34,7 +34,7 @@ def crust(rng, n_layers, hs, src_type=1):
                 src_type=src_type)
 
 
-def config1_model(seed=0):
+def crust4_model(seed=0):
     """Four layers over a half-space (tops 0/2/10/20/35 km), Vp 3.0/5.8/6.5/7.0/8.0,
     Vs = Vp/1.73, rho = 1.74 Vp^0.25, Qp 200, Qs 100; source 10 km; 10
     receivers at 10..100 km."""
@@ -45,14 +45,14 @@ def config1_model(seed=0):
     return m, np.arange(10.0, 101.0, 10.0)
 
 
-def config2_model(seed):
+def crust20_model(seed):
     """20 layers + half-space, source 15 km, 200 receivers log-spaced 5-300 km."""
     rng = np.random.default_rng(seed)
     m = crust(rng, 20, 15.0)
     return m, np.logspace(np.log10(5.0), np.log10(300.0), 200)
 
 
-def config3_model(seed, n_receivers=1000, hs=None):
+def crust40_model(seed, n_receivers=1000, hs=None):
     """40 layers + half-space, receivers uniform in 1-500 km (sorted); source
     15 km unless given."""
     rng = np.random.default_rng(seed)
@@ -60,7 +60,7 @@ def config3_model(seed, n_receivers=1000, hs=None):
     return m, np.sort(rng.uniform(1.0, 500.0, n_receivers))
 
 
-def config4_models(seed, n_models=256):
+def uneven_models(seed, n_models=256):
     """Uneven batch: layer counts U{3..60}, source depth U(1, 30) km, random
     double-couple (strike, dip, rake), 16-512 receivers in 5-400 km, N in
     {1024, 2048, 4096} samples at dt 0.05 s.  Yields dicts with keys model,

@@ -31,7 +31,7 @@ extern "C" {
 #define GRT_ERR_CUDA 5         /* CUDA runtime error (message in grt_last_error) */
 #define GRT_ERR_NOMEM 6        /* device or host allocation failed */
 #define GRT_ERR_TIMEOUT 7      /* a bounded device wait gave up */
-#define GRT_ERR_UNSUPPORTED 8  /* size beyond what this build handles */
+#define GRT_ERR_UNSUPPORTED 8  /* size beyond what this library handles */
 
 /* wavenumber grids */
 #define GRT_K_REFERENCE 0      /* per-frequency k_max rule of the reference, dk = 2 pi / L */

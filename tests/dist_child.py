@@ -13,7 +13,7 @@ import bench  # noqa: E402
 
 def main():
     ws, rank, local, td = bench.dist_setup()
-    work = bench.config5_models(rank, 2, 3)
+    work = bench.heldout_models(rank, 2, 3)
     seeds = [float(m["hs"]) for m, _ in work]
     bench.barrier(td)
     t = bench.allmax(td, 1.0 + rank)

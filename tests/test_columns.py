@@ -14,7 +14,7 @@ FIXC = O.FIX_ALL | O.STABLE | O.FIX_COLS
 
 def _model():
     from grtm_cuda_gb300 import synth
-    m, _ = synth.config1_model()
+    m, _ = synth.crust4_model()
     return m
 
 

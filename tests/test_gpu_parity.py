@@ -52,7 +52,7 @@ def _oracle_traces(oracle, hs, hr, st, fix, kw, dists):
 
 GEOMETRIES = [
     # (hs, hr, src_type, fix): receiver above / in / below the source layer
-    (10.0005, 0.0, 1, 0),    # r < s, moment tensor (config-1 geometry)
+    (10.0005, 0.0, 1, 0),    # r < s, moment tensor (4-layer crust geometry)
     (10.0005, 0.0, 0, 0),    # r < s, single force
     (5.0, 3.0, 1, 0),        # same layer, receiver above the source
     (5.0, 4.0, 0, 7),        # same layer, receiver below the source
@@ -77,8 +77,8 @@ def test_geometries_fp64_and_fp32(g, ctx, oracle, hs, hr, st, fix):
         assert rel(t32[:, c], ref[:, c]) < 5e-5, c
 
 
-def test_config1_double_couple_full_size(g, ctx, oracle):
-    """Config-1 grid: 10 receivers 10-100 km, nt 1024, dt 0.1, nk 4096,
+def test_crust4_double_couple_full_size(g, ctx, oracle):
+    """4-layer crust, full grid: 10 receivers 10-100 km, nt 1024, dt 0.1, nk 4096,
     sigma = pi/T; the source is moved 0.5 m off the 10 km interface."""
     kw = dict(dt=0.1, log2n=10, t0=0.0, taper=0.3, sigma_factor=np.pi, k_mode=g.K_FIXED, nk_fixed=4096)
     dists = np.arange(10.0, 101.0, 10.0)
@@ -167,7 +167,7 @@ def test_green_reports_bad_input(g, tmp_path):
 
 
 def test_reference_k_rule_grid(g, ctx, oracle):
-    """Ragged per-frequency k_max grid (the reference's rule) on the config-1
+    """Ragged per-frequency k_max grid (the reference's rule) on the 4-layer crust
     model: same (w,k) count as the oracle and the same traces."""
     kw = dict(dt=0.1, log2n=9, t0=0.0, taper=0.3, sigma_factor=2.0, k_mode=g.K_REFERENCE, nk_fixed=0)
     dists = [15.0, 60.0]

@@ -60,7 +60,7 @@ def test_features_finite_on_generators():
             m = synth.crust(np.random.default_rng(seed), nl, 1.0 + 5 * seed)
             f = learned.layer_features(m)
             assert f.shape == (12,) and np.all(np.isfinite(f))
-    m, _ = synth.config1_model()
+    m, _ = synth.crust4_model()
     assert np.all(np.isfinite(learned.layer_features(m)))
 
 

@@ -42,7 +42,7 @@ def job():
     import grtm_cuda_gb300 as g
     from grtm_cuda_gb300 import synth
     ctx = g.Context()
-    m, _ = synth.config1_model()
+    m, _ = synth.crust4_model()
     d = np.array([12.0, 40.0, 77.0])
     o = g.make_opts(0.1, 10, sigma_factor=math.pi, k_mode=g.K_FIXED, nk_fixed=2048, fix=g.FIX_ALL)
     p = g.Plan(ctx, g.make_model(**m), o, d)
@@ -84,7 +84,7 @@ def test_synthesis_linear_and_rotation_invariant(job):
 def test_synthesis_needs_moment_tensor(job):
     g, p, tr, o = job
     from grtm_cuda_gb300 import synth
-    m, _ = synth.config1_model()
+    m, _ = synth.crust4_model()
     m = dict(m, src_type=0)
     ctx = p.ctx
     ps = g.Plan(ctx, g.make_model(**m), o, [10.0])
