@@ -188,7 +188,7 @@ int job_setup(Job &J, double dt, int log2n, double t0, double taper, double sigm
             if (k_stride[iw] < 1 || k_stride[iw] > 64) { err = "k stride must be in 1..64"; return kErrArg; }
             J.ks[iw] = k_stride[iw];
         }
-        if ((long long)(nk - 1) * J.ks[iw] + 1 > (1 << 24)) { err = "custom k grid: (nk - 1) * stride too large"; return kErrArg; }
+        if ((long long)(nk - 1) * J.ks[iw] + 1 > (1 << 24)) { err = "k grid: (nk - 1) * stride + 1 beyond 2^24 wavenumbers"; return kErrArg; }
         J.nk[iw] = nk;
         J.koff[iw] = tot;
         tot += nk;
