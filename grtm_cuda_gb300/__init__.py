@@ -19,6 +19,7 @@ OK, ERR_ARG, ERR_IO, ERR_PARSE, ERR_MODEL, ERR_CUDA, ERR_NOMEM, ERR_TIMEOUT, ERR
 K_REFERENCE, K_FIXED, K_CUSTOM = 0, 1, 2
 FP32, FP64 = 0, 1
 FIX_RLAYER, FIX_REXUT, FIX_DZ, FIX_COLS = 1, 2, 4, 8
+FIX_SHSRC = 16   # moment-tensor SH source terms with the jump structure of their order
 FIX_ALL = FIX_RLAYER | FIX_REXUT | FIX_DZ
 
 _dp = ctypes.POINTER(ctypes.c_double)

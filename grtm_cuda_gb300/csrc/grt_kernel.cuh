@@ -618,8 +618,16 @@ __device__ __forceinline__ void grt_point(const GrtArgs<R> &A, const LayerW<R> *
         mv2(Wp, s0a, s0b, &q0a, &q0b);
         mv2(Wm, s1a, s1b, &q1a, &q1b);
         mv2(Wp, s2a, s2b, &q2a, &q2b);
+        // green.cu:1409-1412 give the m = 1 and m = 2 SH terms one factor;
+        // GRT_FIX_SHSRC gives m = 1 a displacement jump's (1 - e R e up) and
+        // m = 2 a traction jump's (e R e + 1 down), as the P-SV terms have
         C<R> shf = up ? fu : fd - R(1);
-        C<R> h1 = shf * S.v * ssh, h2 = shf * k * ssh;
+        C<R> shf1 = shf, shf2 = shf;
+        if (A.fix & kFixShsrc) {
+            if (up) shf1 = R(2) - fu;
+            else shf2 = fd + R(1);
+        }
+        C<R> h1 = shf1 * S.v * ssh, h2 = shf2 * k * ssh;
         C<R> v0, v1;
         store_q<kTensor>(A, QT_B1, out, y0 * h1);
         store_q<kTensor>(A, QT_B2, out, y0 * h2);

@@ -41,7 +41,7 @@ enum QTensor { QT_B1 = 0, QT_B2, QT_A00, QT_A01, QT_A10, QT_A11, QT_A20, QT_A21,
 enum GrtSpec { kSpecGeneric = 0, kSpecAboveTensor = 1 };
 
 // reference-quirk switches (0 = reproduce the reference)
-enum Fix { kFixRLayer = 1, kFixRexut = 2, kFixDz = 4, kFixCols = 8 };
+enum Fix { kFixRLayer = 1, kFixRexut = 2, kFixDz = 4, kFixCols = 8, kFixShsrc = 16 };
 
 template <typename R>
 struct GrtArgs {

@@ -51,6 +51,12 @@ extern "C" {
                                 * with b1), single force d/dr column 10 with its 1/r, Bessel second
                                 * derivatives from Bessel's equation.  The 30-column layout runs the
                                 * SIMT wavenumber sum. */
+#define GRT_FIX_SHSRC 16       /* moment-tensor SH source terms: the reference (get_src_tensor,
+                                * green.cu:1409-1412) gives the m = 1 and m = 2 SH terms one
+                                * reflection factor; with this bit m = 1 (a jump of the SH
+                                * displacement) takes 1 - e Rdu e above the source and m = 2 (a jump
+                                * of the SH traction) 1 + e Rud e below it, and the moment-tensor
+                                * solution satisfies reciprocity with the single-force one. */
 
 /* A layered model: n_layer layers given by the depth of their top (ztop[0] = 0),
  * the last one being the half-space.  Units: km, km/s, g/cm^3. */

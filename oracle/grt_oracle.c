@@ -584,10 +584,14 @@ static void point_eval(const grto_job *J, const cplx *alpha, const cplx *beta, d
             sd2[i] = wrd1[i][0] * s2[0] + wrd1[i][1] * s2[1];
         }
         cplx shd_fac = sexu[1] * G[s].rud0 * sexu[1] - 1.;
-        shu1 = shu_fac * sv * ssh;
+        /* green.cu:1409-1412 give m = 1 and m = 2 one factor; GRTO_FIX_SHSRC
+         * gives m = 1 a displacement jump's (1 - e R e up) and m = 2 a
+         * traction jump's (e R e + 1 down) */
+        int fsh = (J->fix & GRTO_FIX_SHSRC) != 0;
+        shu1 = (fsh ? 2. - shu_fac : shu_fac) * sv * ssh;
         shd1 = shd_fac * sv * ssh;
         shu2 = shu_fac * k * ssh;
-        shd2 = shd_fac * k * ssh;
+        shd2 = (fsh ? shd_fac + 2. : shd_fac) * k * ssh;
     }
 
     /* receiver side: get_ypars_a_single green.cu:615-939 and
@@ -1001,8 +1005,9 @@ static void point_eval_stable(const grto_job *J, const cplx *alpha, const cplx *
         m2vec(wru0, s1, su1); m2vec(wrd0, s1, sd1);
         m2vec(wru1, s2, su2); m2vec(wrd1, s2, sd2);
         cplx shd_fac = sexu1 * rud0[s] * sexu1 - 1.;
-        shu1 = shu_fac * S->v * ssh; shd1 = shd_fac * S->v * ssh;
-        shu2 = shu_fac * k * ssh; shd2 = shd_fac * k * ssh;
+        int fsh = (J->fix & GRTO_FIX_SHSRC) != 0;   /* as in point_eval */
+        shu1 = (fsh ? 2. - shu_fac : shu_fac) * S->v * ssh; shd1 = shd_fac * S->v * ssh;
+        shu2 = shu_fac * k * ssh; shd2 = (fsh ? shd_fac + 2. : shd_fac) * k * ssh;
     }
     m2_t yu_psv = m2inv(m2add(m2eye(), m2mul(ED, EU), -1));
     m2_t yd_psv = m2inv(m2add(m2eye(), m2mul(EU, ED), -1));

@@ -50,6 +50,15 @@ extern "C" {
  * with the 1/r of its b1 k J1' term; second Bessel derivatives from Bessel's
  * equation instead of dd_besselj (green.cu:1540-1554). */
 #define GRTO_FIX_COLS 16
+/* SH source terms of the moment tensor (get_src_tensor, green.cu:1409-1412):
+ * the reference gives the m = 1 and m = 2 SH terms one reflection factor,
+ * 1 + e Rdu e up and e Rud e - 1 down.  m = 1 (a vertical couple: a jump of
+ * the SH displacement) needs opposite signs up and down, 1 - e Rdu e up;
+ * m = 2 (a jump of the SH traction) the same sign, 1 + e Rud e down -- as the
+ * P-SV terms beside them have (wru0/wrd0 for m = 1, wru1/wrd1 for m = 0, 2).
+ * With this bit the moment-tensor SH coefficients satisfy reciprocity with
+ * the single-force solution. */
+#define GRTO_FIX_SHSRC 32
 
 typedef struct grto_job {
     /* model after source-interface insertion (green.cu:1995-2049) */

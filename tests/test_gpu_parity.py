@@ -77,6 +77,36 @@ def test_geometries_fp64_and_fp32(g, ctx, oracle, hs, hr, st, fix):
         assert rel(t32[:, c], ref[:, c]) < 5e-5, c
 
 
+# moment-tensor columns holding an SH term in the reference layout: b2 in
+# 0, 4, 5 (5 reads b2 for b1) and their d/dr 10, 14, 15; b1 in 1 and 11
+SH_B1_COLS, SH_B2_COLS = (1, 11), (0, 4, 5, 10, 14, 15)
+
+
+@pytest.mark.parametrize("hs,hr", [(10.0005, 0.0), (14.0, 12.0), (5.0, 15.0), (12.0, 14.0)])
+def test_sh_source_fix(g, ctx, oracle, hs, hr):
+    """GRT_FIX_SHSRC on moment-tensor jobs, receiver above the source (surface,
+    same layer) and below it (other layer, same layer): FP64 GPU equals the
+    oracle, FP32 within the regional tolerance (whole job); against the run without the
+    bit only the SH columns of the receiver's side move (b1 above, b2 below)."""
+    kw = dict(dt=0.1, log2n=8, t0=0.0, taper=0.3, sigma_factor=np.pi, k_mode=g.K_FIXED, nk_fixed=1024)
+    dists = [10.0, 35.0, 80.0]
+    ref, job = _oracle_traces(oracle, hs, hr, 1, oracle.FIX_ALL | oracle.FIX_SHSRC, kw, dists)
+    m = g.make_model(TOPS, VP, VS, RHO, QP, QS, hs, hr, 1)
+    t64, _, rep = g.run(m, g.make_opts(precision=g.FP64, fix=g.FIX_ALL | g.FIX_SHSRC, **kw), dists, ctx)
+    assert (rep["s_layer"], rep["r_layer"]) == (job.s_layer, job.r_layer)
+    for c in range(20):
+        assert rel(t64[:, c], ref[:, c]) < 1e-10, c
+    t32, _, _ = g.run(m, g.make_opts(precision=g.FP32, fix=g.FIX_ALL | g.FIX_SHSRC, **kw), dists, ctx)
+    assert rel(t32, ref) < 5e-5
+    plain, _, _ = g.run(m, g.make_opts(precision=g.FP64, fix=g.FIX_ALL, **kw), dists, ctx)
+    moved = SH_B1_COLS if hr < hs else SH_B2_COLS
+    for c in range(20):
+        if c in moved:
+            assert rel(t64[:, c], plain[:, c]) > 1e-3, c
+        else:
+            assert rel(t64[:, c], plain[:, c]) < 1e-13, c
+
+
 def test_crust4_double_couple_full_size(g, ctx, oracle):
     """4-layer crust, full grid: 10 receivers 10-100 km, nt 1024, dt 0.1, nk 4096,
     sigma = pi/T; the source is moved 0.5 m off the 10 km interface."""
