@@ -283,19 +283,21 @@ constexpr __device__ Term kSingleFixTerms[] = {
 };
 
 // corrected moment tensor: 30 columns -- displacement 0-9 (column 5, the m = 1
-// transverse term, with b1 where green.cu:1657 has b2), d/dz 10-19 from the
-// z-derivative coefficients (the block green.cu:1666-1677 writes and then
-// overwrites), d/dr 20-29 (green.cu:1680-1691, column 25 with b1)
+// transverse term, with b1 where green.cu:1657 has b2; the m = 0 radial
+// columns 2, 3 with the radial coefficients a20, a00 where green.cu:1652-1653
+// have the vertical a21, a01), d/dz 10-19 from the z-derivative coefficients
+// (the block green.cu:1666-1677 writes and then overwrites), d/dr 20-29
+// (green.cu:1680-1691, column 25 with b1, 22 and 23 radial)
 constexpr int QTT = QT_N;   // offset of the z-derivative coefficient columns
 constexpr __device__ Pair kTensorFixPairs[] = {
-    {QT_B2, 0, BJ2},   {QT_A20, 1, BJ2D},  {QT_B1, 0, BJ1},    {QT_A10, 1, BJ1D},  {QT_A21, 1, BJ0D},
-    {QT_A01, 1, BJ0D}, {QT_B2, 1, BJ2D},   {QT_A20, 0, BJ2},   {QT_B2, 1, BJ1D},   {QT_A10, 0, BJ1},
+    {QT_B2, 0, BJ2},   {QT_A20, 1, BJ2D},  {QT_B1, 0, BJ1},    {QT_A10, 1, BJ1D},  {QT_A20, 1, BJ0D},
+    {QT_A00, 1, BJ0D}, {QT_B2, 1, BJ2D},   {QT_A20, 0, BJ2},   {QT_B2, 1, BJ1D},   {QT_A10, 0, BJ1},
     {QT_A21, 1, BJ2},  {QT_A11, 1, BJ1},   {QT_A01, 1, BJ0},   {QT_A21, 1, BJ0},   {QT_A20, 2, BJ2DD},
-    {QT_B1, 1, BJ1D},  {QT_A10, 2, BJ1DD}, {QT_A21, 2, BJ0DD}, {QT_A01, 2, BJ0DD}, {QT_B2, 2, BJ2DD},
+    {QT_B1, 1, BJ1D},  {QT_A10, 2, BJ1DD}, {QT_A20, 2, BJ0DD}, {QT_A00, 2, BJ0DD}, {QT_B2, 2, BJ2DD},
     {QT_B2, 2, BJ1DD}, {QT_A21, 2, BJ2D},  {QT_A11, 2, BJ1D},  {QT_A01, 2, BJ0D},  {QT_A21, 2, BJ0D},
     // 25..38: z-derivative coefficients
     {QTT + QT_B2, 0, BJ2},   {QTT + QT_A20, 1, BJ2D}, {QTT + QT_B1, 0, BJ1},  {QTT + QT_A10, 1, BJ1D},
-    {QTT + QT_A21, 1, BJ0D}, {QTT + QT_A01, 1, BJ0D}, {QTT + QT_B2, 1, BJ2D}, {QTT + QT_A20, 0, BJ2},
+    {QTT + QT_A20, 1, BJ0D}, {QTT + QT_A00, 1, BJ0D}, {QTT + QT_B2, 1, BJ2D}, {QTT + QT_A20, 0, BJ2},
     {QTT + QT_B1, 1, BJ1D},  {QTT + QT_A10, 0, BJ1},  {QTT + QT_A21, 1, BJ2}, {QTT + QT_A11, 1, BJ1},
     {QTT + QT_A01, 1, BJ0},  {QTT + QT_A21, 1, BJ0},
     // 39: b1 k^2 J1''

@@ -48,9 +48,10 @@ extern "C" {
 #define GRT_FIX_DZ 4           /* d/dz terms without the doubled factor / reused product */
 #define GRT_FIX_COLS 8         /* corrected output columns: moment tensor 30 defined columns (0-9
                                 * displacement, 10-19 d/dz, 20-29 d/dr; the m = 1 transverse terms
-                                * with b1), single force d/dr column 10 with its 1/r, Bessel second
-                                * derivatives from Bessel's equation.  The 30-column layout runs the
-                                * SIMT wavenumber sum. */
+                                * with b1; the m = 0 radial terms 2, 3 with the radial coefficients
+                                * where green.cu:1652-1653 take the vertical ones), single force d/dr
+                                * column 10 with its 1/r, Bessel second derivatives from Bessel's
+                                * equation.  The 30-column layout runs the SIMT wavenumber sum. */
 #define GRT_FIX_SHSRC 16       /* moment-tensor SH source terms: the reference (get_src_tensor,
                                 * green.cu:1409-1412) gives the m = 1 and m = 2 SH terms one
                                 * reflection factor; with this bit m = 1 (a jump of the SH

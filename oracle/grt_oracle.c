@@ -1149,8 +1149,13 @@ static void integrand(int src_type, int fix, const ypar_t *p, double k, double d
         cplx b1u = cf ? p->b1 : p->b2, b1tu = cf ? p->b1t : p->b2t;   /* green.cu:1657, 1672, 1686 use b2 */
         out[0] = p->b2 * 2.0 * j2 / dist + p->a2[0] * k * j2d;
         out[1] = p->b1 * j1 / dist + p->a1[0] * k * j1d;
-        out[2] = p->a2[1] * k * j0d;
-        out[3] = p->a0[1] * k * j0d;
+        /* green.cu:1652-1653 build the m = 0 radial terms from the vertical
+         * coefficients (a2[1], a0[1]); GRTO_FIX_COLS takes the radial ones, as
+         * every other radial column does (the free surface's zero shear
+         * traction, d/dz a[0] = k a[1] at z = 0, shows a[0] radial) */
+        const cplx *a2h = cf ? &p->a2[0] : &p->a2[1], *a0h = cf ? &p->a0[0] : &p->a0[1];
+        out[2] = *a2h * k * j0d;
+        out[3] = *a0h * k * j0d;
         out[4] = p->b2 * k * j2d + 2.0 * p->a2[0] * j2 / dist;
         out[5] = b1u * k * j1d + p->a1[0] * j1 / dist;
         out[6] = p->a2[1] * k * j2;
@@ -1161,8 +1166,8 @@ static void integrand(int src_type, int fix, const ypar_t *p, double k, double d
         if (cf) {
             out[10] = p->b2t * 2.0 * j2 / dist + p->a2t[0] * k * j2d;
             out[11] = p->b1t * j1 / dist + p->a1t[0] * k * j1d;
-            out[12] = p->a2t[1] * k * j0d;
-            out[13] = p->a0t[1] * k * j0d;
+            out[12] = p->a2t[0] * k * j0d;
+            out[13] = p->a0t[0] * k * j0d;
             out[14] = p->b2t * k * j2d + 2.0 * p->a2t[0] * j2 / dist;
             out[15] = b1tu * k * j1d + p->a1t[0] * j1 / dist;
             out[16] = p->a2t[1] * k * j2;
@@ -1172,8 +1177,8 @@ static void integrand(int src_type, int fix, const ypar_t *p, double k, double d
         }
         out[o + 0] = -p->b2 * 2.0 * j2 / dist / dist + p->b2 * 2.0 * j2d * k / dist + p->a2[0] * k * j2dd * k;
         out[o + 1] = -p->b1 * j1 / dist / dist + p->b1 * j1d * k / dist + p->a1[0] * k * j1dd * k;
-        out[o + 2] = p->a2[1] * k * j0dd * k;
-        out[o + 3] = p->a0[1] * k * j0dd * k;
+        out[o + 2] = *a2h * k * j0dd * k;
+        out[o + 3] = *a0h * k * j0dd * k;
         out[o + 4] = p->b2 * k * j2dd * k - 2.0 * p->a2[0] * j2 / dist / dist + 2.0 * p->a2[0] * j2d * k / dist;
         out[o + 5] = b1u * k * j1dd * k - p->a1[0] * j1 / dist / dist + p->a1[0] * j1d * k / dist;
         out[o + 6] = p->a2[1] * k * j2d * k;

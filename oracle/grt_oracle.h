@@ -48,7 +48,10 @@ extern "C" {
  * (the block green.cu:1666-1677 writes and then overwrites), d/dr 20-29
  * (green.cu:1680-1691, column 25 with b1); single force: the d/dr column 10
  * with the 1/r of its b1 k J1' term; second Bessel derivatives from Bessel's
- * equation instead of dd_besselj (green.cu:1540-1554). */
+ * equation instead of dd_besselj (green.cu:1540-1554); the m = 0 radial
+ * moment-tensor columns 2, 3 (and their d/dz 12, 13, d/dr 22, 23) from the
+ * radial coefficients a2[0], a0[0] where green.cu:1652-1653 use the vertical
+ * ones a2[1], a0[1]. */
 #define GRTO_FIX_COLS 16
 /* SH source terms of the moment tensor (get_src_tensor, green.cu:1409-1412):
  * the reference gives the m = 1 and m = 2 SH terms one reflection factor,

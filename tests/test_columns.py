@@ -49,11 +49,30 @@ def test_derivative_columns_are_derivatives(src):
 def test_reference_layout_unchanged_without_the_bit():
     s_ref, _ = _spec(1, 3.0, 40.0, fix=O.FIX_ALL | O.STABLE)
     s_fix, _ = _spec(1, 3.0, 40.0)
-    # columns 0-9 agree except the m = 1 transverse term (5), 10-19 of the
+    # columns 0-9 agree except the m = 0 radial terms (2, 3: radial instead of
+    # vertical coefficients) and the m = 1 transverse term (5); 10-19 of the
     # reference hold d/dr, 20-29 are empty there
-    for c in (0, 1, 2, 3, 4, 6, 7, 8, 9):
+    for c in (0, 1, 4, 6, 7, 8, 9):
         assert np.array_equal(s_ref[..., c], s_fix[..., c])
+    for c in (2, 3, 5):
+        assert not np.allclose(s_ref[..., c], s_fix[..., c])
     assert np.all(s_ref[..., 20:] == 0) and np.any(s_fix[..., 20:] != 0)
+
+
+@pytest.mark.parametrize("src", [1, 0])
+def test_free_surface_has_no_shear_traction(src):
+    """At a surface receiver sigma_rz = mu (du_r/dz + du_z/dr) vanishes: in the
+    corrected layout the d/dz of each radial column equals the d/dr of the
+    vertical column of its azimuthal family (the SH parts' d/dz vanish there).
+    Moment tensor: (radial, vertical) = (0, 6), (1, 7), (2, 9), (3, 8); single
+    force (1, 4), (0, 3).  The reference's m = 0 radial columns 2 and 3, built
+    from the vertical coefficients, fail it."""
+    s, _ = _spec(src, 0.0, [15.0, 40.0], fix=FIXC | O.FIX_SHSRC)
+    nw = s.shape[1] // 2
+    pairs = [(10, 26), (11, 27), (12, 29), (13, 28)] if src == 1 else [(6, 14), (5, 13)]
+    for dz_col, dr_col in pairs:
+        a, b = s[:, :nw, dz_col], s[:, :nw, dr_col]
+        assert np.abs(a - b).max() <= 1e-12 * np.abs(b).max(), (dz_col, dr_col)
 
 
 @pytest.mark.gpu
