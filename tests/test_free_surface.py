@@ -1,4 +1,6 @@
-"""The free surface is traction free (CPU, FP64 oracle, per (w, k)).
+"""Boundary conditions of the layered medium (CPU, FP64 oracle, per (w, k)):
+the free surface is traction free, and displacement and traction are
+continuous across every internal interface.
 
 At a receiver on the surface, the receiver coefficients of every azimuthal
 order m (a_m[0] radial, a_m[1] vertical, suffix t their receiver-depth
@@ -86,3 +88,49 @@ def test_reference_dz_quirk_breaks_the_free_surface(oracle):
         # the source two layers down: both conditions fail
         shear, normal = _traction_residuals(oracle, model, 12.0, src, fix)
         assert shear > 0.1 and normal > 0.1, (shear, normal)
+
+
+def _lame(model, i, w):
+    """Attenuated (lambda, mu) of layer i at complex frequency w."""
+    _, vp, vs, rho, qp, qs = model
+    lw = np.log(w / (2 * math.pi))
+    a = vp[i] * (1 + lw / (math.pi * qp[i]) + 0.5j / qp[i])
+    b = vs[i] * (1 + lw / (math.pi * qs[i]) + 0.5j / qs[i])
+    mu = rho[i] * b * b
+    return rho[i] * a * a - 2 * mu, mu
+
+
+@pytest.mark.parametrize("src", [0, 1])
+def test_continuity_across_interfaces(oracle, src):
+    """Receivers 1e-10 km above and below each internal interface (other
+    layers, other propagators): displacement, sigma_rz = mu (u_H,z - k u_V),
+    sigma_zz = (lambda + 2 mu) u_V,z + lambda k u_H and the SH pair (v,
+    mu v_z) agree across it; the residual shrinks in proportion to the gap."""
+    model = _models()["crust4"]
+    fix = oracle.FIX_ALL | oracle.FIX_SHSRC
+    eps = 1e-10
+
+    def rel(a, b):
+        return abs(a - b) / max(abs(a), abs(b), 1e-300)
+
+    for hs in (1.0, 12.0, 25.0):              # source above, between and below the interfaces
+        for zi, (iu, il) in ((2.0, (0, 1)), (10.0, (1, 2)), (20.0, (2, 3))):
+            ju = oracle.model(*model, hs, zi - eps, src)
+            jl = oracle.model(*model, hs, zi + eps, src)
+            for j in (ju, jl):
+                oracle.setup(j, DT, LOG2N, 0.0, 0.3, 2.0, oracle.K_REFERENCE, 0, fix=fix)
+            for iw, k in POINTS:
+                yu, yl = oracle.point(ju, iw, k), oracle.point(jl, iw, k)
+                w = complex(2 * math.pi * ju.df * iw, -ju.sigma)
+                (lu, mu_u), (ll, mu_l) = _lame(model, iu, w), _lame(model, il, w)
+                for r, z in ORDERS:
+                    if yu[r] == 0 and yu[z] == 0:
+                        continue
+                    assert rel(yu[r], yl[r]) < 1e-7 and rel(yu[z], yl[z]) < 1e-7
+                    assert rel(mu_u * (yu[T + r] - k * yu[z]), mu_l * (yl[T + r] - k * yl[z])) < 1e-7
+                    assert rel((lu + 2 * mu_u) * yu[T + z] + lu * k * yu[r],
+                               (ll + 2 * mu_l) * yl[T + z] + ll * k * yl[r]) < 1e-7
+                for b in (6, 7):                    # SH: b1, b2
+                    if yu[b] != 0:
+                        assert rel(yu[b], yl[b]) < 1e-7
+                        assert rel(mu_u * yu[T + b], mu_l * yl[T + b]) < 1e-7
