@@ -21,6 +21,9 @@ FP32, FP64 = 0, 1
 FIX_RLAYER, FIX_REXUT, FIX_DZ, FIX_COLS = 1, 2, 4, 8
 FIX_SHSRC = 16   # moment-tensor SH source terms with the jump structure of their order
 FIX_ALL = FIX_RLAYER | FIX_REXUT | FIX_DZ
+# every correction of the reference: the receiver layer and d/dz terms, the corrected
+# column layouts and the moment tensor's SH source terms (0 reproduces the reference)
+FIX_PHYSICAL = FIX_ALL | FIX_COLS | FIX_SHSRC
 
 _dp = ctypes.POINTER(ctypes.c_double)
 
