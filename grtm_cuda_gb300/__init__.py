@@ -129,6 +129,16 @@ def dc_moment(strike, dip, rake, m0=1.0):
     return np.array(list(m))
 
 
+def mt_weights(m6, azimuth):
+    """Weights [3 (Z up, R away, T clockwise), 30] of the moment-tensor columns
+    for moment tensor m6 (Mxx, Myy, Mzz, Mxy, Mxz, Myz; x north, y east, z down)
+    at the receiver's azimuth from the source (degrees clockwise from north)."""
+    m = np.ascontiguousarray(m6, dtype=np.float64)
+    w = np.zeros((3, 30))
+    lib().grt_mt_weights(_ptr(m), float(azimuth), _ptr(w))
+    return w
+
+
 class Job(ctypes.Structure):
     _fields_ = [("model", ctypes.POINTER(Model)), ("opts", ctypes.POINTER(Opts)), ("n_dist", ctypes.c_int),
                 ("dist", _dp), ("out_f32", ctypes.POINTER(ctypes.c_float))]
@@ -158,7 +168,8 @@ EXPORTS = ("grt_create", "grt_destroy", "grt_last_error", "grt_status_string", "
            "grt_green", "green", "grt_run_noalloc", "grt_sweep_kmax", "grt_mlp_create", "grt_mlp_destroy",
            "grt_mlp_n_params", "grt_mlp_get_params", "grt_mlp_set_params", "grt_mlp_forward",
            "grt_mlp_loss_grad", "grt_mlp_train", "grt_batch_create", "grt_batch_execute", "grt_batch_fetch",
-           "grt_batch_fetch_freqs", "grt_batch_info", "grt_batch_destroy", "grt_dc_moment", "grt_plan_synth",
+           "grt_batch_fetch_freqs", "grt_batch_info", "grt_batch_destroy", "grt_dc_moment", "grt_mt_weights",
+           "grt_plan_synth",
            "grt_batch_synth", "grt_flatten", "grt_plan_write", "grt_plan_fetch_f32", "grt_batch_fetch_f32",
            "grt_host_alloc", "grt_host_free", "grt_trim", "grt_batch_fetch_f32_async", "grt_batch_wait")
 
@@ -235,6 +246,8 @@ def lib():
                               _dp, _dp, _dp, _dp]
     L.grt_dc_moment.argtypes = [ctypes.c_double] * 4 + [_dp]
     L.grt_dc_moment.restype = None
+    L.grt_mt_weights.argtypes = [_dp, ctypes.c_double, _dp]
+    L.grt_mt_weights.restype = None
     L.grt_plan_synth.argtypes = [vp, P(Source), _dp, _dp]
     L.grt_batch_synth.argtypes = [vp, ctypes.c_int, P(Source), _dp, _dp]
     _lib = L

@@ -1560,13 +1560,20 @@ extern "C" void grt_dc_moment(double strike, double dip, double rake, double m0,
 }
 
 // weights of the displacement columns (0-9) of the moment-tensor output for
-// component Z, R, T at azimuth phi (degrees clockwise from north)
+// component Z (up), R (away from the source), T (clockwise) at azimuth phi (the
+// receiver's azimuth from the source, degrees clockwise from north).  The
+// horizontal-isotropic term (columns 2, 9) and the m = 1 terms (1, 5, 7) take a
+// minus sign: the m = 0 and m = 2 parts of the horizontal moments share the
+// coefficients a2, u_z = a2z k (h J0 - c2 J2), and the m = 1 columns carry the
+// opposite orientation; with these signs every family equals the displacement
+// that reciprocity with the single-force solution gives.
 static void mt_weights(const double *m, double phi_deg, double w[3][grt::kTensorFixNC])
 {
     for (int i = 0; i < 3; i++)
         for (int c = 0; c < grt::kTensorFixNC; c++) w[i][c] = 0.0;
     const double ph = phi_deg * PI / 180.0;
-    const double w2c = 0.5 * (m[0] - m[1]), w2s = m[3], w1c = m[4], w1s = m[5], w0 = m[2], w0h = 0.5 * (m[0] + m[1]);
+    const double w2c = 0.5 * (m[0] - m[1]), w2s = m[3], w1c = -m[4], w1s = -m[5], w0 = m[2],
+                 w0h = -0.5 * (m[0] + m[1]);
     const double c2 = w2c * std::cos(2 * ph) + w2s * std::sin(2 * ph), s2 = -w2c * std::sin(2 * ph) + w2s * std::cos(2 * ph);
     const double c1 = w1c * std::cos(ph) + w1s * std::sin(ph), s1 = -w1c * std::sin(ph) + w1s * std::cos(ph);
     // Z: m = 2, 1, 0 families and the horizontal-isotropic part of the m = 2 family
@@ -1575,6 +1582,15 @@ static void mt_weights(const double *m, double phi_deg, double w[3][grt::kTensor
     w[1][0] = c2; w[1][1] = c1; w[1][3] = w0; w[1][2] = w0h;
     // T
     w[2][4] = s2; w[2][5] = s1;
+}
+
+extern "C" void grt_mt_weights(const double *m, double azimuth, double *w)
+{
+    if (!m || !w) return;
+    double t[3][grt::kTensorFixNC];
+    mt_weights(m, azimuth, t);
+    for (int i = 0; i < 3; i++)
+        for (int c = 0; c < grt::kTensorFixNC; c++) w[i * grt::kTensorFixNC + c] = t[i][c];
 }
 
 template <typename R>

@@ -264,12 +264,19 @@ GRT_API int grt_flatten(int n_layer, const double *ztop, const double *vp, const
  * spectrum, phase/taper/scale, Hermitian fill, inverse DFT, e^{sigma t}).
  * Combination, in the azimuthal families of the displacement columns 0-9
  * (m = 2: columns 0, 4, 6; m = 1: 1, 5, 7; m = 0: 3, 8; the isotropic
- * horizontal part of the m = 2 family: 2, 9), phi = azimuth:
- *   Z = c2 G6 + c1 G7 + Mzz G8 + h G9,  R = c2 G0 + c1 G1 + Mzz G3 + h G2,
- *   T = s2 G4 + s1 G5,
+ * horizontal part of the m = 2 family: 2, 9), phi = the receiver's azimuth
+ * from the source:
+ *   Z = c2 G6 - c1 G7 + Mzz G8 - h G9,  R = c2 G0 - c1 G1 + Mzz G3 - h G2,
+ *   T = s2 G4 - s1 G5,
  *   c2 = (Mxx-Myy)/2 cos 2phi + Mxy sin 2phi, s2 = -(Mxx-Myy)/2 sin 2phi + Mxy cos 2phi,
  *   c1 = Mxz cos phi + Myz sin phi,            s1 = -Mxz sin phi + Myz cos phi,
- *   h = (Mxx+Myy)/2.
+ *   h = (Mxx+Myy)/2,
+ * giving displacement Z up, R away from the source, T clockwise (azimuth
+ * increasing): by reciprocity every term equals the moment tensor contracted
+ * with the gradient, at the source, of the single-force solution for a unit
+ * force at the receiver.  The corrected layout (GRT_FIX_COLS) and
+ * GRT_FIX_SHSRC are needed for that; with the reference's columns R of Mzz
+ * and h, and the SH parts, keep the reference's errors.
  * The source-time function s_n (at opts.dt) enters as dt sum_n s_n e^{-i (w - i sigma) n dt},
  * so the seismogram is dt sum_m s_m G(t - m dt) (circularly, with the damped
  * wrap-around of the method).  No counterpart in the reference, which stops
@@ -281,6 +288,11 @@ typedef struct grt_source {
 } grt_source;
 /* double couple: strike, dip, rake in degrees, scalar moment m0 -> m[6] (Aki & Richards, Box 4.4) */
 GRT_API void grt_dc_moment(double strike, double dip, double rake, double m0, double *m);
+/* The combination above as weights: w[3 (Z, R, T)][30] of the moment-tensor
+ * columns for moment tensor m[6] at one azimuth (degrees), for callers that
+ * combine fetched or written columns themselves.  Host only (no device).  No
+ * counterpart in the reference. */
+GRT_API void grt_mt_weights(const double *m, double azimuth, double *w);
 /* azimuth: degrees clockwise from north, one per receiver; seis: [n_dist][3 (Z, R, T)][N] */
 GRT_API int grt_plan_synth(grt_plan *plan, const grt_source *src, const double *azimuth, double *seis);
 GRT_API int grt_batch_synth(grt_batch *batch, int job, const grt_source *src, const double *azimuth, double *seis);

@@ -23,10 +23,17 @@ def dc_moment(strike, dip, rake, m0=1.0):
 
 
 def weights(m, phi_deg):
-    """[3 (Z, R, T), 20] weights of the moment-tensor columns at azimuth phi."""
+    """[3 (Z, R, T), 20] weights of the moment-tensor columns at azimuth phi
+    (the receiver's azimuth from the source, clockwise from north) for
+    displacement Z up, R away from the source, T clockwise.  Relative to the
+    column families the horizontal-isotropic term (columns 2, 9) and the
+    m = 1 terms (1, 5, 7) enter with a minus sign: the m = 0 and m = 2 parts of
+    the horizontal moments share the coefficients a2 with u_z = a2z k (h J0 -
+    c2 J2), and the m = 1 columns carry the opposite orientation -- the
+    signs for which every family equals the displacement reciprocity gives."""
     ph = np.radians(phi_deg)
-    w2c, w2s, w1c, w1s = 0.5 * (m[0] - m[1]), m[3], m[4], m[5]
-    w0, w0h = m[2], 0.5 * (m[0] + m[1])
+    w2c, w2s, w1c, w1s = 0.5 * (m[0] - m[1]), m[3], -m[4], -m[5]
+    w0, w0h = m[2], -0.5 * (m[0] + m[1])
     c2 = w2c * np.cos(2 * ph) + w2s * np.sin(2 * ph)
     s2 = -w2c * np.sin(2 * ph) + w2s * np.cos(2 * ph)
     c1 = w1c * np.cos(ph) + w1s * np.sin(ph)
