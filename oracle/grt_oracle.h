@@ -11,6 +11,13 @@
  * (cangyeone/grtm_cuda, cusrc/popm/func/green.cu) computes, including the
  * reference's known quirks (they are switchable, see GRTO_FIX_*), so that the
  * reference's own golden vectors demo/oname_{t,w}.txt can be reproduced.
+ *
+ * Pinned: to those golden vectors (single force, surface receiver), and with
+ * the quirks corrected, to first principles the tests check per (w, k) and
+ * per trace -- source-receiver reciprocity, the traction-free surface,
+ * continuity across interfaces, the source's jump conditions and the
+ * moment-tensor displacement obtained by reciprocity.  Those checks found the
+ * quirks GRTO_FIX_SHSRC and the m = 0 radial columns of GRTO_FIX_COLS.
  */
 #ifndef GRT_ORACLE_H_
 #define GRT_ORACLE_H_
