@@ -219,3 +219,54 @@ def test_source_discontinuities(oracle, src):
                 scale = max(abs(x) for x in up + dn)
                 for a, b, e in zip(up, dn, want_sh[m]):
                     assert abs((b - a) - e) <= 1e-7 * scale, (hs, iw, k, m, b - a, e)
+
+
+BRANCHES = {                     # (hs, hr) on the 4-layer crust
+    "same layer, receiver below": (12.0, 14.0),
+    "same layer, receiver above": (14.0, 12.0),
+    "receiver above, other layer": (12.0, 3.0),
+    "receiver below, other layer": (5.0, 15.0),
+    "receiver in the half-space": (5.0, 40.0),
+}
+
+
+def _derivative_residual(oracle, hs, hr, fix, dz=1e-5):
+    """Worst relative difference between the receiver-depth derivative
+    coefficients (t) and central differences of the displacement coefficients
+    in receiver depth, at fixed (w, k), both sources."""
+    model = _models()["crust4"]
+    worst = 0.0
+
+    def coef(z, src, iw, k):
+        j = oracle.model(*model, hs, z, src)
+        oracle.setup(j, DT, LOG2N, 0.0, 0.3, 2.0, oracle.K_REFERENCE, 0, fix=fix)
+        return oracle.point(j, iw, k)
+
+    for src in (0, 1):
+        for iw, k in POINTS[1:4]:
+            y = coef(hr, src, iw, k)
+            dy = (coef(hr + dz, src, iw, k) - coef(hr - dz, src, iw, k)) / (2 * dz)
+            for c in range(8):
+                scale = max(abs(dy[c]), abs(y[T + c]))
+                if scale > 0:
+                    worst = max(worst, abs(dy[c] - y[T + c]) / scale)
+    return worst
+
+
+@pytest.mark.parametrize("branch", list(BRANCHES))
+def test_receiver_derivative_terms(oracle, branch):
+    """The d/dz receiver terms are the receiver-depth derivatives of the
+    displacement terms in every branch of the receiver propagation with the
+    quirks corrected; the reference's d/dz quirks each break some branches:
+    the doubled factor / reused product (GRT_FIX_DZ: green.cu:720, 842, 902)
+    the receiver-above-source ones, the first point's nu (GRT_FIX_REXUT:
+    green.cu:674-675) the others away from the source's own level."""
+    hs, hr = BRANCHES[branch]
+    assert _derivative_residual(oracle, hs, hr, oracle.FIX_ALL) <= 1e-7
+    dz_quirk = _derivative_residual(oracle, hs, hr, oracle.FIX_RLAYER | oracle.FIX_REXUT)
+    rexut_quirk = _derivative_residual(oracle, hs, hr, oracle.FIX_RLAYER | oracle.FIX_DZ)
+    above = hr < hs
+    assert (dz_quirk > 0.1) == above, dz_quirk
+    expect_rexut = branch in ("same layer, receiver below", "receiver above, other layer",
+                              "receiver below, other layer")
+    assert (rexut_quirk > 0.1) == expect_rexut, rexut_quirk
