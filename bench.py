@@ -5,7 +5,8 @@ models of 40 layers over a half-space (thickness U(0.5, 5) km, Vp 2.5 -> 8.0
 km/s linear plus N(0, 0.15), Vs = Vp / U(1.65, 1.85), Gardner density, Qs
 U(50, 300), Qp = 2 Qs), double-couple source at U(1, 30) km, 1000 receivers
 uniform in 1-500 km per model, nt = 8192, dt = 0.05 s, sigma = pi / T, the
-reference's quirks corrected.  A trace is one receiver with its 20
+reference's receiver-layer and d/dz quirks corrected (FIX_ALL: its 20-column
+layout and tensor-core sums).  A trace is one receiver with its 20
 moment-tensor Green's-function columns over all nt samples.
 
 Arms (all FP32 arithmetic, checked against the FP64 path of the same method):

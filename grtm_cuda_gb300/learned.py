@@ -41,7 +41,8 @@ N_FEAT, N_IN, N_OUT = 12, 15, 2
 MAGIC = b"GRTKSMP1"
 
 # the plain grid the sampler is trained against and judged by.  Synthetic
-# models run with the reference's quirks corrected (FIX_ALL): with its
+# models run with the reference's receiver-layer and d/dz quirks corrected
+# (FIX_ALL, the 20-column layout of the tensor-core sums): with its
 # receiver-layer search (green.cu:2092-2101) a surface receiver whose source
 # sits deeper in its layer than the top layer is thick lands at a negative
 # depth in a deeper layer, and the field grows like e^{nu |z|} (overflow).
