@@ -139,6 +139,16 @@ def mt_weights(m6, azimuth):
     return w
 
 
+def sf_weights(force, azimuth):
+    """Weights [3 (Z up, R away, T clockwise), 15] of the single-force columns
+    for force (Fx, Fy, Fz; x north, y east, z down) at the receiver's azimuth
+    from the source (degrees clockwise from north)."""
+    f = np.ascontiguousarray(force, dtype=np.float64)
+    w = np.zeros((3, 15))
+    lib().grt_sf_weights(_ptr(f), float(azimuth), _ptr(w))
+    return w
+
+
 class Job(ctypes.Structure):
     _fields_ = [("model", ctypes.POINTER(Model)), ("opts", ctypes.POINTER(Opts)), ("n_dist", ctypes.c_int),
                 ("dist", _dp), ("out_f32", ctypes.POINTER(ctypes.c_float))]
@@ -169,6 +179,7 @@ EXPORTS = ("grt_create", "grt_destroy", "grt_last_error", "grt_status_string", "
            "grt_mlp_n_params", "grt_mlp_get_params", "grt_mlp_set_params", "grt_mlp_forward",
            "grt_mlp_loss_grad", "grt_mlp_train", "grt_batch_create", "grt_batch_execute", "grt_batch_fetch",
            "grt_batch_fetch_freqs", "grt_batch_info", "grt_batch_destroy", "grt_dc_moment", "grt_mt_weights",
+           "grt_sf_weights",
            "grt_plan_synth",
            "grt_batch_synth", "grt_flatten", "grt_plan_write", "grt_plan_fetch_f32", "grt_batch_fetch_f32",
            "grt_host_alloc", "grt_host_free", "grt_trim", "grt_batch_fetch_f32_async", "grt_batch_wait")
@@ -248,6 +259,8 @@ def lib():
     L.grt_dc_moment.restype = None
     L.grt_mt_weights.argtypes = [_dp, ctypes.c_double, _dp]
     L.grt_mt_weights.restype = None
+    L.grt_sf_weights.argtypes = [_dp, ctypes.c_double, _dp]
+    L.grt_sf_weights.restype = None
     L.grt_plan_synth.argtypes = [vp, P(Source), _dp, _dp]
     L.grt_batch_synth.argtypes = [vp, ctypes.c_int, P(Source), _dp, _dp]
     _lib = L

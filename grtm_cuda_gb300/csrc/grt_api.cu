@@ -1584,6 +1584,22 @@ static void mt_weights(const double *m, double phi_deg, double w[3][grt::kTensor
     w[2][4] = s2; w[2][5] = s1;
 }
 
+// weights [3 (Z up, R away, T clockwise)][15] of the single-force displacement
+// columns (0: R and 2: T and 3: Z of a horizontal force, 1: R and 4: Z of a
+// vertical one) for force f = (Fx, Fy, Fz; x north, y east, z down) at the
+// receiver's azimuth from the source; the same orientation as mt_weights,
+// checked against the reciprocal displacement
+extern "C" void grt_sf_weights(const double *f, double azimuth, double *w)
+{
+    if (!f || !w) return;
+    for (int i = 0; i < 3 * grt::kSingleNC; i++) w[i] = 0.0;
+    const double ph = azimuth * PI / 180.0;
+    const double fr = f[0] * std::cos(ph) + f[1] * std::sin(ph), ft = -f[0] * std::sin(ph) + f[1] * std::cos(ph);
+    w[0 * grt::kSingleNC + 3] = fr; w[0 * grt::kSingleNC + 4] = f[2];
+    w[1 * grt::kSingleNC + 0] = fr; w[1 * grt::kSingleNC + 1] = f[2];
+    w[2 * grt::kSingleNC + 2] = ft;
+}
+
 extern "C" void grt_mt_weights(const double *m, double azimuth, double *w)
 {
     if (!m || !w) return;

@@ -293,6 +293,15 @@ GRT_API void grt_dc_moment(double strike, double dip, double rake, double m0, do
  * combine fetched or written columns themselves.  Host only (no device).  No
  * counterpart in the reference. */
 GRT_API void grt_mt_weights(const double *m, double azimuth, double *w);
+/* Single force: w[3 (Z up, R away, T clockwise)][15] of the single-force
+ * columns for force f[3] = (Fx, Fy, Fz; x north, y east, z down) at the
+ * receiver's azimuth from the source (degrees clockwise from north):
+ *   Z = Fr G3 + Fz G4,  R = Fr G0 + Fz G1,  T = Ft G2,
+ *   Fr = Fx cos phi + Fy sin phi, Ft = -Fx sin phi + Fy cos phi.
+ * The displacement columns 0-4 are the reference's in both layouts.  Host
+ * only (no device); grt_plan_synth combines moment tensors only.  No
+ * counterpart in the reference. */
+GRT_API void grt_sf_weights(const double *f, double azimuth, double *w);
 /* azimuth: degrees clockwise from north, one per receiver; seis: [n_dist][3 (Z, R, T)][N] */
 GRT_API int grt_plan_synth(grt_plan *plan, const grt_source *src, const double *azimuth, double *seis);
 GRT_API int grt_batch_synth(grt_batch *batch, int job, const grt_source *src, const double *azimuth, double *seis);

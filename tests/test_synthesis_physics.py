@@ -1,5 +1,5 @@
-"""The moment-tensor synthesis gives the physical displacement (CPU, FP64
-oracle columns, corrected layout).
+"""The moment-tensor synthesis and the single-force weights give the
+physical displacement (CPU, FP64 oracle columns, corrected layout).
 
 Reciprocity: the displacement u_n at a surface receiver x_r from a moment
 tensor M at the source point xi is M : grad u^(n)(xi), where u^(n) is the
@@ -117,3 +117,44 @@ def test_double_couple_and_explosion(spectra):
     # an explosion has no transverse motion and no azimuthal dependence
     w = [g.mt_weights([1.0, 1, 1, 0, 0, 0], phi) for phi in (0.0, 77.0)]
     assert np.array_equal(w[0], w[1]) and not np.any(w[0][2])
+
+
+@pytest.fixture(scope="module")
+def force_spectra(oracle):
+    from grtm_cuda_gb300 import synth
+    m, _ = synth.crust4_model()
+    fix = oracle.FIX_ALL | oracle.STABLE | oracle.FIX_COLS | oracle.FIX_SHSRC
+
+    def run(hs, hr):
+        j = oracle.model(m["ztop"], m["vp"], m["vs"], m["rho"], m["qp"], m["qs"], hs, hr, 0)
+        oracle.setup(j, 0.1, 9, 0.0, 0.3, math.pi, oracle.K_FIXED, 2048, 0.0, fix)
+        s, _ = oracle.run(j, DISTS, nthreads=0, want_sig=False)
+        return s[:, : j.nw, :]
+
+    return run(ZS, 0.0), run(0.0, ZS)       # force at depth / force at the surface (swapped)
+
+
+@pytest.mark.parametrize("phi", [37.0, 200.0])
+def test_single_force_weights_equal_the_reciprocal_displacement(force_spectra, phi):
+    """grt_sf_weights: u_n(x_r) from a force F at xi equals F . u^(n)(xi), the
+    field at the source point of a unit force along e_n at the receiver."""
+    import grtm_cuda_gb300 as g
+    s_src, s_rcv = force_spectra
+    ph = math.radians(phi)
+    psi = ph + math.pi
+    Q = np.array([[math.cos(psi), math.sin(psi), 0.0], [-math.sin(psi), math.cos(psi), 0.0], [0.0, 0.0, 1.0]])
+    for force in ([0.0, 0.0, 1.0], [1.0, 0.0, 0.0], [0.0, 1.0, 0.0], [0.3, -0.7, 0.5]):
+        f = np.array(force)
+        fl = Q @ f
+        got = np.einsum("kc,dnc->kdn", g.sf_weights(f, phi), s_src[:, :, :15])
+        want = []
+        for kind, th in (("down", 0.0), ("h", psi - ph), ("h", psi - ph - math.pi / 2)):
+            c, s = math.cos(th), math.sin(th)
+            S = s_rcv
+            u = ([S[..., 1], 0 * S[..., 1], -S[..., 4]] if kind == "down"
+                 else [S[..., 0] * c, -S[..., 2] * s, -S[..., 3] * c])
+            want.append(sum(fl[i] * u[i] for i in range(3)))
+        want[0] = -want[0]                  # up
+        want = np.stack(want)
+        scale = np.abs(want).max()
+        assert np.abs(got - want).max() <= 1e-12 * scale, (force, phi)
