@@ -133,3 +133,51 @@ def test_reference_sh_source_terms_miss_the_direct_wave(oracle):
     m6 = np.array(MOMENTS["Mxy"], float)
     ours = _convolve(g.mt_weights(m6, PHI) @ tr)
     assert _rel(ours, _aki_richards(_tensor(m6), hs, hr)) > 0.5
+
+
+def _stokes_spectrum(w, R, gam, Qp, Qs, rho_of_beta):
+    """Stokes' solution at complex frequency w for a downward unit force in a
+    whole space with the attenuated velocities of the method's law
+    (green.cu:177-180) and density rho_of_beta(beta(w)); (radial, down)."""
+    lw = np.log(w / (2 * math.pi))
+    al = ALPHA * (1 + lw / (math.pi * Qp) + 0.5j / Qp)
+    be = BETA * (1 + lw / (math.pi * Qs) + 0.5j / Qs)
+
+    def prim(t):                                      # antiderivative of t e^{-i w t}
+        return np.exp(-1j * w * t) * (1 + 1j * w * t) / (w * w)
+
+    near = prim(R / be) - prim(R / al)
+    out = []
+    for i, dz in ((0, 0.0), (1, 1.0)):
+        gi, gz = gam[i], gam[1]
+        out.append(((3 * gi * gz - dz) / R ** 3 * near + gi * gz / (al * al * R) * np.exp(-1j * w * R / al)
+                    - (gi * gz - dz) / (be * be * R) * np.exp(-1j * w * R / be)) / (4 * math.pi * rho_of_beta(be)))
+    return np.array(out)
+
+
+def test_attenuation_convention(oracle):
+    """With attenuation the method's medium is the viscoelastic one of density
+    rho (beta0 / beta(w))^2: its stress rows keep the real mu0 = rho beta0^2
+    (green.cu:182, 2048).  Source and receiver 1000 km deep, so the free
+    surface's reflections stay out of the spectrum; the spectral scale is
+    taken from a nearly elastic run."""
+    hs, hr = 1000.0, 1020.0
+    R = math.hypot(DIST, hr - hs)
+    gam = np.array([DIST / R, (hr - hs) / R])
+
+    def spectra(Q):
+        job = oracle.model([0.0, 3000.0], [ALPHA] * 2, [BETA] * 2, [RHO] * 2, [2 * Q] * 2, [Q] * 2, hs, hr, 0)
+        oracle.setup(job, DT, LOG2N, 0.0, 0.3, math.pi, oracle.K_FIXED, NK, 0.0, oracle.FIX_ALL | oracle.STABLE)
+        s, _ = oracle.run(job, [DIST], want_sig=False)
+        iw = np.arange(5, int(0.6 * job.nw))           # below the taper
+        return np.array([s[0, iw, 1], -s[0, iw, 4]]), 2 * math.pi * job.df * iw - 1j * job.sigma
+
+    ours, w = spectra(1e6)
+    scale = ours / _stokes_spectrum(w, R, gam, 2e6, 1e6, lambda be: RHO)
+    assert np.std(scale) <= 1e-4 * abs(np.mean(scale))
+    scale = np.mean(scale)
+    ours, w = spectra(50.0)
+    reference = scale * _stokes_spectrum(w, R, gam, 100.0, 50.0, lambda be: RHO * BETA ** 2 / be ** 2)
+    standard = scale * _stokes_spectrum(w, R, gam, 100.0, 50.0, lambda be: RHO)
+    assert np.abs(ours - reference).max() <= 1e-3 * np.abs(reference).max()
+    assert np.abs(ours - standard).max() >= 2e-2 * np.abs(standard).max()
