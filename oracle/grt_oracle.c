@@ -413,7 +413,7 @@ typedef struct {
 
 /* vertical wavenumbers and E matrix of one layer: set_pars green.cu:184-194,
  * mat_PSV_E green.cu:196-214 */
-static void layer_pars(double k, cplx w, cplx a, cplx b, double u, cplx *r, cplx *v, cplx E[4][4])
+static void layer_pars(double k, cplx w, cplx a, cplx b, cplx u, cplx *r, cplx *v, cplx E[4][4])
 {
     cplx wa = w / a, wb = w / b;
     *r = c_sqrt(k * k - wa * wa);
@@ -439,6 +439,15 @@ static void layer_pars(double k, cplx w, cplx a, cplx b, double u, cplx *r, cplx
     E[3][3] = E[3][1];
 }
 
+/* shear modulus of each layer at this frequency: the reference's real
+ * mu0 = b0^2 rho (green.cu:182, 2048), or with GRTO_ATTEN_MU the standard
+ * viscoelastic rho beta(w)^2 from the attenuated S velocity */
+static void shear_moduli(const grto_job *J, const cplx *beta, cplx *mue)
+{
+    for (int i = 0; i < J->n_layer; i++)
+        mue[i] = (J->fix & GRTO_ATTEN_MU) ? J->rho[i] * beta[i] * beta[i] : (cplx)J->mu[i];
+}
+
 static void point_eval(const grto_job *J, const cplx *alpha, const cplx *beta, double k,
                        cplx w, const cplx slot0[2], ypar_t *Y)
 {
@@ -450,7 +459,9 @@ static void point_eval(const grto_job *J, const cplx *alpha, const cplx *beta, d
     static __thread grt_t G[GRTO_MAXL + 1];
     memset(G, 0, sizeof(grt_t) * (L + 1));
 
-    for (int i = 0; i < L; i++) layer_pars(k, w, alpha[i], beta[i], J->mu[i], &rr[i], &vv[i], E[i]);
+    cplx mue[GRTO_MAXL];
+    shear_moduli(J, beta, mue);
+    for (int i = 0; i < L; i++) layer_pars(k, w, alpha[i], beta[i], mue[i], &rr[i], &vv[i], E[i]);
 
     /* interface R/T: get_emat_e1e2 green.cu:235-262, cuBLAS solve, get_mrt_psv
      * green.cu:359-387; SH closed form get_mrt_sh green.cu:339-353 */
@@ -475,7 +486,7 @@ static void point_eval(const grto_job *J, const cplx *alpha, const cplx *beta, d
                 M[j].rdu1[i][c] = E2[i + 2][c];
                 M[j].rud1[i][c] = E2[i][c + 2];
             }
-        cplx wa = vv[j] * J->mu[j], wb = vv[j + 1] * J->mu[j + 1];
+        cplx wa = vv[j] * mue[j], wb = vv[j + 1] * mue[j + 1];
         M[j].tdd0 = 2. * wa / (wa + wb);
         M[j].rdu0 = (wa - wb) / (wa + wb);
         M[j].rud0 = -M[j].rdu0;
@@ -538,7 +549,8 @@ static void point_eval(const grto_job *J, const cplx *alpha, const cplx *beta, d
 
     /* source terms: get_src_single green.cu:1271-1332, get_src_tensor 1334-1413 */
     const cplx sr = rr[s], sv = vv[s], sa = alpha[s], sb = beta[s];
-    const double su = J->mu[s], sh = J->h[s];
+    const cplx su = mue[s];
+    const double sh = J->h[s];
     cplx sexd[2] = {c_exp(-sr * (sh - zs)), c_exp(-sv * (sh - zs))};
     cplx sexu[2] = {c_exp(-sr * zs), c_exp(-sv * zs)};
     const cplx (*RD)[2] = (const cplx (*)[2])G[s + 1].rdu1;
@@ -835,12 +847,12 @@ static void m2vec(m2_t a, const cplx x[2], cplx y[2])
 
 typedef struct {
     cplx a, b, r, v, x, rmv, wa2, wb2;
-    double mu;
+    cplx mu;
     cplx p[4], d[4];
     cplx detG, detH, detT;
 } slay_t;
 
-static void slayer(double k, cplx w, cplx a, cplx b, double mu, slay_t *L)
+static void slayer(double k, cplx w, cplx a, cplx b, cplx mu, slay_t *L)
 {
     cplx wa = w / a, wb = w / b;
     L->a = a; L->b = b; L->mu = mu;
@@ -931,7 +943,9 @@ static void point_eval_stable(const grto_job *J, const cplx *alpha, const cplx *
     static __thread smrt_t M[GRTO_MAXL];
     static __thread m2_t Rud[GRTO_MAXL + 1], Rdu[GRTO_MAXL + 1], Tu[GRTO_MAXL + 1], Td[GRTO_MAXL + 1];
     static __thread cplx rud0[GRTO_MAXL + 1], rdu0[GRTO_MAXL + 1], tu0[GRTO_MAXL + 1], td0[GRTO_MAXL + 1];
-    for (int i = 0; i < L; i++) slayer(k, w, alpha[i], beta[i], J->mu[i], &Ls[i]);
+    cplx mue[GRTO_MAXL];
+    shear_moduli(J, beta, mue);
+    for (int i = 0; i < L; i++) slayer(k, w, alpha[i], beta[i], mue[i], &Ls[i]);
     for (int j = 0; j < L - 1; j++) sinterface(&Ls[j], &Ls[j + 1], &M[j]);
 
     /* free surface: R = T^{-1} diag(1,-1) T with T = stress rows of E_d */
@@ -983,7 +997,7 @@ static void point_eval_stable(const grto_job *J, const cplx *alpha, const cplx *
     m2_t ED = m2mul(Ldn, m2mul(RD, Ldn)), EU = m2mul(Lup, m2mul(RU, Lup));
     m2_t wru0 = m2add(ED, m2eye(), -1), wrd0 = m2add(m2eye(), EU, -1);
     m2_t wru1 = m2add(ED, m2eye(), 1), wrd1 = m2add(m2eye(), EU, 1);
-    const double su = S->mu;
+    const cplx su = S->mu;
     cplx ssh = 1. / (2. * su * S->v);
     cplx gu0[2], gd0[2], gu1[2], gd1[2], gshu = 0, gshd = 0;
     cplx su0[2], sd0[2], su1[2], sd1[2], su2[2], sd2[2], shu1 = 0, shd1 = 0, shu2 = 0, shd2 = 0;

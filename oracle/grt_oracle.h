@@ -69,6 +69,12 @@ extern "C" {
  * With this bit the moment-tensor SH coefficients satisfy reciprocity with
  * the single-force solution. */
 #define GRTO_FIX_SHSRC 32
+/* Not a correction of a quirk but of a convention, in the oracle only: the
+ * reference's stress terms take the real mu0 = b0^2 rho with attenuated
+ * velocities -- the viscoelastic medium of density rho (b0 / beta(w))^2.
+ * With this bit they take mu = rho beta(w)^2, the standard viscoelastic
+ * medium of density rho. */
+#define GRTO_ATTEN_MU 64
 
 typedef struct grto_job {
     /* model after source-interface insertion (green.cu:1995-2049) */

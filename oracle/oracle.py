@@ -24,6 +24,7 @@ FIX_ALL = FIX_RLAYER | FIX_REXUT | FIX_DZ
 STABLE = 8
 FIX_COLS = 16   # corrected output columns (not the reference layout)
 FIX_SHSRC = 32  # moment-tensor SH source terms with the jump structure of their order
+ATTEN_MU = 64   # standard viscoelastic shear modulus rho beta(w)^2 (oracle only)
 MAXL = 256
 
 

@@ -181,3 +181,26 @@ def test_attenuation_convention(oracle):
     standard = scale * _stokes_spectrum(w, R, gam, 100.0, 50.0, lambda be: RHO)
     assert np.abs(ours - reference).max() <= 1e-3 * np.abs(reference).max()
     assert np.abs(ours - standard).max() >= 2e-2 * np.abs(standard).max()
+
+
+def test_standard_viscoelastic_option(oracle):
+    """The oracle's ATTEN_MU (mu = rho beta(w)^2, not in the CUDA library) is the
+    standard viscoelastic medium: its spectra equal Stokes' solution with the
+    real density -- the reference for a future library option."""
+    hs, hr = 1000.0, 1020.0
+    R = math.hypot(DIST, hr - hs)
+    gam = np.array([DIST / R, (hr - hs) / R])
+
+    def spectra(Q, extra):
+        job = oracle.model([0.0, 3000.0], [ALPHA] * 2, [BETA] * 2, [RHO] * 2, [2 * Q] * 2, [Q] * 2, hs, hr, 0)
+        oracle.setup(job, DT, LOG2N, 0.0, 0.3, math.pi, oracle.K_FIXED, NK, 0.0,
+                     oracle.FIX_ALL | oracle.STABLE | extra)
+        s, _ = oracle.run(job, [DIST], want_sig=False)
+        iw = np.arange(5, int(0.6 * job.nw))
+        return np.array([s[0, iw, 1], -s[0, iw, 4]]), 2 * math.pi * job.df * iw - 1j * job.sigma
+
+    ours, w = spectra(1e6, oracle.ATTEN_MU)
+    scale = np.mean(ours / _stokes_spectrum(w, R, gam, 2e6, 1e6, lambda be: RHO))
+    ours, w = spectra(50.0, oracle.ATTEN_MU)
+    standard = scale * _stokes_spectrum(w, R, gam, 100.0, 50.0, lambda be: RHO)
+    assert np.abs(ours - standard).max() <= 1e-3 * np.abs(standard).max()

@@ -270,3 +270,21 @@ def test_receiver_derivative_terms(oracle, branch):
     expect_rexut = branch in ("same layer, receiver below", "receiver above, other layer",
                               "receiver below, other layer")
     assert (rexut_quirk > 0.1) == expect_rexut, rexut_quirk
+
+
+@pytest.mark.parametrize("src", [0, 1])
+def test_standard_viscoelastic_option_is_continuous(oracle, src):
+    """With the oracle's ATTEN_MU (mu = rho beta(w)^2) the tractions are
+    continuous under the standard law, where Q changes across interfaces."""
+    model = _models()["crust15"]
+    tops = model[0]
+    fix = oracle.FIX_ALL | oracle.FIX_SHSRC | oracle.ATTEN_MU
+    eps = 1e-10
+    for i in (1, 2, 4):
+        for iw, k in POINTS:
+            psv, sh, _ = _jumps(oracle, model, 0.5 * (tops[5] + tops[6]), tops[i] - eps, tops[i] + eps, src, fix,
+                                lambda w: _lame_attenuated(model, i - 1, w), lambda w: _lame_attenuated(model, i, w),
+                                iw, k)
+            for up, dn in list(psv.values()) + list(sh.values()):
+                for a, b in zip(up, dn):
+                    assert _rel(a, b) < 1e-7, (i, iw, k)

@@ -94,11 +94,12 @@ def _tensor_relations(t, f, k):
     ]
 
 
+@pytest.mark.parametrize("atten_mu", [False, True])
 @pytest.mark.parametrize("stable", [False, True])
 @pytest.mark.parametrize("name", ["crust4", "crust12"])
-def test_moment_tensor_reciprocity_with_sh_source_fix(oracle, name, stable):
+def test_moment_tensor_reciprocity_with_sh_source_fix(oracle, name, stable, atten_mu):
     model = _models()[name]
-    fix = oracle.FIX_ALL | oracle.FIX_SHSRC | (oracle.STABLE if stable else 0)
+    fix = oracle.FIX_ALL | oracle.FIX_SHSRC | (oracle.STABLE if stable else 0) | (oracle.ATTEN_MU if atten_mu else 0)
     for zs, zr in _pairs(model):
         for iw, k in POINTS:
             t = _coef(oracle, model, zs, zr, 1, fix, iw, k)
