@@ -147,3 +147,43 @@ def test_options_out_of_range():
         assert _status(grid_with(k_mode=g.K_CUSTOM, nk_custom=nk, k_stride=st)) == g.ERR_ARG
     # a stride without a custom grid
     assert _status(grid_with(k_stride=np.ones(128, dtype=np.int32))) == g.ERR_ARG
+
+
+def test_grid_matches_oracle_on_random_jobs(oracle):
+    """200 seeded random jobs (2-60 layers, any source / receiver depth above the
+    half-space, 2^6-2^13 samples, dt 0.01-0.5 s, both receiver-layer rules):
+    the library's set-up and the oracle agree on every layer index, depth and
+    step and on each frequency's wavenumber count (their sum and maximum)."""
+    import grtm_cuda_gb300 as g
+    from grtm_cuda_gb300 import synth
+    rng = np.random.default_rng(77)
+    checked = 0
+    for _ in range(200):
+        n = int(rng.integers(1, 60))
+        mk = synth.crust(rng, n, 1.0)
+        depth = float(mk["ztop"][-1])
+        hs = float(rng.uniform(0.05, depth - 0.3))
+        hr = float(rng.choice([0.0, rng.uniform(0.0, depth - 0.3)]))
+        src = int(rng.integers(0, 2))
+        dt, log2n = float(rng.uniform(0.01, 0.5)), int(rng.integers(6, 14))
+        fix = int(rng.integers(0, 2))
+        m = g.make_model(mk["ztop"], mk["vp"], mk["vs"], mk["rho"], mk["qp"], mk["qs"], hs, hr, src)
+        o = g.make_opts(dt, log2n, 0.0, 0.3, 2.0, g.K_REFERENCE, 0, fix=fix)
+        job = oracle.model(mk["ztop"], mk["vp"], mk["vs"], mk["rho"], mk["qp"], mk["qs"], hs, hr, src)
+        try:
+            rep = g.grid(m, o)
+        except g.GrtError as e:
+            # the reference's receiver search (fix 0) can leave the receiver
+            # without a layer; the oracle refuses the same jobs
+            with pytest.raises(RuntimeError):
+                oracle.setup(job, dt, log2n, 0.0, 0.3, 2.0, oracle.K_REFERENCE, 0, fix=fix)
+            assert e.status == g.ERR_MODEL and fix == 0
+            continue
+        oracle.setup(job, dt, log2n, 0.0, 0.3, 2.0, oracle.K_REFERENCE, 0, fix=fix)
+        nk = oracle.nk_list(job)
+        assert (rep["n_layer"], rep["s_layer"], rep["r_layer"]) == (job.n_layer, job.s_layer, job.r_layer)
+        assert rep["zs"] == pytest.approx(job.zs, abs=1e-9) and rep["zr"] == pytest.approx(job.zr, abs=1e-9)
+        assert rep["dk"] == pytest.approx(job.dk, rel=1e-14) and rep["sigma"] == pytest.approx(job.sigma, rel=1e-14)
+        assert rep["n_wk"] == int(nk.sum()) and rep["nk_max"] == int(nk.max())
+        checked += 1
+    assert checked >= 150
