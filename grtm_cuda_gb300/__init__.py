@@ -596,12 +596,14 @@ def run(model, opts, dists, ctx=None, spectra=False):
             ctx.close()
 
 
-def run_noalloc(model, opts, dists, device=0, n_cols=None):
+def run_noalloc(model, opts, dists, device=0):
     """grt_run_noalloc: the same traces as run() for small FP32 jobs, with no
-    device allocation (library-owned scratch; see the C header)."""
+    device allocation (library-owned scratch; see the C header).  The C call
+    writes 15 columns for a single force and 20 for a moment tensor (it
+    refuses the corrected 30-column layout), so the output is sized from the
+    source type."""
     d = _arr(np.atleast_1d(dists))
-    if n_cols is None:
-        n_cols = 15 if model.src_type == 0 else 20
+    n_cols = 15 if model.src_type == 0 else 20
     out = np.empty((len(d), n_cols, 1 << opts.log2n))
     rc = lib().grt_run_noalloc(int(device), ctypes.byref(model), ctypes.byref(opts), len(d), _ptr(d), _ptr(out))
     if rc:

@@ -11,14 +11,19 @@
 // lives in one file-scope device array of kScratchBytes.  The host-side job
 // tables are staged in a file-scope host array of kStageBytes.
 //
-// Set-up: the first call on a device (made current by that call) looks up the
-// array's device address with cudaGetSymbolAddress and keeps it; make that
-// first call before any stream capture.  Every GPU that loads the library
-// holds the array until the process exits.  All calls share the array (and
-// the host staging array): calls that overlap on the GPU, or run from several
-// host threads at once, race.  The only scratch word that must start at zero
-// (the device error flag) is cleared by every call; all other scratch is
-// fully written before it is read.
+// Set-up: every call makes its device current and looks up the array's device
+// address there with cudaGetSymbolAddress (cheap, allocates nothing), so a
+// context torn down and recreated by the caller (cudaDeviceReset) never leaves
+// a stale address behind.  The call copies synchronously and waits for its
+// kernels, so no part of it may be captured into a CUDA graph.  A device takes
+// the array when the library's kernels are first loaded there (with CUDA's
+// default lazy loading, at the first grt_run_noalloc call on that device;
+// with CUDA_MODULE_LOADING=EAGER, when the context is created) and holds it
+// until the process exits.  All calls share the array (and the host staging
+// array): calls that overlap on the GPU, or run from several host threads at
+// once, race.  The only scratch word that must start at zero (the device
+// error flag) is cleared by every call; all other scratch is fully written
+// before it is read.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -38,14 +43,12 @@ namespace {
 
 constexpr size_t kScratchBytes = 32ull << 20;  // device scratch per GPU: 32 MiB
 constexpr size_t kStageBytes = 4ull << 20;     // host staging of the job tables: 4 MiB
-constexpr int kMaxDevices = 64;
 constexpr double PI = 3.1415926535897932384626433;
 
 }  // namespace
 
 static __device__ __align__(256) unsigned char g_grt_scratch[kScratchBytes];
 alignas(256) static unsigned char g_grt_stage[kStageBytes];
-static void *g_scratch_addr[kMaxDevices];
 
 static size_t up256(size_t n) { return (n + 255) & ~size_t(255); }
 
@@ -67,21 +70,23 @@ extern "C" GRT_API int grt_run_noalloc(int device, const grt_model *m, const grt
     using grt::Job;
     using cd = std::complex<double>;
     if (!m || !o || !dist || !traces || n_dist < 1) return fail(GRT_ERR_ARG, "null argument or no receivers");
-    if (device < 0 || device >= kMaxDevices) return fail(GRT_ERR_ARG, "device ordinal out of range");
+    if (device < 0) return fail(GRT_ERR_ARG, "device ordinal out of range");
     if (o->precision != GRT_FP32) return fail(GRT_ERR_ARG, "the allocation-free entry point runs in FP32 only");
     for (int i = 0; i < n_dist; i++)
         if (!(dist[i] > 0)) return fail(GRT_ERR_ARG, "distances must be > 0");
 
-    // set-up, once per device, with that device current
+    // the scratch array's address on this device, looked up on every call with
+    // the device current (host code must never pass g_grt_scratch itself: in
+    // host code that name is a host-side stand-in, not a device address)
     CUN(cudaSetDevice(device));
-    if (!g_scratch_addr[device]) {
+    unsigned char *scratch = nullptr;
+    {
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_grt_scratch);
         if (e != cudaSuccess || !p)
             return fail(GRT_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-        g_scratch_addr[device] = p;
+        scratch = (unsigned char *)p;
     }
-    unsigned char *scratch = (unsigned char *)g_scratch_addr[device];
 
     if (o->k_mode == GRT_K_CUSTOM || o->k_stride) return fail(GRT_ERR_UNSUPPORTED, "custom k grids need grt_run");
     if (o->fix & GRT_FIX_COLS) return fail(GRT_ERR_UNSUPPORTED, "corrected column layouts need grt_run");

@@ -315,13 +315,18 @@ GRT_API int grt_run(grt_ctx *ctx, const grt_model *model, const grt_opts *opts, 
  * with a fixed device budget) or code running where cudaMalloc is not
  * permitted.  Same traces as grt_run (FP32 only) for small jobs, allocating
  * nothing on the device: all intermediates live in one library-owned device
- * array of 32 MiB per GPU (held from library load until exit) and the job
- * tables in a 4 MiB host array.  Jobs that need more return
- * GRT_ERR_UNSUPPORTED with the sizes on stderr.  The first call on a device
- * does a one-time set-up (cudaGetSymbolAddress); make it before any stream
+ * array of 32 MiB per GPU and the job tables in a 4 MiB host array.  A GPU
+ * takes the device array when the library's kernels are first loaded on it
+ * (with CUDA's default lazy module loading, at the first grt_run_noalloc call
+ * there; with CUDA_MODULE_LOADING=EAGER, when its context is created) and
+ * holds it until the process exits.  Jobs that need more return
+ * GRT_ERR_UNSUPPORTED with the sizes on stderr.  Every call looks up the
+ * array's address on `device` (cudaGetSymbolAddress, no allocation), copies
+ * synchronously and waits for its kernels: do not call it inside a stream
  * capture.  Calls share the arrays: calls that overlap on the GPU, or come
  * from several host threads at once, race.  Runs on the default stream of
- * `device`; traces: host [n_dist][n_cols][N] doubles.
+ * `device`; traces: host [n_dist][n_cols][N] doubles (n_cols 15 for a single
+ * force, 20 for a moment tensor).
  * Reference-rule and fixed grids of all frequencies only (GRT_K_CUSTOM or a
  * frequency selection: GRT_ERR_UNSUPPORTED).
  * No counterpart in the reference. */

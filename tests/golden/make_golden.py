@@ -5,7 +5,7 @@ GPU library wrote for it, demo/oname_w.txt (spectra) and demo/oname_t.txt
 (time series).  This script copies the input and packs the defined part of the
 outputs (columns 0-14 of a single-force run; columns 15-29 are zero there) into
 tests/golden/demo_golden.npz.  It needs the reference checkout, so it runs only
-where that is mounted:
+where that is mounted, given as the argument or as GRTM_REFERENCE:
 
     python tests/golden/make_golden.py /path/to/reference
 """
@@ -52,4 +52,7 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("GRTM_REFERENCE")
+    if not ref:
+        sys.exit("usage: make_golden.py REFERENCE_CHECKOUT (or set GRTM_REFERENCE)")
+    main(ref)

@@ -49,9 +49,9 @@ def test_gpu_moment_tensor_equals_aki_richards(gctx, hs, hr, prec):
 
 
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
-def test_gpu_single_force_equals_stokes(gctx, prec):
+@pytest.mark.parametrize("hs,hr", [(60.0, 80.0), (80.0, 60.0)])
+def test_gpu_single_force_equals_stokes(gctx, hs, hr, prec):
     g, ctx = gctx
-    hs, hr = 60.0, 80.0
     tr = _gpu_traces(g, ctx, hs, hr, 0, g.FP64 if prec == "fp64" else g.FP32)
     for F in ([0.0, 0.0, 1.0], [1.0, 0.0, 0.0], [0.3, -0.7, 0.5]):
         ours = A._convolve(g.sf_weights(F, A.PHI) @ tr)
