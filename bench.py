@@ -49,9 +49,12 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-F_LAYER = 1490.0   # algorithmic flops per (w,k,layer), counted on the method (cmul 6, cdiv 11, cexp/csqrt 20)
-F_SRC_TENSOR = 710.0
-F_SRC_SINGLE = 449.0
+# Algorithmic flops per (w,k) point: L * F_LAYER + F_SRC, counted by the
+# operation-counting oracle (oracle/op_count.py: cmul 6, cadd 2, cdiv 11,
+# cexp/csqrt/clog 20; every layer, per-frequency quantities excluded)
+F_LAYER = 1465
+F_SRC_TENSOR = 2631
+F_SRC_SINGLE = 2348
 
 
 WORKLOAD_CRUST20 = dict(dt=0.05, log2n=12, t0=0.0, taper=0.3, sigma_factor=np.pi, nk=16384)

@@ -20,7 +20,6 @@
  */
 #include "grt_oracle.h"
 
-#include <complex.h>
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -29,7 +28,17 @@
 #include <omp.h>
 #endif
 
+#ifdef GRTO_COUNT
+/* op_count.cpp builds this file as C++ with an operation-counting complex type */
+#include "grt_count.hpp"
+thread_local grto_tally grto_cnt;
+#else
+#include <complex.h>
 typedef double _Complex cplx;
+#define GRTO_COUNT_PAUSE ((void)0)
+#define GRTO_COUNT_RESUME ((void)0)
+#define GRTO_COUNT_FN(n) ((void)0)
+#endif
 
 #define PI 3.1415926535897932384626433
 #define PI2 (3.1415926535897932384626433 * 2)
@@ -38,17 +47,33 @@ typedef double _Complex cplx;
 /* complex helpers (cucomplex.hpp semantics)                           */
 /* ------------------------------------------------------------------ */
 static inline cplx mkc(double re, double im) { return re + im * I; }
-static inline cplx c_log(cplx z) { return mkc(log(hypot(creal(z), cimag(z))), atan2(cimag(z), creal(z))); }
+/* (the operation count takes 20 for each of these three) */
+static inline cplx c_log(cplx z)
+{
+    GRTO_COUNT_FN(20);
+    GRTO_COUNT_PAUSE;
+    cplx r = mkc(log(hypot(creal(z), cimag(z))), atan2(cimag(z), creal(z)));
+    GRTO_COUNT_RESUME;
+    return r;
+}
 static inline cplx c_sqrt(cplx z)
 {
+    GRTO_COUNT_FN(20);
+    GRTO_COUNT_PAUSE;
     double m = sqrt(hypot(creal(z), cimag(z)));
     double t = atan2(cimag(z), creal(z)) / 2.0;
-    return mkc(m * cos(t), m * sin(t));
+    cplx r = mkc(m * cos(t), m * sin(t));
+    GRTO_COUNT_RESUME;
+    return r;
 }
 static inline cplx c_exp(cplx z)
 {
+    GRTO_COUNT_FN(20);
+    GRTO_COUNT_PAUSE;
     double e = exp(creal(z));
-    return mkc(e * cos(cimag(z)), e * sin(cimag(z)));
+    cplx r = mkc(e * cos(cimag(z)), e * sin(cimag(z)));
+    GRTO_COUNT_RESUME;
+    return r;
 }
 
 /* 2x2 inverse in place, green.cu:388-400 (mat_inv_2) */
@@ -854,16 +879,20 @@ typedef struct {
 
 static void slayer(double k, cplx w, cplx a, cplx b, cplx mu, slay_t *L)
 {
+    /* (w/a)^2, (w/b)^2 and their difference depend on the frequency only:
+     * not counted as per-(w,k) work */
+    GRTO_COUNT_PAUSE;
     cplx wa = w / a, wb = w / b;
     L->a = a; L->b = b; L->mu = mu;
     L->wa2 = wa * wa;
     L->wb2 = wb * wb;
+    cplx W = L->wb2 - L->wa2;          /* v^2 - r^2 with sign: r^2 - v^2 = W */
+    GRTO_COUNT_RESUME;
     L->r = c_sqrt(k * k - L->wa2);
     L->v = c_sqrt(k * k - L->wb2);
     if (creal(L->r) < 0) L->r = -L->r;
     if (creal(L->v) < 0) L->v = -L->v;
     L->x = k * k + L->v * L->v;
-    cplx W = L->wb2 - L->wa2;          /* v^2 - r^2 with sign: r^2 - v^2 = W */
     cplx rpv = L->r + L->v;
     L->rmv = W / rpv;                    /* r - v */
     cplx dv = L->wb2 / (k + L->v);       /* k - v */
@@ -944,7 +973,9 @@ static void point_eval_stable(const grto_job *J, const cplx *alpha, const cplx *
     static __thread m2_t Rud[GRTO_MAXL + 1], Rdu[GRTO_MAXL + 1], Tu[GRTO_MAXL + 1], Td[GRTO_MAXL + 1];
     static __thread cplx rud0[GRTO_MAXL + 1], rdu0[GRTO_MAXL + 1], tu0[GRTO_MAXL + 1], td0[GRTO_MAXL + 1];
     cplx mue[GRTO_MAXL];
+    GRTO_COUNT_PAUSE;
     shear_moduli(J, beta, mue);
+    GRTO_COUNT_RESUME;
     for (int i = 0; i < L; i++) slayer(k, w, alpha[i], beta[i], mue[i], &Ls[i]);
     for (int j = 0; j < L - 1; j++) sinterface(&Ls[j], &Ls[j + 1], &M[j]);
 
@@ -1225,6 +1256,23 @@ int grto_point(const grto_job *J, int iw, double k, double *out)
     for (int i = 0; i < 16; i++) { out[2 * i] = creal(v[i]); out[2 * i + 1] = cimag(v[i]); }
     return GRTO_OK;
 }
+
+#ifdef GRTO_COUNT
+/* Complex operations of one per-(w,k) evaluation (point_any), the
+ * per-frequency attenuation and slot-0 wavenumbers excluded. */
+extern "C" long long grto_count_point(const grto_job *J, int iw, double k)
+{
+    cplx a[GRTO_MAXL], b[GRTO_MAXL], slot0[2];
+    ypar_t Y;
+    cplx w = omega(J, iw);
+    attenuate(J, w, a, b);
+    slot0_nu(J, slot0);
+    grto_cnt.flops = 0;
+    grto_cnt.paused = 0;
+    point_any(J, a, b, k, w, slot0, &Y);
+    return grto_cnt.flops;
+}
+#endif
 
 int grto_integrand(const grto_job *J, int iw, double k, double r, double *out)
 {
