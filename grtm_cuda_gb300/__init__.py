@@ -18,6 +18,7 @@ LIB_PATH = os.environ.get("GRTM_GB300_LIB", os.path.join(HERE, "_lib", "libgrtm_
 OK, ERR_ARG, ERR_IO, ERR_PARSE, ERR_MODEL, ERR_CUDA, ERR_NOMEM, ERR_TIMEOUT, ERR_UNSUPPORTED = range(9)
 K_REFERENCE, K_FIXED, K_CUSTOM = 0, 1, 2
 FP32, FP64 = 0, 1
+TC_3XTF32, TC_3XBF16 = 0, 1   # split forms of the tensor-core wavenumber sum
 FIX_RLAYER, FIX_REXUT, FIX_DZ, FIX_COLS = 1, 2, 4, 8
 FIX_SHSRC = 16   # moment-tensor SH source terms with the jump structure of their order
 FIX_ALL = FIX_RLAYER | FIX_REXUT | FIX_DZ
@@ -40,7 +41,7 @@ class Opts(ctypes.Structure):
                 ("nk_fixed", ctypes.c_int), ("dk", ctypes.c_double), ("precision", ctypes.c_int),
                 ("fix", ctypes.c_int), ("nk_custom", ctypes.POINTER(ctypes.c_int)),
                 ("k_stride", ctypes.POINTER(ctypes.c_int)), ("n_freq_sel", ctypes.c_int),
-                ("freq_sel", ctypes.POINTER(ctypes.c_int)), ("k_slice", ctypes.c_int)]
+                ("freq_sel", ctypes.POINTER(ctypes.c_int)), ("k_slice", ctypes.c_int), ("tc_split", ctypes.c_int)]
 
 
 class Report(ctypes.Structure):
@@ -182,7 +183,8 @@ EXPORTS = ("grt_create", "grt_destroy", "grt_last_error", "grt_status_string", "
            "grt_sf_weights",
            "grt_plan_synth",
            "grt_batch_synth", "grt_flatten", "grt_plan_write", "grt_plan_fetch_f32", "grt_batch_fetch_f32",
-           "grt_host_alloc", "grt_host_free", "grt_trim", "grt_batch_fetch_f32_async", "grt_batch_wait")
+           "grt_host_alloc", "grt_host_free", "grt_trim", "grt_batch_fetch_f32_async", "grt_batch_wait",
+           "grt_plan_error_estimate", "grt_batch_error_estimate")
 
 _lib = None
 
@@ -262,6 +264,8 @@ def lib():
     L.grt_sf_weights.argtypes = [_dp, ctypes.c_double, _dp]
     L.grt_sf_weights.restype = None
     L.grt_plan_synth.argtypes = [vp, P(Source), _dp, _dp]
+    L.grt_plan_error_estimate.argtypes = [vp, ctypes.c_double, _dp]
+    L.grt_batch_error_estimate.argtypes = [vp, ctypes.c_int, ctypes.c_double, _dp]
     L.grt_batch_synth.argtypes = [vp, ctypes.c_int, P(Source), _dp, _dp]
     _lib = L
     return L
@@ -318,13 +322,14 @@ def make_model(ztop, vp, vs, rho, qp, qs, hs, hr=0.0, src_type=0):
 
 
 def make_opts(dt, log2n, t0=0.0, taper=0.3, sigma_factor=2.0, k_mode=K_REFERENCE, nk_fixed=0, dk=0.0,
-              precision=FP32, fix=0, nk_custom=None, k_stride=None, freq_sel=None, k_slice=0):
+              precision=FP32, fix=0, nk_custom=None, k_stride=None, freq_sel=None, k_slice=0, tc_split=0):
     """nk_custom: points per frequency (N/2 ints) for K_CUSTOM grids;
     k_stride: optional per-frequency stride m (k_j = j m dk);
     freq_sel: evaluate only these frequency indices (a spectra-only plan);
-    k_slice: wavenumbers per split-K slice of the tensor-core sum (0: auto)."""
+    k_slice: wavenumbers per split-K slice of the tensor-core sum (0: auto);
+    tc_split: TC_3XTF32 (default) or TC_3XBF16, the split form of the tensor-core sum."""
     o = Opts(float(dt), int(log2n), float(t0), float(taper), float(sigma_factor), int(k_mode),
-             int(nk_fixed), float(dk), int(precision), int(fix), None, None, 0, None, int(k_slice))
+             int(nk_fixed), float(dk), int(precision), int(fix), None, None, 0, None, int(k_slice), int(tc_split))
     o._keep = []
     if nk_custom is not None:
         arr = np.ascontiguousarray(nk_custom, dtype=np.int32)
@@ -391,6 +396,16 @@ class Plan:
         if rc:
             raise GrtError(rc, self.ctx.error())
         return out
+
+    def error_estimate(self, eps=0.0):
+        """Predicted relative L2 error of each receiver's traces against the
+        FP64 path (grt_plan_error_estimate; eps 0: the coefficients' noise
+        measured against FP64 at spot frequencies)."""
+        est = np.empty(len(self.dists))
+        rc = lib().grt_plan_error_estimate(self.h, float(eps), _ptr(est))
+        if rc:
+            raise GrtError(rc, self.ctx.error())
+        return est
 
     def fetch_freqs(self, freq_idx):
         """Spectra at selected frequency indices: complex [n_dist, n_cols, n_freq]."""
@@ -556,6 +571,14 @@ class Batch:
             raise GrtError(rc, self.ctx.error())
         return out
 
+    def error_estimate(self, job, eps=0.0):
+        """grt_batch_error_estimate: predicted per-receiver error of a job's traces."""
+        est = np.empty(len(self.dists[job]))
+        rc = lib().grt_batch_error_estimate(self.h, int(job), float(eps), _ptr(est))
+        if rc:
+            raise GrtError(rc, self.ctx.error())
+        return est
+
     def fetch_freqs(self, job, freq_idx):
         r, _ = self.info(job)
         fi = np.ascontiguousarray(freq_idx, dtype=np.int32)
@@ -591,6 +614,40 @@ def run(model, opts, dists, ctx=None, spectra=False):
         rep = p.report.as_dict()
         p.close()
         return t, s, rep
+    finally:
+        if own:
+            ctx.close()
+
+
+def with_precision(opts, precision):
+    """A copy of opts at another working precision (arrays shared)."""
+    o = Opts.from_buffer_copy(opts)
+    o.precision = int(precision)
+    o._keep = getattr(opts, "_keep", [])
+    return o
+
+
+def run_judged(model, opts, dists, ctx=None, tol=1e-3, eps=0.0, safety=3.0):
+    """FP32 traces, judged: every receiver whose predicted error against FP64
+    (grt_plan_error_estimate) exceeds tol / safety is recomputed by the FP64
+    path.
+
+    Returns (traces [n_dist, n_cols, N], info) with info["est"] the predicted
+    errors, info["fp64"] the receivers recomputed."""
+    own = ctx is None
+    ctx = ctx or Context()
+    try:
+        d = _arr(np.atleast_1d(dists))
+        p = Plan(ctx, model, with_precision(opts, FP32), d)
+        p.execute()
+        t, _ = p.fetch(True, False)
+        est = p.error_estimate(eps)
+        p.close()
+        bad = np.nonzero(est * safety > tol)[0]
+        if bad.size:
+            t64, _, _ = run(model, with_precision(opts, FP64), d[bad], ctx)
+            t[bad] = t64
+        return t, {"est": est, "fp64": bad}
     finally:
         if own:
             ctx.close()

@@ -25,6 +25,8 @@ using grt::Job;
 using cd = std::complex<double>;
 static const double PI = 3.1415926535897932384626433;
 
+#include <cublas_v2.h>
+
 #include "grt_ctx.h"
 
 struct grt_plan {
@@ -34,7 +36,14 @@ struct grt_plan {
     int nd = 0, nc = 0, nq = 0, ntiles = 0;
     int rt = 128, jt = 1;
     int use_tc = 0, nsplit = 1, kslice = 0;   // tensor-core wavenumber sum and its split-K
+    // plain FP32 sum as SGEMMs (unit k strides, outside batches): planar
+    // coefficients [nq][2][nw][nkp], one Bessel operand [nkp][nd], pair products
+    // [gslices][np][2][nw][nd]
+    bool gemm_ok = false;
+    float *Ag = nullptr, *Bg = nullptr, *Dg = nullptr;
+    int nkp = 0, gslices = 1;
     int kslice_req = 0;                       // requested k per slice (0: chosen here)
+    int tc_bf16 = 0;                          // tensor-core sum in the 3xBF16 form (else 3xTF32)
     int gspec = 0;                            // compiled form of the GRT evaluation (grt::GrtSpec)
     int bt_rows = 0;                          // > 0: Bessel table tiled by 32 receivers (unit strides)
     int cols = 0;                             // output column layout (grt::ColKind)
@@ -52,6 +61,7 @@ struct grt_plan {
     double *ddist = nullptr, *damp = nullptr;
     unsigned *derr = nullptr;
     bool own_derr = true;                     // false inside a batch (the batch's error word)
+    bool ran = false;                         // executed at least once (traces on the device)
     grt_report rep{};
 };
 
@@ -187,6 +197,7 @@ extern "C" void grt_destroy(grt_ctx *ctx)
         cudaStreamSynchronize(ctx->stream);
         cudaStreamDestroy(ctx->stream);
     }
+    if (ctx->blas) cublasDestroy((cublasHandle_t)ctx->blas);
     pool_trim(ctx, 0);
     delete ctx;
 }
@@ -198,7 +209,8 @@ extern "C" void grt_plan_destroy(grt_plan *p)
     if (!p) return;
     cudaSetDevice(p->ctx->device);
     void *bufs[] = {p->tab, p->K, p->B, p->S, p->post, p->tw, p->spec, p->sig, p->tiles, p->nk, p->koff, p->ddist,
-                    p->damp, p->own_derr ? p->derr : nullptr, p->P, p->Kt, p->kt_base, p->ks, p->tfirst};
+                    p->damp, p->own_derr ? p->derr : nullptr, p->P, p->Kt, p->kt_base, p->ks, p->tfirst,
+                    p->Ag, p->Bg, p->Dg};
     for (void *b : bufs) dev_free(p->ctx, b);
     delete p;
 }
@@ -234,6 +246,10 @@ static int tc_tiles(int kind)
     constexpr grt::TcPlan ts = grt::make_tcplan<grt::kColSingle>(), tt = grt::make_tcplan<grt::kColTensor>();
     return kind == grt::kColTensor ? tt.nqu : (kind == grt::kColTensorFix ? 0 : ts.nqu);
 }
+static const grt::ColTerms kColTermsTab[4] = {grt::make_colterms<grt::kColSingle>(), grt::make_colterms<grt::kColTensor>(),
+                                              grt::make_colterms<grt::kColSingleFix>(),
+                                              grt::make_colterms<grt::kColTensorFix>()};
+
 static int coef_count(int kind)
 {
     return kind == grt::kColTensorFix ? 2 * (int)grt::QT_N : (kind == grt::kColTensor ? (int)grt::QT_N : (int)grt::QS_N);
@@ -294,7 +310,8 @@ static int upload(grt_plan *p)
     // every frequency has a unit stride (a stage's rows are then contiguous)
     bool unit = true;
     for (int m : J.ks) unit = unit && m == 1;
-    if (p->use_tc && unit) p->bt_rows = (J.nbrow + grt::tc::kKT - 1) / grt::tc::kKT * grt::tc::kKT;
+    const int KT = p->tc_bf16 ? grt::tc::TcPrec<grt::tc::kBF16>::KT : grt::tc::TcPrec<grt::tc::kTF32>::KT;
+    if (p->use_tc && unit) p->bt_rows = (J.nbrow + KT - 1) / KT * KT;
     const size_t szB = p->bt_rows ? (size_t)((p->nd + grt::kBesselTile - 1) / grt::kBesselTile) * grt::kBesselTile *
                                         p->bt_rows * grt::NBASIS * sizeof(R)
                                   : (size_t)J.nbrow * grt::NBASIS * p->nd * sizeof(R);
@@ -327,7 +344,7 @@ static int upload(grt_plan *p)
             2LL * ((J.nw + grt::tc::kW - 1) / grt::tc::kW) * ((p->nd + grt::tc::kN - 1) / grt::tc::kN);
         int best = 1;
         double best_cost = 1e30;
-        const int maxs = std::max(1, std::min(64, J.nkmax / (8 * grt::tc::kKT)));
+        const int maxs = std::max(1, std::min(64, J.nkmax / (8 * KT)));
         for (int s = 1; s <= maxs; s++) {
             const long long n = tiles * s;
             const long long waves = (n + nsm - 1) / nsm;
@@ -336,7 +353,7 @@ static int upload(grt_plan *p)
             if (cost < best_cost) { best_cost = cost; best = s; }
         }
         p->nsplit = best;
-        p->kslice = ((J.nkmax + best - 1) / best + grt::tc::kKT - 1) / grt::tc::kKT * grt::tc::kKT;
+        p->kslice = ((J.nkmax + best - 1) / best + KT - 1) / KT * KT;
         if (p->kslice_req > 0) {
             p->kslice = p->kslice_req;
             p->nsplit = (J.nkmax + p->kslice - 1) / p->kslice;
@@ -344,7 +361,7 @@ static int upload(grt_plan *p)
         p->rep.k_slice = p->kslice;
         // partial sums of every (k slice, column group)
         CU(dev_alloc(ctx, &p->P, (size_t)p->nsplit * 2 * ntr * J.nw * 2 * sizeof(float)));
-        // operand blocks of (frequency tile of 64, k stage of 8): nq x (hi, lo) x 1024 floats each
+        // operand blocks of (frequency tile of 64, k stage of KT): nq x (hi, lo) x 4 KB each
         const int nwt = (J.nw + grt::tc::kW - 1) / grt::tc::kW;
         std::vector<long long> base(nwt);
         long long tot = 0;
@@ -352,9 +369,9 @@ static int upload(grt_plan *p)
         for (int t = 0; t < nwt; t++) {
             int mx = 0;
             for (int i = t * grt::tc::kW; i < std::min(J.nw, (t + 1) * grt::tc::kW); i++) mx = std::max(mx, J.nk[i]);
-            const int ns = (mx + grt::tc::kKT - 1) / grt::tc::kKT;
+            const int ns = (mx + KT - 1) / KT;
             for (int i = t * grt::tc::kW; i < std::min(J.nw, (t + 1) * grt::tc::kW); i++)
-                if (J.nk[i] != ns * grt::tc::kKT) padded = true;
+                if (J.nk[i] != ns * KT) padded = true;
             base[t] = tot;
             tot += (long long)ns * tc_tiles(p->cols) * 2 * grt::tc::kM * grt::tc::kKT;
         }
@@ -424,8 +441,11 @@ extern "C" int grt_plan_create(grt_ctx *ctx, const grt_model *m, const grt_opts 
     // the corrected 30-column tensor layout needs 16 coefficient columns: beyond the
     // tensor-core sum's shared and tensor memory, it runs the SIMT sum
     p->use_tc = (p->prec == GRT_FP32) && !(ks && !strcmp(ks, "simt")) && p->cols != grt::kColTensorFix;
-    if (o->k_slice < 0 || o->k_slice % grt::tc::kKT)
-        return set_err(ctx, GRT_ERR_ARG, "k_slice must be a non-negative multiple of 8");
+    if (o->tc_split != GRT_TC_3XTF32 && o->tc_split != GRT_TC_3XBF16) return set_err(ctx, GRT_ERR_ARG, "bad tc_split");
+    p->tc_bf16 = o->tc_split == GRT_TC_3XBF16;
+    const int kt_step = p->tc_bf16 ? 16 : 8;
+    if (o->k_slice < 0 || o->k_slice % kt_step)
+        return set_err(ctx, GRT_ERR_ARG, "k_slice must be a non-negative multiple of 8 (16 for the 3xBF16 sum)");
     if (o->k_slice > 0 && (J.nkmax + o->k_slice - 1) / o->k_slice > 4096)
         return set_err(ctx, GRT_ERR_ARG, "k_slice too small: more than 4096 slices");
     p->kslice_req = o->k_slice;
@@ -433,7 +453,12 @@ extern "C" int grt_plan_create(grt_ctx *ctx, const grt_model *m, const grt_opts 
     // reference's 8 coefficient columns) run the GRT evaluation compiled for that case
     p->gspec = (p->prec == GRT_FP32 && J.src == 1 && J.rl < J.s && p->nq == grt::QT_N) ? grt::kSpecAboveTensor
                                                                                        : grt::kSpecGeneric;
-    p->rep.ksum_impl = p->use_tc;
+    p->rep.ksum_impl = p->use_tc ? (p->tc_bf16 ? 3 : 1) : 0;
+    // the plain FP32 sum runs as SGEMMs when every frequency has a unit k stride
+    p->gemm_ok = p->prec == GRT_FP32 && !p->use_tc && p->cols != grt::kColTensorFix;
+    for (int iw = 0; iw < J.nw; iw++) p->gemm_ok = p->gemm_ok && J.ks[iw] == 1;
+    if (p->gemm_ok) p->rep.ksum_impl = 2;
+
     // the tensor-core sum multiplies a tile of 64 frequencies by one Bessel operand:
     // the frequencies of a tile share their k stride
     if (p->use_tc)
@@ -451,19 +476,25 @@ extern "C" int grt_plan_create(grt_ctx *ctx, const grt_model *m, const grt_opts 
 }
 
 template <int SRC>
-static cudaError_t raise_tc_limits()
+static cudaError_t raise_tc_limits(int bf16)
 {
-    return raise_smem_limit(grt::ksum_tc_kernel<SRC>, grt::tc::smem_bytes<SRC>());
+    return bf16 ? raise_smem_limit(grt::ksum_tc_kernel<SRC, grt::tc::kBF16>, grt::tc::smem_bytes<SRC, grt::tc::kBF16>())
+                : raise_smem_limit(grt::ksum_tc_kernel<SRC, grt::tc::kTF32>, grt::tc::smem_bytes<SRC, grt::tc::kTF32>());
 }
 
 // one launch for both column groups: 2 CTAs per (frequency tile, receiver tile, k slice)
-template <int SRC>
-static cudaError_t launch_tc_groups(const grt::KsumTcArgs<float> &T, unsigned grid, cudaStream_t st)
+template <int SRC, int PREC>
+static cudaError_t launch_tc_form(const grt::KsumTcArgs<float> &T, unsigned grid, cudaStream_t st)
 {
-    cudaError_t e = raise_tc_limits<SRC>();
+    cudaError_t e = raise_smem_limit(grt::ksum_tc_kernel<SRC, PREC>, grt::tc::smem_bytes<SRC, PREC>());
     if (e != cudaSuccess) return e;
-    grt::ksum_tc_kernel<SRC><<<2 * grid, grt::tc::kThreads, grt::tc::smem_bytes<SRC>(), st>>>(T);
+    grt::ksum_tc_kernel<SRC, PREC><<<2 * grid, grt::tc::kThreads, grt::tc::smem_bytes<SRC, PREC>(), st>>>(T);
     return cudaGetLastError();
+}
+template <int SRC>
+static cudaError_t launch_tc_groups(const grt::KsumTcArgs<float> &T, unsigned grid, cudaStream_t st, int bf16)
+{
+    return bf16 ? launch_tc_form<SRC, grt::tc::kBF16>(T, grid, st) : launch_tc_form<SRC, grt::tc::kTF32>(T, grid, st);
 }
 
 // tensor-core wavenumber sum (FP32 path): split-K partial sums, then TwoSum reduction
@@ -491,9 +522,9 @@ static int launch_ksum_tc(grt_plan *p, cudaStream_t st, int &launches)
     T.err = p->derr;
     const int nwt = (J.nw + grt::tc::kW - 1) / grt::tc::kW, nrt = (p->nd + grt::tc::kN - 1) / grt::tc::kN;
     const unsigned grid = (unsigned)(nwt * nrt * p->nsplit);
-    if (p->cols == grt::kColSingle) CU(launch_tc_groups<grt::kColSingle>(T, grid, st));
-    else if (p->cols == grt::kColSingleFix) CU(launch_tc_groups<grt::kColSingleFix>(T, grid, st));
-    else CU(launch_tc_groups<grt::kColTensor>(T, grid, st));
+    if (p->cols == grt::kColSingle) CU(launch_tc_groups<grt::kColSingle>(T, grid, st, p->tc_bf16));
+    else if (p->cols == grt::kColSingleFix) CU(launch_tc_groups<grt::kColSingleFix>(T, grid, st, p->tc_bf16));
+    else CU(launch_tc_groups<grt::kColTensor>(T, grid, st, p->tc_bf16));
     launches++;
     const long long n = (long long)p->nd * p->nc * J.nw * 2;
     grt::ksum_tc_reduce_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>((const float *)p->P, (float *)p->S, n,
@@ -527,6 +558,7 @@ static grt::GrtArgs<R> grt_args(const grt_plan *p)
     A.Kt = p->use_tc ? p->Kt : nullptr;
     A.kt_base = p->kt_base;
     A.nqt = tc_tiles(p->cols);
+    A.kt_bf16 = p->tc_bf16;
     return A;
 }
 
@@ -544,6 +576,87 @@ static int launch_bessel(grt_plan *p, cudaStream_t st, int &launches)
     return GRT_OK;
 }
 
+// plain FP32 sum as cuBLAS SGEMMs (see gemm_a_kernel): planar coefficient
+// matrices, then per (power, Bessel function) class its operand and the
+// products of every pair of the class, one per k slice, then the combination
+template <int SRC>
+static cudaError_t launch_gemm_combine(const grt_plan *p, cudaStream_t st)
+{
+    const long long n = (long long)p->J.nw * p->nd;
+    grt::gemm_combine_kernel<SRC><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(p->Dg, p->gslices, p->J.nw, p->nd,
+                                                                              p->ddist, (float *)p->S);
+    return cudaGetLastError();
+}
+
+static int launch_ksum_gemm(grt_plan *p, cudaStream_t st, int &launches)
+{
+    grt_ctx *ctx = p->ctx;
+    const Job &J = p->J;
+    if (!ctx->blas) {
+        cublasHandle_t h = nullptr;
+        if (cublasCreate(&h) != CUBLAS_STATUS_SUCCESS) return set_err(ctx, GRT_ERR_CUDA, "cublasCreate failed");
+        cublasSetMathMode(h, CUBLAS_PEDANTIC_MATH);   // FP32 products and sums, no TF32
+        ctx->blas = h;
+    }
+    cublasHandle_t h = (cublasHandle_t)ctx->blas;
+    if (cublasSetStream(h, st) != CUBLAS_STATUS_SUCCESS) return set_err(ctx, GRT_ERR_CUDA, "cublasSetStream failed");
+    const grt::ColTerms &CT = kColTermsTab[p->cols];
+    if (!p->Ag) {
+        // buffers on first use; k slices of at most 8192 wavenumbers
+        p->nkp = (J.nkmax + 3) / 4 * 4;
+        p->gslices = std::max(1, (p->nkp + 8191) / 8192);
+        CU(dev_alloc(ctx, &p->Ag, (size_t)p->nq * 2 * J.nw * p->nkp * sizeof(float)));
+        CU(dev_alloc(ctx, &p->Bg, (size_t)p->nkp * p->nd * sizeof(float)));
+        CU(dev_alloc(ctx, &p->Dg, (size_t)p->gslices * CT.np * 2 * J.nw * p->nd * sizeof(float)));
+    }
+    const int nw = J.nw, nr = p->nd, nkp = p->nkp;
+    {
+        const long long n = (long long)p->nq * nw * nkp;
+        grt::gemm_a_kernel<<<(unsigned)std::min<long long>((n + 255) / 256, 16384), 256, 0, st>>>(
+            (const float *)p->K, p->nk, p->koff, J.nkw, nw, nkp, p->nq, p->Ag);
+        CU(cudaGetLastError());
+        launches++;
+    }
+    const int klen = (nkp + p->gslices - 1) / p->gslices;
+    const float one = 1.f, zero = 0.f;
+    bool done[48] = {};
+    for (int p0 = 0; p0 < CT.np; p0++) {
+        if (done[p0]) continue;
+        const int kp = CT.pkp[p0], b = CT.pb[p0];
+        const long long n = (long long)nkp * nr;
+        grt::gemm_b_kernel<<<(unsigned)std::min<long long>((n + 255) / 256, 16384), 256, 0, st>>>(
+            (const float *)p->B, J.nbrow, nr, nkp, J.dk, kp, b, p->Bg);
+        CU(cudaGetLastError());
+        launches++;
+        for (int pp = p0; pp < CT.np; pp++) {
+            if (done[pp] || CT.pkp[pp] != kp || CT.pb[pp] != b) continue;
+            done[pp] = true;
+            const float *Aq = p->Ag + (size_t)CT.pq[pp] * 2 * nw * nkp;
+            for (int sl = 0; sl < p->gslices; sl++) {
+                const int k0 = sl * klen, kl = std::min(klen, nkp - k0);
+                float *Dp = p->Dg + ((size_t)sl * CT.np + pp) * 2 * nw * nr;
+                if (kl <= 0) {
+                    CU(cudaMemsetAsync(Dp, 0, (size_t)2 * nw * nr * sizeof(float), st));
+                    continue;
+                }
+                // column-major: D^T [nr x 2nw] = Bc^T [nr x kl] * A^T [kl x 2nw]
+                if (cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, nr, 2 * nw, kl, &one, p->Bg + (size_t)k0 * nr, nr,
+                                Aq + k0, nkp, &zero, Dp, nr) != CUBLAS_STATUS_SUCCESS)
+                    return set_err(ctx, GRT_ERR_CUDA, "cublasSgemm failed");
+                launches++;
+            }
+        }
+    }
+    switch (p->cols) {
+    case grt::kColSingle: CU(launch_gemm_combine<grt::kColSingle>(p, st)); break;
+    case grt::kColSingleFix: CU(launch_gemm_combine<grt::kColSingleFix>(p, st)); break;
+    case grt::kColTensorFix: CU(launch_gemm_combine<grt::kColTensorFix>(p, st)); break;
+    default: CU(launch_gemm_combine<grt::kColTensor>(p, st)); break;
+    }
+    launches++;
+    return GRT_OK;
+}
+
 template <typename R>
 static int launch_ksum(grt_plan *p, cudaStream_t st, int &launches)
 {
@@ -555,6 +668,10 @@ static int launch_ksum(grt_plan *p, cudaStream_t st, int &launches)
     grt::KsumArgs<R> S{};
     S.K = (const R *)p->K; S.B = (const R *)p->B; S.nk = p->nk; S.ks = p->ks; S.koff = p->koff; S.dist = p->ddist;
     S.S = (R *)p->S; S.nkw = J.nkw; S.dk = J.dk; S.nw = J.nw; S.nr = p->nd; S.rt = p->rt; S.jt = p->jt;
+    if constexpr (std::is_same<R, float>::value) {
+        // plans (not batch jobs, whose work is captured in a graph) on unit-stride grids
+        if (p->gemm_ok && p->own_derr) return launch_ksum_gemm(p, st, launches);
+    }
     const int grid = J.nw * ((p->nd + p->rt - 1) / p->rt);
     switch (p->cols) {
     case grt::kColSingle: grt::ksum_kernel<R, grt::kColSingle><<<grid, grt::kSumThreads, 0, st>>>(S); break;
@@ -707,6 +824,7 @@ extern "C" int grt_plan_execute(grt_plan *p, grt_report *r)
     CU(cudaSetDevice(ctx->device));
     int rc = p->prec ? execute<double>(p) : execute<float>(p);
     if (rc) return rc;
+    p->ran = true;
     if (r) grt_plan_info(p, r);
     return GRT_OK;
 }
@@ -777,6 +895,216 @@ extern "C" int grt_plan_fetch(grt_plan *p, double *traces, double *spectra)
     if (!p->J.fsel.empty()) return set_err(ctx, GRT_ERR_UNSUPPORTED, "a frequency-selection plan has spectra only");
     CU(cudaSetDevice(ctx->device));
     return p->prec ? fetch<double>(p, traces, spectra) : fetch<float>(p, traces, spectra);
+}
+
+// ------------------------------------------------------------------ error estimate
+// Predicted relative L2 error of each receiver's traces against the FP64 path
+// of the same method (the judge of the FP32 path; see noise_kernel).  The
+// k-sum noise variance of every column, carried through the spectral stage
+// (|post|^2, the Hermitian pair, the inverse DFT and the de-damping,
+// E|dx|^2 = sum_n damp_n^2 * 2 sum_w |post_w|^2 v_w), over the trace's norm,
+// times eps.  Receivers between two distance bands interpolate linearly.
+// The coefficients' noise level eps(w) of an FP32 plan, measured: a
+// spectra-only FP64 plan over kSpotFreqs spot frequencies (half spread
+// geometrically over the lowest quarter of the band, where the far receivers'
+// energy is, the rest evenly up to the last) evaluates the same (w, k)
+// points; eps^2(w_s) = sum num / sum den of spot_noise_kernel, interpolated
+// linearly between spot frequencies.
+constexpr int kSpotFreqs = 16;
+
+static int spot_noise(grt_plan *p, const grt::NoiseArgs<float> &A, std::vector<int> &rows, std::vector<double> &eps2)
+{
+    grt_ctx *ctx = p->ctx;
+    const Job &J = p->J;
+    std::vector<int> sel;
+    const int nlo = kSpotFreqs / 2;   // geometric over 1 .. nw/4 (the far receivers' band), the rest even above
+    for (int i = 0; i < nlo; i++)
+        sel.push_back((int)std::lround(std::exp(std::log(std::max(1, J.nw / 4)) * i / (nlo - 1.0))));
+    for (int i = 1; i <= kSpotFreqs - nlo; i++)
+        sel.push_back((int)std::lround(J.nw / 4.0 + (J.nw - 1 - J.nw / 4.0) * i / (kSpotFreqs - nlo)));
+    for (int &v : sel) v = std::min(J.nw - 1, std::max(0, v));
+    std::sort(sel.begin(), sel.end());
+    sel.erase(std::unique(sel.begin(), sel.end()), sel.end());
+    rows = sel;
+    // the FP64 spot plan: this plan's job over the spot frequencies, one receiver
+    std::unique_ptr<grt_plan> q(new grt_plan);
+    q->ctx = ctx;
+    q->J = J;
+    std::string err;
+    int rc = grt::job_select(q->J, (int)sel.size(), sel.data(), err);
+    if (rc) return set_err(ctx, rc, err);
+    q->prec = GRT_FP64;
+    q->nd = 1;
+    q->dist.assign(1, p->dist[0]);
+    q->cols = p->cols;
+    q->nc = p->nc;
+    q->nq = p->nq;
+    q->rt = 1;
+    q->jt = 128;
+    if ((rc = upload<double>(q.get())) || (rc = execute<double>(q.get()))) {
+        grt_plan_destroy(q.release());
+        return rc;
+    }
+    const int ns = (int)sel.size();
+    int *drows = nullptr;
+    double *dout = nullptr;
+    cudaError_t e = dev_alloc(ctx, &drows, ns * sizeof(int));
+    if (e == cudaSuccess) e = dev_alloc(ctx, &dout, (size_t)ns * A.ncls * 2 * sizeof(double));
+    cudaStream_t st = ctx->stream;
+    std::vector<double> h((size_t)ns * A.ncls * 2);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(drows, sel.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+        grt::spot_noise_kernel<float><<<(unsigned)(ns * A.ncls), grt::kNoiseThreads, 0, st>>>(
+            A, (const double *)q->K, q->koff, q->J.nkw, drows, dout);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), dout, h.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    dev_free(ctx, drows);
+    dev_free(ctx, dout);
+    grt_plan_destroy(q.release());
+    CU(e);
+    eps2.assign(ns, 0.0);
+    for (int i = 0; i < ns; i++) {
+        double num = 0, den = 0;
+        for (int c = 0; c < A.ncls; c++) {
+            num += h[((size_t)i * A.ncls + c) * 2];
+            den += h[((size_t)i * A.ncls + c) * 2 + 1];
+        }
+        eps2[i] = den > 0 ? num / den : 0.0;
+    }
+    return GRT_OK;
+}
+
+template <typename R>
+static int error_estimate(grt_plan *p, double eps, double *est)
+{
+    grt_ctx *ctx = p->ctx;
+    const Job &J = p->J;
+    const grt::ColTerms &CT = kColTermsTab[p->cols];
+    constexpr int NB = grt::kNoiseBands;
+    grt::NoiseArgs<R> A{};
+    int tcls[48];
+    A.ncls = 0;
+    for (int t = 0; t < CT.nt; t++) {
+        int c = 0;
+        while (c < A.ncls && !(A.cls_q[c] == CT.q[t] && A.cls_p[c] == CT.kp[t])) c++;
+        if (c == A.ncls) {
+            A.cls_q[c] = CT.q[t];
+            A.cls_p[c] = CT.kp[t];
+            A.ncls++;
+        }
+        tcls[t] = c;
+    }
+    const double rmin = *std::min_element(p->dist.begin(), p->dist.end());
+    const double rmax = *std::max_element(p->dist.begin(), p->dist.end());
+    const double l0 = std::log(rmin), l1 = std::log(std::max(rmax, rmin * 1.0001));
+    for (int b = 0; b < NB; b++) A.rb[b] = (float)std::exp(l0 + (l1 - l0) * b / (NB - 1));
+    if (p->use_tc) {
+        A.Kt = p->Kt;
+        A.kt_base = p->kt_base;
+        A.nqt = tc_tiles(p->cols);
+        A.kt_bf16 = p->tc_bf16;
+        const grt::TcPlan tp = p->cols == grt::kColTensor ? grt::make_tcplan<grt::kColTensor>()
+                                                          : (p->cols == grt::kColSingleFix ? grt::make_tcplan<grt::kColSingleFix>()
+                                                                                           : grt::make_tcplan<grt::kColSingle>());
+        for (int q = 0; q < 16; q++) A.qslot[q] = tp.qslot[q];
+    } else {
+        A.K = (const R *)p->K;
+    }
+    A.nk = p->nk;
+    A.ks = p->ks;
+    A.koff = p->koff;
+    A.nkw = J.nkw;
+    A.dk = J.dk;
+    A.nw = J.nw;
+    // the coefficients' noise level: given, or measured against FP64 (FP32 plans)
+    std::vector<int> srow;
+    std::vector<double> seps2;
+    if (eps > 0) {
+        srow.assign(1, 0);
+        seps2.assign(1, eps * eps);
+    } else if constexpr (std::is_same<R, float>::value) {
+        int rc = spot_noise(p, A, srow, seps2);
+        if (rc) return rc;
+    } else {
+        srow.assign(1, 0);
+        seps2.assign(1, GRT_EPS_FP64 * GRT_EPS_FP64);
+    }
+    auto eps2_at = [&](int row) {
+        if (row <= srow.front()) return seps2.front();
+        if (row >= srow.back()) return seps2.back();
+        size_t i = std::upper_bound(srow.begin(), srow.end(), row) - srow.begin();
+        const double f = (double)(row - srow[i - 1]) / (srow[i] - srow[i - 1]);
+        return (1 - f) * seps2[i - 1] + f * seps2[i];
+    };
+    float *H = nullptr;
+    double *nrm = nullptr;
+    CU(dev_alloc(ctx, &H, (size_t)J.nw * A.ncls * NB * sizeof(float)));
+    A.H = H;
+    cudaError_t e = dev_alloc(ctx, &nrm, (size_t)p->nd * sizeof(double));
+    if (e != cudaSuccess) {
+        dev_free(ctx, H);
+        CU(e);
+    }
+    cudaStream_t st = ctx->stream;
+    grt::noise_kernel<R><<<(unsigned)(J.nw * A.ncls), grt::kNoiseThreads, 0, st>>>(A);
+    grt::trace_norm_kernel<R><<<(unsigned)p->nd, 256, 0, st>>>((const R *)p->sig, (long long)p->nc * J.N, nrm);
+    std::vector<float> h((size_t)J.nw * A.ncls * NB);
+    std::vector<double> n2(p->nd);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), H, h.size() * sizeof(float), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(n2.data(), nrm, n2.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    dev_free(ctx, H);
+    dev_free(ctx, nrm);
+    CU(e);
+    // G[c][b] = sum_w eps^2(w) 2 |post_w|^2 H[w][c][b]
+    const int wc = (int)((double)J.nwf * (1 - J.taper));
+    const double coef = J.df * J.nwf / PI;
+    std::vector<double> G((size_t)A.ncls * NB, 0.0);
+    for (int row = 0; row < J.nw; row++) {
+        const int iw = grt::job_freq(J, row);
+        const double st0 = iw > wc ? 0.5 * (1. + std::cos((iw - wc + 1) * PI / (J.nwf - wc + 1))) : 1.0;
+        const double wgt = eps2_at(row) * 2.0 * (st0 * coef) * (st0 * coef);
+        for (size_t i = 0; i < G.size(); i++) G[i] += wgt * h[(size_t)row * A.ncls * NB + i];
+    }
+    double damp2 = 0.0;
+    for (int n = 0; n < J.N; n++) {
+        const double d = std::exp(J.sigma * (n * J.dt + J.t0)) / J.N;
+        damp2 += d * d;
+    }
+    // the wavenumber sum's own rounding (FP32: 3xTF32 products and TMEM chains, or
+    // compensated SIMT / SGEMM slices), a floor under the coefficients' noise
+    const double floor = p->prec ? 0.0 : (p->use_tc ? 3e-5 : 3e-6);
+    for (int r = 0; r < p->nd; r++) {
+        const double x = l1 > l0 ? (std::log(p->dist[r]) - l0) / (l1 - l0) * (NB - 1) : 0.0;
+        const int b0 = std::min(NB - 2, std::max(0, (int)x));
+        const double f = std::min(1.0, std::max(0.0, x - b0));
+        double var = 0.0;
+        for (int t = 0; t < CT.nt; t++) {
+            const double g = (1 - f) * G[(size_t)tcls[t] * NB + b0] + f * G[(size_t)tcls[t] * NB + b0 + 1];
+            var += CT.coef[t] * CT.coef[t] * std::pow(p->dist[r], -2.0 * CT.rpow[t]) * g;
+        }
+        est[r] = n2[r] > 0 ? std::sqrt(var * damp2 / n2[r] + floor * floor) : HUGE_VAL;
+    }
+    return GRT_OK;
+}
+
+static int plan_error_estimate(grt_plan *p, double eps, double *est)
+{
+    grt_ctx *ctx = p->ctx;
+    if (!p->J.fsel.empty()) return set_err(ctx, GRT_ERR_UNSUPPORTED, "a frequency-selection plan has no traces");
+    if (!p->ran) return set_err(ctx, GRT_ERR_ARG, "execute the plan first");
+    if (!(eps >= 0)) return set_err(ctx, GRT_ERR_ARG, "eps must be >= 0");
+    CU(cudaSetDevice(ctx->device));
+    return p->prec ? error_estimate<double>(p, eps, est) : error_estimate<float>(p, eps, est);
+}
+
+extern "C" int grt_plan_error_estimate(grt_plan *p, double eps, double *est)
+{
+    if (!p || !est) return GRT_ERR_ARG;
+    return plan_error_estimate(p, eps, est);
 }
 
 // ------------------------------------------------------------------ convergence sweep
@@ -1418,9 +1746,9 @@ static int batch_build(grt_batch *b, int autotune)
     for (grt_plan *p : b->jobs) {
         CU(raise_smem_limit(grt::spectral_kernel<R>, (int)((size_t)p->J.N * sizeof(grt::C<R>))));
         if (p->use_tc) {
-            CU(raise_tc_limits<grt::kColSingle>());
-            CU(raise_tc_limits<grt::kColSingleFix>());
-            CU(raise_tc_limits<grt::kColTensor>());
+            CU(raise_tc_limits<grt::kColSingle>(p->tc_bf16));
+            CU(raise_tc_limits<grt::kColSingleFix>(p->tc_bf16));
+            CU(raise_tc_limits<grt::kColTensor>(p->tc_bf16));
         }
     }
     CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -1507,6 +1835,7 @@ extern "C" int grt_batch_execute(grt_batch *b, grt_report *r)
         h2d += p->rep.h2d_bytes;
         d2h += p->rep.d2h_bytes;
         ncol = std::max(ncol, p->nc);
+        p->ran = true;
     }
     b->rep.n_wk = nwk;
     b->rep.h2d_bytes = h2d;
@@ -1527,6 +1856,12 @@ extern "C" int grt_batch_fetch_freqs(grt_batch *b, int job, int n_freq, const in
 {
     if (!b || job < 0 || job >= (int)b->jobs.size()) return GRT_ERR_ARG;
     return grt_plan_fetch_freqs(b->jobs[job], n_freq, freq_idx, spectra);
+}
+
+extern "C" int grt_batch_error_estimate(grt_batch *b, int job, double eps, double *est)
+{
+    if (!b || job < 0 || job >= (int)b->jobs.size() || !est) return GRT_ERR_ARG;
+    return plan_error_estimate(b->jobs[job], eps, est);
 }
 
 extern "C" int grt_batch_info(const grt_batch *b, int job, grt_report *r, grt_tune *t)

@@ -2,6 +2,7 @@
 // kernels, templated on the real type (float for the product path, double for
 // the FP64 GPU check path).  Plain structs, all in registers.
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <math.h>
 
@@ -101,6 +102,23 @@ __host__ __device__ constexpr unsigned kt_tile_off(int row, int k)
 {
     return (unsigned)((((row >> 3) * (kTileK / 4) + (k >> 2)) * 128) + (row & 7) * 16 + (k & 3) * 4);
 }
+// The 3xBF16 form of the same tiles: 16 k per tile (one kind::f16 MMA K
+// step), 8 bf16 per 16-byte core-matrix row, 2 k blocks per row block; a
+// tile is 4 KB in both forms.
+constexpr int kTileK16 = 16;
+__host__ __device__ constexpr unsigned kt_tile_off16(int row, int k)
+{
+    return (unsigned)((((row >> 3) * 2 + (k >> 3)) * 128) + (row & 7) * 16 + (k & 7) * 2);
+}
+// FP32 -> BF16 bits, round to nearest even; and the split x = hi + lo + O(2^-17 |x|)
+__device__ __forceinline__ unsigned short bf16_bits(float x) { return __bfloat16_as_ushort(__float2bfloat16_rn(x)); }
+__device__ __forceinline__ float bf16_val(unsigned short b) { return __bfloat162float(__ushort_as_bfloat16(b)); }
+__device__ __forceinline__ void bf16_split(float x, unsigned short &hi, unsigned short &lo)
+{
+    hi = bf16_bits(x);
+    lo = bf16_bits(x - bf16_val(hi));
+}
+
 // FP32 -> TF32, round to nearest (ties away from zero)
 __device__ __forceinline__ float tf32_rna(float x)
 {

@@ -18,4 +18,6 @@ struct grt_ctx {
     std::multimap<size_t, void *> pool;
     std::map<void *, size_t> live;
     size_t pooled = 0, pool_cap = 0;
+    // cuBLAS handle of the plain FP32 wavenumber sum (created on first use)
+    void *blas = nullptr;
 };

@@ -342,25 +342,25 @@ constexpr int kTensorFixNC = 30;
 
 template <int SRC> struct Cols;
 template <> struct Cols<kSingle> {
-    static constexpr int NP = kSingleNP, NC = kSingleNC, NQ = QS_N;
+    static constexpr int NP = kSingleNP, NC = kSingleNC, NQ = QS_N, NT = sizeof(kSingleTerms) / sizeof(Term);
     __device__ static constexpr Pair pair(int i) { return kSinglePairs[i]; }
     __device__ static constexpr Term term(int i) { return kSingleTerms[i]; }
     __device__ static constexpr int col(int i) { return kSingleCol[i]; }
 };
 template <> struct Cols<kTensor> {
-    static constexpr int NP = kTensorNP, NC = kTensorNC, NQ = QT_N;
+    static constexpr int NP = kTensorNP, NC = kTensorNC, NQ = QT_N, NT = sizeof(kTensorTerms) / sizeof(Term);
     __device__ static constexpr Pair pair(int i) { return kTensorPairs[i]; }
     __device__ static constexpr Term term(int i) { return kTensorTerms[i]; }
     __device__ static constexpr int col(int i) { return kTensorCol[i]; }
 };
 template <> struct Cols<kColSingleFix> {
-    static constexpr int NP = kSingleNP, NC = kSingleNC, NQ = QS_N;
+    static constexpr int NP = kSingleNP, NC = kSingleNC, NQ = QS_N, NT = sizeof(kSingleFixTerms) / sizeof(Term);
     __device__ static constexpr Pair pair(int i) { return kSinglePairs[i]; }
     __device__ static constexpr Term term(int i) { return kSingleFixTerms[i]; }
     __device__ static constexpr int col(int i) { return kSingleCol[i]; }
 };
 template <> struct Cols<kColTensorFix> {
-    static constexpr int NP = kTensorFixNP, NC = kTensorFixNC, NQ = 2 * QT_N;
+    static constexpr int NP = kTensorFixNP, NC = kTensorFixNC, NQ = 2 * QT_N, NT = sizeof(kTensorFixTerms) / sizeof(Term);
     __device__ static constexpr Pair pair(int i) { return kTensorFixPairs[i]; }
     __device__ static constexpr Term term(int i) { return kTensorFixTerms[i]; }
     __device__ static constexpr int col(int i) { return kTensorFixCol[i]; }
@@ -549,6 +549,269 @@ __global__ void __launch_bounds__(kSumThreads) ksum_kernel(KsumArgs<R> A)
             }
         }
         if (lane == 0 && rvalid) S[((long long)r * NC + c) * A.nw + iw] = C<R>{v0, v1};
+    }
+}
+
+// ---------------------------------------------------------------- error estimate
+// Terms of a column layout flattened for host code: term t adds
+// coef[t] r^-rpow[t] w_k k^kp[t] J_b[t](k r) K_q[t](w, k) to column c for
+// col[c] <= t < col[c + 1].
+struct ColTerms {
+    int nc, nt, np;
+    int col[32], q[48], kp[48], b[48], rpow[48], pair[48];
+    double coef[48];
+    int pq[48], pkp[48], pb[48];   // pair p = (coefficient column, power of k, Bessel function)
+};
+#pragma nv_diagnostic push
+#pragma nv_diag_suppress 20091
+template <int SRC> __host__ __device__ constexpr ColTerms make_colterms()
+{
+    ColTerms o{};
+    o.nc = Cols<SRC>::NC;
+    o.nt = Cols<SRC>::NT;
+    for (int c = 0; c <= o.nc; c++) o.col[c] = Cols<SRC>::col(c);
+    for (int t = 0; t < o.nt; t++) {
+        const Term T = Cols<SRC>::term(t);
+        const Pair P = Cols<SRC>::pair(T.pair);
+        o.q[t] = P.q;
+        o.kp[t] = P.kp;
+        o.b[t] = P.b;
+        o.rpow[t] = T.rpow;
+        o.coef[t] = T.coef;
+        o.pair[t] = T.pair;
+    }
+    o.np = Cols<SRC>::NP;
+    for (int i = 0; i < o.np; i++) {
+        const Pair P = Cols<SRC>::pair(i);
+        o.pq[i] = P.q;
+        o.pkp[i] = P.kp;
+        o.pb[i] = P.b;
+    }
+    return o;
+}
+#pragma nv_diagnostic pop
+
+// Noise-floor estimate of the wavenumber sums (the judge of the FP32 path).
+// With relative rounding noise eps on every coefficient K_q(w, k),
+// independent from one wavenumber to the next, a column's k-sum at distance r
+// has the variance eps^2 sum_t coef_t^2 r^-2rpow_t sum_k w_k^2 k^2kp_t
+// |K_q_t(w, k)|^2 J_b_t(k r)^2; J^2 is replaced by its mean 1 / (1 + pi k r).
+// This kernel forms, per frequency, class c = (q, kp) and distance band b,
+//   H[iw][c][b] = sum_k w_k^2 k^(2 kp_c) |K_qc(w, k)|^2 / (1 + pi k r_b),
+// reading the coefficients from the flat columns or from the tensor-core
+// operand tiles (hi + lo words).  One block per (frequency, class).
+constexpr int kNoiseBands = 16;
+constexpr int kNoiseThreads = 128;
+template <typename R>
+struct NoiseArgs {
+    const R *K;              // [nq][nkw] complex, or null
+    const float *Kt;         // tensor-core operand tiles (FP32 plans), or null
+    const long long *kt_base;
+    int nqt, kt_bf16;        // tiles per stage block; the 3xBF16 form
+    int qslot[16];           // tile of coefficient column q (tensor-core layout)
+    const int *nk, *ks;
+    const long long *koff;
+    long long nkw;
+    double dk;
+    int nw, ncls;
+    int cls_q[32], cls_p[32];
+    float rb[kNoiseBands];   // band distances, km
+    float *H;                // [nw][ncls][kNoiseBands]
+};
+
+// coefficient K_q(w_iw, k_j) read back from the tensor-core operand tiles (hi + lo)
+template <typename R>
+__device__ __forceinline__ void tile_coef(const NoiseArgs<R> &A, int iw, int q, int j, float &re, float &im)
+{
+    const int wl = iw % (kTileRows / 2), tk = A.kt_bf16 ? kTileK16 : kTileK;
+    const float *t = A.Kt + A.kt_base[iw / (kTileRows / 2)] +
+                     ((long long)(j / tk) * A.nqt + A.qslot[q]) * 2 * (kTileRows * kTileK);
+    if (A.kt_bf16) {
+        const unsigned short *u = reinterpret_cast<const unsigned short *>(t);
+        const unsigned ore = kt_tile_off16(wl, j % tk) / 2, oim = kt_tile_off16(kTileRows / 2 + wl, j % tk) / 2;
+        re = bf16_val(u[ore]) + bf16_val(u[2 * kTileRows * kTileK + ore]);
+        im = bf16_val(u[oim]) + bf16_val(u[2 * kTileRows * kTileK + oim]);
+        return;
+    }
+    const unsigned ore = kt_tile_off(wl, j % tk) / 4, oim = kt_tile_off(kTileRows / 2 + wl, j % tk) / 4;
+    re = t[ore] + t[kTileRows * kTileK + ore];
+    im = t[oim] + t[kTileRows * kTileK + oim];
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kNoiseThreads) noise_kernel(NoiseArgs<R> A)
+{
+    __shared__ float red[kNoiseThreads][kNoiseBands + 1];
+    const int iw = blockIdx.x / A.ncls, c = blockIdx.x % A.ncls;
+    const int q = A.cls_q[c], kp = A.cls_p[c];
+    const int nk = A.nk[iw], m = A.ks ? A.ks[iw] : 1;
+    const double dkm = A.dk * m;
+    float acc[kNoiseBands];
+#pragma unroll
+    for (int b = 0; b < kNoiseBands; b++) acc[b] = 0.f;
+    for (int j = threadIdx.x; j < nk; j += blockDim.x) {
+        float re, im;
+        if (A.Kt) {
+            tile_coef(A, iw, q, j, re, im);
+        } else {
+            const C<R> v = reinterpret_cast<const C<R> *>(A.K)[(long long)q * A.nkw + A.koff[iw] + j];
+            re = (float)v.x;
+            im = (float)v.y;
+        }
+        const float k = (float)(dkm * j), w = (float)(j == 0 ? 0.5 * dkm : dkm);
+        float a = w * w * (re * re + im * im);
+        for (int e = 0; e < kp; e++) a *= k * k;
+#pragma unroll
+        for (int b = 0; b < kNoiseBands; b++) acc[b] += a / (1.f + 3.14159265f * k * A.rb[b]);
+    }
+#pragma unroll
+    for (int b = 0; b < kNoiseBands; b++) red[threadIdx.x][b] = acc[b];
+    __syncthreads();
+    if (threadIdx.x < kNoiseBands) {
+        float s = 0.f;
+        for (int t = 0; t < (int)blockDim.x; t++) s += red[t][threadIdx.x];
+        A.H[((long long)iw * A.ncls + c) * kNoiseBands + threadIdx.x] = s;
+    }
+}
+
+// The coefficients' actual FP32 noise at a few spot frequencies, against an
+// FP64 evaluation of the same (w, k) points: per spot frequency s and class c,
+//   num[s][c] = sum_k w_k^2 k^(2 kp) |K32_q - K64_q|^2,  den[s][c] = sum_k w_k^2 k^(2 kp) |K64_q|^2,
+// weighted as the wavenumber sum weights them.  K64: flat [nq][nkw64]
+// complex of a spectra-only FP64 plan over the spot frequencies (koff64).
+template <typename R>
+__global__ void __launch_bounds__(kNoiseThreads) spot_noise_kernel(NoiseArgs<R> A, const double *K64,
+                                                                   const long long *koff64, long long nkw64,
+                                                                   const int *rows, double *out)
+{
+    __shared__ double red[2][kNoiseThreads];
+    const int s = blockIdx.x / A.ncls, c = blockIdx.x % A.ncls;
+    const int iw = rows[s], q = A.cls_q[c], kp = A.cls_p[c];
+    const int nk = A.nk[iw], m = A.ks ? A.ks[iw] : 1;
+    const double dkm = A.dk * m;
+    double num = 0.0, den = 0.0;
+    for (int j = threadIdx.x; j < nk; j += blockDim.x) {
+        double re, im;
+        if (A.Kt) {
+            float fr, fi;
+            tile_coef(A, iw, q, j, fr, fi);
+            re = fr;
+            im = fi;
+        } else {
+            const C<R> v = reinterpret_cast<const C<R> *>(A.K)[(long long)q * A.nkw + A.koff[iw] + j];
+            re = (double)v.x;
+            im = (double)v.y;
+        }
+        const C<double> v64 = reinterpret_cast<const C<double> *>(K64)[(long long)q * nkw64 + koff64[s] + j];
+        const double k = dkm * j, w = (j == 0 ? 0.5 * dkm : dkm);
+        double f = w * w;
+        for (int e = 0; e < kp; e++) f *= k * k;
+        num += f * ((re - v64.x) * (re - v64.x) + (im - v64.y) * (im - v64.y));
+        den += f * (v64.x * v64.x + v64.y * v64.y);
+    }
+    red[0][threadIdx.x] = num;
+    red[1][threadIdx.x] = den;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) {
+            red[0][threadIdx.x] += red[0][threadIdx.x + h];
+            red[1][threadIdx.x] += red[1][threadIdx.x + h];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[2 * blockIdx.x] = red[0][0];
+        out[2 * blockIdx.x + 1] = red[1][0];
+    }
+}
+
+// sum of squares of each receiver's traces [nr][nc][N] (one block per receiver)
+template <typename R>
+__global__ void trace_norm_kernel(const R *sig, long long per_rcv, double *out)
+{
+    __shared__ double red[256];
+    const R *x = sig + blockIdx.x * per_rcv;
+    double s = 0.0;
+    for (long long i = threadIdx.x; i < per_rcv; i += blockDim.x) s += (double)x[i] * (double)x[i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[blockIdx.x] = red[0];
+}
+
+// ---------------------------------------------------------------- plain sum as GEMMs
+// The plain FP32 wavenumber sum written as real matrix products, one per
+// pair p = (q, kp, b) of the integrand tables (green.cu:1582-1600 /
+// 1650-1691):
+//   D_p[part][w][r] = sum_k A_q[part][w][k] Bc_(kp,b)[k][r],
+//   A_q = Re / Im K_q(w, k) (planar rows), Bc = w_k k^kp J_b(k r),
+// then S_c(w, r) = sum_(t in c) coef_t r^-rpow_t D_p(t)(w, r).  The products
+// run as cuBLAS SGEMM in FP32 (a plain library GEMM), k split in slices whose
+// partial products the combination adds with TwoSum.
+// A[q][part][w][j], zero beyond the frequency's nk (grid-stride, j fastest)
+static __global__ void gemm_a_kernel(const float *K, const int *nk, const long long *koff, long long nkw, int nw, int nkp,
+                              int nq, float *A)
+{
+    const long long n = (long long)nq * nw * nkp;
+    const float2 *Kc = reinterpret_cast<const float2 *>(K);
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const int j = (int)(e % nkp);
+        const long long qw = e / nkp;
+        const int iw = (int)(qw % nw), q = (int)(qw / nw);
+        float2 v = make_float2(0.f, 0.f);
+        if (j < nk[iw]) v = Kc[(long long)q * nkw + koff[iw] + j];
+        A[(((long long)q * 2) * nw + iw) * nkp + j] = v.x;
+        A[(((long long)q * 2 + 1) * nw + iw) * nkp + j] = v.y;
+    }
+}
+
+// Bc[j][r] = w_j k_j^kp J_b(k_j r) from the Bessel table B[j][b][r] (zero beyond its rows)
+static __global__ void gemm_b_kernel(const float *B, int nbrow, int nr, int nkp, double dk, int kp, int b, float *Bc)
+{
+    const long long n = (long long)nkp * nr;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const int r = (int)(e % nr), j = (int)(e / nr);
+        float v = 0.f;
+        if (j < nbrow) {
+            const double k = dk * j;
+            double f = (j == 0) ? 0.5 * dk : dk;
+            for (int i = 0; i < kp; i++) f *= k;
+            v = (float)f * B[((long long)j * NBASIS + b) * nr + r];
+        }
+        Bc[e] = v;
+    }
+}
+
+// S[r][c][w] = sum over the column's terms and the k slices of
+// coef_t r^-rpow_t D[s][p_t][part][w][r], with TwoSum; one thread per (w, r)
+template <int SRC>
+__global__ void gemm_combine_kernel(const float *D, int ns, int nw, int nr, const double *dist, float *S)
+{
+    using CT = Cols<SRC>;
+    const long long n = (long long)nw * nr;
+    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const int r = (int)(e % nr), w = (int)(e / nr);
+    const double dr = dist[r];
+    const float ir = (float)(1.0 / dr), ir2 = (float)(1.0 / (dr * dr));
+    const long long pstride = 2LL * nw * nr, sstride = (long long)CT::NP * pstride;
+    C<float> *So = reinterpret_cast<C<float> *>(S);
+#pragma unroll 1
+    for (int c = 0; c < CT::NC; c++) {
+        float hr = 0.f, lr = 0.f, hi = 0.f, li = 0.f;
+        for (int t = CT::col(c); t < CT::col(c + 1); t++) {
+            const Term T = CT::term(t);
+            const float f = (float)T.coef * (T.rpow == 1 ? ir : T.rpow == 2 ? ir2 : 1.f);
+            const float *Dp = D + T.pair * pstride + (long long)w * nr + r;
+            for (int s = 0; s < ns; s++) {
+                two_sum_acc(hr, lr, f * Dp[s * sstride]);
+                two_sum_acc(hi, li, f * Dp[s * sstride + (long long)nw * nr]);
+            }
+        }
+        So[((long long)r * CT::NC + c) * nw + w] = C<float>{hr + lr, hi + li};
     }
 }
 

@@ -262,18 +262,27 @@ __device__ GRT_INLINE_IF void interface_rt(const SL<R> &U, const SL<R> &D, R k, 
 struct KOut {
     long long idx;        // koff[iw] + j
     float *blk;           // operand block, or null
-    unsigned ore, oim;    // float offsets of the re / im rows inside a q tile
+    unsigned ore, oim;    // offsets of the re / im rows inside a q tile (floats; bf16 words in the BF16 form)
+    int bf16;             // the 3xBF16 form
 };
 
 template <typename R>
 __device__ __forceinline__ KOut make_kout(const GrtArgs<R> &A, int iw, int j)
 {
-    KOut o{A.koff[iw] + j, nullptr, 0u, 0u};
+    KOut o{A.koff[iw] + j, nullptr, 0u, 0u, 0};
     if (sizeof(R) == 4 && A.Kt) {
         const int wl = iw % (kTileRows / 2);
-        o.blk = A.Kt + A.kt_base[iw / (kTileRows / 2)] + (long long)(j / kTileK) * A.nqt * 2 * (kTileRows * kTileK);
-        o.ore = kt_tile_off(wl, j % kTileK) / 4;
-        o.oim = kt_tile_off(kTileRows / 2 + wl, j % kTileK) / 4;
+        // a stage block is nqt x (hi, lo) tiles of 4 KB in both forms
+        const int tk = A.kt_bf16 ? kTileK16 : kTileK;
+        o.blk = A.Kt + A.kt_base[iw / (kTileRows / 2)] + (long long)(j / tk) * A.nqt * 2 * (kTileRows * kTileK);
+        if (A.kt_bf16) {
+            o.bf16 = 1;
+            o.ore = kt_tile_off16(wl, j % tk) / 2;
+            o.oim = kt_tile_off16(kTileRows / 2 + wl, j % tk) / 2;
+        } else {
+            o.ore = kt_tile_off(wl, j % tk) / 4;
+            o.oim = kt_tile_off(kTileRows / 2 + wl, j % tk) / 4;
+        }
     }
     return o;
 }
@@ -287,9 +296,20 @@ __device__ __forceinline__ void store_q(const GrtArgs<R> &A, int q, const KOut &
         constexpr TcPlan tp = make_tcplan<SRCK == kTensor ? kColTensor : kColSingle>();
         const int slot = q < 16 ? tp.qslot[q] : -1;
         if (slot < 0) return;
-        // TF32 hi / lo words of the 3xTF32 product, [tile][hi|lo] tiles of 1024 floats
         float *t = o.blk + slot * 2 * (kTileRows * kTileK);
         const float x = (float)v.x, y = (float)v.y;
+        if (o.bf16) {
+            // BF16 hi / lo words of the 3xBF16 product, [tile][hi|lo] tiles of 2048 bf16
+            unsigned short *u = reinterpret_cast<unsigned short *>(t), xh, xl, yh, yl;
+            bf16_split(x, xh, xl);
+            bf16_split(y, yh, yl);
+            u[o.ore] = xh;
+            u[2 * kTileRows * kTileK + o.ore] = xl;
+            u[o.oim] = yh;
+            u[2 * kTileRows * kTileK + o.oim] = yl;
+            return;
+        }
+        // TF32 hi / lo words of the 3xTF32 product, [tile][hi|lo] tiles of 1024 floats
         const float xh = tf32_rna(x), yh = tf32_rna(y);
         t[o.ore] = xh;
         t[kTileRows * kTileK + o.ore] = tf32_rna(x - xh);

@@ -51,22 +51,31 @@ namespace tc {
 constexpr int kM = 128;        // rows: 64 frequencies x (re, im)
 constexpr int kW = 64;         // frequencies per CTA
 constexpr int kN = 32;         // receivers per CTA
-constexpr int kKT = 8;         // k per stage = one tf32 MMA K
-constexpr int kStages = 3;
-constexpr int kProdWarps = 8;  // 32 receivers x 8 k per stage, one per thread
+constexpr int kKT = 8;         // k per stage of the 3xTF32 form = one tf32 MMA K (the granularity of k slices)
+constexpr int kProdWarps = 8;  // 32 receivers x 8 k pairs... one (receiver, k group) per thread
 constexpr int kProducers = 32 * kProdWarps;
 constexpr int kCopyWarp = kProdWarps, kMmaWarp = kProdWarps + 1;
 constexpr int kThreads = kProducers + 64;
 constexpr int kCoreBytes = 128;                      // 8 rows x 16 bytes
-constexpr int kATileBytes = (kM / 8) * (kKT / 4) * kCoreBytes;   // 4096: one q, one split
-constexpr int kBTileBytes = (kN / 8) * (kKT / 4) * kCoreBytes;   // 1024: one pair, one split
-constexpr int kRawBytes = kKT * NBASIS * kN * 4;                 // raw Bessel rows of a stage
+constexpr int kATileBytes = (kM / 8) * 2 * kCoreBytes;   // 4096: one q, one split (2 core matrices along K)
+constexpr int kBTileBytes = (kN / 8) * 2 * kCoreBytes;   // 1024: one pair, one split
 constexpr uint32_t kTmemCols = 512;
 static_assert(kN == kBesselTile, "a CTA's receivers are one tile of the Bessel table");
-static_assert(kProducers == kN * kKT, "one producer per (receiver, k) of a stage");
+
+// The two split-precision forms.  3xTF32: 8 k per stage (a row of a tile is 8
+// tf32 = 32 bytes), one (receiver, k) per producer, 3 stages.  3xBF16: 16 k
+// per stage (16 bf16 = 32 bytes), two consecutive k per producer (their bf16
+// words packed in one store), 2 stages (the raw Bessel rows of a stage double).
+enum TcForm { kTF32 = 0, kBF16 = 1 };
+template <int PREC> struct TcPrec;
+template <> struct TcPrec<kTF32> { static constexpr int KT = 8, STAGES = 3, KPT = 1; };
+template <> struct TcPrec<kBF16> { static constexpr int KT = 16, STAGES = 2, KPT = 2; };
+template <int PREC> constexpr int raw_bytes() { return TcPrec<PREC>::KT * NBASIS * kN * 4; }
+static_assert(kProducers * TcPrec<kTF32>::KPT == kN * TcPrec<kTF32>::KT, "producers cover a stage");
+static_assert(kProducers * TcPrec<kBF16>::KPT == kN * TcPrec<kBF16>::KT, "producers cover a stage");
 
 // one group of a column layout's tensor-core plan
-template <int SRC, int GRP> struct TcGroup {
+template <int SRC, int GRP, int PREC> struct TcGroup {
     static constexpr TcPlan P = make_tcplan<SRC>();
     static constexpr int NQ = P.gnq[GRP];     // operand tiles (coefficient columns)
     static constexpr int NP = P.gnp[GRP];     // pairs
@@ -74,26 +83,33 @@ template <int SRC, int GRP> struct TcGroup {
     static constexpr int NQU = P.nqu;         // tiles in a stage block (both groups)
     static constexpr int kABytes = NQ * 2 * kATileBytes;
     static constexpr int kBBytes = NP * 2 * kBTileBytes;
+    static constexpr int kRawBytes = raw_bytes<PREC>();
     static constexpr int kStageBytes = kABytes + kBBytes + kRawBytes;
     static_assert(NP * kN <= (int)kTmemCols, "accumulators exceed tensor memory");
     static_assert(kStageBytes % 1024 == 0, "stages stay 1024-byte aligned");
 };
 
-template <int SRC> constexpr int smem_bytes()
+template <int SRC, int PREC> constexpr int smem_bytes()
 {
-    return kStages * (TcGroup<SRC, 1>::kStageBytes > TcGroup<SRC, 0>::kStageBytes ? TcGroup<SRC, 1>::kStageBytes
-                                                                                  : TcGroup<SRC, 0>::kStageBytes) +
+    return TcPrec<PREC>::STAGES * (TcGroup<SRC, 1, PREC>::kStageBytes > TcGroup<SRC, 0, PREC>::kStageBytes
+                                       ? TcGroup<SRC, 1, PREC>::kStageBytes
+                                       : TcGroup<SRC, 0, PREC>::kStageBytes) +
            1024;
 }
 
 static_assert(kKT == kTileK && kM == kTileRows, "tile shape shared with the GRT kernel");
-__device__ __forceinline__ uint32_t tile_off(int row, int k) { return kt_tile_off(row, k); }
+static_assert(TcPrec<kBF16>::KT == kTileK16, "tile shape shared with the GRT kernel");
+template <int PREC> __device__ __forceinline__ uint32_t tile_off(int row, int k)
+{
+    return PREC == kBF16 ? kt_tile_off16(row, k) : kt_tile_off(row, k);
+}
 
 // shared-memory matrix descriptor: K-major, no swizzle.  LBO = distance of
-// core matrices adjacent in K (128 B), SBO = distance of 8-row groups.
+// core matrices adjacent in K (128 B), SBO = distance of 8-row groups (two
+// core matrices along K in both forms).
 __device__ __forceinline__ uint64_t sdesc(uint32_t saddr)
 {
-    const uint64_t lbo = kCoreBytes, sbo = (uint64_t)(kKT / 4) * kCoreBytes;
+    const uint64_t lbo = kCoreBytes, sbo = 2 * kCoreBytes;
     uint64_t d = 0;
     d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
     d |= (uint64_t)(lbo >> 4) << 16;
@@ -102,10 +118,12 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t saddr)
     return d;                     // base offset 0, layout type 0 (no swizzle)
 }
 
-// instruction descriptor: dense, D = F32, A = B = TF32, both K-major, M = 128, N = n
-constexpr uint32_t idesc_n(int n)
+// instruction descriptor: dense, D = F32, A = B = TF32 (kind::tf32, format 2)
+// or BF16 (kind::f16, format 1), both K-major, M = 128, N = n
+template <int PREC> constexpr uint32_t idesc_n(int n)
 {
-    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kM >> 4) << 24);
+    constexpr uint32_t fmt = PREC == kBF16 ? 1u : 2u;
+    return (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kM >> 4) << 24);
 }
 
 __device__ __forceinline__ float tf32_rna(float x) { return grt::tf32_rna(x); }
@@ -155,6 +173,22 @@ __device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t adesc, uint64_
         "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
         : "memory");
 }
+// A = B = BF16 (kind::f16), D = F32
+__device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
+        : "memory");
+}
+template <int PREC>
+__device__ __forceinline__ void mma_split(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc)
+{
+    if constexpr (PREC == kBF16) mma_bf16(dtmem, adesc, bdesc, idesc, acc);
+    else mma_tf32(dtmem, adesc, bdesc, idesc, acc);
+}
 __device__ __forceinline__ void mma_commit(uint32_t bar)
 {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
@@ -196,14 +230,15 @@ struct KsumTcArgs {
 };
 
 // One CTA of column group GRP; blk = (frequency tile, receiver tile, k slice).
-template <int SRC, int GRP>
+template <int SRC, int GRP, int PREC>
 __device__ __forceinline__ void ksum_tc_cta(const KsumTcArgs<float> &A, int blk, unsigned char *smem_tc,
                                             unsigned long long *bars, float *ir_s)
 {
     using namespace tc;
     using CT = Cols<SRC>;
-    using TG = TcGroup<SRC, GRP>;
+    using TG = TcGroup<SRC, GRP, PREC>;
     constexpr int NC = CT::NC, NQ = TG::NQ, NP = TG::NP;
+    constexpr int KT = TcPrec<PREC>::KT, kStages = TcPrec<PREC>::STAGES, KPT = TcPrec<PREC>::KPT;
     constexpr TcPlan TP = make_tcplan<SRC>();
     constexpr unsigned kBasis = group_basis_mask<SRC, GRP>();
     __shared__ uint32_t tmem_base_s;
@@ -222,7 +257,7 @@ __device__ __forceinline__ void ksum_tc_cta(const KsumTcArgs<float> &A, int blk,
         if (w0 + i < A.nw) nkt = max(nkt, A.nk[w0 + i]);
     const int kb = sp * A.kslice;
     const int ke = min(nkt, kb + A.kslice);
-    const int nstage = ke > kb ? (ke - kb + kKT - 1) / kKT : 0;
+    const int nstage = ke > kb ? (ke - kb + KT - 1) / KT : 0;
 
     unsigned char *sm = (unsigned char *)(((uintptr_t)smem_tc + 1023) & ~(uintptr_t)1023);
     const uint32_t sm_s = (uint32_t)__cvta_generic_to_shared(sm);
@@ -284,14 +319,16 @@ __device__ __forceinline__ void ksum_tc_cta(const KsumTcArgs<float> &A, int blk,
                     break;
                 }
                 if (fail_s) break;
-                const int k0 = kb + st * kKT;
+                const int k0 = kb + st * KT;
                 // this group's coefficient tiles of the (frequency tile, k stage) block
-                const float *src = kt_tile + ((long long)(k0 / kKT) * TG::NQU + TG::Q0) * (2 * kM * kKT);
+                // (a stage block is NQU x (hi, lo) tiles of 4 KB = 2048 floats per tile pair)
+                const float *src = kt_tile + ((long long)(k0 / KT) * TG::NQU + TG::Q0) * (2 * kM * kKT);
                 tc::mbar_expect_tx(land_bar(s), (uint32_t)TG::kABytes);
                 tc::bulk_copy(sm_s + a_tile(s, 0, 0), src, (uint32_t)TG::kABytes, land_bar(s));
                 if (tiled) {
-                    tc::mbar_expect_tx(raw_bar(s), (uint32_t)kRawBytes);
-                    tc::bulk_copy(sm_s + raw_off(s), braw + (size_t)k0 * NBASIS * kN, (uint32_t)kRawBytes, raw_bar(s));
+                    tc::mbar_expect_tx(raw_bar(s), (uint32_t)TG::kRawBytes);
+                    tc::bulk_copy(sm_s + raw_off(s), braw + (size_t)k0 * NBASIS * kN, (uint32_t)TG::kRawBytes,
+                                  raw_bar(s));
                 }
                 issued = st + 1;
             }
@@ -303,24 +340,26 @@ __device__ __forceinline__ void ksum_tc_cta(const KsumTcArgs<float> &A, int blk,
         }
     } else if (warp < kProdWarps) {
         // ---------------- producers of the Bessel operand
-        // (receiver, k) of this thread in a stage: a warp covers one 8-receiver x
-        // 4-k core matrix, so its B-operand stores fill 32 distinct banks
-        const int br = (warp & 3) * 8 + (lane >> 2), bk = (warp >> 2) * 4 + (lane & 3);
+        // (receiver, first k) of this thread in a stage: a warp covers one
+        // 8-receiver x 32-byte core-matrix row block, so its B-operand stores
+        // fill 32 distinct banks; KPT consecutive k per thread
+        const int br = (warp & 3) * 8 + (lane >> 2), bk = (warp >> 2) * (4 * KPT) + (lane & 3) * KPT;
         const int rg = min(r0 + br, A.nr - 1);
         const bool rok = (r0 + br) < A.nr;
         const int ksm = A.ks ? A.ks[w0] : 1;
         const float dk = (float)(A.dk * ksm);
-        // the tiled table permutes a row's receivers by r ^ 8 (k & 3); kb is a multiple of 8
-        const int bcol = br ^ ((bk & 3) << 3);
         // untiled table: Bessel values of the next stage loaded one stage ahead
-        float bv[NBASIS];
+        float bv[KPT][NBASIS];
         auto load_b = [&](int st_) {
-            const int k = kb + st_ * kKT + bk;
-            const bool kok = st_ < nstage && k < ke && rok;
 #pragma unroll
-            for (int b = 0; b < NBASIS; b++)
-                if ((kBasis >> b) & 1u)
-                    bv[b] = kok ? __ldg(A.B + ((long long)k * ksm * NBASIS + b) * A.nr + rg) : 0.f;
+            for (int i = 0; i < KPT; i++) {
+                const int k = kb + st_ * KT + bk + i;
+                const bool kok = st_ < nstage && k < ke && rok;
+#pragma unroll
+                for (int b = 0; b < NBASIS; b++)
+                    if ((kBasis >> b) & 1u)
+                        bv[i][b] = kok ? __ldg(A.B + ((long long)k * ksm * NBASIS + b) * A.nr + rg) : 0.f;
+            }
         };
         if (!tiled) load_b(0);
         // each producer warp runs on its own (no barrier among them: the copy
@@ -335,9 +374,8 @@ __device__ __forceinline__ void ksum_tc_cta(const KsumTcArgs<float> &A, int blk,
                 fail_s = 1;
                 break;
             }
-            // B operand: pair values k^kp w J_b(k r) for (receiver br, k bk)
-            const int k = kb + st * kKT + bk;
-            float cur[NBASIS];
+            // B operand: pair values k^kp w J_b(k r) for (receiver br, k bk + i)
+            float cur[KPT][NBASIS];
             if (tiled) {
                 const bool raw_ok = tc::mbar_wait_b(raw_bar(s), (st / kStages) & 1);
                 if (__any_sync(0xffffffffu, !raw_ok)) {
@@ -346,25 +384,49 @@ __device__ __forceinline__ void ksum_tc_cta(const KsumTcArgs<float> &A, int blk,
                     break;
                 }
                 const float *rs = reinterpret_cast<const float *>(sm + raw_off(s));
-                const bool kok = k < ke && rok;
 #pragma unroll
-                for (int b = 0; b < NBASIS; b++)
-                    if ((kBasis >> b) & 1u) cur[b] = kok ? rs[(bk * NBASIS + b) * kN + bcol] : 0.f;
+                for (int i = 0; i < KPT; i++) {
+                    // the tiled table permutes a row's receivers by r ^ 8 (k & 3); kb is a multiple of KT
+                    const int kk = bk + i, bcol = br ^ ((kk & 3) << 3);
+                    const bool kok = kb + st * KT + kk < ke && rok;
+#pragma unroll
+                    for (int b = 0; b < NBASIS; b++)
+                        if ((kBasis >> b) & 1u) cur[i][b] = kok ? rs[(kk * NBASIS + b) * kN + bcol] : 0.f;
+                }
             } else {
 #pragma unroll
-                for (int b = 0; b < NBASIS; b++) cur[b] = bv[b];
+                for (int i = 0; i < KPT; i++)
+#pragma unroll
+                    for (int b = 0; b < NBASIS; b++) cur[i][b] = bv[i][b];
                 load_b(st + 1);
             }
-            const float kf = dk * (float)k;
-            const float w = (k == 0) ? 0.5f * dk : dk;
-            const float wk[3] = {w, w * kf, w * kf * kf};
+            float wk[KPT][3];
+#pragma unroll
+            for (int i = 0; i < KPT; i++) {
+                const int k = kb + st * KT + bk + i;
+                const float kf = dk * (float)k;
+                const float w = (k == 0) ? 0.5f * dk : dk;
+                wk[i][0] = w;
+                wk[i][1] = w * kf;
+                wk[i][2] = w * kf * kf;
+            }
+            const uint32_t boff = tc::tile_off<PREC>(br, bk);
 #pragma unroll
             for (int slot = 0; slot < NP; slot++) {
                 const Pair P = CT::pair(TP.gpair[GRP][slot]);
-                const float v = wk[P.kp] * cur[P.b];
-                const float h = tc::tf32_rna(v), l = tc::tf32_rna(v - h);
-                *reinterpret_cast<float *>(sm + b_tile(s, slot, 0) + tc::tile_off(br, bk)) = h;
-                *reinterpret_cast<float *>(sm + b_tile(s, slot, 1) + tc::tile_off(br, bk)) = l;
+                if constexpr (PREC == kBF16) {
+                    // two consecutive k of one receiver: their bf16 words share a 32-bit store
+                    unsigned short h0, l0, h1, l1;
+                    bf16_split(wk[0][P.kp] * cur[0][P.b], h0, l0);
+                    bf16_split(wk[1][P.kp] * cur[1][P.b], h1, l1);
+                    *reinterpret_cast<uint32_t *>(sm + b_tile(s, slot, 0) + boff) = (uint32_t)h0 | ((uint32_t)h1 << 16);
+                    *reinterpret_cast<uint32_t *>(sm + b_tile(s, slot, 1) + boff) = (uint32_t)l0 | ((uint32_t)l1 << 16);
+                } else {
+                    const float v = wk[0][P.kp] * cur[0][P.b];
+                    const float h = tc::tf32_rna(v), l = tc::tf32_rna(v - h);
+                    *reinterpret_cast<float *>(sm + b_tile(s, slot, 0) + boff) = h;
+                    *reinterpret_cast<float *>(sm + b_tile(s, slot, 1) + boff) = l;
+                }
             }
             // make the generic-proxy writes visible to the tensor cores, then one
             // lane signals for the warp
@@ -390,14 +452,14 @@ __device__ __forceinline__ void ksum_tc_cta(const KsumTcArgs<float> &A, int blk,
 #pragma unroll
             for (int i = 0; i < NQ; i++) {
                 const int first = TP.tfirst[TG::Q0 + i], count = TP.tcount[TG::Q0 + i];
-                const uint32_t idesc = tc::idesc_n(count * kN);
+                const uint32_t idesc = tc::idesc_n<PREC>(count * kN);
                 const uint32_t d = tmem + (uint32_t)(first * kN);
                 const uint64_t ah = dbase + ((uint64_t)a_tile(0, i, 0) >> 4), al = dbase + ((uint64_t)a_tile(0, i, 1) >> 4);
                 const uint64_t bh = dbase + ((uint64_t)b_tile(0, first, 0) >> 4);
                 const uint64_t bl = dbase + ((uint64_t)b_tile(0, first, 1) >> 4);
-                tc::mma_tf32(d, ah, bh, idesc, acc0);
-                tc::mma_tf32(d, ah, bl, idesc, 1u);
-                tc::mma_tf32(d, al, bh, idesc, 1u);
+                tc::mma_split<PREC>(d, ah, bh, idesc, acc0);
+                tc::mma_split<PREC>(d, ah, bl, idesc, 1u);
+                tc::mma_split<PREC>(d, al, bh, idesc, 1u);
             }
             tc::mma_commit(empty_bar(s));   // stage s may be refilled once these MMAs finish
         }
@@ -466,15 +528,15 @@ __device__ __forceinline__ void ksum_tc_cta(const KsumTcArgs<float> &A, int blk,
 }
 
 // Both column groups in one launch (even blocks group 0, odd blocks group 1),
-// so that their CTAs share the waves of the SMs.
-template <int SRC>
+// so that their CTAs share the waves of the SMs.  PREC: tc::kTF32 or tc::kBF16.
+template <int SRC, int PREC>
 __global__ void __launch_bounds__(tc::kThreads, 1) ksum_tc_kernel(KsumTcArgs<float> A)
 {
     extern __shared__ __align__(1024) unsigned char smem_tc[];
-    __shared__ __align__(8) unsigned long long bars[4 * tc::kStages + 1];
+    __shared__ __align__(8) unsigned long long bars[4 * 3 + 1];   // 4 barriers per stage (at most 3) + done
     __shared__ float ir_s[2 * tc::kN];
-    if (blockIdx.x & 1) ksum_tc_cta<SRC, 1>(A, (int)(blockIdx.x >> 1), smem_tc, bars, ir_s);
-    else ksum_tc_cta<SRC, 0>(A, (int)(blockIdx.x >> 1), smem_tc, bars, ir_s);
+    if (blockIdx.x & 1) ksum_tc_cta<SRC, 1, PREC>(A, (int)(blockIdx.x >> 1), smem_tc, bars, ir_s);
+    else ksum_tc_cta<SRC, 0, PREC>(A, (int)(blockIdx.x >> 1), smem_tc, bars, ir_s);
 }
 
 // S[r][c][w] = sum over the partial sums (k slices x groups) with TwoSum

@@ -67,6 +67,7 @@ struct GrtArgs {
     float *Kt;
     const long long *kt_base;
     int nqt;
+    int kt_bf16;               // tiles in the 3xBF16 form (16 k per stage, bf16 hi/lo words)
 };
 
 // Bessel basis functions of k r, in the order the integrand formulas use them

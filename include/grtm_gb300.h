@@ -87,10 +87,16 @@ typedef struct grt_opts {
     int n_freq_sel;       /* > 0: evaluate only these positive frequencies (a spectra-only plan: */
     const int *freq_sel;  /* distinct indices in 0..N/2-1, any order; grt_plan_fetch_freqs reads them,
                            * traces, synthesis and files are GRT_ERR_UNSUPPORTED).  0 / NULL: all. */
-    int k_slice;          /* FP32 tensor-core sum: wavenumbers per split-K slice, a multiple of 8 (0: chosen
-                           * to fill the GPU).  Plans with one k_slice add each frequency's wavenumbers in
-                           * the same order: their sums agree bit for bit on a common k range. */
+    int k_slice;          /* FP32 tensor-core sum: wavenumbers per split-K slice, a multiple of 8 (16 for
+                           * 3xBF16; 0: chosen to fill the GPU).  Plans with one k_slice add each frequency's
+                           * wavenumbers in the same order: their sums agree bit for bit on a common k range. */
+    int tc_split;         /* FP32 tensor-core sum: GRT_TC_3XTF32 (hi*hi + hi*lo + lo*hi of TF32 halves, about
+                           * 2^-21 per product) or GRT_TC_3XBF16 (the same with BF16 halves, about 2^-16 per
+                           * product, half the operand bytes and twice the MMA rate) */
 } grt_opts;
+
+#define GRT_TC_3XTF32 0
+#define GRT_TC_3XBF16 1
 
 typedef struct grt_report {
     int n_layer;          /* after source-interface insertion */
@@ -106,7 +112,8 @@ typedef struct grt_report {
     int kernel_launches;  /* kernels launched by the last execute */
     long long h2d_bytes;  /* bytes the plan uploads (layer tables, grids, receivers) */
     long long d2h_bytes;  /* bytes one fetch of the traces downloads */
-    int ksum_impl;        /* wavenumber sum: 0 SIMT FP32/FP64, 1 tensor cores (3xTF32) */
+    int ksum_impl;        /* wavenumber sum: 0 SIMT FP32/FP64, 1 tensor cores 3xTF32, 2 FP32 SGEMMs (cuBLAS),
+                           * 3 tensor cores 3xBF16 */
     int k_slice;          /* tensor-core sum: wavenumbers per split-K slice (0 for the SIMT sum) */
 } grt_report;
 
@@ -305,6 +312,27 @@ GRT_API void grt_sf_weights(const double *f, double azimuth, double *w);
 /* azimuth: degrees clockwise from north, one per receiver; seis: [n_dist][3 (Z, R, T)][N] */
 GRT_API int grt_plan_synth(grt_plan *plan, const grt_source *src, const double *azimuth, double *seis);
 GRT_API int grt_batch_synth(grt_batch *batch, int job, const grt_source *src, const double *azimuth, double *seis);
+
+/* Predicted error of a plan's traces (the judge of the FP32 path): for each
+ * receiver, the relative L2 error its traces [n_cols][N] are expected to have
+ * against the FP64 path of the same method.  The per-(w,k) coefficients carry
+ * relative rounding noise eps(w), independent from one wavenumber to the
+ * next; the wavenumber sum adds it up, the spectral stage carries it to the
+ * trace (taper, inverse DFT, e^{sigma t} de-damping), and it is compared with
+ * the trace's own norm; the sum's own rounding is a floor under it.  eps > 0
+ * gives eps(w) = eps; eps = 0 measures it: an FP64 evaluation of the plan's
+ * (w,k) points at 16 spot frequencies (about 16 / (N/2) of an FP64 plan's GRT
+ * work) against the plan's FP32 coefficients (FP64 plans: GRT_EPS_FP64).
+ * The estimate follows the measured error over five orders of magnitude,
+ * including the far receivers of short windows where the wavenumber sum
+ * cancels by a factor 10^6 and FP32 cannot reach 1e-3; a caller recomputes
+ * the receivers above its tolerance in FP64.  After grt_plan_execute /
+ * grt_batch_execute; est: n_dist doubles.  Full plans only (a frequency
+ * selection has no traces: GRT_ERR_UNSUPPORTED).  No counterpart in the
+ * reference (FP64 only). */
+#define GRT_EPS_FP64 1e-15
+GRT_API int grt_plan_error_estimate(grt_plan *plan, double eps, double *est);
+GRT_API int grt_batch_error_estimate(grt_batch *batch, int job, double eps, double *est);
 
 /* create + execute + fetch + destroy */
 GRT_API int grt_run(grt_ctx *ctx, const grt_model *model, const grt_opts *opts, int n_dist,

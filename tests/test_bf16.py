@@ -1,0 +1,87 @@
+"""The 3xBF16 form of the tensor-core wavenumber sum (GB300).
+
+Each FP32 operand of the [w x k] x [k x r] products is split into BF16 halves,
+x = hi + lo + O(2^-17 |x|), and the product is hi*hi + hi*lo + lo*hi with FP32
+accumulation in tensor memory (kind::f16 MMAs, 16 wavenumbers per stage).  It
+must agree with the 3xTF32 form and the FP64 oracle on the small grids of the
+parity tests, and with the FP64 path per receiver on a 40-layer crust."""
+import math
+
+import numpy as np
+import pytest
+
+import test_gpu_parity as P
+
+pytestmark = pytest.mark.gpu
+
+TOL_ORACLE = 3e-4     # relative L2 per column, 4-layer crust, receivers to 80 km
+TOL_FP64 = 1e-3       # per receiver, 40 layers, receivers to 500 km
+
+
+@pytest.fixture(scope="module")
+def gctx():
+    import grtm_cuda_gb300 as g
+    g.lib()
+    c = g.Context()
+    yield g, c
+    c.close()
+
+
+@pytest.mark.parametrize("hs,hr,st,fix", [P.GEOMETRIES[0], P.GEOMETRIES[1], P.GEOMETRIES[3]])
+def test_bf16_matches_oracle_and_tf32(gctx, oracle, hs, hr, st, fix):
+    g, ctx = gctx
+    kw = dict(dt=0.1, log2n=8, t0=0.0, taper=0.3, sigma_factor=np.pi, k_mode=g.K_FIXED, nk_fixed=1024)
+    dists = [10.0, 35.0, 80.0]
+    ref, _ = P._oracle_traces(oracle, hs, hr, st, fix, kw, dists)
+    m = g.make_model(P.TOPS, P.VP, P.VS, P.RHO, P.QP, P.QS, hs, hr, st)
+    tb, _, rb = g.run(m, g.make_opts(precision=g.FP32, fix=fix, tc_split=g.TC_3XBF16, **kw), dists, ctx)
+    tt, _, rt = g.run(m, g.make_opts(precision=g.FP32, fix=fix, **kw), dists, ctx)
+    assert rb["ksum_impl"] == 3 and rt["ksum_impl"] == 1
+    eb = max(P.rel(tb[:, c], ref[:, c]) for c in range(ref.shape[1]))
+    et = max(P.rel(tt[:, c], ref[:, c]) for c in range(ref.shape[1]))
+    print(f"3xBF16 {eb:.2e}  3xTF32 {et:.2e}")
+    assert eb <= TOL_ORACLE and et <= 5e-5
+
+
+def test_bf16_per_receiver_against_fp64(gctx):
+    """40-layer crust, 64 receivers 1-500 km, nt 1024, nk 4096 (the small
+    profiling case of the 40-layer configuration): both split forms per
+    receiver against the FP64 path, as the tensor-core configuration asks."""
+    g, ctx = gctx
+    from grtm_cuda_gb300 import synth
+    mk, d = synth.crust40_model(1234, n_receivers=64)
+    m = g.make_model(**mk)
+    o = lambda prec, split: g.make_opts(0.05, 10, 0.0, 0.3, math.pi, g.K_FIXED, 4096, precision=prec,
+                                        fix=g.FIX_ALL, tc_split=split)
+    t64, _, _ = g.run(m, o(g.FP64, 0), d, ctx)
+    den = np.linalg.norm(t64, axis=(1, 2))
+    eb = np.linalg.norm(g.run(m, o(g.FP32, g.TC_3XBF16), d, ctx)[0] - t64, axis=(1, 2)) / den
+    et = np.linalg.norm(g.run(m, o(g.FP32, g.TC_3XTF32), d, ctx)[0] - t64, axis=(1, 2)) / den
+    print(f"per receiver vs FP64: 3xBF16 max {eb.max():.2e} median {np.median(eb):.2e}; "
+          f"3xTF32 max {et.max():.2e} median {np.median(et):.2e}")
+    assert eb.max() <= TOL_FP64 and et.max() <= TOL_FP64
+
+
+def test_bf16_in_a_batch_equals_single_jobs(gctx):
+    g, ctx = gctx
+    from grtm_cuda_gb300 import synth
+    jobs = []
+    for seed, n in ((5, 12), (6, 30)):
+        rng = np.random.default_rng(seed)
+        mk = synth.crust(rng, n, 9.0)
+        jobs.append((g.make_model(**mk), g.make_opts(0.05, 10, 0.0, 0.3, math.pi, g.K_FIXED, 2048,
+                                                     fix=g.FIX_ALL, tc_split=g.TC_3XBF16),
+                     np.sort(rng.uniform(3.0, 200.0, 40))))
+    b = g.Batch(ctx, jobs, autotune=False)
+    b.execute()
+    for j, (m, o, d) in enumerate(jobs):
+        tb, _ = b.fetch(j)
+        ts, _, _ = g.run(m, o, d, ctx)
+        assert np.array_equal(tb, ts), j
+    b.close()
+    # k_slice must be a multiple of 16 in this form
+    m, o, d = jobs[0]
+    o.k_slice = 8
+    with pytest.raises(g.GrtError) as e:
+        g.Plan(ctx, m, o, d)
+    assert e.value.status == g.ERR_ARG

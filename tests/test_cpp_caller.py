@@ -78,6 +78,7 @@ def test_reference_caller_on_the_demo_matches_golden(tmp_path, golden, oracle):
     ow, ot = str(tmp_path / "w.txt"), str(tmp_path / "t.txt")
     _run(exe, tmp_path, os.path.join(GOLDEN, "demo_input.txt"), ow, ot)
     job = oracle.parse(os.path.join(GOLDEN, "demo_input.txt"))
+    oracle.setup(job, job.dt, job.log2n, job.t0, job.taper)
     w = g.read_table(ow, complex_pairs=True)
     assert w.shape == (2048, 30)
     assert np.array_equal(w[job.nw + 1:], np.conj(w[job.nw - 1:0:-1]))

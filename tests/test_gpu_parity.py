@@ -196,14 +196,20 @@ def test_green_reports_bad_input(g, tmp_path):
     assert rc == g.ERR_IO
 
 
-def test_reference_k_rule_grid(g, ctx, oracle):
+@pytest.mark.parametrize("impl", ["tc", "simt"])
+def test_reference_k_rule_grid(g, ctx, oracle, impl, monkeypatch):
     """Ragged per-frequency k_max grid (the reference's rule) on the 4-layer crust
-    model: same (w,k) count as the oracle and the same traces."""
+    model: same (w,k) count as the oracle and the same traces, with the
+    tensor-core sum and with the blocked SIMT sum (ragged k counts, 256
+    frequencies, 11 receivers: partial frequency and receiver tiles)."""
+    if impl == "simt":
+        monkeypatch.setenv("GRT_KSUM", "simt")
     kw = dict(dt=0.1, log2n=9, t0=0.0, taper=0.3, sigma_factor=2.0, k_mode=g.K_REFERENCE, nk_fixed=0)
-    dists = [15.0, 60.0]
+    dists = [15.0, 60.0, 3.0, 7.5, 22.0, 31.0, 44.0, 71.0, 90.0, 120.0, 150.0]
     ref, job = _oracle_traces(oracle, 10.0005, 0.0, 1, 0, kw, dists)
     m = g.make_model(TOPS, VP, VS, RHO, QP, QS, 10.0005, 0.0, 1)
     t32, _, rep = g.run(m, g.make_opts(precision=g.FP32, **kw), dists, ctx)
     assert rep["n_wk"] == int(oracle.nk_list(job).sum())
+    assert rep["ksum_impl"] == (1 if impl == "tc" else 2)   # unit strides: the plain sum runs as SGEMMs
     for c in range(20):
         assert rel(t32[:, c], ref[:, c]) < 5e-5, c

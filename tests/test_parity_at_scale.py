@@ -108,4 +108,5 @@ def test_spectra_match_oracle_at_config_size(gctx, case, prec):
     s = gpu_spectra(g, ctx, name, g.FP64 if prec == "fp64" else g.FP32, sel)
     e = per_receiver(s, ref)
     tol = TOL_FP64 if prec == "fp64" else TOL_FP32
+    print(f"{name} {prec}: per-receiver rel-L2 max {e.max():.3e} median {np.median(e):.3e}")
     assert np.isfinite(e).all() and e.max() <= tol, (name, prec, float(e.max()), float(np.median(e)))
