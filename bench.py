@@ -729,7 +729,8 @@ def bench_tile(args, ws, rank, local, td):
     (m, d), = heldout_models(rank, 1, args.receivers)
     sel = np.linspace(1, 4095, 64).astype(np.int32)
     ctx = g.Context(local)
-    plan = g.Plan(ctx, g.make_model(**m), learned.plain_opts(freq_sel=sel), d)
+    bf16 = args.tc_split == "bf16"
+    plan = g.Plan(ctx, g.make_model(**m), learned.plain_opts(freq_sel=sel, tc_split=g.TC_3XBF16 if bf16 else 0), d)
     for _ in range(args.warmup):
         plan.execute()
     barrier(td)
@@ -738,23 +739,26 @@ def bench_tile(args, ws, rank, local, td):
     plan.close()
     ctx.close()
     t = float(np.median(ms)) * 1e-3
-    tf32_peak = 0.5 * float(measured_peaks().get("bf16_tflops", 1859.0))
+    # dense rate of the split form's MMAs: the measured bf16 burst, TF32 at half of it
+    mma_peak = float(measured_peaks().get("bf16_tflops", 1859.0)) * (1.0 if bf16 else 0.5)
     # executed MMA work: 3 TF32 products x (25 pairs x 32-receiver tiles x 128 rows x k)
     n_rt = (len(d) + 31) // 32
     mma_flop = 3 * 2 * 25 * n_rt * 32 * 128 * 32768
     algo_flop = 2 * 2 * 64 * 32768 * len(d) * 32
+    form = "3xBF16" if bf16 else "3xTF32"
     out = {"metric": "tensor-core wavenumber sum, one 64-frequency tile (TFLOP/s, algorithmic)",
            "value": algo_flop / t / 1e12, "unit": "TFLOP/s", "n_gpus": ws, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f32 (3xTF32 products, FP32 accumulation)", "data": "synthetic (seeded)",
+           "vs_baseline": None, "dtype": f"f32 ({form} products, FP32 accumulation)", "data": "synthetic (seeded)",
            "config": {"workload": "k-sum tile: held-out 40-layer model 0 of the default workload, 64 frequencies "
                                   "spread over nt 8192, 32768 wavenumbers, %d receivers" % len(d),
                       "l2": "inputs larger than L2 (coefficients 235 MB, Bessel table 1.2 GB)"},
-           "roofline": {"bound": "tensor", "achieved": algo_flop / t / 1e12, "peak": tf32_peak, "unit": "TFLOP/s",
-                        "frac": algo_flop / t / 1e12 / tf32_peak, "traffic": None,
-                        "executed_tflops": mma_flop / t / 1e12, "executed_frac": mma_flop / t / 1e12 / tf32_peak,
-                        "peak_source": "half of the measured bf16 burst (MEASURED_PEAKS.json bf16_tflops): the "
-                                       "dense TF32 rate of the tensor cores",
+           "roofline": {"bound": "tensor", "achieved": algo_flop / t / 1e12, "peak": mma_peak, "unit": "TFLOP/s",
+                        "frac": algo_flop / t / 1e12 / mma_peak, "traffic": None,
+                        "executed_tflops": mma_flop / t / 1e12, "executed_frac": mma_flop / t / 1e12 / mma_peak,
+                        "peak_source": ("the measured bf16 burst (MEASURED_PEAKS.json bf16_tflops)" if bf16 else
+                                        "half of the measured bf16 burst (MEASURED_PEAKS.json bf16_tflops): the "
+                                        "dense TF32 rate of the tensor cores"),
                         "kernel": "ksum_tc_kernel<tensor>", "k_slice": r.k_slice},
            "gpu_launches": 2 * args.steps}
     if rank == 0:
@@ -779,6 +783,8 @@ def main():
     ap.add_argument("--models", type=int, default=2, help="batch40: models per batch")
     ap.add_argument("--receivers", type=int, default=1000, help="batch40: receivers per model")
     ap.add_argument("--chunk", type=int, default=32, help="uneven256: models per batch")
+    ap.add_argument("--tc-split", default="tf32", choices=["tf32", "bf16"],
+                    help="split form of the tensor-core wavenumber sums (tile case)")
     args = ap.parse_args()
     ws, rank, local, td = dist_setup()
     if args.case == "batch40":
