@@ -904,15 +904,16 @@ extern "C" int grt_plan_fetch(grt_plan *p, double *traces, double *spectra)
 // (|post|^2, the Hermitian pair, the inverse DFT and the de-damping,
 // E|dx|^2 = sum_n damp_n^2 * 2 sum_w |post_w|^2 v_w), over the trace's norm,
 // times eps.  Receivers between two distance bands interpolate linearly.
-// The coefficients' noise level eps(w) of an FP32 plan, measured: a
-// spectra-only FP64 plan over kSpotFreqs spot frequencies (half spread
-// geometrically over the lowest quarter of the band, where the far receivers'
-// energy is, the rest evenly up to the last) evaluates the same (w, k)
-// points; eps^2(w_s) = sum num / sum den of spot_noise_kernel, interpolated
-// linearly between spot frequencies.
+// The coefficients' noise level eps(w, class, band) of an FP32 plan,
+// measured: a spectra-only FP64 plan over kSpotFreqs spot frequencies (half
+// spread geometrically over the lowest quarter of the band, where the far
+// receivers' energy is, the rest evenly up to the last) evaluates the same
+// (w, k) points; eps^2 = num / den of spot_noise_kernel per (spot, class,
+// band), interpolated linearly in frequency between spots.
 constexpr int kSpotFreqs = 16;
 
 static int spot_noise(grt_plan *p, const grt::NoiseArgs<float> &A, std::vector<int> &rows, std::vector<double> &eps2)
+// eps2: [spot][class][band]
 {
     grt_ctx *ctx = p->ctx;
     const Job &J = p->J;
@@ -949,9 +950,10 @@ static int spot_noise(grt_plan *p, const grt::NoiseArgs<float> &A, std::vector<i
     int *drows = nullptr;
     double *dout = nullptr;
     cudaError_t e = dev_alloc(ctx, &drows, ns * sizeof(int));
-    if (e == cudaSuccess) e = dev_alloc(ctx, &dout, (size_t)ns * A.ncls * 2 * sizeof(double));
+    constexpr int NB = grt::kNoiseBands;
+    if (e == cudaSuccess) e = dev_alloc(ctx, &dout, (size_t)ns * A.ncls * 2 * NB * sizeof(double));
     cudaStream_t st = ctx->stream;
-    std::vector<double> h((size_t)ns * A.ncls * 2);
+    std::vector<double> h((size_t)ns * A.ncls * 2 * NB);
     if (e == cudaSuccess) e = cudaMemcpyAsync(drows, sel.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) {
         grt::spot_noise_kernel<float><<<(unsigned)(ns * A.ncls), grt::kNoiseThreads, 0, st>>>(
@@ -964,15 +966,13 @@ static int spot_noise(grt_plan *p, const grt::NoiseArgs<float> &A, std::vector<i
     dev_free(ctx, dout);
     grt_plan_destroy(q.release());
     CU(e);
-    eps2.assign(ns, 0.0);
-    for (int i = 0; i < ns; i++) {
-        double num = 0, den = 0;
-        for (int c = 0; c < A.ncls; c++) {
-            num += h[((size_t)i * A.ncls + c) * 2];
-            den += h[((size_t)i * A.ncls + c) * 2 + 1];
-        }
-        eps2[i] = den > 0 ? num / den : 0.0;
-    }
+    eps2.assign((size_t)ns * A.ncls * NB, 0.0);
+    for (int i = 0; i < ns; i++)
+        for (int c = 0; c < A.ncls; c++)
+            for (int b = 0; b < NB; b++) {
+                const double *o = &h[((size_t)i * A.ncls + c) * 2 * NB];
+                eps2[((size_t)i * A.ncls + c) * NB + b] = o[NB + b] > 0 ? o[b] / o[NB + b] : 0.0;
+            }
     return GRT_OK;
 }
 
@@ -1019,24 +1019,29 @@ static int error_estimate(grt_plan *p, double eps, double *est)
     A.dk = J.dk;
     A.nw = J.nw;
     // the coefficients' noise level: given, or measured against FP64 (FP32 plans)
+    // eps^2 per (spot row, class, band)
     std::vector<int> srow;
     std::vector<double> seps2;
-    if (eps > 0) {
+    const size_t per = (size_t)A.ncls * NB;
+    if (eps > 0 || !std::is_same<R, float>::value) {
+        const double e0 = eps > 0 ? eps : GRT_EPS_FP64;
         srow.assign(1, 0);
-        seps2.assign(1, eps * eps);
+        seps2.assign(per, e0 * e0);
     } else if constexpr (std::is_same<R, float>::value) {
         int rc = spot_noise(p, A, srow, seps2);
         if (rc) return rc;
-    } else {
-        srow.assign(1, 0);
-        seps2.assign(1, GRT_EPS_FP64 * GRT_EPS_FP64);
     }
+    // eps^2 at a row, interpolated between spot rows (constant beyond them)
+    std::vector<double> e2row(per);
     auto eps2_at = [&](int row) {
-        if (row <= srow.front()) return seps2.front();
-        if (row >= srow.back()) return seps2.back();
-        size_t i = std::upper_bound(srow.begin(), srow.end(), row) - srow.begin();
-        const double f = (double)(row - srow[i - 1]) / (srow[i] - srow[i - 1]);
-        return (1 - f) * seps2[i - 1] + f * seps2[i];
+        size_t i1 = std::upper_bound(srow.begin(), srow.end(), row) - srow.begin();
+        if (i1 == 0 || i1 == srow.size()) {
+            const size_t i = i1 == 0 ? 0 : srow.size() - 1;
+            for (size_t x = 0; x < per; x++) e2row[x] = seps2[i * per + x];
+        } else {
+            const double f = (double)(row - srow[i1 - 1]) / (srow[i1] - srow[i1 - 1]);
+            for (size_t x = 0; x < per; x++) e2row[x] = (1 - f) * seps2[(i1 - 1) * per + x] + f * seps2[i1 * per + x];
+        }
     };
     float *H = nullptr;
     double *nrm = nullptr;
@@ -1066,8 +1071,9 @@ static int error_estimate(grt_plan *p, double eps, double *est)
     for (int row = 0; row < J.nw; row++) {
         const int iw = grt::job_freq(J, row);
         const double st0 = iw > wc ? 0.5 * (1. + std::cos((iw - wc + 1) * PI / (J.nwf - wc + 1))) : 1.0;
-        const double wgt = eps2_at(row) * 2.0 * (st0 * coef) * (st0 * coef);
-        for (size_t i = 0; i < G.size(); i++) G[i] += wgt * h[(size_t)row * A.ncls * NB + i];
+        const double wgt = 2.0 * (st0 * coef) * (st0 * coef);
+        eps2_at(row);
+        for (size_t i = 0; i < G.size(); i++) G[i] += wgt * e2row[i] * h[(size_t)row * A.ncls * NB + i];
     }
     double damp2 = 0.0;
     for (int n = 0; n < J.N; n++) {

@@ -675,21 +675,27 @@ __global__ void __launch_bounds__(kNoiseThreads) noise_kernel(NoiseArgs<R> A)
 }
 
 // The coefficients' actual FP32 noise at a few spot frequencies, against an
-// FP64 evaluation of the same (w, k) points: per spot frequency s and class c,
-//   num[s][c] = sum_k w_k^2 k^(2 kp) |K32_q - K64_q|^2,  den[s][c] = sum_k w_k^2 k^(2 kp) |K64_q|^2,
-// weighted as the wavenumber sum weights them.  K64: flat [nq][nkw64]
-// complex of a spectra-only FP64 plan over the spot frequencies (koff64).
+// FP64 evaluation of the same (w, k) points: per spot frequency s, class c and
+// distance band b,
+//   num[s][c][b] = sum_k w_k^2 k^(2 kp) |K32_q - K64_q|^2 / (1 + pi k r_b),
+//   den[s][c][b] = sum_k w_k^2 k^(2 kp) |K64_q|^2 / (1 + pi k r_b),
+// weighted as the wavenumber sum at band distance r_b weights them (the
+// relative error of the coefficients varies with k, and a far receiver
+// weighs the small wavenumbers more).  K64: flat [nq][nkw64] complex of a
+// spectra-only FP64 plan over the spot frequencies (koff64).
 template <typename R>
 __global__ void __launch_bounds__(kNoiseThreads) spot_noise_kernel(NoiseArgs<R> A, const double *K64,
                                                                    const long long *koff64, long long nkw64,
                                                                    const int *rows, double *out)
 {
-    __shared__ double red[2][kNoiseThreads];
+    __shared__ float red[kNoiseThreads][2 * kNoiseBands + 1];
     const int s = blockIdx.x / A.ncls, c = blockIdx.x % A.ncls;
     const int iw = rows[s], q = A.cls_q[c], kp = A.cls_p[c];
     const int nk = A.nk[iw], m = A.ks ? A.ks[iw] : 1;
     const double dkm = A.dk * m;
-    double num = 0.0, den = 0.0;
+    float num[kNoiseBands], den[kNoiseBands];
+#pragma unroll
+    for (int b = 0; b < kNoiseBands; b++) num[b] = den[b] = 0.f;
     for (int j = threadIdx.x; j < nk; j += blockDim.x) {
         double re, im;
         if (A.Kt) {
@@ -706,22 +712,25 @@ __global__ void __launch_bounds__(kNoiseThreads) spot_noise_kernel(NoiseArgs<R> 
         const double k = dkm * j, w = (j == 0 ? 0.5 * dkm : dkm);
         double f = w * w;
         for (int e = 0; e < kp; e++) f *= k * k;
-        num += f * ((re - v64.x) * (re - v64.x) + (im - v64.y) * (im - v64.y));
-        den += f * (v64.x * v64.x + v64.y * v64.y);
-    }
-    red[0][threadIdx.x] = num;
-    red[1][threadIdx.x] = den;
-    __syncthreads();
-    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
-        if ((int)threadIdx.x < h) {
-            red[0][threadIdx.x] += red[0][threadIdx.x + h];
-            red[1][threadIdx.x] += red[1][threadIdx.x + h];
+        const float dn = (float)(f * ((re - v64.x) * (re - v64.x) + (im - v64.y) * (im - v64.y)));
+        const float dd = (float)(f * (v64.x * v64.x + v64.y * v64.y));
+#pragma unroll
+        for (int b = 0; b < kNoiseBands; b++) {
+            const float wr = 1.f / (1.f + 3.14159265f * (float)k * A.rb[b]);
+            num[b] += dn * wr;
+            den[b] += dd * wr;
         }
-        __syncthreads();
     }
-    if (threadIdx.x == 0) {
-        out[2 * blockIdx.x] = red[0][0];
-        out[2 * blockIdx.x + 1] = red[1][0];
+#pragma unroll
+    for (int b = 0; b < kNoiseBands; b++) {
+        red[threadIdx.x][b] = num[b];
+        red[threadIdx.x][kNoiseBands + b] = den[b];
+    }
+    __syncthreads();
+    if (threadIdx.x < 2 * kNoiseBands) {
+        double t = 0.0;
+        for (int i = 0; i < (int)blockDim.x; i++) t += red[i][threadIdx.x];
+        out[(long long)blockIdx.x * 2 * kNoiseBands + threadIdx.x] = t;   // [s][c][num b..., den b...]
     }
 }
 
