@@ -484,7 +484,15 @@ def bench_uneven(args, ws, rank, local, td):
     """Batched uneven instances: seeded models with 3-60 layers, source U(1,30)
     km, 16-512 receivers in 5-400 km, N in {1024, 2048, 4096} at dt 0.05 s,
     the reference's k rule, run as batches of up to --chunk models (one CUDA
-    graph each) against the same jobs as one plan at a time."""
+    graph each) against the same jobs as one plan at a time.
+
+    Judged (the headline of this case): after each batch, the error estimate
+    of every job (grt_batch_error_estimate: the coefficients' FP32 noise
+    measured against FP64 at 16 spot frequencies, carried through the
+    wavenumber sum and the spectral stage) flags the receivers whose traces
+    may exceed 1e-3 against FP64 (estimate above 1e-3 / 3); those are
+    recomputed by the FP64 path.  Every trace of every model is then checked
+    against the FP64 path (untimed)."""
     import grtm_cuda_gb300 as g
     from grtm_cuda_gb300 import synth
     work = synth.uneven_models(4000 + rank, args.models)
@@ -494,7 +502,7 @@ def bench_uneven(args, ws, rank, local, td):
                           "k rule, quirks corrected",
               "models": args.models, "chunk": chunk, "traces_per_step": int(sum(len(w["dists"]) for w in work)),
               "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}
-    metric = "Green's-fn traces/s, batched uneven models vs one plan at a time (1 GB300)"
+    metric = "Green's-fn traces/s at <=1e-3 rel-L2 vs FP64, batched uneven models (1 GB300)"
     ntr = config["traces_per_step"]
     if args.impl == "reference":
         if rank == 0:
@@ -518,26 +526,51 @@ def bench_uneven(args, ws, rank, local, td):
         return (g.make_model(**w["model"]), o, w["dists"])
 
     jobs = [job(w) for w in work]
-    chunks = [jobs[i:i + chunk] for i in range(0, len(jobs), chunk)]
-    # batched: build each chunk's graph once, then time the graph launches
-    def batched_pass(keep):
-        ms = 0.0
-        for c in chunks:
+    starts = list(range(0, len(jobs), chunk))
+
+    def batched_pass(judge):
+        """One pass over all models: (graph ms, judge s, FP64 fallback s,
+        per-trace errors of the FP32 and of the judged traces against the FP64
+        path, FP64 receivers by model).  The FP64 check of every trace runs
+        outside the timed parts."""
+        ms, t_est, t_fb = 0.0, 0.0, 0.0
+        e32, ej, routed = [], [], []
+        for c0 in starts:
+            c = jobs[c0:c0 + chunk]
             b = g.Batch(ctx, c, autotune=True)
-            for _ in range(keep):
-                r = b.execute()
-            ms += r.ms_total
+            ms += b.execute().ms_total
+            if judge:
+                for j, (m, o, d) in enumerate(c):
+                    t = time.time()
+                    est = b.error_estimate(j)
+                    bad = np.nonzero(3.0 * est > 1e-3)[0]
+                    t_est += time.time() - t
+                    tr, _ = b.fetch(j)
+                    t = time.time()
+                    t_bad = g.run(m, g.with_precision(o, g.FP64), np.asarray(d)[bad], ctx)[0] if bad.size else None
+                    t_fb += time.time() - t
+                    # check (untimed): every receiver against the FP64 path
+                    t64, _, _ = g.run(m, g.with_precision(o, g.FP64), d, ctx)
+                    den = np.linalg.norm(t64, axis=(1, 2))
+                    e32.append(np.linalg.norm(tr - t64, axis=(1, 2)) / den)
+                    if bad.size:
+                        tr[bad] = t_bad
+                    ej.append(np.linalg.norm(tr - t64, axis=(1, 2)) / den)
+                    routed.append(bad)
             b.close()
-        return ms
-    batched_pass(1)
+        return ms, t_est, t_fb, e32, ej, routed
+
+    batched_pass(False)
     clocks = ClockSampler(local)
     clocks.start()
     barrier(td)
     device_sync()
     t0 = time.time()
-    ms_b = [batched_pass(1) for _ in range(args.steps)]
+    ms_b = [batched_pass(False)[0] for _ in range(args.steps)]
     wall = (time.time() - t0) / args.steps
     clk = clocks.stop()
+    # the judged pass (once): graph time + estimates + FP64 recomputation
+    ms_j, t_est, t_fb, e_fp32, e_judged, routed = batched_pass(True)
     # one plan at a time (same arithmetic)
     ms_p = 0.0
     for j in jobs:
@@ -546,32 +579,30 @@ def bench_uneven(args, ws, rank, local, td):
         ms_p += p.execute().ms_total
         p.close()
     t_b = allmax(td, float(np.median(ms_b)) * 1e-3)
-    # accuracy against FP64 on 8 models spread over the batch's sizes
-    cost = np.array([len(w["model"]["vp"]) * (1 << w["log2n"]) * len(w["dists"]) for w in work])
-    sample = np.argsort(cost)[np.linspace(0, len(work) - 1, min(8, len(work))).astype(int)]
-    errs = []
-    for i in sample:
-        t32, _, _ = g.run(*job(work[i]), ctx=ctx)
-        t64, _, _ = g.run(*job(work[i], g.FP64), ctx=ctx)
-        errs.append(np.linalg.norm(t32 - t64, axis=(1, 2)) / np.linalg.norm(t64, axis=(1, 2)))
-    errs = np.concatenate(errs)
-    frac_ok = float(np.mean(errs <= 1e-3))
+    t_j = allmax(td, ms_j * 1e-3 + t_est + t_fb)
+    e_fp32, e_judged = np.concatenate(e_fp32), np.concatenate(e_judged)
+    n_routed = int(sum(r.size for r in routed))
+    n_models_routed = int(sum(1 for r in routed if r.size))
     if rank != 0:
         barrier(td)
         return
-    out = {"metric": metric, "value": ws * ntr / t_b, "unit": "traces/s", "n_gpus": ws, "steps": args.steps,
-           "warmup": 1, "ms_per_step": 1000 * t_b, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-           "dtype": "c64", "data": "synthetic (seeded)", "config": config,
+    out = {"metric": metric, "value": ws * ntr / t_j, "unit": "traces/s", "n_gpus": ws, "steps": 1,
+           "warmup": 1, "ms_per_step": 1000 * t_j, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "c64 (FP32 path; receivers the judge flags recomputed in FP64)", "data": "synthetic (seeded)",
+           "config": config,
+           "judged": {"graph_ms": ms_j, "s_estimate": t_est, "s_fp64_fallback": t_fb,
+                      "traces_routed_to_fp64": n_routed, "models_with_routed_traces": n_models_routed,
+                      "accuracy": err_stats(e_judged)},
+           "fp32_only": {"value": ws * ntr / t_b, "ms": 1000 * t_b, "steps": args.steps,
+                         "value_at_1e-3": ws * ntr / t_b * float(np.mean(e_fp32 <= 1e-3)),
+                         "accuracy": err_stats(e_fp32),
+                         "note": "the FP32 batches alone; traces beyond 1e-3 are far receivers of short windows, "
+                                 "whose wavenumber sums cancel beyond what FP32 coefficients resolve"},
            "one_plan_at_a_time": {"value": ntr / (ms_p * 1e-3), "ms": ms_p},
            "speedup_batched": (ms_p * 1e-3) / t_b,
            "e2e": {"value": ws * ntr / wall, "unit": "traces/s", "h2d_bytes_per_step": None,
-                   "d2h_bytes_per_step": None, "note": "graph build + execution per step, no download"},
-           "accuracy": {"models_checked": int(len(sample)), "traces_checked": int(errs.size),
-                        "max": float(errs.max()), "median": float(np.median(errs)), "frac_le_1e-3": frac_ok},
-           "value_at_1e-3": ws * ntr / t_b * frac_ok,
-           "accuracy_note": "traces beyond 1e-3 are far receivers of short windows (arrivals after the "
-                            "nt*dt window): the FP32 noise floor of the GRT coefficients then dominates "
-                            "the little that stays in the window",
+                   "d2h_bytes_per_step": None, "note": "FP32 graph build + execution per step, no download"},
+           "accuracy_checked": f"every trace of all {len(work)} models ({e_judged.size}) against the FP64 path",
            "clocks": clk}
     print(json.dumps(out))
     barrier(td)
