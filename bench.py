@@ -480,6 +480,12 @@ def bench_batch(args, ws, rank, local, td):
     barrier(td)
 
 
+# The judge's margin: over 15 calibration models the measured FP32 error of a
+# trace near 1e-3 was 0.4-2.6 times its estimate; a receiver is recomputed in
+# FP64 when 4 times its estimate exceeds the tolerance.
+JUDGE_SAFETY = 4.0
+
+
 def bench_uneven(args, ws, rank, local, td):
     """Batched uneven instances: seeded models with 3-60 layers, source U(1,30)
     km, 16-512 receivers in 5-400 km, N in {1024, 2048, 4096} at dt 0.05 s,
@@ -490,7 +496,7 @@ def bench_uneven(args, ws, rank, local, td):
     of every job (grt_batch_error_estimate: the coefficients' FP32 noise
     measured against FP64 at 16 spot frequencies, carried through the
     wavenumber sum and the spectral stage) flags the receivers whose traces
-    may exceed 1e-3 against FP64 (estimate above 1e-3 / 3); those are
+    may exceed 1e-3 against FP64 (estimate above 1e-3 / JUDGE_SAFETY); those are
     recomputed by the FP64 path.  Every trace of every model is then checked
     against the FP64 path (untimed)."""
     import grtm_cuda_gb300 as g
@@ -543,7 +549,7 @@ def bench_uneven(args, ws, rank, local, td):
                 for j, (m, o, d) in enumerate(c):
                     t = time.time()
                     est = b.error_estimate(j)
-                    bad = np.nonzero(3.0 * est > 1e-3)[0]
+                    bad = np.nonzero(JUDGE_SAFETY * est > 1e-3)[0]
                     t_est += time.time() - t
                     tr, _ = b.fetch(j)
                     t = time.time()

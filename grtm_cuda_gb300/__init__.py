@@ -627,7 +627,7 @@ def with_precision(opts, precision):
     return o
 
 
-def run_judged(model, opts, dists, ctx=None, tol=1e-3, eps=0.0, safety=3.0):
+def run_judged(model, opts, dists, ctx=None, tol=1e-3, eps=0.0, safety=4.0):
     """FP32 traces, judged: every receiver whose predicted error against FP64
     (grt_plan_error_estimate) exceeds tol / safety is recomputed by the FP64
     path.
