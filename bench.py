@@ -412,6 +412,14 @@ def bench_batch(args, ws, rank, local, td):
     tc_grt_ms = r.ms_grt
     _, tc_tune = btc.info()
     btc.close()
+    # the fast arm with every correction of the reference in the tensor-core
+    # layout (FIX_PHYSICAL_TC: physical displacement and d/dr columns), same models
+    phys_plain = dict(learned.PLAIN, fix=g.FIX_PHYSICAL_TC)
+    phys_ms = []
+    for _ in range(3):
+        _, pi_ = learned.run_learned_batch(sampler, models, dists, ctx=ctx, out=pinned, plain=phys_plain)
+        phys_ms.append(pi_["ms_batch_gpu"] * 1e-3 + pi_["s_judge"] + pi_["s_fallback"])
+    phys_value = ws * ntr / float(np.median(phys_ms[1:]))
     if rank != 0:
         barrier(td)
         return
@@ -447,6 +455,10 @@ def bench_batch(args, ws, rank, local, td):
                      "stride_mean": last["stride_mean"], "fallback_traces": last["n_fallback"],
                      "tune": infos[0]["tune"]},
             "tc": {"value": ntr / (min(tc_ms) * 1e-3), "ms": min(tc_ms), "ms_grt": tc_grt_ms, "tune": tc_tune},
+            "fast_physical": {"value": phys_value, "fix": "FIX_PHYSICAL_TC (corrected 20-column layout, SH source "
+                                                        "terms, receiver layer and d/dz terms)",
+                              "fallback_traces": int(pi_["n_fallback"]), "points_vs_plain":
+                                  pi_["nkw_learned"] / pi_["nkw_plain"]},
             "plain": {"value": ntr / (min(plain_ms) * 1e-3), "ms": min(plain_ms), "ms_grt": plain_grt_ms,
                       "ms_ksum": plain_ksum_ms, "e2e": plain_e2e,
                       "ksum": {"kernel": "cuBLAS SGEMM (FP32, no TF32): one product per pair of the integrand "

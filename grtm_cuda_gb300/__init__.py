@@ -25,6 +25,10 @@ FIX_ALL = FIX_RLAYER | FIX_REXUT | FIX_DZ
 # every correction of the reference: the receiver layer and d/dz terms, the corrected
 # column layouts and the moment tensor's SH source terms (0 reproduces the reference)
 FIX_PHYSICAL = FIX_ALL | FIX_COLS | FIX_SHSRC
+# the same corrections in the 20-column layout (displacement and d/dr, no d/dz):
+# physical moment-tensor output on the tensor-core wavenumber sum
+FIX_COLS20 = 32
+FIX_PHYSICAL_TC = FIX_ALL | FIX_COLS20 | FIX_SHSRC
 
 _dp = ctypes.POINTER(ctypes.c_double)
 

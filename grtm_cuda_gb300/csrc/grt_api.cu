@@ -233,26 +233,49 @@ static cudaError_t raise_smem_limit(F *kernel, int bytes)
 // output column layout, count and coefficient columns of a job
 static int col_kind(const Job &J)
 {
-    const bool fix = (J.fix & grt::kFixCols) != 0;
-    return J.src == 0 ? (fix ? grt::kColSingleFix : grt::kColSingle) : (fix ? grt::kColTensorFix : grt::kColTensor);
+    const bool fix = (J.fix & grt::kFixCols) != 0, fix20 = (J.fix & grt::kFixCols20) != 0;
+    if (J.src == 0) return (fix || fix20) ? grt::kColSingleFix : grt::kColSingle;
+    return fix ? grt::kColTensorFix : (fix20 ? grt::kColTensorFix20 : grt::kColTensor);
 }
 static int col_count(int kind)
 {
-    return kind == grt::kColTensorFix ? grt::kTensorFixNC : (kind == grt::kColTensor ? grt::kTensorNC : grt::kSingleNC);
+    return kind == grt::kColTensorFix ? grt::kTensorFixNC
+                                      : ((kind == grt::kColTensor || kind == grt::kColTensorFix20) ? grt::kTensorNC
+                                                                                                : grt::kSingleNC);
+}
+// the tensor-core plan of a column layout (the 30-column layout has none: SIMT sums)
+static grt::TcPlan tc_plan(int kind)
+{
+    static constexpr grt::TcPlan ts = grt::make_tcplan<grt::kColSingle>(), tt = grt::make_tcplan<grt::kColTensor>(),
+                                 tsf = grt::make_tcplan<grt::kColSingleFix>(),
+                                 tt20 = grt::make_tcplan<grt::kColTensorFix20>();
+    switch (kind) {
+    case grt::kColTensor: return tt;
+    case grt::kColSingleFix: return tsf;
+    case grt::kColTensorFix20: return tt20;
+    case grt::kColTensorFix: {
+        grt::TcPlan none{};
+        for (int q = 0; q < 16; q++) none.qslot[q] = -1;
+        return none;
+    }
+    default: return ts;
+    }
 }
 // operand tiles per stage block of the tensor-core sum (coefficient columns it reads)
 static int tc_tiles(int kind)
 {
-    constexpr grt::TcPlan ts = grt::make_tcplan<grt::kColSingle>(), tt = grt::make_tcplan<grt::kColTensor>();
-    return kind == grt::kColTensor ? tt.nqu : (kind == grt::kColTensorFix ? 0 : ts.nqu);
+    return kind == grt::kColTensorFix ? 0 : tc_plan(kind).nqu;
 }
-static const grt::ColTerms kColTermsTab[4] = {grt::make_colterms<grt::kColSingle>(), grt::make_colterms<grt::kColTensor>(),
+static const grt::ColTerms kColTermsTab[5] = {grt::make_colterms<grt::kColSingle>(), grt::make_colterms<grt::kColTensor>(),
                                               grt::make_colterms<grt::kColSingleFix>(),
-                                              grt::make_colterms<grt::kColTensorFix>()};
+                                              grt::make_colterms<grt::kColTensorFix>(),
+                                              grt::make_colterms<grt::kColTensorFix20>()};
 
 static int coef_count(int kind)
 {
-    return kind == grt::kColTensorFix ? 2 * (int)grt::QT_N : (kind == grt::kColTensor ? (int)grt::QT_N : (int)grt::QS_N);
+    return kind == grt::kColTensorFix ? 2 * (int)grt::QT_N
+                                      : ((kind == grt::kColTensor || kind == grt::kColTensorFix20) ? (int)grt::QT_N
+                                                                                                : (int)grt::QS_N);
 }
 
 // ------------------------------------------------------------------ host tables
@@ -524,6 +547,7 @@ static int launch_ksum_tc(grt_plan *p, cudaStream_t st, int &launches)
     const unsigned grid = (unsigned)(nwt * nrt * p->nsplit);
     if (p->cols == grt::kColSingle) CU(launch_tc_groups<grt::kColSingle>(T, grid, st, p->tc_bf16));
     else if (p->cols == grt::kColSingleFix) CU(launch_tc_groups<grt::kColSingleFix>(T, grid, st, p->tc_bf16));
+    else if (p->cols == grt::kColTensorFix20) CU(launch_tc_groups<grt::kColTensorFix20>(T, grid, st, p->tc_bf16));
     else CU(launch_tc_groups<grt::kColTensor>(T, grid, st, p->tc_bf16));
     launches++;
     const long long n = (long long)p->nd * p->nc * J.nw * 2;
@@ -559,6 +583,10 @@ static grt::GrtArgs<R> grt_args(const grt_plan *p)
     A.kt_base = p->kt_base;
     A.nqt = tc_tiles(p->cols);
     A.kt_bf16 = p->tc_bf16;
+    {
+        const grt::TcPlan tp = tc_plan(p->cols);
+        for (int q = 0; q < 16; q++) A.qslot[q] = (signed char)tp.qslot[q];
+    }
     return A;
 }
 
@@ -570,7 +598,7 @@ static int launch_bessel(grt_plan *p, cudaStream_t st, int &launches)
     const long long n = (long long)J.nbrow * p->nd;
     const int blocks = (int)((n + 255) / 256);
     grt::bessel_table_kernel<R><<<blocks, 256, 0, st>>>((R *)p->B, J.nbrow, p->nd, J.dk, p->ddist, p->bt_rows,
-                                                        (J.fix & grt::kFixCols) ? 1 : 0);
+                                                        (J.fix & (grt::kFixCols | grt::kFixCols20)) ? 1 : 0);
     launches++;
     CU(cudaGetLastError());
     return GRT_OK;
@@ -651,6 +679,7 @@ static int launch_ksum_gemm(grt_plan *p, cudaStream_t st, int &launches)
     case grt::kColSingle: CU(launch_gemm_combine<grt::kColSingle>(p, st)); break;
     case grt::kColSingleFix: CU(launch_gemm_combine<grt::kColSingleFix>(p, st)); break;
     case grt::kColTensorFix: CU(launch_gemm_combine<grt::kColTensorFix>(p, st)); break;
+    case grt::kColTensorFix20: CU(launch_gemm_combine<grt::kColTensorFix20>(p, st)); break;
     default: CU(launch_gemm_combine<grt::kColTensor>(p, st)); break;
     }
     launches++;
@@ -677,6 +706,7 @@ static int launch_ksum(grt_plan *p, cudaStream_t st, int &launches)
     case grt::kColSingle: grt::ksum_kernel<R, grt::kColSingle><<<grid, grt::kSumThreads, 0, st>>>(S); break;
     case grt::kColSingleFix: grt::ksum_kernel<R, grt::kColSingleFix><<<grid, grt::kSumThreads, 0, st>>>(S); break;
     case grt::kColTensorFix: grt::ksum_kernel<R, grt::kColTensorFix><<<grid, grt::kSumThreads, 0, st>>>(S); break;
+    case grt::kColTensorFix20: grt::ksum_kernel<R, grt::kColTensorFix20><<<grid, grt::kSumThreads, 0, st>>>(S); break;
     default: grt::ksum_kernel<R, grt::kColTensor><<<grid, grt::kSumThreads, 0, st>>>(S); break;
     }
     launches++;
@@ -1005,9 +1035,7 @@ static int error_estimate(grt_plan *p, double eps, double *est)
         A.kt_base = p->kt_base;
         A.nqt = tc_tiles(p->cols);
         A.kt_bf16 = p->tc_bf16;
-        const grt::TcPlan tp = p->cols == grt::kColTensor ? grt::make_tcplan<grt::kColTensor>()
-                                                          : (p->cols == grt::kColSingleFix ? grt::make_tcplan<grt::kColSingleFix>()
-                                                                                           : grt::make_tcplan<grt::kColSingle>());
+        const grt::TcPlan tp = tc_plan(p->cols);
         for (int q = 0; q < 16; q++) A.qslot[q] = tp.qslot[q];
     } else {
         A.K = (const R *)p->K;
@@ -1754,6 +1782,7 @@ static int batch_build(grt_batch *b, int autotune)
         if (p->use_tc) {
             CU(raise_tc_limits<grt::kColSingle>(p->tc_bf16));
             CU(raise_tc_limits<grt::kColSingleFix>(p->tc_bf16));
+            CU(raise_tc_limits<grt::kColTensorFix20>(p->tc_bf16));
             CU(raise_tc_limits<grt::kColTensor>(p->tc_bf16));
         }
     }

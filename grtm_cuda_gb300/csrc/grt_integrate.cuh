@@ -340,6 +340,44 @@ constexpr __device__ int kTensorFixCol[31] = {0,  2,  4,  5,  6,  8,  10, 11, 12
                                               24, 25, 26, 27, 28, 31, 34, 35, 36, 39, 42, 43, 44, 45, 46};
 constexpr int kTensorFixNC = 30;
 
+// corrected moment tensor in the 20-column layout of the tensor-core sum:
+// displacement 0-9 and d/dr 10-19 as in the 30-column corrected layout (its
+// columns 0-9 and 20-29) -- the m = 0 radial columns 2, 3 (d/dr 12, 13) with
+// the radial coefficients a20, a00 where green.cu:1652-1653 take a21, a01,
+// the m = 1 transverse column 5 (d/dr 15) with b1 where green.cu:1657, 1686
+// have b2 -- without the d/dz block the reference overwrites
+constexpr __device__ Pair kTensorFix20Pairs[] = {
+    {QT_B2, 0, BJ2},   {QT_A20, 1, BJ2D},  {QT_B1, 0, BJ1},    {QT_A10, 1, BJ1D},  {QT_A20, 1, BJ0D},
+    {QT_A00, 1, BJ0D}, {QT_B2, 1, BJ2D},   {QT_A20, 0, BJ2},   {QT_B1, 2, BJ1DD},  {QT_A10, 0, BJ1},
+    {QT_A21, 1, BJ2},  {QT_A11, 1, BJ1},   {QT_A01, 1, BJ0},   {QT_A21, 1, BJ0},   {QT_A20, 2, BJ2DD},
+    {QT_B1, 1, BJ1D},  {QT_A10, 2, BJ1DD}, {QT_A20, 2, BJ0DD}, {QT_A00, 2, BJ0DD}, {QT_B2, 2, BJ2DD},
+    {QT_A21, 2, BJ2D}, {QT_A11, 2, BJ1D},  {QT_A01, 2, BJ0D},  {QT_A21, 2, BJ0D},
+};
+constexpr int kTensorFix20NP = sizeof(kTensorFix20Pairs) / sizeof(Pair);
+constexpr __device__ Term kTensorFix20Terms[] = {
+    {0, 1, 2.0}, {1, 0, 1.0},                    // 0
+    {2, 1, 1.0}, {3, 0, 1.0},                    // 1
+    {4, 0, 1.0},                                 // 2
+    {5, 0, 1.0},                                 // 3
+    {6, 0, 1.0}, {7, 1, 2.0},                    // 4
+    {15, 0, 1.0}, {9, 1, 1.0},                   // 5
+    {10, 0, 1.0},                                // 6
+    {11, 0, 1.0},                                // 7
+    {12, 0, 1.0},                                // 8
+    {13, 0, 1.0},                                // 9
+    {0, 2, -2.0}, {6, 1, 2.0}, {14, 0, 1.0},     // 10: d/dr
+    {2, 2, -1.0}, {15, 1, 1.0}, {16, 0, 1.0},    // 11
+    {17, 0, 1.0},                                // 12
+    {18, 0, 1.0},                                // 13
+    {19, 0, 1.0}, {7, 2, -2.0}, {1, 1, 2.0},     // 14
+    {8, 0, 1.0}, {9, 2, -1.0}, {3, 1, 1.0},      // 15
+    {20, 0, 1.0},                                // 16
+    {21, 0, 1.0},                                // 17
+    {22, 0, 1.0},                                // 18
+    {23, 0, 1.0},                                // 19
+};
+constexpr __device__ int kTensorFix20Col[21] = {0, 2, 4, 5, 6, 8, 10, 11, 12, 13, 14, 17, 20, 21, 22, 25, 28, 29, 30, 31, 32};
+
 template <int SRC> struct Cols;
 template <> struct Cols<kSingle> {
     static constexpr int NP = kSingleNP, NC = kSingleNC, NQ = QS_N, NT = sizeof(kSingleTerms) / sizeof(Term);
@@ -358,6 +396,12 @@ template <> struct Cols<kColSingleFix> {
     __device__ static constexpr Pair pair(int i) { return kSinglePairs[i]; }
     __device__ static constexpr Term term(int i) { return kSingleFixTerms[i]; }
     __device__ static constexpr int col(int i) { return kSingleCol[i]; }
+};
+template <> struct Cols<kColTensorFix20> {
+    static constexpr int NP = kTensorFix20NP, NC = kTensorNC, NQ = QT_N, NT = sizeof(kTensorFix20Terms) / sizeof(Term);
+    __device__ static constexpr Pair pair(int i) { return kTensorFix20Pairs[i]; }
+    __device__ static constexpr Term term(int i) { return kTensorFix20Terms[i]; }
+    __device__ static constexpr int col(int i) { return kTensorFix20Col[i]; }
 };
 template <> struct Cols<kColTensorFix> {
     static constexpr int NP = kTensorFixNP, NC = kTensorFixNC, NQ = 2 * QT_N, NT = sizeof(kTensorFixTerms) / sizeof(Term);
@@ -388,9 +432,10 @@ struct TcPlan {
 template <int SRC>
 __host__ __device__ constexpr TcPlan make_tcplan()
 {
-    static_assert(SRC == kColSingle || SRC == kColTensor || SRC == kColSingleFix, "tensor-core layouts only");
+    static_assert(SRC == kColSingle || SRC == kColTensor || SRC == kColSingleFix || SRC == kColTensorFix20,
+                  "tensor-core layouts only");
     constexpr int NQ = Cols<SRC>::NQ, NP = Cols<SRC>::NP;
-    auto pair_q = [](int p) { return SRC == kColTensor ? kTensorPairs[p].q : kSinglePairs[p].q; };
+    auto pair_q = [](int p) { return Cols<SRC>::pair(p).q; };
     TcPlan t{};
     int cnt[16] = {}, grp[16] = {};
     for (int q = 0; q < 16; q++) {

@@ -287,14 +287,13 @@ __device__ __forceinline__ KOut make_kout(const GrtArgs<R> &A, int iw, int j)
     return o;
 }
 
-// SRCK: the job's source kind (kSingle / kTensor), which fixes the tensor-core
-// tile of each coefficient column (make_tcplan; columns no pair reads are not stored)
+// the tensor-core tile of each coefficient column comes with the job
+// (make_tcplan of its column layout; columns no pair reads are not stored)
 template <int SRCK, typename R>
 __device__ __forceinline__ void store_q(const GrtArgs<R> &A, int q, const KOut &o, C<R> v)
 {
     if (sizeof(R) == 4 && o.blk) {
-        constexpr TcPlan tp = make_tcplan<SRCK == kTensor ? kColTensor : kColSingle>();
-        const int slot = q < 16 ? tp.qslot[q] : -1;
+        const int slot = q < 16 ? A.qslot[q] : -1;
         if (slot < 0) return;
         float *t = o.blk + slot * 2 * (kTileRows * kTileK);
         const float x = (float)v.x, y = (float)v.y;

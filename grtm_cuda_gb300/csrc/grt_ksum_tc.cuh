@@ -204,7 +204,7 @@ template <int SRC, int GRP> __host__ __device__ constexpr unsigned group_basis_m
     unsigned m = 0;
     for (int s = 0; s < T.gnp[GRP]; s++) {
         const int p = T.gpair[GRP][s];
-        m |= 1u << (SRC == kColTensor ? kTensorPairs[p].b : kSinglePairs[p].b);
+        m |= 1u << Cols<SRC>::pair(p).b;
     }
     return m;
 }

@@ -89,7 +89,7 @@ extern "C" GRT_API int grt_run_noalloc(int device, const grt_model *m, const grt
     }
 
     if (o->k_mode == GRT_K_CUSTOM || o->k_stride) return fail(GRT_ERR_UNSUPPORTED, "custom k grids need grt_run");
-    if (o->fix & GRT_FIX_COLS) return fail(GRT_ERR_UNSUPPORTED, "corrected column layouts need grt_run");
+    if (o->fix & (GRT_FIX_COLS | GRT_FIX_COLS20)) return fail(GRT_ERR_UNSUPPORTED, "corrected column layouts need grt_run");
     if (o->n_freq_sel > 0 || o->freq_sel) return fail(GRT_ERR_UNSUPPORTED, "frequency selections need a plan");
     if (o->k_slice) return fail(GRT_ERR_UNSUPPORTED, "a fixed k_slice needs a plan");
     // the job on the host (same rules as grt_run)

@@ -31,7 +31,9 @@ enum SrcKind { kSingle = 0, kTensor = 1 };
 // output column layouts: the reference's (bug-compatible) ones, and the
 // corrected ones selected by GRT_FIX_COLS (single force: the d/dr column 10
 // with its 1/r; moment tensor: 30 defined columns, d/dz in 10-19, d/dr in 20-29)
-enum ColKind { kColSingle = 0, kColTensor = 1, kColSingleFix = 2, kColTensorFix = 3 };
+// kColTensorFix20: the moment tensor's corrected columns in the 20-column
+// layout of the tensor-core sum (displacement 0-9 and d/dr 10-19, no d/dz)
+enum ColKind { kColSingle = 0, kColTensor = 1, kColSingleFix = 2, kColTensorFix = 3, kColTensorFix20 = 4 };
 // single force: b1, a0[0], a0[1], a1[0], a1[1] and their d/dz versions
 enum QSingle { QS_B1 = 0, QS_A00, QS_A01, QS_A10, QS_A11, QS_B1T, QS_A0T0, QS_A0T1, QS_A1T0, QS_A1T1, QS_N };
 // moment tensor: b1, b2, a0[0..1], a1[0..1], a2[0..1]
@@ -41,7 +43,7 @@ enum QTensor { QT_B1 = 0, QT_B2, QT_A00, QT_A01, QT_A10, QT_A11, QT_A20, QT_A21,
 enum GrtSpec { kSpecGeneric = 0, kSpecAboveTensor = 1 };
 
 // reference-quirk switches (0 = reproduce the reference)
-enum Fix { kFixRLayer = 1, kFixRexut = 2, kFixDz = 4, kFixCols = 8, kFixShsrc = 16 };
+enum Fix { kFixRLayer = 1, kFixRexut = 2, kFixDz = 4, kFixCols = 8, kFixShsrc = 16, kFixCols20 = 32 };
 
 template <typename R>
 struct GrtArgs {
@@ -68,6 +70,7 @@ struct GrtArgs {
     const long long *kt_base;
     int nqt;
     int kt_bf16;               // tiles in the 3xBF16 form (16 k per stage, bf16 hi/lo words)
+    signed char qslot[16];     // tile of coefficient column q in a stage block (-1: not stored)
 };
 
 // Bessel basis functions of k r, in the order the integrand formulas use them

@@ -58,6 +58,12 @@ extern "C" {
                                 * displacement) takes 1 - e Rdu e above the source and m = 2 (a jump
                                 * of the SH traction) 1 + e Rud e below it, and the moment-tensor
                                 * solution satisfies reciprocity with the single-force one. */
+#define GRT_FIX_COLS20 32      /* corrected moment-tensor columns in the reference's 20-column layout, the one
+                                * the tensor-core sum takes: displacement 0-9 and d/dr 10-19 as GRT_FIX_COLS
+                                * gives them in its columns 0-9 and 20-29 (the m = 0 radial columns 2, 3 and
+                                * d/dr 12, 13 with the radial coefficients a20, a00; the m = 1 transverse
+                                * column 5 and d/dr 15 with b1), no d/dz columns; Bessel second derivatives from
+                                * Bessel's equation; single forces as GRT_FIX_COLS.  Ignored with GRT_FIX_COLS. */
 
 /* A layered model: n_layer layers given by the depth of their top (ztop[0] = 0),
  * the last one being the half-space.  Units: km, km/s, g/cm^3. */
@@ -281,7 +287,7 @@ GRT_API int grt_flatten(int n_layer, const double *ztop, const double *vp, const
  * giving displacement Z up, R away from the source, T clockwise (azimuth
  * increasing): by reciprocity every term equals the moment tensor contracted
  * with the gradient, at the source, of the single-force solution for a unit
- * force at the receiver.  The corrected layout (GRT_FIX_COLS) and
+ * force at the receiver.  A corrected layout (GRT_FIX_COLS or GRT_FIX_COLS20) and
  * GRT_FIX_SHSRC are needed for that; with the reference's columns R of Mzz
  * and h, and the SH parts, keep the reference's errors.
  * The source-time function s_n (at opts.dt) enters as dt sum_n s_n e^{-i (w - i sigma) n dt},

@@ -100,3 +100,26 @@ def test_gpu_corrected_columns_match_oracle(src):
         t_ref = np.transpose(t_o, (0, 2, 1))[:, :ncol]
         err = np.linalg.norm(t - t_ref, axis=-1) / np.linalg.norm(t_ref, axis=-1).max(axis=-1, keepdims=True)
         assert err.max() <= tol, (prec, err.max())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("hr", [0.0, 3.0])
+def test_gpu_corrected_20_column_layout_on_the_tensor_cores(hr):
+    """GRT_FIX_COLS20: the corrected moment-tensor columns in the 20-column
+    layout the tensor-core sum takes.  Its columns 0-9 and 10-19 are the
+    oracle's corrected displacement (0-9) and d/dr (20-29) columns, with the
+    SH source terms corrected too; FP32 runs on the tensor cores (3xTF32),
+    FP64 on the SIMT sum."""
+    import grtm_cuda_gb300 as g
+    m = dict(_model(), hr=hr, src_type=1)
+    d = np.array([15.0, 40.0, 90.0])
+    _, t_o = _spec(1, hr, d, fix=FIXC | O.FIX_SHSRC, log2n=8, nk=1536)
+    t_ref = np.transpose(t_o, (0, 2, 1))
+    t_ref = np.concatenate([t_ref[:, :10], t_ref[:, 20:30]], axis=1)
+    for prec, tol, impl in ((g.FP64, 1e-10, 0), (g.FP32, 5e-5, 1)):
+        o = g.make_opts(0.2, 8, sigma_factor=math.pi, k_mode=g.K_FIXED, nk_fixed=1536, precision=prec,
+                        fix=g.FIX_PHYSICAL_TC)
+        t, _, rep = g.run(g.make_model(**m), o, d)
+        assert rep["n_cols"] == 20 and rep["ksum_impl"] == impl
+        err = np.linalg.norm(t - t_ref, axis=-1) / np.linalg.norm(t_ref, axis=-1).max(axis=-1, keepdims=True)
+        assert err.max() <= tol, (prec, err.max())
