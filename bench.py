@@ -437,6 +437,14 @@ def bench_batch(args, ws, rank, local, td):
                 kernel="grt_batch_kernel (fast arm)",
                 peak_source="cuBLAS FP32 SGEMM (TF32 off) measured in this run; MEASURED_PEAKS.json has no "
                             "FP32 CUDA-core figure")
+    # executed work: the layers the kernel evaluated (depth truncation starts the
+    # recursion above the half-space where the S wave is evanescent), counted by the kernel
+    pts = last["nkw_learned"]
+    ex_flops = last["n_layer_evals"] * F_LAYER + pts * F_SRC_TENSOR
+    ex = ex_flops / (last["ms_batch_grt"] * 1e-3) / 1e12
+    roof["executed"] = {"layers_evaluated": last["n_layer_evals"],
+                        "layers_of_formula": float(sum(n * frac_pts * L for n, L in nk_plain_by_model)),
+                        "flops": ex_flops, "achieved": ex, "frac": ex / fp32_peak if fp32_peak else None}
     out = {
         "metric": metric, "value": value, "unit": "traces/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * t_dev, "higher_is_better": True, "scaling": "weak",

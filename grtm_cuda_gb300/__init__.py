@@ -56,7 +56,8 @@ class Report(ctypes.Structure):
                 ("sigma", ctypes.c_double), ("ms_grt", ctypes.c_float), ("ms_bessel", ctypes.c_float),
                 ("ms_ksum", ctypes.c_float), ("ms_spectral", ctypes.c_float), ("ms_total", ctypes.c_float),
                 ("kernel_launches", ctypes.c_int), ("h2d_bytes", ctypes.c_longlong),
-                ("d2h_bytes", ctypes.c_longlong), ("ksum_impl", ctypes.c_int), ("k_slice", ctypes.c_int)]
+                ("d2h_bytes", ctypes.c_longlong), ("ksum_impl", ctypes.c_int), ("k_slice", ctypes.c_int),
+                ("n_layer_evals", ctypes.c_longlong)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -62,6 +62,8 @@ struct grt_plan {
     unsigned *derr = nullptr;
     bool own_derr = true;                     // false inside a batch (the batch's error word)
     bool ran = false;                         // executed at least once (traces on the device)
+    unsigned long long *nlev = nullptr;       // kNlevSlots counters of layers the GRT kernel evaluated
+    bool own_nlev = true;                     // false inside a batch (the batch's counters)
     grt_report rep{};
 };
 
@@ -210,7 +212,7 @@ extern "C" void grt_plan_destroy(grt_plan *p)
     cudaSetDevice(p->ctx->device);
     void *bufs[] = {p->tab, p->K, p->B, p->S, p->post, p->tw, p->spec, p->sig, p->tiles, p->nk, p->koff, p->ddist,
                     p->damp, p->own_derr ? p->derr : nullptr, p->P, p->Kt, p->kt_base, p->ks, p->tfirst,
-                    p->Ag, p->Bg, p->Dg};
+                    p->Ag, p->Bg, p->Dg, p->own_nlev ? p->nlev : nullptr};
     for (void *b : bufs) dev_free(p->ctx, b);
     delete p;
 }
@@ -358,6 +360,7 @@ static int upload(grt_plan *p)
     if (!sel) CU(dev_alloc(ctx, &p->sig, ntr * J.N * sizeof(R)));
     CU(dev_alloc(ctx, &p->spec, ntr * (sel ? J.nw : J.N) * 2 * sizeof(R)));
     CU(dev_alloc(ctx, &p->derr, sizeof(unsigned)));
+    CU(dev_alloc(ctx, &p->nlev, grt::kNlevSlots * sizeof(unsigned long long)));
     if (p->use_tc) {
         // split the k range so that the CTA count (both column groups) fills whole
         // waves of the SMs (one CTA per SM)
@@ -579,6 +582,7 @@ static grt::GrtArgs<R> grt_args(const grt_plan *p)
     A.L = J.L; A.s = J.s; A.rl = J.rl; A.src = J.src; A.fix = J.fix; A.nq = p->nq;
     for (int i = 0; i < 4; i++) A.slot0[i] = (R)p->slot0[i];
     A.err = p->derr;
+    A.nlev = p->nlev;
     A.Kt = p->use_tc ? p->Kt : nullptr;
     A.kt_base = p->kt_base;
     A.nqt = tc_tiles(p->cols);
@@ -752,6 +756,18 @@ static int check_device_error(grt_ctx *ctx, const unsigned *derr)
     return GRT_OK;
 }
 
+// the layers the GRT kernel evaluated, summed over its counters
+static cudaError_t read_nlev(const unsigned long long *d, long long *out)
+{
+    unsigned long long h[grt::kNlevSlots];
+    cudaError_t e = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return e;
+    unsigned long long t = 0;
+    for (unsigned long long v : h) t += v;
+    *out = (long long)t;
+    return cudaSuccess;
+}
+
 template <typename R>
 static int execute(grt_plan *p)
 {
@@ -762,6 +778,7 @@ static int execute(grt_plan *p)
     // 1. per-(w,k) GRT kernel
     const grt::GrtArgs<R> A = grt_args<R>(p);
     const size_t smem = (size_t)J.L * sizeof(grt::LayerW<R>);
+    CU(cudaMemsetAsync(p->nlev, 0, grt::kNlevSlots * sizeof(unsigned long long), st));
     CU(cudaEventRecord(ctx->ev[0], st));
     bool launched = false;
     if constexpr (std::is_same<R, float>::value) {
@@ -791,6 +808,7 @@ static int execute(grt_plan *p)
     p->rep.ms_spectral = t[3];
     p->rep.ms_total = t[0] + t[1] + t[2] + t[3];
     p->rep.kernel_launches = launches;
+    CU(read_nlev(p->nlev, &p->rep.n_layer_evals));
     return GRT_OK;
 }
 
@@ -1473,6 +1491,7 @@ struct grt_batch {
     int ntiles[3] = {};
     long long points = 0;
     unsigned *derr = nullptr;
+    unsigned long long *nlev = nullptr;  // counters of layers the GRT launch evaluated
     cudaStream_t side[kSide] = {};
     cudaStream_t copy = nullptr;     // trace downloads started by grt_batch_fetch_f32_async
     std::vector<float *> outs;       // per job: page-locked destination the graph downloads into (or null)
@@ -1501,6 +1520,7 @@ extern "C" void grt_batch_destroy(grt_batch *b)
     dev_free(b->ctx, b->d_rows);
     for (auto *t : b->d_tiles) dev_free(b->ctx, t);
     dev_free(b->ctx, b->derr);
+    dev_free(b->ctx, b->nlev);
     for (auto &s : b->side)
         if (s) cudaStreamDestroy(s);
     cudaEvent_t evs[] = {b->ev_start, b->ev_grt, b->ev_end, b->fork0, b->fork1};
@@ -1666,6 +1686,7 @@ static int batch_record(grt_batch *b, cudaStream_t st)
     const int sh = b->tune.grt_shape;
     // timing events are recorded as graph nodes (external), the fork/join
     // events only order the streams
+    CU(cudaMemsetAsync(b->nlev, 0, grt::kNlevSlots * sizeof(unsigned long long), st));
     CU(record_timing(b->ev_start, st));
     CU(cudaEventRecord(b->fork0, st));
     for (int s = 0; s < kSide; s++) CU(cudaStreamWaitEvent(b->side[s], b->fork0, 0));
@@ -1733,6 +1754,9 @@ static int batch_build(grt_batch *b, int autotune)
         if (p->own_derr) dev_free(ctx, p->derr);
         p->derr = b->derr;
         p->own_derr = false;
+        if (p->own_nlev) dev_free(ctx, p->nlev);
+        p->nlev = b->nlev;
+        p->own_nlev = false;
         args.push_back(grt_args<R>(p));
     }
     CU(dev_alloc(ctx, &b->d_args, args.size() * sizeof(args[0])));
@@ -1831,6 +1855,7 @@ extern "C" int grt_batch_create(grt_ctx *ctx, int n_jobs, const grt_job *jobs, i
     CU(cudaDeviceGetAttribute(&b->nsm, cudaDevAttrMultiProcessorCount, ctx->device));
     CU(dev_alloc(ctx, &b->derr, sizeof(unsigned)));
     CU(cudaMemset(b->derr, 0, sizeof(unsigned)));
+    CU(dev_alloc(ctx, &b->nlev, grt::kNlevSlots * sizeof(unsigned long long)));
     for (auto &s : b->side) CU(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     CU(cudaStreamCreateWithFlags(&b->copy, cudaStreamNonBlocking));
     b->done.assign(b->jobs.size(), nullptr);
@@ -1862,6 +1887,7 @@ extern "C" int grt_batch_execute(grt_batch *b, grt_report *r)
     CU(cudaEventElapsedTime(&t_all, b->ev_start, b->ev_end));
     b->rep.ms_grt = t_grt;
     b->rep.ms_total = t_all;
+    CU(read_nlev(b->nlev, &b->rep.n_layer_evals));
     b->rep.ms_bessel = b->rep.ms_ksum = b->rep.ms_spectral = 0.f;
     long long nwk = 0, h2d = 0, d2h = 0;
     int ncol = 0;

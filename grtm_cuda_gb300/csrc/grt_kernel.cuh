@@ -345,8 +345,10 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigne
 // Its code is a third shorter (the other receiver cases and source kinds
 // compiled out), which the instruction cache repays: a 40-layer job's GRT
 // went from 174 to 159 ms.
+// Returns the layers it evaluated: every layer without depth truncation (the
+// roofline's L), fewer where the recursion starts above the half-space.
 template <typename R, int SPEC>
-__device__ __forceinline__ void grt_point(const GrtArgs<R> &A, const LayerW<R> *T, int iw, int j)
+__device__ __forceinline__ int grt_point(const GrtArgs<R> &A, const LayerW<R> *T, int iw, int j)
 {
     const int L = A.L, s = A.s, rl = A.rl;
     constexpr bool kAboveTensor = SPEC == kSpecAboveTensor;
@@ -673,6 +675,16 @@ __device__ __forceinline__ void grt_point(const GrtArgs<R> &A, const LayerW<R> *
             store_q<kTensor>(A, QT_N + QT_A21, out, v1);
         }
     }
+    return jlow + 2;
+}
+
+// add the layers the calling lanes evaluated to one of the kNlevSlots counters
+__device__ __forceinline__ void count_levals(unsigned long long *c, int v)
+{
+    if (!c) return;
+    const unsigned m = __activemask();
+    const unsigned sum = __reduce_add_sync(m, (unsigned)v);
+    if ((int)(threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(c + (blockIdx.x % kNlevSlots), (unsigned long long)sum);
 }
 
 #ifndef GRT_POINT_MINB
@@ -742,7 +754,7 @@ __global__ void __launch_bounds__(kGrtThreads, GRT_POINT_MINB) grt_point_kernel(
     // for the table copy it issued): evaluating them would hold their warps
     if (j >= A.nk[iw]) return;
     if (!mbar_wait(sbar, 0, A.err)) return;
-    grt_point<R, SPEC>(A, T, iw, j);
+    count_levals(A.nlev, grt_point<R, SPEC>(A, T, iw, j));
 }
 
 // Many jobs in one launch.  tiles[t] = (job, frequency, first wavenumber
@@ -781,7 +793,7 @@ __global__ void __launch_bounds__(NT, 1) grt_batch_kernel(const GrtArgs<R> *__re
         const int j = tl.z + threadIdx.x;
         if (j >= sA.nk[tl.y]) return;              // lane 0 is valid: it waits for its copy
         if (!mbar_wait(sbar, 0, err)) return;
-        grt_point<R, SPEC>(sA, T, tl.y, j);
+        count_levals(sA.nlev, grt_point<R, SPEC>(sA, T, tl.y, j));
         return;
     }
     __syncthreads();
@@ -803,7 +815,7 @@ __global__ void __launch_bounds__(NT, 1) grt_batch_kernel(const GrtArgs<R> *__re
             cur_iw = tl.y;
         }
         const int j = tl.z + threadIdx.x;
-        if (j < sA.nk[tl.y]) grt_point<R, SPEC>(sA, T, tl.y, j);
+        if (j < sA.nk[tl.y]) count_levals(sA.nlev, grt_point<R, SPEC>(sA, T, tl.y, j));
     }
 }
 

@@ -6,6 +6,7 @@ namespace grt {
 
 constexpr int kMaxLayers = 256;     // after source-interface insertion
 constexpr int kGrtThreads = 128;    // one (w,k) point per thread, 128 k per tile
+constexpr int kNlevSlots = 64;      // counters of layers evaluated, spread to keep their atomics apart
 
 // Per (frequency, layer) record, built on the host in FP64 once per
 // frequency (the reference rebuilds these per (w,k): set_pars, green.cu:164-195).
@@ -60,6 +61,7 @@ struct GrtArgs {
     int L, s, rl, src, fix, nq;
     R slot0[4];                // nu_alpha, nu_beta of layer rl at (w = -i sigma, k = 0)
     unsigned int *err;         // device error word (bounded waits that gave up)
+    unsigned long long *nlev;  // kNlevSlots counters of layers evaluated (depth truncation), or null
     // tensor-core layout of the coefficients (FP32 plans): when Kt is set the
     // kernel writes, instead of K, TF32 hi/lo words straight into the operand
     // tiles of the wavenumber GEMM: block (frequency tile of 64, k stage of 8)

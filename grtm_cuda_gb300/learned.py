@@ -514,6 +514,7 @@ def run_learned_batch(sampler, models, dists_list, ctx=None, plain=PLAIN, spec_t
                     nkw_plain=int(sum(int(g_[3]["nw"]) * plain["nk"] for g_ in grids)),
                     stride_mean=float(np.mean([g_[1].mean() for g_ in grids])), fallback=fallback,
                     n_fallback=n_fb, ms_batch_gpu=rep.ms_total, ms_batch_grt=rep.ms_grt,
+                    n_layer_evals=int(rep.n_layer_evals),
                     gpu_launches=rep.kernel_launches, tune=tune, s_predict=t[1] - t[0], s_build=t[2] - t[1],
                     s_execute=t[3] - t[2], s_fetch=t[3] - t_exec, s_fetch_wait=t[4] - t_wait,
                     s_judge=t_wait - t[3], s_fallback=t[5] - t[4],

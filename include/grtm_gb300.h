@@ -121,6 +121,8 @@ typedef struct grt_report {
     int ksum_impl;        /* wavenumber sum: 0 SIMT FP32/FP64, 1 tensor cores 3xTF32, 2 FP32 SGEMMs (cuBLAS),
                            * 3 tensor cores 3xBF16 */
     int k_slice;          /* tensor-core sum: wavenumbers per split-K slice (0 for the SIMT sum) */
+    long long n_layer_evals;  /* layers the GRT kernel evaluated over all (w,k) points (below n_wk x n_layer
+                               * where depth truncation starts the recursion above the half-space) */
 } grt_report;
 
 typedef struct grt_ctx grt_ctx;
