@@ -741,7 +741,8 @@ def bench_single(args, ws, rank, local, td):
                "spectral": rep["ms_spectral"]}
     dom = max(kernels, key=kernels.get)
     ksum_flops = 2.0 * rep["n_wk"] * len(dists) * 25 * 2   # 25 complex x real pairs per (w,k,receiver)
-    spec_bytes = len(dists) * 20 * (rep["nw"] * 8 + rep["n_samples"] * 4 + rep["n_samples"] * 8)
+    # spectral stage: the k-sums in (8 B per frequency), the traces out (4 B per sample)
+    spec_bytes = len(dists) * 20 * (rep["nw"] * 8 + rep["n_samples"] * 4)
     rl = {
         "grt_point": {"bound": "fp32", "achieved": grt_flops / (rep["ms_grt"] * 1e-3) / 1e12,
                       "peak": fp32_peak, "unit": "TFLOP/s", "traffic": None,

@@ -62,6 +62,7 @@ struct grt_plan {
     unsigned *derr = nullptr;
     bool own_derr = true;                     // false inside a batch (the batch's error word)
     bool ran = false;                         // executed at least once (traces on the device)
+    bool spec_valid = false;                  // full plans: spec holds the last execute's spectra
     unsigned long long *nlev = nullptr;       // kNlevSlots counters of layers the GRT kernel evaluated
     bool own_nlev = true;                     // false inside a batch (the batch's counters)
     grt_report rep{};
@@ -725,7 +726,9 @@ static int launch_spectral(grt_plan *p, cudaStream_t st, int &launches)
     const Job &J = p->J;
     grt::SpecArgs<R> S{};
     S.S = (const R *)p->S; S.post = (const R *)p->post; S.tw = (const R *)p->tw; S.damp = p->damp;
-    S.spec_out = (R *)p->spec; S.sig_out = (R *)p->sig; S.nw = J.nw; S.logn = J.log2n;
+    // the full spectra are filled only when a caller fetches them (ensure_spec)
+    S.spec_out = nullptr; S.sig_out = (R *)p->sig; S.nw = J.nw; S.logn = J.log2n;
+    p->spec_valid = false;
     if (!J.fsel.empty()) {
         // spectra-only plan: phase, taper and scale of each selected frequency
         const long long n = (long long)p->nd * p->nc * J.nw;
@@ -877,10 +880,29 @@ extern "C" int grt_plan_execute(grt_plan *p, grt_report *r)
     return GRT_OK;
 }
 
+// full plans: fill the spectra of the last execute from its k-sums (taper,
+// phase, scale and Hermitian fill), the first time a caller asks for them
+template <typename R>
+static int ensure_spec(grt_plan *p)
+{
+    grt_ctx *ctx = p->ctx;
+    if (!p->J.fsel.empty() || p->spec_valid) return GRT_OK;
+    const long long n = (long long)p->nd * p->nc * p->J.N;
+    grt::spec_fill_kernel<R><<<(unsigned)std::min<long long>((n + 255) / 256, 65535), 256, 0, ctx->stream>>>(
+        (const R *)p->S, (const R *)p->post, (R *)p->spec, (long long)p->nd * p->nc, p->J.nw);
+    CU(cudaGetLastError());
+    p->spec_valid = true;
+    return GRT_OK;
+}
+
 template <typename R>
 static int fetch(grt_plan *p, double *traces, double *spectra)
 {
     grt_ctx *ctx = p->ctx;
+    if (spectra) {
+        int rc = ensure_spec<R>(p);
+        if (rc) return rc;
+    }
     const size_t n = (size_t)p->nd * p->nc * p->J.N;
     std::vector<R> h;
     if (traces) {
@@ -902,6 +924,8 @@ template <typename R>
 static int fetch_freqs(grt_plan *p, int n_freq, const int *freq_idx, double *spectra)
 {
     grt_ctx *ctx = p->ctx;
+    int rc = ensure_spec<R>(p);
+    if (rc) return rc;
     const size_t rows = (size_t)p->nd * p->nc;
     std::vector<grt::C<R>> h(rows * n_freq);
     // one strided copy per frequency: element iw of every (receiver, column) row
@@ -1897,6 +1921,7 @@ extern "C" int grt_batch_execute(grt_batch *b, grt_report *r)
         d2h += p->rep.d2h_bytes;
         ncol = std::max(ncol, p->nc);
         p->ran = true;
+        p->spec_valid = false;
     }
     b->rep.n_wk = nwk;
     b->rep.h2d_bytes = h2d;

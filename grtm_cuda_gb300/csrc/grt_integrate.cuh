@@ -881,13 +881,55 @@ struct SpecArgs {
     int nw, logn;
 };
 
-// in-place radix-2 decimation-in-time inverse DFT (exp(+2 pi i) kernel) of the
-// bit-reversed spectrum in x, then Re(x) e^{sigma t} / N into out
+// In-place radix-2 decimation-in-time inverse DFT (exp(+2 pi i) kernel) of
+// the bit-reversed spectrum in x (the block's shared memory).  Three
+// consecutive stages run fused: a thread takes the 8 elements
+// base + m half (m = 0..7) of one group through stages s, s+1, s+2 in
+// registers -- the same butterflies and twiddles as three separate stages
+// (pairs (m, m+1), then (m, m+2) for m = 0, 1, 4, 5, then (m, m+4)), so one
+// barrier per three stages; the remaining one or two stages run unfused.
 template <typename R>
-__device__ __forceinline__ void ifft_dedamp(C<R> *x, const C<R> *tw, const double *damp, int logn, R *out)
+__device__ __forceinline__ void ifft_inplace(C<R> *x, const C<R> *tw, int logn)
 {
     const int N = 1 << logn;
-    for (int s = 1; s <= logn; s++) {
+    int s = 1;
+    for (; s + 2 <= logn; s += 3) {
+        const int half = 1 << (s - 1);
+        for (int t = threadIdx.x; t < N / 8; t += blockDim.x) {
+            const int pos = t & (half - 1), base = (t >> (s - 1)) * 8 * half + pos;
+            C<R> v[8];
+#pragma unroll
+            for (int m = 0; m < 8; m++) v[m] = x[base + m * half];
+            {
+                const C<R> w = tw[pos * (N >> s)];
+#pragma unroll
+                for (int m = 0; m < 8; m += 2) {
+                    const C<R> u = v[m], q = v[m + 1] * w;
+                    v[m] = u + q;
+                    v[m + 1] = u - q;
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const int m = (i & 1) + (i >> 1) * 4;   // 0, 1, 4, 5
+                const C<R> w = tw[(pos + (m & 1) * half) * (N >> (s + 1))];
+                const C<R> u = v[m], q = v[m + 2] * w;
+                v[m] = u + q;
+                v[m + 2] = u - q;
+            }
+#pragma unroll
+            for (int m = 0; m < 4; m++) {
+                const C<R> w = tw[(pos + m * half) * (N >> (s + 2))];
+                const C<R> u = v[m], q = v[m + 4] * w;
+                v[m] = u + q;
+                v[m + 4] = u - q;
+            }
+#pragma unroll
+            for (int m = 0; m < 8; m++) x[base + m * half] = v[m];
+        }
+        __syncthreads();
+    }
+    for (; s <= logn; s++) {
         const int half = 1 << (s - 1);
         const int tstride = N >> s;
         for (int b = threadIdx.x; b < N / 2; b += blockDim.x) {
@@ -900,6 +942,14 @@ __device__ __forceinline__ void ifft_dedamp(C<R> *x, const C<R> *tw, const doubl
         }
         __syncthreads();
     }
+}
+
+// the inverse DFT above, then Re(x) e^{sigma t} / N into out
+template <typename R>
+__device__ __forceinline__ void ifft_dedamp(C<R> *x, const C<R> *tw, const double *damp, int logn, R *out)
+{
+    ifft_inplace(x, tw, logn);
+    const int N = 1 << logn;
     if (out)
         for (int n = threadIdx.x; n < N; n += blockDim.x) out[n] = (R)((double)x[n].x * damp[n]);
 }
@@ -960,6 +1010,28 @@ __global__ void select_kernel(const R *S, const R *post, R *out, long long n, in
         y[e] = s[e] * q[e % nw];
 }
 
+// The full spectrum of every trace (the reference's `out` after taper and
+// Hermitian fill), written only when a caller fetches spectra: Y[tr][n] =
+// S[tr][n] post[n] for n < nw, 0 at nw, conj(Y[N - n]) above.
+template <typename R>
+__global__ void spec_fill_kernel(const R *S_, const R *post_, R *spec, long long ntr, int nw)
+{
+    const int N = 2 * nw;
+    const C<R> *S = reinterpret_cast<const C<R> *>(S_), *post = reinterpret_cast<const C<R> *>(post_);
+    C<R> *Y = reinterpret_cast<C<R> *>(spec);
+    const long long n_all = ntr * N;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n_all;
+         e += (long long)gridDim.x * blockDim.x) {
+        const long long tr = e / N;
+        const int n = (int)(e % N);
+        C<R> y;
+        if (n < nw) y = S[tr * nw + n] * post[n];
+        else if (n == nw) y = C<R>{R(0), R(0)};
+        else y = conj(S[tr * nw + N - n] * post[N - n]);
+        Y[e] = y;
+    }
+}
+
 template <typename R>
 __global__ void __launch_bounds__(512) spectral_kernel(SpecArgs<R> A)
 {
@@ -981,20 +1053,7 @@ __global__ void __launch_bounds__(512) spectral_kernel(SpecArgs<R> A)
         x[rev] = y;
     }
     __syncthreads();
-    // in-place radix-2 decimation in time, exp(+2 pi i) kernel
-    for (int s = 1; s <= A.logn; s++) {
-        const int half = 1 << (s - 1);
-        const int tstride = N >> s;
-        for (int b = threadIdx.x; b < N / 2; b += blockDim.x) {
-            const int grp = b >> (s - 1), pos = b & (half - 1);
-            const int i0 = grp * (half << 1) + pos, i1 = i0 + half;
-            const C<R> w = tw[pos * tstride];
-            const C<R> u = x[i0], v = x[i1] * w;
-            x[i0] = u + v;
-            x[i1] = u - v;
-        }
-        __syncthreads();
-    }
+    ifft_inplace(x, tw, A.logn);
     if (A.sig_out) {
         for (int n = threadIdx.x; n < N; n += blockDim.x)
             A.sig_out[tr * N + n] = (R)((double)x[n].x * A.damp[n]);
