@@ -168,14 +168,16 @@ class Tune(ctypes.Structure):
                 ("grt_blocks", ctypes.c_int),
                 ("n_cand", ctypes.c_int), ("cand_threads", ctypes.c_int * TUNE_MAX),
                 ("cand_blocks", ctypes.c_int * TUNE_MAX), ("cand_ms", ctypes.c_float * TUNE_MAX),
-                ("sample_fraction", ctypes.c_double)]
+                ("sample_fraction", ctypes.c_double), ("tc_tuned", ctypes.c_int), ("tc_nsplit", ctypes.c_int),
+                ("tc_n_cand", ctypes.c_int), ("tc_cand_split", ctypes.c_int * 4), ("tc_cand_ms", ctypes.c_float * 4)]
 
     def as_dict(self):
         n = self.n_cand
         return {"tuned": self.tuned, "grt_shape": self.grt_shape, "grt_threads": self.grt_threads,
                 "grt_blocks": self.grt_blocks,
                 "candidates": [(self.cand_threads[i], self.cand_blocks[i], self.cand_ms[i]) for i in range(n)],
-                "sample_fraction": self.sample_fraction}
+                "sample_fraction": self.sample_fraction, "tc_tuned": self.tc_tuned, "tc_nsplit": self.tc_nsplit,
+                "tc_candidates": [(self.tc_cand_split[i], self.tc_cand_ms[i]) for i in range(self.tc_n_cand)]}
 
 
 # every symbol the public header declares

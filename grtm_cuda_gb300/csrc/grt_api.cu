@@ -44,6 +44,8 @@ struct grt_plan {
     int nkp = 0, gslices = 1;
     int kslice_req = 0;                       // requested k per slice (0: chosen here)
     int tc_bf16 = 0;                          // tensor-core sum in the 3xBF16 form (else 3xTF32)
+    int nsplit_default = 1;                   // the wave-filling split (before batch tuning)
+    size_t P_bytes = 0;                       // capacity of the split-K partial sums
     int gspec = 0;                            // compiled form of the GRT evaluation (grt::GrtSpec)
     int bt_rows = 0;                          // > 0: Bessel table tiled by 32 receivers (unit strides)
     int cols = 0;                             // output column layout (grt::ColKind)
@@ -311,6 +313,21 @@ static void build_tables(const Job &J, std::vector<grt::LayerW<R>> &tab, std::ve
     for (int n = 0; n < N; n++) damp[n] = std::exp(n * J.dt * J.sigma) * std::exp(J.t0 * J.sigma) / (double)N;
 }
 
+// the tensor-core sum's k split: at most 64 slices of at least 8 stages
+static int tc_max_split(const grt_plan *p)
+{
+    const int KT = p->tc_bf16 ? grt::tc::TcPrec<grt::tc::kBF16>::KT : grt::tc::TcPrec<grt::tc::kTF32>::KT;
+    return std::max(1, std::min(64, p->J.nkmax / (8 * KT)));
+}
+static void set_tc_split(grt_plan *p, int s)
+{
+    const int KT = p->tc_bf16 ? grt::tc::TcPrec<grt::tc::kBF16>::KT : grt::tc::TcPrec<grt::tc::kTF32>::KT;
+    s = std::max(1, std::min(tc_max_split(p), s));
+    p->kslice = ((p->J.nkmax + s - 1) / s + KT - 1) / KT * KT;
+    p->nsplit = (p->J.nkmax + p->kslice - 1) / p->kslice;
+    p->rep.k_slice = p->kslice;
+}
+
 template <typename R>
 static int upload(grt_plan *p)
 {
@@ -371,7 +388,7 @@ static int upload(grt_plan *p)
             2LL * ((J.nw + grt::tc::kW - 1) / grt::tc::kW) * ((p->nd + grt::tc::kN - 1) / grt::tc::kN);
         int best = 1;
         double best_cost = 1e30;
-        const int maxs = std::max(1, std::min(64, J.nkmax / (8 * KT)));
+        const int maxs = tc_max_split(p);
         for (int s = 1; s <= maxs; s++) {
             const long long n = tiles * s;
             const long long waves = (n + nsm - 1) / nsm;
@@ -379,15 +396,16 @@ static int upload(grt_plan *p)
             const double cost = (double)waves * ((double)J.nkmax / s + 64.0) + 2.0 * s;
             if (cost < best_cost) { best_cost = cost; best = s; }
         }
-        p->nsplit = best;
-        p->kslice = ((J.nkmax + best - 1) / best + KT - 1) / KT * KT;
+        p->nsplit_default = best;
+        set_tc_split(p, best);
         if (p->kslice_req > 0) {
             p->kslice = p->kslice_req;
             p->nsplit = (J.nkmax + p->kslice - 1) / p->kslice;
         }
         p->rep.k_slice = p->kslice;
         // partial sums of every (k slice, column group)
-        CU(dev_alloc(ctx, &p->P, (size_t)p->nsplit * 2 * ntr * J.nw * 2 * sizeof(float)));
+        p->P_bytes = (size_t)p->nsplit * 2 * ntr * J.nw * 2 * sizeof(float);
+        CU(dev_alloc(ctx, &p->P, p->P_bytes));
         // operand blocks of (frequency tile of 64, k stage of KT): nq x (hi, lo) x 4 KB each
         const int nwt = (J.nw + grt::tc::kW - 1) / grt::tc::kW;
         std::vector<long long> base(nwt);
@@ -1692,6 +1710,80 @@ static int batch_autotune(grt_batch *b, bool run)
     return check_device_error(ctx, b->derr);
 }
 
+// FP32 batches: the tensor-core sums' k split, timed.  Candidates around the
+// wave-filling default of the largest job (in (w,k) points x receivers); the
+// best one's ratio to the default is applied to every job that did not fix its
+// k_slice, and the context remembers it per deepest model.
+static int tc_ensure_P(grt_plan *p)
+{
+    grt_ctx *ctx = p->ctx;
+    const size_t need = (size_t)p->nsplit * 2 * p->nd * p->nc * p->J.nw * 2 * sizeof(float);
+    if (need <= p->P_bytes) return GRT_OK;
+    dev_free(ctx, p->P);
+    p->P = nullptr;
+    CU(dev_alloc(ctx, &p->P, need));
+    p->P_bytes = need;
+    return GRT_OK;
+}
+
+static int tc_autotune(grt_batch *b, bool run)
+{
+    grt_ctx *ctx = b->ctx;
+    cudaStream_t st = ctx->stream;
+    grt_plan *big = nullptr;
+    for (grt_plan *p : b->jobs)
+        if (p->use_tc && !p->kslice_req &&
+            (!big || (double)p->J.nkw * p->nd > (double)big->J.nkw * big->nd))
+            big = p;
+    b->tune.tc_tuned = 0;
+    b->tune.tc_n_cand = 0;
+    if (!big) return GRT_OK;
+    double ratio = 1.0;
+    auto it = ctx->tuned_tc.find(b->maxL);
+    if (run && it != ctx->tuned_tc.end()) {
+        ratio = it->second;
+        b->tune.tc_tuned = 2;
+    } else if (run) {
+        const int s0 = big->nsplit_default;
+        const int cand[4] = {s0, std::max(1, s0 / 2), std::max(1, (3 * s0 + 2) / 4), s0 * 2};
+        float best = 1e30f;
+        int sbest = s0;
+        std::vector<int> seen;
+        for (int c : cand) {
+            set_tc_split(big, c);
+            if (std::find(seen.begin(), seen.end(), big->nsplit) != seen.end()) continue;
+            seen.push_back(big->nsplit);
+            int rc = tc_ensure_P(big), launches = 0;
+            if (!rc) rc = launch_ksum_tc(big, st, launches);                 // warm-up
+            if (rc) return rc;
+            CU(cudaEventRecord(ctx->ev[0], st));
+            if ((rc = launch_ksum_tc(big, st, launches))) return rc;
+            CU(cudaEventRecord(ctx->ev[1], st));
+            CU(cudaEventSynchronize(ctx->ev[1]));
+            float ms = 0.f;
+            CU(cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]));
+            const int i = b->tune.tc_n_cand++;
+            b->tune.tc_cand_split[i] = big->nsplit;
+            b->tune.tc_cand_ms[i] = ms;
+            if (ms < best) {
+                best = ms;
+                sbest = c;
+            }
+        }
+        ratio = (double)sbest / s0;
+        ctx->tuned_tc[b->maxL] = ratio;
+        b->tune.tc_tuned = 1;
+    }
+    for (grt_plan *p : b->jobs)
+        if (p->use_tc && !p->kslice_req) {
+            set_tc_split(p, (int)std::lround(p->nsplit_default * ratio));
+            int rc = tc_ensure_P(p);
+            if (rc) return rc;
+        }
+    b->tune.tc_nsplit = big->nsplit;
+    return check_device_error(ctx, b->derr);
+}
+
 // a timing event: inside a stream capture it must become a graph node (external)
 static cudaError_t record_timing(cudaEvent_t ev, cudaStream_t st)
 {
@@ -1823,6 +1915,7 @@ static int batch_build(grt_batch *b, int autotune)
     CU(cudaStreamSynchronize(st));
     int rc = batch_autotune<R>(b, autotune != 0);
     if (rc) return rc;
+    if (std::is_same<R, float>::value && (rc = tc_autotune(b, autotune != 0))) return rc;
     // kernel attributes are set before the capture (a captured graph replays
     // every job's launch sizes)
     for (grt_plan *p : b->jobs) {

@@ -13,6 +13,8 @@ struct grt_ctx {
     std::string err;
     // batch launch shapes picked by the autotuner, by (precision, deepest model)
     std::map<std::pair<int, int>, std::pair<int, int>> tuned;
+    // tensor-core k split picked for batches, as a ratio to the wave-filling default, by deepest model
+    std::map<int, double> tuned_tc;
     // device blocks released by plans and batches, kept for reuse (by size),
     // and the blocks handed out from this cache
     std::multimap<size_t, void *> pool;

@@ -235,6 +235,14 @@ typedef struct grt_tune {
     int cand_threads[GRT_TUNE_MAX], cand_blocks[GRT_TUNE_MAX];
     float cand_ms[GRT_TUNE_MAX];   /* their times on the sample */
     double sample_fraction;        /* fraction of the tiles timed */
+    /* the tensor-core wavenumber sums' split of the k range (FP32 batches; jobs without opts.k_slice):
+     * candidate splits of the largest job timed, the best one's ratio to the wave-filling default
+     * applied to every job */
+    int tc_tuned;                  /* 1 timed, 2 reused from an earlier batch of the same kind, 0 default */
+    int tc_nsplit;                 /* the largest job's k slices */
+    int tc_n_cand;
+    int tc_cand_split[4];
+    float tc_cand_ms[4];
 } grt_tune;
 
 typedef struct grt_batch grt_batch;

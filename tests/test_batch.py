@@ -40,7 +40,10 @@ def test_batch_equals_single_jobs(ctx, prec):
         assert np.array_equal(b.fetch_f32(j), first[j].astype(np.float32))
     b.execute()                                        # the graph replays
     for j, (m, o, d) in enumerate(jobs):
-        t1, _, _ = g.run(m, o, d, ctx=ctx)
+        # the single job with the batch's (tuned) tensor-core k split adds in the same order
+        oj = g.with_precision(o, o.precision)
+        oj.k_slice = b.info(j)[0]["k_slice"]
+        t1, _, _ = g.run(m, oj, d, ctx=ctx)
         t2 = b.fetch(j)[0]
         assert np.array_equal(t2, first[j])
         assert np.array_equal(t1, t2)
@@ -49,10 +52,15 @@ def test_batch_equals_single_jobs(ctx, prec):
         assert tune["tuned"] == 1 and len(tune["candidates"]) >= 3
         assert (tune["grt_threads"], tune["grt_blocks"]) in [(c[0], c[1]) for c in tune["candidates"]]
         assert 0 <= tune["grt_shape"] <= 4
+        # the tensor-core k split was timed too, and the largest job runs the fastest candidate
+        assert tune["tc_tuned"] == 1 and len(tune["tc_candidates"]) >= 2
+        best = min(tune["tc_candidates"], key=lambda c: c[1])
+        assert tune["tc_nsplit"] == best[0]
         # a second batch of the same kind on this context reuses the shape
         b2 = g.Batch(ctx, jobs, autotune=True)
         _, t2 = b2.info()
         assert t2["tuned"] == 2 and (t2["grt_threads"], t2["grt_blocks"]) == (tune["grt_threads"], tune["grt_blocks"])
+        assert t2["tc_tuned"] == 2 and t2["tc_nsplit"] == tune["tc_nsplit"]
         b2.execute()
         assert np.array_equal(b2.fetch(0)[0], first[0])
         b2.close()
