@@ -38,7 +38,8 @@ from . import FIX_ALL, K_FIXED, Context, GrtError, Plan, grid, lib, make_model, 
 HERE = os.path.dirname(os.path.abspath(__file__))
 WEIGHTS = os.path.join(HERE, "data", "ksampler.bin")
 N_FEAT, N_IN, N_OUT = 12, 15, 2
-MAGIC = b"GRTKSMP1"
+MAGIC = b"GRTKSMP1"      # one k margin for every frequency
+MAGIC2 = b"GRTKSMP2"     # k margins per band of log w
 
 # the plain grid the sampler is trained against and judged by.  Synthetic
 # models run with the reference's receiver-layer and d/dz quirks corrected
@@ -233,23 +234,50 @@ def sweep_dataset(ctx, seeds, n_freq=8, n_band=8, tol=1e-4, plain=PLAIN, rng_see
 # ---------------------------------------------------------------- the sampler
 class Sampler:
     """Trained network parameters with their input/output standardisation
-    and the safety margins measured on held-out sweeps."""
+    and the safety margins measured on held-out sweeps.
 
-    def __init__(self, params, x_mean, x_std, y_mean, y_std, margin_k=1.25, margin_d=1.0, tol=1e-4):
+    The k_max margin is either one factor (margin_k) or, when kbands is set,
+    a factor per band of log w: kbands = (edges [nb + 1], margins [nb]),
+    frequencies below the first edge or above the last take the end bands.
+    The network's relative error differs with frequency (at low frequencies
+    k_max is a few grid steps and its log is coarse); one margin sized by the
+    worst band lifts every high frequency to the top of the plain grid."""
+
+    def __init__(self, params, x_mean, x_std, y_mean, y_std, margin_k=1.25, margin_d=1.0, tol=1e-4, kbands=None):
         self.params = np.ascontiguousarray(params, dtype=np.float32)
         self.x_mean, self.x_std = np.asarray(x_mean, np.float64), np.asarray(x_std, np.float64)
         self.y_mean, self.y_std = np.asarray(y_mean, np.float64), np.asarray(y_std, np.float64)
         self.margin_k, self.margin_d, self.tol = float(margin_k), float(margin_d), float(tol)
+        self.kbands = None
+        if kbands is not None:
+            e, mg = (np.asarray(a, np.float64) for a in kbands)
+            if e.ndim != 1 or mg.shape != (e.size - 1,) or e.size < 2 or np.any(np.diff(e) <= 0):
+                raise ValueError("kbands: edges [nb + 1] ascending and margins [nb]")
+            self.kbands = (e, mg)
         self._net = None
 
+    def k_margin(self, log_w):
+        """The k_max margin at log angular frequencies log_w."""
+        log_w = np.asarray(log_w, np.float64)
+        if self.kbands is None:
+            return np.full(log_w.shape, self.margin_k)
+        e, mg = self.kbands
+        return mg[np.clip(np.searchsorted(e, log_w, side="right") - 1, 0, mg.size - 1)]
+
     # tiny binary file: magic, n_in, n_out, n_params (int32), margins and tol
-    # (float64), then standardisation (float64) and parameters (float32)
+    # (float64), [MAGIC2: the band count (int32), edges and margins (float64)],
+    # then standardisation (float64) and parameters (float32)
     def save(self, path):
         os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
         with open(path, "wb") as f:
-            f.write(MAGIC)
+            f.write(MAGIC if self.kbands is None else MAGIC2)
             f.write(struct.pack("<3i", N_IN, N_OUT, self.params.size))
             f.write(struct.pack("<3d", self.margin_k, self.margin_d, self.tol))
+            if self.kbands is not None:
+                e, mg = self.kbands
+                f.write(struct.pack("<i", mg.size))
+                f.write(np.asarray(e, "<f8").tobytes())
+                f.write(np.asarray(mg, "<f8").tobytes())
             for a in (self.x_mean, self.x_std, self.y_mean, self.y_std):
                 f.write(np.asarray(a, "<f8").tobytes())
             f.write(self.params.astype("<f4").tobytes())
@@ -258,13 +286,24 @@ class Sampler:
     def load(cls, path=WEIGHTS):
         with open(path, "rb") as f:
             b = f.read()
-        if b[:8] != MAGIC:
+        if b[:8] not in (MAGIC, MAGIC2):
             raise ValueError(f"{path}: not a sampler file")
         n_in, n_out, n_p = struct.unpack_from("<3i", b, 8)
         if (n_in, n_out) != (N_IN, N_OUT):
             raise ValueError(f"{path}: network {n_in}->{n_out}, expected {N_IN}->{N_OUT}")
         mk, md, tol = struct.unpack_from("<3d", b, 20)
         o = 44
+        kb = None
+        if b[:8] == MAGIC2:
+            nb, = struct.unpack_from("<i", b, o)
+            o += 4
+            if not 0 < nb < 1024:
+                raise ValueError(f"{path}: bad band count {nb}")
+            e = np.frombuffer(b, "<f8", nb + 1, o).copy()
+            o += 8 * (nb + 1)
+            mg = np.frombuffer(b, "<f8", nb, o).copy()
+            o += 8 * nb
+            kb = (e, mg)
         arrs = []
         for n in (n_in, n_in, n_out, n_out):
             arrs.append(np.frombuffer(b, "<f8", n, o).copy())
@@ -272,7 +311,7 @@ class Sampler:
         p = np.frombuffer(b, "<f4", n_p, o).copy()
         if o + 4 * n_p != len(b):
             raise ValueError(f"{path}: size mismatch")
-        return cls(p, *arrs, margin_k=mk, margin_d=md, tol=tol)
+        return cls(p, *arrs, margin_k=mk, margin_d=md, tol=tol, kbands=kb)
 
     def net(self, ctx):
         if self._net is None or self._net.ctx is not ctx:
@@ -305,15 +344,28 @@ class Sampler:
         net.close()
         return s, hist
 
-    def calibrate(self, ctx, X, Y, q_k=0.995, q_d=0.95):
+    def calibrate(self, ctx, X, Y, q_k=0.995, q_d=0.95, n_bands=0, min_per_band=256):
         """Margins from held-out sweeps: k_max is scaled by the q_k-quantile of
         the under-prediction ratio; the step multiple is lowered by the
-        q_d-quantile of its over-prediction (the judge catches the rest)."""
+        q_d-quantile of its over-prediction (the judge catches the rest).
+        n_bands > 0: one k margin per band of log w, the bands holding equal
+        numbers of sweeps (at least min_per_band each), the outer edges open."""
         y = self.predict(ctx, X)
         under_k = np.exp(Y[:, 0] - y[:, 0])            # > 1 where the net predicts too small
         self.margin_k = float(max(1.0, np.quantile(under_k, q_k)))
         over_d = 2.0 ** (y[:, 1] - Y[:, 1])            # > 1 where the net predicts too coarse
         self.margin_d = float(max(1.0, np.quantile(over_d, q_d)))
+        self.kbands = None
+        nb = min(int(n_bands), len(X) // max(1, int(min_per_band)))
+        if nb >= 2:
+            lw = X[:, 12]
+            e = np.quantile(lw, np.linspace(0.0, 1.0, nb + 1))
+            e[0], e[-1] = lw.min() - 1.0, lw.max() + 1.0
+            e = np.unique(e)
+            band = np.clip(np.searchsorted(e, lw, side="right") - 1, 0, e.size - 2)
+            mg = np.array([max(1.0, np.quantile(under_k[band == i], q_k)) if np.any(band == i) else self.margin_k
+                           for i in range(e.size - 1)])
+            self.kbands = (e, mg)
         return self.margin_k, self.margin_d
 
     # ------------------------------------------------------------ inference
@@ -334,7 +386,7 @@ class Sampler:
         feat = layer_features(m)
         y = self.predict(ctx, np.concatenate([net_inputs(feat, om, d.min(), m["hs"]),
                                               net_inputs(feat, om, d.max(), m["hs"])]))
-        kmax = np.minimum(np.exp(y[:nw, 0]) * self.margin_k, (nk_plain - 1) * dkp)
+        kmax = np.minimum(np.exp(y[:nw, 0]) * self.k_margin(np.log(om)), (nk_plain - 1) * dkp)
         # one octave below the prediction (aliasing errors do not average out over frequencies)
         l2 = np.clip(y[nw:, 1] - math.log2(self.margin_d) - 1.0, 0.0, 5.0) if use_stride else np.zeros(nw)
         nt = (nw + tile - 1) // tile

@@ -3,6 +3,7 @@ grid, and evaluate it on held-out models.
 
     python -m grtm_cuda_gb300.train_sampler --out grtm_cuda_gb300/data/ksampler.bin
     python -m grtm_cuda_gb300.train_sampler --eval --weights ... --eval-models 8
+    python -m grtm_cuda_gb300.train_sampler --recalibrate --weights ... --out ...
 
 Training data: 320 seeded 40-layer crustal models (source depth U(1, 30) km),
 8 frequencies x 8 distances each (20480 sweeps) on the plain grid of
@@ -23,6 +24,30 @@ from .learned import PLAIN, WEIGHTS, Sampler, plain_opts, run_learned, sweep_dat
 TRAIN_SEEDS = range(1000, 1320)
 VAL_SEEDS = range(2000, 2064)
 HELD_OUT_SEEDS = range(3000, 3256)
+CAL_SEEDS = range(5000, 5256)      # further sweeps for the per-band margins
+
+
+def recalibrate(weights, out, n_bands=8, n_cal=256, tol=1e-4, log=sys.stdout, dump=None):
+    """Keep a trained network and measure its k_max margins per band of log w
+    on the validation sweeps and n_cal further models (the bands need more
+    sweeps than one global quantile)."""
+    s = Sampler.load(weights)
+    ctx = Context()
+    t0 = time.perf_counter()
+    Xv, Yv = sweep_dataset(ctx, list(VAL_SEEDS), tol=tol, rng_seed=2)
+    Xc, Yc = sweep_dataset(ctx, list(CAL_SEEDS)[:n_cal], tol=tol, rng_seed=3)
+    X, Y = np.concatenate([Xv, Xc]), np.concatenate([Yv, Yc])
+    t1 = time.perf_counter()
+    if dump:
+        np.savez_compressed(dump, X=X, Y=Y, pred=s.predict(ctx, X))
+    mk, md = s.calibrate(ctx, X, Y, n_bands=n_bands)
+    s.save(out)
+    ctx.close()
+    e, mg = s.kbands if s.kbands is not None else ([], [])
+    res = dict(n_sweeps=len(X), s_sweeps=t1 - t0, margin_k=mk, margin_d=md,
+               band_edges_hz=[float(np.exp(x) / (2 * np.pi)) for x in e], band_margins=[float(x) for x in mg])
+    print(json.dumps(res), file=log)
+    return s, res
 
 
 def train(out, n_models=320, n_val=64, tol=1e-4, log=sys.stdout, dump=None):
@@ -97,8 +122,13 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--dump", default=None, help="also write the sweep dataset (npz)")
     ap.add_argument("--no-stride", action="store_true", help="evaluate with unit k stride")
+    ap.add_argument("--recalibrate", action="store_true",
+                    help="keep the network of --weights, measure per-band k margins, write --out")
+    ap.add_argument("--bands", type=int, default=8, help="recalibrate: bands of log w")
     a = ap.parse_args()
-    if a.eval:
+    if a.recalibrate:
+        recalibrate(a.weights, a.out, n_bands=a.bands, tol=a.tol, dump=a.dump)
+    elif a.eval:
         evaluate(a.weights, a.eval_models, a.receivers, not a.no_fp64, use_stride=not a.no_stride)
     else:
         train(a.out, a.models, tol=a.tol, dump=a.dump)

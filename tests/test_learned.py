@@ -46,7 +46,15 @@ def test_sampler_file_roundtrip(tmp_path):
     r = Sampler.load(path)
     assert np.array_equal(r.params, s.params.astype(np.float32))
     assert np.array_equal(r.x_std, s.x_std) and np.array_equal(r.y_mean, s.y_mean)
-    assert (r.margin_k, r.margin_d, r.tol) == (1.3, 1.5, 2e-4)
+    assert (r.margin_k, r.margin_d, r.tol) == (1.3, 1.5, 2e-4) and r.kbands is None
+    # per-band k margins: edges in log w, the outer bands open
+    s.kbands = (np.array([0.0, 1.0, 2.5]), np.array([2.0, 1.1]))
+    s.save(path)
+    r = Sampler.load(path)
+    assert np.array_equal(r.kbands[0], s.kbands[0]) and np.array_equal(r.kbands[1], s.kbands[1])
+    assert np.array_equal(r.k_margin([-5.0, 0.5, 1.0, 2.0, 9.0]), [2.0, 2.0, 1.1, 1.1, 1.1])
+    with pytest.raises(ValueError):
+        Sampler(s.params, s.x_mean, s.x_std, s.y_mean, s.y_std, kbands=([1.0, 0.0], [1.0]))
     with open(path, "r+b") as f:
         f.write(b"XXXXXXXX")
     with pytest.raises(ValueError):
@@ -71,6 +79,8 @@ def test_committed_weights_load():
     s = learned.Sampler.load()
     assert s.params.size == MO.layout(N_IN, N_OUT)[1]
     assert s.margin_k >= 1.0 and s.margin_d >= 1.0 and 0 < s.tol < 1e-2
+    if s.kbands is not None:
+        assert np.all(s.kbands[1] >= 1.0) and np.all(s.kbands[1] <= s.margin_k * 4)
     # the oracle's forward of the committed network gives finite outputs
     x = np.zeros((4, N_IN))
     y, _ = MO.forward(s.params, x, N_IN, N_OUT)
@@ -272,7 +282,7 @@ def test_learned_judge_falls_back(ctx):
     if not os.path.exists(learned.WEIGHTS):
         pytest.skip("no trained sampler in the tree")
     s = learned.Sampler.load()
-    s.margin_k = 0.2
+    s.margin_k, s.kbands = 0.2, None
     m, d = _learned_case(3011, 4)
     tl, info = learned.run_learned(s, m, d, ctx=ctx)
     assert len(info["fallback"]) == len(d)
