@@ -31,7 +31,8 @@ Other cases: --case crust20 (one 20-layer model, 200 receivers 5-300 km, nt
 4096, nk 16384), --case crust4 (4 layers, 10 receivers) and --case crust40s
 (one 40-layer model, 64 receivers, nt 1024, nk 4096: the small profiling
 case) time the single-model path; --case uneven256 times 256 uneven models
-in batches; --case tile times the tensor-core wavenumber sum alone.
+in batches; --case tile times the tensor-core wavenumber sum alone and
+--case spectral the FP32 spectral stage alone.
 
 Launch: python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 (for N > 1 under torch.distributed.run: every rank runs its own seeded
@@ -300,6 +301,15 @@ def grt_roofline(n_wk_by_layers, ms, fp32_peak):
                           f"{F_SRC_TENSOR:.0f}) flops = {flops:.3e}"}
 
 
+def spectral_roofline(nbytes, ms):
+    """HBM roofline of the spectral stage: algorithmic bytes over its device time."""
+    peak = measured_peaks().get("hbm_gbs")
+    gbs = nbytes / (ms * 1e-3) / 1e9 if ms > 0 else None
+    return {"kernel": "c2r_kernel (FP32 spectral stage)", "bound": "hbm", "bytes": int(nbytes), "ms": ms,
+            "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak if gbs and peak else None,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth)"}
+
+
 def bench_batch(args, ws, rank, local, td):
     kw = dict(dt=0.05, log2n=13, t0=0.0, taper=0.3, sigma_factor=np.pi, nk=32768)
     work = heldout_models(rank, args.models, args.receivers)
@@ -376,6 +386,8 @@ def bench_batch(args, ws, rank, local, td):
     plain_grt_ms = sum(p.report.ms_grt for p in plain_plans)
     tp = [p.fetch(True, False)[0] for p in plain_plans]
     plain_ksum_ms = sum(p.report.ms_ksum for p in plain_plans)
+    plain_spec_ms = sum(p.report.ms_spectral for p in plain_plans)
+    plain_spec_nw = [p.report.nw for p in plain_plans]
     for p in plain_plans:
         p.close()
     t = time.time()
@@ -479,6 +491,10 @@ def bench_batch(args, ws, rank, local, td):
                                         "in the time)"}},
         },
         "speedup_vs_plain": {"device": value / (ntr / (min(plain_ms) * 1e-3)), "e2e": e2e / plain_e2e},
+        # the spectral stage (complex-to-real inverse FFT with phase, taper and de-damping) of the plain
+        # arm's plans: the k-sums in (8 B per frequency), the traces out (4 B per sample)
+        "spectral": spectral_roofline(sum(len(d) * 20 * (nw * 8 + 8192 * 4) for d, nw in zip(dists, plain_spec_nw)),
+                                      plain_spec_ms),
         "wall_s_timed": wall,
         "gpu_launches": int(sum(i["gpu_launches"] for i in infos)),
         "roofline": roof,
@@ -560,7 +576,7 @@ def bench_uneven(args, ws, rank, local, td):
         path, FP64 receivers by model).  The FP64 check of every trace runs
         outside the timed parts."""
         ms, t_est, t_fb = 0.0, 0.0, 0.0
-        e32, ej, routed = [], [], []
+        e32, ej, routed, ests = [], [], [], []
         for c0 in starts:
             c = jobs[c0:c0 + chunk]
             b = g.Batch(ctx, c, autotune=True)
@@ -583,8 +599,9 @@ def bench_uneven(args, ws, rank, local, td):
                         tr[bad] = t_bad
                     ej.append(np.linalg.norm(tr - t64, axis=(1, 2)) / den)
                     routed.append(bad)
+                    ests.append(est)
             b.close()
-        return ms, t_est, t_fb, e32, ej, routed
+        return ms, t_est, t_fb, e32, ej, routed, ests
 
     batched_pass(False)
     clocks = ClockSampler(local)
@@ -596,7 +613,24 @@ def bench_uneven(args, ws, rank, local, td):
     wall = (time.time() - t0) / args.steps
     clk = clocks.stop()
     # the judged pass (once): graph time + estimates + FP64 recomputation
-    ms_j, t_est, t_fb, e_fp32, e_judged, routed = batched_pass(True)
+    ms_j, t_est, t_fb, e_fp32, e_judged, routed, ests = batched_pass(True)
+    # the traces the estimate under-rated most (error over estimate), for the record
+    diag = []
+    for i, (w, a, b_, est) in enumerate(zip(work, e_fp32, e_judged, ests)):
+        for r in range(len(a)):
+            if a[r] > 1e-4:
+                diag.append({"model": i, "n_layer": len(w["model"]["vs"]), "log2n": w["log2n"],
+                             "hs": float(w["model"]["hs"]), "dist": float(w["dists"][r]), "est": float(est[r]),
+                             "err_fp32": float(a[r]), "err_judged": float(b_[r]),
+                             "ratio": float(a[r] / max(est[r], 1e-30))})
+    diag.sort(key=lambda x: -x["ratio"])
+    misses = [x for x in diag if x["err_judged"] > 1e-3]
+    # what other margins would have routed and missed (every trace's estimate and FP32 error)
+    ea, ee = np.concatenate(e_fp32), np.concatenate(ests)
+    margins = {str(sf): {"routed": int(np.sum(sf * ee > 1e-3)),
+                         "missed": int(np.sum((ea > 1e-3) & (sf * ee <= 1e-3)))} for sf in (1, 1.5, 2, 3, 4, 6, 8)}
+    big = ea > 1e-4
+    ratio_q = np.quantile(ea[big] / ee[big], [0.01, 0.1, 0.5, 0.9, 0.99, 1.0]).tolist() if big.any() else []
     # one plan at a time (same arithmetic)
     ms_p = 0.0
     for j in jobs:
@@ -618,7 +652,11 @@ def bench_uneven(args, ws, rank, local, td):
            "config": config,
            "judged": {"graph_ms": ms_j, "s_estimate": t_est, "s_fp64_fallback": t_fb,
                       "traces_routed_to_fp64": n_routed, "models_with_routed_traces": n_models_routed,
-                      "accuracy": err_stats(e_judged)},
+                      "accuracy": err_stats(e_judged), "misses": misses[:20],
+                      "most_underrated": diag[:10],
+                      "error_over_estimate_quantiles": {"q": [0.01, 0.1, 0.5, 0.9, 0.99, 1.0], "value": ratio_q,
+                                                        "traces": int(big.sum()), "of": "traces with FP32 error > 1e-4"},
+                      "by_margin": margins},
            "fp32_only": {"value": ws * ntr / t_b, "ms": 1000 * t_b, "steps": args.steps,
                          "value_at_1e-3": ws * ntr / t_b * float(np.mean(e_fp32 <= 1e-3)),
                          "accuracy": err_stats(e_fp32),
@@ -824,6 +862,42 @@ def bench_tile(args, ws, rank, local, td):
     barrier(td)
 
 
+def bench_spectral(args, ws, rank, local, td):
+    """The FP32 spectral stage alone (its profiling case): one plan of the
+    4-layer crust with 250 receivers (20 columns each: 5000 traces), nt 8192,
+    on a fixed grid of 256 wavenumbers so that the GRT and the wavenumber sum
+    stay small; reports the stage's device time per execute and its HBM rate
+    (k-sums in, traces out: 4096 x 8 + 8192 x 4 bytes per trace)."""
+    import grtm_cuda_gb300 as g
+    from grtm_cuda_gb300 import synth
+    m, _ = synth.crust4_model()
+    d = np.linspace(5.0, 300.0, 250)
+    ctx = g.Context(local)
+    o = g.make_opts(0.05, 13, sigma_factor=np.pi, k_mode=g.K_FIXED, nk_fixed=256, precision=g.FP32, fix=g.FIX_ALL)
+    plan = g.Plan(ctx, g.make_model(**m), o, d)
+    for _ in range(args.warmup):
+        plan.execute()
+    barrier(td)
+    ms = [plan.execute().ms_spectral for _ in range(args.steps)]
+    r = plan.report
+    ntr = len(d) * r.n_cols
+    plan.close()
+    ctx.close()
+    t = float(np.median(ms))
+    roof = spectral_roofline(ntr * (r.nw * 8 + r.n_samples * 4), t)
+    out = {"metric": "spectral stage (complex-to-real inverse FFT, phase, taper, de-damping), HBM GB/s",
+           "value": roof["achieved"], "unit": "GB/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": t, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32", "data": "synthetic (seeded)",
+           "config": {"workload": f"spectral stage: {ntr} traces of nt 8192 (4-layer crust, {len(d)} receivers "
+                                  "5-300 km, 20 columns, fixed grid of 256 wavenumbers)",
+                      "l2": "inputs and outputs larger than L2 (164 MB each)"},
+           "roofline": roof, "gpu_launches": args.steps}
+    if rank == 0:
+        print(json.dumps(out))
+    barrier(td)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -832,12 +906,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--case", default="batch40",
-                    choices=["batch40", "uneven256", "crust20", "crust4", "crust40s", "tile"],
+                    choices=["batch40", "uneven256", "crust20", "crust4", "crust40s", "tile", "spectral"],
                     help="batch40: batch of held-out 40-layer models (the metric's workload); crust20: one "
                          "20-layer model, 200 receivers; crust4: 4 layers, 10 receivers; crust40s: one 40-layer "
                          "model, 64 receivers, nt 1024, nk 4096 (small profiling case); tile: the tensor-core "
                          "wavenumber sum on one 64-frequency tile of batch40's model 0; uneven256: 256 uneven models "
-                         "in batches")
+                         "in batches; spectral: the FP32 spectral stage on 5000 traces of nt 8192")
     ap.add_argument("--models", type=int, default=2, help="batch40: models per batch")
     ap.add_argument("--receivers", type=int, default=1000, help="batch40: receivers per model")
     ap.add_argument("--chunk", type=int, default=32, help="uneven256: models per batch")
@@ -849,6 +923,8 @@ def main():
         bench_batch(args, ws, rank, local, td)
     elif args.case == "tile":
         bench_tile(args, ws, rank, local, td)
+    elif args.case == "spectral":
+        bench_spectral(args, ws, rank, local, td)
     elif args.case == "uneven256":
         if args.models == 2:
             args.models = 256

@@ -20,6 +20,7 @@
 #include "grt_kernel.cuh"
 #include "grt_tables.h"
 #include "grt_ksum_tc.cuh"
+#include "grt_fft.cuh"
 
 using grt::Job;
 using cd = std::complex<double>;
@@ -61,6 +62,8 @@ struct grt_plan {
     int *nk = nullptr, *ks = nullptr;
     long long *koff = nullptr, *tfirst = nullptr;
     double *ddist = nullptr, *damp = nullptr;
+    float *dampf = nullptr;                   // FP32 plans: the de-damping factors in FP32 (c2r_kernel)
+    float *twp = nullptr;                     // FP32 plans: the c2r_kernel's pass twiddles
     unsigned *derr = nullptr;
     bool own_derr = true;                     // false inside a batch (the batch's error word)
     bool ran = false;                         // executed at least once (traces on the device)
@@ -214,7 +217,7 @@ extern "C" void grt_plan_destroy(grt_plan *p)
     if (!p) return;
     cudaSetDevice(p->ctx->device);
     void *bufs[] = {p->tab, p->K, p->B, p->S, p->post, p->tw, p->spec, p->sig, p->tiles, p->nk, p->koff, p->ddist,
-                    p->damp, p->own_derr ? p->derr : nullptr, p->P, p->Kt, p->kt_base, p->ks, p->tfirst,
+                    p->damp, p->dampf, p->twp, p->own_derr ? p->derr : nullptr, p->P, p->Kt, p->kt_base, p->ks, p->tfirst,
                     p->Ag, p->Bg, p->Dg, p->own_nlev ? p->nlev : nullptr};
     for (void *b : bufs) dev_free(p->ctx, b);
     delete p;
@@ -373,6 +376,14 @@ static int upload(grt_plan *p)
     CU(dev_alloc(ctx, &p->post, post.size() * sizeof(R)));
     CU(dev_alloc(ctx, &p->tw, tw.size() * sizeof(R)));
     CU(dev_alloc(ctx, &p->damp, damp.size() * sizeof(double)));
+    std::vector<float> dampf, twp;
+    if (std::is_same<R, float>::value) {
+        dampf.assign(damp.begin(), damp.end());
+        CU(dev_alloc(ctx, &p->dampf, dampf.size() * sizeof(float)));
+        twp.resize(2 * (size_t)std::max(1, grt::fft::pass_twiddle_count(J.log2n - 1)), 0.f);
+        grt::fft::pass_twiddles(J.log2n, twp.data());
+        CU(dev_alloc(ctx, &p->twp, twp.size() * sizeof(float)));
+    }
     // spectra-only plans (a frequency selection) keep [tr][row] spectra and no traces
     const bool sel = !J.fsel.empty();
     if (!sel) CU(dev_alloc(ctx, &p->sig, ntr * J.N * sizeof(R)));
@@ -439,10 +450,14 @@ static int upload(grt_plan *p)
     CU(cudaMemcpyAsync(p->post, post.data(), post.size() * sizeof(R), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(p->tw, tw.data(), tw.size() * sizeof(R), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(p->damp, damp.data(), damp.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (p->dampf)
+        CU(cudaMemcpyAsync(p->dampf, dampf.data(), dampf.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+    if (p->twp) CU(cudaMemcpyAsync(p->twp, twp.data(), twp.size() * sizeof(float), cudaMemcpyHostToDevice, st));
     CU(cudaMemsetAsync(p->derr, 0, sizeof(unsigned), st));
     p->rep.h2d_bytes = (long long)(tab.size() * sizeof(tab[0]) +
                                    J.nw * (2 * sizeof(int) + 2 * sizeof(long long)) + p->nd * sizeof(double) +
-                                   (post.size() + tw.size()) * sizeof(R) + damp.size() * sizeof(double));
+                                   (post.size() + tw.size()) * sizeof(R) + damp.size() * sizeof(double) +
+                                   (dampf.size() + twp.size()) * sizeof(float));
     p->rep.d2h_bytes = (long long)(ntr * (sel ? 2 * J.nw : J.N) * sizeof(R));
     CU(cudaStreamSynchronize(st));
     return GRT_OK;
@@ -473,8 +488,9 @@ extern "C" int grt_plan_create(grt_ctx *ctx, const grt_model *m, const grt_opts 
     p->cols = col_kind(J);
     p->nc = col_count(p->cols);
     p->nq = coef_count(p->cols);
-    const size_t esz = p->prec ? sizeof(grt::C<double>) : sizeof(grt::C<float>);
-    if ((size_t)J.N * esz > 128 * 1024)
+    // FP32: the complex-to-real kernel takes every N the job accepts (up to 2^15);
+    // FP64: the shared-memory FFT holds N complex doubles
+    if (p->prec && (size_t)J.N * sizeof(grt::C<double>) > 128 * 1024)
         return set_err(ctx, GRT_ERR_UNSUPPORTED, "N too large for the shared-memory FFT at this precision");
     if (J.nkmax > (1 << 24)) return set_err(ctx, GRT_ERR_UNSUPPORTED, "too many wavenumbers");
     // receivers per block / k-lanes per receiver of the wavenumber sum
@@ -756,6 +772,15 @@ static int launch_spectral(grt_plan *p, cudaStream_t st, int &launches)
         CU(cudaGetLastError());
         return GRT_OK;
     }
+    if constexpr (std::is_same<R, float>::value) {
+        // FP32: the complex-to-real transform of half length, one CTA per trace
+        grt::fft::C2RArgs F{};
+        F.S = (const float2 *)p->S; F.post = (const float2 *)p->post; F.tw = (const float2 *)p->tw;
+        F.twp = (const float2 *)p->twp; F.damp = p->dampf; F.out = (float *)p->sig;
+        CU(grt::fft::launch_c2r(F, (long long)p->nd * p->nc, J.log2n, st));
+        launches++;
+        return GRT_OK;
+    }
     const size_t smem2 = (size_t)J.N * sizeof(grt::C<R>);
     CU(raise_smem_limit(grt::spectral_kernel<R>, (int)smem2));
     const int threads = std::min(512, std::max(32, J.N / 2));
@@ -1002,8 +1027,10 @@ extern "C" int grt_plan_fetch(grt_plan *p, double *traces, double *spectra)
 // band), interpolated linearly in frequency between spots.
 constexpr int kSpotFreqs = 16;
 
-static int spot_noise(grt_plan *p, const grt::NoiseArgs<float> &A, std::vector<int> &rows, std::vector<double> &eps2)
-// eps2: [spot][class][band]
+static int spot_noise(grt_plan *p, const grt::NoiseArgs<float> &A, std::vector<int> &rows, std::vector<double> &eps2,
+                      const std::vector<int> &reps, std::vector<double> &s64)
+// eps2: [spot][class][band]; s64: the k-sums of the receivers reps (indices
+// into p->dist) at the spot rows in FP64, [rep][col][spot] complex
 {
     grt_ctx *ctx = p->ctx;
     const Job &J = p->J;
@@ -1025,13 +1052,15 @@ static int spot_noise(grt_plan *p, const grt::NoiseArgs<float> &A, std::vector<i
     int rc = grt::job_select(q->J, (int)sel.size(), sel.data(), err);
     if (rc) return set_err(ctx, rc, err);
     q->prec = GRT_FP64;
-    q->nd = 1;
-    q->dist.assign(1, p->dist[0]);
+    q->nd = (int)reps.size();
+    q->dist.clear();
+    for (int r : reps) q->dist.push_back(p->dist[r]);
     q->cols = p->cols;
     q->nc = p->nc;
     q->nq = p->nq;
-    q->rt = 1;
-    q->jt = 128;
+    q->rt = 128;
+    while (q->rt > 1 && q->rt / 2 >= q->nd) q->rt /= 2;
+    q->jt = 128 / q->rt;
     if ((rc = upload<double>(q.get())) || (rc = execute<double>(q.get()))) {
         grt_plan_destroy(q.release());
         return rc;
@@ -1051,6 +1080,9 @@ static int spot_noise(grt_plan *p, const grt::NoiseArgs<float> &A, std::vector<i
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), dout, h.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
+    s64.resize((size_t)q->nd * q->nc * ns * 2);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(s64.data(), q->S, s64.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     dev_free(ctx, drows);
     dev_free(ctx, dout);
@@ -1111,13 +1143,25 @@ static int error_estimate(grt_plan *p, double eps, double *est)
     std::vector<int> srow;
     std::vector<double> seps2;
     const size_t per = (size_t)A.ncls * NB;
+    // receivers checked directly at the spot frequencies: the one nearest (in
+    // log distance) to each band distance
+    std::vector<int> reps;
+    std::vector<double> s64;
+    bool measured = false;
     if (eps > 0 || !std::is_same<R, float>::value) {
         const double e0 = eps > 0 ? eps : GRT_EPS_FP64;
         srow.assign(1, 0);
         seps2.assign(per, e0 * e0);
     } else if constexpr (std::is_same<R, float>::value) {
-        int rc = spot_noise(p, A, srow, seps2);
+        for (int b = 0; b < NB; b++) {
+            int best = 0;
+            for (int r = 1; r < p->nd; r++)
+                if (std::fabs(std::log(p->dist[r] / A.rb[b])) < std::fabs(std::log(p->dist[best] / A.rb[b]))) best = r;
+            if (std::find(reps.begin(), reps.end(), best) == reps.end()) reps.push_back(best);
+        }
+        int rc = spot_noise(p, A, srow, seps2, reps, s64);
         if (rc) return rc;
+        measured = true;
     }
     // eps^2 at a row, interpolated between spot rows (constant beyond them)
     std::vector<double> e2row(per);
@@ -1171,15 +1215,78 @@ static int error_estimate(grt_plan *p, double eps, double *est)
     // the wavenumber sum's own rounding (FP32: 3xTF32 products and TMEM chains, or
     // compensated SIMT / SGEMM slices), a floor under the coefficients' noise
     const double floor = p->prec ? 0.0 : (p->use_tc ? 3e-5 : 3e-6);
-    for (int r = 0; r < p->nd; r++) {
-        const double x = l1 > l0 ? (std::log(p->dist[r]) - l0) / (l1 - l0) * (NB - 1) : 0.0;
-        const int b0 = std::min(NB - 2, std::max(0, (int)x));
-        const double f = std::min(1.0, std::max(0.0, x - b0));
+    // band position of a distance and the modelled variance of receiver r,
+    // summed over frequencies with weights gsum (G) or at one row
+    auto band_at = [&](double d, int &b0, double &f) {
+        const double x = l1 > l0 ? (std::log(d) - l0) / (l1 - l0) * (NB - 1) : 0.0;
+        b0 = std::min(NB - 2, std::max(0, (int)x));
+        f = std::min(1.0, std::max(0.0, x - b0));
+    };
+    auto model_var = [&](double d, const double *g_cls_band) {
+        int b0;
+        double f;
+        band_at(d, b0, f);
         double var = 0.0;
         for (int t = 0; t < CT.nt; t++) {
-            const double g = (1 - f) * G[(size_t)tcls[t] * NB + b0] + f * G[(size_t)tcls[t] * NB + b0 + 1];
-            var += CT.coef[t] * CT.coef[t] * std::pow(p->dist[r], -2.0 * CT.rpow[t]) * g;
+            const double g = (1 - f) * g_cls_band[(size_t)tcls[t] * NB + b0] + f * g_cls_band[(size_t)tcls[t] * NB + b0 + 1];
+            var += CT.coef[t] * CT.coef[t] * std::pow(d, -2.0 * CT.rpow[t]) * g;
         }
+        return var;
+    };
+    // The noise model assumes errors independent from one wavenumber to the
+    // next; where they are not, the actual error of a sum differs from the
+    // model by a factor that depends on the distance.  Measured: the FP32
+    // k-sums of the representative receivers at the spot rows against the FP64
+    // spot plan's, over the model's prediction at the same rows (both weighted
+    // as the trace weighs the rows); the factor of a receiver is interpolated
+    // in log distance between the representatives (ends held), kept within
+    // [0.5, 64].
+    std::vector<double> cfac(reps.size(), 1.0);
+    if (measured && !reps.empty()) {
+        const int ns = (int)srow.size(), nc = p->nc;
+        std::vector<float> s32((size_t)nc * J.nw * 2);
+        std::vector<double> gs(per);
+        for (size_t i = 0; i < reps.size(); i++) {
+            CU(cudaMemcpy(s32.data(), (const float *)p->S + (size_t)reps[i] * nc * J.nw * 2, s32.size() * sizeof(float),
+                          cudaMemcpyDeviceToHost));
+            double act = 0.0, mod = 0.0;
+            for (int si = 0; si < ns; si++) {
+                const int row = srow[si];
+                const int iw = grt::job_freq(J, row);
+                const double st0 = iw > wc ? 0.5 * (1. + std::cos((iw - wc + 1) * PI / (J.nwf - wc + 1))) : 1.0;
+                const double wgt = 2.0 * (st0 * coef) * (st0 * coef);
+                double a = 0.0;
+                for (int c = 0; c < nc; c++) {
+                    const double *z = &s64[(((size_t)i * nc + c) * ns + si) * 2];
+                    const double dr = s32[((size_t)c * J.nw + row) * 2] - z[0];
+                    const double di = s32[((size_t)c * J.nw + row) * 2 + 1] - z[1];
+                    a += dr * dr + di * di;
+                }
+                for (size_t x = 0; x < per; x++) gs[x] = seps2[(size_t)si * per + x] * h[(size_t)row * per + x];
+                act += wgt * a;
+                mod += wgt * model_var(p->dist[reps[i]], gs.data());
+            }
+            if (mod > 0 && act > 0) cfac[i] = std::min(64.0, std::max(0.5, act / mod));
+        }
+    }
+    std::vector<int> order(reps.size());
+    for (size_t i = 0; i < order.size(); i++) order[i] = (int)i;
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return p->dist[reps[a]] < p->dist[reps[b]]; });
+    auto cfac_at = [&](double d) {
+        if (order.empty()) return 1.0;
+        if (d <= p->dist[reps[order.front()]]) return cfac[order.front()];
+        if (d >= p->dist[reps[order.back()]]) return cfac[order.back()];
+        for (size_t i = 1; i < order.size(); i++) {
+            const double d0 = p->dist[reps[order[i - 1]]], d1 = p->dist[reps[order[i]]];
+            if (d <= d1) {
+                const double f = d1 > d0 ? std::log(d / d0) / std::log(d1 / d0) : 1.0;
+                return (1 - f) * cfac[order[i - 1]] + f * cfac[order[i]];
+            }
+        }
+        return cfac[order.back()];
+    };
+    for (int r = 0; r < p->nd; r++) {
+        const double var = model_var(p->dist[r], G.data()) * cfac_at(p->dist[r]);
         est[r] = n2[r] > 0 ? std::sqrt(var * damp2 / n2[r] + floor * floor) : HUGE_VAL;
     }
     return GRT_OK;
@@ -1919,7 +2026,8 @@ static int batch_build(grt_batch *b, int autotune)
     // kernel attributes are set before the capture (a captured graph replays
     // every job's launch sizes)
     for (grt_plan *p : b->jobs) {
-        CU(raise_smem_limit(grt::spectral_kernel<R>, (int)((size_t)p->J.N * sizeof(grt::C<R>))));
+        if (std::is_same<R, float>::value) CU(grt::fft::c2r_prepare(p->J.log2n));
+        else CU(raise_smem_limit(grt::spectral_kernel<R>, (int)((size_t)p->J.N * sizeof(grt::C<R>))));
         if (p->use_tc) {
             CU(raise_tc_limits<grt::kColSingle>(p->tc_bf16));
             CU(raise_tc_limits<grt::kColSingleFix>(p->tc_bf16));
@@ -2189,6 +2297,9 @@ extern "C" int grt_plan_synth(grt_plan *p, const grt_source *src, const double *
     if (!p->J.fsel.empty()) return set_err(ctx, GRT_ERR_UNSUPPORTED, "a frequency-selection plan has spectra only");
     if (src->n_stf < 0 || (src->n_stf > 0 && !src->stf) || src->n_stf > p->J.N)
         return set_err(ctx, GRT_ERR_ARG, "source-time function: 0 <= n_stf <= N samples");
+    // the seismogram kernel holds one trace's N complex values in shared memory
+    if ((size_t)p->J.N * (p->prec ? sizeof(grt::C<double>) : sizeof(grt::C<float>)) > 128 * 1024)
+        return set_err(ctx, GRT_ERR_UNSUPPORTED, "seismograms: N too large for the shared-memory FFT");
     CU(cudaSetDevice(ctx->device));
     return p->prec ? synth<double>(p, src, azimuth, seis) : synth<float>(p, src, azimuth, seis);
 }

@@ -34,6 +34,7 @@
 #include <string>
 
 #include "../../include/grtm_gb300.h"
+#include "grt_fft.cuh"
 #include "grt_integrate.cuh"
 #include "grt_job.h"
 #include "grt_kernel.cuh"
@@ -116,8 +117,9 @@ extern "C" GRT_API int grt_run_noalloc(int device, const grt_model *m, const grt
     const size_t o_koff = off; off = up256(off + (size_t)nw * sizeof(long long));
     const size_t o_dist = off; off = up256(off + (size_t)nd * sizeof(double));
     const size_t o_post = off; off = up256(off + (size_t)nw * 2 * sizeof(float));
-    const size_t o_tw = off; off = up256(off + (size_t)N * sizeof(float));
-    const size_t o_damp = off; off = up256(off + (size_t)N * sizeof(double));
+    // twiddles: e^{2 pi i m/N} (N/2 complex), then the spectral kernel's pass table (< N/2)
+    const size_t o_tw = off; off = up256(off + (size_t)2 * N * sizeof(float));
+    const size_t o_damp = off; off = up256(off + (size_t)N * sizeof(float));
     const size_t staged = off;
     const size_t o_K = off; off = up256(off + (size_t)nq * J.nkw * 2 * sizeof(float));
     const size_t o_B = off; off = up256(off + (size_t)J.nkmax * grt::NBASIS * nd * sizeof(float));
@@ -159,8 +161,10 @@ extern "C" GRT_API int grt_run_noalloc(int device, const grt_model *m, const grt
         tw[2 * k] = (float)std::cos(2 * PI * k / N);
         tw[2 * k + 1] = (float)std::sin(2 * PI * k / N);
     }
-    double *damp = (double *)(h + o_damp);
-    for (int n = 0; n < N; n++) damp[n] = std::exp(n * J.dt * J.sigma) * std::exp(J.t0 * J.sigma) / (double)N;
+    grt::fft::pass_twiddles(J.log2n, tw + N);
+    // the FP32 spectral stage takes the de-damping factors in FP32
+    float *damp = (float *)(h + o_damp);
+    for (int n = 0; n < N; n++) damp[n] = (float)(std::exp(n * J.dt * J.sigma) * std::exp(J.t0 * J.sigma) / (double)N);
     float slot0[4];
     {
         const LW &t0r = tab[J.rl];
@@ -215,19 +219,14 @@ extern "C" GRT_API int grt_run_noalloc(int device, const grt_model *m, const grt
         CUN(cudaGetLastError());
     }
     {
-        grt::SpecArgs<float> S{};
-        S.S = (const float *)(scratch + o_S);
-        S.post = (const float *)(scratch + o_post);
-        S.tw = (const float *)(scratch + o_tw);
-        S.damp = (const double *)(scratch + o_damp);
-        S.spec_out = nullptr;
-        S.sig_out = (float *)(scratch + o_sig);
-        S.nw = nw;
-        S.logn = J.log2n;
-        const size_t smem = (size_t)N * sizeof(grt::C<float>);
-        CUN(cudaFuncSetAttribute(grt::spectral_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        grt::spectral_kernel<float><<<(unsigned)(nd * nc), std::min(512, std::max(32, N / 2)), smem, st>>>(S);
-        CUN(cudaGetLastError());
+        grt::fft::C2RArgs F{};
+        F.S = (const float2 *)(scratch + o_S);
+        F.post = (const float2 *)(scratch + o_post);
+        F.tw = (const float2 *)(scratch + o_tw);
+        F.twp = (const float2 *)(scratch + o_tw) + N / 2;
+        F.damp = (const float *)(scratch + o_damp);
+        F.out = (float *)(scratch + o_sig);
+        CUN(grt::fft::launch_c2r(F, (long long)nd * nc, J.log2n, st));
     }
     CUN(cudaStreamSynchronize(st));
     unsigned herr = 0;

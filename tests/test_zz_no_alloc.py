@@ -68,7 +68,7 @@ def _scratch_bytes(g, m, o, nd):
     L, nw, N, nk = gr["n_layer"], gr["nw"], gr["n_samples"], o.nk_fixed
     nq, nc = (10, 15) if m.src_type == 0 else (8, 20)
     ntiles = nw * ((nk + 127) // 128)
-    sizes = [nw * L * 112, ntiles * 8, nw * 4, nw * 8, nd * 8, nw * 8, N * 4, N * 8,
+    sizes = [nw * L * 112, ntiles * 8, nw * 4, nw * 8, nd * 8, nw * 8, N * 8, N * 4,
              nq * nw * nk * 8, nk * 9 * nd * 4, nd * nc * nw * 8, nd * nc * N * 4, 4]
     return sum(up(x) for x in sizes)
 
