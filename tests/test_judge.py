@@ -46,9 +46,11 @@ def test_estimate_follows_the_fp32_error(case, impl, monkeypatch):
     assert err.max() > 1e-2 and err.min() < 1e-5            # the model spans the range
     big = err > 1e-5
     ratio = err[big] / est[big]
-    assert 0.25 < ratio.min() and ratio.max() < 2.0, (ratio.min(), ratio.max())
-    # the receivers the judge sends to FP64 (est above 1e-3 / 4) include every one beyond 1e-3
-    assert np.all(4 * est[err > 1e-3] > 1e-3)
+    # the estimate may run high (near receivers take their band's measured
+    # factor, set where the sum's own rounding dominates) but rarely low
+    assert 0.1 < ratio.min() and ratio.max() < 2.0, (ratio.min(), ratio.max())
+    # the receivers the judge sends to FP64 include every one beyond 1e-3
+    assert np.all(g.JUDGE_SAFETY * est[err > 1e-3] > 1e-3)
 
 
 def test_judged_run_is_within_tolerance(case):
@@ -57,4 +59,4 @@ def test_judged_run_is_within_tolerance(case):
     err = _rel(t, t64)
     assert err.max() <= 1e-3, err.max()
     assert 0 < len(info["fp64"]) < len(w["dists"])
-    assert set(info["fp64"]) == set(np.nonzero(4 * info["est"] > 1e-3)[0])
+    assert set(info["fp64"]) == set(np.nonzero(g.JUDGE_SAFETY * info["est"] > 1e-3)[0])
