@@ -21,7 +21,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # its parity with the FP64 oracle is unchanged (FP64 code is not affected)
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-fvisibility=hidden", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"]
-SOURCES = ["grt_api.cu", "grt_job.cpp", "grt_noalloc.cu", "grt_mlp.cu"]
+SOURCES = ["grt_api.cu", "grt_grt_f32.cu", "grt_grt_f64.cu", "grt_tc_tf32.cu", "grt_tc_bf16.cu", "grt_job.cpp",
+           "grt_noalloc.cu", "grt_mlp.cu"]
 # extra nvcc flags (e.g. -DGRT_POINT_MINB=4) and an alternative output path,
 # for timing build variants side by side
 EXTRA = os.environ.get("GRT_NVCC_EXTRA", "").split()

@@ -21,6 +21,7 @@
 #include "grt_tables.h"
 #include "grt_ksum_tc.cuh"
 #include "grt_fft.cuh"
+#include "grt_launch.h"
 
 using grt::Job;
 using cd = std::complex<double>;
@@ -64,6 +65,7 @@ struct grt_plan {
     double *ddist = nullptr, *damp = nullptr;
     float *dampf = nullptr;                   // FP32 plans: the de-damping factors in FP32 (c2r_kernel)
     float *twp = nullptr;                     // FP32 plans: the c2r_kernel's pass twiddles
+    float *rdu = nullptr;                     // two-pass GRT evaluation: R^du at the source between the passes
     unsigned *derr = nullptr;
     bool own_derr = true;                     // false inside a batch (the batch's error word)
     bool ran = false;                         // executed at least once (traces on the device)
@@ -217,7 +219,7 @@ extern "C" void grt_plan_destroy(grt_plan *p)
     if (!p) return;
     cudaSetDevice(p->ctx->device);
     void *bufs[] = {p->tab, p->K, p->B, p->S, p->post, p->tw, p->spec, p->sig, p->tiles, p->nk, p->koff, p->ddist,
-                    p->damp, p->dampf, p->twp, p->own_derr ? p->derr : nullptr, p->P, p->Kt, p->kt_base, p->ks, p->tfirst,
+                    p->damp, p->dampf, p->twp, p->rdu, p->own_derr ? p->derr : nullptr, p->P, p->Kt, p->kt_base, p->ks, p->tfirst,
                     p->Ag, p->Bg, p->Dg, p->own_nlev ? p->nlev : nullptr};
     for (void *b : bufs) dev_free(p->ctx, b);
     delete p;
@@ -438,6 +440,10 @@ static int upload(grt_plan *p)
         if (padded) CU(cudaMemsetAsync(p->Kt, 0, (size_t)tot * sizeof(float), ctx->stream));
         CU(cudaStreamSynchronize(ctx->stream));
     }
+    // the specialised FP32 evaluation runs as two passes (bottom-up, then the
+    // rest): kRduPlanes floats per (w,k) between them
+    if (p->gspec == grt::kSpecAboveTensor && std::is_same<R, float>::value)
+        CU(dev_alloc(ctx, &p->rdu, (size_t)grt::kRduPlanes * J.nkw * sizeof(float)));
     cudaStream_t st = ctx->stream;
     CU(cudaMemcpyAsync(p->tab, tab.data(), tab.size() * sizeof(tab[0]), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(p->nk, J.nk.data(), J.nw * sizeof(int), cudaMemcpyHostToDevice, st));
@@ -536,27 +542,6 @@ extern "C" int grt_plan_create(grt_ctx *ctx, const grt_model *m, const grt_opts 
     return GRT_OK;
 }
 
-template <int SRC>
-static cudaError_t raise_tc_limits(int bf16)
-{
-    return bf16 ? raise_smem_limit(grt::ksum_tc_kernel<SRC, grt::tc::kBF16>, grt::tc::smem_bytes<SRC, grt::tc::kBF16>())
-                : raise_smem_limit(grt::ksum_tc_kernel<SRC, grt::tc::kTF32>, grt::tc::smem_bytes<SRC, grt::tc::kTF32>());
-}
-
-// one launch for both column groups: 2 CTAs per (frequency tile, receiver tile, k slice)
-template <int SRC, int PREC>
-static cudaError_t launch_tc_form(const grt::KsumTcArgs<float> &T, unsigned grid, cudaStream_t st)
-{
-    cudaError_t e = raise_smem_limit(grt::ksum_tc_kernel<SRC, PREC>, grt::tc::smem_bytes<SRC, PREC>());
-    if (e != cudaSuccess) return e;
-    grt::ksum_tc_kernel<SRC, PREC><<<2 * grid, grt::tc::kThreads, grt::tc::smem_bytes<SRC, PREC>(), st>>>(T);
-    return cudaGetLastError();
-}
-template <int SRC>
-static cudaError_t launch_tc_groups(const grt::KsumTcArgs<float> &T, unsigned grid, cudaStream_t st, int bf16)
-{
-    return bf16 ? launch_tc_form<SRC, grt::tc::kBF16>(T, grid, st) : launch_tc_form<SRC, grt::tc::kTF32>(T, grid, st);
-}
 
 // tensor-core wavenumber sum (FP32 path): split-K partial sums, then TwoSum reduction
 static int launch_ksum_tc(grt_plan *p, cudaStream_t st, int &launches)
@@ -583,10 +568,8 @@ static int launch_ksum_tc(grt_plan *p, cudaStream_t st, int &launches)
     T.err = p->derr;
     const int nwt = (J.nw + grt::tc::kW - 1) / grt::tc::kW, nrt = (p->nd + grt::tc::kN - 1) / grt::tc::kN;
     const unsigned grid = (unsigned)(nwt * nrt * p->nsplit);
-    if (p->cols == grt::kColSingle) CU(launch_tc_groups<grt::kColSingle>(T, grid, st, p->tc_bf16));
-    else if (p->cols == grt::kColSingleFix) CU(launch_tc_groups<grt::kColSingleFix>(T, grid, st, p->tc_bf16));
-    else if (p->cols == grt::kColTensorFix20) CU(launch_tc_groups<grt::kColTensorFix20>(T, grid, st, p->tc_bf16));
-    else CU(launch_tc_groups<grt::kColTensor>(T, grid, st, p->tc_bf16));
+    // one launch for both column groups (grt_tc_tf32.cu, grt_tc_bf16.cu)
+    CU(grt::ksum_tc_launch(p->cols == grt::kColTensorFix ? grt::kColTensor : p->cols, p->tc_bf16, T, grid, st));
     launches++;
     const long long n = (long long)p->nd * p->nc * J.nw * 2;
     grt::ksum_tc_reduce_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>((const float *)p->P, (float *)p->S, n,
@@ -626,6 +609,7 @@ static grt::GrtArgs<R> grt_args(const grt_plan *p)
         const grt::TcPlan tp = tc_plan(p->cols);
         for (int q = 0; q < 16; q++) A.qslot[q] = (signed char)tp.qslot[q];
     }
+    A.rdu = (R *)p->rdu;
     return A;
 }
 
@@ -826,16 +810,7 @@ static int execute(grt_plan *p)
     const size_t smem = (size_t)J.L * sizeof(grt::LayerW<R>);
     CU(cudaMemsetAsync(p->nlev, 0, grt::kNlevSlots * sizeof(unsigned long long), st));
     CU(cudaEventRecord(ctx->ev[0], st));
-    bool launched = false;
-    if constexpr (std::is_same<R, float>::value) {
-        if (p->gspec == grt::kSpecAboveTensor) {
-            grt::grt_point_kernel<R, grt::kSpecAboveTensor><<<p->ntiles, grt::kGrtThreads, smem, st>>>(A);
-            launched = true;
-        }
-    }
-    if (!launched) grt::grt_point_kernel<R><<<p->ntiles, grt::kGrtThreads, smem, st>>>(A);
-    launches++;
-    CU(cudaGetLastError());
+    CU(grt::grt_point_launch<R>(A, p->gspec, (unsigned)p->ntiles, smem, st, &launches));
     CU(cudaEventRecord(ctx->ev[1], st));
     // 2. Bessel table, 3. wavenumber sum, 4. spectral stage + inverse DFT
     if ((rc = launch_bessel<R>(p, st, launches))) return rc;
@@ -1516,8 +1491,8 @@ extern "C" int grt_sweep_kmax(grt_ctx *ctx, const grt_model *m, const grt_opts *
         for (int i = 0; i < 4; i++) A.slot0[i] = (float)s0[i];
     }
     A.err = (unsigned *)d_err;
-    grt::grt_point_kernel<float><<<(unsigned)tiles.size(), grt::kGrtThreads, (size_t)J.L * sizeof(grt::LayerW<float>), st>>>(A);
-    CU(cudaGetLastError());
+    CU(grt::grt_point_launch<float>(A, grt::kSpecGeneric, (unsigned)tiles.size(), (size_t)J.L * sizeof(grt::LayerW<float>),
+                                    st, nullptr));
     const int nt = n_freq * n_band;
     SweepOut O{};
     O.tol_abs = (const double *)d_tabs;
@@ -1633,7 +1608,7 @@ struct grt_batch {
     grt_ctx *ctx = nullptr;
     std::vector<grt_plan *> jobs;
     int prec = 0, maxL = 0, nsm = 0;
-    int gspec = 0;                   // every job allows the specialised GRT form (grt::GrtSpec)
+    int gspec = 0;                   // every job allows the specialised (two-pass) GRT form (grt::GrtSpec)
     void *d_args = nullptr;          // GrtArgs<R>[n_jobs]
     void *d_rows = nullptr;          // per (job, frequency) row: id, nk, first tile of each width
     int4 *d_tiles[3] = {};           // tile lists for 64 / 128 / 256 threads per block
@@ -1689,65 +1664,31 @@ constexpr Shape kShapes[5] = {{64, false}, {128, false}, {256, false}, {128, tru
 int nt_index(int nt) { return nt == 64 ? 0 : nt == 128 ? 1 : 2; }
 }
 
-template <typename R, int NT, bool P>
-static void launch_batch_kernel(grt_batch *b, int grid, int ntiles, cudaStream_t st)
-{
-    const size_t smem = (size_t)b->maxL * sizeof(grt::LayerW<R>);
-    // one-tile forms of FP32 batches whose jobs all allow it: the specialised evaluation
-    if constexpr (!P && std::is_same<R, float>::value) {
-        if (b->gspec == grt::kSpecAboveTensor) {
-            grt::grt_batch_kernel<R, NT, P, grt::kSpecAboveTensor><<<grid, NT, smem, st>>>(
-                (const grt::GrtArgs<R> *)b->d_args, b->d_tiles[nt_index(NT)], ntiles, b->derr);
-            return;
-        }
-    }
-    grt::grt_batch_kernel<R, NT, P><<<grid, NT, smem, st>>>((const grt::GrtArgs<R> *)b->d_args,
-                                                            b->d_tiles[nt_index(NT)], ntiles, b->derr);
-}
-
+// the GRT launch of a batch in shape `shape` (grt_launch.h; the kernels live
+// in grt_grt_f32.cu / grt_grt_f64.cu); *launches counts the kernels
 template <typename R>
-static int batch_launch_grt(grt_batch *b, int shape, int grid, int ntiles, cudaStream_t st)
+static int batch_launch_grt(grt_batch *b, int shape, int grid, int ntiles, cudaStream_t st, int *launches = nullptr)
 {
     grt_ctx *ctx = b->ctx;
-    switch (shape) {
-    case 0: launch_batch_kernel<R, 64, false>(b, ntiles, ntiles, st); break;
-    case 1: launch_batch_kernel<R, 128, false>(b, ntiles, ntiles, st); break;
-    case 2: launch_batch_kernel<R, 256, false>(b, ntiles, ntiles, st); break;
-    case 3: launch_batch_kernel<R, 128, true>(b, grid, ntiles, st); break;
-    default: launch_batch_kernel<R, 256, true>(b, grid, ntiles, st); break;
-    }
-    CU(cudaGetLastError());
+    const size_t smem = (size_t)b->maxL * sizeof(grt::LayerW<R>);
+    const Shape sh = kShapes[shape < 0 || shape > 4 ? 4 : shape];
+    CU(grt::grt_batch_launch<R>((const grt::GrtArgs<R> *)b->d_args, b->gspec, sh.nt, sh.persist,
+                                b->d_tiles[nt_index(sh.nt)], ntiles, grid, smem, b->derr, st, launches));
     return GRT_OK;
 }
 
 template <typename R>
 static int batch_occupancy(int shape, size_t smem, int *blocks)
 {
-    cudaError_t e = cudaSuccess;
     *blocks = 1;
-    if (shape == 3) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, grt::grt_batch_kernel<R, 128, true>, 128, smem);
-    if (shape == 4) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, grt::grt_batch_kernel<R, 256, true>, 256, smem);
-    if (*blocks < 1) *blocks = 1;
-    return e == cudaSuccess ? GRT_OK : GRT_ERR_CUDA;
+    if (shape != 3 && shape != 4) return GRT_OK;
+    return grt::grt_batch_occupancy<R>(kShapes[shape].nt, smem, blocks) == cudaSuccess ? GRT_OK : GRT_ERR_CUDA;
 }
 
 template <typename R>
 static cudaError_t raise_batch_limits(int smem)
 {
-    cudaError_t e;
-    if ((e = raise_smem_limit(grt::grt_batch_kernel<R, 64, false>, smem)) != cudaSuccess) return e;
-    if ((e = raise_smem_limit(grt::grt_batch_kernel<R, 128, false>, smem)) != cudaSuccess) return e;
-    if ((e = raise_smem_limit(grt::grt_batch_kernel<R, 256, false>, smem)) != cudaSuccess) return e;
-    if ((e = raise_smem_limit(grt::grt_batch_kernel<R, 128, true>, smem)) != cudaSuccess) return e;
-    if constexpr (std::is_same<R, float>::value) {
-        if ((e = raise_smem_limit(grt::grt_batch_kernel<R, 64, false, grt::kSpecAboveTensor>, smem)) != cudaSuccess)
-            return e;
-        if ((e = raise_smem_limit(grt::grt_batch_kernel<R, 128, false, grt::kSpecAboveTensor>, smem)) != cudaSuccess)
-            return e;
-        if ((e = raise_smem_limit(grt::grt_batch_kernel<R, 256, false, grt::kSpecAboveTensor>, smem)) != cudaSuccess)
-            return e;
-    }
-    return raise_smem_limit(grt::grt_batch_kernel<R, 256, true>, smem);
+    return grt::grt_batch_limits<R>(smem);
 }
 
 // Time the candidate shapes on a prefix of the tiles (up to 3e8 points: the
@@ -1916,8 +1857,8 @@ static int batch_record(grt_batch *b, cudaStream_t st)
     // Bessel tables depend on the receivers only: they run beside the GRT launch
     for (size_t j = 0; j < b->jobs.size(); j++)
         if ((rc = launch_bessel<R>(b->jobs[j], b->side[j % kSide], launches))) return rc;
-    if ((rc = batch_launch_grt<R>(b, sh, b->tune.grt_blocks, b->ntiles[nt_index(kShapes[sh].nt)], st))) return rc;
-    launches++;
+    if ((rc = batch_launch_grt<R>(b, sh, b->tune.grt_blocks, b->ntiles[nt_index(kShapes[sh].nt)], st, &launches)))
+        return rc;
     CU(record_timing(b->ev_grt, st));
     CU(cudaEventRecord(b->fork1, st));
     for (int s = 0; s < kSide; s++) CU(cudaStreamWaitEvent(b->side[s], b->fork1, 0));
@@ -2029,10 +1970,10 @@ static int batch_build(grt_batch *b, int autotune)
         if (std::is_same<R, float>::value) CU(grt::fft::c2r_prepare(p->J.log2n));
         else CU(raise_smem_limit(grt::spectral_kernel<R>, (int)((size_t)p->J.N * sizeof(grt::C<R>))));
         if (p->use_tc) {
-            CU(raise_tc_limits<grt::kColSingle>(p->tc_bf16));
-            CU(raise_tc_limits<grt::kColSingleFix>(p->tc_bf16));
-            CU(raise_tc_limits<grt::kColTensorFix20>(p->tc_bf16));
-            CU(raise_tc_limits<grt::kColTensor>(p->tc_bf16));
+            CU(grt::ksum_tc_limits(grt::kColSingle, p->tc_bf16));
+            CU(grt::ksum_tc_limits(grt::kColSingleFix, p->tc_bf16));
+            CU(grt::ksum_tc_limits(grt::kColTensorFix20, p->tc_bf16));
+            CU(grt::ksum_tc_limits(grt::kColTensor, p->tc_bf16));
         }
     }
     CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));

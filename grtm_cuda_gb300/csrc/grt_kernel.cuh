@@ -347,7 +347,12 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigne
 // went from 174 to 159 ms.
 // Returns the layers it evaluated: every layer without depth truncation (the
 // roofline's L), fewer where the recursion starts above the half-space.
-template <typename R, int SPEC>
+// PASS: 0 the whole evaluation; 1 the bottom-up pass alone, which leaves
+// R^du and R^du_0 at the source in A.rdu; 2 the rest, which takes them from
+// there.  Two passes keep one layer loop per kernel: run as one, warps at
+// different depths of the truncated bottom-up loop and of the top-down loop
+// share the instruction cache (instruction-fetch stalls were the top stall).
+template <typename R, int SPEC, int PASS = 0>
 __device__ __forceinline__ int grt_point(const GrtArgs<R> &A, const LayerW<R> *T, int iw, int j)
 {
     const int L = A.L, s = A.s, rl = A.rl;
@@ -364,7 +369,6 @@ __device__ __forceinline__ int grt_point(const GrtArgs<R> &A, const LayerW<R> *T
 
     // ---------------- bottom-up pass: R^du and T^d from the half-space to s+1
     SL<R> D, U;
-    make_layer(T[L - 1], k2, k, D);
     M2<R> Rdu = zero2<R>();
     C<R> rdu0 = zero;
     M2<R> PD = eye2<R>();      // r_layer > s: Td(rl) Lam(rl-1) ... Td(s+1)
@@ -377,6 +381,9 @@ __device__ __forceinline__ int grt_point(const GrtArgs<R> &A, const LayerW<R> *T
     const R zr = (R)A.zr;
     const Zd<R> Zr = zd<R>(A.zr), Zhr = zd<R>(A.hr_layer), Zhr_r = zd<R>(A.hr_layer - A.zr);
 
+    int jlow = L - 2;
+    if constexpr (PASS != 2) {
+    make_layer(T[L - 1], k2, k, D);
     // Depth truncation: below the source (below the receiver when it lies
     // deeper), a wave reflected from beneath the layer where the slower, S,
     // vertical wavenumber has accumulated sum Re(v) h > lim comes back damped
@@ -384,7 +391,6 @@ __device__ __forceinline__ int grt_point(const GrtArgs<R> &A, const LayerW<R> *T
     // 3e-8), 4e-18 with lim = 20 in FP64, under the working precision; the
     // recursion starts there with the layer beneath as the half-space.  At
     // wavenumbers where S is evanescent this skips most of the deep stack.
-    int jlow = L - 2;
     {
         const R lim = sizeof(R) == 4 ? R(9) : R(20);
         const int j0 = below ? rl + 1 : s + 1;
@@ -460,6 +466,24 @@ __device__ __forceinline__ int grt_point(const GrtArgs<R> &A, const LayerW<R> *T
         Utrec = Ed * Ldt;
         u0 = ldv;
         u0t = -(U.v * ldv);
+    }
+    }   // PASS != 2
+    const long long fi = A.koff[iw] + j;   // this point in the flattened (w,k) list
+    if constexpr (PASS == 1) {
+        R *o = A.rdu + fi;
+        const R v[kRduPlanes] = {Rdu.a.x, Rdu.a.y, Rdu.b.x, Rdu.b.y, Rdu.c.x, Rdu.c.y, Rdu.d.x, Rdu.d.y,
+                                 rdu0.x, rdu0.y};
+#pragma unroll
+        for (int c = 0; c < kRduPlanes; c++) o[(long long)c * A.nkw] = v[c];
+        return jlow + 2 - s;
+    }
+    if constexpr (PASS == 2) {
+        const R *o = A.rdu + fi;
+        R v[kRduPlanes];
+#pragma unroll
+        for (int c = 0; c < kRduPlanes; c++) v[c] = o[(long long)c * A.nkw];
+        Rdu = M2<R>{{v[0], v[1]}, {v[2], v[3]}, {v[4], v[5]}, {v[6], v[7]}};
+        rdu0 = C<R>{v[8], v[9]};
     }
     const M2<R> RD = Rdu;      // R^du at the bottom of the source layer
     const C<R> RD0 = rdu0;
@@ -676,7 +700,7 @@ __device__ __forceinline__ int grt_point(const GrtArgs<R> &A, const LayerW<R> *T
             store_q<kTensor>(A, QT_N + QT_A21, out, v1);
         }
     }
-    return jlow + 2;
+    return PASS == 2 ? s : jlow + 2;
 }
 
 // add the layers the calling lanes evaluated to one of the kNlevSlots counters
@@ -734,8 +758,8 @@ static __global__ void batch_tiles_kernel(const int2 *row_id, const int *row_nk,
 }
 
 // One job: one block per (frequency, block of kGrtThreads wavenumbers).
-template <typename R, int SPEC = kSpecGeneric>
-__global__ void __launch_bounds__(kGrtThreads, GRT_POINT_MINB) grt_point_kernel(GrtArgs<R> A)
+template <typename R, int SPEC = kSpecGeneric, int PASS = 0>
+__global__ void __launch_bounds__(kGrtThreads, PASS == 1 ? 512 / kGrtThreads : PASS == 2 ? 384 / kGrtThreads : GRT_POINT_MINB) grt_point_kernel(GrtArgs<R> A)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) unsigned long long bar;
@@ -755,7 +779,7 @@ __global__ void __launch_bounds__(kGrtThreads, GRT_POINT_MINB) grt_point_kernel(
     // for the table copy it issued): evaluating them would hold their warps
     if (j >= A.nk[iw]) return;
     if (!mbar_wait(sbar, 0, A.err)) return;
-    count_levals(A.nlev, grt_point<R, SPEC>(A, T, iw, j));
+    count_levals(A.nlev, grt_point<R, SPEC, PASS>(A, T, iw, j));
 }
 
 // Many jobs in one launch.  tiles[t] = (job, frequency, first wavenumber
@@ -771,8 +795,8 @@ __global__ void __launch_bounds__(kGrtThreads, GRT_POINT_MINB) grt_point_kernel(
 // block per tile, idle lanes leave at once, no barrier after the staging.
 // The autotuner picks the form and shape on the batch.
 constexpr int kRun = 4;
-template <typename R, int NT, bool PERSIST, int SPEC = kSpecGeneric>
-__global__ void __launch_bounds__(NT, 1) grt_batch_kernel(const GrtArgs<R> *__restrict__ jobs,
+template <typename R, int NT, bool PERSIST, int SPEC = kSpecGeneric, int PASS = 0>
+__global__ void __launch_bounds__(NT, PASS == 1 ? 512 / NT : PASS == 2 ? 384 / NT : 1) grt_batch_kernel(const GrtArgs<R> *__restrict__ jobs,
                                                            const int4 *__restrict__ tiles, int ntiles,
                                                            unsigned int *err)
 {
@@ -794,7 +818,7 @@ __global__ void __launch_bounds__(NT, 1) grt_batch_kernel(const GrtArgs<R> *__re
         const int j = tl.z + threadIdx.x;
         if (j >= sA.nk[tl.y]) return;              // lane 0 is valid: it waits for its copy
         if (!mbar_wait(sbar, 0, err)) return;
-        count_levals(sA.nlev, grt_point<R, SPEC>(sA, T, tl.y, j));
+        count_levals(sA.nlev, grt_point<R, SPEC, PASS>(sA, T, tl.y, j));
         return;
     }
     __syncthreads();
@@ -816,7 +840,7 @@ __global__ void __launch_bounds__(NT, 1) grt_batch_kernel(const GrtArgs<R> *__re
             cur_iw = tl.y;
         }
         const int j = tl.z + threadIdx.x;
-        if (j < sA.nk[tl.y]) count_levals(sA.nlev, grt_point<R, SPEC>(sA, T, tl.y, j));
+        if (j < sA.nk[tl.y]) count_levals(sA.nlev, grt_point<R, SPEC, PASS>(sA, T, tl.y, j));
     }
 }
 

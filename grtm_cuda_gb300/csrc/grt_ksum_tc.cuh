@@ -540,7 +540,7 @@ __global__ void __launch_bounds__(tc::kThreads, 1) ksum_tc_kernel(KsumTcArgs<flo
 }
 
 // S[r][c][w] = sum over the partial sums (k slices x groups) with TwoSum
-__global__ void ksum_tc_reduce_kernel(const float *P, float *S, long long n, int nparts)
+static __global__ void ksum_tc_reduce_kernel(const float *P, float *S, long long n, int nparts)
 {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= n) return;

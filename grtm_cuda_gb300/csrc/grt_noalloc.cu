@@ -35,6 +35,7 @@
 
 #include "../../include/grtm_gb300.h"
 #include "grt_fft.cuh"
+#include "grt_launch.h"
 #include "grt_integrate.cuh"
 #include "grt_job.h"
 #include "grt_kernel.cuh"
@@ -193,8 +194,7 @@ extern "C" GRT_API int grt_run_noalloc(int device, const grt_model *m, const grt
     A.L = L; A.s = J.s; A.rl = J.rl; A.src = J.src; A.fix = J.fix; A.nq = nq;
     for (int i = 0; i < 4; i++) A.slot0[i] = slot0[i];
     A.err = (unsigned *)(scratch + o_err);
-    grt::grt_point_kernel<float><<<(unsigned)ntiles, grt::kGrtThreads, (size_t)L * sizeof(LW), st>>>(A);
-    CUN(cudaGetLastError());
+    CUN(grt::grt_point_launch<float>(A, grt::kSpecGeneric, (unsigned)ntiles, (size_t)L * sizeof(LW), st, nullptr));
     {
         long long n = (long long)J.nkmax * nd;
         grt::bessel_table_kernel<float><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(

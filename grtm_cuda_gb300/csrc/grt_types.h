@@ -73,7 +73,12 @@ struct GrtArgs {
     int nqt;
     int kt_bf16;               // tiles in the 3xBF16 form (16 k per stage, bf16 hi/lo words)
     signed char qslot[16];     // tile of coefficient column q in a stage block (-1: not stored)
+    // two-pass evaluation (specialised FP32 form): the bottom-up pass leaves
+    // R^du and its SH term at the source here, [kRduPlanes][nkw], for the
+    // pass that follows (null: one pass)
+    R *rdu;
 };
+constexpr int kRduPlanes = 10;   // R^du (2 x 2 complex) and R^du_0 (complex)
 
 // Bessel basis functions of k r, in the order the integrand formulas use them
 enum Basis { BJ0 = 0, BJ1, BJ2, BJ0D, BJ1D, BJ2D, BJ0DD, BJ1DD, BJ2DD, NBASIS };
