@@ -826,7 +826,8 @@ def bench_tile(args, ws, rank, local, td):
     sel = np.linspace(1, 4095, 64).astype(np.int32)
     ctx = g.Context(local)
     bf16 = args.tc_split == "bf16"
-    plan = g.Plan(ctx, g.make_model(**m), learned.plain_opts(freq_sel=sel, tc_split=g.TC_3XBF16 if bf16 else 0), d)
+    plan = g.Plan(ctx, g.make_model(**m), learned.plain_opts(freq_sel=sel, tc_split=g.TC_3XBF16 if bf16 else 0,
+                                                             k_slice=args.k_slice), d)
     for _ in range(args.warmup):
         plan.execute()
     barrier(td)
@@ -857,6 +858,9 @@ def bench_tile(args, ws, rank, local, td):
                                         "dense TF32 rate of the tensor cores"),
                         "kernel": "ksum_tc_kernel<tensor>", "k_slice": r.k_slice},
            "gpu_launches": 2 * args.steps}
+    n_cta = 2 * ((len(d) + 31) // 32) * ((32768 + r.k_slice - 1) // r.k_slice)
+    out["roofline"]["ctas"] = n_cta
+    out["roofline"]["us_per_stage_per_cta"] = t * 1e6 / (r.k_slice / (16 if bf16 else 8)) / max(1.0, n_cta / 148.0)
     if rank == 0:
         print(json.dumps(out))
     barrier(td)
@@ -917,6 +921,8 @@ def main():
     ap.add_argument("--chunk", type=int, default=32, help="uneven256: models per batch")
     ap.add_argument("--tc-split", default="tf32", choices=["tf32", "bf16"],
                     help="split form of the tensor-core wavenumber sums (tile case)")
+    ap.add_argument("--k-slice", type=int, default=0,
+                    help="tile case: wavenumbers per CTA (0: the default split that fills the GPU)")
     args = ap.parse_args()
     ws, rank, local, td = dist_setup()
     if args.case == "batch40":

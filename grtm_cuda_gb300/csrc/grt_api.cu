@@ -1608,7 +1608,8 @@ struct grt_batch {
     grt_ctx *ctx = nullptr;
     std::vector<grt_plan *> jobs;
     int prec = 0, maxL = 0, nsm = 0;
-    int gspec = 0;                   // every job allows the specialised (two-pass) GRT form (grt::GrtSpec)
+    int nspec[3] = {};               // leading tiles (per block width) of jobs that allow the specialised
+                                     // two-pass GRT form (their rows come first in the tile lists)
     void *d_args = nullptr;          // GrtArgs<R>[n_jobs]
     void *d_rows = nullptr;          // per (job, frequency) row: id, nk, first tile of each width
     int4 *d_tiles[3] = {};           // tile lists for 64 / 128 / 256 threads per block
@@ -1672,8 +1673,9 @@ static int batch_launch_grt(grt_batch *b, int shape, int grid, int ntiles, cudaS
     grt_ctx *ctx = b->ctx;
     const size_t smem = (size_t)b->maxL * sizeof(grt::LayerW<R>);
     const Shape sh = kShapes[shape < 0 || shape > 4 ? 4 : shape];
-    CU(grt::grt_batch_launch<R>((const grt::GrtArgs<R> *)b->d_args, b->gspec, sh.nt, sh.persist,
-                                b->d_tiles[nt_index(sh.nt)], ntiles, grid, smem, b->derr, st, launches));
+    CU(grt::grt_batch_launch<R>((const grt::GrtArgs<R> *)b->d_args, std::min(ntiles, b->nspec[nt_index(sh.nt)]),
+                                sh.nt, sh.persist, b->d_tiles[nt_index(sh.nt)], ntiles, grid, smem, b->derr, st,
+                                launches));
     return GRT_OK;
 }
 
@@ -1925,16 +1927,23 @@ static int batch_build(grt_batch *b, int autotune)
     }
     CU(dev_alloc(ctx, &b->d_args, args.size() * sizeof(args[0])));
     CU(cudaMemcpyAsync(b->d_args, args.data(), args.size() * sizeof(args[0]), cudaMemcpyHostToDevice, st));
-    // tile lists for each block width, written on the device from one offset per (job, frequency)
+    // tile lists for each block width, written on the device from one offset per
+    // (job, frequency): the rows of jobs that allow the specialised two-pass
+    // GRT form first (a prefix the one-tile forms launch as such), then the others
     std::vector<int2> row_id;
     std::vector<int> row_nk;
-    for (size_t j = 0; j < b->jobs.size(); j++) {
-        const Job &J = b->jobs[j]->J;
-        for (int iw = 0; iw < J.nw; iw++) {
-            row_id.push_back(make_int2((int)j, iw));
-            row_nk.push_back(J.nk[iw]);
+    size_t nrow_spec = 0;
+    for (int cls = 0; cls < 2; cls++)
+        for (size_t j = 0; j < b->jobs.size(); j++) {
+            const grt_plan *p = b->jobs[j];
+            if ((p->gspec == grt::kSpecAboveTensor && std::is_same<R, float>::value) != (cls == 0)) continue;
+            const Job &J = p->J;
+            for (int iw = 0; iw < J.nw; iw++) {
+                row_id.push_back(make_int2((int)j, iw));
+                row_nk.push_back(J.nk[iw]);
+            }
+            if (cls == 0) nrow_spec = row_id.size();
         }
-    }
     const size_t nrow = row_id.size();
     CU(dev_alloc(ctx, &b->d_rows, nrow * (sizeof(int2) + sizeof(int) + 3 * sizeof(long long)) + 8));
     int2 *d_id = (int2 *)b->d_rows;
@@ -1946,9 +1955,11 @@ static int batch_build(grt_batch *b, int autotune)
     for (int w = 0; w < 3; w++) {
         long long n = 0;
         for (size_t r = 0; r < nrow; r++) {
+            if (r == nrow_spec) b->nspec[w] = (int)n;
             first[w * nrow + r] = n;
             n += (row_nk[r] + kNtOpts[w] - 1) / kNtOpts[w];
         }
+        if (nrow_spec == nrow) b->nspec[w] = (int)n;
         if (n >= (1LL << 31)) return set_err(ctx, GRT_ERR_UNSUPPORTED, "too many (w,k) tiles for one launch");
         b->ntiles[w] = (int)n;
         CU(dev_alloc(ctx, &b->d_tiles[w], n * sizeof(int4)));
@@ -2015,9 +2026,7 @@ extern "C" int grt_batch_create(grt_ctx *ctx, int n_jobs, const grt_job *jobs, i
         b->points += p->J.nkw;
     }
     b->prec = jobs[0].opts->precision;
-    b->gspec = grt::kSpecAboveTensor;
-    for (grt_plan *p : b->jobs)
-        if (p->gspec != grt::kSpecAboveTensor) b->gspec = grt::kSpecGeneric;
+
     CU(cudaDeviceGetAttribute(&b->nsm, cudaDevAttrMultiProcessorCount, ctx->device));
     CU(dev_alloc(ctx, &b->derr, sizeof(unsigned)));
     CU(cudaMemset(b->derr, 0, sizeof(unsigned)));

@@ -27,18 +27,23 @@ cudaError_t raise_smem(F *kernel, int bytes)
 }
 
 template <typename R, int NT, bool P>
-void batch(const GrtArgs<R> *jobs, int spec, const int4 *tiles, int ntiles, int grid, size_t smem, unsigned *err,
+void batch(const GrtArgs<R> *jobs, int nspec, const int4 *tiles, int ntiles, int grid, size_t smem, unsigned *err,
            cudaStream_t st, int *launches)
 {
-    // one-tile forms of FP32 batches whose jobs all allow it: the specialised
-    // evaluation in two passes (bottom-up, then the rest; GrtArgs::rdu between)
+    // one-tile forms: the leading tiles of jobs that allow the specialised
+    // evaluation in two passes (bottom-up, then the rest; GrtArgs::rdu
+    // between), the remaining tiles in the generic one
     if constexpr (!P && std::is_same<R, float>::value) {
-        if (spec == kSpecAboveTensor) {
-            grt_batch_kernel<R, NT, P, kSpecAboveTensor, 1><<<grid, NT, smem, st>>>(jobs, tiles, ntiles, err);
-            grt_batch_kernel<R, NT, P, kSpecAboveTensor, 2><<<grid, NT, smem, st>>>(jobs, tiles, ntiles, err);
+        if (nspec > 0) {
+            grt_batch_kernel<R, NT, P, kSpecAboveTensor, 1><<<nspec, NT, smem, st>>>(jobs, tiles, nspec, err);
+            grt_batch_kernel<R, NT, P, kSpecAboveTensor, 2><<<nspec, NT, smem, st>>>(jobs, tiles, nspec, err);
             if (launches) *launches += 2;
-            return;
         }
+        if (ntiles > nspec) {
+            grt_batch_kernel<R, NT, P><<<ntiles - nspec, NT, smem, st>>>(jobs, tiles + nspec, ntiles - nspec, err);
+            if (launches) *launches += 1;
+        }
+        return;
     }
     grt_batch_kernel<R, NT, P><<<grid, NT, smem, st>>>(jobs, tiles, ntiles, err);
     if (launches) *launches += 1;
@@ -64,17 +69,19 @@ cudaError_t grt_point_launch(const GrtArgs<R> &A, int spec, unsigned nblocks, si
 }
 
 template <typename R>
-cudaError_t grt_batch_launch(const GrtArgs<R> *jobs, int spec, int nt, bool persist, const int4 *tiles, int ntiles,
+cudaError_t grt_batch_launch(const GrtArgs<R> *jobs, int nspec, int nt, bool persist, const int4 *tiles, int ntiles,
                              int grid, size_t smem, unsigned *err, cudaStream_t st, int *launches)
 {
     using namespace launch_detail;
+    if (ntiles <= 0) return cudaSuccess;
+    nspec = nspec < 0 ? 0 : nspec > ntiles ? ntiles : nspec;
     if (!persist) {
-        if (nt == 64) batch<R, 64, false>(jobs, spec, tiles, ntiles, ntiles, smem, err, st, launches);
-        else if (nt == 128) batch<R, 128, false>(jobs, spec, tiles, ntiles, ntiles, smem, err, st, launches);
-        else batch<R, 256, false>(jobs, spec, tiles, ntiles, ntiles, smem, err, st, launches);
+        if (nt == 64) batch<R, 64, false>(jobs, nspec, tiles, ntiles, ntiles, smem, err, st, launches);
+        else if (nt == 128) batch<R, 128, false>(jobs, nspec, tiles, ntiles, ntiles, smem, err, st, launches);
+        else batch<R, 256, false>(jobs, nspec, tiles, ntiles, ntiles, smem, err, st, launches);
     } else {
-        if (nt == 128) batch<R, 128, true>(jobs, spec, tiles, ntiles, grid, smem, err, st, launches);
-        else batch<R, 256, true>(jobs, spec, tiles, ntiles, grid, smem, err, st, launches);
+        if (nt == 128) batch<R, 128, true>(jobs, nspec, tiles, ntiles, grid, smem, err, st, launches);
+        else batch<R, 256, true>(jobs, nspec, tiles, ntiles, grid, smem, err, st, launches);
     }
     return cudaGetLastError();
 }

@@ -17,8 +17,7 @@
 // (pairs x 32 columns).  Halving the pairs per CTA doubles the receivers an
 // operand tile is multiplied with: shared-memory traffic per multiply-add
 // (operand copies, tensor-core reads, Bessel-operand stores), the limit of the
-// earlier 16-receiver form, falls by 40 %, and a stage shrinks enough for
-// three of them to fit.
+// earlier 16-receiver form, falls by 40 %.
 //
 // Precision: 3xTF32 -- each FP32 operand x is split into hi = tf32(x) and
 // lo = tf32(x - hi) and the product is hi*hi + hi*lo + lo*hi with FP32
@@ -31,12 +30,13 @@
 // accumulators at the end (warps w and w + 4 share a quarter of the
 // tensor-memory lanes and split the output columns); one thread of warp 8
 // issues the bulk copies of the coefficient tiles and raw Bessel rows up to
-// three stages ahead; warp 9 allocates tensor memory and one of its threads
-// issues tcgen05.mma and tcgen05.commit.  Each stage is guarded by "full"
-// (producers), "land" (coefficient copy), "raw" (Bessel copy) and "empty"
-// (MMAs done) mbarriers.  Every wait is bounded: on timeout the CTA records
-// an error, skips to the end, waits (bounded) for its copies in flight and
-// still frees its tensor memory.
+// SA stages ahead (the copy ring, TcRing); warp 9 allocates tensor memory and
+// one of its threads issues tcgen05.mma and tcgen05.commit.  A copy slot is
+// guarded by "land" (coefficient copy), "raw" (Bessel copy) and "empty"
+// (MMAs done) mbarriers, an operand slot by "full" (producers) and "bempty"
+// (MMAs done).  Every wait is bounded: on timeout the CTA records an error,
+// skips to the end, waits (bounded) for its copies in flight and still frees
+// its tensor memory.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -63,13 +63,13 @@ constexpr uint32_t kTmemCols = 512;
 static_assert(kN == kBesselTile, "a CTA's receivers are one tile of the Bessel table");
 
 // The two split-precision forms.  3xTF32: 8 k per stage (a row of a tile is 8
-// tf32 = 32 bytes), one (receiver, k) per producer, 3 stages.  3xBF16: 16 k
-// per stage (16 bf16 = 32 bytes), two consecutive k per producer (their bf16
-// words packed in one store), 2 stages (the raw Bessel rows of a stage double).
+// tf32 = 32 bytes), one (receiver, k) per producer.  3xBF16: 16 k per stage
+// (16 bf16 = 32 bytes), two consecutive k per producer (their bf16 words
+// packed in one store; the raw Bessel rows of a stage double).
 enum TcForm { kTF32 = 0, kBF16 = 1 };
 template <int PREC> struct TcPrec;
-template <> struct TcPrec<kTF32> { static constexpr int KT = 8, STAGES = 3, KPT = 1; };
-template <> struct TcPrec<kBF16> { static constexpr int KT = 16, STAGES = 2, KPT = 2; };
+template <> struct TcPrec<kTF32> { static constexpr int KT = 8, KPT = 1; };
+template <> struct TcPrec<kBF16> { static constexpr int KT = 16, KPT = 2; };
 template <int PREC> constexpr int raw_bytes() { return TcPrec<PREC>::KT * NBASIS * kN * 4; }
 static_assert(kProducers * TcPrec<kTF32>::KPT == kN * TcPrec<kTF32>::KT, "producers cover a stage");
 static_assert(kProducers * TcPrec<kBF16>::KPT == kN * TcPrec<kBF16>::KT, "producers cover a stage");
@@ -84,18 +84,34 @@ template <int SRC, int GRP, int PREC> struct TcGroup {
     static constexpr int kABytes = NQ * 2 * kATileBytes;
     static constexpr int kBBytes = NP * 2 * kBTileBytes;
     static constexpr int kRawBytes = raw_bytes<PREC>();
-    static constexpr int kStageBytes = kABytes + kBBytes + kRawBytes;
+    static constexpr int kASlotBytes = kABytes + kRawBytes;   // a slot of the copy ring
     static_assert(NP * kN <= (int)kTmemCols, "accumulators exceed tensor memory");
-    static_assert(kStageBytes % 1024 == 0, "stages stay 1024-byte aligned");
+    static_assert(kASlotBytes % 1024 == 0 && kBBytes % 1024 == 0, "slots stay 1024-byte aligned");
 };
 
-template <int SRC, int PREC> constexpr int smem_bytes()
-{
-    return TcPrec<PREC>::STAGES * (TcGroup<SRC, 1, PREC>::kStageBytes > TcGroup<SRC, 0, PREC>::kStageBytes
-                                       ? TcGroup<SRC, 1, PREC>::kStageBytes
-                                       : TcGroup<SRC, 0, PREC>::kStageBytes) +
-           1024;
-}
+// Two rings of shared-memory slots.  The copy ring (SA slots) holds what the
+// bulk copies bring: the coefficient tiles and the raw Bessel rows of a
+// stage, issued up to SA stages ahead of the MMAs.  The operand ring (SB = 2
+// slots) holds the Bessel operand the producers form from the raw rows just
+// before its MMAs.  Only the copies need the depth (their latency is the
+// long one), so SA is as large as shared memory allows: 4 for the moment
+// tensor's 3xTF32 sums (3 shared stages before), 3 elsewhere.
+constexpr int kSmemBudget = 232448 - 2048 - 1024;   // the opt-in limit less static data and alignment
+template <int SRC, int PREC> struct TcRing {
+    static constexpr int SB = 2;
+    static constexpr int need(int sa, int g)
+    {
+        return g == 0 ? sa * TcGroup<SRC, 0, PREC>::kASlotBytes + SB * TcGroup<SRC, 0, PREC>::kBBytes
+                      : sa * TcGroup<SRC, 1, PREC>::kASlotBytes + SB * TcGroup<SRC, 1, PREC>::kBBytes;
+    }
+    static constexpr int need2(int sa) { return need(sa, 0) > need(sa, 1) ? need(sa, 0) : need(sa, 1); }
+    static constexpr int SA = need2(4) <= kSmemBudget ? 4 : need2(3) <= kSmemBudget ? 3 : 2;
+    static constexpr int bytes = need2(SA);
+    static_assert(bytes <= kSmemBudget, "the rings exceed shared memory");
+};
+constexpr int kMaxASlots = 4;
+
+template <int SRC, int PREC> constexpr int smem_bytes() { return TcRing<SRC, PREC>::bytes + 1024; }
 
 static_assert(kKT == kTileK && kM == kTileRows, "tile shape shared with the GRT kernel");
 static_assert(TcPrec<kBF16>::KT == kTileK16, "tile shape shared with the GRT kernel");
@@ -238,7 +254,8 @@ __device__ __forceinline__ void ksum_tc_cta(const KsumTcArgs<float> &A, int blk,
     using CT = Cols<SRC>;
     using TG = TcGroup<SRC, GRP, PREC>;
     constexpr int NC = CT::NC, NQ = TG::NQ, NP = TG::NP;
-    constexpr int KT = TcPrec<PREC>::KT, kStages = TcPrec<PREC>::STAGES, KPT = TcPrec<PREC>::KPT;
+    constexpr int KT = TcPrec<PREC>::KT, KPT = TcPrec<PREC>::KPT;
+    constexpr int SA = TcRing<SRC, PREC>::SA, SB = TcRing<SRC, PREC>::SB;
     constexpr TcPlan TP = make_tcplan<SRC>();
     constexpr unsigned kBasis = group_basis_mask<SRC, GRP>();
     __shared__ uint32_t tmem_base_s;
@@ -262,27 +279,35 @@ __device__ __forceinline__ void ksum_tc_cta(const KsumTcArgs<float> &A, int blk,
     unsigned char *sm = (unsigned char *)(((uintptr_t)smem_tc + 1023) & ~(uintptr_t)1023);
     const uint32_t sm_s = (uint32_t)__cvta_generic_to_shared(sm);
     auto bar_at = [&](int i) { return (uint32_t)__cvta_generic_to_shared(&bars[i]); };
-    auto full_bar = [&](int s) { return bar_at(s); };                   // producers' B tiles
-    auto empty_bar = [&](int s) { return bar_at(kStages + s); };        // the stage's MMAs are done
-    auto land_bar = [&](int s) { return bar_at(2 * kStages + s); };     // coefficient tiles copied
-    auto raw_bar = [&](int s) { return bar_at(3 * kStages + s); };      // raw Bessel rows copied
-    const uint32_t done_bar = bar_at(4 * kStages);
+    // copy ring slot a: land (coefficient tiles copied), raw (Bessel rows
+    // copied), empty (the MMAs that read it are done); operand ring slot b:
+    // full (the producers' Bessel operand written), bempty (its MMAs done)
+    auto land_bar = [&](int a) { return bar_at(a); };
+    auto raw_bar = [&](int a) { return bar_at(SA + a); };
+    auto empty_bar = [&](int a) { return bar_at(2 * SA + a); };
+    auto full_bar = [&](int b) { return bar_at(3 * SA + b); };
+    auto bempty_bar = [&](int b) { return bar_at(3 * SA + SB + b); };
+    const uint32_t done_bar = bar_at(3 * SA + 2 * SB);
     const bool tiled = A.bt_rows > 0;
-    // stage s: [A: NQ x (hi, lo) tiles][B: (hi | lo) x NP tiles][raw Bessel rows]
-    auto a_tile = [&](int s, int i, int split) {
-        return (uint32_t)(s * TG::kStageBytes + (i * 2 + split) * kATileBytes);
+    // copy slot a: [A: NQ x (hi, lo) tiles][raw Bessel rows]; after the SA
+    // copy slots, operand slot b: [B: (hi | lo) x NP tiles]
+    auto a_tile = [&](int a, int i, int split) {
+        return (uint32_t)(a * TG::kASlotBytes + (i * 2 + split) * kATileBytes);
     };
-    auto b_tile = [&](int s, int slot, int split) {
-        return (uint32_t)(s * TG::kStageBytes + TG::kABytes + (split * NP + slot) * kBTileBytes);
+    auto raw_off = [&](int a) { return (uint32_t)(a * TG::kASlotBytes + TG::kABytes); };
+    auto b_tile = [&](int b, int slot, int split) {
+        return (uint32_t)(SA * TG::kASlotBytes + b * TG::kBBytes + (split * NP + slot) * kBTileBytes);
     };
-    auto raw_off = [&](int s) { return (uint32_t)(s * TG::kStageBytes + TG::kABytes + TG::kBBytes); };
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < kStages; s++) {
-            tc::mbar_init(full_bar(s), kProdWarps);   // one arrival per producer warp
-            tc::mbar_init(empty_bar(s), 1);
-            tc::mbar_init(land_bar(s), 1);
-            tc::mbar_init(raw_bar(s), 1);
+        for (int a = 0; a < SA; a++) {
+            tc::mbar_init(land_bar(a), 1);
+            tc::mbar_init(raw_bar(a), 1);
+            tc::mbar_init(empty_bar(a), 1);
+        }
+        for (int b = 0; b < SB; b++) {
+            tc::mbar_init(full_bar(b), kProdWarps);   // one arrival per producer warp
+            tc::mbar_init(bempty_bar(b), 1);
         }
         tc::mbar_init(done_bar, 1);
         fail_s = 0;
@@ -306,14 +331,14 @@ __device__ __forceinline__ void ksum_tc_cta(const KsumTcArgs<float> &A, int blk,
     const uint32_t tmem = tmem_base_s;
 
     if (warp == kCopyWarp) {
-        // ---------------- bulk copies, up to kStages ahead of the MMAs
+        // ---------------- bulk copies, up to SA stages ahead of the MMAs
         if (lane == 0) {
             const float *kt_tile = A.Kt + A.kt_base[wt];
             const float *braw = tiled ? A.B + (size_t)rt * A.bt_rows * NBASIS * kN : nullptr;
             int issued = 0;
             for (int st = 0; st < nstage; st++) {
-                const int s = st % kStages;
-                if (st >= kStages && !tc::mbar_wait_b(empty_bar(s), ((st / kStages) - 1) & 1)) {
+                const int s = st % SA;
+                if (st >= SA && !tc::mbar_wait_b(empty_bar(s), ((st / SA) - 1) & 1)) {
                     atomicOr(A.err, 2u);
                     fail_s = 1;
                     break;
@@ -333,9 +358,9 @@ __device__ __forceinline__ void ksum_tc_cta(const KsumTcArgs<float> &A, int blk,
                 issued = st + 1;
             }
             // copies still in flight are waited for (bounded) before the block may leave
-            for (int st = max(0, issued - kStages); st < issued; st++) {
-                tc::mbar_wait_b(land_bar(st % kStages), (st / kStages) & 1);
-                if (tiled) tc::mbar_wait_b(raw_bar(st % kStages), (st / kStages) & 1);
+            for (int st = max(0, issued - SA); st < issued; st++) {
+                tc::mbar_wait_b(land_bar(st % SA), (st / SA) & 1);
+                if (tiled) tc::mbar_wait_b(raw_bar(st % SA), (st / SA) & 1);
             }
         }
     } else if (warp < kProdWarps) {
@@ -363,12 +388,13 @@ __device__ __forceinline__ void ksum_tc_cta(const KsumTcArgs<float> &A, int blk,
         };
         if (!tiled) load_b(0);
         // each producer warp runs on its own (no barrier among them: the copy
-        // thread refills a stage's raw rows only after its MMAs, hence after every
-        // producer has read them); a wait that gives up in any lane ends the
-        // warp's loop (one decision per warp, as its lanes share a __syncwarp)
+        // thread refills a slot's raw rows only after its MMAs, which wait for
+        // every producer's operand, hence after every producer has read them);
+        // a wait that gives up in any lane ends the warp's loop (one decision
+        // per warp, as its lanes share a __syncwarp)
         for (int st = 0; st < nstage; st++) {
-            const int s = st % kStages;
-            const bool free_ok = st < kStages || tc::mbar_wait_b(empty_bar(s), ((st / kStages) - 1) & 1);
+            const int s = st % SA, sb = st % SB;
+            const bool free_ok = st < SB || tc::mbar_wait_b(bempty_bar(sb), ((st / SB) - 1) & 1);
             if (__any_sync(0xffffffffu, !free_ok)) {
                 atomicOr(A.err, 2u);
                 fail_s = 1;
@@ -377,7 +403,7 @@ __device__ __forceinline__ void ksum_tc_cta(const KsumTcArgs<float> &A, int blk,
             // B operand: pair values k^kp w J_b(k r) for (receiver br, k bk + i)
             float cur[KPT][NBASIS];
             if (tiled) {
-                const bool raw_ok = tc::mbar_wait_b(raw_bar(s), (st / kStages) & 1);
+                const bool raw_ok = tc::mbar_wait_b(raw_bar(s), (st / SA) & 1);
                 if (__any_sync(0xffffffffu, !raw_ok)) {
                     atomicOr(A.err, 2u);
                     fail_s = 1;
@@ -419,49 +445,53 @@ __device__ __forceinline__ void ksum_tc_cta(const KsumTcArgs<float> &A, int blk,
                     unsigned short h0, l0, h1, l1;
                     bf16_split(wk[0][P.kp] * cur[0][P.b], h0, l0);
                     bf16_split(wk[1][P.kp] * cur[1][P.b], h1, l1);
-                    *reinterpret_cast<uint32_t *>(sm + b_tile(s, slot, 0) + boff) = (uint32_t)h0 | ((uint32_t)h1 << 16);
-                    *reinterpret_cast<uint32_t *>(sm + b_tile(s, slot, 1) + boff) = (uint32_t)l0 | ((uint32_t)l1 << 16);
+                    *reinterpret_cast<uint32_t *>(sm + b_tile(sb, slot, 0) + boff) = (uint32_t)h0 | ((uint32_t)h1 << 16);
+                    *reinterpret_cast<uint32_t *>(sm + b_tile(sb, slot, 1) + boff) = (uint32_t)l0 | ((uint32_t)l1 << 16);
                 } else {
                     const float v = wk[0][P.kp] * cur[0][P.b];
                     const float h = tc::tf32_rna(v), l = tc::tf32_rna(v - h);
-                    *reinterpret_cast<float *>(sm + b_tile(s, slot, 0) + boff) = h;
-                    *reinterpret_cast<float *>(sm + b_tile(s, slot, 1) + boff) = l;
+                    *reinterpret_cast<float *>(sm + b_tile(sb, slot, 0) + boff) = h;
+                    *reinterpret_cast<float *>(sm + b_tile(sb, slot, 1) + boff) = l;
                 }
             }
             // make the generic-proxy writes visible to the tensor cores, then one
             // lane signals for the warp
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             __syncwarp();
-            if (lane == 0) tc::mbar_arrive(full_bar(s));
+            if (lane == 0) tc::mbar_arrive(full_bar(sb));
         }
     } else if (lane == 0) {
         // ---------------- MMA issuer (one thread of warp 9)
         for (int st = 0; st < nstage; st++) {
-            const int s = st % kStages;
-            const uint32_t par = (st / kStages) & 1;
-            if (!tc::mbar_wait_b(land_bar(s), par) || !tc::mbar_wait_b(full_bar(s), par)) {
+            const int s = st % SA, sb = st % SB;
+            if (!tc::mbar_wait_b(land_bar(s), (st / SA) & 1) || !tc::mbar_wait_b(full_bar(sb), (st / SB) & 1)) {
                 atomicOr(A.err, 4u);
                 fail_s = 1;
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             // fully unrolled: tile, operand and accumulator offsets are compile-time
-            // constants; descriptors are the stage's base descriptor plus a constant
-            const uint64_t dbase = tc::sdesc(sm_s + (uint32_t)(s * TG::kStageBytes));
+            // constants; descriptors are the slots' base descriptors plus a constant
+            // (b_tile(0, ...) carries the operand ring's offset after the copy ring)
+            const uint64_t abase = tc::sdesc(sm_s + (uint32_t)(s * TG::kASlotBytes));
+            const uint64_t bbase = tc::sdesc(sm_s + (uint32_t)(sb * TG::kBBytes));
             const uint32_t acc0 = st == 0 ? 0u : 1u;
 #pragma unroll
             for (int i = 0; i < NQ; i++) {
                 const int first = TP.tfirst[TG::Q0 + i], count = TP.tcount[TG::Q0 + i];
                 const uint32_t idesc = tc::idesc_n<PREC>(count * kN);
                 const uint32_t d = tmem + (uint32_t)(first * kN);
-                const uint64_t ah = dbase + ((uint64_t)a_tile(0, i, 0) >> 4), al = dbase + ((uint64_t)a_tile(0, i, 1) >> 4);
-                const uint64_t bh = dbase + ((uint64_t)b_tile(0, first, 0) >> 4);
-                const uint64_t bl = dbase + ((uint64_t)b_tile(0, first, 1) >> 4);
+                const uint64_t ah = abase + ((uint64_t)a_tile(0, i, 0) >> 4), al = abase + ((uint64_t)a_tile(0, i, 1) >> 4);
+                const uint64_t bh = bbase + ((uint64_t)b_tile(0, first, 0) >> 4);
+                const uint64_t bl = bbase + ((uint64_t)b_tile(0, first, 1) >> 4);
                 tc::mma_split<PREC>(d, ah, bh, idesc, acc0);
                 tc::mma_split<PREC>(d, ah, bl, idesc, 1u);
                 tc::mma_split<PREC>(d, al, bh, idesc, 1u);
             }
-            tc::mma_commit(empty_bar(s));   // stage s may be refilled once these MMAs finish
+            // each commit arrives once every MMA issued so far is done: copy slot s
+            // may then be refilled, operand slot sb rewritten
+            tc::mma_commit(empty_bar(s));
+            tc::mma_commit(bempty_bar(sb));
         }
         tc::mma_commit(done_bar);           // all MMAs of this CTA
     }
@@ -533,7 +563,7 @@ template <int SRC, int PREC>
 __global__ void __launch_bounds__(tc::kThreads, 1) ksum_tc_kernel(KsumTcArgs<float> A)
 {
     extern __shared__ __align__(1024) unsigned char smem_tc[];
-    __shared__ __align__(8) unsigned long long bars[4 * 3 + 1];   // 4 barriers per stage (at most 3) + done
+    __shared__ __align__(8) unsigned long long bars[3 * tc::kMaxASlots + 2 * 2 + 1];   // copy ring, operand ring, done
     __shared__ float ir_s[2 * tc::kN];
     if (blockIdx.x & 1) ksum_tc_cta<SRC, 1, PREC>(A, (int)(blockIdx.x >> 1), smem_tc, bars, ir_s);
     else ksum_tc_cta<SRC, 0, PREC>(A, (int)(blockIdx.x >> 1), smem_tc, bars, ir_s);

@@ -17,9 +17,11 @@ cudaError_t grt_point_launch(const GrtArgs<R> &A, int spec, unsigned nblocks, si
                              int *launches);
 
 // Many jobs: nt threads per block (64, 128, 256), one block per tile
-// (grid = ntiles) or persistent (grid blocks); spec as above (one-tile forms).
+// (grid = ntiles) or persistent (grid blocks).  The first nspec tiles belong to
+// FP32 jobs that allow the specialised form: the one-tile forms run them in
+// two passes and the rest in one; the persistent forms run every tile in one.
 template <typename R>
-cudaError_t grt_batch_launch(const GrtArgs<R> *jobs, int spec, int nt, bool persist, const int4 *tiles, int ntiles,
+cudaError_t grt_batch_launch(const GrtArgs<R> *jobs, int nspec, int nt, bool persist, const int4 *tiles, int ntiles,
                              int grid, size_t smem, unsigned *err, cudaStream_t st, int *launches);
 
 // resident blocks per SM of a persistent batch form

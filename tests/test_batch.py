@@ -155,3 +155,30 @@ def test_in_graph_downloads(ctx):
                 assert np.array_equal(o, ref[j])
         assert np.array_equal(b.fetch_f32(1), ref[1])
     b.close()
+
+
+@pytest.mark.gpu
+def test_mixed_batch_runs_each_form(ctx):
+    """A batch whose jobs do not all allow the specialised (two-pass) GRT form:
+    those that do run it, the others (a receiver below the source's layer, a
+    single force) the generic one, in separate launches over their own tiles;
+    every job equals its single run bitwise."""
+    import grtm_cuda_gb300 as g
+    from grtm_cuda_gb300 import synth
+    jobs = []
+    for seed, nl, hs, hr, src in ((21, 9, 12.0, 0.0, 1), (22, 12, 3.0, 14.0, 1), (23, 7, 8.0, 0.0, 0),
+                                  (24, 15, 20.0, 0.0, 1)):
+        rng = np.random.default_rng(seed)
+        m = dict(synth.crust(rng, nl, hs, src_type=src), hr=hr)
+        d = np.sort(rng.uniform(5.0, 150.0, 4))
+        o = g.make_opts(0.05, 9, sigma_factor=math.pi, k_mode=g.K_FIXED, nk_fixed=700 + 13 * seed,
+                        precision=g.FP32, fix=g.FIX_ALL)
+        jobs.append((g.make_model(**m), o, d))
+    b = g.Batch(ctx, jobs, autotune=True)
+    b.execute()
+    for j, (m, o, d) in enumerate(jobs):
+        oj = g.with_precision(o, o.precision)
+        oj.k_slice = b.info(j)[0]["k_slice"]
+        t1, _, _ = g.run(m, oj, d, ctx=ctx)
+        assert np.array_equal(b.fetch(j)[0], t1), j
+    b.close()
