@@ -97,19 +97,22 @@ template <int SRC, int GRP, int PREC> struct TcGroup {
 // long one), so SA is as large as shared memory allows: 4 for the moment
 // tensor's 3xTF32 sums (3 shared stages before), 3 elsewhere.
 constexpr int kSmemBudget = 232448 - 2048 - 1024;   // the opt-in limit less static data and alignment
+#ifndef TC_OPERAND_SLOTS
+#define TC_OPERAND_SLOTS 2
+#endif
 template <int SRC, int PREC> struct TcRing {
-    static constexpr int SB = 2;
-    static constexpr int need(int sa, int g)
+    static constexpr int need(int sa, int sb, int g)
     {
-        return g == 0 ? sa * TcGroup<SRC, 0, PREC>::kASlotBytes + SB * TcGroup<SRC, 0, PREC>::kBBytes
-                      : sa * TcGroup<SRC, 1, PREC>::kASlotBytes + SB * TcGroup<SRC, 1, PREC>::kBBytes;
+        return g == 0 ? sa * TcGroup<SRC, 0, PREC>::kASlotBytes + sb * TcGroup<SRC, 0, PREC>::kBBytes
+                      : sa * TcGroup<SRC, 1, PREC>::kASlotBytes + sb * TcGroup<SRC, 1, PREC>::kBBytes;
     }
-    static constexpr int need2(int sa) { return need(sa, 0) > need(sa, 1) ? need(sa, 0) : need(sa, 1); }
-    static constexpr int SA = need2(4) <= kSmemBudget ? 4 : need2(3) <= kSmemBudget ? 3 : 2;
-    static constexpr int bytes = need2(SA);
+    static constexpr int need2(int sa, int sb) { return need(sa, sb, 0) > need(sa, sb, 1) ? need(sa, sb, 0) : need(sa, sb, 1); }
+    static constexpr int SB = TC_OPERAND_SLOTS;
+    static constexpr int SA = need2(4, SB) <= kSmemBudget ? 4 : need2(3, SB) <= kSmemBudget ? 3 : 2;
+    static constexpr int bytes = need2(SA, SB);
     static_assert(bytes <= kSmemBudget, "the rings exceed shared memory");
 };
-constexpr int kMaxASlots = 4;
+constexpr int kMaxASlots = 4, kMaxBSlots = 3;
 
 template <int SRC, int PREC> constexpr int smem_bytes() { return TcRing<SRC, PREC>::bytes + 1024; }
 
@@ -563,7 +566,7 @@ template <int SRC, int PREC>
 __global__ void __launch_bounds__(tc::kThreads, 1) ksum_tc_kernel(KsumTcArgs<float> A)
 {
     extern __shared__ __align__(1024) unsigned char smem_tc[];
-    __shared__ __align__(8) unsigned long long bars[3 * tc::kMaxASlots + 2 * 2 + 1];   // copy ring, operand ring, done
+    __shared__ __align__(8) unsigned long long bars[3 * tc::kMaxASlots + 2 * tc::kMaxBSlots + 1];   // copy ring, operand ring, done
     __shared__ float ir_s[2 * tc::kN];
     if (blockIdx.x & 1) ksum_tc_cta<SRC, 1, PREC>(A, (int)(blockIdx.x >> 1), smem_tc, bars, ir_s);
     else ksum_tc_cta<SRC, 0, PREC>(A, (int)(blockIdx.x >> 1), smem_tc, bars, ir_s);
