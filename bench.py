@@ -283,9 +283,12 @@ def max_ok_distance(dists, errs, tol):
     return float(bad.min()) if bad.size else float(d.max())
 
 
-# DRAM bytes per (w,k) point of the FP32 GRT kernel (tensor-core operand layout), from one ncu capture
-# of the small 40-layer case: 5.7 MB read + 181.3 MB written for 2.10 M points (profiles/grt_point_crust40s.md)
-GRT_DRAM_BYTES_PER_POINT = (5.668864e6 + 181.344512e6) / (512 * 4096)
+# DRAM bytes per (w,k) point of the FP32 GRT kernels (two passes, tensor-core operand layout), from one
+# ncu capture of the small 40-layer case (2.10 M points, profiles/grt_point_crust40s.md): pass 1 reads
+# 2.6 MB and writes 23.4 MB, pass 2 reads 88.4 MB and writes 180.6 MB.  There the 84 MB of R^du planes the
+# passes exchange stay partly in L2; on a large batch they travel to DRAM and back (40 + 40 B per point).
+GRT_DRAM_BYTES_PER_POINT = (2.591488e6 + 23.446016e6 + 88.392448e6 + 180.646656e6) / (512 * 4096)
+GRT_RDU_BYTES_PER_POINT = 80.0
 
 
 def grt_roofline(n_wk_by_layers, ms, fp32_peak):
@@ -295,8 +298,10 @@ def grt_roofline(n_wk_by_layers, ms, fp32_peak):
     return {"bound": "fp32", "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s",
             "frac": (ach / fp32_peak) if fp32_peak else None,
             "traffic": pts * GRT_DRAM_BYTES_PER_POINT,
-            "traffic_note": "bytes per launch, scaled by the points from the small-case ncu capture "
-                            f"({GRT_DRAM_BYTES_PER_POINT:.1f} B per point; the writes grow with the points)",
+            "traffic_bound_if_rdu_in_dram": pts * max(GRT_DRAM_BYTES_PER_POINT, 112.0 + GRT_RDU_BYTES_PER_POINT),
+            "traffic_note": "bytes per launch pair (two passes), scaled by the points from the small-case ncu "
+                            f"capture ({GRT_DRAM_BYTES_PER_POINT:.1f} B per point; the writes grow with the points; "
+                            "the R^du planes between the passes, 80 B per point, stay partly in L2 in that case)",
             "per_launch": f"{sum(n for n, _ in n_wk_by_layers)} (w,k) points x (layers x {F_LAYER:.0f} + "
                           f"{F_SRC_TENSOR:.0f}) flops = {flops:.3e}"}
 

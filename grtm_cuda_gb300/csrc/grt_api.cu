@@ -942,22 +942,36 @@ template <typename R>
 static int fetch_freqs(grt_plan *p, int n_freq, const int *freq_idx, double *spectra)
 {
     grt_ctx *ctx = p->ctx;
-    int rc = ensure_spec<R>(p);
-    if (rc) return rc;
     const size_t rows = (size_t)p->nd * p->nc;
     std::vector<grt::C<R>> h(rows * n_freq);
-    // one strided copy per frequency: element iw of every (receiver, column) row
-    // full plans: spec [tr][N] by frequency; selections: spec [tr][row]
+    // gathered on the device ([f][row]) and downloaded in one copy: full plans
+    // from the k-sums and the phase/taper table (no full spectrum is filled),
+    // spectra-only plans from their [row][selected frequency] spectra
     const Job &J = p->J;
-    const size_t pitch = J.fsel.empty() ? (size_t)J.N : (size_t)J.nw;
-    for (int f = 0; f < n_freq; f++) {
-        int col = freq_idx[f];
-        if (!J.fsel.empty()) col = (int)(std::find(J.fsel.begin(), J.fsel.end(), col) - J.fsel.begin());
-        CU(cudaMemcpy2DAsync(h.data() + f * rows, sizeof(grt::C<R>), (const grt::C<R> *)p->spec + col,
-                             pitch * sizeof(grt::C<R>), sizeof(grt::C<R>), rows, cudaMemcpyDeviceToHost,
-                             ctx->stream));
+    std::vector<int> idx(freq_idx, freq_idx + n_freq), sel;
+    if (!J.fsel.empty())
+        for (int f = 0; f < n_freq; f++)
+            sel.push_back((int)(std::find(J.fsel.begin(), J.fsel.end(), freq_idx[f]) - J.fsel.begin()));
+    int *d_idx = nullptr;
+    R *d_out = nullptr;
+    cudaError_t e = dev_alloc(ctx, &d_idx, 2 * (size_t)n_freq * sizeof(int));
+    if (e == cudaSuccess) e = dev_alloc(ctx, &d_out, h.size() * 2 * sizeof(R));
+    cudaStream_t st = ctx->stream;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_idx, idx.data(), n_freq * sizeof(int), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && !sel.empty())
+        e = cudaMemcpyAsync(d_idx + n_freq, sel.data(), n_freq * sizeof(int), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+        const long long n = (long long)rows * n_freq;
+        grt::gather_freqs_kernel<R><<<(unsigned)std::min<long long>((n + 255) / 256, 4096), 256, 0, st>>>(
+            (const R *)p->S, (const R *)p->post, (const R *)p->spec, d_idx, sel.empty() ? nullptr : d_idx + n_freq,
+            (long long)rows, J.nw, n_freq, d_out);
+        e = cudaGetLastError();
     }
-    CU(cudaStreamSynchronize(ctx->stream));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), d_out, h.size() * sizeof(grt::C<R>), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    dev_free(ctx, d_idx);
+    dev_free(ctx, d_out);
+    CU(e);
     for (size_t r = 0; r < rows; r++)
         for (int f = 0; f < n_freq; f++) {
             spectra[2 * (r * n_freq + f)] = (double)h[f * rows + r].x;

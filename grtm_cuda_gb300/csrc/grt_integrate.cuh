@@ -1010,6 +1010,35 @@ __global__ void select_kernel(const R *S, const R *post, R *out, long long n, in
         y[e] = s[e] * q[e % nw];
 }
 
+// Spectra of every trace at nf chosen frequencies, gathered on the device
+// (the fetch of a few frequencies without filling the full spectra):
+// Y[f][tr] = S[tr][n] post[n] for n = idx[f] < nw, 0 at nw, conj(Y at N - n)
+// above; with sel (a spectra-only plan) the already-scaled spec[tr][sel[f]].
+template <typename R>
+__global__ void gather_freqs_kernel(const R *S_, const R *post_, const R *spec_, const int *idx, const int *sel,
+                                    long long ntr, int nw, int nf, R *out_)
+{
+    const C<R> *S = reinterpret_cast<const C<R> *>(S_), *post = reinterpret_cast<const C<R> *>(post_);
+    const C<R> *spec = reinterpret_cast<const C<R> *>(spec_);
+    C<R> *out = reinterpret_cast<C<R> *>(out_);
+    const long long n_all = ntr * nf;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n_all;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int f = (int)(e / ntr);
+        const long long tr = e % ntr;
+        C<R> y;
+        if (sel) {
+            y = spec[tr * nw + sel[f]];
+        } else {
+            const int n = idx[f], N = 2 * nw;
+            if (n < nw) y = S[tr * nw + n] * post[n];
+            else if (n == nw) y = C<R>{R(0), R(0)};
+            else y = conj(S[tr * nw + N - n] * post[N - n]);
+        }
+        out[e] = y;
+    }
+}
+
 // The full spectrum of every trace (the reference's `out` after taper and
 // Hermitian fill), written only when a caller fetches spectra: Y[tr][n] =
 // S[tr][n] post[n] for n < nw, 0 at nw, conj(Y[N - n]) above.

@@ -534,16 +534,21 @@ def run_learned_batch(sampler, models, dists_list, ctx=None, plain=PLAIN, spec_t
         tj.append(time.perf_counter())
         n_fb = 0
         fallback = []
+        t_sw = t_ff = 0.0
         for j, (mo, (nk, st, kmax, gr), d) in enumerate(zip(mods, grids, dists_list)):
             d = np.asarray(d, np.float64)
             sp = spots[j]
             bands = np.unique(np.array([d.min(), math.sqrt(d.min() * d.max()), d.max()]))
+            t_a = time.perf_counter()
             sw = sweep_kmax(mo, plain_opts(plain), sp, bands, sampler.tol,
                             k_judge=np.repeat(kmax[sp][:, None], len(bands), 1), ctx=ctx, env=True)
+            t_b = time.perf_counter()
             w = np.maximum(taper_weight(sp, gr["nw"], plain["taper"]), 1e-6)[:, None]
             excess = sw["tail"] * sw["env"] * w / (sampler.tol * sw["env"].max(0)[None, :])
             s_plain = sb.fetch_freqs(j, sp)
             s_learn = b.fetch_freqs(j, sp)
+            t_sw += t_b - t_a
+            t_ff += time.perf_counter() - t_b
             _, bad = spectral_verdict(s_learn, s_plain, spec_tol)
             below = np.clip(np.searchsorted(bands, d * (1 + 1e-12), side="right") - 1, 0, len(bands) - 1)
             bad |= (excess.max(0) > 10.0)[below]
@@ -571,7 +576,8 @@ def run_learned_batch(sampler, models, dists_list, ctx=None, plain=PLAIN, spec_t
                     s_execute=t[3] - t[2], s_fetch=t[3] - t_exec, s_fetch_wait=t[4] - t_wait,
                     s_judge=t_wait - t[3], s_fallback=t[5] - t[4],
                     s_total=t[5] - t[0],
-                    s_judge_parts=dict(spot_build=tj[1] - tj[0], spot_exec=tj[2] - tj[1], sweeps_compare=tj[3] - tj[2]))
+                    s_judge_parts=dict(spot_build=tj[1] - tj[0], spot_exec=tj[2] - tj[1], sweeps_compare=tj[3] - tj[2],
+                                       sweeps=t_sw, fetch_spots=t_ff))
         b.close()
         return traces, info
     finally:

@@ -110,3 +110,22 @@ def test_fixed_k_slice_sums_in_the_same_order(ctx):
         with pytest.raises(g.GrtError) as e:
             g.Plan(ctx, m, o, d)
         assert e.value.status == g.ERR_ARG
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_fetch_freqs_equals_full_spectra(ctx, prec):
+    """A full plan's spectra at chosen frequencies (gathered on the device from
+    the k-sums) are its full spectra's columns there, bitwise: positive
+    frequencies, the zeroed Nyquist bin and the Hermitian mirror above it."""
+    import grtm_cuda_gb300 as g
+    m, o, d = _job(g, g.FP32 if prec == "fp32" else g.FP64)
+    p = g.Plan(ctx, m, o, d)
+    p.execute()
+    idx = [0, 1, 77, 511, 512, 513, 900, 1023]
+    s = p.fetch_freqs(idx)
+    _, full = p.fetch(False, True)
+    p.close()
+    assert np.array_equal(s, full[..., idx])
+    assert np.all(s[..., idx.index(512)] == 0)
+    assert np.array_equal(s[..., idx.index(513)], np.conj(full[..., 511]))
