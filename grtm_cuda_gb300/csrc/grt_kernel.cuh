@@ -715,6 +715,12 @@ __device__ __forceinline__ void count_levals(unsigned long long *c, int v)
 #ifndef GRT_POINT_MINB
 #define GRT_POINT_MINB 1   // resident blocks per SM the register allocation must allow
 #endif
+// resident threads per SM the register allocation of the two passes must
+// allow: pass 1 512 (128 registers, no spills), pass 2 GRT_PASS2_THREADS
+// (384: 167 registers, no spills)
+#ifndef GRT_PASS2_THREADS
+#define GRT_PASS2_THREADS 384
+#endif
 
 // stage the layer table of (job, frequency) into shared memory with a TMA bulk
 // copy issued by thread 0; every thread waits on the mbarrier phase
@@ -759,7 +765,7 @@ static __global__ void batch_tiles_kernel(const int2 *row_id, const int *row_nk,
 
 // One job: one block per (frequency, block of kGrtThreads wavenumbers).
 template <typename R, int SPEC = kSpecGeneric, int PASS = 0>
-__global__ void __launch_bounds__(kGrtThreads, PASS == 1 ? 512 / kGrtThreads : PASS == 2 ? 384 / kGrtThreads : GRT_POINT_MINB) grt_point_kernel(GrtArgs<R> A)
+__global__ void __launch_bounds__(kGrtThreads, PASS == 1 ? 512 / kGrtThreads : PASS == 2 ? GRT_PASS2_THREADS / kGrtThreads : GRT_POINT_MINB) grt_point_kernel(GrtArgs<R> A)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) unsigned long long bar;
@@ -796,7 +802,7 @@ __global__ void __launch_bounds__(kGrtThreads, PASS == 1 ? 512 / kGrtThreads : P
 // The autotuner picks the form and shape on the batch.
 constexpr int kRun = 4;
 template <typename R, int NT, bool PERSIST, int SPEC = kSpecGeneric, int PASS = 0>
-__global__ void __launch_bounds__(NT, PASS == 1 ? 512 / NT : PASS == 2 ? 384 / NT : 1) grt_batch_kernel(const GrtArgs<R> *__restrict__ jobs,
+__global__ void __launch_bounds__(NT, PASS == 1 ? 512 / NT : PASS == 2 ? GRT_PASS2_THREADS / NT : 1) grt_batch_kernel(const GrtArgs<R> *__restrict__ jobs,
                                                            const int4 *__restrict__ tiles, int ntiles,
                                                            unsigned int *err)
 {
