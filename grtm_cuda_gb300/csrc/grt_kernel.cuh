@@ -717,9 +717,10 @@ __device__ __forceinline__ void count_levals(unsigned long long *c, int v)
 #endif
 // resident threads per SM the register allocation of the two passes must
 // allow: pass 1 512 (128 registers, no spills), pass 2 GRT_PASS2_THREADS
-// (384: 167 registers, no spills)
+// (512: 128 registers and 32 bytes of spills, 1-2 % faster than 384 with 167
+// registers and none)
 #ifndef GRT_PASS2_THREADS
-#define GRT_PASS2_THREADS 384
+#define GRT_PASS2_THREADS 512
 #endif
 
 // stage the layer table of (job, frequency) into shared memory with a TMA bulk

@@ -267,7 +267,8 @@ def test_learned_path_gain_and_accuracy(ctx):
     t64, _, _ = g.run(model, learned.plain_opts(precision=g.FP64), d, ctx=ctx)
     tl, info = learned.run_learned(s, m, d, ctx=ctx)
     err = np.sqrt(np.sum((tl - t64) ** 2, axis=(1, 2)) / np.sum(t64 ** 2, axis=(1, 2)))
-    assert info["nkw_plain"] / info["nkw_learned"] >= 1.15
+    # per-band k margins: 1.46x fewer points here (1.20x with one margin)
+    assert info["nkw_plain"] / info["nkw_learned"] >= 1.35
     assert info["fallback"] == []                      # a sound grid passes its judge
     assert np.sqrt(np.sum((tl - t64) ** 2) / np.sum(t64 ** 2)) <= 1e-3
     assert np.median(err) <= 1e-3
