@@ -4,6 +4,7 @@ Tolerances (relative L2 over each output column's time series):
   FP64 GPU vs FP64 oracle (same method)         1e-10
   FP32 GPU vs FP64 oracle, regional distances   5e-5
   FP32 GPU vs FP64 oracle, the 10000 km demo    5e-4  (its k-sum cancels by ~1e3)
+  judged FP32 (run_judged, tol 1e-4), the demo  1e-4
   vs the reference's golden demo output: above its own noise floor (bins
   iw >= 3; see test_oracle.py), 5e-6 masked time-domain for FP64.
 """
@@ -166,6 +167,19 @@ def test_demo_fp32_matches_oracle(g, ctx, demo_oracle):
     tr, _, _ = g.run(m, g.make_opts(precision=g.FP32, **kw), [dist], ctx)
     for c in range(15):
         assert rel(tr[0, c], osig[:, c]) < 5e-4, c
+
+
+def test_demo_judged_within_1e_4(g, ctx, demo_oracle):
+    """The plain FP32 path misses 1e-4 on the 10 000 km demo (its k-sum
+    cancels by ~1e3); the judged run at tolerance 1e-4 (error estimate, FP64
+    for the receivers it flags) meets it against the oracle."""
+    job, osig = demo_oracle
+    m, kw, dist = _demo_model(g)
+    tr, info = g.run_judged(m, g.make_opts(precision=g.FP32, **kw), [dist], ctx, tol=1e-4)
+    for c in range(15):
+        assert rel(tr[0, c], osig[:, c]) < 1e-4, c
+    # the estimate is consistent with what it decided
+    assert (len(info["fp64"]) > 0) == bool(g.JUDGE_SAFETY * info["est"][0] > 1e-4)
 
 
 def test_green_file_interface(g, tmp_path, golden, demo_oracle):
