@@ -21,7 +21,9 @@ Arms (all FP32 arithmetic, checked against the FP64 path of the same method):
           per pair of the integrand tables).
 
   value  traces/s of the fast arm on device-resident inputs: device time of
-         the batch graph plus the wall time of its judge and fallback.
+         the batch graph plus the wall time of its judge and fallback (the
+         judge's own GPU work runs on a second context beside the graph; the
+         time it adds beyond the graph's end is counted).
   e2e    traces/s of the fast arm through the public call with host inputs
          and outputs: prediction, batch build (with autotuning), execution,
          judge, fallback and the download of every trace (float32, into

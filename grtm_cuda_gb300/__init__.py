@@ -297,6 +297,7 @@ class Context:
 
     def __init__(self, device=0):
         self.h = ctypes.c_void_p()
+        self.device = int(device)
         rc = lib().grt_create(ctypes.byref(self.h), device)
         if rc:
             raise GrtError(rc, "grt_create failed")

@@ -9,6 +9,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <memory>
 #include <string>
 #include <type_traits>
@@ -226,11 +227,14 @@ extern "C" void grt_plan_destroy(grt_plan *p)
 }
 
 // Raise a kernel's dynamic shared-memory limit (never lower it: a captured
-// graph replays launches of several sizes).  Not thread-safe, like contexts.
+// graph replays launches of several sizes).  One table for all contexts; a
+// context itself is used from one host thread at a time.
 template <typename F>
 static cudaError_t raise_smem_limit(F *kernel, int bytes)
 {
     static std::map<std::pair<int, const void *>, int> current;   // (device, kernel) -> limit set
+    static std::mutex mu;   // contexts on other host threads share the table
+    std::lock_guard<std::mutex> lock(mu);
     int dev = 0;
     cudaGetDevice(&dev);
     int &cur = current[{dev, (const void *)kernel}];

@@ -2,6 +2,7 @@
 // included by the per-precision translation units.
 #pragma once
 #include <map>
+#include <mutex>
 #include <type_traits>
 #include <utility>
 
@@ -12,11 +13,13 @@ namespace grt {
 namespace launch_detail {
 
 // raise a kernel's dynamic shared-memory limit, never lowering it (a captured
-// graph replays launches of several sizes); not thread-safe, like contexts
+// graph replays launches of several sizes); one table for all contexts
 template <typename F>
 cudaError_t raise_smem(F *kernel, int bytes)
 {
     static std::map<std::pair<int, const void *>, int> current;   // (device, kernel) -> limit set
+    static std::mutex mu;   // contexts on other host threads share the table
+    std::lock_guard<std::mutex> lock(mu);
     int dev = 0;
     cudaGetDevice(&dev);
     int &cur = current[{dev, (const void *)kernel}];

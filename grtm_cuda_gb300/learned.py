@@ -29,6 +29,7 @@ import ctypes
 import math
 import os
 import struct
+import threading
 import time
 
 import numpy as np
@@ -493,14 +494,34 @@ def run_learned(sampler, m, dists, ctx=None, plain=PLAIN, tail_tol=None, spec_to
             ctx.close()
 
 
+_JUDGE_CTX = {}
+
+
+def judge_context(ctx):
+    """A second context on ctx's device for the judge's work, kept for the
+    process (its cached memory serves every later judge)."""
+    dev = getattr(ctx, "device", 0)
+    jc = _JUDGE_CTX.get(dev)
+    if jc is None or not jc.h:
+        jc = _JUDGE_CTX[dev] = Context(dev)
+    return jc
+
+
 def run_learned_batch(sampler, models, dists_list, ctx=None, plain=PLAIN, spec_tol=3e-3, autotune=True,
-                      use_stride=True, out=None):
+                      use_stride=True, out=None, overlap=True):
     """run_learned for many models at once: one batch (one CUDA graph, one
     GRT launch) on the learned grids, the judge's spot evaluations as a
     second batch, sweeps per model, and the plain grid for any receiver the
     judge rejects.  Returns (list of float32 traces, info); with `out` (one
     float32 [n_dist, n_cols, N] array per model, e.g. pinned_empty ones) the
-    traces are fetched into those arrays."""
+    traces are fetched into those arrays.
+
+    overlap: the judge's own GPU work (the plain grid at the spot
+    frequencies, the tail sweeps) needs only the models and the batch's k
+    split, so it runs on a second context while the batch's graph runs on
+    this one (the graph in a host thread; both share the GPU); only the
+    comparison with the batch's spectra waits for the graph.  info's s_judge
+    is the judge's time not hidden behind the graph."""
     own = ctx is None
     ctx = ctx or Context()
     try:
@@ -517,45 +538,79 @@ def run_learned_batch(sampler, models, dists_list, ctx=None, plain=PLAIN, spec_t
         # copies behind them on the copy engine: 20 -> 83 ms of judge)
         b = Batch(ctx, jobs, autotune=autotune, outs=out)
         t.append(time.perf_counter())
-        rep = b.execute()
-        t_exec = time.perf_counter()
+        spots = [judge_spots(gr["nw"], st) for (nk, st, kmax, gr) in grids]
+        spot_jobs = [(mo, spot_opts(gr["nw"], gr["dk"], sp, b.info(j)[0]["k_slice"], plain), d)
+                     for j, (mo, (nk, st, kmax, gr), d, sp) in enumerate(zip(mods, grids, dists_list, spots))]
+        done = {}
+
+        def execute():
+            try:
+                done["rep"] = b.execute()
+            except BaseException as e:   # re-raised on the calling thread
+                done["exc"] = e
+            done["t"] = time.perf_counter()
+
+        jctx = judge_context(ctx) if overlap else ctx
+        runner = None
+        if overlap:
+            runner = threading.Thread(target=execute)
+            runner.start()
+        else:
+            execute()
+            t_exec = done["t"]
+        # judge, the part that does not need the batch: spot frequencies on the
+        # plain grid (batched), tails by sweep
+        tj = [time.perf_counter()]
+        t_sw = t_ff = 0.0
+        pre = []
+        try:
+            sb = Batch(jctx, spot_jobs, autotune=False)
+            tj.append(time.perf_counter())
+            sb.execute()
+            tj.append(time.perf_counter())
+            for j, (mo, (nk, st, kmax, gr), d) in enumerate(zip(mods, grids, dists_list)):
+                d = np.asarray(d, np.float64)
+                sp = spots[j]
+                bands = np.unique(np.array([d.min(), math.sqrt(d.min() * d.max()), d.max()]))
+                t_a = time.perf_counter()
+                sw = sweep_kmax(mo, plain_opts(plain), sp, bands, sampler.tol,
+                                k_judge=np.repeat(kmax[sp][:, None], len(bands), 1), ctx=jctx, env=True)
+                t_b = time.perf_counter()
+                w = np.maximum(taper_weight(sp, gr["nw"], plain["taper"]), 1e-6)[:, None]
+                excess = sw["tail"] * sw["env"] * w / (sampler.tol * sw["env"].max(0)[None, :])
+                s_plain = sb.fetch_freqs(j, sp)
+                t_sw += t_b - t_a
+                t_ff += time.perf_counter() - t_b
+                pre.append((d, bands, excess, s_plain))
+            sb.close()
+            t_pre = time.perf_counter()
+        finally:
+            # the graph's thread ends before anything of this context may go
+            if runner is not None:
+                runner.join()
+        if runner is not None:
+            t_exec = done["t"]
+        if "exc" in done:
+            raise done["exc"]
+        rep = done["rep"]
         traces = list(out) if out is not None else [b.fetch_f32(j) for j in range(len(jobs))]
         t.append(time.perf_counter())
-        # judge: spot frequencies on the plain grid (batched), tails by sweep
-        spot_jobs, spots = [], []
-        for j, (mo, (nk, st, kmax, gr), d) in enumerate(zip(mods, grids, dists_list)):
-            sp = judge_spots(gr["nw"], st)
-            spot_jobs.append((mo, spot_opts(gr["nw"], gr["dk"], sp, b.info(j)[0]["k_slice"], plain), d))
-            spots.append(sp)
-        tj = [time.perf_counter()]
-        sb = Batch(ctx, spot_jobs, autotune=False)
-        tj.append(time.perf_counter())
-        sb.execute()
-        tj.append(time.perf_counter())
+        # judge, the part that needs the batch: each receiver's spectra at the
+        # spot frequencies against the plain grid's
+        t_c = time.perf_counter()
         n_fb = 0
         fallback = []
-        t_sw = t_ff = 0.0
-        for j, (mo, (nk, st, kmax, gr), d) in enumerate(zip(mods, grids, dists_list)):
-            d = np.asarray(d, np.float64)
+        for j, (d, bands, excess, s_plain) in enumerate(pre):
             sp = spots[j]
-            bands = np.unique(np.array([d.min(), math.sqrt(d.min() * d.max()), d.max()]))
             t_a = time.perf_counter()
-            sw = sweep_kmax(mo, plain_opts(plain), sp, bands, sampler.tol,
-                            k_judge=np.repeat(kmax[sp][:, None], len(bands), 1), ctx=ctx, env=True)
-            t_b = time.perf_counter()
-            w = np.maximum(taper_weight(sp, gr["nw"], plain["taper"]), 1e-6)[:, None]
-            excess = sw["tail"] * sw["env"] * w / (sampler.tol * sw["env"].max(0)[None, :])
-            s_plain = sb.fetch_freqs(j, sp)
             s_learn = b.fetch_freqs(j, sp)
-            t_sw += t_b - t_a
-            t_ff += time.perf_counter() - t_b
+            t_ff += time.perf_counter() - t_a
             _, bad = spectral_verdict(s_learn, s_plain, spec_tol)
             below = np.clip(np.searchsorted(bands, d * (1 + 1e-12), side="right") - 1, 0, len(bands) - 1)
             bad |= (excess.max(0) > 10.0)[below]
             fallback.append(np.nonzero(bad)[0].tolist())
             n_fb += int(bad.sum())
         tj.append(time.perf_counter())
-        sb.close()
         t_wait = time.perf_counter()
         b.wait()
         t.append(time.perf_counter())
@@ -567,6 +622,9 @@ def run_learned_batch(sampler, models, dists_list, ctx=None, plain=PLAIN, spec_t
                 p.close()
         t.append(time.perf_counter())
         _, tune = b.info()
+        # the judge's time beyond the graph: its part before the graph ended
+        # (when it outlasted the graph) and its part after
+        exposed_pre = max(0.0, t_pre - t_exec) if overlap else t_pre - tj[0]
         info = dict(nkw_learned=int(sum(int(g_[0].sum()) for g_ in grids)),
                     nkw_plain=int(sum(int(g_[3]["nw"]) * plain["nk"] for g_ in grids)),
                     stride_mean=float(np.mean([g_[1].mean() for g_ in grids])), fallback=fallback,
@@ -574,10 +632,12 @@ def run_learned_batch(sampler, models, dists_list, ctx=None, plain=PLAIN, spec_t
                     n_layer_evals=int(rep.n_layer_evals),
                     gpu_launches=rep.kernel_launches, tune=tune, s_predict=t[1] - t[0], s_build=t[2] - t[1],
                     s_execute=t[3] - t[2], s_fetch=t[3] - t_exec, s_fetch_wait=t[4] - t_wait,
-                    s_judge=t_wait - t[3], s_fallback=t[5] - t[4],
-                    s_total=t[5] - t[0],
-                    s_judge_parts=dict(spot_build=tj[1] - tj[0], spot_exec=tj[2] - tj[1], sweeps_compare=tj[3] - tj[2],
-                                       sweeps=t_sw, fetch_spots=t_ff))
+                    s_judge=exposed_pre + (t_wait - t_c), s_fallback=t[5] - t[4],
+                    s_total=t[5] - t[0], judge_overlapped=bool(overlap),
+                    s_judge_parts=dict(spot_build=tj[1] - tj[0], spot_exec=tj[2] - tj[1],
+                                       sweeps_compare=(t_pre - tj[2]) + (tj[3] - t_c), sweeps=t_sw,
+                                       fetch_spots=t_ff, before_graph_end=max(0.0, t_exec - tj[0]) if overlap
+                                       else 0.0, total=(t_pre - tj[0]) + (t_wait - t_c)))
         b.close()
         return traces, info
     finally:

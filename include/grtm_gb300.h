@@ -130,7 +130,9 @@ typedef struct grt_plan grt_plan;
 
 /* Contexts own a CUDA stream on one device and a cache of the device memory
  * their plans and batches release (reused by the next ones, up to half the
- * device memory); not thread-safe.  Destroy plans and batches first. */
+ * device memory).  A context (with its plans and batches) is used from one
+ * host thread at a time; different contexts may run on different threads at
+ * once (their work then shares the GPU).  Destroy plans and batches first. */
 GRT_API int grt_create(grt_ctx **ctx, int device);
 GRT_API void grt_destroy(grt_ctx *ctx);
 /* Return the context's cached device memory to the driver. */

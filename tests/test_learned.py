@@ -254,6 +254,27 @@ def _learned_case(seed=3007, n_rec=8):
 
 
 @pytest.mark.gpu
+def test_learned_batch_judge_overlap(ctx):
+    """The batched learned path with its judge run beside the batch's graph (a
+    second context on another host thread) gives the traces and verdicts of
+    the judge run after it, and reports only the judge time the graph did
+    not hide."""
+    from grtm_cuda_gb300 import learned
+    if not os.path.exists(learned.WEIGHTS):
+        pytest.skip("no trained sampler in the tree")
+    s = learned.Sampler.load()
+    cases = [_learned_case(3007, 6), _learned_case(3011, 5)]
+    ms, ds = [m for m, _ in cases], [d for _, d in cases]
+    t1, i1 = learned.run_learned_batch(s, ms, ds, ctx=ctx, overlap=False)
+    t2, i2 = learned.run_learned_batch(s, ms, ds, ctx=ctx, overlap=True)
+    for a, b in zip(t1, t2):
+        assert np.array_equal(a, b)
+    assert i1["fallback"] == i2["fallback"] and i1["nkw_learned"] == i2["nkw_learned"]
+    assert i2["judge_overlapped"] and not i1["judge_overlapped"]
+    assert 0.0 <= i2["s_judge"] <= i2["s_judge_parts"]["total"] + 1e-6
+
+
+@pytest.mark.gpu
 def test_learned_path_gain_and_accuracy(ctx):
     """On a held-out model the trained sampler evaluates far fewer (w,k)
     points than the plain fixed grid and stays within 1e-3 of FP64."""
