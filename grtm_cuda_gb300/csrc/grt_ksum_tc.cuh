@@ -479,18 +479,20 @@ __device__ __forceinline__ void ksum_tc_cta(const KsumTcArgs<float> &A, int blk,
             const uint64_t abase = tc::sdesc(sm_s + (uint32_t)(s * TG::kASlotBytes));
             const uint64_t bbase = tc::sdesc(sm_s + (uint32_t)(sb * TG::kBBytes));
             const uint32_t acc0 = st == 0 ? 0u : 1u;
+            // the three split products of every column, round robin over the
+            // columns: consecutive MMAs write different accumulators (the
+            // order within one accumulator, hi*hi then hi*lo then lo*hi, stays)
 #pragma unroll
-            for (int i = 0; i < NQ; i++) {
-                const int first = TP.tfirst[TG::Q0 + i], count = TP.tcount[TG::Q0 + i];
-                const uint32_t idesc = tc::idesc_n<PREC>(count * kN);
-                const uint32_t d = tmem + (uint32_t)(first * kN);
-                const uint64_t ah = abase + ((uint64_t)a_tile(0, i, 0) >> 4), al = abase + ((uint64_t)a_tile(0, i, 1) >> 4);
-                const uint64_t bh = bbase + ((uint64_t)b_tile(0, first, 0) >> 4);
-                const uint64_t bl = bbase + ((uint64_t)b_tile(0, first, 1) >> 4);
-                tc::mma_split<PREC>(d, ah, bh, idesc, acc0);
-                tc::mma_split<PREC>(d, ah, bl, idesc, 1u);
-                tc::mma_split<PREC>(d, al, bh, idesc, 1u);
-            }
+            for (int sp3 = 0; sp3 < 3; sp3++)
+#pragma unroll
+                for (int i = 0; i < NQ; i++) {
+                    const int first = TP.tfirst[TG::Q0 + i], count = TP.tcount[TG::Q0 + i];
+                    const uint32_t idesc = tc::idesc_n<PREC>(count * kN);
+                    const uint32_t d = tmem + (uint32_t)(first * kN);
+                    const uint64_t a = abase + ((uint64_t)a_tile(0, i, sp3 == 2 ? 1 : 0) >> 4);
+                    const uint64_t b = bbase + ((uint64_t)b_tile(0, first, sp3 == 1 ? 1 : 0) >> 4);
+                    tc::mma_split<PREC>(d, a, b, idesc, sp3 == 0 ? acc0 : 1u);
+                }
             // each commit arrives once every MMA issued so far is done: copy slot s
             // may then be refilled, operand slot sb rewritten
             tc::mma_commit(empty_bar(s));
