@@ -12,7 +12,9 @@
 //  spectral_kernel      phase e^{i w t0}, cosine taper and scale
 //                       (green.cu:1905-1921), Hermitian fill (1925-1938),
 //                       inverse DFT and e^{sigma t} de-damping (2227-2239),
-//                       one trace per block, FFT in shared memory.
+//                       one trace per block, FFT in shared memory: the FP64
+//                       plans' form (FP32 plans run fft::c2r_kernel,
+//                       grt_fft.cuh).
 #pragma once
 #include "grt_cplx.cuh"
 #include "grt_types.h"
