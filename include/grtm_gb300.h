@@ -359,8 +359,9 @@ GRT_API int grt_run(grt_ctx *ctx, const grt_model *model, const grt_opts *opts, 
 /* For callers that cannot allocate device memory -- a process whose GPU memory
  * is reserved by another runtime (a framework's caching allocator, a service
  * with a fixed device budget) or code running where cudaMalloc is not
- * permitted.  Same traces as grt_run (FP32 only) for small jobs, allocating
- * nothing on the device: all intermediates live in one library-owned device
+ * permitted.  The traces grt_run gives in FP32, to FP32 rounding (it runs
+ * the generic GRT form and the SIMT wavenumber sum), for small jobs,
+ * allocating nothing on the device: all intermediates live in one library-owned device
  * array of 32 MiB per GPU and the job tables in a 4 MiB host array.  A GPU
  * takes the device array when the library's kernels are first loaded on it
  * (with CUDA's default lazy module loading, at the first grt_run_noalloc call
