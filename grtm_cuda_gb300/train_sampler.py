@@ -27,7 +27,7 @@ HELD_OUT_SEEDS = range(3000, 3256)
 CAL_SEEDS = range(5000, 5256)      # further sweeps for the per-band margins
 
 
-def recalibrate(weights, out, n_bands=8, n_cal=256, tol=1e-4, log=sys.stdout, dump=None):
+def recalibrate(weights, out, n_bands=8, n_cal=256, tol=1e-4, log=sys.stdout, dump=None, q_k=0.995):
     """Keep a trained network and measure its k_max margins per band of log w
     on the validation sweeps and n_cal further models (the bands need more
     sweeps than one global quantile)."""
@@ -40,11 +40,11 @@ def recalibrate(weights, out, n_bands=8, n_cal=256, tol=1e-4, log=sys.stdout, du
     t1 = time.perf_counter()
     if dump:
         np.savez_compressed(dump, X=X, Y=Y, pred=s.predict(ctx, X))
-    mk, md = s.calibrate(ctx, X, Y, n_bands=n_bands)
+    mk, md = s.calibrate(ctx, X, Y, q_k=q_k, n_bands=n_bands)
     s.save(out)
     ctx.close()
     e, mg = s.kbands if s.kbands is not None else ([], [])
-    res = dict(n_sweeps=len(X), s_sweeps=t1 - t0, margin_k=mk, margin_d=md,
+    res = dict(n_sweeps=len(X), s_sweeps=t1 - t0, q_k=q_k, margin_k=mk, margin_d=md,
                band_edges_hz=[float(np.exp(x) / (2 * np.pi)) for x in e], band_margins=[float(x) for x in mg])
     print(json.dumps(res), file=log)
     return s, res
@@ -125,9 +125,11 @@ def main():
     ap.add_argument("--recalibrate", action="store_true",
                     help="keep the network of --weights, measure per-band k margins, write --out")
     ap.add_argument("--bands", type=int, default=8, help="recalibrate: bands of log w")
+    ap.add_argument("--q-k", type=float, default=0.995,
+                    help="recalibrate: quantile of the k_max under-prediction a band's margin covers")
     a = ap.parse_args()
     if a.recalibrate:
-        recalibrate(a.weights, a.out, n_bands=a.bands, tol=a.tol, dump=a.dump)
+        recalibrate(a.weights, a.out, n_bands=a.bands, tol=a.tol, dump=a.dump, q_k=a.q_k)
     elif a.eval:
         evaluate(a.weights, a.eval_models, a.receivers, not a.no_fp64, use_stride=not a.no_stride)
     else:
