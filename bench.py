@@ -503,7 +503,7 @@ def bench_batch(args, ws, rank, local, td):
         "spectral": spectral_roofline(sum(len(d) * 20 * (nw * 8 + 8192 * 4) for d, nw in zip(dists, plain_spec_nw)),
                                       plain_spec_ms),
         "wall_s_timed": wall,
-        "gpu_launches": int(sum(i["gpu_launches"] for i in infos)),
+        "gpu_launches": int(sum(i["gpu_launches"] + i.get("judge_launches", 0) for i in infos)),
         "roofline": roof,
         "e2e": {"value": e2e, "unit": "traces/s", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None},
         "clocks": clk,

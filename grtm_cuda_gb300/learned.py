@@ -563,10 +563,11 @@ def run_learned_batch(sampler, models, dists_list, ctx=None, plain=PLAIN, spec_t
         tj = [time.perf_counter()]
         t_sw = t_ff = 0.0
         pre = []
+        n_judge_launches = 0
         try:
             sb = Batch(jctx, spot_jobs, autotune=False)
             tj.append(time.perf_counter())
-            sb.execute()
+            n_judge_launches = sb.execute().kernel_launches
             tj.append(time.perf_counter())
             for j, (mo, (nk, st, kmax, gr), d) in enumerate(zip(mods, grids, dists_list)):
                 d = np.asarray(d, np.float64)
@@ -630,7 +631,9 @@ def run_learned_batch(sampler, models, dists_list, ctx=None, plain=PLAIN, spec_t
                     stride_mean=float(np.mean([g_[1].mean() for g_ in grids])), fallback=fallback,
                     n_fallback=n_fb, ms_batch_gpu=rep.ms_total, ms_batch_grt=rep.ms_grt,
                     n_layer_evals=int(rep.n_layer_evals),
-                    gpu_launches=rep.kernel_launches, tune=tune, s_predict=t[1] - t[0], s_build=t[2] - t[1],
+                    gpu_launches=rep.kernel_launches,
+                    # the judge's: its spot batch, per model a sweep (GRT and sweep kernels) and two gathers
+                    judge_launches=int(n_judge_launches) + 4 * len(models), tune=tune, s_predict=t[1] - t[0], s_build=t[2] - t[1],
                     s_execute=t[3] - t[2], s_fetch=t[3] - t_exec, s_fetch_wait=t[4] - t_wait,
                     s_judge=exposed_pre + (t_wait - t_c), s_fallback=t[5] - t[4],
                     s_total=t[5] - t[0], judge_overlapped=bool(overlap),
