@@ -27,7 +27,9 @@ Arms (all FP32 arithmetic, checked against the FP64 path of the same method):
   e2e    traces/s of the fast arm through the public call with host inputs
          and outputs: prediction, batch build (with autotuning), execution,
          judge, fallback and the download of every trace (float32, into
-         page-locked host arrays allocated once), per step.
+         page-locked host arrays allocated once), per step, over K steps of
+         the pipelined call (learned.run_learned_stream: a step's prediction,
+         build and judge run beside the previous step's graph).
 
 Other cases: --case crust20 (one 20-layer model, 200 receivers 5-300 km, nt
 4096, nk 16384), --case crust4 (4 layers, 10 receivers) and --case crust40s
@@ -154,13 +156,14 @@ def allmax(td, x):
     return float(t.item())
 
 
-def device_sync():
-    try:
-        import torch
-        if torch.cuda.is_available():
-            torch.cuda.synchronize()
-    except Exception:
-        pass
+def device_sync(device=0):
+    """cudaDeviceSynchronize through the library (grt_device_synchronize).
+    Initialising torch's CUDA runtime in the process made the pipelined fast
+    arm's host loop 3-40 ms slower per step, so torch is not used for it."""
+    import grtm_cuda_gb300 as g
+    rc = g.lib().grt_device_synchronize(int(device))
+    if rc:
+        raise RuntimeError(f"grt_device_synchronize: status {rc}")
 
 
 def fp32_peak_tflops():
@@ -357,32 +360,43 @@ def bench_batch(args, ws, rank, local, td):
 
     # the traces come back into page-locked host arrays, allocated once
     grids0 = [g.grid(g.make_model(**m), learned.plain_opts()) for m in models]
-    pinned = [g.pinned_empty((len(d), gr["n_cols"], gr["n_samples"])) for d, gr in zip(dists, grids0)]
+    outs = tuple([g.pinned_empty((len(d), gr["n_cols"], gr["n_samples"])) for d, gr in zip(dists, grids0)]
+                 for _ in range(2))
+    pinned = outs[0]
+    ctx2 = g.Context(local)
 
-    def fast_step():
-        return learned.run_learned_batch(sampler, models, dists, ctx=ctx, out=pinned)
+    def fast_steps(n):
+        # n steps through the pipelined public call: step i+1's prediction,
+        # batch build and judge run beside step i's graph (two contexts and
+        # two sets of page-locked outputs, alternating)
+        return learned.run_learned_stream(sampler, [(models, dists)] * n, (ctx, ctx2), outs=outs)
 
     # the fast arm runs first in the process: after the FP64 reference plan (24
     # GB of buffers) had run, fetches into page-locked host memory on this host
     # stayed 5x slower (40 instead of 8 ms per 0.66 GB) for the rest of the process
-    for _ in range(args.warmup):
-        tr_fast, info = fast_step()
-    del tr_fast
+    for _ in fast_steps(args.warmup):
+        pass
 
     clocks = ClockSampler(local)
     clocks.start()
     barrier(td)
-    device_sync()
+    device_sync(local)
     infos = []
     t0 = time.time()
-    for _ in range(args.steps):
-        _, info = fast_step()
+    step_wall = []
+    t_s = t0
+    for _, info in fast_steps(args.steps):
+        t_e = time.time()
+        step_wall.append(t_e - t_s)   # between consecutive results (the first fills the pipeline)
+        t_s = t_e
         infos.append(info)
-    device_sync()
+    device_sync(local)
     wall = time.time() - t0
     barrier(td)
     clk = clocks.stop()
-    tr0 = np.array(pinned[0])   # the last timed step's traces of model 0
+    ctx2.close()
+    pinned = outs[(args.steps - 1) % 2]   # the last timed step's traces
+    tr0 = np.array(pinned[0])
     # plain: per-model plans, SIMT sums, fixed grid (timed by device events, then freed)
     os.environ["GRT_KSUM"] = "simt"
     plain_plans = [g.Plan(ctx, g.make_model(**m), learned.plain_opts(), d) for m, d in zip(models, dists)]
@@ -478,6 +492,13 @@ def bench_batch(args, ws, rank, local, td):
                      "s_fetch_wait": last["s_fetch_wait"],
                      "s_judge": last["s_judge"],
                      "s_fallback": last["s_fallback"], "judge_parts": last.get("s_judge_parts"),
+                     "s_close": last.get("s_close"),
+                     "step_wall_ms": [round(w * 1e3, 2) for w in step_wall],
+                     "step_call_ms": [round(i.get("s_call", 0.0) * 1e3, 2) for i in infos],
+                     "step_gpu_ms": [round(i["ms_batch_gpu"], 2) for i in infos],
+                     "step_graph_call_ms": [round(i.get("s_graph_call", 0.0) * 1e3, 2) for i in infos],
+                     "step_graph_gap_ms": [round((b["t_graph_start"] - a["t_graph_end"]) * 1e3, 2)
+                                           for a, b in zip(infos, infos[1:]) if "t_graph_start" in b],
                      "points_vs_plain": frac_pts,
                      "stride_mean": last["stride_mean"], "fallback_traces": last["n_fallback"],
                      "tune": infos[0]["tune"]},
@@ -614,7 +635,7 @@ def bench_uneven(args, ws, rank, local, td):
     clocks = ClockSampler(local)
     clocks.start()
     barrier(td)
-    device_sync()
+    device_sync(local)
     t0 = time.time()
     ms_b = [batched_pass(False)[0] for _ in range(args.steps)]
     wall = (time.time() - t0) / args.steps
@@ -747,12 +768,12 @@ def bench_single(args, ws, rank, local, td):
     clocks = ClockSampler(local)
     clocks.start()
     barrier(td)
-    device_sync()
+    device_sync(local)
     reps = []
     t0 = time.time()
     for _ in range(args.steps):
         reps.append(plan.execute().as_dict())
-    device_sync()
+    device_sync(local)
     wall = time.time() - t0
     barrier(td)
     dev_ms = float(np.sum([r["ms_total"] for r in reps]))
@@ -764,10 +785,10 @@ def bench_single(args, ws, rank, local, td):
     # e2e through the public call with host buffers
     e2e_t = []
     for i in range(max(2, min(args.steps, 4)) + 1):
-        device_sync()
+        device_sync(local)
         t = time.time()
         tr, _, r = g.run(m, o32, dists, ctx)
-        device_sync()
+        device_sync(local)
         if i > 0:
             e2e_t.append(time.time() - t)
     e2e_t = allmax(td, float(np.median(e2e_t)))

@@ -191,7 +191,8 @@ EXPORTS = ("grt_create", "grt_destroy", "grt_last_error", "grt_status_string", "
            "grt_plan_synth",
            "grt_batch_synth", "grt_flatten", "grt_plan_write", "grt_plan_fetch_f32", "grt_batch_fetch_f32",
            "grt_host_alloc", "grt_host_free", "grt_trim", "grt_batch_fetch_f32_async", "grt_batch_wait",
-           "grt_plan_error_estimate", "grt_batch_error_estimate")
+           "grt_plan_error_estimate", "grt_batch_error_estimate", "grt_set_priority",
+           "grt_tune_clear", "grt_device_synchronize")
 
 _lib = None
 
@@ -262,6 +263,10 @@ def lib():
     L.grt_batch_wait.argtypes = [vp]
     L.grt_trim.argtypes = [vp]
     L.grt_trim.restype = None
+    L.grt_set_priority.argtypes = [vp, ctypes.c_int]
+    L.grt_tune_clear.argtypes = []
+    L.grt_device_synchronize.argtypes = [ctypes.c_int]
+    L.grt_tune_clear.restype = None
     L.grt_flatten.argtypes = [ctypes.c_int, _dp, _dp, _dp, ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp,
                               _dp, _dp, _dp, _dp]
     L.grt_dc_moment.argtypes = [ctypes.c_double] * 4 + [_dp]
@@ -309,6 +314,13 @@ class Context:
         """Return the device memory cached for reuse by later plans."""
         if self.h:
             lib().grt_trim(self.h)
+
+    def set_priority(self, high=True):
+        """The device's greatest stream priority for this context's work
+        (grt_set_priority); only while it holds no plan or batch."""
+        rc = lib().grt_set_priority(self.h, int(bool(high)))
+        if rc:
+            raise GrtError(rc, self.error())
 
     def close(self):
         if self.h:

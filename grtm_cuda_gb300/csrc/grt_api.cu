@@ -10,6 +10,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <tuple>
 #include <memory>
 #include <string>
 #include <type_traits>
@@ -157,6 +158,9 @@ static void dev_free(grt_ctx *ctx, void *p)
     if (ctx->pooled > ctx->pool_cap) pool_trim(ctx, ctx->pool_cap);
 }
 
+// set-up and fetch work runs on the context's auxiliary stream (grt_ctx.h)
+static cudaError_t setup_stream(grt_ctx *ctx, cudaStream_t *st) { return grt_setup_stream(ctx, st); }
+
 extern "C" void grt_trim(grt_ctx *ctx)
 {
     if (!ctx) return;
@@ -190,6 +194,10 @@ extern "C" int grt_create(grt_ctx **out, int device)
     c->device = device;
     CU(cudaSetDevice(device));
     CU(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    int least = 0, greatest = 0;
+    CU(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    CU(cudaStreamCreateWithPriority(&c->aux, cudaStreamNonBlocking, greatest));
+    CU(cudaEventCreateWithFlags(&c->aux_ev, cudaEventDisableTiming));
     for (auto &e : c->ev) CU(cudaEventCreate(&e));
     size_t free_b = 0, total_b = 0;
     CU(cudaMemGetInfo(&free_b, &total_b));
@@ -208,9 +216,39 @@ extern "C" void grt_destroy(grt_ctx *ctx)
         cudaStreamSynchronize(ctx->stream);
         cudaStreamDestroy(ctx->stream);
     }
+    if (ctx->aux) {
+        cudaStreamSynchronize(ctx->aux);
+        cudaStreamDestroy(ctx->aux);
+    }
+    if (ctx->aux_ev) cudaEventDestroy(ctx->aux_ev);
     if (ctx->blas) cublasDestroy((cublasHandle_t)ctx->blas);
     pool_trim(ctx, 0);
     delete ctx;
+}
+
+extern "C" int grt_device_synchronize(int device)
+{
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    return e == cudaSuccess ? GRT_OK : GRT_ERR_CUDA;
+}
+
+extern "C" int grt_set_priority(grt_ctx *ctx, int high)
+{
+    if (!ctx) return GRT_ERR_ARG;
+    if (!ctx->live.empty()) return set_err(ctx, GRT_ERR_ARG, "grt_set_priority: the context holds plans or batches");
+    CU(cudaSetDevice(ctx->device));
+    int least = 0, greatest = 0;
+    CU(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    const int prio = high ? greatest : 0;
+    if (prio == ctx->priority) return GRT_OK;
+    cudaStream_t s = nullptr;
+    CU(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, prio));
+    cudaStreamSynchronize(ctx->stream);
+    cudaStreamDestroy(ctx->stream);
+    ctx->stream = s;
+    ctx->priority = prio;
+    return GRT_OK;
 }
 
 extern "C" const char *grt_last_error(const grt_ctx *ctx) { return ctx ? ctx->err.c_str() : "no context"; }
@@ -219,6 +257,7 @@ extern "C" void grt_plan_destroy(grt_plan *p)
 {
     if (!p) return;
     cudaSetDevice(p->ctx->device);
+    cudaStreamSynchronize(p->ctx->aux);   // set-up left in flight by a failed creation
     void *bufs[] = {p->tab, p->K, p->B, p->S, p->post, p->tw, p->spec, p->sig, p->tiles, p->nk, p->koff, p->ddist,
                     p->damp, p->dampf, p->twp, p->rdu, p->own_derr ? p->derr : nullptr, p->P, p->Kt, p->kt_base, p->ks, p->tfirst,
                     p->Ag, p->Bg, p->Dg, p->own_nlev ? p->nlev : nullptr};
@@ -342,6 +381,8 @@ static int upload(grt_plan *p)
 {
     grt_ctx *ctx = p->ctx;
     const Job &J = p->J;
+    cudaStream_t st = nullptr;
+    CU(setup_stream(ctx, &st));
     std::vector<grt::LayerW<R>> tab;
     std::vector<R> post, tw;
     std::vector<double> damp;
@@ -377,7 +418,7 @@ static int upload(grt_plan *p)
     CU(dev_alloc(ctx, &p->ddist, p->nd * sizeof(double)));
     if (!p->use_tc) CU(dev_alloc(ctx, &p->K, szK));
     CU(dev_alloc(ctx, &p->B, szB));
-    if (p->bt_rows) CU(cudaMemsetAsync(p->B, 0, szB, ctx->stream));   // padding rows and receivers stay zero
+    if (p->bt_rows) CU(cudaMemsetAsync(p->B, 0, szB, st));   // padding rows and receivers stay zero
     CU(dev_alloc(ctx, &p->S, ntr * J.nw * 2 * sizeof(R)));
     CU(dev_alloc(ctx, &p->post, post.size() * sizeof(R)));
     CU(dev_alloc(ctx, &p->tw, tw.size() * sizeof(R)));
@@ -439,16 +480,15 @@ static int upload(grt_plan *p)
         }
         CU(dev_alloc(ctx, &p->Kt, (size_t)tot * sizeof(float)));
         CU(dev_alloc(ctx, &p->kt_base, nwt * sizeof(long long)));
-        CU(cudaMemcpyAsync(p->kt_base, base.data(), nwt * sizeof(long long), cudaMemcpyHostToDevice, ctx->stream));
+        CU(cudaMemcpyAsync(p->kt_base, base.data(), nwt * sizeof(long long), cudaMemcpyHostToDevice, st));
         // slots beyond a frequency's k range stay zero: the GRT kernel only writes valid (w,k)
-        if (padded) CU(cudaMemsetAsync(p->Kt, 0, (size_t)tot * sizeof(float), ctx->stream));
-        CU(cudaStreamSynchronize(ctx->stream));
+        if (padded) CU(cudaMemsetAsync(p->Kt, 0, (size_t)tot * sizeof(float), st));
+        CU(cudaStreamSynchronize(st));
     }
     // the specialised FP32 evaluation runs as two passes (bottom-up, then the
     // rest): kRduPlanes floats per (w,k) between them
     if (p->gspec == grt::kSpecAboveTensor && std::is_same<R, float>::value)
         CU(dev_alloc(ctx, &p->rdu, (size_t)grt::kRduPlanes * J.nkw * sizeof(float)));
-    cudaStream_t st = ctx->stream;
     CU(cudaMemcpyAsync(p->tab, tab.data(), tab.size() * sizeof(tab[0]), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(p->nk, J.nk.data(), J.nw * sizeof(int), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(p->tfirst, tfirst.data(), J.nw * sizeof(long long), cudaMemcpyHostToDevice, st));
@@ -778,10 +818,15 @@ static int launch_spectral(grt_plan *p, cudaStream_t st, int &launches)
     return GRT_OK;
 }
 
+// (the small reads below go through the auxiliary stream: a synchronous copy on
+// the legacy stream waited behind other contexts' pending graph copies)
 static int check_device_error(grt_ctx *ctx, const unsigned *derr)
 {
     unsigned herr = 0;
-    CU(cudaMemcpy(&herr, derr, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    cudaStream_t st = nullptr;
+    CU(setup_stream(ctx, &st));
+    CU(cudaMemcpyAsync(&herr, derr, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
     if (herr)
         return set_err(ctx, GRT_ERR_TIMEOUT,
                        std::string("a bounded device wait gave up: ") + ((herr & 1) ? "layer-table copy " : "") +
@@ -791,10 +836,13 @@ static int check_device_error(grt_ctx *ctx, const unsigned *derr)
 }
 
 // the layers the GRT kernel evaluated, summed over its counters
-static cudaError_t read_nlev(const unsigned long long *d, long long *out)
+static cudaError_t read_nlev(grt_ctx *ctx, const unsigned long long *d, long long *out)
 {
     unsigned long long h[grt::kNlevSlots];
-    cudaError_t e = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
+    cudaStream_t st = nullptr;
+    cudaError_t e = setup_stream(ctx, &st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, d, sizeof h, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return e;
     unsigned long long t = 0;
     for (unsigned long long v : h) t += v;
@@ -833,7 +881,7 @@ static int execute(grt_plan *p)
     p->rep.ms_spectral = t[3];
     p->rep.ms_total = t[0] + t[1] + t[2] + t[3];
     p->rep.kernel_launches = launches;
-    CU(read_nlev(p->nlev, &p->rep.n_layer_evals));
+    CU(read_nlev(ctx, p->nlev, &p->rep.n_layer_evals));
     return GRT_OK;
 }
 
@@ -960,7 +1008,8 @@ static int fetch_freqs(grt_plan *p, int n_freq, const int *freq_idx, double *spe
     R *d_out = nullptr;
     cudaError_t e = dev_alloc(ctx, &d_idx, 2 * (size_t)n_freq * sizeof(int));
     if (e == cudaSuccess) e = dev_alloc(ctx, &d_out, h.size() * 2 * sizeof(R));
-    cudaStream_t st = ctx->stream;
+    cudaStream_t st = nullptr;
+    if (e == cudaSuccess) e = setup_stream(ctx, &st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_idx, idx.data(), n_freq * sizeof(int), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess && !sel.empty())
         e = cudaMemcpyAsync(d_idx + n_freq, sel.data(), n_freq * sizeof(int), cudaMemcpyHostToDevice, st);
@@ -973,6 +1022,7 @@ static int fetch_freqs(grt_plan *p, int n_freq, const int *freq_idx, double *spe
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), d_out, h.size() * sizeof(grt::C<R>), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    else if (st) cudaStreamSynchronize(st);   // nothing in flight when the blocks go back
     dev_free(ctx, d_idx);
     dev_free(ctx, d_out);
     CU(e);
@@ -1652,6 +1702,7 @@ extern "C" void grt_batch_destroy(grt_batch *b)
 {
     if (!b) return;
     cudaSetDevice(b->ctx->device);
+    cudaStreamSynchronize(b->ctx->aux);   // set-up left in flight by a failed creation
     if (b->copy) {
         cudaStreamSynchronize(b->copy);
         cudaStreamDestroy(b->copy);
@@ -1714,19 +1765,39 @@ static cudaError_t raise_batch_limits(int smem)
 // Time the candidate shapes on a prefix of the tiles (up to 3e8 points: the
 // coefficient writes of a smaller sample would fit the address translation
 // better than the full batch does and favour the wrong shape).  The choice is
-// remembered on the context for batches of the same precision and depth.
+// remembered for batches of the same precision and depth on the device.
+// Autotuner choices are kept per device for the process, not per context: they
+// depend on the kernels and the GPU.  A second context (one that builds its
+// batches beside another context's running graph, say) reuses a choice
+// instead of timing candidates while the GPU is shared.
+static std::mutex g_tune_mu;
+static std::map<std::tuple<int, int, int>, std::pair<int, int>> g_tuned;   // (device, sizeof R, deepest) -> shape, blocks
+static std::map<std::pair<int, int>, double> g_tuned_tc;                    // (device, deepest) -> k split ratio
+
+extern "C" void grt_tune_clear(void)
+{
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tuned.clear();
+    g_tuned_tc.clear();
+}
+
 template <typename R>
 static int batch_autotune(grt_batch *b, bool run)
 {
     grt_ctx *ctx = b->ctx;
     cudaStream_t st = ctx->stream;
     const size_t smem = (size_t)b->maxL * sizeof(grt::LayerW<R>);
-    const auto key = std::make_pair((int)sizeof(R), b->maxL);
+    const auto key = std::make_tuple(ctx->device, (int)sizeof(R), b->maxL);
     if (run) {
-        auto it = ctx->tuned.find(key);
-        if (it != ctx->tuned.end()) {   // this context already tuned batches of this kind
-            b->tune.grt_shape = it->second.first;
-            b->tune.grt_blocks = it->second.second;
+        std::pair<int, int> hit{-1, 0};
+        {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            auto it = g_tuned.find(key);
+            if (it != g_tuned.end()) hit = it->second;
+        }
+        if (hit.first >= 0) {   // batches of this kind were tuned on this device
+            b->tune.grt_shape = hit.first;
+            b->tune.grt_blocks = hit.second;
             b->tune.grt_threads = kShapes[b->tune.grt_shape].nt;
             b->tune.tuned = 2;
             b->tune.n_cand = 0;
@@ -1774,14 +1845,17 @@ static int batch_autotune(grt_batch *b, bool run)
     b->tune.n_cand = std::min(n, GRT_TUNE_MAX);
     b->tune.tuned = run;
     b->tune.sample_fraction = run ? frac : 0.0;
-    if (run) ctx->tuned[key] = std::make_pair(b->tune.grt_shape, b->tune.grt_blocks);
+    if (run) {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tuned[key] = std::make_pair(b->tune.grt_shape, b->tune.grt_blocks);
+    }
     return check_device_error(ctx, b->derr);
 }
 
 // FP32 batches: the tensor-core sums' k split, timed.  Candidates around the
 // wave-filling default of the largest job (in (w,k) points x receivers); the
 // best one's ratio to the default is applied to every job that did not fix its
-// k_slice, and the context remembers it per deepest model.
+// k_slice, and it is remembered per device and deepest model.
 static int tc_ensure_P(grt_plan *p)
 {
     grt_ctx *ctx = p->ctx;
@@ -1806,10 +1880,14 @@ static int tc_autotune(grt_batch *b, bool run)
     b->tune.tc_tuned = 0;
     b->tune.tc_n_cand = 0;
     if (!big) return GRT_OK;
-    double ratio = 1.0;
-    auto it = ctx->tuned_tc.find(b->maxL);
-    if (run && it != ctx->tuned_tc.end()) {
-        ratio = it->second;
+    double ratio = 1.0, hit = 0.0;
+    if (run) {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tuned_tc.find(std::make_pair(ctx->device, b->maxL));
+        if (it != g_tuned_tc.end()) hit = it->second;
+    }
+    if (hit > 0.0) {
+        ratio = hit;
         b->tune.tc_tuned = 2;
     } else if (run) {
         const int s0 = big->nsplit_default;
@@ -1839,7 +1917,10 @@ static int tc_autotune(grt_batch *b, bool run)
             }
         }
         ratio = (double)sbest / s0;
-        ctx->tuned_tc[b->maxL] = ratio;
+        {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            g_tuned_tc[std::make_pair(ctx->device, b->maxL)] = ratio;
+        }
         b->tune.tc_tuned = 1;
     }
     for (grt_plan *p : b->jobs)
@@ -1930,7 +2011,8 @@ template <typename R>
 static int batch_build(grt_batch *b, int autotune)
 {
     grt_ctx *ctx = b->ctx;
-    cudaStream_t st = ctx->stream;
+    cudaStream_t st = nullptr;   // the set-up; the graph is captured on the main stream
+    CU(setup_stream(ctx, &st));
     // per-job arguments in device memory; every job reports waits to the batch's error word
     std::vector<grt::GrtArgs<R>> args;
     for (grt_plan *p : b->jobs) {
@@ -2005,10 +2087,10 @@ static int batch_build(grt_batch *b, int autotune)
             CU(grt::ksum_tc_limits(grt::kColTensor, p->tc_bf16));
         }
     }
-    CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    rc = batch_record<R>(b, st);
+    CU(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    rc = batch_record<R>(b, ctx->stream);
     cudaGraph_t g = nullptr;
-    cudaError_t ce = cudaStreamEndCapture(st, &g);
+    cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
     if (rc) {
         if (g) cudaGraphDestroy(g);
         return rc;
@@ -2047,10 +2129,13 @@ extern "C" int grt_batch_create(grt_ctx *ctx, int n_jobs, const grt_job *jobs, i
 
     CU(cudaDeviceGetAttribute(&b->nsm, cudaDevAttrMultiProcessorCount, ctx->device));
     CU(dev_alloc(ctx, &b->derr, sizeof(unsigned)));
-    CU(cudaMemset(b->derr, 0, sizeof(unsigned)));
+    cudaStream_t su = nullptr;
+    CU(setup_stream(ctx, &su));
+    CU(cudaMemsetAsync(b->derr, 0, sizeof(unsigned), su));
+    CU(cudaStreamSynchronize(su));
     CU(dev_alloc(ctx, &b->nlev, grt::kNlevSlots * sizeof(unsigned long long)));
-    for (auto &s : b->side) CU(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-    CU(cudaStreamCreateWithFlags(&b->copy, cudaStreamNonBlocking));
+    for (auto &s : b->side) CU(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, ctx->priority));
+    CU(cudaStreamCreateWithPriority(&b->copy, cudaStreamNonBlocking, ctx->priority));
     b->done.assign(b->jobs.size(), nullptr);
     for (auto &e : b->done) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     CU(cudaEventCreate(&b->ev_start));
@@ -2080,7 +2165,7 @@ extern "C" int grt_batch_execute(grt_batch *b, grt_report *r)
     CU(cudaEventElapsedTime(&t_all, b->ev_start, b->ev_end));
     b->rep.ms_grt = t_grt;
     b->rep.ms_total = t_all;
-    CU(read_nlev(b->nlev, &b->rep.n_layer_evals));
+    CU(read_nlev(ctx, b->nlev, &b->rep.n_layer_evals));
     b->rep.ms_bessel = b->rep.ms_ksum = b->rep.ms_spectral = 0.f;
     long long nwk = 0, h2d = 0, d2h = 0;
     int ncol = 0;

@@ -209,8 +209,13 @@ __global__ void adam_step(float *P, const float *G, float *M, float *V, int n, f
 
 struct grt_mlp {
     grt_ctx *ctx = nullptr;
+    int device = 0;
     Layout lo{1, 1};
     float *P = nullptr, *G = nullptr, *M = nullptr, *V = nullptr, *loss = nullptr;
+    // the forward pass's inputs and outputs, kept between calls (grown when a
+    // call needs more): a cudaFree per call would wait for the whole device
+    float *fx = nullptr, *fy = nullptr;
+    size_t fx_n = 0, fy_n = 0;
     long long step = 0;
     grt_mlp(int ni, int no) : lo(ni, no) {}
 };
@@ -248,6 +253,7 @@ extern "C" int grt_mlp_create(grt_ctx *ctx, int n_in, int n_out, unsigned long l
         return mfail(ctx, GRT_ERR_ARG, "mlp: 1 <= n_in <= 32, 1 <= n_out <= 4");
     std::unique_ptr<grt_mlp> m(new grt_mlp(n_in, n_out));
     m->ctx = ctx;
+    m->device = ctx->device;
     const int n = m->lo.n;
     CUM(cudaSetDevice(ctx->device));
     CUM(cudaMalloc(&m->P, n * sizeof(float)));
@@ -285,8 +291,9 @@ extern "C" int grt_mlp_create(grt_ctx *ctx, int n_in, int n_out, unsigned long l
 extern "C" void grt_mlp_destroy(grt_mlp *m)
 {
     if (!m) return;
-    cudaSetDevice(m->ctx->device);
+    cudaSetDevice(m->device);
     cudaFree(m->P); cudaFree(m->G); cudaFree(m->M); cudaFree(m->V); cudaFree(m->loss);
+    cudaFree(m->fx); cudaFree(m->fy);
     delete m;
 }
 
@@ -317,21 +324,22 @@ static size_t work_floats(int n) { return (size_t)n * (3 * H + kDS + 1); }
 
 // forward (and, with dT, backward into m->G / m->loss) over n samples;
 // work: work_floats(n) floats (only for the backward)
-static int launch_fb(grt_mlp *m, int n, const float *dX, const float *dT, const int *didx, float *dY, float *work)
+static int launch_fb(grt_mlp *m, int n, const float *dX, const float *dT, const int *didx, float *dY, float *work,
+                     cudaStream_t st)
 {
     grt_ctx *ctx = m->ctx;
     const Layout &L = m->lo;
     const unsigned grid = (unsigned)((n + kThreads - 1) / kThreads);
     float *act = dT ? work : nullptr, *D = work + (size_t)n * 3 * H, *ls = D + (size_t)n * kDS;
     CUM(cudaFuncSetAttribute(mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fwd_smem(L)));
-    mlp_forward<<<grid, kThreads, fwd_smem(L), ctx->stream>>>(m->P, L.ni, L.no, n, dX, didx, dY, act);
+    mlp_forward<<<grid, kThreads, fwd_smem(L), st>>>(m->P, L.ni, L.no, n, dX, didx, dY, act);
     CUM(cudaGetLastError());
     if (dT) {
         CUM(cudaFuncSetAttribute(mlp_delta, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fwd_smem(L)));
-        mlp_delta<<<grid, kThreads, fwd_smem(L), ctx->stream>>>(m->P, L.ni, L.no, n, 1.f / ((float)n * L.no), dT,
+        mlp_delta<<<grid, kThreads, fwd_smem(L), st>>>(m->P, L.ni, L.no, n, 1.f / ((float)n * L.no), dT,
                                                                  didx, dY, act, D, ls);
         CUM(cudaGetLastError());
-        mlp_grad<<<(L.n + 1 + 127) / 128, 128, 0, ctx->stream>>>(L.ni, L.no, n, dX, didx, act, D, ls, m->G, m->loss);
+        mlp_grad<<<(L.n + 1 + 127) / 128, 128, 0, st>>>(L.ni, L.no, n, dX, didx, act, D, ls, m->G, m->loss);
         CUM(cudaGetLastError());
     }
     return GRT_OK;
@@ -341,14 +349,32 @@ extern "C" int grt_mlp_forward(grt_mlp *m, int n, const float *x, float *y)
 {
     if (!m || !x || !y || n < 1) return GRT_ERR_ARG;
     grt_ctx *ctx = m->ctx;
-    DevBufs b;
-    float *dX = (float *)b.get((size_t)n * m->lo.ni * sizeof(float)), *dY = (float *)b.get((size_t)n * m->lo.no * sizeof(float));
-    if (!dX || !dY) return mfail(ctx, GRT_ERR_NOMEM, "mlp forward buffers");
-    CUM(cudaMemcpyAsync(dX, x, (size_t)n * m->lo.ni * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
-    int rc = launch_fb(m, n, dX, nullptr, nullptr, dY, nullptr);
-    if (rc) return rc;
-    CUM(cudaMemcpyAsync(y, dY, (size_t)n * m->lo.no * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
-    CUM(cudaStreamSynchronize(ctx->stream));
+    CUM(cudaSetDevice(m->device));
+    cudaStream_t st = nullptr;
+    CUM(grt_setup_stream(ctx, &st));
+    const size_t nx = (size_t)n * m->lo.ni, ny = (size_t)n * m->lo.no;
+    if (nx > m->fx_n || ny > m->fy_n) {
+        CUM(cudaStreamSynchronize(st));
+        const size_t gx = std::max(nx, 2 * m->fx_n), gy = std::max(ny, 2 * m->fy_n);
+        cudaFree(m->fx);
+        cudaFree(m->fy);
+        m->fx = m->fy = nullptr;
+        m->fx_n = m->fy_n = 0;
+        if (cudaMalloc(&m->fx, gx * sizeof(float)) != cudaSuccess || cudaMalloc(&m->fy, gy * sizeof(float)) != cudaSuccess) {
+            cudaGetLastError();
+            return mfail(ctx, GRT_ERR_NOMEM, "mlp forward buffers");
+        }
+        m->fx_n = gx;
+        m->fy_n = gy;
+    }
+    CUM(cudaMemcpyAsync(m->fx, x, nx * sizeof(float), cudaMemcpyHostToDevice, st));
+    int rc = launch_fb(m, n, m->fx, nullptr, nullptr, m->fy, nullptr, st);
+    if (rc) {
+        cudaStreamSynchronize(st);
+        return rc;
+    }
+    CUM(cudaMemcpyAsync(y, m->fy, ny * sizeof(float), cudaMemcpyDeviceToHost, st));
+    CUM(cudaStreamSynchronize(st));
     return GRT_OK;
 }
 
@@ -363,7 +389,7 @@ extern "C" int grt_mlp_loss_grad(grt_mlp *m, int n, const float *x, const float 
     if (!dX || !dT || !dY || !dA) return mfail(ctx, GRT_ERR_NOMEM, "mlp gradient buffers");
     CUM(cudaMemcpyAsync(dX, x, (size_t)n * L.ni * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
     CUM(cudaMemcpyAsync(dT, t, (size_t)n * L.no * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
-    int rc = launch_fb(m, n, dX, dT, nullptr, dY, dA);
+    int rc = launch_fb(m, n, dX, dT, nullptr, dY, dA, ctx->stream);
     if (rc) return rc;
     if (loss) CUM(cudaMemcpyAsync(loss, m->loss, sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
     if (grad) CUM(cudaMemcpyAsync(grad, m->G, L.n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
@@ -398,7 +424,7 @@ extern "C" int grt_mlp_train(grt_mlp *m, int n, const float *x, const float *t, 
         CUM(cudaMemcpyAsync(dI, perm.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
         CUM(cudaStreamSynchronize(ctx->stream));
         for (int s0 = 0; s0 + batch <= n; s0 += batch) {
-            int rc = launch_fb(m, batch, dX, dT, dI + s0, dY, dA);
+            int rc = launch_fb(m, batch, dX, dT, dI + s0, dY, dA, ctx->stream);
             if (rc) return rc;
             m->step++;
             const float b1 = 0.9f, b2 = 0.999f;

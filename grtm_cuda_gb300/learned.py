@@ -31,6 +31,7 @@ import os
 import struct
 import threading
 import time
+import weakref
 
 import numpy as np
 
@@ -255,7 +256,7 @@ class Sampler:
             if e.ndim != 1 or mg.shape != (e.size - 1,) or e.size < 2 or np.any(np.diff(e) <= 0):
                 raise ValueError("kbands: edges [nb + 1] ascending and margins [nb]")
             self.kbands = (e, mg)
-        self._net = None
+        self._nets = {}
 
     def k_margin(self, log_w):
         """The k_max margin at log angular frequencies log_w."""
@@ -315,10 +316,18 @@ class Sampler:
         return cls(p, *arrs, margin_k=mk, margin_d=md, tol=tol, kbands=kb)
 
     def net(self, ctx):
-        if self._net is None or self._net.ctx is not ctx:
-            self._net = Mlp(ctx)
-            self._net.set_params(self.params)
-        return self._net
+        """The network on ctx's device, one per context (kept while the
+        context lives: building one allocates and uploads the weights, and
+        freeing one waits for the whole device)."""
+        for k in [k for k, (r, _) in self._nets.items() if r() is None or not r().h]:
+            self._nets.pop(k)[1].close()
+        e = self._nets.get(id(ctx))
+        if e is None or e[0]() is not ctx:
+            net = Mlp(ctx)
+            net.set_params(self.params)
+            self._nets[id(ctx)] = (weakref.ref(ctx), net)
+            return net
+        return e[1]
 
     def predict(self, ctx, x):
         """Un-standardised outputs (log k_max, log2 step multiple) for raw inputs."""
@@ -499,12 +508,176 @@ _JUDGE_CTX = {}
 
 def judge_context(ctx):
     """A second context on ctx's device for the judge's work, kept for the
-    process (its cached memory serves every later judge)."""
+    process (its cached memory serves every later judge).  Its streams have
+    the greatest priority: the judge's small kernels (its plans' set-up, the
+    spot sums, the sweeps) are scheduled ahead of the batch graph's pending
+    blocks instead of after each of its long kernels."""
     dev = getattr(ctx, "device", 0)
     jc = _JUDGE_CTX.get(dev)
     if jc is None or not jc.h:
-        jc = _JUDGE_CTX[dev] = Context(dev)
+        jc = Context(dev)
+        jc.set_priority(True)
+        _JUDGE_CTX[dev] = jc
     return jc
+
+
+class _LearnedBatch:
+    """One learned batch in stages: prepare (prediction, the batch and its
+    judge's spot jobs), start (the batch's graph in a host thread), judge_pre
+    (the judge's work that does not need the batch: the plain grid at the
+    spot frequencies and the tail sweeps, on the judge's context), join
+    (the graph done) and finish (the comparison, fallbacks, the info).
+    run_learned_batch runs them back to back; run_learned_stream interleaves
+    consecutive batches."""
+
+    def __init__(self, sampler, models, dists_list, ctx, plain, spec_tol, autotune, use_stride, out):
+        from . import Batch
+        self.sampler, self.plain, self.spec_tol, self.out = sampler, plain, spec_tol, out
+        self.ctx, self.dists_list = ctx, dists_list
+        self.t = [time.perf_counter()]
+        self.grids = [sampler.grid(ctx, m, d, plain, use_stride=use_stride) for m, d in zip(models, dists_list)]
+        self.t.append(time.perf_counter())
+        self.mods = [make_model(**m) for m in models]
+        jobs = [(mo, custom_opts(nk, gr["dk"], plain, k_stride=st), d)
+                for mo, (nk, st, _, gr), d in zip(self.mods, self.grids, dists_list)]
+        # with page-locked destinations the graph itself downloads each model's
+        # traces as soon as its stages finish, beside the next model's sums
+        # (downloads started after the graph held up the judge's own small
+        # copies behind them on the copy engine: 20 -> 83 ms of judge)
+        self.b = Batch(ctx, jobs, autotune=autotune, outs=out)
+        self.t.append(time.perf_counter())
+        self.spots = [judge_spots(gr["nw"], st) for (nk, st, kmax, gr) in self.grids]
+        self.spot_jobs = [(mo, spot_opts(gr["nw"], gr["dk"], sp, self.b.info(j)[0]["k_slice"], plain), d)
+                          for j, (mo, (nk, st, kmax, gr), d, sp) in
+                          enumerate(zip(self.mods, self.grids, dists_list, self.spots))]
+        self.done, self.runner, self.pre = {}, None, None
+        self.t_sw = self.t_ff = 0.0
+        self.n_judge_launches = 0
+
+    def _execute(self):
+        try:
+            self.done["rep"] = self.b.execute()
+        except BaseException as e:   # re-raised on the calling thread
+            self.done["exc"] = e
+        self.done["t"] = time.perf_counter()
+
+    def start(self, threaded=True):
+        self.t_start = time.perf_counter()
+        if threaded:
+            self.runner = threading.Thread(target=self._execute)
+            self.runner.start()
+        else:
+            self._execute()
+
+    def judge_pre(self, jctx):
+        """The judge's part that does not need the batch's spectra."""
+        self.tj = [time.perf_counter()]
+        from . import Batch
+        sb = Batch(jctx, self.spot_jobs, autotune=False)
+        self.tj.append(time.perf_counter())
+        self.n_judge_launches = sb.execute().kernel_launches
+        self.tj.append(time.perf_counter())
+        pre = []
+        try:
+            for j, (mo, (nk, st, kmax, gr), d) in enumerate(zip(self.mods, self.grids, self.dists_list)):
+                d = np.asarray(d, np.float64)
+                sp = self.spots[j]
+                bands = np.unique(np.array([d.min(), math.sqrt(d.min() * d.max()), d.max()]))
+                t_a = time.perf_counter()
+                sw = sweep_kmax(mo, plain_opts(self.plain), sp, bands, self.sampler.tol,
+                                k_judge=np.repeat(kmax[sp][:, None], len(bands), 1), ctx=jctx, env=True)
+                t_b = time.perf_counter()
+                w = np.maximum(taper_weight(sp, gr["nw"], self.plain["taper"]), 1e-6)[:, None]
+                excess = sw["tail"] * sw["env"] * w / (self.sampler.tol * sw["env"].max(0)[None, :])
+                s_plain = sb.fetch_freqs(j, sp)
+                self.t_sw += t_b - t_a
+                self.t_ff += time.perf_counter() - t_b
+                pre.append((d, bands, excess, s_plain))
+        finally:
+            sb.close()
+        self.pre = pre
+        self.t_pre = time.perf_counter()
+
+    def join(self):
+        """Wait for the graph's thread (always, before anything of the batch's
+        context may be used again); re-raise its error."""
+        if self.runner is not None:
+            self.runner.join()
+            self.runner = None
+        if "exc" in self.done:
+            raise self.done["exc"]
+        self.t_exec = self.done["t"]
+
+    def finish(self, overlap):
+        b, ctx = self.b, self.ctx
+        t = self.t
+        rep = self.done["rep"]
+        traces = list(self.out) if self.out is not None else [b.fetch_f32(j) for j in range(len(self.mods))]
+        t.append(time.perf_counter())
+        # judge, the part that needs the batch: each receiver's spectra at the
+        # spot frequencies against the plain grid's
+        t_c = time.perf_counter()
+        n_fb = 0
+        fallback = []
+        for j, (d, bands, excess, s_plain) in enumerate(self.pre):
+            sp = self.spots[j]
+            t_a = time.perf_counter()
+            s_learn = b.fetch_freqs(j, sp)
+            self.t_ff += time.perf_counter() - t_a
+            _, bad = spectral_verdict(s_learn, s_plain, self.spec_tol)
+            below = np.clip(np.searchsorted(bands, d * (1 + 1e-12), side="right") - 1, 0, len(bands) - 1)
+            bad |= (excess.max(0) > 10.0)[below]
+            fallback.append(np.nonzero(bad)[0].tolist())
+            n_fb += int(bad.sum())
+        tj = self.tj
+        tj.append(time.perf_counter())
+        t_wait = time.perf_counter()
+        b.wait()
+        t.append(time.perf_counter())
+        for j, idx in enumerate(fallback):
+            if idx:
+                p = Plan(ctx, self.mods[j], plain_opts(self.plain), np.asarray(self.dists_list[j], np.float64)[idx])
+                p.execute()
+                traces[j][idx] = p.fetch(True, False)[0].astype(np.float32)
+                p.close()
+        t.append(time.perf_counter())
+        _, tune = b.info()
+        grids, t_exec, t_pre = self.grids, self.t_exec, self.t_pre
+        # the judge's time beyond the graph: its part before the graph ended
+        # (when it outlasted the graph) and its part after
+        exposed_pre = max(0.0, t_pre - t_exec) if overlap else t_pre - tj[0]
+        info = dict(nkw_learned=int(sum(int(g_[0].sum()) for g_ in grids)),
+                    nkw_plain=int(sum(int(g_[3]["nw"]) * self.plain["nk"] for g_ in grids)),
+                    stride_mean=float(np.mean([g_[1].mean() for g_ in grids])), fallback=fallback,
+                    n_fallback=n_fb, ms_batch_gpu=rep.ms_total, ms_batch_grt=rep.ms_grt,
+                    n_layer_evals=int(rep.n_layer_evals),
+                    gpu_launches=rep.kernel_launches,
+                    # the judge's: its spot batch, per model a sweep (GRT and sweep kernels) and two gathers
+                    judge_launches=int(self.n_judge_launches) + 4 * len(self.mods), tune=tune,
+                    s_predict=t[1] - t[0], s_build=t[2] - t[1],
+                    s_execute=t[3] - t[2], s_fetch=t[3] - t_exec, s_fetch_wait=t[4] - t_wait,
+                    s_judge=exposed_pre + (t_wait - t_c), s_fallback=t[5] - t[4],
+                    s_total=t[5] - t[0], judge_overlapped=bool(overlap),
+                    s_judge_parts=dict(spot_build=tj[1] - tj[0], spot_exec=tj[2] - tj[1],
+                                       sweeps_compare=(t_pre - tj[2]) + (tj[3] - t_c), sweeps=self.t_sw,
+                                       fetch_spots=self.t_ff, before_graph_end=max(0.0, t_exec - tj[0]) if overlap
+                                       else 0.0, total=(t_pre - tj[0]) + (t_wait - t_c)))
+        t_close = time.perf_counter()
+        b.close()
+        info["s_close"] = time.perf_counter() - t_close
+        info["s_graph_call"] = t_exec - self.t_start   # the batch's execute call (graph launch to results)
+        info["t_graph_start"], info["t_graph_end"] = self.t_start, t_exec
+        info["s_call"] = time.perf_counter() - t[0]
+        return traces, info
+
+    def abandon(self):
+        """After an error: the graph's thread ends before the batch goes."""
+        try:
+            if self.runner is not None:
+                self.runner.join()
+                self.runner = None
+        finally:
+            self.b.close()
 
 
 def run_learned_batch(sampler, models, dists_list, ctx=None, plain=PLAIN, spec_tol=3e-3, autotune=True,
@@ -525,124 +698,72 @@ def run_learned_batch(sampler, models, dists_list, ctx=None, plain=PLAIN, spec_t
     own = ctx is None
     ctx = ctx or Context()
     try:
-        from . import Batch
-        t = [time.perf_counter()]
-        grids = [sampler.grid(ctx, m, d, plain, use_stride=use_stride) for m, d in zip(models, dists_list)]
-        t.append(time.perf_counter())
-        mods = [make_model(**m) for m in models]
-        jobs = [(mo, custom_opts(nk, gr["dk"], plain, k_stride=st), d)
-                for mo, (nk, st, _, gr), d in zip(mods, grids, dists_list)]
-        # with page-locked destinations the graph itself downloads each model's
-        # traces as soon as its stages finish, beside the next model's sums
-        # (downloads started after the graph held up the judge's own small
-        # copies behind them on the copy engine: 20 -> 83 ms of judge)
-        b = Batch(ctx, jobs, autotune=autotune, outs=out)
-        t.append(time.perf_counter())
-        spots = [judge_spots(gr["nw"], st) for (nk, st, kmax, gr) in grids]
-        spot_jobs = [(mo, spot_opts(gr["nw"], gr["dk"], sp, b.info(j)[0]["k_slice"], plain), d)
-                     for j, (mo, (nk, st, kmax, gr), d, sp) in enumerate(zip(mods, grids, dists_list, spots))]
-        done = {}
-
-        def execute():
-            try:
-                done["rep"] = b.execute()
-            except BaseException as e:   # re-raised on the calling thread
-                done["exc"] = e
-            done["t"] = time.perf_counter()
-
-        jctx = judge_context(ctx) if overlap else ctx
-        runner = None
-        if overlap:
-            runner = threading.Thread(target=execute)
-            runner.start()
-        else:
-            execute()
-            t_exec = done["t"]
-        # judge, the part that does not need the batch: spot frequencies on the
-        # plain grid (batched), tails by sweep
-        tj = [time.perf_counter()]
-        t_sw = t_ff = 0.0
-        pre = []
-        n_judge_launches = 0
+        lb = _LearnedBatch(sampler, models, dists_list, ctx, plain, spec_tol, autotune, use_stride, out)
         try:
-            sb = Batch(jctx, spot_jobs, autotune=False)
-            tj.append(time.perf_counter())
-            n_judge_launches = sb.execute().kernel_launches
-            tj.append(time.perf_counter())
-            for j, (mo, (nk, st, kmax, gr), d) in enumerate(zip(mods, grids, dists_list)):
-                d = np.asarray(d, np.float64)
-                sp = spots[j]
-                bands = np.unique(np.array([d.min(), math.sqrt(d.min() * d.max()), d.max()]))
-                t_a = time.perf_counter()
-                sw = sweep_kmax(mo, plain_opts(plain), sp, bands, sampler.tol,
-                                k_judge=np.repeat(kmax[sp][:, None], len(bands), 1), ctx=jctx, env=True)
-                t_b = time.perf_counter()
-                w = np.maximum(taper_weight(sp, gr["nw"], plain["taper"]), 1e-6)[:, None]
-                excess = sw["tail"] * sw["env"] * w / (sampler.tol * sw["env"].max(0)[None, :])
-                s_plain = sb.fetch_freqs(j, sp)
-                t_sw += t_b - t_a
-                t_ff += time.perf_counter() - t_b
-                pre.append((d, bands, excess, s_plain))
-            sb.close()
-            t_pre = time.perf_counter()
-        finally:
-            # the graph's thread ends before anything of this context may go
-            if runner is not None:
-                runner.join()
-        if runner is not None:
-            t_exec = done["t"]
-        if "exc" in done:
-            raise done["exc"]
-        rep = done["rep"]
-        traces = list(out) if out is not None else [b.fetch_f32(j) for j in range(len(jobs))]
-        t.append(time.perf_counter())
-        # judge, the part that needs the batch: each receiver's spectra at the
-        # spot frequencies against the plain grid's
-        t_c = time.perf_counter()
-        n_fb = 0
-        fallback = []
-        for j, (d, bands, excess, s_plain) in enumerate(pre):
-            sp = spots[j]
-            t_a = time.perf_counter()
-            s_learn = b.fetch_freqs(j, sp)
-            t_ff += time.perf_counter() - t_a
-            _, bad = spectral_verdict(s_learn, s_plain, spec_tol)
-            below = np.clip(np.searchsorted(bands, d * (1 + 1e-12), side="right") - 1, 0, len(bands) - 1)
-            bad |= (excess.max(0) > 10.0)[below]
-            fallback.append(np.nonzero(bad)[0].tolist())
-            n_fb += int(bad.sum())
-        tj.append(time.perf_counter())
-        t_wait = time.perf_counter()
-        b.wait()
-        t.append(time.perf_counter())
-        for j, idx in enumerate(fallback):
-            if idx:
-                p = Plan(ctx, mods[j], plain_opts(plain), np.asarray(dists_list[j], np.float64)[idx])
-                p.execute()
-                traces[j][idx] = p.fetch(True, False)[0].astype(np.float32)
-                p.close()
-        t.append(time.perf_counter())
-        _, tune = b.info()
-        # the judge's time beyond the graph: its part before the graph ended
-        # (when it outlasted the graph) and its part after
-        exposed_pre = max(0.0, t_pre - t_exec) if overlap else t_pre - tj[0]
-        info = dict(nkw_learned=int(sum(int(g_[0].sum()) for g_ in grids)),
-                    nkw_plain=int(sum(int(g_[3]["nw"]) * plain["nk"] for g_ in grids)),
-                    stride_mean=float(np.mean([g_[1].mean() for g_ in grids])), fallback=fallback,
-                    n_fallback=n_fb, ms_batch_gpu=rep.ms_total, ms_batch_grt=rep.ms_grt,
-                    n_layer_evals=int(rep.n_layer_evals),
-                    gpu_launches=rep.kernel_launches,
-                    # the judge's: its spot batch, per model a sweep (GRT and sweep kernels) and two gathers
-                    judge_launches=int(n_judge_launches) + 4 * len(models), tune=tune, s_predict=t[1] - t[0], s_build=t[2] - t[1],
-                    s_execute=t[3] - t[2], s_fetch=t[3] - t_exec, s_fetch_wait=t[4] - t_wait,
-                    s_judge=exposed_pre + (t_wait - t_c), s_fallback=t[5] - t[4],
-                    s_total=t[5] - t[0], judge_overlapped=bool(overlap),
-                    s_judge_parts=dict(spot_build=tj[1] - tj[0], spot_exec=tj[2] - tj[1],
-                                       sweeps_compare=(t_pre - tj[2]) + (tj[3] - t_c), sweeps=t_sw,
-                                       fetch_spots=t_ff, before_graph_end=max(0.0, t_exec - tj[0]) if overlap
-                                       else 0.0, total=(t_pre - tj[0]) + (t_wait - t_c)))
-        b.close()
-        return traces, info
+            lb.start(threaded=overlap)
+            lb.judge_pre(judge_context(ctx) if overlap else ctx)
+        except BaseException:
+            lb.abandon()
+            raise
+        try:
+            lb.join()
+        except BaseException:
+            lb.abandon()
+            raise
+        return lb.finish(overlap)
     finally:
         if own:
             ctx.close()
+
+
+def run_learned_stream(sampler, work, ctxs, outs=None, plain=PLAIN, spec_tol=3e-3, autotune=True,
+                       use_stride=True):
+    """run_learned_batch over a sequence of batches, pipelined: while batch
+    i's graph runs, batch i+1 is predicted and built and its judge's own GPU
+    work runs; batch i+1's graph starts as soon as batch i's ends, and batch
+    i's comparison, fallbacks and clean-up run beside it.  Yields
+    (traces, info) per batch, in order.
+
+    work: iterable of (models, dists_list); ctxs: two contexts on one device
+    (consecutive batches alternate between them: a context is used by one
+    host thread at a time); outs: optional pair of per-model page-locked
+    output lists, alternating the same way (the graph of batch i+2 writes
+    into batch i's arrays: use or copy a batch's traces before asking for
+    the next batch)."""
+    if len(ctxs) != 2:
+        raise ValueError("run_learned_stream needs two contexts")
+    jctx = judge_context(ctxs[0])
+    it = iter(work)
+
+    def make(i, item):
+        models, dists_list = item
+        out = outs[i % 2] if outs is not None else None
+        return _LearnedBatch(sampler, models, dists_list, ctxs[i % 2], plain, spec_tol, autotune, use_stride, out)
+
+    item = next(it, None)
+    if item is None:
+        return
+    cur, i = make(0, item), 0
+    nxt = None
+    try:
+        cur.start()
+        cur.judge_pre(jctx)
+        while cur is not None:
+            item = next(it, None)
+            nxt = make(i + 1, item) if item is not None else None
+            if nxt is not None:
+                nxt.judge_pre(jctx)
+            cur.join()
+            if nxt is not None:
+                nxt.start()
+            res = cur.finish(True)
+            cur, nxt, i = nxt, None, i + 1
+            yield res
+    except BaseException:
+        for lb in (cur, nxt):
+            if lb is not None:
+                try:
+                    lb.abandon()
+                except Exception:
+                    pass
+        raise

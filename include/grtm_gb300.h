@@ -137,6 +137,15 @@ GRT_API int grt_create(grt_ctx **ctx, int device);
 GRT_API void grt_destroy(grt_ctx *ctx);
 /* Return the context's cached device memory to the driver. */
 GRT_API void grt_trim(grt_ctx *ctx);
+/* high != 0: the context's streams (its own and those of the batches made on
+ * it afterwards) take the device's greatest stream priority, so its kernels'
+ * blocks are scheduled ahead of other contexts' pending blocks (a small job
+ * beside a long batch on another context); 0: the default priority.  Only
+ * while the context holds no plan or batch (GRT_ERR_ARG otherwise). */
+GRT_API int grt_set_priority(grt_ctx *ctx, int high);
+/* Wait for all work the process queued on a device (every context's streams):
+ * cudaDeviceSynchronize, for callers that hold no CUDA runtime of their own. */
+GRT_API int grt_device_synchronize(int device);
 GRT_API const char *grt_last_error(const grt_ctx *ctx);
 GRT_API const char *grt_status_string(int status);
 
@@ -229,7 +238,8 @@ typedef struct grt_job {
 #define GRT_TUNE_MAX 16
 typedef struct grt_tune {
     int tuned;                     /* 1: picked by timing; 2: reused from an earlier batch of the
-                                    * same precision and deepest model on this context; 0: default */
+                                    * same precision and deepest model on this device (any context of
+                                    * the process); 0: default */
     int grt_shape;                 /* chosen GRT launch: 0-2 one block per tile of 64/128/256
                                     * wavenumbers, 3-4 persistent with 128/256 threads */
     int grt_threads, grt_blocks;   /* its threads per block; persistent grid (0: one per tile) */
@@ -264,6 +274,10 @@ GRT_API int grt_batch_wait(grt_batch *batch);
 GRT_API int grt_batch_fetch_freqs(grt_batch *batch, int job, int n_freq, const int *freq_idx, double *spectra);
 /* job = -1: the batch's aggregate report */
 GRT_API int grt_batch_info(const grt_batch *batch, int job, grt_report *report, grt_tune *tune);
+/* Forget the autotuner's choices (kept per device for the process, shared by
+ * its contexts): the next autotuned batch of each kind times its candidates
+ * again. */
+GRT_API void grt_tune_clear(void);
 GRT_API void grt_batch_destroy(grt_batch *batch);
 
 /* Binary output of a plan's traces (beside the reference's %.18e text,

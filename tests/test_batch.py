@@ -32,6 +32,7 @@ def ctx():
 def test_batch_equals_single_jobs(ctx, prec):
     import grtm_cuda_gb300 as g
     jobs = _jobs(g, g.FP32 if prec == "fp32" else g.FP64)
+    g.lib().grt_tune_clear()                           # the choices are kept per device for the process
     b = g.Batch(ctx, jobs, autotune=(prec == "fp32"))
     rep = b.execute()
     assert rep.n_wk == sum(g.grid(m, o)["n_wk"] for m, o, _ in jobs)
@@ -56,14 +57,16 @@ def test_batch_equals_single_jobs(ctx, prec):
         assert tune["tc_tuned"] == 1 and len(tune["tc_candidates"]) >= 2
         best = min(tune["tc_candidates"], key=lambda c: c[1])
         assert tune["tc_nsplit"] == best[0]
-        # a second batch of the same kind on this context reuses the shape
-        b2 = g.Batch(ctx, jobs, autotune=True)
+        # a second batch of the same kind, on another context of this device, reuses the shape
+        c2 = g.Context()
+        b2 = g.Batch(c2, jobs, autotune=True)
         _, t2 = b2.info()
         assert t2["tuned"] == 2 and (t2["grt_threads"], t2["grt_blocks"]) == (tune["grt_threads"], tune["grt_blocks"])
         assert t2["tc_tuned"] == 2 and t2["tc_nsplit"] == tune["tc_nsplit"]
         b2.execute()
         assert np.array_equal(b2.fetch(0)[0], first[0])
         b2.close()
+        c2.close()
     b.close()
 
 

@@ -275,6 +275,42 @@ def test_learned_batch_judge_overlap(ctx):
 
 
 @pytest.mark.gpu
+def test_learned_stream_matches_batches(ctx):
+    """The pipelined stream (batch i+1 predicted, built and judged beside
+    batch i's graph; two contexts alternating) gives every batch the traces
+    and verdicts of run_learned_batch, with and without page-locked outputs
+    written by the graphs."""
+    import grtm_cuda_gb300 as g
+    from grtm_cuda_gb300 import learned
+    if not os.path.exists(learned.WEIGHTS):
+        pytest.skip("no trained sampler in the tree")
+    s = learned.Sampler.load()
+    work = [([m], [d]) for m, d in (_learned_case(3007, 6), _learned_case(3011, 5), _learned_case(3013, 4))]
+    ref = [learned.run_learned_batch(s, ms, ds, ctx=ctx, autotune=False) for ms, ds in work]
+    c1 = g.Context()
+    try:
+        n = 0
+        for (tr, info), (rt, ri) in zip(learned.run_learned_stream(s, work, (ctx, c1), autotune=False), ref):
+            assert np.array_equal(tr[0], rt[0])
+            assert info["fallback"] == ri["fallback"] and info["nkw_learned"] == ri["nkw_learned"]
+            n += 1
+        assert n == len(work)
+        # one batch repeated into two alternating sets of page-locked outputs
+        ms, ds = work[0]
+        gr = g.grid(g.make_model(**ms[0]), learned.plain_opts())
+        outs = tuple([g.pinned_empty((len(ds[0]), gr["n_cols"], gr["n_samples"]))] for _ in range(2))
+        got = [np.array(tr[0]) for tr, _ in learned.run_learned_stream(s, [work[0]] * 3, (ctx, c1), outs=outs,
+                                                                         autotune=False)]
+        assert len(got) == 3
+        for t in got:
+            assert np.array_equal(t, ref[0][0][0])
+        assert learned.run_learned_stream(s, [], (ctx, c1)) is not None
+        assert list(learned.run_learned_stream(s, [], (ctx, c1))) == []
+    finally:
+        c1.close()
+
+
+@pytest.mark.gpu
 def test_learned_path_gain_and_accuracy(ctx):
     """On a held-out model the trained sampler evaluates far fewer (w,k)
     points than the plain fixed grid and stays within 1e-3 of FP64."""
