@@ -47,6 +47,7 @@ def test_priority_context_gives_identical_results():
         c1.set_priority(False)
         t2, _, _ = g.run(m, o, d, c1)
         assert np.array_equal(t2, t0)
+        assert g.lib().grt_device_synchronize(0) == g.OK
     finally:
         c1.close()
         c0.close()
