@@ -97,8 +97,10 @@ static int set_err(grt_ctx *ctx, int code, const std::string &msg)
 // and handed to the next request of a similar size, so a plan or batch made
 // per call pays neither cudaMalloc's page mapping nor cudaFree's device-wide
 // synchronisation.  All work on a context's memory is ordered on its stream
-// (batch graphs join their side streams back into it), so a block is reused
-// only by work queued after the work that last used it.
+// (batch graphs join their side streams back into it; the auxiliary stream's
+// set-up and fetch work is queued after it by an event and synchronised by the
+// host before the call returns), so a block is reused only by work queued
+// after the work that last used it.
 static size_t pool_round(size_t n)
 {
     const size_t g = n < ((size_t)1 << 20) ? 256 : ((size_t)2 << 20);
