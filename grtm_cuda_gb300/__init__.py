@@ -192,7 +192,8 @@ EXPORTS = ("grt_create", "grt_destroy", "grt_last_error", "grt_status_string", "
            "grt_batch_synth", "grt_flatten", "grt_plan_write", "grt_plan_fetch_f32", "grt_batch_fetch_f32",
            "grt_host_alloc", "grt_host_free", "grt_trim", "grt_batch_fetch_f32_async", "grt_batch_wait",
            "grt_plan_error_estimate", "grt_batch_error_estimate", "grt_set_priority",
-           "grt_tune_clear", "grt_device_synchronize")
+           "grt_tune_clear", "grt_device_synchronize", "grt_batch_launch", "grt_batch_wait_stages",
+           "grt_batch_finish")
 
 _lib = None
 
@@ -248,6 +249,7 @@ def lib():
                                 ctypes.c_ulonglong, fp]
     L.grt_batch_create.argtypes = [vp, ctypes.c_int, P(Job), ctypes.c_int, P(vp)]
     L.grt_batch_execute.argtypes = [vp, P(Report)]
+    L.grt_batch_finish.argtypes = [vp, P(Report)]
     L.grt_batch_fetch.argtypes = [vp, ctypes.c_int, _dp, _dp]
     L.grt_batch_fetch_freqs.argtypes = [vp, ctypes.c_int, ctypes.c_int, ip, _dp]
     L.grt_batch_info.argtypes = [vp, ctypes.c_int, P(Report), P(Tune)]
@@ -266,6 +268,8 @@ def lib():
     L.grt_set_priority.argtypes = [vp, ctypes.c_int]
     L.grt_tune_clear.argtypes = []
     L.grt_device_synchronize.argtypes = [ctypes.c_int]
+    L.grt_batch_launch.argtypes = [vp]
+    L.grt_batch_wait_stages.argtypes = [vp]
     L.grt_tune_clear.restype = None
     L.grt_flatten.argtypes = [ctypes.c_int, _dp, _dp, _dp, ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp,
                               _dp, _dp, _dp, _dp]
@@ -523,6 +527,27 @@ class Batch:
 
     def execute(self):
         rc = lib().grt_batch_execute(self.h, ctypes.byref(self.report))
+        if rc:
+            raise GrtError(rc, self.ctx.error())
+        return self.report
+
+    def launch(self):
+        """execute() in three steps (grt_batch_launch, grt_batch_wait_stages,
+        grt_batch_finish): start the graph."""
+        rc = lib().grt_batch_launch(self.h)
+        if rc:
+            raise GrtError(rc, self.ctx.error())
+
+    def wait_stages(self):
+        """Block until every job's device stages are done; the last job's
+        download into its out array is then still draining."""
+        rc = lib().grt_batch_wait_stages(self.h)
+        if rc:
+            raise GrtError(rc, self.ctx.error())
+
+    def finish(self):
+        """Wait for the last download; the execution's report."""
+        rc = lib().grt_batch_finish(self.h, ctypes.byref(self.report))
         if rc:
             raise GrtError(rc, self.ctx.error())
         return self.report

@@ -1696,6 +1696,7 @@ struct grt_batch {
     cudaEvent_t fork0 = nullptr, fork1 = nullptr, join[kSide] = {};         // dependencies between streams
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    bool launched = false, staged = false;   // grt_batch_launch / grt_batch_wait_stages done
     grt_tune tune{};
     grt_report rep{};
 };
@@ -1705,6 +1706,7 @@ extern "C" void grt_batch_destroy(grt_batch *b)
     if (!b) return;
     cudaSetDevice(b->ctx->device);
     cudaStreamSynchronize(b->ctx->aux);   // set-up left in flight by a failed creation
+    if (b->launched) cudaStreamSynchronize(b->ctx->stream);   // a launch never waited for
     if (b->copy) {
         cudaStreamSynchronize(b->copy);
         cudaStreamDestroy(b->copy);
@@ -1977,7 +1979,9 @@ static int batch_record(grt_batch *b, cudaStream_t st)
             grt_plan *p = b->jobs[j];
             if ((rc = launch_ksum<R>(p, b->side[0], launches))) return rc;
             if ((rc = launch_spectral<R>(p, b->side[0], launches))) return rc;
-            if (b->outs[j]) {
+            // the last job's download follows the graph (grt_batch_wait_stages):
+            // a caller may start its next work while it drains
+            if (b->outs[j] && j + 1 < b->jobs.size()) {
                 cudaStream_t cs = b->side[1 + j % (kSide - 1)];
                 CU(cudaEventRecord(b->done[j], b->side[0]));
                 CU(cudaStreamWaitEvent(cs, b->done[j], 0));
@@ -2152,14 +2156,45 @@ extern "C" int grt_batch_create(grt_ctx *ctx, int n_jobs, const grt_job *jobs, i
     return GRT_OK;
 }
 
-extern "C" int grt_batch_execute(grt_batch *b, grt_report *r)
+extern "C" int grt_batch_launch(grt_batch *b)
 {
     if (!b) return GRT_ERR_ARG;
     grt_ctx *ctx = b->ctx;
     CU(cudaSetDevice(ctx->device));
+    if (b->launched) CU(cudaStreamSynchronize(ctx->stream));   // an execution left unfinished
+    b->launched = b->staged = false;
     CU(cudaStreamSynchronize(b->copy));     // downloads of the previous results are done
     CU(cudaGraphLaunch(b->exec, ctx->stream));
-    CU(cudaStreamSynchronize(ctx->stream));  // the graph, in-graph downloads included
+    b->launched = true;
+    return GRT_OK;
+}
+
+extern "C" int grt_batch_wait_stages(grt_batch *b)
+{
+    if (!b) return GRT_ERR_ARG;
+    grt_ctx *ctx = b->ctx;
+    if (!b->launched) return set_err(ctx, GRT_ERR_ARG, "grt_batch_wait_stages: no launch pending");
+    CU(cudaSetDevice(ctx->device));
+    CU(cudaStreamSynchronize(ctx->stream));  // the graph, its in-graph downloads included
+    b->launched = false;
+    const size_t last = b->jobs.size() - 1;
+    if (b->outs[last]) {
+        const grt_plan *p = b->jobs[last];
+        CU(cudaMemcpyAsync(b->outs[last], p->sig, (size_t)p->nd * p->nc * p->J.N * sizeof(float),
+                           cudaMemcpyDeviceToHost, b->copy));
+    }
+    b->staged = true;
+    return GRT_OK;
+}
+
+extern "C" int grt_batch_finish(grt_batch *b, grt_report *r)
+{
+    if (!b) return GRT_ERR_ARG;
+    grt_ctx *ctx = b->ctx;
+    if (!b->staged) return set_err(ctx, GRT_ERR_ARG, "grt_batch_finish: grt_batch_wait_stages has not returned");
+    CU(cudaSetDevice(ctx->device));
+    CU(cudaStreamSynchronize(b->copy));      // the last job's download
+    b->staged = false;
     int rc = check_device_error(ctx, b->derr);
     if (rc) return rc;
     float t_grt = 0.f, t_all = 0.f;
@@ -2186,6 +2221,14 @@ extern "C" int grt_batch_execute(grt_batch *b, grt_report *r)
     b->rep.ksum_impl = b->jobs[0]->use_tc;
     if (r) *r = b->rep;
     return GRT_OK;
+}
+
+extern "C" int grt_batch_execute(grt_batch *b, grt_report *r)
+{
+    int rc = grt_batch_launch(b);
+    if (!rc) rc = grt_batch_wait_stages(b);
+    if (!rc) rc = grt_batch_finish(b, r);
+    return rc;
 }
 
 extern "C" int grt_batch_fetch(grt_batch *b, int job, double *traces, double *spectra)

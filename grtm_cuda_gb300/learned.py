@@ -555,14 +555,31 @@ class _LearnedBatch:
         self.n_judge_launches = 0
 
     def _execute(self):
+        # the batch's execute in its three steps; `staged` is set once the
+        # device stages are done (the last model's download then drains
+        # beside whatever the caller starts next), or when a step failed
         try:
-            self.done["rep"] = self.b.execute()
+            self.b.launch()
+            self.b.wait_stages()
+            self.done["t_staged"] = time.perf_counter()
+            self.staged.set()
+            self.done["rep"] = self.b.finish()
         except BaseException as e:   # re-raised on the calling thread
             self.done["exc"] = e
+        finally:
+            self.staged.set()
         self.done["t"] = time.perf_counter()
+
+    def wait_stages(self):
+        """Block until the batch's device stages are done (its graph thread
+        may still be waiting for the last download)."""
+        self.staged.wait()
+        if "exc" in self.done:
+            self.join()
 
     def start(self, threaded=True):
         self.t_start = time.perf_counter()
+        self.staged = threading.Event()
         if threaded:
             self.runner = threading.Thread(target=self._execute)
             self.runner.start()
@@ -666,7 +683,7 @@ class _LearnedBatch:
         b.close()
         info["s_close"] = time.perf_counter() - t_close
         info["s_graph_call"] = t_exec - self.t_start   # the batch's execute call (graph launch to results)
-        info["t_graph_start"], info["t_graph_end"] = self.t_start, t_exec
+        info["t_graph_start"], info["t_graph_end"] = self.t_start, self.done.get("t_staged", t_exec)
         info["s_call"] = time.perf_counter() - t[0]
         return traces, info
 
@@ -753,9 +770,10 @@ def run_learned_stream(sampler, work, ctxs, outs=None, plain=PLAIN, spec_tol=3e-
             nxt = make(i + 1, item) if item is not None else None
             if nxt is not None:
                 nxt.judge_pre(jctx)
-            cur.join()
+            cur.wait_stages()
             if nxt is not None:
                 nxt.start()
+            cur.join()
             res = cur.finish(True)
             cur, nxt, i = nxt, None, i + 1
             yield res

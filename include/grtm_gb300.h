@@ -261,6 +261,17 @@ typedef struct grt_batch grt_batch;
 GRT_API int grt_batch_create(grt_ctx *ctx, int n_jobs, const grt_job *jobs, int autotune, grt_batch **batch);
 /* report: aggregate (n_wk, bytes, launches; ms_grt and ms_total of the graph) */
 GRT_API int grt_batch_execute(grt_batch *batch, grt_report *report);
+/* grt_batch_execute in three steps, for callers that overlap consecutive
+ * batches: grt_batch_launch starts the graph and returns; grt_batch_wait_stages
+ * returns once every job's device stages are done (the traces of all jobs but
+ * the last one already downloaded into their out_f32 destinations; the last
+ * job's download is started on the batch's copy stream), so that the caller
+ * can launch its next batch while that download drains; grt_batch_finish
+ * waits for it, checks the device error word and fills the report.  Call
+ * them in this order, once each per execution. */
+GRT_API int grt_batch_launch(grt_batch *batch);
+GRT_API int grt_batch_wait_stages(grt_batch *batch);
+GRT_API int grt_batch_finish(grt_batch *batch, grt_report *report);
 GRT_API int grt_batch_fetch(grt_batch *batch, int job, double *traces, double *spectra);
 GRT_API int grt_batch_fetch_f32(grt_batch *batch, int job, float *traces);
 /* The same without waiting (FP32 batches): the copy of the last execute's

@@ -161,6 +161,42 @@ def test_in_graph_downloads(ctx):
 
 
 @pytest.mark.gpu
+def test_batch_execute_in_steps(ctx):
+    """grt_batch_launch / grt_batch_wait_stages / grt_batch_finish give the
+    traces and device time of grt_batch_execute (the last job's download
+    drains between the last two steps); out of order they are refused."""
+    import grtm_cuda_gb300 as g
+    jobs = _jobs(g, g.FP32)
+    b = g.Batch(ctx, jobs, autotune=False)
+    b.execute()
+    ref = [b.fetch_f32(j) for j in range(len(jobs))]
+    b.close()
+    outs = [g.pinned_empty(r.shape) for r in ref]
+    b = g.Batch(ctx, jobs, autotune=False, outs=outs)
+    try:
+        for o in outs:
+            o[...] = -1.0
+        with pytest.raises(g.GrtError) as e:
+            b.wait_stages()
+        assert e.value.status == g.ERR_ARG
+        b.launch()
+        with pytest.raises(g.GrtError):
+            b.finish()
+        b.wait_stages()
+        r = b.finish()
+        assert r.ms_total > 0 and r.ms_grt > 0
+        for j, o in enumerate(outs):
+            assert np.array_equal(o, ref[j])
+        for o in outs:
+            o[...] = -1.0
+        b.execute()                                  # the one-call form after the steps
+        for j, o in enumerate(outs):
+            assert np.array_equal(o, ref[j])
+    finally:
+        b.close()
+
+
+@pytest.mark.gpu
 def test_mixed_batch_runs_each_form(ctx):
     """A batch whose jobs do not all allow the specialised (two-pass) GRT form:
     those that do run it, the others (a receiver below the source's layer, a
