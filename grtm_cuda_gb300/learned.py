@@ -737,8 +737,9 @@ def run_learned_stream(sampler, work, ctxs, outs=None, plain=PLAIN, spec_tol=3e-
                        use_stride=True):
     """run_learned_batch over a sequence of batches, pipelined: while batch
     i's graph runs, batch i+1 is predicted and built and its judge's own GPU
-    work runs; batch i+1's graph starts as soon as batch i's ends, and batch
-    i's comparison, fallbacks and clean-up run beside it.  Yields
+    work runs; batch i+1's graph starts as soon as batch i's device stages
+    end (batch i's last download drains beside it), and batch i's
+    comparison, fallbacks and clean-up run beside it.  Yields
     (traces, info) per batch, in order.
 
     work: iterable of (models, dists_list); ctxs: two contexts on one device
