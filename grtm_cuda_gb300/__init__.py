@@ -64,15 +64,24 @@ class Report(ctypes.Structure):
 
 
 class Source(ctypes.Structure):
-    _fields_ = [("m", ctypes.c_double * 6), ("n_stf", ctypes.c_int), ("stf", _dp)]
+    _fields_ = [("m", ctypes.c_double * 6), ("n_stf", ctypes.c_int), ("stf", _dp), ("f", ctypes.c_double * 3)]
 
 
 def make_source(m6, stf=None):
-    """A moment-tensor source (Mxx, Myy, Mzz, Mxy, Mxz, Myz) with an optional
-    source-time function sampled at the job's dt."""
+    """A source with an optional source-time function sampled at the job's
+    dt: a moment tensor (Mxx, Myy, Mzz, Mxy, Mxz, Myz) for moment-tensor
+    jobs, or a force (Fx, Fy, Fz; x north, y east, z down) for single-force
+    jobs."""
     s = Source()
-    for i in range(6):
-        s.m[i] = float(m6[i])
+    v = np.asarray(m6, dtype=np.float64).ravel()
+    if v.size == 3:
+        for i in range(3):
+            s.f[i] = float(v[i])
+    elif v.size == 6:
+        for i in range(6):
+            s.m[i] = float(v[i])
+    else:
+        raise ValueError("a source is a moment tensor (6 values) or a force (3 values)")
     if stf is not None:
         a = _arr(stf)
         s.n_stf = len(a)
@@ -411,8 +420,9 @@ class Plan:
             raise GrtError(rc, self.ctx.error())
 
     def synth(self, m6, azimuth, stf=None):
-        """Seismograms [n_dist, 3 (Z, R, T), N] for moment tensor m6 at the
-        receivers' azimuths (degrees), convolved with stf (samples at dt)."""
+        """Seismograms [n_dist, 3 (Z, R, T), N] for moment tensor m6 (or, for
+        a single-force job, a force of 3 components) at the receivers'
+        azimuths (degrees), convolved with stf (samples at dt)."""
         src = make_source(m6, stf)
         az = _arr(np.broadcast_to(azimuth, self.dists.shape))
         out = np.empty((len(self.dists), 3, self.report.n_samples))

@@ -2337,6 +2337,15 @@ static int synth(grt_plan *p, const grt_source *src, const double *azimuth, doub
     const int nd = p->nd, nc = p->nc, N = J.N, nw = J.nw;
     std::vector<R> W((size_t)nd * 3 * nc, R(0));
     for (int r = 0; r < nd; r++) {
+        if (J.src == 0) {
+            // single force: the weights of its displacement columns (15)
+            double w[3 * grt::kSingleNC];
+            grt_sf_weights(src->f, azimuth[r], w);
+            for (int i = 0; i < 3; i++)
+                for (int c = 0; c < nc && c < grt::kSingleNC; c++)
+                    W[((size_t)r * 3 + i) * nc + c] = (R)w[i * grt::kSingleNC + c];
+            continue;
+        }
         double w[3][grt::kTensorFixNC];
         mt_weights(src->m, azimuth[r], w);
         for (int i = 0; i < 3; i++)
@@ -2391,7 +2400,6 @@ extern "C" int grt_plan_synth(grt_plan *p, const grt_source *src, const double *
 {
     if (!p || !src || !azimuth || !seis) return GRT_ERR_ARG;
     grt_ctx *ctx = p->ctx;
-    if (p->J.src == 0) return set_err(ctx, GRT_ERR_UNSUPPORTED, "seismograms need a moment-tensor job");
     if (!p->J.fsel.empty()) return set_err(ctx, GRT_ERR_UNSUPPORTED, "a frequency-selection plan has spectra only");
     if (src->n_stf < 0 || (src->n_stf > 0 && !src->stf) || src->n_stf > p->J.N)
         return set_err(ctx, GRT_ERR_ARG, "source-time function: 0 <= n_stf <= N samples");

@@ -307,8 +307,10 @@ GRT_API int grt_plan_write(grt_plan *plan, const char *path);
 GRT_API int grt_flatten(int n_layer, const double *ztop, const double *vp, const double *vs, double hs, double hr,
                         double r_earth, double *ztop_f, double *vp_f, double *vs_f, double *hs_f, double *hr_f);
 
-/* Seismograms from a moment-tensor job: after grt_plan_execute (or
- * grt_batch_execute), the receivers' Green's-function columns are combined
+/* Seismograms from a moment-tensor job (a single-force job: its displacement
+ * columns weighted by grt_sf_weights for the force src->f, below): after
+ * grt_plan_execute (or grt_batch_execute), the receivers' Green's-function
+ * columns are combined
  * for a source mechanism and azimuth, convolved with a source-time function,
  * and brought to the time domain in one fused kernel (combination, source
  * spectrum, phase/taper/scale, Hermitian fill, inverse DFT, e^{sigma t}).
@@ -332,9 +334,10 @@ GRT_API int grt_flatten(int n_layer, const double *ztop, const double *vp, const
  * wrap-around of the method).  No counterpart in the reference, which stops
  * at the columns. */
 typedef struct grt_source {
-    double m[6];          /* Mxx, Myy, Mzz, Mxy, Mxz, Myz; x north, y east, z down */
+    double m[6];          /* Mxx, Myy, Mzz, Mxy, Mxz, Myz; x north, y east, z down (moment-tensor jobs) */
     int n_stf;            /* source-time samples (0: impulse) */
     const double *stf;
+    double f[3];          /* Fx, Fy, Fz; x north, y east, z down (single-force jobs) */
 } grt_source;
 /* double couple: strike, dip, rake in degrees, scalar moment m0 -> m[6] (Aki & Richards, Box 4.4) */
 GRT_API void grt_dc_moment(double strike, double dip, double rake, double m0, double *m);
@@ -349,8 +352,8 @@ GRT_API void grt_mt_weights(const double *m, double azimuth, double *w);
  *   Z = Fr G3 + Fz G4,  R = Fr G0 + Fz G1,  T = Ft G2,
  *   Fr = Fx cos phi + Fy sin phi, Ft = -Fx sin phi + Fy cos phi.
  * The displacement columns 0-4 are the reference's in both layouts.  Host
- * only (no device); grt_plan_synth combines moment tensors only.  No
- * counterpart in the reference. */
+ * only (no device); grt_plan_synth applies them to single-force jobs (with
+ * src->f).  No counterpart in the reference. */
 GRT_API void grt_sf_weights(const double *f, double azimuth, double *w);
 /* azimuth: degrees clockwise from north, one per receiver; seis: [n_dist][3 (Z, R, T)][N] */
 GRT_API int grt_plan_synth(grt_plan *plan, const grt_source *src, const double *azimuth, double *seis);

@@ -81,18 +81,37 @@ def test_synthesis_linear_and_rotation_invariant(job):
 
 
 @pytest.mark.gpu
-def test_synthesis_needs_moment_tensor(job):
+def test_single_force_synthesis(job):
+    """A single-force job's seismograms are its displacement columns weighted
+    by grt_sf_weights (the spectral stage is linear): fused synthesis equals
+    that combination of the fetched traces, and is linear in the force."""
+    import ctypes
     g, p, tr, o = job
     from grtm_cuda_gb300 import synth
     m, _ = synth.crust4_model()
     m = dict(m, src_type=0)
-    ctx = p.ctx
-    ps = g.Plan(ctx, g.make_model(**m), o, [10.0])
-    ps.execute()
-    with pytest.raises(g.GrtError) as e:
-        ps.synth(g.dc_moment(0, 90, 0), [0.0])
-    assert e.value.status == g.ERR_UNSUPPORTED
-    ps.close()
+    d = np.array([12.0, 40.0, 77.0])
+    ps = g.Plan(p.ctx, g.make_model(**m), o, d)
+    try:
+        ps.execute()
+        t, _ = ps.fetch()
+        f = np.array([0.3, -1.1, 0.7])
+        az = np.array([10.0, 130.0, 250.0])
+        out = ps.synth(f, az)
+        dp = ctypes.POINTER(ctypes.c_double)
+        for r in range(len(d)):
+            w = np.zeros(3 * 15)
+            g.lib().grt_sf_weights(f.ctypes.data_as(dp), float(az[r]), w.ctypes.data_as(dp))
+            ref = w.reshape(3, 15) @ t[r][:15]
+            assert np.linalg.norm(out[r] - ref) <= 1e-5 * np.linalg.norm(ref)
+        f2 = np.array([-0.5, 0.2, 1.3])
+        a = ps.synth(f, az) + 2.0 * ps.synth(f2, az)
+        b = ps.synth(f + 2.0 * f2, az)
+        assert np.linalg.norm(a - b) <= 1e-5 * np.linalg.norm(b)
+        with pytest.raises(ValueError):
+            ps.synth([1.0, 2.0], az)
+    finally:
+        ps.close()
 
 
 @pytest.mark.gpu
