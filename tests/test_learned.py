@@ -346,3 +346,37 @@ def test_learned_judge_falls_back(ctx):
     assert len(info["fallback"]) == len(d)
     tp, _, _ = g.run(g.make_model(**m), learned.plain_opts(), d, ctx=ctx)
     assert np.array_equal(tl, tp)
+
+
+def test_sampler_network_per_context_without_gpu(monkeypatch):
+    """The sampler keeps one network per live context (building one uploads
+    the weights, freeing one waits for the whole device) and drops those of
+    closed or collected contexts."""
+    from grtm_cuda_gb300 import learned
+    made, closed = [], []
+
+    class FakeMlp:
+        def __init__(self, ctx):
+            self.ctx = ctx
+            made.append(self)
+
+        def set_params(self, p):
+            pass
+
+        def close(self):
+            closed.append(self)
+
+    class FakeCtx:
+        def __init__(self):
+            self.h = 1
+
+    monkeypatch.setattr(learned, "Mlp", FakeMlp)
+    s = learned.Sampler(np.zeros(4, np.float32), np.zeros(15), np.ones(15), np.zeros(2), np.ones(2))
+    a, b = FakeCtx(), FakeCtx()
+    na, nb = s.net(a), s.net(b)
+    assert na is not nb and s.net(a) is na and s.net(b) is nb and len(made) == 2
+    b.h = 0                                   # b closed: its network goes at the next lookup
+    assert s.net(a) is na and closed == [nb]
+    del b
+    c = FakeCtx()
+    assert s.net(c) is not na and len(made) == 3

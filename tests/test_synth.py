@@ -9,6 +9,17 @@ import pytest
 from oracle import synth_oracle as SO
 
 
+def test_source_forms_without_gpu():
+    """A source is a moment tensor (6 values) or a force (3 values)."""
+    import grtm_cuda_gb300 as g
+    s = g.make_source([1.0, 2.0, 3.0], stf=np.ones(4))
+    assert list(s.f) == [1.0, 2.0, 3.0] and list(s.m) == [0.0] * 6 and s.n_stf == 4
+    s = g.make_source(np.arange(6.0))
+    assert list(s.m) == list(np.arange(6.0)) and list(s.f) == [0.0] * 3 and s.n_stf == 0
+    with pytest.raises(ValueError):
+        g.make_source([1.0, 2.0])
+
+
 def test_dc_moment_known_cases():
     # vertical strike-slip along north: pure Mxy; 45-degree thrust: Mzz = -Myy... traceless
     assert np.allclose(SO.dc_moment(0, 90, 0), [0, 0, 0, 1, 0, 0], atol=1e-12)
